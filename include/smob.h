@@ -1,0 +1,153 @@
+/*
+ * smob.h — C ABI of the GB300 sphere mobility library (libsmob.so).
+ *
+ * One context holds one or more independent mobility problems (a "batch"); each
+ * problem is a set of rigid spheres whose surface densities live on the
+ * (p+1) x (2p+2) Gauss-Legendre x uniform grid of each sphere. The context owns a
+ * CUDA stream and all device memory; every call is synchronous with respect to the
+ * host unless its name ends in _async. All entry points return an smob_status and
+ * never throw; smob_last_error() gives the message of the last failure on the
+ * calling host thread. A context is not re-entrant: use one context per host thread
+ * (the reference operator keeps mutable scratch and is not re-entrant either,
+ * BIE/SphereSTKSHOperator.hpp:123-157).
+ *
+ * Vector layouts follow the reference:
+ *   - grid vectors: 3M doubles, interleaved (x,y,z) per point, spheres concatenated
+ *     in input order, points of a sphere in the order j*(2p+2)+k (theta ring j from
+ *     north to south, phi index k), poles excluded (Sphere/Shexp.cpp:206-271,
+ *     BIE/SphereSTKSHOperator.cpp:83-122);
+ *   - rigid-body vectors: 6N doubles (fx,fy,fz,tx,ty,tz) in, (vx,vy,vz,wx,wy,wz) out
+ *     per sphere (BIE/SphereSTKMobMat.cpp:174-192,261-285);
+ *   - spectral coefficients (smob_sh_* entry points): per sphere 3(p+1)(p+2) doubles,
+ *     the project's own layout: three blocks [radial | surface-gradient | toroidal],
+ *     each (p+1)(p+2)/2 complex numbers (re,im), n-major with m = 0..n, for the
+ *     vector spherical harmonics Y r, grad_s Y, r x grad_s Y of the body frame with
+ *     orthonormal Y_n^m without Condon-Shortley phase. The reference's SCTL layout
+ *     has the same size; its exact convention is not reproduced.
+ *   - quaternions: (w,x,y,z) per sphere, rotating the body frame into the lab frame.
+ */
+#ifndef SMOB_H
+#define SMOB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct smob_ctx smob_ctx;
+
+typedef enum {
+    SMOB_OK = 0,
+    SMOB_ERR_ARG = 1,          /* invalid argument (sizes, null pointers, overlapping spheres, order range) */
+    SMOB_ERR_CUDA = 2,         /* CUDA runtime failure (message has the CUDA error string) */
+    SMOB_ERR_NOMEM = 3,        /* device memory could not be allocated */
+    SMOB_ERR_NOT_CONVERGED = 4,/* solve stopped at its iteration limit (outputs are still written) */
+    SMOB_ERR_NONFINITE = 5,    /* NaN/Inf met in inputs or in the Krylov recurrence */
+    SMOB_ERR_STATE = 6,        /* call not valid in the context's current state */
+    SMOB_ERR_NO_DEVICE = 7     /* no usable CUDA device */
+} smob_status;
+
+typedef enum {
+    SMOB_PREC_FP64 = 0,  /* every kernel in FP64 */
+    SMOB_PREC_MIXED = 1  /* FP32 operator inside FP64 iterative refinement (FP64 Arnoldi, Givens, residuals) */
+} smob_precision;
+
+typedef struct {
+    int n_spheres;
+    const double* centers;  /* 3N */
+    const double* radii;    /* N, > 0 */
+    const double* quats;    /* 4N (w,x,y,z), or NULL for identity orientations */
+    const int* orders;      /* N, spherical-harmonic order p per sphere, 1 <= p <= 32 */
+    const int* problem;     /* N, problem index per sphere (non-decreasing, 0..P-1), or NULL: one problem */
+    double viscosity;       /* fluid viscosity (same for all problems), > 0 */
+} smob_geometry;
+
+typedef struct {
+    double tol;        /* relative residual |b - A mu| / |b| target (mobilitySolver.yaml "Convergence Tolerance") */
+    int restart;       /* Krylov vectors per cycle ("Num Blocks") */
+    int max_iters;     /* total GMRES iterations ("Maximum Iterations") */
+    int precision;     /* smob_precision */
+    int warm_start;    /* nonzero: start from the previous solution of each problem (SphereSTKMobMat.cpp:222) */
+    double inner_tol;  /* MIXED only: relative tolerance of each FP32 inner solve (<= 0: library default 1e-5) */
+} smob_solve_opts;
+
+typedef struct {
+    int status;        /* smob_status of this problem */
+    int iterations;    /* GMRES iterations (MIXED: summed over refinement sweeps) */
+    int refinements;   /* MIXED: refinement sweeps; FP64: restart cycles */
+    int operator_passes_fp64; /* high-precision operator applications (including b and the final velocity) */
+    int operator_passes_fp32; /* FP32 operator applications */
+    double relres;     /* final true relative residual |b - A mu|/|b| computed in the high-precision operator */
+    double bnorm;      /* |b| */
+} smob_problem_stats;
+
+/* ---- lifetime ---- */
+smob_status smob_create(smob_ctx** ctx, const smob_geometry* geom, int device);
+smob_status smob_destroy(smob_ctx* ctx);
+const char* smob_last_error(void);
+smob_status smob_version(int* major, int* minor);
+
+/* ---- sizes and grid (SphereSTKSHOperator::getGridCoords/Norms/Weights, hpp:218-223) ---- */
+smob_status smob_get_sizes(const smob_ctx* ctx, int* n_spheres, int* n_points, int* n_problems, int* n_near_pairs);
+smob_status smob_get_grid(const smob_ctx* ctx, double* coords3m, double* norms3m, double* weights_m);
+smob_status smob_get_near_pairs(const smob_ctx* ctx, int* trg, int* src);
+
+/* ---- SphereSTKSHOperator (BIE/SphereSTKSHOperator.hpp:112-231), host pointers ---- */
+/* Y = alpha * A X + beta * Y with A = 0.5 I + K + L, on n_cols columns of length 3M
+ * (column-major, leading dimension 3M). Replaces SphereSTKSHOperator::apply (cpp:153-236). */
+smob_status smob_apply(smob_ctx* ctx, const double* X, double* Y, int n_cols, double alpha, double beta,
+                       int precision);
+/* out += c_id*in + c_sl*S[in] + c_trac*K[in] (add-into). Replaces applyP2POP (cpp:262-485). */
+smob_status smob_apply_p2p(smob_ctx* ctx, const double* in, double* out, double c_id, double c_sl, double c_trac,
+                           int precision);
+/* out += c_lop * L[in] (add-into). Replaces applyLOP (cpp:487-521). */
+smob_status smob_apply_lop(smob_ctx* ctx, const double* in, double* out, double c_lop);
+/* in-place projection onto each sphere's band-limited space. Replaces projectNullSpace (cpp:239-260). */
+smob_status smob_project_null_space(smob_ctx* ctx, double* inout);
+
+/* ---- kernel-level pieces for parity tests (host pointers, add-into) ---- */
+/* far field over all sources except the target's own sphere and its near-pair source spheres */
+smob_status smob_far_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
+/* spectral evaluation of the near-pair source spheres at their targets (no direct subtraction) */
+smob_status smob_near_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
+/* per-sphere G2S / S2G in the layout above (Shexp::calcSpectralCoeff / calcGridValue, Shexp.cpp:342-447) */
+smob_status smob_sh_g2s(smob_ctx* ctx, const double* grid3m, double* coeff);
+smob_status smob_sh_s2g(smob_ctx* ctx, const double* coeff, double* grid3m);
+smob_status smob_coeff_offsets(const smob_ctx* ctx, int* offsets /* N+1, in doubles */);
+
+/* ---- SphereSTKMobMat (BIE/SphereSTKMobMat.hpp:26-79) ---- */
+/* force6N -> vel6N for every problem of the context; density3M (may be NULL) receives rho+mu
+ * (getDensitySolution, hpp:76); stats (may be NULL) has one entry per problem.
+ * Replaces SphereSTKMobMat::solveMob (cpp:146-286) and apply (cpp:98-144). */
+smob_status smob_solve_mob(smob_ctx* ctx, const double* force6n, double* vel6n, double* density3m,
+                           const smob_solve_opts* opts, smob_problem_stats* stats);
+/* the same with device pointers (inputs already resident; no host copies) */
+smob_status smob_solve_mob_device(smob_ctx* ctx, const double* d_force6n, double* d_vel6n, double* d_density3m,
+                                  const smob_solve_opts* opts, smob_problem_stats* stats);
+/* Y = alpha * M X + beta * Y for the mobility matrix M (6N x 6N), n_cols columns (SphereSTKMobMat::apply) */
+smob_status smob_mob_apply(smob_ctx* ctx, const double* X, double* Y, int n_cols, double alpha, double beta,
+                           const smob_solve_opts* opts);
+
+/* ---- device memory helpers for callers that time resident inputs ---- */
+smob_status smob_device_alloc(smob_ctx* ctx, size_t bytes, void** ptr);
+smob_status smob_device_free(smob_ctx* ctx, void* ptr);
+smob_status smob_memcpy_h2d(smob_ctx* ctx, void* dst, const void* src, size_t bytes);
+smob_status smob_memcpy_d2h(smob_ctx* ctx, void* dst, const void* src, size_t bytes);
+smob_status smob_synchronize(smob_ctx* ctx);
+
+/* ---- instrumentation ---- */
+/* enable/disable CUDA-event timing of every kernel launch on the context's stream */
+smob_status smob_profile_enable(smob_ctx* ctx, int on);
+/* per-kernel totals since the last reset: name (NUL-terminated, truncated to name_len), launches, milliseconds */
+smob_status smob_profile_count(const smob_ctx* ctx, int* n_kernels);
+smob_status smob_profile_get(const smob_ctx* ctx, int i, char* name, int name_len, long long* launches, double* ms);
+smob_status smob_profile_reset(smob_ctx* ctx);
+/* total kernel launches issued by the library on this context since creation */
+smob_status smob_launch_count(const smob_ctx* ctx, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMOB_H */

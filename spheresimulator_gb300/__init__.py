@@ -1,0 +1,247 @@
+"""spheresimulator_gb300 — GB300-native sphere mobility operator and mobility solve.
+
+Host-side mirror of the reference's operator interface over the C ABI of libsmob.so
+(include/smob.h). The names follow the reference classes:
+
+  SphereSTKSHOperator  (BIE/SphereSTKSHOperator.hpp:112-231): A = 0.5 I + K + L on the
+                       spheres' grid densities; apply / applyP2POP / applyLOP / projectNullSpace
+  SphereSTKMobMat      (BIE/SphereSTKMobMat.hpp:26-79): mobility matrix 6N -> 6N through a
+                       GMRES boundary-integral solve; solveMob / apply / getDensitySolution
+
+Every computation runs in the CUDA library; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from ._native import PREC_FP64, PREC_MIXED, SmobError
+
+__all__ = ["SphereSTKSHOperator", "SphereSTKMobMat", "SmobError", "PREC_FP64", "PREC_MIXED", "solve_opts",
+           "grid_number", "spectral_dof"]
+
+
+def grid_number(p):
+    """(p+1)(2p+2) grid points per sphere (Sphere/Shexp.hpp:65)."""
+    return (p + 1) * (2 * p + 2)
+
+
+def spectral_dof(p):
+    """3(p+1)(p+2) doubles of spectral coefficients per sphere (Sphere/Shexp.hpp:66)."""
+    return 3 * (p + 1) * (p + 2)
+
+
+def solve_opts(tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False, inner_tol=0.0):
+    """GMRES settings (mobilitySolver.yaml:3-16 names: Convergence Tolerance, Num Blocks, Maximum Iterations)."""
+    return N.SolveOpts(float(tol), int(restart), int(max_iters), int(precision), int(bool(warm_start)),
+                       float(inner_tol))
+
+
+class _Context:
+    def __init__(self, centers, radii, orders, quats=None, problem=None, viscosity=1.0, device=0):
+        self._L = N.lib()
+        self.centers = N.f64(centers).reshape(-1, 3)
+        self.radii = N.f64(radii).reshape(-1)
+        self.orders = N.i32(orders).reshape(-1)
+        self.quats = None if quats is None else N.f64(quats).reshape(-1, 4)
+        self.problem = None if problem is None else N.i32(problem).reshape(-1)
+        n = len(self.radii)
+        if self.centers.shape[0] != n or self.orders.shape[0] != n:
+            raise ValueError("centers, radii and orders must describe the same number of spheres")
+        geo = N.Geometry(n, N.dptr(self.centers), N.dptr(self.radii), N.dptr(self.quats), N.iptr(self.orders),
+                         N.iptr(self.problem), float(viscosity))
+        h = ctypes.c_void_p()
+        N.check(self._L.smob_create(ctypes.byref(h), ctypes.byref(geo), int(device)))
+        self._h = h
+        ns, npt, npb, nnp = (ctypes.c_int() for _ in range(4))
+        N.check(self._L.smob_get_sizes(h, ctypes.byref(ns), ctypes.byref(npt), ctypes.byref(npb), ctypes.byref(nnp)))
+        self.n_spheres, self.n_points, self.n_problems, self.n_near_pairs = ns.value, npt.value, npb.value, nnp.value
+        self.viscosity = float(viscosity)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.smob_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # grid getters (SphereSTKSHOperator.hpp:218-223)
+    def _grid(self):
+        c = np.zeros((self.n_points, 3))
+        nn = np.zeros((self.n_points, 3))
+        w = np.zeros(self.n_points)
+        N.check(self._L.smob_get_grid(self._h, N.dptr(c), N.dptr(nn), N.dptr(w)))
+        return c, nn, w
+
+    def getGridCoords(self):
+        return self._grid()[0]
+
+    def getGridNorms(self):
+        return self._grid()[1]
+
+    def getGridWeights(self):
+        return self._grid()[2]
+
+    def getGridNumberIndex(self):
+        lens = np.array([grid_number(p) for p in self.orders])
+        return np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+
+    def near_pairs(self):
+        t = np.zeros(max(self.n_near_pairs, 1), np.int32)
+        s = np.zeros(max(self.n_near_pairs, 1), np.int32)
+        N.check(self._L.smob_get_near_pairs(self._h, N.iptr(t), N.iptr(s)))
+        return t[:self.n_near_pairs], s[:self.n_near_pairs]
+
+    def launch_count(self):
+        v = ctypes.c_longlong()
+        N.check(self._L.smob_launch_count(self._h, ctypes.byref(v)))
+        return v.value
+
+    def profile(self, on=True):
+        N.check(self._L.smob_profile_enable(self._h, int(on)))
+
+    def profile_reset(self):
+        N.check(self._L.smob_profile_reset(self._h))
+
+    def profile_table(self):
+        n = ctypes.c_int()
+        N.check(self._L.smob_profile_count(self._h, ctypes.byref(n)))
+        out = {}
+        for i in range(n.value):
+            name = ctypes.create_string_buffer(64)
+            la = ctypes.c_longlong()
+            ms = ctypes.c_double()
+            N.check(self._L.smob_profile_get(self._h, i, name, 64, ctypes.byref(la), ctypes.byref(ms)))
+            out[name.value.decode()] = (la.value, ms.value)
+        return out
+
+
+class SphereSTKSHOperator(_Context):
+    """A = 0.5 I + K + L (the operator SphereSTKMobMat builds with cId=0.5, cSL=0, cTrac=1, cLOP=1,
+    BIE/SphereSTKMobMat.cpp:17), applied on the GPU."""
+
+    def _vec(self, x):
+        x = N.f64(x).reshape(-1)
+        if x.shape[0] != 3 * self.n_points:
+            raise ValueError("expected a vector of length 3M = %d" % (3 * self.n_points))
+        return x
+
+    def apply(self, X, Y=None, alpha=1.0, beta=0.0, precision=PREC_FP64):
+        """Y = alpha*A*X + beta*Y (Tpetra::Operator::apply, BIE/SphereSTKSHOperator.cpp:153-236);
+        X may have shape (3M,) or (ncol, 3M)."""
+        X = N.f64(X)
+        one = X.ndim == 1
+        X2 = X.reshape(1, -1) if one else X
+        if X2.shape[1] != 3 * self.n_points:
+            raise ValueError("expected columns of length 3M")
+        Y2 = np.zeros_like(X2) if Y is None else N.f64(Y).reshape(X2.shape).copy()
+        N.check(self._L.smob_apply(self._h, N.dptr(X2), N.dptr(Y2), X2.shape[0], float(alpha), float(beta),
+                                   int(precision)))
+        return Y2.reshape(-1) if one else Y2
+
+    def applyP2POP(self, inp, out=None, cId=0.0, cSL=0.0, cTrac=0.0, precision=PREC_FP64):
+        """out += cId*in + cSL*S[in] + cTrac*K[in] (BIE/SphereSTKSHOperator.cpp:262-485)."""
+        inp = self._vec(inp)
+        out = np.zeros(3 * self.n_points) if out is None else self._vec(out).copy()
+        N.check(self._L.smob_apply_p2p(self._h, N.dptr(inp), N.dptr(out), float(cId), float(cSL), float(cTrac),
+                                       int(precision)))
+        return out
+
+    def applyLOP(self, inp, out=None, cLOP=1.0):
+        """out += cLOP * L[in] (BIE/SphereSTKSHOperator.cpp:487-521)."""
+        inp = self._vec(inp)
+        out = np.zeros(3 * self.n_points) if out is None else self._vec(out).copy()
+        N.check(self._L.smob_apply_lop(self._h, N.dptr(inp), N.dptr(out), float(cLOP)))
+        return out
+
+    def projectNullSpace(self, x):
+        """Projection onto each sphere's band-limited space (BIE/SphereSTKSHOperator.cpp:239-260)."""
+        x = self._vec(x).copy()
+        N.check(self._L.smob_project_null_space(self._h, N.dptr(x)))
+        return x
+
+    def far_field(self, inp, cSL=0.0, cTrac=0.0, precision=PREC_FP64):
+        inp = self._vec(inp)
+        out = np.zeros(3 * self.n_points)
+        N.check(self._L.smob_far_field(self._h, N.dptr(inp), N.dptr(out), float(cSL), float(cTrac), int(precision)))
+        return out
+
+    def near_field(self, inp, cSL=0.0, cTrac=0.0, precision=PREC_FP64):
+        inp = self._vec(inp)
+        out = np.zeros(3 * self.n_points)
+        N.check(self._L.smob_near_field(self._h, N.dptr(inp), N.dptr(out), float(cSL), float(cTrac), int(precision)))
+        return out
+
+    def coeff_offsets(self):
+        off = np.zeros(self.n_spheres + 1, np.int32)
+        N.check(self._L.smob_coeff_offsets(self._h, N.iptr(off)))
+        return off
+
+    def sh_g2s(self, grid):
+        grid = self._vec(grid)
+        out = np.zeros(int(self.coeff_offsets()[-1]))
+        N.check(self._L.smob_sh_g2s(self._h, N.dptr(grid), N.dptr(out)))
+        return out
+
+    def sh_s2g(self, coeff):
+        coeff = N.f64(coeff).reshape(-1)
+        out = np.zeros(3 * self.n_points)
+        N.check(self._L.smob_sh_s2g(self._h, N.dptr(coeff), N.dptr(out)))
+        return out
+
+
+class SphereSTKMobMat(SphereSTKSHOperator):
+    """Mobility matrix force/torque (6N) -> velocity/angular velocity (6N)
+    (BIE/SphereSTKMobMat.cpp:98-286). One context may hold several independent problems
+    (``problem`` ids per sphere); they are solved together, each with its own Krylov space."""
+
+    def __init__(self, *args, **kw):
+        super().__init__(*args, **kw)
+        self._density = None
+        self.last_stats = None
+
+    def solveMob(self, force, tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False,
+                 inner_tol=0.0, want_density=True, raise_on_not_converged=True):
+        """force (6N) -> velocity (6N); also keeps rho+mu (getDensitySolution)."""
+        force = N.f64(force).reshape(-1)
+        if force.shape[0] != 6 * self.n_spheres:
+            raise ValueError("expected 6N forces/torques")
+        vel = np.zeros(6 * self.n_spheres)
+        dens = np.zeros(3 * self.n_points) if want_density else None
+        stats = (N.ProblemStats * self.n_problems)()
+        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol)
+        code = self._L.smob_solve_mob(self._h, N.dptr(force), N.dptr(vel), N.dptr(dens), ctypes.byref(opts), stats)
+        allow = () if raise_on_not_converged else (N.SMOB_ERR_NOT_CONVERGED,)
+        N.check(code, allow)
+        self._density = dens
+        self.last_stats = [s.as_dict() for s in stats]
+        return vel
+
+    def getDensitySolution(self):
+        """rho + mu from the last solve (BIE/SphereSTKMobMat.hpp:76)."""
+        return self._density
+
+    def apply(self, X, Y=None, alpha=1.0, beta=0.0, tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64):
+        """Y = alpha*M X + beta*Y for the mobility matrix M (BIE/SphereSTKMobMat.cpp:98-144)."""
+        X = N.f64(X)
+        one = X.ndim == 1
+        X2 = X.reshape(1, -1) if one else X
+        Y2 = np.zeros_like(X2) if Y is None else N.f64(Y).reshape(X2.shape).copy()
+        opts = solve_opts(tol, restart, max_iters, precision)
+        N.check(self._L.smob_mob_apply(self._h, N.dptr(X2), N.dptr(Y2), X2.shape[0], float(alpha), float(beta),
+                                       ctypes.byref(opts)))
+        return Y2.reshape(-1) if one else Y2

@@ -1,0 +1,136 @@
+"""ctypes binding of libsmob.so (the CUDA library). No CPU fallback exists: if the library
+cannot be built or loaded, or no GPU is present, every call raises."""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+SMOB_OK = 0
+SMOB_ERR_ARG = 1
+SMOB_ERR_CUDA = 2
+SMOB_ERR_NOMEM = 3
+SMOB_ERR_NOT_CONVERGED = 4
+SMOB_ERR_NONFINITE = 5
+SMOB_ERR_STATE = 6
+SMOB_ERR_NO_DEVICE = 7
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+STATUS_NAMES = {0: "OK", 1: "ARG", 2: "CUDA", 3: "NOMEM", 4: "NOT_CONVERGED", 5: "NONFINITE", 6: "STATE",
+                7: "NO_DEVICE"}
+
+
+class SmobError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("smob error %s (%d): %s" % (STATUS_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Geometry(ctypes.Structure):
+    _fields_ = [("n_spheres", ctypes.c_int), ("centers", ctypes.POINTER(ctypes.c_double)),
+                ("radii", ctypes.POINTER(ctypes.c_double)), ("quats", ctypes.POINTER(ctypes.c_double)),
+                ("orders", ctypes.POINTER(ctypes.c_int)), ("problem", ctypes.POINTER(ctypes.c_int)),
+                ("viscosity", ctypes.c_double)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("restart", ctypes.c_int), ("max_iters", ctypes.c_int),
+                ("precision", ctypes.c_int), ("warm_start", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+
+
+class ProblemStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
+                ("operator_passes_fp64", ctypes.c_int), ("operator_passes_fp32", ctypes.c_int),
+                ("relres", ctypes.c_double), ("bnorm", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_VP = ctypes.c_void_p
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load (building first if stale) libsmob.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    L = ctypes.CDLL(path)
+    S = ctypes.c_int
+    sig = {
+        "smob_create": (S, [ctypes.POINTER(_VP), ctypes.POINTER(Geometry), ctypes.c_int]),
+        "smob_destroy": (S, [_VP]),
+        "smob_last_error": (ctypes.c_char_p, []),
+        "smob_version": (S, [_IP, _IP]),
+        "smob_get_sizes": (S, [_VP, _IP, _IP, _IP, _IP]),
+        "smob_get_grid": (S, [_VP, _DP, _DP, _DP]),
+        "smob_get_near_pairs": (S, [_VP, _IP, _IP]),
+        "smob_apply": (S, [_VP, _DP, _DP, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+        "smob_apply_p2p": (S, [_VP, _DP, _DP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+        "smob_apply_lop": (S, [_VP, _DP, _DP, ctypes.c_double]),
+        "smob_project_null_space": (S, [_VP, _DP]),
+        "smob_far_field": (S, [_VP, _DP, _DP, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+        "smob_near_field": (S, [_VP, _DP, _DP, ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+        "smob_sh_g2s": (S, [_VP, _DP, _DP]),
+        "smob_sh_s2g": (S, [_VP, _DP, _DP]),
+        "smob_coeff_offsets": (S, [_VP, _IP]),
+        "smob_solve_mob": (S, [_VP, _DP, _DP, _DP, ctypes.POINTER(SolveOpts), ctypes.POINTER(ProblemStats)]),
+        "smob_solve_mob_device": (S, [_VP, _VP, _VP, _VP, ctypes.POINTER(SolveOpts), ctypes.POINTER(ProblemStats)]),
+        "smob_mob_apply": (S, [_VP, _DP, _DP, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                               ctypes.POINTER(SolveOpts)]),
+        "smob_device_alloc": (S, [_VP, ctypes.c_size_t, ctypes.POINTER(_VP)]),
+        "smob_device_free": (S, [_VP, _VP]),
+        "smob_memcpy_h2d": (S, [_VP, _VP, _VP, ctypes.c_size_t]),
+        "smob_memcpy_d2h": (S, [_VP, _VP, _VP, ctypes.c_size_t]),
+        "smob_synchronize": (S, [_VP]),
+        "smob_profile_enable": (S, [_VP, ctypes.c_int]),
+        "smob_profile_count": (S, [_VP, _IP]),
+        "smob_profile_get": (S, [_VP, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                 _DP]),
+        "smob_profile_reset": (S, [_VP]),
+        "smob_launch_count": (S, [_VP, ctypes.POINTER(ctypes.c_longlong)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names of the entry points declared in include/smob.h that the binding resolves."""
+    return [n for n in dir(lib()) if n.startswith("smob_")]
+
+
+def check(code, allow=()):
+    if code != SMOB_OK and code not in allow:
+        raise SmobError(code, lib().smob_last_error().decode(errors="replace"))
+    return code
+
+
+def dptr(a):
+    return None if a is None else a.ctypes.data_as(_DP)
+
+
+def iptr(a):
+    return None if a is None else a.ctypes.data_as(_IP)
+
+
+def f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)

@@ -1,0 +1,1260 @@
+// api.cu — host runtime of libsmob: context set-up, operator application, the batched
+// restarted GMRES / iterative-refinement driver and the C ABI declared in include/smob.h.
+//
+// Reference counterparts:
+//   SphereSTKSHOperator ctor / setupDOF / setupFMM / setupNearEval (BIE/SphereSTKSHOperator.cpp:7-144,539-573)
+//     -> smob_create (grid, weights, normals, neighbour list, far-field work items, tables)
+//   SphereSTKSHOperator::apply / applyP2POP / applyLOP / projectNullSpace (:153-521)
+//     -> smob_apply / smob_apply_p2p / smob_apply_lop / smob_project_null_space
+//   SphereSTKMobMat::solveMob / apply (BIE/SphereSTKMobMat.cpp:98-286) -> smob_solve_mob / smob_mob_apply
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/smob.h"
+#include "krylov.h"
+#include "sh_host.h"
+#include "smob_internal.h"
+
+using namespace smob;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct SmobError : std::runtime_error {
+    smob_status code;
+    SmobError(smob_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CUDA_OK(expr)                                                                                   \
+    do {                                                                                                \
+        cudaError_t e_ = (expr);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            throw SmobError(e_ == cudaErrorMemoryAllocation ? SMOB_ERR_NOMEM : SMOB_ERR_CUDA,          \
+                            std::string(#expr) + ": " + cudaGetErrorString(e_));                        \
+        }                                                                                               \
+    } while (0)
+
+// device buffer (RAII)
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t b) {
+        if (b <= bytes && p) return;
+        release();
+        if (b == 0) b = 16;
+        CUDA_OK(cudaMalloc(&p, b));
+        bytes = b;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+    template <typename T>
+    void upload(const std::vector<T>& v) {
+        alloc(v.size() * sizeof(T));
+        if (!v.empty()) CUDA_OK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+};
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+}  // namespace
+
+struct smob_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int N = 0, M = 0, P = 0, pmax = 0;
+    double viscosity = 1.0;
+    std::vector<double> centers, radii, quats, coords, norms, weights;
+    std::vector<int> orders, prob, gidx, glen, coff, sid;
+    std::vector<Problem> problems;
+    std::vector<int> nbr_start, nbr_src, near_src_slot, slot_sphere;
+    int ncoef_total = 0;  // complex numbers
+    long long set_stride_trac = 0, set_stride_sl = 0;
+    std::vector<FarItem> items32, items64;
+    long long partial32 = 0, partial64 = 0;
+    std::vector<VecChunk> chunks;
+
+    // device geometry
+    DBuf d_center, d_radius, d_quat, d_order, d_gidx, d_glen, d_coff, d_prob, d_coords, d_norms, d_weights, d_sid;
+    DBuf d_pos32, d_nrm32, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_near_slot, d_slot_sphere, d_problems, d_tabs;
+    DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_chunks;
+    DBuf d_active;
+    // operator workspace
+    DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
+    DBuf d_in, d_out, d_tmp;  // host-pointer API staging
+    // solver workspace
+    int restart_cap = 0;
+    DBuf d_V, d_w, d_r, d_x, d_xlast, d_b, d_rho, d_u, d_force, d_vel;
+    DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
+    bool have_xlast = false;
+
+    DevGeom g{};
+    long long launches = 0;
+
+    // profiling
+    bool prof = false;
+    struct ProfRec {
+        long long launches = 0;
+        double ms = 0;
+    };
+    std::map<std::string, ProfRec> prof_tab;
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+
+    KrylovLaunch kl() {
+        KrylovLaunch L;
+        L.chunks = d_chunks.as<VecChunk>();
+        L.nchunks = (int)chunks.size();
+        L.problems = d_problems.as<Problem>();
+        L.P = P;
+        L.partial = d_partial_red.as<double>();
+        return L;
+    }
+
+    ~smob_ctx() {
+        for (auto& p : pending) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+// ---------------------------------------------------------------- profiling helpers
+struct ProfScope {
+    smob_ctx* c;
+    const char* name;
+    cudaEvent_t a{}, b{};
+    ProfScope(smob_ctx* ctx, const char* n) : c(ctx), name(n) {
+        if (c->prof) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c->st);
+        }
+    }
+    ~ProfScope() {
+        if (c->prof) {
+            cudaEventRecord(b, c->st);
+            c->pending.push_back({name, a, b});
+        }
+    }
+};
+
+void prof_flush(smob_ctx* c) {
+    if (c->pending.empty()) return;
+    cudaStreamSynchronize(c->st);
+    for (auto& p : c->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        auto& r = c->prof_tab[p.name];
+        r.launches += 1;
+        r.ms += ms;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    c->pending.clear();
+}
+
+void check_launch(smob_ctx* c, int n) {
+    c->launches += n;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw SmobError(SMOB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+}
+
+inline void qrot_h(const double* q, const double* v, double* o) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double tx = 2 * (y * v[2] - z * v[1]);
+    const double ty = 2 * (z * v[0] - x * v[2]);
+    const double tz = 2 * (x * v[1] - y * v[0]);
+    o[0] = v[0] + w * tx + (y * tz - z * ty);
+    o[1] = v[1] + w * ty + (z * tx - x * tz);
+    o[2] = v[2] + w * tz + (x * ty - y * tx);
+}
+
+// ---------------------------------------------------------------- context set-up
+void build_context(smob_ctx* c, const smob_geometry* geo) {
+    const int N = geo->n_spheres;
+    c->N = N;
+    c->viscosity = geo->viscosity;
+    c->centers.assign(geo->centers, geo->centers + 3 * N);
+    c->radii.assign(geo->radii, geo->radii + N);
+    c->orders.assign(geo->orders, geo->orders + N);
+    c->quats.resize(4 * N);
+    for (int i = 0; i < N; ++i) {
+        if (geo->quats) {
+            const double* q = geo->quats + 4 * i;
+            const double nq = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+            if (!(nq > 0) || !std::isfinite(nq)) throw SmobError(SMOB_ERR_ARG, "quaternion of sphere " + std::to_string(i) + " is zero or not finite");
+            for (int k = 0; k < 4; ++k) c->quats[4 * i + k] = q[k] / nq;
+        } else {
+            c->quats[4 * i] = 1;
+            c->quats[4 * i + 1] = c->quats[4 * i + 2] = c->quats[4 * i + 3] = 0;
+        }
+    }
+    c->prob.resize(N);
+    for (int i = 0; i < N; ++i) c->prob[i] = geo->problem ? geo->problem[i] : 0;
+    for (int i = 0; i < N; ++i) {
+        if (!(c->radii[i] > 0) || !std::isfinite(c->radii[i]))
+            throw SmobError(SMOB_ERR_ARG, "radius of sphere " + std::to_string(i) + " must be positive and finite");
+        if (c->orders[i] < 1 || c->orders[i] > kMaxOrder)
+            throw SmobError(SMOB_ERR_ARG, "order of sphere " + std::to_string(i) + " outside [1, 32]");
+        for (int k = 0; k < 3; ++k)
+            if (!std::isfinite(c->centers[3 * i + k]))
+                throw SmobError(SMOB_ERR_ARG, "centre of sphere " + std::to_string(i) + " is not finite");
+        if (i > 0 && c->prob[i] < c->prob[i - 1]) throw SmobError(SMOB_ERR_ARG, "problem ids must be non-decreasing");
+        if (c->prob[i] < 0) throw SmobError(SMOB_ERR_ARG, "problem ids must be >= 0");
+    }
+    if (N > 0 && c->prob[0] != 0) throw SmobError(SMOB_ERR_ARG, "problem ids must start at 0");
+    for (int i = 1; i < N; ++i)
+        if (c->prob[i] > c->prob[i - 1] + 1) throw SmobError(SMOB_ERR_ARG, "problem ids must be contiguous");
+    c->P = N > 0 ? c->prob[N - 1] + 1 : 0;
+    c->pmax = *std::max_element(c->orders.begin(), c->orders.end());
+
+    // points and coefficient offsets
+    c->gidx.resize(N);
+    c->glen.resize(N);
+    c->coff.resize(N);
+    int off = 0, coffs = 0;
+    for (int i = 0; i < N; ++i) {
+        const int p = c->orders[i];
+        c->gidx[i] = off;
+        c->glen[i] = (p + 1) * (2 * p + 2);
+        off += c->glen[i];
+        c->coff[i] = coffs;
+        coffs += 3 * ncoef(p);
+    }
+    c->M = off;
+    c->ncoef_total = coffs;
+    c->coords.resize(3 * off);
+    c->norms.resize(3 * off);
+    c->weights.resize(off);
+    c->sid.resize(off);
+    for (int i = 0; i < N; ++i) {
+        const HostOrderTables& T = host_tables(c->orders[i]);
+        const double a = c->radii[i];
+        for (int j = 0; j < T.nt; ++j)
+            for (int k = 0; k < T.nphi; ++k) {
+                const int id = c->gidx[i] + j * T.nphi + k;
+                const double v[3] = {T.st[j] * T.cph[k], T.st[j] * T.sph[k], T.ct[j]};
+                double o[3];
+                qrot_h(&c->quats[4 * i], v, o);
+                for (int d = 0; d < 3; ++d) {
+                    c->norms[3 * id + d] = o[d];
+                    c->coords[3 * id + d] = a * o[d] + c->centers[3 * i + d];
+                }
+                c->weights[id] = a * a * T.wq[j];
+                c->sid[id] = i;
+            }
+    }
+
+    // problems
+    c->problems.assign(c->P, Problem{});
+    for (int p = 0; p < c->P; ++p) {
+        c->problems[p].s0 = N;
+        c->problems[p].s1 = 0;
+    }
+    for (int i = 0; i < N; ++i) {
+        Problem& pr = c->problems[c->prob[i]];
+        pr.s0 = std::min(pr.s0, i);
+        pr.s1 = std::max(pr.s1, i + 1);
+    }
+    for (auto& pr : c->problems) {
+        pr.p0 = c->gidx[pr.s0];
+        pr.p1 = c->gidx[pr.s1 - 1] + c->glen[pr.s1 - 1];
+        pr.v0 = 3 * pr.p0;
+        pr.v1 = 3 * pr.p1;
+    }
+
+    // near pairs (MPI/NearInteraction.txx:430-447; Rad = 1.5*radius, SphereSTKSHOperator.cpp:547),
+    // within each problem, sorted by target then source; overlapping spheres are rejected
+    c->nbr_start.assign(N + 1, 0);
+    c->nbr_src.clear();
+    for (const auto& pr : c->problems)
+        for (int t = pr.s0; t < pr.s1; ++t) {
+            for (int s = pr.s0; s < pr.s1; ++s) {
+                double r2 = 0;
+                for (int k = 0; k < 3; ++k) {
+                    const double d = c->centers[3 * s + k] - c->centers[3 * t + k];
+                    r2 += d * d;
+                }
+                if (s != t && std::sqrt(r2) <= c->radii[s] + c->radii[t])
+                    throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(s) +
+                                                      " overlap or touch");
+                const double Rn = 1.5 * c->radii[s] + 1.5 * c->radii[t];
+                if (r2 > 0 && r2 < Rn * Rn) c->nbr_src.push_back(s);
+            }
+            c->nbr_start[t + 1] = (int)c->nbr_src.size();
+        }
+    c->near_src_slot.assign(N, -1);
+    c->slot_sphere.clear();
+    for (int s : c->nbr_src)
+        if (c->near_src_slot[s] < 0) {
+            c->near_src_slot[s] = (int)c->slot_sphere.size();
+            c->slot_sphere.push_back(s);
+        }
+    std::sort(c->slot_sphere.begin(), c->slot_sphere.end());
+    for (size_t k = 0; k < c->slot_sphere.size(); ++k) c->near_src_slot[c->slot_sphere[k]] = (int)k;
+    const int ndmax = ncoef(c->pmax + 3);
+    c->set_stride_trac = 2LL * kNearSetsTrac * ndmax;
+    c->set_stride_sl = 2LL * kNearSetsSL * ndmax;
+
+    // far-field work items: target blocks x source-sphere chunks; the chunking depends only on
+    // the problem itself, so a problem's sums are identical alone or inside any batch
+    auto make_items = [&](int tblock, std::vector<FarItem>& items, long long& partial_elems) {
+        items.clear();
+        long long poff = 0;
+        for (int pi = 0; pi < c->P; ++pi) {
+            Problem& pr = c->problems[pi];
+            const int mp = pr.p1 - pr.p0;
+            const int ch = std::max(2048, (mp + 15) / 16);
+            std::vector<std::pair<int, int>> chunks;
+            int cs = pr.s0, acc = 0;
+            for (int s = pr.s0; s < pr.s1; ++s) {
+                acc += c->glen[s];
+                if (acc >= ch || s + 1 == pr.s1) {
+                    chunks.push_back({cs, s + 1});
+                    cs = s + 1;
+                    acc = 0;
+                }
+            }
+            pr.nchunks = (int)chunks.size();
+            pr.poff = poff;
+            poff += 3LL * mp * pr.nchunks;
+            for (int t0 = pr.p0; t0 < pr.p1; t0 += tblock)
+                for (int ci = 0; ci < pr.nchunks; ++ci)
+                    items.push_back(FarItem{t0, std::min(t0 + tblock, pr.p1), chunks[ci].first, chunks[ci].second, pi, ci});
+        }
+        partial_elems = poff;
+    };
+    // both item lists share the chunking rule, so Problem.nchunks/poff are the same for both
+    make_items(kFarTargets64, c->items64, c->partial64);
+    make_items(kFarTargets32, c->items32, c->partial32);
+    // heavier problems first helps the tail of uneven batches
+    auto by_cost = [&](std::vector<FarItem>& items) {
+        std::stable_sort(items.begin(), items.end(), [&](const FarItem& a, const FarItem& b) {
+            const Problem& pa = c->problems[a.problem];
+            const Problem& pb = c->problems[b.problem];
+            return (pa.p1 - pa.p0) > (pb.p1 - pb.p0);
+        });
+    };
+    by_cost(c->items32);
+    by_cost(c->items64);
+
+    // reduction chunks for the Krylov vectors
+    c->chunks.clear();
+    for (int pi = 0; pi < c->P; ++pi) {
+        Problem& pr = c->problems[pi];
+        pr.c0 = (int)c->chunks.size();
+        for (long long l = pr.v0; l < pr.v1; l += kVecChunk)
+            c->chunks.push_back(VecChunk{l, std::min<long long>(l + kVecChunk, pr.v1), pi, 0});
+        pr.c1 = (int)c->chunks.size();
+    }
+
+    // tables per order present (and p+1 synthesis tables are host-only)
+    std::vector<OrderTables> tabs(kMaxOrder + 1);
+    std::vector<double> tab;
+    std::vector<int> rowptr, col;
+    std::vector<double> mval;
+    std::vector<char> present(kMaxOrder + 1, 0);
+    for (int p : c->orders) present[p] = 1;
+    for (int p = 1; p <= kMaxOrder; ++p) {
+        if (!present[p]) continue;
+        const HostOrderTables& T = host_tables(p);
+        OrderTables& o = tabs[p];
+        o.p = p;
+        o.nt = T.nt;
+        o.nphi = T.nphi;
+        o.nc = T.nc;
+        o.ring = (int)tab.size();
+        tab.insert(tab.end(), T.ct.begin(), T.ct.end());
+        tab.insert(tab.end(), T.st.begin(), T.st.end());
+        tab.insert(tab.end(), T.wq.begin(), T.wq.end());
+        o.leg = (int)tab.size();
+        tab.insert(tab.end(), T.P.begin(), T.P.end());
+        tab.insert(tab.end(), T.dP.begin(), T.dP.end());
+        tab.insert(tab.end(), T.Ps.begin(), T.Ps.end());
+        o.twiddle = (int)tab.size();
+        tab.insert(tab.end(), T.cosmk.begin(), T.cosmk.end());
+        tab.insert(tab.end(), T.sinmk.begin(), T.sinmk.end());
+        o.cph = (int)tab.size();
+        tab.insert(tab.end(), T.cph.begin(), T.cph.end());
+        tab.insert(tab.end(), T.sph.begin(), T.sph.end());
+        o.trac_map = o.sl_map = -1;
+        o.trac_rows = o.sl_rows = 0;
+    }
+    // near maps only for orders of spheres that are near sources
+    std::vector<char> near_p(kMaxOrder + 1, 0);
+    for (int s : c->slot_sphere) near_p[c->orders[s]] = 1;
+    rowptr.clear();
+    for (int p = 1; p <= kMaxOrder; ++p) {
+        if (!near_p[p]) continue;
+        for (int kind = 0; kind < 2; ++kind) {
+            const SparseMap& mp = near_map(p, kind == 0);
+            const int base = (int)rowptr.size();
+            const int e0 = (int)col.size();
+            for (int r = 0; r < mp.rows; ++r) rowptr.push_back(e0 + mp.rowptr[r]);
+            rowptr.push_back(e0 + mp.rowptr[mp.rows]);
+            col.insert(col.end(), mp.col.begin(), mp.col.end());
+            mval.insert(mval.end(), mp.val.begin(), mp.val.end());
+            if (kind == 0) {
+                tabs[p].trac_map = base;
+                tabs[p].trac_rows = mp.rows;
+            } else {
+                tabs[p].sl_map = base;
+                tabs[p].sl_rows = mp.rows;
+            }
+        }
+    }
+    std::vector<double> c1, c2, dg;
+    theta_recurrence(kMaxOrder + 4, c1, c2, dg);
+    c->g.th_c1 = (int)tab.size();
+    tab.insert(tab.end(), c1.begin(), c1.end());
+    c->g.th_c2 = (int)tab.size();
+    tab.insert(tab.end(), c2.begin(), c2.end());
+    c->g.th_diag = (int)tab.size();
+    tab.insert(tab.end(), dg.begin(), dg.end());
+
+    // FP32/FP64 point data relative to each problem's origin (centre of its sphere bounding box)
+    std::vector<float4> pos32(c->M), nrm32(c->M);
+    std::vector<double4> pos64(c->M), nrm64(c->M);
+    for (const auto& pr : c->problems) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int s = pr.s0; s < pr.s1; ++s)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], c->centers[3 * s + k]);
+                hi[k] = std::max(hi[k], c->centers[3 * s + k]);
+            }
+        double org[3];
+        for (int k = 0; k < 3; ++k) org[k] = 0.5 * (lo[k] + hi[k]);
+        for (int i = pr.p0; i < pr.p1; ++i) {
+            int sidbits = c->sid[i];
+            float fs;
+            std::memcpy(&fs, &sidbits, 4);
+            const double x = c->coords[3 * i] - org[0], y = c->coords[3 * i + 1] - org[1], z = c->coords[3 * i + 2] - org[2];
+            pos32[i] = make_float4(float(x), float(y), float(z), fs);
+            nrm32[i] = make_float4(float(c->norms[3 * i]), float(c->norms[3 * i + 1]), float(c->norms[3 * i + 2]), 0.f);
+            pos64[i] = make_double4(x, y, z, 0.0);
+            nrm64[i] = make_double4(c->norms[3 * i], c->norms[3 * i + 1], c->norms[3 * i + 2], 0.0);
+        }
+    }
+
+    // upload
+    c->d_center.upload(c->centers);
+    c->d_radius.upload(c->radii);
+    c->d_quat.upload(c->quats);
+    c->d_order.upload(c->orders);
+    c->d_gidx.upload(c->gidx);
+    c->d_glen.upload(c->glen);
+    c->d_coff.upload(c->coff);
+    c->d_prob.upload(c->prob);
+    c->d_coords.upload(c->coords);
+    c->d_norms.upload(c->norms);
+    c->d_weights.upload(c->weights);
+    c->d_sid.upload(c->sid);
+    c->d_pos32.upload(pos32);
+    c->d_nrm32.upload(nrm32);
+    c->d_pos64.upload(pos64);
+    c->d_nrm64.upload(nrm64);
+    c->d_nbr_start.upload(c->nbr_start);
+    c->d_nbr_src.upload(c->nbr_src);
+    c->d_near_slot.upload(c->near_src_slot);
+    c->d_slot_sphere.upload(c->slot_sphere);
+    c->d_problems.upload(c->problems);
+    c->d_tabs.upload(tabs);
+    c->d_tab_d.upload(tab);
+    std::vector<float> tabf(tab.begin(), tab.end());
+    c->d_tab_f.upload(tabf);
+    c->d_map_rowptr.upload(rowptr);
+    c->d_map_col.upload(col);
+    c->d_map_val_d.upload(mval);
+    std::vector<float> mvalf(mval.begin(), mval.end());
+    c->d_map_val_f.upload(mvalf);
+    c->d_items32.upload(c->items32);
+    c->d_items64.upload(c->items64);
+    c->d_chunks.upload(c->chunks);
+    std::vector<unsigned char> act(c->P, 1);
+    c->d_active.upload(act);
+
+    // operator workspace
+    c->d_src32.alloc(sizeof(float4) * c->M);
+    c->d_src64.alloc(sizeof(double4) * c->M);
+    c->d_partial32.alloc(sizeof(float) * c->partial32);
+    c->d_partial64.alloc(sizeof(double) * c->partial64);
+    c->d_coef32.alloc(sizeof(float) * 2 * c->ncoef_total);
+    c->d_coef64.alloc(sizeof(double) * 2 * c->ncoef_total);
+    const size_t nsl = c->slot_sphere.size();
+    c->d_sets32.alloc(sizeof(float) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
+    c->d_sets64.alloc(sizeof(double) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
+    c->d_in.alloc(sizeof(double) * 3 * c->M);
+    c->d_out.alloc(sizeof(double) * 3 * c->M);
+    c->d_tmp.alloc(sizeof(double) * 3 * c->M);
+    c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * 2);
+
+    DevGeom& g = c->g;
+    g.N = c->N;
+    g.M = c->M;
+    g.P = c->P;
+    g.pmax = c->pmax;
+    g.center = c->d_center.as<double>();
+    g.radius = c->d_radius.as<double>();
+    g.quat = c->d_quat.as<double>();
+    g.order = c->d_order.as<int>();
+    g.gidx = c->d_gidx.as<int>();
+    g.glen = c->d_glen.as<int>();
+    g.coff = c->d_coff.as<int>();
+    g.prob = c->d_prob.as<int>();
+    g.coords = c->d_coords.as<double>();
+    g.norms = c->d_norms.as<double>();
+    g.weights = c->d_weights.as<double>();
+    g.sid = c->d_sid.as<int>();
+    g.pos32 = c->d_pos32.as<float4>();
+    g.nrm32 = c->d_nrm32.as<float4>();
+    g.pos64 = c->d_pos64.as<double4>();
+    g.nrm64 = c->d_nrm64.as<double4>();
+    g.nbr_start = c->d_nbr_start.as<int>();
+    g.nbr_src = c->d_nbr_src.as<int>();
+    g.near_src_slot = c->d_near_slot.as<int>();
+    g.problems = c->d_problems.as<Problem>();
+    g.tabs = c->d_tabs.as<OrderTables>();
+    g.tab_d = c->d_tab_d.as<double>();
+    g.tab_f = c->d_tab_f.as<float>();
+    g.map_rowptr = c->d_map_rowptr.as<int>();
+    g.map_col = c->d_map_col.as<int>();
+    g.map_val_d = c->d_map_val_d.as<double>();
+    g.map_val_f = c->d_map_val_f.as<float>();
+    g.active = c->d_active.as<unsigned char>();
+}
+
+void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
+    CUDA_OK(cudaMemcpyAsync(c->d_active.p, act.data(), act.size(), cudaMemcpyHostToDevice, c->st));
+    // the host vector must stay valid until the copy ran: make it synchronous with the stream
+    CUDA_OK(cudaStreamSynchronize(c->st));
+}
+
+// ---------------------------------------------------------------- the operator
+// out (device) += c_id*x + c_sl*S[x] + c_trac*K[x] + c_lop*L[x] on active problems
+void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_sl, double c_trac, double c_lop,
+              bool fp32) {
+    const DevGeom& g = c->g;
+    const bool trac = std::fabs(c_trac) > 1e-9, sl = std::fabs(c_sl) > 1e-9;
+    const bool id = std::fabs(c_id) > 1e-9;
+    void* coef = fp32 ? c->d_coef32.p : c->d_coef64.p;
+    void* sets = fp32 ? c->d_sets32.p : c->d_sets64.p;
+    void* partial = fp32 ? c->d_partial32.p : c->d_partial64.p;
+    const int nslots = (int)c->slot_sphere.size();
+    const FarItem* items = fp32 ? c->d_items32.as<FarItem>() : c->d_items64.as<FarItem>();
+    const int nitems = (int)(fp32 ? c->items32.size() : c->items64.size());
+    auto kind_pass = [&](bool tr, double cc, bool with_id_lop) {
+        {
+            ProfScope ps(c, "sphere_self");
+            check_launch(c, launch_sphere_op(g, x, out, with_id_lop && id ? c_id : 0.0, cc, tr ? 3 : 0,
+                                             with_id_lop ? c_lop : 0.0, coef, fp32, c->st));
+        }
+        if (nslots > 0) {
+            {
+                ProfScope ps(c, "near_sets");
+                check_launch(c, launch_near_sets(g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(),
+                                                 tr ? c->set_stride_trac : c->set_stride_sl, c->st));
+            }
+            {
+                ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
+                check_launch(c, launch_near_eval(g, sets, tr ? c->set_stride_trac : c->set_stride_sl, tr, fp32, cc, out,
+                                                 c->st));
+            }
+        }
+        {
+            ProfScope ps(c, "far_pack");
+            check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
+        }
+        {
+            ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
+            check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                             c->d_src64.as<double4>(), partial, c->st));
+        }
+        {
+            ProfScope ps(c, "far_reduce");
+            check_launch(c, launch_far_reduce(g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), out, c->st));
+        }
+    };
+    if (trac) kind_pass(true, c_trac, true);
+    if (sl) kind_pass(false, c_sl, !trac);
+    if (!trac && !sl && (id || std::fabs(c_lop) > 0)) {
+        ProfScope ps(c, "sphere_self");
+        check_launch(c, launch_sphere_op(g, x, out, id ? c_id : 0.0, 0.0, -1, c_lop, nullptr, fp32, c->st));
+    }
+}
+
+// ---------------------------------------------------------------- solver
+void ensure_solver(smob_ctx* c, int m) {
+    const size_t n = 3 * (size_t)c->M;
+    if (m > c->restart_cap) {
+        c->d_V.alloc(sizeof(double) * n * (m + 1));
+        c->d_H.alloc(sizeof(double) * c->P * m * (m + 1));
+        c->d_g.alloc(sizeof(double) * c->P * (m + 1));
+        c->d_cs.alloc(sizeof(double) * c->P * m);
+        c->d_sn.alloc(sizeof(double) * c->P * m);
+        c->d_y.alloc(sizeof(double) * c->P * m);
+        c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * (m + 1));
+        c->restart_cap = m;
+    }
+    c->d_w.alloc(sizeof(double) * n);
+    c->d_r.alloc(sizeof(double) * n);
+    c->d_x.alloc(sizeof(double) * n);
+    c->d_b.alloc(sizeof(double) * n);
+    c->d_rho.alloc(sizeof(double) * n);
+    c->d_u.alloc(sizeof(double) * n);
+    c->d_force.alloc(sizeof(double) * 6 * c->N);
+    c->d_vel.alloc(sizeof(double) * 6 * c->N);
+    c->d_kc.alloc(sizeof(int) * c->P);
+    c->d_ks.alloc(sizeof(KrylovState) * c->P);
+    c->d_norm.alloc(sizeof(double) * c->P);
+    c->d_hn.alloc(sizeof(double) * c->P);
+    c->d_beta.alloc(sizeof(double) * c->P);
+    c->d_incycle.alloc(c->P);
+    if (!c->d_xlast.p) {
+        c->d_xlast.alloc(sizeof(double) * n);
+        CUDA_OK(cudaMemsetAsync(c->d_xlast.p, 0, sizeof(double) * n, c->st));
+    }
+}
+
+std::vector<double> seg_norms(smob_ctx* c, const double* v, const unsigned char* active) {
+    KrylovLaunch L = c->kl();
+    check_launch(c, launch_dots(L, v, 0, 1, v, active, c->d_norm.as<double>(), 1, 0, false, true, c->st));
+    std::vector<double> h(c->P);
+    CUDA_OK(cudaMemcpyAsync(h.data(), c->d_norm.p, sizeof(double) * c->P, cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    return h;
+}
+
+// the mobility solve on device pointers (SphereSTKMobMat::solveMob, BIE/SphereSTKMobMat.cpp:146-286)
+smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, double* d_density,
+                         const smob_solve_opts* o, smob_problem_stats* stats) {
+    const int m = std::max(1, o->restart);
+    const bool mixed = o->precision == SMOB_PREC_MIXED;
+    const double tol = o->tol;
+    const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+    const int maxit = std::max(1, o->max_iters);
+    ensure_solver(c, m);
+    const size_t n = 3 * (size_t)c->M;
+    const int P = c->P;
+    KrylovLaunch L = c->kl();
+    cudaStream_t st = c->st;
+    double* V = c->d_V.as<double>();
+    double* w = c->d_w.as<double>();
+    double* r = c->d_r.as<double>();
+    double* x = c->d_x.as<double>();
+    double* b = c->d_b.as<double>();
+    double* rho = c->d_rho.as<double>();
+    double* u = c->d_u.as<double>();
+    unsigned char* act = c->d_active.as<unsigned char>();
+    unsigned char* incyc = c->d_incycle.as<unsigned char>();
+    KrylovState* ks = c->d_ks.as<KrylovState>();
+
+    std::vector<unsigned char> all(P, 1);
+    set_active(c, all);
+    std::vector<KrylovState> hks(P);
+    for (auto& k : hks) k = KrylovState{0, 0, 0, 0, 0, 0, 0};
+    CUDA_OK(cudaMemcpyAsync(ks, hks.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
+    std::vector<int> passes64(P, 0), cycles(P, 0);
+
+    // step 1: rigid density; step 2: b = -(I/2 + K) rho  (high precision)
+    check_launch(c, launch_rigid_density(c->g, d_force, rho, st));
+    CUDA_OK(cudaMemsetAsync(b, 0, sizeof(double) * n, st));
+    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, false);
+    for (auto& v : passes64) v++;
+    std::vector<double> bnorm = seg_norms(c, b, act);
+
+    // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution or zero
+    std::vector<char> done(P, 0), conv(P, 0);
+    std::vector<double> beta(P, 0.0);
+    if (o->warm_start && c->have_xlast) {
+        CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, false);
+        for (auto& v : passes64) v++;
+        check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+        check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+    } else {
+        CUDA_OK(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+        CUDA_OK(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    beta = seg_norms(c, r, act);
+    bool nonfinite_any = false;
+    for (int p = 0; p < P; ++p) {
+        if (!std::isfinite(bnorm[p]) || !std::isfinite(beta[p])) {
+            done[p] = 1;
+            nonfinite_any = true;
+        } else if (bnorm[p] < 1e-5) {  // forcing is zero: density correction is zero (SphereSTKMobMat.cpp:217)
+            done[p] = 1;
+            conv[p] = 1;
+        }
+    }
+    if (std::any_of(done.begin(), done.end(), [](char d) { return d; })) {
+        // zero the correction of finished problems
+        std::vector<unsigned char> zm(P, 0);
+        for (int p = 0; p < P; ++p) zm[p] = done[p] ? 1 : 0;
+        set_active(c, zm);
+        check_launch(c, launch_axpby_seg(L, 0.0, x, 0.0, act, x, st));
+    }
+
+    // Restart cycles in lockstep over the problems still running. FP64: each cycle is a
+    // GMRES(m) cycle on the FP64 operator, followed by the explicit residual (Belos' restart).
+    // MIXED: each cycle solves A d = r with the FP32 operator (FP64 Arnoldi/Givens) to a relative
+    // inner tolerance, x += d, and the refinement residual r = b - A x uses the FP64 operator.
+    std::vector<KrylovState> kst(P);
+    std::vector<unsigned char> hact(P);
+    const long long hs = (long long)m * (m + 1);
+    while (true) {
+        CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
+        CUDA_OK(cudaStreamSynchronize(st));
+        std::vector<unsigned char> cyc(P, 0);
+        int ncyc = 0;
+        for (int p = 0; p < P; ++p) {
+            if (done[p]) continue;
+            if (beta[p] / bnorm[p] < tol) {
+                done[p] = 1;
+                conv[p] = 1;
+                continue;
+            }
+            if (kst[p].iters >= maxit || kst[p].nonfinite) {
+                done[p] = 1;
+                continue;
+            }
+            cyc[p] = 1;
+            ++ncyc;
+            cycles[p]++;
+            kst[p].tol_abs = mixed ? std::max(inner_tol * beta[p], 0.5 * tol * bnorm[p]) : tol * bnorm[p];
+            kst[p].cycle_fp32 = mixed ? 1 : 0;
+        }
+        if (ncyc == 0) break;
+        CUDA_OK(cudaMemcpyAsync(ks, kst.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
+        CUDA_OK(cudaMemcpyAsync(incyc, cyc.data(), P, cudaMemcpyHostToDevice, st));
+        CUDA_OK(cudaMemcpyAsync(c->d_beta.p, beta.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
+        set_active(c, cyc);
+        check_launch(c, launch_scale(L, r, c->d_beta.as<double>(), 1, true, act, V, st));
+        check_launch(c, launch_cycle_init(L, m, incyc, c->d_beta.as<double>(), ks, c->d_H.as<double>(),
+                                          c->d_g.as<double>(), st));
+        for (int j = 0; j < m; ++j) {
+            const double* Vj = V + n * j;
+            // w = A V_j,  A = I/2 + K + L (SphereSTKMobMat.cpp:17)
+            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+            op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, mixed);
+            // CGS2: h = V^T w; w -= V h (twice), H[:, j] = h1 + h2
+            double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
+            double* hscr = c->d_y.as<double>();
+            for (int pass = 0; pass < 2; ++pass) {
+                check_launch(c, launch_dots(L, V, (long long)n, j + 1, w, act, hscr, m, 0, false, false, st, Hcol, hs,
+                                            pass == 1));
+                check_launch(c, launch_update(L, V, (long long)n, j + 1, nullptr, hscr, m, -1.0, act, w, st));
+            }
+            check_launch(c, launch_dots(L, w, 0, 1, w, act, c->d_hn.as<double>(), 1, 0, false, true, st));
+            check_launch(c, launch_givens(L, j, m, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_cs.as<double>(),
+                                          c->d_sn.as<double>(), c->d_hn.as<double>(), act, maxit, st));
+            if (j + 1 < m) check_launch(c, launch_scale(L, w, c->d_hn.as<double>(), 1, true, act, V + n * (j + 1), st));
+            CUDA_OK(cudaMemcpyAsync(hact.data(), act, P, cudaMemcpyDeviceToHost, st));
+            CUDA_OK(cudaStreamSynchronize(st));
+            if (std::none_of(hact.begin(), hact.end(), [](unsigned char a) { return a != 0; })) break;
+        }
+        // x += V y for the problems of this cycle
+        check_launch(c, launch_trisolve(L, m, incyc, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_y.as<double>(),
+                                        c->d_kc.as<int>(), st));
+        set_active(c, cyc);
+        check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, x, st));
+        // explicit residual in FP64
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, false);
+        for (int p = 0; p < P; ++p)
+            if (cyc[p]) passes64[p]++;
+        check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+        check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+        std::vector<double> nb = seg_norms(c, r, act);
+        for (int p = 0; p < P; ++p)
+            if (cyc[p]) beta[p] = nb[p];
+    }
+
+    // step 4: rho += mu; u = S[rho] (FP64); rigid averages / viscosity (SphereSTKMobMat.cpp:243-285)
+    set_active(c, all);
+    check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, rho, st));
+    CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+    op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, false);
+    for (auto& v : passes64) v++;
+    check_launch(c, launch_rigid_average(c->g, u, 1.0 / c->viscosity, d_vel, st));
+    if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    CUDA_OK(cudaMemcpyAsync(c->d_xlast.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    c->have_xlast = true;
+    CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
+    CUDA_OK(cudaStreamSynchronize(st));
+
+    smob_status worst = SMOB_OK;
+    for (int p = 0; p < P; ++p) {
+        smob_status sp = SMOB_OK;
+        if (!std::isfinite(bnorm[p]) || kst[p].nonfinite || !std::isfinite(beta[p])) sp = SMOB_ERR_NONFINITE;
+        else if (!conv[p]) sp = SMOB_ERR_NOT_CONVERGED;
+        if (sp != SMOB_OK && worst == SMOB_OK) worst = sp;
+        if (stats) {
+            smob_problem_stats& s = stats[p];
+            s.status = sp;
+            s.iterations = kst[p].iters;
+            s.refinements = cycles[p];
+            s.operator_passes_fp64 = passes64[p] + kst[p].passes64;
+            s.operator_passes_fp32 = kst[p].passes32;
+            s.bnorm = bnorm[p];
+            s.relres = bnorm[p] < 1e-5 ? 0.0 : beta[p] / bnorm[p];
+        }
+    }
+    if (nonfinite_any && worst == SMOB_OK) worst = SMOB_ERR_NONFINITE;
+    if (worst == SMOB_ERR_NONFINITE) g_err = "non-finite values in the mobility solve";
+    else if (worst == SMOB_ERR_NOT_CONVERGED) g_err = "GMRES stopped at its iteration limit";
+    return worst;
+}
+
+template <typename F>
+smob_status guarded(F&& f) {
+    try {
+        return f();
+    } catch (const SmobError& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_err = "host allocation failed";
+        return SMOB_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return SMOB_ERR_CUDA;
+    }
+}
+
+void need(bool cond, const char* msg) {
+    if (!cond) throw SmobError(SMOB_ERR_ARG, msg);
+}
+
+void set_device(const smob_ctx* c) { CUDA_OK(cudaSetDevice(c->device)); }
+
+// copy a host 3M vector in, run f(d_in, d_out) with d_out preloaded from host out, copy back
+template <typename F>
+void host_io(smob_ctx* c, const double* in, double* out, bool load_out, F&& f) {
+    const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
+    CUDA_OK(cudaMemcpyAsync(c->d_in.p, in, bytes, cudaMemcpyHostToDevice, c->st));
+    if (load_out) CUDA_OK(cudaMemcpyAsync(c->d_out.p, out, bytes, cudaMemcpyHostToDevice, c->st));
+    else CUDA_OK(cudaMemsetAsync(c->d_out.p, 0, bytes, c->st));
+    f(c->d_in.as<double>(), c->d_out.as<double>());
+    CUDA_OK(cudaMemcpyAsync(out, c->d_out.p, bytes, cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+}
+
+void all_active(smob_ctx* c) {
+    std::vector<unsigned char> a(c->P, 1);
+    set_active(c, a);
+}
+
+}  // namespace
+
+// ================================================================ C ABI
+extern "C" {
+
+const char* smob_last_error(void) { return g_err.c_str(); }
+
+smob_status smob_version(int* major, int* minor) {
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+    return SMOB_OK;
+}
+
+smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
+    return guarded([&]() -> smob_status {
+        need(out != nullptr && geo != nullptr, "null argument");
+        *out = nullptr;
+        need(geo->n_spheres > 0, "n_spheres must be positive");
+        need(geo->centers && geo->radii && geo->orders, "centers, radii and orders are required");
+        need(geo->viscosity > 0 && std::isfinite(geo->viscosity), "viscosity must be positive");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw SmobError(SMOB_ERR_NO_DEVICE, "no CUDA device available");
+        }
+        need(device >= 0 && device < ndev, "device index out of range");
+        std::unique_ptr<smob_ctx> c(new smob_ctx);
+        c->device = device;
+        CUDA_OK(cudaSetDevice(device));
+        CUDA_OK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        configure_sphere_kernels();
+        build_context(c.get(), geo);
+        CUDA_OK(cudaDeviceSynchronize());
+        *out = c.release();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_destroy(smob_ctx* c) {
+    if (!c) return SMOB_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->st);
+    delete c;
+    return SMOB_OK;
+}
+
+smob_status smob_get_sizes(const smob_ctx* c, int* n_spheres, int* n_points, int* n_problems, int* n_near_pairs) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (n_spheres) *n_spheres = c->N;
+        if (n_points) *n_points = c->M;
+        if (n_problems) *n_problems = c->P;
+        if (n_near_pairs) *n_near_pairs = (int)c->nbr_src.size();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_get_grid(const smob_ctx* c, double* coords, double* norms, double* weights) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (coords) std::copy(c->coords.begin(), c->coords.end(), coords);
+        if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
+        if (weights) std::copy(c->weights.begin(), c->weights.end(), weights);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_get_near_pairs(const smob_ctx* c, int* trg, int* src) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        int k = 0;
+        for (int t = 0; t < c->N; ++t)
+            for (int e = c->nbr_start[t]; e < c->nbr_start[t + 1]; ++e, ++k) {
+                if (trg) trg[k] = t;
+                if (src) src[k] = c->nbr_src[e];
+            }
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_coeff_offsets(const smob_ctx* c, int* offsets) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr && offsets != nullptr, "null argument");
+        for (int i = 0; i < c->N; ++i) offsets[i] = 2 * c->coff[i];
+        offsets[c->N] = 2 * c->ncoef_total;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_apply_p2p(smob_ctx* c, const double* in, double* out, double c_id, double c_sl, double c_trac,
+                           int precision) {
+    return guarded([&]() -> smob_status {
+        need(c && in && out, "null argument");
+        set_device(c);
+        all_active(c);
+        host_io(c, in, out, true, [&](const double* din, double* dout) {
+            op_apply(c, din, dout, c_id, c_sl, c_trac, 0.0, precision == SMOB_PREC_MIXED);
+        });
+        prof_flush(c);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_apply_lop(smob_ctx* c, const double* in, double* out, double c_lop) {
+    return guarded([&]() -> smob_status {
+        need(c && in && out, "null argument");
+        set_device(c);
+        all_active(c);
+        host_io(c, in, out, true, [&](const double* din, double* dout) {
+            check_launch(c, launch_sphere_op(c->g, din, dout, 0.0, 0.0, -1, c_lop, nullptr, false, c->st));
+        });
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, double alpha, double beta, int precision) {
+    return guarded([&]() -> smob_status {
+        need(c && X && Y && n_cols >= 1, "invalid argument");
+        set_device(c);
+        all_active(c);
+        const size_t n = 3 * (size_t)c->M;
+        std::vector<double> tmp(n);
+        for (int col = 0; col < n_cols; ++col) {
+            host_io(c, X + n * col, tmp.data(), false, [&](const double* din, double* dout) {
+                op_apply(c, din, dout, 0.5, 0.0, 1.0, 1.0, precision == SMOB_PREC_MIXED);
+            });
+            double* y = Y + n * col;
+            for (size_t i = 0; i < n; ++i) y[i] = (beta == 0.0 ? 0.0 : beta * y[i]) + alpha * tmp[i];
+        }
+        prof_flush(c);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_project_null_space(smob_ctx* c, double* inout) {
+    return guarded([&]() -> smob_status {
+        need(c && inout, "null argument");
+        set_device(c);
+        all_active(c);
+        const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
+        CUDA_OK(cudaMemcpyAsync(c->d_in.p, inout, bytes, cudaMemcpyHostToDevice, c->st));
+        check_launch(c, launch_sh_g2s(c->g, c->d_in.as<double>(), c->d_coef64.as<double>(), c->st));
+        check_launch(c, launch_sh_s2g(c->g, c->d_coef64.as<double>(), c->d_out.as<double>(), c->st));
+        CUDA_OK(cudaMemcpyAsync(inout, c->d_out.p, bytes, cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_sl, double c_trac, int precision) {
+    return guarded([&]() -> smob_status {
+        need(c && in && out, "null argument");
+        set_device(c);
+        all_active(c);
+        const bool fp32 = precision == SMOB_PREC_MIXED;
+        host_io(c, in, out, true, [&](const double* din, double* dout) {
+            const FarItem* items = fp32 ? c->d_items32.as<FarItem>() : c->d_items64.as<FarItem>();
+            const int nitems = (int)(fp32 ? c->items32.size() : c->items64.size());
+            void* partial = fp32 ? c->d_partial32.p : c->d_partial64.p;
+            for (int k = 0; k < 2; ++k) {
+                const bool tr = k == 0;
+                const double cc = tr ? c_trac : c_sl;
+                if (cc == 0.0) continue;
+                check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
+                {
+                    ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
+                    check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                                     c->d_src64.as<double4>(), partial, c->st));
+                }
+                check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st));
+            }
+        });
+        prof_flush(c);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c_sl, double c_trac, int precision) {
+    return guarded([&]() -> smob_status {
+        need(c && in && out, "null argument");
+        set_device(c);
+        all_active(c);
+        const bool fp32 = precision == SMOB_PREC_MIXED;
+        const int nslots = (int)c->slot_sphere.size();
+        host_io(c, in, out, true, [&](const double* din, double* dout) {
+            if (nslots == 0) return;
+            void* coef = fp32 ? c->d_coef32.p : c->d_coef64.p;
+            void* sets = fp32 ? c->d_sets32.p : c->d_sets64.p;
+            // coefficients only: a sphere pass with no self term and no output contribution
+            CUDA_OK(cudaMemsetAsync(c->d_tmp.p, 0, sizeof(double) * 3 * c->M, c->st));
+            check_launch(c, launch_sphere_op(c->g, din, c->d_tmp.as<double>(), 0.0, 0.0, 3, 0.0, coef, fp32, c->st));
+            for (int k = 0; k < 2; ++k) {
+                const bool tr = k == 0;
+                const double cc = tr ? c_trac : c_sl;
+                if (cc == 0.0) continue;
+                const long long stride = tr ? c->set_stride_trac : c->set_stride_sl;
+                check_launch(c, launch_near_sets(c->g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(), stride, c->st));
+                check_launch(c, launch_near_eval(c->g, sets, stride, tr, fp32, cc, dout, c->st));
+            }
+        });
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_sh_g2s(smob_ctx* c, const double* grid, double* coeff) {
+    return guarded([&]() -> smob_status {
+        need(c && grid && coeff, "null argument");
+        set_device(c);
+        all_active(c);
+        const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
+        CUDA_OK(cudaMemcpyAsync(c->d_in.p, grid, bytes, cudaMemcpyHostToDevice, c->st));
+        check_launch(c, launch_sh_g2s(c->g, c->d_in.as<double>(), c->d_coef64.as<double>(), c->st));
+        CUDA_OK(cudaMemcpyAsync(coeff, c->d_coef64.p, sizeof(double) * 2 * c->ncoef_total, cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_sh_s2g(smob_ctx* c, const double* coeff, double* grid) {
+    return guarded([&]() -> smob_status {
+        need(c && grid && coeff, "null argument");
+        set_device(c);
+        all_active(c);
+        CUDA_OK(cudaMemcpyAsync(c->d_coef64.p, coeff, sizeof(double) * 2 * c->ncoef_total, cudaMemcpyHostToDevice, c->st));
+        check_launch(c, launch_sh_s2g(c->g, c->d_coef64.as<double>(), c->d_out.as<double>(), c->st));
+        CUDA_OK(cudaMemcpyAsync(grid, c->d_out.p, sizeof(double) * 3 * c->M, cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+static smob_status check_opts(const smob_solve_opts* o) {
+    if (!o) throw SmobError(SMOB_ERR_ARG, "null solve options");
+    if (!(o->tol > 0) || o->restart < 1 || o->max_iters < 1) throw SmobError(SMOB_ERR_ARG, "invalid solve options");
+    if (o->precision != SMOB_PREC_FP64 && o->precision != SMOB_PREC_MIXED)
+        throw SmobError(SMOB_ERR_ARG, "unknown precision");
+    return SMOB_OK;
+}
+
+smob_status smob_solve_mob_device(smob_ctx* c, const double* d_force, double* d_vel, double* d_density,
+                                  const smob_solve_opts* o, smob_problem_stats* stats) {
+    return guarded([&]() -> smob_status {
+        need(c && d_force && d_vel, "null argument");
+        check_opts(o);
+        set_device(c);
+        smob_status s = solve_device(c, d_force, d_vel, d_density, o, stats);
+        prof_flush(c);
+        return s;
+    });
+}
+
+smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double* density, const smob_solve_opts* o,
+                           smob_problem_stats* stats) {
+    return guarded([&]() -> smob_status {
+        need(c && force && vel, "null argument");
+        check_opts(o);
+        set_device(c);
+        for (int i = 0; i < 6 * c->N; ++i)
+            if (!std::isfinite(force[i])) throw SmobError(SMOB_ERR_NONFINITE, "force/torque input is not finite");
+        ensure_solver(c, std::max(1, o->restart));
+        CUDA_OK(cudaMemcpyAsync(c->d_force.p, force, sizeof(double) * 6 * c->N, cudaMemcpyHostToDevice, c->st));
+        smob_status s = solve_device(c, c->d_force.as<double>(), c->d_vel.as<double>(),
+                                     density ? c->d_out.as<double>() : nullptr, o, stats);
+        CUDA_OK(cudaMemcpyAsync(vel, c->d_vel.p, sizeof(double) * 6 * c->N, cudaMemcpyDeviceToHost, c->st));
+        if (density)
+            CUDA_OK(cudaMemcpyAsync(density, c->d_out.p, sizeof(double) * 3 * c->M, cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        prof_flush(c);
+        return s;
+    });
+}
+
+smob_status smob_mob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, double alpha, double beta,
+                           const smob_solve_opts* o) {
+    return guarded([&]() -> smob_status {
+        need(c && X && Y && n_cols >= 1, "invalid argument");
+        const size_t n6 = 6 * (size_t)c->N;
+        std::vector<double> v(n6);
+        smob_status worst = SMOB_OK;
+        for (int col = 0; col < n_cols; ++col) {
+            smob_status s = smob_solve_mob(c, X + n6 * col, v.data(), nullptr, o, nullptr);
+            if (s != SMOB_OK && s != SMOB_ERR_NOT_CONVERGED) return s;
+            if (s != SMOB_OK) worst = s;
+            double* y = Y + n6 * col;
+            for (size_t i = 0; i < n6; ++i) y[i] = (beta == 0.0 ? 0.0 : beta * y[i]) + alpha * v[i];
+        }
+        return worst;
+    });
+}
+
+smob_status smob_device_alloc(smob_ctx* c, size_t bytes, void** ptr) {
+    return guarded([&]() -> smob_status {
+        need(c && ptr, "null argument");
+        set_device(c);
+        CUDA_OK(cudaMalloc(ptr, bytes ? bytes : 16));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_device_free(smob_ctx* c, void* ptr) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        if (ptr) CUDA_OK(cudaFree(ptr));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_memcpy_h2d(smob_ctx* c, void* dst, const void* src, size_t bytes) {
+    return guarded([&]() -> smob_status {
+        need(c && dst && src, "null argument");
+        set_device(c);
+        CUDA_OK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_memcpy_d2h(smob_ctx* c, void* dst, const void* src, size_t bytes) {
+    return guarded([&]() -> smob_status {
+        need(c && dst && src, "null argument");
+        set_device(c);
+        CUDA_OK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_synchronize(smob_ctx* c) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_profile_enable(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        prof_flush(c);
+        c->prof = on != 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_profile_count(const smob_ctx* c, int* n) {
+    return guarded([&]() -> smob_status {
+        need(c && n, "null argument");
+        *n = (int)c->prof_tab.size();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_profile_get(const smob_ctx* c, int i, char* name, int name_len, long long* launches, double* ms) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        need(i >= 0 && i < (int)c->prof_tab.size(), "profile index out of range");
+        auto it = c->prof_tab.begin();
+        std::advance(it, i);
+        if (name && name_len > 0) {
+            std::strncpy(name, it->first.c_str(), name_len - 1);
+            name[name_len - 1] = 0;
+        }
+        if (launches) *launches = it->second.launches;
+        if (ms) *ms = it->second.ms;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_profile_reset(smob_ctx* c) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        prof_flush(c);
+        c->prof_tab.clear();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_launch_count(const smob_ctx* c, long long* launches) {
+    return guarded([&]() -> smob_status {
+        need(c && launches, "null argument");
+        *launches = c->launches;
+        return SMOB_OK;
+    });
+}
+
+}  // extern "C"
+

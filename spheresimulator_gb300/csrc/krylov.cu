@@ -1,0 +1,219 @@
+// krylov.cu — device-side restarted GMRES building blocks for a batch of independent problems.
+//
+// Replaces the Belos pseudo-block GMRES that SphereSTKMobMat drives (BIE/SphereSTKMobMat.cpp:55-61,
+// 209-241; settings in mobilitySolver.yaml:3-16). Every vector of the batch is the concatenation
+// of the problems' segments; reductions run over fixed chunks that never cross a problem
+// boundary and are finalised in a fixed order, so each problem's arithmetic is the same alone
+// or inside any batch. Orthogonalisation is classical Gram-Schmidt applied twice (CGS2), which
+// gives the same Krylov basis to rounding as the reference's iterated modified Gram-Schmidt
+// while needing two reductions per pass instead of j+1 dependent ones.
+#include "krylov.h"
+
+namespace smob {
+
+namespace {
+
+__device__ __forceinline__ double block_reduce(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int i = 0; i < nw; ++i) s += red[i];
+    }
+    return s;
+}
+
+__global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* __restrict__ A, long long lda,
+                             const double* __restrict__ b, const unsigned char* __restrict__ active,
+                             double* __restrict__ partial, int nchunks) {
+    __shared__ double red[32];
+    const VecChunk ch = chunks[blockIdx.x];
+    if (active && !active[ch.problem]) return;
+    const int i = blockIdx.y;
+    const double* a = A + lda * i;
+    double s = 0;
+    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) s = fma(a[l], b[l], s);
+    s = block_reduce(s, red);
+    if (threadIdx.x == 0) partial[(long long)i * nchunks + blockIdx.x] = s;
+}
+
+// out[p*ostride + ooff + i] (+)= sum over the problem's chunks, i < nvec; optionally also into out2
+__global__ void k_chunk_finalize(const Problem* __restrict__ probs, int P, const double* __restrict__ partial,
+                                 int nchunks, int nvec, const unsigned char* __restrict__ active, double* out,
+                                 long long ostride, long long ooff, int accumulate, int take_sqrt, double* out2,
+                                 long long ostride2, int accumulate2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P * nvec) return;
+    const int p = t / nvec, i = t - p * nvec;
+    if (active && !active[p]) return;
+    const Problem pr = probs[p];
+    double s = 0;
+    for (int c = pr.c0; c < pr.c1; ++c) s += partial[(long long)i * nchunks + c];
+    if (take_sqrt) s = sqrt(s);
+    double* o = out + ostride * p + ooff + i;
+    *o = accumulate ? *o + s : s;
+    if (out2) {
+        double* o2 = out2 + ostride2 * p + i;
+        *o2 = accumulate2 ? *o2 + s : s;
+    }
+}
+
+// w[l] += sign * sum_{i < n_p} h[p*hstride + i] * V[i*ldv + l]
+__global__ void k_chunk_update(const VecChunk* __restrict__ chunks, const double* __restrict__ V, long long ldv,
+                               int nvec, const int* __restrict__ nvec_p, const double* __restrict__ h,
+                               long long hstride, double sign, const unsigned char* __restrict__ active,
+                               double* __restrict__ w) {
+    const VecChunk ch = chunks[blockIdx.x];
+    if (active && !active[ch.problem]) return;
+    const int n = nvec_p ? nvec_p[ch.problem] : nvec;
+    const double* hp = h + hstride * ch.problem;
+    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) {
+        double s = 0;
+        for (int i = 0; i < n; ++i) s = fma(hp[i], V[ldv * i + l], s);
+        w[l] = fma(sign, s, w[l]);
+    }
+}
+
+// dst[l] = src[l] * f(p) with f = 1/val[p] (invert) or val[p]
+__global__ void k_chunk_scale(const VecChunk* __restrict__ chunks, const double* __restrict__ src,
+                              const double* __restrict__ val, long long vstride, int invert,
+                              const unsigned char* __restrict__ active, double* __restrict__ dst) {
+    const VecChunk ch = chunks[blockIdx.x];
+    if (active && !active[ch.problem]) return;
+    double f = val[vstride * ch.problem];
+    if (invert) f = f != 0 ? 1.0 / f : 0.0;
+    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) dst[l] = src[l] * f;
+}
+
+// y = a*x + b*y on active problems (b == 0 overwrites)
+__global__ void k_chunk_axpby(const VecChunk* __restrict__ chunks, double a, const double* __restrict__ x, double b,
+                              const unsigned char* __restrict__ active, double* __restrict__ y) {
+    const VecChunk ch = chunks[blockIdx.x];
+    if (active && !active[ch.problem]) return;
+    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x)
+        y[l] = (b == 0.0) ? a * x[l] : fma(a, x[l], b * y[l]);
+}
+
+__global__ void k_cycle_init(int P, int m, const unsigned char* __restrict__ in_cycle, const double* __restrict__ beta,
+                             KrylovState* __restrict__ ks, double* __restrict__ H, double* __restrict__ gv) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !in_cycle[p]) return;
+    double* Hp = H + (long long)p * m * (m + 1);
+    for (int i = 0; i < m * (m + 1); ++i) Hp[i] = 0;
+    double* g = gv + (long long)p * (m + 1);
+    for (int i = 0; i <= m; ++i) g[i] = 0;
+    g[0] = beta[p];
+    ks[p].kcount = 0;
+}
+
+__global__ void k_givens(int P, int j, int m, KrylovState* __restrict__ ks, double* __restrict__ H,
+                         double* __restrict__ gv, double* __restrict__ cs, double* __restrict__ sn,
+                         const double* __restrict__ hnorm, unsigned char* __restrict__ active, int maxit) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !active[p]) return;
+    double* Hc = H + (long long)p * m * (m + 1) + (long long)j * (m + 1);
+    double* c = cs + (long long)p * m;
+    double* s = sn + (long long)p * m;
+    double* g = gv + (long long)p * (m + 1);
+    const double hn = hnorm[p];
+    Hc[j + 1] = hn;
+    for (int i = 0; i < j; ++i) {
+        const double a = Hc[i], b = Hc[i + 1];
+        Hc[i] = c[i] * a + s[i] * b;
+        Hc[i + 1] = -s[i] * a + c[i] * b;
+    }
+    const double a = Hc[j], b = Hc[j + 1];
+    const double d = hypot(a, b);
+    c[j] = d > 0 ? a / d : 1.0;
+    s[j] = d > 0 ? b / d : 0.0;
+    Hc[j] = d;
+    Hc[j + 1] = 0;
+    g[j + 1] = -s[j] * g[j];
+    g[j] = c[j] * g[j];
+    KrylovState& k = ks[p];
+    k.kcount = j + 1;
+    k.iters += 1;
+    k.passes32 += k.cycle_fp32;
+    k.passes64 += 1 - k.cycle_fp32;
+    const bool finite = isfinite(g[j + 1]) && isfinite(hn);
+    if (!finite) k.nonfinite = 1;
+    if (!finite || fabs(g[j + 1]) < k.tol_abs || hn == 0.0 || j + 1 == m || k.iters >= maxit) active[p] = 0;
+}
+
+__global__ void k_trisolve(int P, int m, const unsigned char* __restrict__ in_cycle, const KrylovState* __restrict__ ks,
+                           const double* __restrict__ H, const double* __restrict__ gv, double* __restrict__ y) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !in_cycle[p]) return;
+    const int k = ks[p].kcount;
+    const double* Hp = H + (long long)p * m * (m + 1);
+    const double* g = gv + (long long)p * (m + 1);
+    double* yp = y + (long long)p * m;
+    for (int i = k - 1; i >= 0; --i) {
+        double t = g[i];
+        for (int l = i + 1; l < k; ++l) t -= Hp[(long long)l * (m + 1) + i] * yp[l];
+        const double d = Hp[(long long)i * (m + 1) + i];
+        yp[i] = d != 0 ? t / d : 0.0;
+    }
+    for (int i = k; i < m; ++i) yp[i] = 0;
+}
+
+__global__ void k_kcount(int P, const KrylovState* __restrict__ ks, int* __restrict__ kc) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) kc[p] = ks[p].kcount;
+}
+
+}  // namespace
+
+int launch_dots(const KrylovLaunch& L, const double* A, long long lda, int nvec, const double* b,
+                const unsigned char* active, double* out, long long ostride, long long ooff, bool accumulate,
+                bool take_sqrt, cudaStream_t st, double* out2, long long ostride2, bool accumulate2) {
+    dim3 grid(L.nchunks, nvec);
+    k_chunk_dots<<<grid, 256, 0, st>>>(L.chunks, A, lda, b, active, L.partial, L.nchunks);
+    const int n = L.P * nvec;
+    k_chunk_finalize<<<(n + 127) / 128, 128, 0, st>>>(L.problems, L.P, L.partial, L.nchunks, nvec, active, out, ostride,
+                                                      ooff, accumulate ? 1 : 0, take_sqrt ? 1 : 0, out2, ostride2,
+                                                      accumulate2 ? 1 : 0);
+    return 2;
+}
+
+int launch_update(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const int* nvec_p, const double* h,
+                  long long hstride, double sign, const unsigned char* active, double* w, cudaStream_t st) {
+    k_chunk_update<<<L.nchunks, 256, 0, st>>>(L.chunks, V, ldv, nvec, nvec_p, h, hstride, sign, active, w);
+    return 1;
+}
+
+int launch_scale(const KrylovLaunch& L, const double* src, const double* val, long long vstride, bool invert,
+                 const unsigned char* active, double* dst, cudaStream_t st) {
+    k_chunk_scale<<<L.nchunks, 256, 0, st>>>(L.chunks, src, val, vstride, invert ? 1 : 0, active, dst);
+    return 1;
+}
+
+int launch_axpby_seg(const KrylovLaunch& L, double a, const double* x, double b, const unsigned char* active, double* y,
+                     cudaStream_t st) {
+    k_chunk_axpby<<<L.nchunks, 256, 0, st>>>(L.chunks, a, x, b, active, y);
+    return 1;
+}
+
+int launch_cycle_init(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const double* beta, KrylovState* ks,
+                      double* H, double* g, cudaStream_t st) {
+    k_cycle_init<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, m, in_cycle, beta, ks, H, g);
+    return 1;
+}
+
+int launch_givens(const KrylovLaunch& L, int j, int m, KrylovState* ks, double* H, double* g, double* cs, double* sn,
+                  const double* hnorm, unsigned char* active, int maxit, cudaStream_t st) {
+    k_givens<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, j, m, ks, H, g, cs, sn, hnorm, active, maxit);
+    return 1;
+}
+
+int launch_trisolve(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const KrylovState* ks, const double* H,
+                    const double* g, double* y, int* kc, cudaStream_t st) {
+    k_trisolve<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, m, in_cycle, ks, H, g, y);
+    k_kcount<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, ks, kc);
+    return 2;
+}
+
+}  // namespace smob

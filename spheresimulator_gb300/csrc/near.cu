@@ -1,0 +1,197 @@
+// near.cu — spectral near-field evaluation for near sphere pairs.
+//
+// Replaces NearEvaluator::operator() (BIE/SphereSTKSHOperator.cpp:575-695), driven by the
+// neighbour list that MPI/NearInteraction.txx:430-447 builds (pairs (t,s), t != s,
+// |c_s - c_t| < 1.5 (a_s + a_t)). The reference adds cTrac*(KL_spectral - direct) at the
+// target's grid points; the far-field kernel here never adds the direct part for near pairs,
+// so only the spectral value is evaluated:
+//   * k_near_sets: per near-source sphere, a sparse linear map (built on the host) takes the
+//     sphere's vector-SH coefficients to coefficient sets of its exterior Laplace potentials
+//     in irregular solid harmonics Th_n^m (degree <= p+3): 25 sets for the traction
+//     (div L and the Hessians of L_x, L_y, L_z, L_r) or 15 for the single layer
+//     (L_j, grad L_j, grad L_r);
+//   * k_near_eval: one CTA per (target sphere, tile of its grid points) walks the target's
+//     neighbour list in order, maps each point into the source's body frame scaled to the unit
+//     sphere, evaluates Th_n^m column by column with the stable three-term recurrence and
+//     contracts it with the sets (broadcast loads), then forms
+//       4 pi t_i = n_i div L - x_j n_k d_i d_k L_j + n_k d_i d_k L_r       (traction)
+//       8 pi u_i = L_i - x_j d_i L_j + d_i L_r                             (single layer, x radius)
+//     and rotates back into the lab frame. Accumulation per target point is in a fixed order.
+#include "smob_internal.h"
+
+namespace smob {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+__device__ __forceinline__ void qrot(const double* q, const double* v, double* o) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double tx = 2 * (y * v[2] - z * v[1]);
+    const double ty = 2 * (z * v[0] - x * v[2]);
+    const double tz = 2 * (x * v[1] - y * v[0]);
+    o[0] = v[0] + w * tx + (y * tz - z * ty);
+    o[1] = v[1] + w * ty + (z * tx - x * tz);
+    o[2] = v[2] + w * tz + (x * ty - y * tx);
+}
+
+template <typename Real>
+__global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real* __restrict__ mapval, bool trac,
+                            const int* __restrict__ slot_sphere, long long stride, Real* __restrict__ sets) {
+    const int slot = blockIdx.x;
+    const int s = slot_sphere[slot];
+    if (g.active && !g.active[g.prob[s]]) return;
+    const int p = g.order[s];
+    const OrderTables T = g.tabs[p];
+    const int nc = T.nc;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* cin = reinterpret_cast<Real*>(smem_raw);
+    const Real* src = coef + 2LL * g.coff[s];
+    for (int i = threadIdx.x; i < 6 * nc; i += blockDim.x) cin[i] = src[i];
+    __syncthreads();
+    const int base = trac ? T.trac_map : T.sl_map;
+    const int rows = trac ? T.trac_rows : T.sl_rows;
+    Real* out = sets + stride * slot;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+        const int e0 = g.map_rowptr[base + r], e1 = g.map_rowptr[base + r + 1];
+        Real acc = 0;
+        for (int e = e0; e < e1; ++e) acc += mapval[e] * cin[g.map_col[e]];
+        out[r] = acc;
+    }
+}
+
+template <typename Real, int NS>
+__device__ __forceinline__ void contract(const Real* __restrict__ set, int idx, Real tr, Real ti, Real* acc) {
+    const Real* c = set + 2 * NS * idx;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) acc[k] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[k]));
+}
+
+template <typename Real, bool TRAC>
+__global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride,
+                                                            const Real* __restrict__ th, int th_c1, int th_c2,
+                                                            int th_diag, double c, double* __restrict__ out) {
+    constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
+    const int t = blockIdx.x;
+    if (g.active && !g.active[g.prob[t]]) return;
+    const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
+    if (e0 == e1) return;
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const int ng = g.glen[t];
+    if (j >= ng) return;
+    const int i = g.gidx[t] + j;
+    const double X[3] = {g.coords[3 * i], g.coords[3 * i + 1], g.coords[3 * i + 2]};
+    const double Nl[3] = {g.norms[3 * i], g.norms[3 * i + 1], g.norms[3 * i + 2]};
+    const Real* c1 = th + th_c1;
+    const Real* c2 = th + th_c2;
+    const Real* dg = th + th_diag;
+    double res[3] = {0, 0, 0};
+    for (int e = e0; e < e1; ++e) {
+        const int s = g.nbr_src[e];
+        const int slot = g.near_src_slot[s];
+        const Real* S = sets + stride * slot;
+        const int Nd = g.order[s] + 3;
+        const double q[4] = {g.quat[4 * s], g.quat[4 * s + 1], g.quat[4 * s + 2], g.quat[4 * s + 3]};
+        const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+        const double a = g.radius[s];
+        const double rel[3] = {X[0] - g.center[3 * s], X[1] - g.center[3 * s + 1], X[2] - g.center[3 * s + 2]};
+        double xb[3], nb[3];
+        qrot(qc, rel, xb);
+        qrot(qc, Nl, nb);
+        const Real x = Real(xb[0] / a), y = Real(xb[1] / a), z = Real(xb[2] / a);
+        const Real r2 = x * x + y * y + z * z;
+        const Real ir2 = Real(1) / r2;
+        Real acc[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) acc[k] = 0;
+        Real dr = Real(1) / sqrt(r2), di = 0;  // Th_0^0
+        for (int m = 0; m <= Nd; ++m) {
+            if (m > 0) {
+                const Real f = -dg[m] * ir2;
+                const Real nr = f * (x * dr - y * di);
+                const Real ni = f * (x * di + y * dr);
+                dr = nr;
+                di = ni;
+            }
+            Real pr = 0, pi = 0, cr = dr, ci = di;
+            for (int n = m; n <= Nd; ++n) {
+                const int idx = n * (n + 1) / 2 + m;
+                contract<Real, NS>(S, idx, cr, ci, acc);
+                if (n < Nd) {
+                    const Real a1 = c1[idx], a2 = c2[idx];
+                    const Real nr = -(a1 * z * cr + a2 * pr) * ir2;
+                    const Real ni = -(a1 * z * ci + a2 * pi) * ir2;
+                    pr = cr;
+                    pi = ci;
+                    cr = nr;
+                    ci = ni;
+                }
+            }
+        }
+        double vb[3];
+        if (TRAC) {
+            const double n0 = nb[0], n1 = nb[1], n2 = nb[2];
+            const double xs[3] = {double(x), double(y), double(z)};
+            // symmetric index s(i,k): 00,11,22,01,02,12 -> 0..5
+            const int S3[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+            const double nn[3] = {n0, n1, n2};
+            for (int ii = 0; ii < 3; ++ii) {
+                double v = nn[ii] * double(acc[0]);
+                for (int kk = 0; kk < 3; ++kk) {
+                    double h = double(acc[19 + S3[ii][kk]]);
+                    for (int jj = 0; jj < 3; ++jj) h -= xs[jj] * double(acc[1 + 6 * jj + S3[ii][kk]]);
+                    v += nn[kk] * h;
+                }
+                vb[ii] = v / (4 * kPi);
+            }
+        } else {
+            const double xs[3] = {double(x), double(y), double(z)};
+            for (int ii = 0; ii < 3; ++ii) {
+                double v = double(acc[ii]) + double(acc[12 + ii]);
+                for (int jj = 0; jj < 3; ++jj) v -= xs[jj] * double(acc[3 + 3 * jj + ii]);
+                vb[ii] = a * v / (8 * kPi);
+            }
+        }
+        double vl[3];
+        qrot(q, vb, vl);
+        res[0] += vl[0];
+        res[1] += vl[1];
+        res[2] += vl[2];
+    }
+    out[3 * i] += c * res[0];
+    out[3 * i + 1] += c * res[1];
+    out[3 * i + 2] += c * res[2];
+}
+
+}  // namespace
+
+int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
+                     const int* slot_sphere, long long stride, cudaStream_t st) {
+    if (nslots <= 0) return 0;
+    const size_t sm = size_t(6 * ncoef(g.pmax)) * (fp32 ? sizeof(float) : sizeof(double));
+    if (fp32)
+        k_near_sets<float><<<nslots, 256, sm, st>>>(g, static_cast<const float*>(coef), g.map_val_f, trac, slot_sphere,
+                                                    stride, static_cast<float*>(sets));
+    else
+        k_near_sets<double><<<nslots, 256, sm, st>>>(g, static_cast<const double*>(coef), g.map_val_d, trac,
+                                                     slot_sphere, stride, static_cast<double*>(sets));
+    return 1;
+}
+
+int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
+                     cudaStream_t st) {
+    const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
+    dim3 grid(g.N, (gmax + kNearThreads - 1) / kNearThreads);
+    if (fp32) {
+        const float* s = static_cast<const float*>(sets);
+        if (trac) k_near_eval<float, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, out);
+        else k_near_eval<float, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, out);
+    } else {
+        const double* s = static_cast<const double*>(sets);
+        if (trac) k_near_eval<double, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, out);
+        else k_near_eval<double, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, out);
+    }
+    return 1;
+}
+
+}  // namespace smob

@@ -1,0 +1,125 @@
+// smob_internal.h — device data layout and kernel entry points of libsmob.
+//
+// Layout in HBM (one context = one batch of independent problems):
+//   spheres  : centre[3N], radius[N], quat[4N] (w,x,y,z), order[N], gidx/glen (point range),
+//              coff (coefficient offset, complex units), prob[N]
+//   points   : coords/norms[3M] (FP64 lab frame), weights[M], sid[M];
+//              pos32/nrm32 float4 (x,y,z relative to the problem's origin, w = sphere id bits);
+//              pos64/nrm64 double4 (same, FP64)
+//   near     : CSR by target sphere (nbr_start[N+1], nbr_src[pairs], sorted by source)
+//   far field: work items (target block x source-sphere chunk) and a partial-sum buffer
+//              laid out per problem as [chunk][point][3] (deterministic fixed-order reduction)
+//   tables   : per SH order p: Legendre tables at the Gauss-Legendre rings, DFT twiddles,
+//              and the sparse linear maps from VSH coefficients to the near-field coefficient sets
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace smob {
+
+constexpr int kMaxOrder = 32;
+constexpr int kFarThreads = 128;         // far-field CTA size (FP32: 2 targets per thread)
+constexpr int kFarTargets32 = 256;       // targets per FP32 far-field work item
+constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
+constexpr int kFarTile = 256;            // sources staged per shared-memory tile
+constexpr int kSphereThreads = 256;      // per-sphere transform CTA
+constexpr int kNearThreads = 128;        // near-field CTA (one target point per thread)
+constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
+constexpr int kNearSetsTrac = 25;        // div L, Hessians of L_x,L_y,L_z,L_r
+constexpr int kNearSetsSL = 15;          // L_j, grad L_j, grad L_r
+
+__host__ __device__ inline int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
+__host__ __device__ inline int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
+
+// per-order table descriptor (offsets into the table buffers, in elements)
+struct OrderTables {
+    int p, nt, nphi, nc;
+    int ring;        // offset of ct, st, wq arrays (nt each) in tab_d
+    int leg;         // offset of P, dP, Ps arrays (nt*nc each) in tab_d
+    int twiddle;     // offset of cos(m phi_k), sin(m phi_k) [(p+1)*nphi each] in tab_d
+    int cph;         // offset of cos(phi_k), sin(phi_k) [nphi each] in tab_d
+    int trac_map;    // offset into sparse map arrays (row pointer base), -1 if absent
+    int sl_map;
+    int trac_rows, sl_rows;  // rows = 2 * sets * ncoef(p+3)
+};
+
+struct FarItem {
+    int t0, t1;      // target point range (one problem)
+    int s0, s1;      // source sphere range (one problem)
+    int problem;
+    int chunk;       // chunk index within the problem
+};
+
+struct Problem {
+    int s0, s1;      // spheres
+    int p0, p1;      // points
+    int nchunks;     // far-field source chunks
+    long long poff;  // partial-buffer offset (elements of 3-vectors * chunks)
+    int v0, v1;      // vector element range [3*p0, 3*p1)
+    int c0, c1;      // reduction chunk range (segmented dots)
+};
+
+struct DevGeom {
+    int N, M, P;
+    int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
+    int th_c1, th_c2, th_diag;  // offsets of the irregular-solid-harmonic recurrence tables in tab_d/tab_f
+    const double* center;
+    const double* radius;
+    const double* quat;   // always present (identity filled in)
+    const int* order;
+    const int* gidx;
+    const int* glen;
+    const int* coff;      // complex offset of each sphere's 3*ncoef(p) coefficients
+    const int* prob;
+    const double* coords;
+    const double* norms;
+    const double* weights;
+    const int* sid;
+    const float4* pos32;
+    const float4* nrm32;
+    const double4* pos64;
+    const double4* nrm64;
+    const int* nbr_start;
+    const int* nbr_src;
+    const int* near_src_slot;  // per sphere: slot in the near-set buffer, -1 if not a near source
+    const Problem* problems;
+    const OrderTables* tabs;   // indexed by p (kMaxOrder+1 entries)
+    const double* tab_d;
+    const float* tab_f;
+    const int* map_rowptr;     // sparse maps (CSR, rows within a map are contiguous)
+    const int* map_col;
+    const double* map_val_d;
+    const float* map_val_f;
+    const unsigned char* active;  // per problem: operator work enabled
+};
+
+// ---------------------------------------------------------------- kernels (launch wrappers)
+// Every wrapper launches on `st` and returns the number of kernels it launched.
+// Far field: out[3M] += sum over far sources of c_sl*S + c_trac*K(dot n_target).
+int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4* src64, bool fp32,
+                    cudaStream_t st);
+int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
+                     const double4* src64, void* partial, cudaStream_t st);
+int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
+
+// Per-sphere operator: out += c_id*x + c_self*Self[x] + c_lop*L[x]; coefficients of x written to coef
+// (self_kind: -1 none, 0 single layer, 3 traction principal value).
+int launch_sphere_op(const DevGeom& g, const double* x, double* out, double c_id, double c_self, int self_kind,
+                     double c_lop, void* coef, bool fp32, cudaStream_t st);
+void configure_sphere_kernels();
+// Transforms only: coef (double) from grid (g2s), or grid from coef (s2g, overwrite)
+int launch_sh_g2s(const DevGeom& g, const double* grid, double* coef, cudaStream_t st);
+int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream_t st);
+
+// Near field: sets from coefficients (per near source sphere), then spectral evaluation per target sphere.
+int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
+                     const int* slot_sphere, long long stride, cudaStream_t st);
+int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
+                     cudaStream_t st);
+
+// Rigid-body pieces of the mobility solve
+int launch_rigid_density(const DevGeom& g, const double* force6n, double* rho, cudaStream_t st);
+int launch_rigid_average(const DevGeom& g, const double* u, double inv_visc, double* vel6n, cudaStream_t st);
+
+
+}  // namespace smob

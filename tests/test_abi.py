@@ -1,0 +1,75 @@
+"""The C-ABI library builds for sm_103a, loads, exports every entry point declared in
+include/*.h, and validates arguments on the host (no device compute here)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(smob_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    from spheresimulator_gb300 import _native
+    L = _native.lib()
+    decl = declared_functions()
+    assert len(decl) >= 25
+    missing = [n for n in decl if not hasattr(L, n)]
+    assert not missing, missing
+    raw = ctypes.CDLL(_native.library_path())
+    for n in decl:
+        getattr(raw, n)
+
+
+def test_library_is_sm103a():
+    from spheresimulator_gb300 import _build
+    assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH)
+    assert os.path.exists(_build.build())
+
+
+def test_argument_validation_on_host():
+    from spheresimulator_gb300 import _native as N
+    L = N.lib()
+    h = ctypes.c_void_p()
+    assert L.smob_create(ctypes.byref(h), None, 0) == N.SMOB_ERR_ARG
+    c = np.zeros((1, 3))
+    r = np.ones(1)
+    o = np.full(1, 8, np.int32)
+    geo = N.Geometry(0, N.dptr(c), N.dptr(r), None, N.iptr(o), None, 1.0)
+    assert L.smob_create(ctypes.byref(h), ctypes.byref(geo), 0) == N.SMOB_ERR_ARG
+    assert b"n_spheres" in L.smob_last_error()
+    geo = N.Geometry(1, N.dptr(c), N.dptr(r), None, N.iptr(o), None, -1.0)
+    assert L.smob_create(ctypes.byref(h), ctypes.byref(geo), 0) == N.SMOB_ERR_ARG
+    assert L.smob_destroy(None) == N.SMOB_OK
+    major, minor = ctypes.c_int(), ctypes.c_int()
+    assert L.smob_version(ctypes.byref(major), ctypes.byref(minor)) == N.SMOB_OK
+
+
+def test_no_device_is_reported_not_faked():
+    """Without a GPU the library refuses to run instead of falling back to the CPU."""
+    from conftest import gpu_available
+    if gpu_available():
+        pytest.skip("a GPU is present")
+    from spheresimulator_gb300 import SphereSTKSHOperator, SmobError
+    with pytest.raises(SmobError) as e:
+        SphereSTKSHOperator([[0, 0, 0]], [1.0], [8])
+    assert e.value.code == 7
+
+
+def test_structures_match_header():
+    """ctypes mirrors of smob_geometry / smob_solve_opts / smob_problem_stats have the C layout."""
+    from spheresimulator_gb300 import _native as N
+    assert ctypes.sizeof(N.Geometry) == 56
+    assert ctypes.sizeof(N.SolveOpts) == 32
+    assert ctypes.sizeof(N.ProblemStats) == 40

@@ -1,0 +1,225 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 CPU oracle.
+
+Tolerances: FP64 kernels agree with the oracle to 1e-11 relative (summation order only);
+FP32 kernels to 2e-5 relative (single-precision pair sums); FP64 solves to 1e-8 relative in
+the velocities at tol 1e-12; mixed-precision solves to 1e-6 relative at tol 1e-10.
+"""
+import numpy as np
+import pytest
+
+from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SmobError, SphereSTKMobMat, SphereSTKSHOperator, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def cluster(seed=0, n=5, p=6, quats=True, gap=0.25):
+    return configs.small_cluster(seed=seed, n=n, p=p, gap=gap, quats=quats)
+
+
+def make(cfg, cls=SphereSTKSHOperator, **kw):
+    return cls(cfg["centers"], cfg["radii"], cfg["orders"], quats=cfg.get("quats"), problem=cfg.get("problem"), **kw)
+
+
+def oracle_op(oracle, cfg, **kw):
+    return oracle.Operator(cfg["centers"], cfg["radii"], cfg["orders"], quats=cfg.get("quats"), **kw)
+
+
+def test_grid_matches_oracle(oracle):
+    cfg = cluster(1)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    c, n, w = o.grid()
+    assert np.abs(g.getGridCoords() - c).max() < 1e-13
+    assert np.abs(g.getGridNorms() - n).max() < 1e-14
+    assert np.abs(g.getGridWeights() - w).max() < 1e-14
+    t, s = g.near_pairs()
+    to, so = o.pairs()
+    assert len(t) > 0 and np.array_equal(t, to) and np.array_equal(s, so)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_far_field(oracle, seed):
+    cfg = cluster(seed)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(3 * g.n_points)
+    for c_sl, c_tr in ((0.0, 1.0), (1.0, 0.0), (0.7, -1.3)):
+        ref = o.far_traction(x, c_tr, excl_near=True) + o.far_sl(x, c_sl, excl_near=True)
+        assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_FP64), ref) < 1e-11
+        assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_MIXED), ref) < 2e-5
+
+
+def test_transforms(oracle):
+    cfg = cluster(2, n=3, p=9)
+    g = make(cfg)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((g.n_points, 3))
+    co = g.sh_g2s(x.reshape(-1))
+    off = g.coeff_offsets()
+    gi = g.getGridNumberIndex()
+    for i in range(g.n_spheres):
+        p = int(cfg["orders"][i])
+        ng = (p + 1) * (2 * p + 2)
+        ref = oracle.sh_g2s(p, x[gi[i]:gi[i] + ng], cfg["quats"][i])
+        assert np.abs(co[off[i]:off[i + 1]] - ref).max() < 1e-12 * np.abs(ref).max()
+    back = g.sh_s2g(co).reshape(-1, 3)
+    for i in range(g.n_spheres):
+        p = int(cfg["orders"][i])
+        ng = (p + 1) * (2 * p + 2)
+        ref = oracle.sh_s2g(p, co[off[i]:off[i + 1]], cfg["quats"][i])
+        assert np.abs(back[gi[i]:gi[i] + ng] - ref).max() < 1e-12 * np.abs(ref).max()
+    proj = g.projectNullSpace(x.reshape(-1))
+    assert np.abs(proj - back.reshape(-1)).max() < 1e-13 * np.abs(back).max()
+
+
+@pytest.mark.parametrize("coefs", [(0.5, 0.0, 1.0), (-0.5, 0.0, -1.0), (0.0, 1.0, 0.0), (0.2, 0.8, -0.4)])
+def test_apply_p2p(oracle, coefs):
+    cfg = cluster(3, n=5, p=7)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(3 * g.n_points)
+    y0 = rng.standard_normal(3 * g.n_points)
+    ref = o.apply_p2p(x, *coefs, out=y0)
+    out = g.applyP2POP(x, y0, *coefs, precision=PREC_FP64)
+    assert rel(out - y0, ref - y0) < 1e-11
+    out32 = g.applyP2POP(x, y0, *coefs, precision=PREC_MIXED)
+    assert rel(out32 - y0, ref - y0) < 2e-5
+
+
+def test_near_field_is_spectral_part(oracle):
+    """far(excluding near spheres) + near(spectral) equals the reference decomposition
+    far(all other spheres) + near(spectral - direct)."""
+    cfg = cluster(5, n=6, p=8)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    assert g.n_near_pairs > 0
+    x = np.random.default_rng(5).standard_normal(3 * g.n_points)
+    mine = g.far_field(x, 0.3, 1.0) + g.near_field(x, 0.3, 1.0)
+    ref = o.far_traction(x, 1.0) + o.far_sl(x, 0.3) + o.near_correction(x, 0.3, 1.0)
+    assert rel(mine, ref) < 1e-11
+
+
+def test_apply_lop_and_apply(oracle):
+    cfg = cluster(6, n=4, p=6)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal(3 * g.n_points)
+    assert rel(g.applyLOP(x, cLOP=1.7), o.apply_lop(x, 1.7)) < 1e-13
+    y = rng.standard_normal(3 * g.n_points)
+    assert rel(g.apply(x, y, alpha=0.7, beta=-0.3), o.apply(x, y, 0.7, -0.3)) < 1e-11
+    X = rng.standard_normal((3, 3 * g.n_points))
+    Y = g.apply(X)
+    for k in range(3):
+        assert rel(Y[k], o.apply(X[k])) < 1e-11
+
+
+def test_apply_cfg2_scale(oracle):
+    """Cfg 2 geometry (64 spheres, p=16): one operator application against the oracle."""
+    cfg = configs.cfg2()
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    x = np.random.default_rng(7).standard_normal(3 * g.n_points)
+    ref = o.apply(x)
+    assert rel(g.apply(x), ref) < 1e-11
+    assert rel(g.apply(x, precision=PREC_MIXED), ref) < 2e-5
+
+
+@pytest.mark.parametrize("which", ["cfg1", "cluster"])
+def test_solve_mob_fp64(oracle, which):
+    cfg = configs.cfg1() if which == "cfg1" else cluster(8, n=6, p=8)
+    g = make(cfg, SphereSTKMobMat)
+    o = oracle_op(oracle, cfg)
+    ref = o.solve_mob(cfg["force"], tol=1e-12, restart=50, maxit=500)
+    vel = g.solveMob(cfg["force"], tol=1e-12, restart=50, max_iters=500)
+    assert rel(vel, ref["vel"]) < 1e-8
+    assert rel(g.getDensitySolution(), ref["density"]) < 1e-8
+    st = g.last_stats[0]
+    assert st["status"] == 0 and st["relres"] < 1e-12
+    assert abs(st["iterations"] - ref["iters"]) <= 1
+
+
+def test_solve_mob_mixed(oracle):
+    cfg = cluster(9, n=6, p=8)
+    g = make(cfg, SphereSTKMobMat)
+    o = oracle_op(oracle, cfg)
+    ref = o.solve_mob(cfg["force"], tol=1e-12)
+    vel = g.solveMob(cfg["force"], tol=1e-10, precision=PREC_MIXED)
+    st = g.last_stats[0]
+    assert st["status"] == 0 and st["relres"] < 1e-10
+    assert st["operator_passes_fp32"] > 0
+    assert rel(vel, ref["vel"]) < 1e-6
+
+
+def test_restart_small(oracle):
+    """GMRES(5) with restarts reaches the same solution."""
+    cfg = cluster(10, n=5, p=6)
+    g = make(cfg, SphereSTKMobMat)
+    o = oracle_op(oracle, cfg)
+    ref = o.solve_mob(cfg["force"], tol=1e-11, restart=5, maxit=400)
+    vel = g.solveMob(cfg["force"], tol=1e-11, restart=5, max_iters=400)
+    assert rel(vel, ref["vel"]) < 1e-8
+    assert g.last_stats[0]["refinements"] > 1
+
+
+def test_batched_equals_alone():
+    """Problems solved together give bitwise the same result as each solved alone."""
+    a = cluster(11, n=4, p=6)
+    b = cluster(12, n=7, p=8)
+    cat = dict(centers=np.concatenate([a["centers"], b["centers"] + 100]), radii=np.concatenate([a["radii"], b["radii"]]),
+               orders=np.concatenate([a["orders"], b["orders"]]), quats=np.concatenate([a["quats"], b["quats"]]),
+               problem=np.concatenate([np.zeros(4, np.int32), np.ones(7, np.int32)]))
+    F = np.concatenate([a["force"], b["force"]])
+    for prec in (PREC_FP64, PREC_MIXED):
+        va = make(a, SphereSTKMobMat).solveMob(a["force"], tol=1e-10, precision=prec)
+        vb = make(b, SphereSTKMobMat).solveMob(b["force"], tol=1e-10, precision=prec)
+        gb = make(cat, SphereSTKMobMat)
+        v = gb.solveMob(F, tol=1e-10, precision=prec)
+        assert np.array_equal(v[:24], va) and np.array_equal(v[24:], vb)
+        assert len(gb.last_stats) == 2
+
+
+def test_isolated_sphere_drag_gpu():
+    rng = np.random.default_rng(13)
+    q = rng.standard_normal(4)
+    g = SphereSTKMobMat([[1.0, 2.0, -3.0]], [0.8], [10], quats=q / np.linalg.norm(q), viscosity=1.7)
+    F = rng.standard_normal(6)
+    v = g.solveMob(F)
+    assert np.allclose(v[:3], F[:3] / (6 * np.pi * 1.7 * 0.8), rtol=1e-11)
+    assert np.allclose(v[3:], F[3:] / (8 * np.pi * 1.7 * 0.8 ** 3), rtol=1e-11)
+    assert g.last_stats[0]["iterations"] == 0
+
+
+def test_determinism_and_warm_start():
+    cfg = cluster(14, n=5, p=7)
+    g = make(cfg, SphereSTKMobMat)
+    v1 = g.solveMob(cfg["force"], tol=1e-10)
+    it1 = g.last_stats[0]["iterations"]
+    v2 = make(cfg, SphereSTKMobMat).solveMob(cfg["force"], tol=1e-10)
+    assert np.array_equal(v1, v2)
+    v3 = g.solveMob(cfg["force"], tol=1e-10, warm_start=True)
+    assert g.last_stats[0]["iterations"] < it1
+    assert rel(v3, v1) < 1e-9
+
+
+def test_error_paths():
+    cfg = cluster(15, n=3, p=5)
+    g = make(cfg, SphereSTKMobMat)
+    f = cfg["force"].copy()
+    f[2] = np.nan
+    with pytest.raises(SmobError) as e:
+        g.solveMob(f)
+    assert e.value.code == 5
+    with pytest.raises(SmobError) as e:
+        SphereSTKSHOperator([[0, 0, 0], [1.5, 0, 0]], [1, 1], [6, 6])
+    assert e.value.code == 1
+    v = g.solveMob(np.zeros(18))
+    assert np.all(v == 0) and g.last_stats[0]["iterations"] == 0
+    v = g.solveMob(cfg["force"], tol=1e-14, max_iters=3, raise_on_not_converged=False)
+    assert g.last_stats[0]["status"] == 4 and g.last_stats[0]["iterations"] == 3
