@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 sphere mobility solve (one JSON line on rank 0).
+
+Workload (one "step"): one mobility solve of configuration 2 — 64 rigid spheres of radius 1
+placed by seeded random sequential addition in a box of side 20 (min surface gap 0.1),
+SH order 16 (36,992 grid points), N(0,1) forces and torques — to 1e-8 relative residual with
+GMRES(50). The headline arm is the mixed-precision solve (FP32 operator inside FP64 iterative
+refinement); the plain FP64 GPU solve of the same problem is timed beside it.
+
+  value : solves/s with the forces already resident in HBM (smob_solve_mob_device), each step timed
+          with CUDA events on the library's stream, L2 evicted (256 MB write) between steps
+  e2e   : the same through smob_solve_mob with host buffers (pinned when torch is importable):
+          host->device copy of the 6N forces and device->host copy of the 6N velocities inside
+  roofline : the dominant kernel (FP32 traction far field): algorithmic FLOPs (30 per pair) per launch
+          / average launch time, against the FP32 FMA issue rate measured in the same run
+  cpu_baseline : the FP64 C++/OpenMP restatement of the reference path, on this host's cores
+
+--impl reference times that CPU restatement alone (the reference itself cannot be built: its
+SCTL/STKFMM/Trilinos dependencies are absent), on the same workload and metric.
+Multi-GPU: replicas only (each rank solves its own copy of the workload on its own GPU).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "mobility solves/s & p50/p99 latency at 1e-8 resid, mixed vs plain FP64 GPU"
+TOL = 1e-8
+RESTART = 50
+L2_FLUSH_BYTES = 256 << 20
+WORKLOAD = ("cfg2: 64 spheres a=1, seeded RSA in box 20 (min gap 0.1), p=16 (36992 points), "
+            "N(0,1) force/torque, GMRES(50) to 1e-8 relative residual")
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def far_pairs(mob):
+    """Pairs per far-field launch: all target-source pairs of different spheres minus the near pairs'
+    sphere blocks (those are evaluated spectrally)."""
+    ng = np.array([(p + 1) * (2 * p + 2) for p in mob.orders], dtype=np.int64)
+    M = ng.sum()
+    pairs = M * M - (ng * ng).sum()
+    t, s = mob.near_pairs()
+    pairs -= (ng[t] * ng[s]).sum()
+    return int(pairs)
+
+
+def run_native(args, world, rank, local, dist):
+    import ctypes
+
+    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKMobMat, configs, solve_opts
+    from spheresimulator_gb300 import _native as N
+
+    L = N.lib()
+    cfg = configs.cfg2()
+    mob = SphereSTKMobMat(cfg["centers"], cfg["radii"], cfg["orders"], device=local)
+    h = mob.handle
+    n6 = 6 * mob.n_spheres
+    force = np.ascontiguousarray(cfg["force"])
+    d_force, d_vel = ctypes.c_void_p(), ctypes.c_void_p()
+    N.check(L.smob_device_alloc(h, 8 * n6, ctypes.byref(d_force)))
+    N.check(L.smob_device_alloc(h, 8 * n6, ctypes.byref(d_vel)))
+    N.check(L.smob_memcpy_h2d(h, d_force, force.ctypes.data_as(ctypes.c_void_p), 8 * n6))
+    stats = (N.ProblemStats * 1)()
+
+    def solve_dev(prec):
+        o = solve_opts(TOL, RESTART, 1000, prec)
+        code = L.smob_solve_mob_device(h, d_force, d_vel, None, ctypes.byref(o), stats)
+        N.check(code)
+        return stats[0].as_dict()
+
+    def timed(prec, steps):
+        ms = []
+        st = None
+        for _ in range(steps):
+            N.check(L.smob_flush_l2(h, L2_FLUSH_BYTES))
+            N.check(L.smob_timer_mark(h))
+            st = solve_dev(prec)
+            t = ctypes.c_double()
+            N.check(L.smob_timer_elapsed(h, ctypes.byref(t)))
+            ms.append(t.value)
+        return np.array(ms), st
+
+    for _ in range(args.warmup):
+        solve_dev(PREC_MIXED)
+    solve_dev(PREC_FP64)
+
+    # ---- headline: mixed precision, inputs resident
+    barrier(dist)
+    l0 = mob.launch_count()
+    with ClockSampler(local) as clk:
+        ms_mixed, st_mixed = timed(PREC_MIXED, args.steps)
+    launches = (mob.launch_count() - l0) / max(args.steps, 1)
+    total_s = allmax(dist, ms_mixed.sum() / 1e3)
+    vel_mixed = np.zeros(n6)
+    N.check(L.smob_memcpy_d2h(h, vel_mixed.ctypes.data_as(ctypes.c_void_p), d_vel, 8 * n6))
+
+    # ---- plain FP64 GPU solve of the same problem
+    fp64_steps = max(1, min(args.steps, args.fp64_steps))
+    ms_fp64, st_fp64 = timed(PREC_FP64, fp64_steps)
+    vel_fp64 = np.zeros(n6)
+    N.check(L.smob_memcpy_d2h(h, vel_fp64.ctypes.data_as(ctypes.c_void_p), d_vel, 8 * n6))
+
+    # ---- end to end through the host-pointer API
+    try:
+        import torch
+        hf = torch.from_numpy(force).pin_memory()
+        hv = torch.zeros(n6, dtype=torch.float64).pin_memory()
+        fptr = ctypes.cast(hf.data_ptr(), N._DP)
+        vptr = ctypes.cast(hv.data_ptr(), N._DP)
+        pinned = True
+    except Exception:
+        hv_np = np.zeros(n6)
+        fptr, vptr = N.dptr(force), N.dptr(hv_np)
+        pinned = False
+    e2e_ms = []
+    for _ in range(args.steps):
+        N.check(L.smob_flush_l2(h, L2_FLUSH_BYTES))
+        o = solve_opts(TOL, RESTART, 1000, PREC_MIXED)
+        N.check(L.smob_timer_mark(h))
+        N.check(L.smob_solve_mob(h, fptr, vptr, None, ctypes.byref(o), stats))
+        t = ctypes.c_double()
+        N.check(L.smob_timer_elapsed(h, ctypes.byref(t)))
+        e2e_ms.append(t.value)
+    e2e_total = allmax(dist, sum(e2e_ms) / 1e3)
+
+    # ---- instrumented pass: per-kernel CUDA-event times on the library stream
+    mob.profile(True)
+    mob.profile_reset()
+    solve_dev(PREC_MIXED)
+    prof = mob.profile_table()
+    mob.profile(False)
+    f32, f64 = ctypes.c_double(), ctypes.c_double()
+    N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
+
+    if rank != 0:
+        return None
+    pairs = far_pairs(mob)
+    k_l, k_ms = prof.get("far_trac_fp32", (0, 0.0))
+    avg_s = (k_ms / max(k_l, 1)) / 1e3
+    achieved = 30.0 * pairs / avg_s / 1e12 if avg_s > 0 else None
+    tot_prof = sum(v[1] for v in prof.values())
+
+    # ---- CPU baseline: one FP64 operator pass of the oracle, times the FP64 solve's pass count
+    cpu = cpu_sample(cfg, st_fp64["operator_passes_fp64"], args.cpu_threads)
+
+    value = world * args.steps / total_s
+    line = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(float(ms_mixed.mean()), 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 operator + f64 refinement (mixed)",
+        "data": "synthetic (seeded RSA packing, N(0,1) forces)",
+        "config": {"workload": WORKLOAD, "tol": TOL, "restart": RESTART, "precision": "mixed",
+                   "l2": "flushed between steps (256 MB device write)", "parallelism": "replicas only"},
+        "latency_ms": {"p50": round(float(np.percentile(ms_mixed, 50)), 4),
+                       "p99": round(float(np.percentile(ms_mixed, 99)), 4)},
+        "mixed": {"iterations": st_mixed["iterations"], "refinements": st_mixed["refinements"],
+                  "passes_fp32": st_mixed["operator_passes_fp32"], "passes_fp64": st_mixed["operator_passes_fp64"],
+                  "relres": st_mixed["relres"]},
+        "fp64": {"solves_per_s": round(world * len(ms_fp64) / allmax(None, ms_fp64.sum() / 1e3), 4),
+                 "p50_ms": round(float(np.percentile(ms_fp64, 50)), 3),
+                 "p99_ms": round(float(np.percentile(ms_fp64, 99)), 3),
+                 "iterations": st_fp64["iterations"], "passes_fp64": st_fp64["operator_passes_fp64"],
+                 "relres": st_fp64["relres"], "steps": len(ms_fp64)},
+        "mixed_vs_fp64_speedup": round(float(ms_fp64.mean() / ms_mixed.mean()), 3),
+        "rel_err_mixed_vs_fp64": float(np.linalg.norm(vel_mixed - vel_fp64) / np.linalg.norm(vel_fp64)),
+        "pair_interactions_per_s": round(pairs * (st_mixed["operator_passes_fp32"] + st_mixed["operator_passes_fp64"])
+                                         / (ms_mixed.mean() / 1e3), 1),
+        "roofline": {"kernel": "far_trac_fp32", "bound": "fp32_simt", "achieved": round(achieved, 3) if achieved else None,
+                     "peak": round(f32.value, 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / f32.value, 4) if achieved else None, "traffic": None,
+                     "peak_source": "FP32 FMA issue rate measured in this run (MEASURED_PEAKS.json has no SIMT entry)",
+                     "flops_per_launch": 30.0 * pairs, "pairs_per_launch": pairs,
+                     "avg_launch_ms": round(avg_s * 1e3, 5), "launches_in_profiled_solve": k_l,
+                     "share_of_kernel_time": round(k_ms / tot_prof, 4) if tot_prof else None,
+                     "fp64_fma_peak_tflops": round(f64.value, 4)},
+        "kernel_ms_profiled_solve": {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items())},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(world * args.steps / e2e_total, 4), "unit": "solves/s",
+                "h2d_bytes_per_step": 8 * n6, "d2h_bytes_per_step": 8 * n6,
+                "host_buffers": "pinned" if pinned else "pageable"},
+        "gpu_launches": int(round(launches)),
+        "clocks": clk.summary(),
+    }
+    return line
+
+
+def cpu_sample(cfg, passes, threads):
+    from oracle import oracle as O
+    nthreads = threads or os.cpu_count()
+    O.set_threads(nthreads)
+    op = O.Operator(cfg["centers"], cfg["radii"], cfg["orders"])
+    x = np.random.default_rng(0).standard_normal(3 * op.m)
+    op.apply(x)
+    t0 = time.perf_counter()
+    op.apply(x)
+    dt = time.perf_counter() - t0
+    return {"value": round(1.0 / (dt * passes), 6), "unit": "solves/s", "cores": nthreads, "kind": "port",
+            "sample": "one FP64 operator pass (0.5I+K+L) of the full cfg2 workload timed = %.3f s, times %d passes "
+                      "(the operator passes of the FP64 solve at 1e-8)" % (dt, passes)}
+
+
+def run_reference(args, rank):
+    """CPU restatement of the reference path (the reference itself cannot be built here)."""
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    from spheresimulator_gb300 import configs
+    nthreads = args.cpu_threads or os.cpu_count()
+    O.set_threads(nthreads)
+    cfg = configs.cfg2()
+    op = O.Operator(cfg["centers"], cfg["radii"], cfg["orders"])
+    # passes of one full FP64 oracle solve at the metric's tolerance (run once, untimed)
+    r = op.solve_mob(cfg["force"], tol=TOL, restart=RESTART, maxit=1000)
+    passes = r["iters"] + 3 + (1 if r["iters"] else 0)
+    x = np.random.default_rng(0).standard_normal(3 * op.m)
+    for _ in range(max(1, args.warmup)):
+        op.apply(x)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        op.apply(x)
+        ts.append(time.perf_counter() - t0)
+    ts = np.array(ts) * passes
+    value = args.steps / ts.sum()
+    cpu = {"value": round(value, 6), "unit": "solves/s", "cores": nthreads, "kind": "port",
+           "sample": "per step: one FP64 operator pass (0.5I+K+L) of the full cfg2 workload, times %d passes "
+                     "(iterations + b + restart residual + final single layer of one full oracle solve at 1e-8)"
+                     % passes}
+    return {"metric": METRIC, "value": round(value, 6), "unit": "solves/s", "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(ts.mean() * 1e3), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded RSA packing, N(0,1) forces)",
+            "config": {"workload": WORKLOAD, "tol": TOL, "restart": RESTART, "precision": "fp64"},
+            "latency_ms": {"p50": round(float(np.percentile(ts, 50) * 1e3), 3),
+                           "p99": round(float(np.percentile(ts, 99) * 1e3), 3)},
+            "cpu_baseline": cpu, "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0},
+            "oracle_solve": {"iterations": r["iters"], "relres": r["relres"]}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "native":
+        args.warmup = 3
+    world, rank, local, dist = dist_init()
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+    else:
+        line = run_native(args, world, rank, local, dist)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

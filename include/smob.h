@@ -146,6 +146,15 @@ smob_status smob_profile_get(const smob_ctx* ctx, int i, char* name, int name_le
 smob_status smob_profile_reset(smob_ctx* ctx);
 /* total kernel launches issued by the library on this context since creation */
 smob_status smob_launch_count(const smob_ctx* ctx, long long* launches);
+/* CUDA-event interval on the context's stream: mark records a start event; elapsed records an
+ * end event, waits for it and returns the milliseconds since the last mark */
+smob_status smob_timer_mark(smob_ctx* ctx);
+smob_status smob_timer_elapsed(smob_ctx* ctx, double* ms);
+/* writes `bytes` of a scratch buffer on the context's stream (used to evict L2 between timings) */
+smob_status smob_flush_l2(smob_ctx* ctx, size_t bytes);
+/* FP32 / FP64 FMA issue rate of a device in TFLOP/s (independent FMA chains): the SIMT roofline
+ * denominators of the far-field kernels, measured in the same run */
+smob_status smob_measure_fma_peaks(int device, double* fp32_tflops, double* fp64_tflops);
 
 #ifdef __cplusplus
 }

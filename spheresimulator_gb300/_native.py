@@ -100,6 +100,10 @@ def lib():
                                  _DP]),
         "smob_profile_reset": (S, [_VP]),
         "smob_launch_count": (S, [_VP, ctypes.POINTER(ctypes.c_longlong)]),
+        "smob_timer_mark": (S, [_VP]),
+        "smob_timer_elapsed": (S, [_VP, _DP]),
+        "smob_flush_l2": (S, [_VP, ctypes.c_size_t]),
+        "smob_measure_fma_peaks": (S, [ctypes.c_int, _DP, _DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -108,6 +108,9 @@ struct smob_ctx {
 
     DevGeom g{};
     long long launches = 0;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    DBuf d_flush;
+    unsigned flush_val = 1;
 
     // profiling
     bool prof = false;
@@ -137,6 +140,8 @@ struct smob_ctx {
             cudaEventDestroy(p.a);
             cudaEventDestroy(p.b);
         }
+        if (ev_a) cudaEventDestroy(ev_a);
+        if (ev_b) cudaEventDestroy(ev_b);
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -1252,6 +1257,43 @@ smob_status smob_launch_count(const smob_ctx* c, long long* launches) {
     return guarded([&]() -> smob_status {
         need(c && launches, "null argument");
         *launches = c->launches;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_timer_mark(smob_ctx* c) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        if (!c->ev_a) {
+            CUDA_OK(cudaEventCreate(&c->ev_a));
+            CUDA_OK(cudaEventCreate(&c->ev_b));
+        }
+        CUDA_OK(cudaEventRecord(c->ev_a, c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_timer_elapsed(smob_ctx* c, double* ms) {
+    return guarded([&]() -> smob_status {
+        need(c && ms, "null argument");
+        need(c->ev_a != nullptr, "smob_timer_mark was not called");
+        CUDA_OK(cudaEventRecord(c->ev_b, c->st));
+        CUDA_OK(cudaEventSynchronize(c->ev_b));
+        float f = 0;
+        CUDA_OK(cudaEventElapsedTime(&f, c->ev_a, c->ev_b));
+        *ms = f;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_flush_l2(smob_ctx* c, size_t bytes) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        c->d_flush.alloc(bytes);
+        CUDA_OK(cudaMemsetAsync(c->d_flush.p, int(c->flush_val++ & 0xff), bytes, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
 }

@@ -169,10 +169,11 @@ def test_restart_small(oracle):
 
 
 def test_batched_equals_alone():
-    """Problems solved together give bitwise the same result as each solved alone."""
+    """Problems solved together give bitwise the same result as each solved alone (problems of a
+    batch may overlap in space: they never interact)."""
     a = cluster(11, n=4, p=6)
     b = cluster(12, n=7, p=8)
-    cat = dict(centers=np.concatenate([a["centers"], b["centers"] + 100]), radii=np.concatenate([a["radii"], b["radii"]]),
+    cat = dict(centers=np.concatenate([a["centers"], b["centers"]]), radii=np.concatenate([a["radii"], b["radii"]]),
                orders=np.concatenate([a["orders"], b["orders"]]), quats=np.concatenate([a["quats"], b["quats"]]),
                problem=np.concatenate([np.zeros(4, np.int32), np.ones(7, np.int32)]))
     F = np.concatenate([a["force"], b["force"]])
