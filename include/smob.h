@@ -117,6 +117,24 @@ smob_status smob_sh_g2s(smob_ctx* ctx, const double* grid3m, double* coeff);
 smob_status smob_sh_s2g(smob_ctx* ctx, const double* coeff, double* grid3m);
 smob_status smob_coeff_offsets(const smob_ctx* ctx, int* offsets /* N+1, in doubles */);
 
+/* Traction far field that allocates no device memory. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc where they need the far field: a host application
+ * that has reserved (nearly) all GPU memory for its own pool leaves nothing to allocate, and a
+ * loop that applies the operator thousands of times cannot pay for cudaMalloc/cudaFree (cudaFree
+ * synchronizes the device). Everything is passed as device pointers: coords/norms/density (3n),
+ * weights (n), sphere id per point (n); out (3n) += -3/(4 pi) * sum over points j on other spheres
+ * of r (r . f_j)(r . n_i)/r^5 with f_j = c * weights[j] * density[j], r = x_i - x_j (near-pair
+ * spheres are not excluded). stream: a cudaStream_t, or NULL for the default stream.
+ * Limit: 1 <= n_points <= 40960, otherwise SMOB_ERR_ARG. The scratch (per-chunk partial sums) is
+ * a fixed 7.5 MiB __device__ array that every GPU loading the library keeps until exit; all calls
+ * on a device share it and it keeps the last call's contents, so calls that overlap on the GPU
+ * (different streams, or host threads) race. The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture. */
+smob_status smob_far_traction_noalloc(const double* d_coords, const double* d_norms, const double* d_weights,
+                                      const double* d_density, const int* d_sphere, int n_points, double c,
+                                      double* d_out, void* stream);
+
 /* ---- SphereSTKMobMat (BIE/SphereSTKMobMat.hpp:26-79) ---- */
 /* force6N -> vel6N for every problem of the context; density3M (may be NULL) receives rho+mu
  * (getDensitySolution, hpp:76); stats (may be NULL) has one entry per problem.

@@ -104,6 +104,7 @@ def lib():
         "smob_timer_elapsed": (S, [_VP, _DP]),
         "smob_flush_l2": (S, [_VP, ctypes.c_size_t]),
         "smob_measure_fma_peaks": (S, [ctypes.c_int, _DP, _DP]),
+        "smob_far_traction_noalloc": (S, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_double, _VP, _VP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -77,6 +77,11 @@ constexpr double kPi = 3.14159265358979323846264338327950288;
 
 }  // namespace
 
+namespace smob {
+// lets entry points outside this file report their message through smob_last_error()
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace smob
+
 struct smob_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
