@@ -211,6 +211,8 @@ def run_native(args, world, rank, local, dist):
     mob.profile(False)
     f32, f64 = ctypes.c_double(), ctypes.c_double()
     N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
+    tpt, tms, tcache = ctypes.c_int(), (ctypes.c_double * 3)(), ctypes.c_int()
+    N.check(L.smob_tuning(h, ctypes.byref(tpt), tms, ctypes.byref(tcache)))
 
     if rank != 0:
         return None
@@ -262,6 +264,8 @@ def run_native(args, world, rank, local, dist):
                      "share_of_kernel_time": round(k_ms / tot_prof, 4) if tot_prof else None,
                      "fp64_fma_peak_tflops": round(f64.value, 4)},
         "kernel_ms_profiled_solve": {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items())},
+        "autotune": {"fp32_targets_per_thread": tpt.value, "variant_ms_tpt_1_2_4": [round(v, 4) for v in tms],
+                     "from_cache": bool(tcache.value)},
         "cpu_baseline": cpu,
         "e2e": {"value": round(world * args.steps / e2e_total, 4), "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * n6, "d2h_bytes_per_step": 8 * n6,

@@ -51,7 +51,10 @@ typedef enum {
 
 typedef enum {
     SMOB_PREC_FP64 = 0,  /* every kernel in FP64 */
-    SMOB_PREC_MIXED = 1  /* FP32 operator inside FP64 iterative refinement (FP64 Arnoldi, Givens, residuals) */
+    SMOB_PREC_MIXED = 1, /* solves: FP32 operator inside high-precision iterative refinement (FP64 Arnoldi,
+                            Givens; residuals with the float-float operator); operator calls: all FP32 */
+    SMOB_PREC_FLOAT_FLOAT = 2 /* operator calls only: FP64 sphere/near kernels, far field in float-float
+                                 (hi+lo float pairs on the FP32 pipe) -- the high-precision operator of MIXED */
 } smob_precision;
 
 typedef struct {
@@ -164,6 +167,9 @@ smob_status smob_profile_get(const smob_ctx* ctx, int i, char* name, int name_le
 smob_status smob_profile_reset(smob_ctx* ctx);
 /* total kernel launches issued by the library on this context since creation */
 smob_status smob_launch_count(const smob_ctx* ctx, long long* launches);
+/* far-field tile shape chosen by the autotuner at smob_create: FP32 targets per thread (1, 2 or 4),
+ * the measured milliseconds of the three variants (0 when the choice came from the process cache) */
+smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* variant_ms, int* from_cache);
 /* CUDA-event interval on the context's stream: mark records a start event; elapsed records an
  * end event, waits for it and returns the milliseconds since the last mark */
 smob_status smob_timer_mark(smob_ctx* ctx);

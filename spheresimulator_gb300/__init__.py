@@ -15,9 +15,9 @@ import ctypes
 import numpy as np
 
 from . import _native as N
-from ._native import PREC_FP64, PREC_MIXED, SmobError
+from ._native import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SmobError
 
-__all__ = ["SphereSTKSHOperator", "SphereSTKMobMat", "SmobError", "PREC_FP64", "PREC_MIXED", "solve_opts",
+__all__ = ["SphereSTKSHOperator", "SphereSTKMobMat", "SmobError", "PREC_FP64", "PREC_MIXED", "PREC_FLOAT_FLOAT", "solve_opts",
            "grid_number", "spectral_dof"]
 
 

@@ -18,6 +18,7 @@ SMOB_ERR_NO_DEVICE = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FLOAT_FLOAT = 2
 
 STATUS_NAMES = {0: "OK", 1: "ARG", 2: "CUDA", 3: "NOMEM", 4: "NOT_CONVERGED", 5: "NONFINITE", 6: "STATE",
                 7: "NO_DEVICE"}
@@ -100,6 +101,7 @@ def lib():
                                  _DP]),
         "smob_profile_reset": (S, [_VP]),
         "smob_launch_count": (S, [_VP, ctypes.POINTER(ctypes.c_longlong)]),
+        "smob_tuning": (S, [_VP, _IP, _DP, _IP]),
         "smob_timer_mark": (S, [_VP]),
         "smob_timer_elapsed": (S, [_VP, _DP]),
         "smob_flush_l2": (S, [_VP, ctypes.c_size_t]),

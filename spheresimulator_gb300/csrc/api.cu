@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -91,15 +92,22 @@ struct smob_ctx {
     std::vector<int> orders, prob, gidx, glen, coff, sid;
     std::vector<Problem> problems;
     std::vector<int> nbr_start, nbr_src, near_src_slot, slot_sphere;
+    std::vector<unsigned char> nbr_precise;
+    int n_precise = 0;
     int ncoef_total = 0;  // complex numbers
     long long set_stride_trac = 0, set_stride_sl = 0;
     std::vector<FarItem> items32, items64;
+    std::vector<FarItem> items_tpt[3];  // FP32 item lists for 1, 2, 4 targets per thread
+    int tpt = 2;                         // FP32 targets per thread chosen by the autotuner
+    double tune_ms[3] = {0, 0, 0};
+    bool tune_cached = false;
     long long partial32 = 0, partial64 = 0;
     std::vector<VecChunk> chunks;
 
     // device geometry
     DBuf d_center, d_radius, d_quat, d_order, d_gidx, d_glen, d_coff, d_prob, d_coords, d_norms, d_weights, d_sid;
-    DBuf d_pos32, d_nrm32, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_near_slot, d_slot_sphere, d_problems, d_tabs;
+    DBuf d_pos32, d_nrm32, d_pos32lo, d_nrm32lo, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_nbr_precise, d_near_slot,
+        d_slot_sphere, d_problems, d_tabs, d_srcdf;
     DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_chunks;
     DBuf d_active;
     // operator workspace
@@ -302,6 +310,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     // within each problem, sorted by target then source; overlapping spheres are rejected
     c->nbr_start.assign(N + 1, 0);
     c->nbr_src.clear();
+    c->nbr_precise.clear();
     for (const auto& pr : c->problems)
         for (int t = pr.s0; t < pr.s1; ++t) {
             for (int s = pr.s0; s < pr.s1; ++s) {
@@ -314,7 +323,11 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
                     throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(s) +
                                                       " overlap or touch");
                 const double Rn = 1.5 * c->radii[s] + 1.5 * c->radii[t];
-                if (r2 > 0 && r2 < Rn * Rn) c->nbr_src.push_back(s);
+                if (r2 > 0 && r2 < Rn * Rn) {
+                    c->nbr_src.push_back(s);
+                    const double gap = std::sqrt(r2) - c->radii[s] - c->radii[t];
+                    c->nbr_precise.push_back(gap < 0.1 * std::min(c->radii[s], c->radii[t]) ? 1 : 0);
+                }
             }
             c->nbr_start[t + 1] = (int)c->nbr_src.size();
         }
@@ -361,7 +374,8 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     };
     // both item lists share the chunking rule, so Problem.nchunks/poff are the same for both
     make_items(kFarTargets64, c->items64, c->partial64);
-    make_items(kFarTargets32, c->items32, c->partial32);
+    for (int k = 0; k < 3; ++k) make_items(kFarThreads << k, c->items_tpt[k], c->partial32);
+    c->items32 = c->items_tpt[1];
     // heavier problems first helps the tail of uneven batches
     auto by_cost = [&](std::vector<FarItem>& items) {
         std::stable_sort(items.begin(), items.end(), [&](const FarItem& a, const FarItem& b) {
@@ -372,6 +386,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     };
     by_cost(c->items32);
     by_cost(c->items64);
+    for (auto& v : c->items_tpt) by_cost(v);
 
     // reduction chunks for the Krylov vectors
     c->chunks.clear();
@@ -448,7 +463,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     tab.insert(tab.end(), dg.begin(), dg.end());
 
     // FP32/FP64 point data relative to each problem's origin (centre of its sphere bounding box)
-    std::vector<float4> pos32(c->M), nrm32(c->M);
+    std::vector<float4> pos32(c->M), nrm32(c->M), pos32lo(c->M), nrm32lo(c->M);
     std::vector<double4> pos64(c->M), nrm64(c->M);
     for (const auto& pr : c->problems) {
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -466,6 +481,11 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
             const double x = c->coords[3 * i] - org[0], y = c->coords[3 * i + 1] - org[1], z = c->coords[3 * i + 2] - org[2];
             pos32[i] = make_float4(float(x), float(y), float(z), fs);
             nrm32[i] = make_float4(float(c->norms[3 * i]), float(c->norms[3 * i + 1]), float(c->norms[3 * i + 2]), 0.f);
+            pos32lo[i] = make_float4(float(x - double(pos32[i].x)), float(y - double(pos32[i].y)),
+                                     float(z - double(pos32[i].z)), 0.f);
+            nrm32lo[i] = make_float4(float(c->norms[3 * i] - double(nrm32[i].x)),
+                                     float(c->norms[3 * i + 1] - double(nrm32[i].y)),
+                                     float(c->norms[3 * i + 2] - double(nrm32[i].z)), 0.f);
             pos64[i] = make_double4(x, y, z, 0.0);
             nrm64[i] = make_double4(c->norms[3 * i], c->norms[3 * i + 1], c->norms[3 * i + 2], 0.0);
         }
@@ -486,10 +506,15 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_sid.upload(c->sid);
     c->d_pos32.upload(pos32);
     c->d_nrm32.upload(nrm32);
+    c->d_pos32lo.upload(pos32lo);
+    c->d_nrm32lo.upload(nrm32lo);
     c->d_pos64.upload(pos64);
     c->d_nrm64.upload(nrm64);
     c->d_nbr_start.upload(c->nbr_start);
     c->d_nbr_src.upload(c->nbr_src);
+    c->d_nbr_precise.upload(c->nbr_precise);
+    c->n_precise = 0;
+    for (unsigned char v : c->nbr_precise) c->n_precise += v;
     c->d_near_slot.upload(c->near_src_slot);
     c->d_slot_sphere.upload(c->slot_sphere);
     c->d_problems.upload(c->problems);
@@ -511,6 +536,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     // operator workspace
     c->d_src32.alloc(sizeof(float4) * c->M);
     c->d_src64.alloc(sizeof(double4) * c->M);
+    c->d_srcdf.alloc(sizeof(float4) * 2 * c->M);
     c->d_partial32.alloc(sizeof(float) * c->partial32);
     c->d_partial64.alloc(sizeof(double) * c->partial64);
     c->d_coef32.alloc(sizeof(float) * 2 * c->ncoef_total);
@@ -542,10 +568,13 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     g.sid = c->d_sid.as<int>();
     g.pos32 = c->d_pos32.as<float4>();
     g.nrm32 = c->d_nrm32.as<float4>();
+    g.pos32lo = c->d_pos32lo.as<float4>();
+    g.nrm32lo = c->d_nrm32lo.as<float4>();
     g.pos64 = c->d_pos64.as<double4>();
     g.nrm64 = c->d_nrm64.as<double4>();
     g.nbr_start = c->d_nbr_start.as<int>();
     g.nbr_src = c->d_nbr_src.as<int>();
+    g.nbr_precise = c->d_nbr_precise.as<unsigned char>();
     g.near_src_slot = c->d_near_slot.as<int>();
     g.problems = c->d_problems.as<Problem>();
     g.tabs = c->d_tabs.as<OrderTables>();
@@ -558,6 +587,60 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     g.active = c->d_active.as<unsigned char>();
 }
 
+// Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on
+// this context's geometry (CUDA events, best of two) and keeps the fastest. Results are cached per
+// (largest order, size bucket of M) for the process, so contexts of similar shape reuse them.
+void autotune_far32(smob_ctx* c) {
+    static std::mutex mu;
+    static std::map<long long, int> cache;
+    const long long key = (long long)c->pmax * 1000 + (long long)std::floor(2.0 * std::log2(double(std::max(c->M, 1))));
+    int best = -1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) best = it->second;
+    }
+    if (best < 0) {
+        cudaEvent_t a, b;
+        CUDA_OK(cudaEventCreate(&a));
+        CUDA_OK(cudaEventCreate(&b));
+        CUDA_OK(cudaMemsetAsync(c->d_src32.p, 0, sizeof(float4) * c->M, c->st));
+        DBuf items;
+        double bestms = 1e300;
+        for (int k = 0; k < 3; ++k) {
+            items.upload(c->items_tpt[k]);
+            const int n = (int)c->items_tpt[k].size();
+            check_launch(c, launch_far_field(c->g, items.as<FarItem>(), n, true, true, c->d_src32.as<float4>(), nullptr,
+                                             c->d_partial32.p, c->st, 1 << k));
+            double ms = 1e300;
+            for (int rep = 0; rep < 2; ++rep) {
+                CUDA_OK(cudaEventRecord(a, c->st));
+                check_launch(c, launch_far_field(c->g, items.as<FarItem>(), n, true, true, c->d_src32.as<float4>(),
+                                                 nullptr, c->d_partial32.p, c->st, 1 << k));
+                CUDA_OK(cudaEventRecord(b, c->st));
+                CUDA_OK(cudaEventSynchronize(b));
+                float f = 0;
+                CUDA_OK(cudaEventElapsedTime(&f, a, b));
+                ms = std::min(ms, double(f));
+            }
+            c->tune_ms[k] = ms;
+            if (ms < bestms) {
+                bestms = ms;
+                best = k;
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        std::lock_guard<std::mutex> lk(mu);
+        cache[key] = best;
+    } else {
+        c->tune_cached = true;
+    }
+    c->tpt = 1 << best;
+    c->items32 = c->items_tpt[best];
+    c->d_items32.upload(c->items32);
+}
+
 void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
     CUDA_OK(cudaMemcpyAsync(c->d_active.p, act.data(), act.size(), cudaMemcpyHostToDevice, c->st));
     // the host vector must stay valid until the copy ran: make it synchronous with the stream
@@ -565,10 +648,15 @@ void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
 }
 
 // ---------------------------------------------------------------- the operator
+// operator precisions: every kernel in FP64; every kernel in FP32; or FP64 sphere and near
+// kernels with the far field in float-float (the high-precision operator of the mixed solve)
+enum OpPrec { OP_FP64 = 0, OP_FP32 = 1, OP_DF = 2 };
+
 // out (device) += c_id*x + c_sl*S[x] + c_trac*K[x] + c_lop*L[x] on active problems
 void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_sl, double c_trac, double c_lop,
-              bool fp32) {
+              int prec) {
     const DevGeom& g = c->g;
+    const bool fp32 = prec == OP_FP32, dfar = prec == OP_DF;
     const bool trac = std::fabs(c_trac) > 1e-9, sl = std::fabs(c_sl) > 1e-9;
     const bool id = std::fabs(c_id) > 1e-9;
     void* coef = fp32 ? c->d_coef32.p : c->d_coef64.p;
@@ -589,20 +677,37 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_near_sets(g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(),
                                                  tr ? c->set_stride_trac : c->set_stride_sl, c->st));
             }
+            const long long stride = tr ? c->set_stride_trac : c->set_stride_sl;
             {
                 ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
-                check_launch(c, launch_near_eval(g, sets, tr ? c->set_stride_trac : c->set_stride_sl, tr, fp32, cc, out,
-                                                 c->st));
+                check_launch(c, launch_near_eval(g, sets, stride, tr, fp32, cc, out, c->st,
+                                                 fp32 && c->n_precise ? 1 : 0));
+            }
+            if (fp32 && c->n_precise) {
+                // near-singular pairs (gap < 0.1 min radius) in FP64 even inside the FP32 operator
+                ProfScope ps(c, "near_singular_fp64");
+                check_launch(c, launch_sh_g2s(g, x, c->d_coef64.as<double>(), c->st));
+                check_launch(c, launch_near_sets(g, c->d_coef64.p, tr, false, c->d_sets64.p, nslots,
+                                                 c->d_slot_sphere.as<int>(), stride, c->st));
+                check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, cc, out, c->st, 2));
             }
         }
-        {
-            ProfScope ps(c, "far_pack");
-            check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
-        }
-        {
+        if (dfar) {
+            {
+                ProfScope ps(c, "far_pack");
+                check_launch(c, launch_far_pack_df(g, x, cc, c->d_srcdf.as<float4>(), c->st));
+            }
+            ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
+            check_launch(c, launch_far_field_df(g, items, nitems, tr, c->d_srcdf.as<float4>(),
+                                                static_cast<double*>(partial), c->st));
+        } else {
+            {
+                ProfScope ps(c, "far_pack");
+                check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
+            }
             ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
             check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                             c->d_src64.as<double4>(), partial, c->st));
+                                             c->d_src64.as<double4>(), partial, c->st, c->tpt));
         }
         {
             ProfScope ps(c, "far_reduce");
@@ -667,6 +772,9 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     const double tol = o->tol;
     const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
     const int maxit = std::max(1, o->max_iters);
+    // high-precision operator (b, refinement residuals, final velocity) and the cycle operator
+    const int hp = mixed ? OP_DF : OP_FP64;
+    const int cyc_prec = mixed ? OP_FP32 : OP_FP64;
     ensure_solver(c, m);
     const size_t n = 3 * (size_t)c->M;
     const int P = c->P;
@@ -693,7 +801,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     // step 1: rigid density; step 2: b = -(I/2 + K) rho  (high precision)
     check_launch(c, launch_rigid_density(c->g, d_force, rho, st));
     CUDA_OK(cudaMemsetAsync(b, 0, sizeof(double) * n, st));
-    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, false);
+    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, hp);
     for (auto& v : passes64) v++;
     std::vector<double> bnorm = seg_norms(c, b, act);
 
@@ -703,7 +811,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     if (o->warm_start && c->have_xlast) {
         CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, false);
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
         for (auto& v : passes64) v++;
         check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
         check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
@@ -771,7 +879,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             const double* Vj = V + n * j;
             // w = A V_j,  A = I/2 + K + L (SphereSTKMobMat.cpp:17)
             CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-            op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, mixed);
+            op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, cyc_prec);
             // CGS2: h = V^T w; w -= V h (twice), H[:, j] = h1 + h2
             double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
             double* hscr = c->d_y.as<double>();
@@ -795,7 +903,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, x, st));
         // explicit residual in FP64
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, false);
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
         for (int p = 0; p < P; ++p)
             if (cyc[p]) passes64[p]++;
         check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
@@ -809,7 +917,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     set_active(c, all);
     check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, rho, st));
     CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-    op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, false);
+    op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, hp);
     for (auto& v : passes64) v++;
     check_launch(c, launch_rigid_average(c->g, u, 1.0 / c->viscosity, d_vel, st));
     if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -875,6 +983,13 @@ void host_io(smob_ctx* c, const double* in, double* out, bool load_out, F&& f) {
     CUDA_OK(cudaStreamSynchronize(c->st));
 }
 
+int op_prec(int precision) {
+    if (precision == SMOB_PREC_MIXED) return OP_FP32;
+    if (precision == SMOB_PREC_FLOAT_FLOAT) return OP_DF;
+    if (precision != SMOB_PREC_FP64) throw SmobError(SMOB_ERR_ARG, "unknown precision");
+    return OP_FP64;
+}
+
 void all_active(smob_ctx* c) {
     std::vector<unsigned char> a(c->P, 1);
     set_active(c, a);
@@ -912,6 +1027,7 @@ smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
         CUDA_OK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
         configure_sphere_kernels();
         build_context(c.get(), geo);
+        autotune_far32(c.get());
         CUDA_OK(cudaDeviceSynchronize());
         *out = c.release();
         return SMOB_OK;
@@ -976,7 +1092,7 @@ smob_status smob_apply_p2p(smob_ctx* c, const double* in, double* out, double c_
         set_device(c);
         all_active(c);
         host_io(c, in, out, true, [&](const double* din, double* dout) {
-            op_apply(c, din, dout, c_id, c_sl, c_trac, 0.0, precision == SMOB_PREC_MIXED);
+            op_apply(c, din, dout, c_id, c_sl, c_trac, 0.0, op_prec(precision));
         });
         prof_flush(c);
         return SMOB_OK;
@@ -1004,7 +1120,7 @@ smob_status smob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, doub
         std::vector<double> tmp(n);
         for (int col = 0; col < n_cols; ++col) {
             host_io(c, X + n * col, tmp.data(), false, [&](const double* din, double* dout) {
-                op_apply(c, din, dout, 0.5, 0.0, 1.0, 1.0, precision == SMOB_PREC_MIXED);
+                op_apply(c, din, dout, 0.5, 0.0, 1.0, 1.0, op_prec(precision));
             });
             double* y = Y + n * col;
             for (size_t i = 0; i < n; ++i) y[i] = (beta == 0.0 ? 0.0 : beta * y[i]) + alpha * tmp[i];
@@ -1035,6 +1151,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
         set_device(c);
         all_active(c);
         const bool fp32 = precision == SMOB_PREC_MIXED;
+        const bool dfar = precision == SMOB_PREC_FLOAT_FLOAT;
         host_io(c, in, out, true, [&](const double* din, double* dout) {
             const FarItem* items = fp32 ? c->d_items32.as<FarItem>() : c->d_items64.as<FarItem>();
             const int nitems = (int)(fp32 ? c->items32.size() : c->items64.size());
@@ -1043,11 +1160,16 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 const bool tr = k == 0;
                 const double cc = tr ? c_trac : c_sl;
                 if (cc == 0.0) continue;
-                check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
-                {
+                if (dfar) {
+                    check_launch(c, launch_far_pack_df(c->g, din, cc, c->d_srcdf.as<float4>(), c->st));
+                    ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
+                    check_launch(c, launch_far_field_df(c->g, items, nitems, tr, c->d_srcdf.as<float4>(),
+                                                        static_cast<double*>(partial), c->st));
+                } else {
+                    check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
                     ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
                     check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                     c->d_src64.as<double4>(), partial, c->st));
+                                                     c->d_src64.as<double4>(), partial, c->st, c->tpt));
                 }
                 check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st));
             }
@@ -1262,6 +1384,17 @@ smob_status smob_launch_count(const smob_ctx* c, long long* launches) {
     return guarded([&]() -> smob_status {
         need(c && launches, "null argument");
         *launches = c->launches;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_tuning(const smob_ctx* c, int* targets_per_thread, double* variant_ms, int* from_cache) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (targets_per_thread) *targets_per_thread = c->tpt;
+        if (variant_ms)
+            for (int k = 0; k < 3; ++k) variant_ms[k] = c->tune_ms[k];
+        if (from_cache) *from_cache = c->tune_cached ? 1 : 0;
         return SMOB_OK;
     });
 }

@@ -67,19 +67,41 @@ __device__ __forceinline__ void contract(const Real* __restrict__ set, int idx, 
     for (int k = 0; k < NS; ++k) acc[k] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[k]));
 }
 
+// One target point per group of kNearLanes lanes. Every lane runs the (cheap) harmonic
+// recurrence; lane l contracts only the coefficient sets k = l, l + kNearLanes, ..., so the
+// lanes of a group read adjacent coefficients (one or two sectors per warp load, shared by the
+// warp's groups) and the sets are gathered with shuffles for the final assembly.
+// pair_filter: 0 every pair, 1 only pairs with gap >= 0.1 min radius, 2 only the
+// near-singular pairs (gap < 0.1 min radius).
+constexpr int kNearLanes = 8;
+
+template <typename Real, int NS>
+__device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, Real tr, Real ti,
+                                              Real* acc) {
+    const Real* c = set + 2 * NS * idx;
+#pragma unroll
+    for (int s = 0; s < (NS + kNearLanes - 1) / kNearLanes; ++s) {
+        const int k = lane + kNearLanes * s;
+        if (k < NS) acc[s] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[s]));
+    }
+}
+
 template <typename Real, bool TRAC>
 __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride,
                                                             const Real* __restrict__ th, int th_c1, int th_c2,
-                                                            int th_diag, double c, double* __restrict__ out) {
+                                                            int th_diag, double c, int pair_filter,
+                                                            double* __restrict__ out) {
     constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
     const int t = blockIdx.x;
     if (g.active && !g.active[g.prob[t]]) return;
     const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
     if (e0 == e1) return;
-    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x % kNearLanes;
+    const int j = blockIdx.y * (kNearThreads / kNearLanes) + threadIdx.x / kNearLanes;
     const int ng = g.glen[t];
-    if (j >= ng) return;
-    const int i = g.gidx[t] + j;
+    if (blockIdx.y * (kNearThreads / kNearLanes) >= ng) return;  // whole CTA past the sphere
+    const bool valid = j < ng;                                   // lanes stay for the shuffles
+    const int i = g.gidx[t] + (valid ? j : 0);
     const double X[3] = {g.coords[3 * i], g.coords[3 * i + 1], g.coords[3 * i + 2]};
     const double Nl[3] = {g.norms[3 * i], g.norms[3 * i + 1], g.norms[3 * i + 2]};
     const Real* c1 = th + th_c1;
@@ -87,6 +109,8 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
     const Real* dg = th + th_diag;
     double res[3] = {0, 0, 0};
     for (int e = e0; e < e1; ++e) {
+        if (pair_filter == 1 && g.nbr_precise[e]) continue;
+        if (pair_filter == 2 && !g.nbr_precise[e]) continue;
         const int s = g.nbr_src[e];
         const int slot = g.near_src_slot[s];
         const Real* S = sets + stride * slot;
@@ -101,9 +125,10 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
         const Real x = Real(xb[0] / a), y = Real(xb[1] / a), z = Real(xb[2] / a);
         const Real r2 = x * x + y * y + z * z;
         const Real ir2 = Real(1) / r2;
-        Real acc[NS];
+        constexpr int NL = (NS + kNearLanes - 1) / kNearLanes;
+        Real accl[NL];
 #pragma unroll
-        for (int k = 0; k < NS; ++k) acc[k] = 0;
+        for (int k = 0; k < NL; ++k) accl[k] = 0;
         Real dr = Real(1) / sqrt(r2), di = 0;  // Th_0^0
         for (int m = 0; m <= Nd; ++m) {
             if (m > 0) {
@@ -116,7 +141,7 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
             Real pr = 0, pi = 0, cr = dr, ci = di;
             for (int n = m; n <= Nd; ++n) {
                 const int idx = n * (n + 1) / 2 + m;
-                contract<Real, NS>(S, idx, cr, ci, acc);
+                contract_lane<Real, NS>(S, idx, lane, cr, ci, accl);
                 if (n < Nd) {
                     const Real a1 = c1[idx], a2 = c2[idx];
                     const Real nr = -(a1 * z * cr + a2 * pr) * ir2;
@@ -128,6 +153,10 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
                 }
             }
         }
+        // gather the NS sets from their owning lanes (set k lives in lane k % kNearLanes, slot k / kNearLanes)
+        Real acc[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) acc[k] = __shfl_sync(0xffffffffu, accl[k / kNearLanes], k % kNearLanes, kNearLanes);
         double vb[3];
         if (TRAC) {
             const double n0 = nb[0], n1 = nb[1], n2 = nb[2];
@@ -158,9 +187,11 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
         res[1] += vl[1];
         res[2] += vl[2];
     }
-    out[3 * i] += c * res[0];
-    out[3 * i + 1] += c * res[1];
-    out[3 * i + 2] += c * res[2];
+    if (valid && lane == 0) {
+        out[3 * i] += c * res[0];
+        out[3 * i + 1] += c * res[1];
+        out[3 * i + 2] += c * res[2];
+    }
 }
 
 }  // namespace
@@ -179,17 +210,18 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
 }
 
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
-                     cudaStream_t st) {
+                     cudaStream_t st, int pair_filter) {
     const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
-    dim3 grid(g.N, (gmax + kNearThreads - 1) / kNearThreads);
+    const int per_cta = kNearThreads / kNearLanes;
+    dim3 grid(g.N, (gmax + per_cta - 1) / per_cta);
     if (fp32) {
         const float* s = static_cast<const float*>(sets);
-        if (trac) k_near_eval<float, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, out);
-        else k_near_eval<float, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, out);
+        if (trac) k_near_eval<float, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
+        else k_near_eval<float, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
     } else {
         const double* s = static_cast<const double*>(sets);
-        if (trac) k_near_eval<double, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, out);
-        else k_near_eval<double, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, out);
+        if (trac) k_near_eval<double, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
+        else k_near_eval<double, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
     }
     return 1;
 }

@@ -21,7 +21,8 @@ constexpr int kMaxOrder = 32;
 constexpr int kFarThreads = 128;         // far-field CTA size (FP32: 2 targets per thread)
 constexpr int kFarTargets32 = 256;       // targets per FP32 far-field work item
 constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
-constexpr int kFarTile = 256;            // sources staged per shared-memory tile
+constexpr int kFarTile = 256;            // sources staged per shared-memory tile (FP64 / float-float)
+constexpr int kFarTile32 = 640;          // FP32 tile: a whole p <= 16 sphere (578 points) in one round
 constexpr int kSphereThreads = 256;      // per-sphere transform CTA
 constexpr int kNearThreads = 128;        // near-field CTA (one target point per thread)
 constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
@@ -77,10 +78,13 @@ struct DevGeom {
     const int* sid;
     const float4* pos32;
     const float4* nrm32;
+    const float4* pos32lo;  // float-float low parts: coordinate - float(coordinate), normal likewise
+    const float4* nrm32lo;
     const double4* pos64;
     const double4* nrm64;
     const int* nbr_start;
     const int* nbr_src;
+    const unsigned char* nbr_precise;  // per pair: surface gap < 0.1 * min radius (evaluated in FP64 in mixed mode)
     const int* near_src_slot;  // per sphere: slot in the near-set buffer, -1 if not a near source
     const Problem* problems;
     const OrderTables* tabs;   // indexed by p (kMaxOrder+1 entries)
@@ -98,9 +102,14 @@ struct DevGeom {
 // Far field: out[3M] += sum over far sources of c_sl*S + c_trac*K(dot n_target).
 int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4* src64, bool fp32,
                     cudaStream_t st);
+// tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
-                     const double4* src64, void* partial, cudaStream_t st);
+                     const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
+// float-float far field (hi/lo float pairs on the FP32 pipe); partial sums in FP64 (the FP64 buffer)
+int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2, cudaStream_t st);
+int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, bool trac, const float4* src2,
+                        double* partial, cudaStream_t st);
 
 // Per-sphere operator: out += c_id*x + c_self*Self[x] + c_lop*L[x]; coefficients of x written to coef
 // (self_kind: -1 none, 0 single layer, 3 traction principal value).
@@ -114,8 +123,9 @@ int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream
 // Near field: sets from coefficients (per near source sphere), then spectral evaluation per target sphere.
 int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
                      const int* slot_sphere, long long stride, cudaStream_t st);
+// pair_filter: 0 all near pairs, 1 pairs with gap >= 0.1 min radius, 2 the near-singular pairs only
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
-                     cudaStream_t st);
+                     cudaStream_t st, int pair_filter = 0);
 
 // Rigid-body pieces of the mobility solve
 int launch_rigid_density(const DevGeom& g, const double* force6n, double* rho, cudaStream_t st);

@@ -7,7 +7,8 @@ the velocities at tol 1e-12; mixed-precision solves to 1e-6 relative at tol 1e-1
 import numpy as np
 import pytest
 
-from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SmobError, SphereSTKMobMat, SphereSTKSHOperator, configs
+from spheresimulator_gb300 import (PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SmobError, SphereSTKMobMat,
+                                   SphereSTKSHOperator, configs)
 
 pytestmark = pytest.mark.gpu
 
@@ -52,6 +53,8 @@ def test_far_field(oracle, seed):
         ref = o.far_traction(x, c_tr, excl_near=True) + o.far_sl(x, c_sl, excl_near=True)
         assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_FP64), ref) < 1e-11
         assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_MIXED), ref) < 2e-5
+        # float-float (hi+lo float pairs): ~48 significant bits
+        assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_FLOAT_FLOAT), ref) < 1e-12
 
 
 def test_transforms(oracle):
@@ -90,6 +93,8 @@ def test_apply_p2p(oracle, coefs):
     assert rel(out - y0, ref - y0) < 1e-11
     out32 = g.applyP2POP(x, y0, *coefs, precision=PREC_MIXED)
     assert rel(out32 - y0, ref - y0) < 2e-5
+    outdf = g.applyP2POP(x, y0, *coefs, precision=PREC_FLOAT_FLOAT)
+    assert rel(outdf - y0, ref - y0) < 1e-12
 
 
 def test_near_field_is_spectral_part(oracle):
