@@ -276,6 +276,142 @@ def run_native(args, world, rank, local, dist):
     return line
 
 
+def run_config(args, world, rank, local, dist):
+    """cfg3 (1024 spheres, near-singular gaps) and cfg4 (256 uneven independent problems, one
+    batched solve) at 1e-8: mixed solves timed; one FP64-accurate reference solve of the same
+    operator (float-float far field, FP64 elsewhere) gives the error; the CPU restatement's cost is
+    extrapolated from its measured pair rate on cfg2."""
+    import ctypes
+
+    from spheresimulator_gb300 import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SphereSTKMobMat, configs, solve_opts
+    from spheresimulator_gb300 import _native as N
+
+    L = N.lib()
+    cfg = getattr(configs, args.config)()
+    mob = SphereSTKMobMat(cfg["centers"], cfg["radii"], cfg["orders"], quats=cfg.get("quats"),
+                          problem=cfg.get("problem"), device=local)
+    h = mob.handle
+    P = mob.n_problems
+    n6 = 6 * mob.n_spheres
+    force = np.ascontiguousarray(cfg["force"])
+    d_force, d_vel = ctypes.c_void_p(), ctypes.c_void_p()
+    N.check(L.smob_device_alloc(h, 8 * n6, ctypes.byref(d_force)))
+    N.check(L.smob_device_alloc(h, 8 * n6, ctypes.byref(d_vel)))
+    N.check(L.smob_memcpy_h2d(h, d_force, force.ctypes.data_as(ctypes.c_void_p), 8 * n6))
+    stats = (N.ProblemStats * P)()
+
+    def solve(prec):
+        o = solve_opts(TOL, RESTART, 2000, prec)
+        N.check(L.smob_flush_l2(h, L2_FLUSH_BYTES))
+        N.check(L.smob_timer_mark(h))
+        N.check(L.smob_solve_mob_device(h, d_force, d_vel, None, ctypes.byref(o), stats))
+        t = ctypes.c_double()
+        N.check(L.smob_timer_elapsed(h, ctypes.byref(t)))
+        v = np.zeros(n6)
+        N.check(L.smob_memcpy_d2h(h, v.ctypes.data_as(ctypes.c_void_p), d_vel, 8 * n6))
+        return t.value, [s.as_dict() for s in stats], v
+
+    for _ in range(args.warmup):
+        solve(PREC_MIXED)
+    barrier(dist)
+    l0 = mob.launch_count()
+    ms, sts = [], None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t, sts, vel = solve(PREC_MIXED)
+            ms.append(t)
+    launches = (mob.launch_count() - l0) / max(args.steps, 1)
+    ms = np.array(ms)
+    total_s = allmax(dist, ms.sum() / 1e3)
+    ref_name = {"ff": PREC_FLOAT_FLOAT, "fp64": PREC_FP64}.get(args.ref)
+    ref = None
+    if ref_name is not None:
+        tr, sts_ref, vref = solve(ref_name)
+        err = float(np.linalg.norm(vel - vref) / np.linalg.norm(vref))
+        ref = {"precision": args.ref, "solve_ms": round(tr, 1), "rel_err_mixed_vs_ref": err,
+               "iterations_total": int(sum(s["iterations"] for s in sts_ref)),
+               "max_relres": max(s["relres"] for s in sts_ref),
+               "speedup_mixed_vs_ref": round(tr / ms.mean(), 3)}
+    mob.profile(True)
+    mob.profile_reset()
+    solve(PREC_MIXED)
+    prof = mob.profile_table()
+    mob.profile(False)
+    f32, f64 = ctypes.c_double(), ctypes.c_double()
+    N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
+    tpt, tms, tcache = ctypes.c_int(), (ctypes.c_double * 3)(), ctypes.c_int()
+    N.check(L.smob_tuning(h, ctypes.byref(tpt), tms, ctypes.byref(tcache)))
+    if rank != 0:
+        return None
+    pairs = far_pairs_batched(mob)
+    k_l, k_ms = prof.get("far_trac_fp32", (0, 0.0))
+    avg_s = (k_ms / max(k_l, 1)) / 1e3
+    achieved = 30.0 * pairs / avg_s / 1e12 if avg_s > 0 else None
+    its = [s["iterations"] for s in sts]
+    # CPU restatement: pair rate measured on cfg2 (one FP64 operator pass), scaled to this workload
+    c2 = configs.cfg2()
+    from oracle import oracle as O
+    nthreads = args.cpu_threads or os.cpu_count()
+    O.set_threads(nthreads)
+    op2 = O.Operator(c2["centers"], c2["radii"], c2["orders"])
+    x2 = np.random.default_rng(0).standard_normal(3 * op2.m)
+    op2.apply(x2)
+    t0 = time.perf_counter()
+    op2.apply(x2)
+    dt2 = time.perf_counter() - t0
+    rate = 1336336000 / dt2
+    passes = sum(s["iterations"] for s in sts) / P + 4
+    cpu_solve_s = passes * (pairs / P) / rate
+    value = world * P * args.steps / total_s
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(float(ms.mean()), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator + f64 refinement (mixed)",
+        "data": "synthetic (seeded RSA packing, N(0,1) forces)",
+        "config": {"workload": args.config + ": " + CONFIG_TEXT[args.config], "tol": TOL, "restart": RESTART,
+                   "problems_per_step": P, "points": mob.n_points, "near_pairs": mob.n_near_pairs,
+                   "l2": "flushed between steps (256 MB device write)", "parallelism": "replicas only"},
+        "latency_ms": {"p50": round(float(np.percentile(ms, 50)), 3), "p99": round(float(np.percentile(ms, 99)), 3),
+                       "meaning": "time of one batched solve step (all problems of the step)"},
+        "mixed": {"iterations_mean": float(np.mean(its)), "iterations_max": int(np.max(its)),
+                  "all_converged": all(s["status"] == 0 for s in sts), "max_relres": max(s["relres"] for s in sts)},
+        "reference_solve": ref,
+        "pair_interactions_per_launch": pairs,
+        "roofline": {"kernel": "far_trac_fp32", "bound": "fp32_simt", "achieved": round(achieved, 3) if achieved else None,
+                     "peak": round(f32.value, 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / f32.value, 4) if achieved else None, "traffic": None,
+                     "avg_launch_ms": round(avg_s * 1e3, 4)},
+        "kernel_ms_profiled_solve": {k: [v[0], round(v[1], 3)] for k, v in sorted(prof.items())},
+        "autotune": {"fp32_targets_per_thread": tpt.value, "variant_ms_tpt_1_2_4": [round(v, 4) for v in tms]},
+        "cpu_baseline": {"value": round(P / (cpu_solve_s * P), 8) if cpu_solve_s > 0 else None, "unit": "solves/s",
+                         "cores": nthreads, "kind": "port",
+                         "sample": "extrapolated: FP64 restatement's pair rate on one cfg2 operator pass (%.3f s for "
+                                   "1.336e9 pairs) x this workload's pairs per problem (%.3g) x %.1f passes per solve"
+                                   % (dt2, pairs / P, passes)},
+        "e2e": None,
+        "gpu_launches": int(round(launches)),
+        "clocks": clk.summary(),
+    }
+
+
+CONFIG_TEXT = {
+    "cfg3": "1024 spheres a~U[0.8,1.2], RSA in box 40 (min gap 0.05), p=16, mixed FP32/FP64 to 1e-8",
+    "cfg4": "256 independent problems, N~U{2..128}, p~U{8,12,16}, a=1, box 4N^(1/3), gap 0.1, one batched solve",
+}
+
+
+def far_pairs_batched(mob):
+    ng = np.array([(p + 1) * (2 * p + 2) for p in mob.orders], dtype=np.int64)
+    prob = mob.problem if mob.problem is not None else np.zeros(len(ng), np.int64)
+    pairs = 0
+    for k in np.unique(prob):
+        g = ng[prob == k]
+        pairs += g.sum() ** 2 - (g * g).sum()
+    t, s = mob.near_pairs()
+    pairs -= (ng[t] * ng[s]).sum()
+    return int(pairs)
+
+
 def cpu_sample(cfg, passes, threads):
     from oracle import oracle as O
     nthreads = threads or os.cpu_count()
@@ -338,12 +474,17 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4"])
+    ap.add_argument("--ref", default="ff", choices=["ff", "fp64", "none"],
+                    help="cfg3/cfg4: reference solve for the error (ff = FP64-accurate float-float far field)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
     world, rank, local, dist = dist_init()
     if args.impl == "reference":
         line = run_reference(args, rank)
+    elif args.config != "cfg2":
+        line = run_config(args, world, rank, local, dist)
     else:
         line = run_native(args, world, rank, local, dist)
     if rank == 0 and line is not None:

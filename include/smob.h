@@ -53,8 +53,9 @@ typedef enum {
     SMOB_PREC_FP64 = 0,  /* every kernel in FP64 */
     SMOB_PREC_MIXED = 1, /* solves: FP32 operator inside high-precision iterative refinement (FP64 Arnoldi,
                             Givens; residuals with the float-float operator); operator calls: all FP32 */
-    SMOB_PREC_FLOAT_FLOAT = 2 /* operator calls only: FP64 sphere/near kernels, far field in float-float
-                                 (hi+lo float pairs on the FP32 pipe) -- the high-precision operator of MIXED */
+    SMOB_PREC_FLOAT_FLOAT = 2 /* FP64 sphere/near kernels with the far field in float-float (hi+lo float
+                                 pairs on the FP32 pipe, ~48 bits): the high-precision operator of MIXED;
+                                 for solves, plain restarted GMRES with this operator throughout */
 } smob_precision;
 
 typedef struct {
@@ -167,6 +168,9 @@ smob_status smob_profile_get(const smob_ctx* ctx, int i, char* name, int name_le
 smob_status smob_profile_reset(smob_ctx* ctx);
 /* total kernel launches issued by the library on this context since creation */
 smob_status smob_launch_count(const smob_ctx* ctx, long long* launches);
+/* CUDA graphs for the Arnoldi steps of the solves (default on): blocks of steps are captured once per
+ * context and replayed; the host checks the per-problem stop flags between blocks */
+smob_status smob_set_graphs(smob_ctx* ctx, int on);
 /* far-field tile shape chosen by the autotuner at smob_create: FP32 targets per thread (1, 2 or 4),
  * the measured milliseconds of the three variants (0 when the choice came from the process cache) */
 smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* variant_ms, int* from_cache);

@@ -111,6 +111,10 @@ class _Context:
         N.check(self._L.smob_launch_count(self._h, ctypes.byref(v)))
         return v.value
 
+    def set_graphs(self, on=True):
+        """CUDA graphs for the Arnoldi steps of the solves (on by default)."""
+        N.check(self._L.smob_set_graphs(self._h, int(on)))
+
     def profile(self, on=True):
         N.check(self._L.smob_profile_enable(self._h, int(on)))
 

@@ -75,6 +75,7 @@ struct DBuf {
 };
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host check of the stop flags
 
 }  // namespace
 
@@ -124,6 +125,17 @@ struct smob_ctx {
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     DBuf d_flush;
     unsigned flush_val = 1;
+    // captured Arnoldi blocks (see solve_device)
+    struct Graph {
+        cudaGraphExec_t exec;
+        long long kernels;
+    };
+    bool use_graphs = true;
+    std::map<long long, Graph> graphs;
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
 
     // profiling
     bool prof = false;
@@ -155,6 +167,7 @@ struct smob_ctx {
         }
         if (ev_a) cudaEventDestroy(ev_a);
         if (ev_b) cudaEventDestroy(ev_b);
+        drop_graphs();
         if (st) cudaStreamDestroy(st);
     }
 };
@@ -554,6 +567,15 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     g.M = c->M;
     g.P = c->P;
     g.pmax = c->pmax;
+    // near-field lanes per target: enough threads to fill the GPU (~152 SMs x 2048 threads) when few
+    // target points have near pairs, one lane (no repeated recurrence) when many do
+    {
+        long long tpts = 0;
+        for (int t = 0; t < c->N; ++t)
+            if (c->nbr_start[t + 1] > c->nbr_start[t]) tpts += c->glen[t];
+        const double want = 152.0 * 2048.0 / double(std::max<long long>(tpts, 1));
+        g.near_lanes = want >= 8 ? 8 : (want >= 4 ? 4 : (want >= 2 ? 2 : 1));
+    }
     g.center = c->d_center.as<double>();
     g.radius = c->d_radius.as<double>();
     g.quat = c->d_quat.as<double>();
@@ -726,6 +748,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
 void ensure_solver(smob_ctx* c, int m) {
     const size_t n = 3 * (size_t)c->M;
     if (m > c->restart_cap) {
+        c->drop_graphs();  // captured blocks hold the old buffer addresses
         c->d_V.alloc(sizeof(double) * n * (m + 1));
         c->d_H.alloc(sizeof(double) * c->P * m * (m + 1));
         c->d_g.alloc(sizeof(double) * c->P * (m + 1));
@@ -772,9 +795,11 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     const double tol = o->tol;
     const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
     const int maxit = std::max(1, o->max_iters);
-    // high-precision operator (b, refinement residuals, final velocity) and the cycle operator
-    const int hp = mixed ? OP_DF : OP_FP64;
-    const int cyc_prec = mixed ? OP_FP32 : OP_FP64;
+    // high-precision operator (b, refinement residuals, final velocity) and the cycle operator;
+    // SMOB_PREC_FLOAT_FLOAT runs the plain restarted GMRES with the float-float far field throughout
+    const bool ffar = o->precision == SMOB_PREC_FLOAT_FLOAT;
+    const int hp = (mixed || ffar) ? OP_DF : OP_FP64;
+    const int cyc_prec = mixed ? OP_FP32 : hp;
     ensure_solver(c, m);
     const size_t n = 3 * (size_t)c->M;
     const int P = c->P;
@@ -796,7 +821,8 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     std::vector<KrylovState> hks(P);
     for (auto& k : hks) k = KrylovState{0, 0, 0, 0, 0, 0, 0};
     CUDA_OK(cudaMemcpyAsync(ks, hks.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
-    std::vector<int> passes64(P, 0), cycles(P, 0);
+    std::vector<int> passes64(P, 0), cycles(P, 0), passes32x(P, 0);
+    std::vector<char> hp_resid_done(P, 0);  // a high-precision residual after a cycle exists
 
     // step 1: rigid density; step 2: b = -(I/2 + K) rho  (high precision)
     check_launch(c, launch_rigid_density(c->g, d_force, rho, st));
@@ -875,12 +901,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         check_launch(c, launch_scale(L, r, c->d_beta.as<double>(), 1, true, act, V, st));
         check_launch(c, launch_cycle_init(L, m, incyc, c->d_beta.as<double>(), ks, c->d_H.as<double>(),
                                           c->d_g.as<double>(), st));
-        for (int j = 0; j < m; ++j) {
+        // one Arnoldi step: w = A V_j (A = I/2 + K + L, SphereSTKMobMat.cpp:17), CGS2 into H[:, j],
+        // Givens update and the per-problem stop test on the device (problems that stop skip all
+        // later work through the active flags)
+        auto step = [&](int j) {
             const double* Vj = V + n * j;
-            // w = A V_j,  A = I/2 + K + L (SphereSTKMobMat.cpp:17)
             CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
             op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, cyc_prec);
-            // CGS2: h = V^T w; w -= V h (twice), H[:, j] = h1 + h2
             double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
             double* hscr = c->d_y.as<double>();
             for (int pass = 0; pass < 2; ++pass) {
@@ -892,22 +919,69 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             check_launch(c, launch_givens(L, j, m, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_cs.as<double>(),
                                           c->d_sn.as<double>(), c->d_hn.as<double>(), act, maxit, st));
             if (j + 1 < m) check_launch(c, launch_scale(L, w, c->d_hn.as<double>(), 1, true, act, V + n * (j + 1), st));
+        };
+        // Steps run in blocks of kGraphBlock; with graphs on, each block is captured once per context
+        // (per block start, cycle precision and restart length) and replayed, and the host looks at
+        // the active flags only between blocks.
+        const bool graphs = c->use_graphs && !c->prof;
+        for (int j0 = 0; j0 < m; j0 += kGraphBlock) {
+            const int cnt = std::min(kGraphBlock, m - j0);
+            if (graphs) {
+                const long long key = ((long long)cyc_prec * 4096 + m) * 4096 + j0;
+                auto it = c->graphs.find(key);
+                if (it == c->graphs.end()) {
+                    const long long before = c->launches;
+                    cudaGraph_t gr;
+                    CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    for (int j = j0; j < j0 + cnt; ++j) step(j);
+                    CUDA_OK(cudaStreamEndCapture(st, &gr));
+                    cudaGraphExec_t ex;
+                    CUDA_OK(cudaGraphInstantiate(&ex, gr, 0));
+                    cudaGraphDestroy(gr);
+                    it = c->graphs.emplace(key, smob_ctx::Graph{ex, c->launches - before}).first;
+                    c->launches = before;
+                }
+                CUDA_OK(cudaGraphLaunch(it->second.exec, st));
+                c->launches += it->second.kernels;
+            } else {
+                for (int j = j0; j < j0 + cnt; ++j) step(j);
+            }
             CUDA_OK(cudaMemcpyAsync(hact.data(), act, P, cudaMemcpyDeviceToHost, st));
             CUDA_OK(cudaStreamSynchronize(st));
             if (std::none_of(hact.begin(), hact.end(), [](unsigned char a) { return a != 0; })) break;
         }
-        // x += V y for the problems of this cycle
+        // d = V y and x += d for the problems of this cycle
         check_launch(c, launch_trisolve(L, m, incyc, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_y.as<double>(),
                                         c->d_kc.as<int>(), st));
         set_active(c, cyc);
-        check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, x, st));
-        // explicit residual in FP64
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
+        check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, w, st));
+        check_launch(c, launch_axpby_seg(L, 1.0, w, 1.0, act, x, st));
+        // Residual. FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos'
+        // restart). MIXED: r = b - A x with the high-precision operator, except once the previous
+        // high-precision residual is below 1e-4 |b|: then r <- r - A32 d, whose FP32 error
+        // ~eps32 * kappa * |r_prev| (<= ~1e-10 |b|) is far below the 1e-8 target, so one
+        // high-precision pass is saved per later refinement sweep.
+        bool upd_all = mixed;
         for (int p = 0; p < P; ++p)
-            if (cyc[p]) passes64[p]++;
-        check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-        check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+            if (cyc[p] && !(hp_resid_done[p] && beta[p] <= 1e-4 * bnorm[p])) upd_all = false;
+        if (upd_all) {
+            CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+            op_apply(c, w, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
+            for (int p = 0; p < P; ++p)
+                if (cyc[p]) passes32x[p]++;
+            check_launch(c, launch_axpby_seg(L, -1.0, u, 1.0, act, r, st));
+        } else {
+            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
+            for (int p = 0; p < P; ++p)
+                if (cyc[p]) {
+                    passes64[p]++;
+                    hp_resid_done[p] = 1;
+                }
+            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+        }
         std::vector<double> nb = seg_norms(c, r, act);
         for (int p = 0; p < P; ++p)
             if (cyc[p]) beta[p] = nb[p];
@@ -938,7 +1012,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             s.iterations = kst[p].iters;
             s.refinements = cycles[p];
             s.operator_passes_fp64 = passes64[p] + kst[p].passes64;
-            s.operator_passes_fp32 = kst[p].passes32;
+            s.operator_passes_fp32 = kst[p].passes32 + passes32x[p];
             s.bnorm = bnorm[p];
             s.relres = bnorm[p] < 1e-5 ? 0.0 : beta[p] / bnorm[p];
         }
@@ -1236,7 +1310,7 @@ smob_status smob_sh_s2g(smob_ctx* c, const double* coeff, double* grid) {
 static smob_status check_opts(const smob_solve_opts* o) {
     if (!o) throw SmobError(SMOB_ERR_ARG, "null solve options");
     if (!(o->tol > 0) || o->restart < 1 || o->max_iters < 1) throw SmobError(SMOB_ERR_ARG, "invalid solve options");
-    if (o->precision != SMOB_PREC_FP64 && o->precision != SMOB_PREC_MIXED)
+    if (o->precision != SMOB_PREC_FP64 && o->precision != SMOB_PREC_MIXED && o->precision != SMOB_PREC_FLOAT_FLOAT)
         throw SmobError(SMOB_ERR_ARG, "unknown precision");
     return SMOB_OK;
 }
@@ -1384,6 +1458,17 @@ smob_status smob_launch_count(const smob_ctx* c, long long* launches) {
     return guarded([&]() -> smob_status {
         need(c && launches, "null argument");
         *launches = c->launches;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_graphs(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        c->use_graphs = on != 0;
+        if (!c->use_graphs) c->drop_graphs();
         return SMOB_OK;
     });
 }

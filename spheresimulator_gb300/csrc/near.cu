@@ -67,31 +67,32 @@ __device__ __forceinline__ void contract(const Real* __restrict__ set, int idx, 
     for (int k = 0; k < NS; ++k) acc[k] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[k]));
 }
 
-// One target point per group of kNearLanes lanes. Every lane runs the (cheap) harmonic
-// recurrence; lane l contracts only the coefficient sets k = l, l + kNearLanes, ..., so the
-// lanes of a group read adjacent coefficients (one or two sectors per warp load, shared by the
-// warp's groups) and the sets are gathered with shuffles for the final assembly.
+// One target point per group of LANES lanes. Every lane runs the (cheap) harmonic recurrence;
+// lane l contracts only the coefficient sets k = l, l + LANES, ..., so the lanes of a group read
+// adjacent coefficients (one or two sectors per warp load, shared by the warp's groups) and the
+// sets are gathered with shuffles for the final assembly. More lanes add parallelism for small
+// problems at the price of repeating the recurrence; the host picks LANES from the number of
+// target points that have near pairs.
 // pair_filter: 0 every pair, 1 only pairs with gap >= 0.1 min radius, 2 only the
 // near-singular pairs (gap < 0.1 min radius).
-constexpr int kNearLanes = 8;
-
-template <typename Real, int NS>
+template <typename Real, int NS, int LANES>
 __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, Real tr, Real ti,
                                               Real* acc) {
     const Real* c = set + 2 * NS * idx;
 #pragma unroll
-    for (int s = 0; s < (NS + kNearLanes - 1) / kNearLanes; ++s) {
-        const int k = lane + kNearLanes * s;
+    for (int s = 0; s < (NS + LANES - 1) / LANES; ++s) {
+        const int k = lane + LANES * s;
         if (k < NS) acc[s] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[s]));
     }
 }
 
-template <typename Real, bool TRAC>
+template <typename Real, bool TRAC, int LANES>
 __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride,
                                                             const Real* __restrict__ th, int th_c1, int th_c2,
                                                             int th_diag, double c, int pair_filter,
                                                             double* __restrict__ out) {
     constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
+    constexpr int kNearLanes = LANES;
     const int t = blockIdx.x;
     if (g.active && !g.active[g.prob[t]]) return;
     const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
             Real pr = 0, pi = 0, cr = dr, ci = di;
             for (int n = m; n <= Nd; ++n) {
                 const int idx = n * (n + 1) / 2 + m;
-                contract_lane<Real, NS>(S, idx, lane, cr, ci, accl);
+                contract_lane<Real, NS, LANES>(S, idx, lane, cr, ci, accl);
                 if (n < Nd) {
                     const Real a1 = c1[idx], a2 = c2[idx];
                     const Real nr = -(a1 * z * cr + a2 * pr) * ir2;
@@ -209,19 +210,38 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
     return 1;
 }
 
-int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
-                     cudaStream_t st, int pair_filter) {
+template <int LANES>
+void launch_near_eval_l(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c,
+                        double* out, cudaStream_t st, int pair_filter) {
     const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
-    const int per_cta = kNearThreads / kNearLanes;
+    const int per_cta = kNearThreads / LANES;
     dim3 grid(g.N, (gmax + per_cta - 1) / per_cta);
     if (fp32) {
         const float* s = static_cast<const float*>(sets);
-        if (trac) k_near_eval<float, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
-        else k_near_eval<float, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
+        if (trac)
+            k_near_eval<float, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
+                                                                           g.th_diag, c, pair_filter, out);
+        else
+            k_near_eval<float, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
+                                                                            g.th_diag, c, pair_filter, out);
     } else {
         const double* s = static_cast<const double*>(sets);
-        if (trac) k_near_eval<double, true><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
-        else k_near_eval<double, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, out);
+        if (trac)
+            k_near_eval<double, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
+                                                                            g.th_diag, c, pair_filter, out);
+        else
+            k_near_eval<double, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
+                                                                             g.th_diag, c, pair_filter, out);
+    }
+}
+
+int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
+                     cudaStream_t st, int pair_filter) {
+    switch (g.near_lanes) {
+        case 1: launch_near_eval_l<1>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;
+        case 2: launch_near_eval_l<2>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;
+        case 4: launch_near_eval_l<4>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;
+        default: launch_near_eval_l<8>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;
     }
     return 1;
 }

@@ -63,6 +63,7 @@ struct Problem {
 struct DevGeom {
     int N, M, P;
     int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
+    int near_lanes;       // lanes per target point in the near-field kernel (1, 2, 4 or 8)
     int th_c1, th_c2, th_diag;  // offsets of the irregular-solid-harmonic recurrence tables in tab_d/tab_f
     const double* center;
     const double* radius;

@@ -191,6 +191,68 @@ def test_batched_equals_alone():
         assert len(gb.last_stats) == 2
 
 
+def test_graphs_match_eager():
+    """Captured Arnoldi blocks replay exactly the kernels the eager path launches."""
+    cfg = cluster(16, n=5, p=7)
+    for prec in (PREC_FP64, PREC_MIXED):
+        g = make(cfg, SphereSTKMobMat)
+        v_graph = g.solveMob(cfg["force"], tol=1e-10, precision=prec)
+        v_graph2 = g.solveMob(cfg["force"], tol=1e-10, precision=prec)  # replay of the cached graphs
+        g.set_graphs(False)
+        v_eager = g.solveMob(cfg["force"], tol=1e-10, precision=prec)
+        assert np.array_equal(v_graph, v_eager) and np.array_equal(v_graph2, v_eager)
+
+
+def test_float_float_solve(oracle):
+    """Restarted GMRES with the float-float far field throughout is FP64-accurate."""
+    cfg = cluster(17, n=6, p=8)
+    g = make(cfg, SphereSTKMobMat)
+    ref = oracle_op(oracle, cfg).solve_mob(cfg["force"], tol=1e-12)
+    vel = g.solveMob(cfg["force"], tol=1e-12, precision=PREC_FLOAT_FLOAT)
+    assert g.last_stats[0]["status"] == 0 and g.last_stats[0]["operator_passes_fp32"] == 0
+    assert rel(vel, ref["vel"]) < 1e-9
+
+
+def test_mixed_with_near_singular_pairs(oracle):
+    """Pairs closer than 0.1 radius are evaluated in FP64 inside the FP32 operator."""
+    cfg = configs.small_cluster(seed=21, n=6, p=8, gap=0.05, quats=True)
+    g = make(cfg, SphereSTKMobMat)
+    t, s = g.near_pairs()
+    gaps = np.linalg.norm(cfg["centers"][t] - cfg["centers"][s], axis=1) - cfg["radii"][t] - cfg["radii"][s]
+    assert np.any(gaps < 0.1 * np.minimum(cfg["radii"][t], cfg["radii"][s]))
+    o = oracle_op(oracle, cfg)
+    x = np.random.default_rng(3).standard_normal(3 * g.n_points)
+    assert rel(make(cfg).apply(x, precision=PREC_MIXED), o.apply(x)) < 2e-5
+    ref = o.solve_mob(cfg["force"], tol=1e-12)
+    vel = g.solveMob(cfg["force"], tol=1e-10, precision=PREC_MIXED)
+    assert g.last_stats[0]["status"] == 0 and rel(vel, ref["vel"]) < 1e-6
+
+
+def rigid_density(op, cfg):
+    """rho = F/(4 pi a^2) + 3/(8 pi a^4) T x (a n) on every grid point (BIE/SphereSTKMobMat.cpp:174-192)."""
+    n = op.getGridNorms()
+    sid = np.repeat(np.arange(op.n_spheres), [(p + 1) * (2 * p + 2) for p in cfg["orders"]])
+    a = np.asarray(cfg["radii"])[sid][:, None]
+    F = np.asarray(cfg["force"]).reshape(-1, 6)[sid]
+    return (F[:, :3] / (4 * np.pi * a * a) + 3 / (8 * np.pi * a ** 4) * np.cross(F[:, 3:], a * n)).reshape(-1)
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_reported_residual_is_true_residual(prec):
+    """|b - A mu|/|b| recomputed independently with the FP64 operator matches the solver's report."""
+    cfg = cluster(18, n=6, p=8, gap=0.1)
+    mob = make(cfg, SphereSTKMobMat)
+    op = make(cfg)
+    mob.solveMob(cfg["force"], tol=1e-10, precision=prec)
+    st = mob.last_stats[0]
+    rho = rigid_density(op, cfg)
+    mu = mob.getDensitySolution() - rho
+    b = op.applyP2POP(rho, cId=-0.5, cSL=0.0, cTrac=-1.0)
+    true = np.linalg.norm(b - op.apply(mu)) / np.linalg.norm(b)
+    assert st["status"] == 0 and true < 1e-10
+    assert abs(true - st["relres"]) < 1e-11
+
+
 def test_isolated_sphere_drag_gpu():
     rng = np.random.default_rng(13)
     q = rng.standard_normal(4)
