@@ -394,6 +394,78 @@ def run_config(args, world, rank, local, dist):
     }
 
 
+def run_serving(args, world, rank, local, dist):
+    """cfg5: Poisson arrivals of independent mobility solves (N log-uniform in [4, nmax], p in
+    {8,12,16,24}, a ~ U[0.9,1.1], gap 0.05, tol 1e-6 or 1e-8) submitted in real time to the
+    continuous-batching server; latency = completion - submission on the server's clock."""
+    import threading as th
+
+    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SolveServer, configs
+    stream = configs.cfg5_stream(seed=5 + rank, n_requests=args.requests, rate=args.rate, nmax=args.nmax)
+
+    def serve(reqs, precision, slots):
+        srv = SolveServer(device=local, max_slots=slots, precision=precision, hbm_budget_bytes=args.hbm_budget)
+        ids = [None] * len(reqs)
+        t_start = time.perf_counter()
+
+        def feeder():
+            for i, r in enumerate(reqs):
+                dt = r["arrival"] - (time.perf_counter() - t_start)
+                if dt > 0:
+                    time.sleep(dt)
+                ids[i] = srv.submit(r["centers"], r["radii"], r["orders"], r["force"], tol=r["tol"])
+
+        f = th.Thread(target=feeder)
+        f.start()
+        f.join()
+        infos = [srv.wait(i)[1] for i in ids]
+        st = srv.stats()
+        srv.close()
+        lat = np.array([x["t_done"] - x["t_submit"] for x in infos])
+        span = max(x["t_done"] for x in infos) - min(x["t_submit"] for x in infos)
+        ok = all(x["status"] == 0 for x in infos)
+        return lat, span, st, ok, infos
+
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        lat, span, st, ok, infos = serve(stream, PREC_MIXED, args.slots)
+    total = allmax(dist, span)
+    sub = None
+    if args.fp64_subset > 0:
+        small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= args.fp64_subset]
+        if small:
+            lm, sm, _, okm, _ = serve(small, PREC_MIXED, args.slots)
+            lf, sf, _, okf, _ = serve(small, PREC_FP64, args.slots)
+            sub = {"requests": len(small), "max_spheres": args.fp64_subset, "submitted": "all at t=0",
+                   "mixed": {"solves_per_s": round(len(small) / sm, 4), "p50_ms": round(1e3 * np.percentile(lm, 50), 2),
+                             "p99_ms": round(1e3 * np.percentile(lm, 99), 2), "all_ok": okm},
+                   "fp64": {"solves_per_s": round(len(small) / sf, 4), "p50_ms": round(1e3 * np.percentile(lf, 50), 2),
+                            "p99_ms": round(1e3 * np.percentile(lf, 99), 2), "all_ok": okf},
+                   "speedup_solves_per_s": round(sf / sm, 3)}
+    if rank != 0:
+        return None
+    sizes = [len(r["radii"]) for r in stream]
+    value = world * len(stream) / total
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": len(stream),
+        "warmup": 0, "ms_per_step": round(1e3 * total / len(stream), 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 operator + f64 refinement (mixed)",
+        "data": "synthetic (seeded RSA packings, N(0,1) forces, Poisson arrivals)",
+        "config": {"workload": "cfg5: served stream, %d requests, Poisson rate %.2f/s, N log-uniform [4,%d], "
+                               "p in {8,12,16,24}, a~U[0.9,1.1], gap 0.05, tol 1e-6/1e-8" % (len(stream), args.rate, args.nmax),
+                   "slots": args.slots, "parallelism": "replicas only",
+                   "l2": "not flushed: requests arrive in real time, latency measured on the server clock"},
+        "latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 2),
+                       "p99": round(1e3 * float(np.percentile(lat, 99)), 2)},
+        "queue_wait_ms_p50": round(1e3 * float(np.percentile([x["t_admit"] - x["t_submit"] for x in infos], 50)), 2),
+        "all_converged": ok, "span_s": round(total, 3),
+        "requests": {"spheres_min": int(min(sizes)), "spheres_max": int(max(sizes)), "spheres_median": float(np.median(sizes))},
+        "server": {"peak_running": st["peak_running"], "peak_bytes": st["peak_bytes"], "budget_bytes": st["budget_bytes"]},
+        "small_request_subset_vs_fp64": sub,
+        "e2e": None, "clocks": clk.summary(),
+    }
+
+
 CONFIG_TEXT = {
     "cfg3": "1024 spheres a~U[0.8,1.2], RSA in box 40 (min gap 0.05), p=16, mixed FP32/FP64 to 1e-8",
     "cfg4": "256 independent problems, N~U{2..128}, p~U{8,12,16}, a=1, box 4N^(1/3), gap 0.1, one batched solve",
@@ -474,15 +546,24 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
-    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4"])
+    ap.add_argument("--config", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5"])
     ap.add_argument("--ref", default="ff", choices=["ff", "fp64", "none"],
                     help="cfg3/cfg4: reference solve for the error (ff = FP64-accurate float-float far field)")
+    ap.add_argument("--requests", type=int, default=32, help="cfg5: requests in the stream")
+    ap.add_argument("--rate", type=float, default=2.0, help="cfg5: Poisson arrival rate (requests/s)")
+    ap.add_argument("--nmax", type=int, default=2048, help="cfg5: largest sphere count of a request")
+    ap.add_argument("--slots", type=int, default=8, help="cfg5: requests on the GPU at once")
+    ap.add_argument("--hbm-budget", type=float, default=0.0, help="cfg5: admission budget in bytes (0: 64 GB)")
+    ap.add_argument("--fp64-subset", type=int, default=0,
+                    help="cfg5: also serve the requests with at most this many spheres in mixed and plain FP64")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
     world, rank, local, dist = dist_init()
     if args.impl == "reference":
         line = run_reference(args, rank)
+    elif args.config == "cfg5":
+        line = run_serving(args, world, rank, local, dist)
     elif args.config != "cfg2":
         line = run_config(args, world, rank, local, dist)
     else:

@@ -152,6 +152,49 @@ smob_status smob_solve_mob_device(smob_ctx* ctx, const double* d_force6n, double
 smob_status smob_mob_apply(smob_ctx* ctx, const double* X, double* Y, int n_cols, double alpha, double beta,
                            const smob_solve_opts* opts);
 
+/* ---- serving: a request loop with continuous batching (no counterpart in the reference, which
+ * solves one system per time step inside SphereSystem::resolveCollision, SRC/SphereSystem.cpp:403-479).
+ * Requests (one independent problem each) are queued FIFO; up to max_slots of them are on the GPU
+ * at once, each admitted when a slot is free and its device-memory footprint (smob_request_bytes)
+ * fits in what the running requests leave of hbm_budget_bytes. Every request runs on its own
+ * stream with its own device-resident Krylov state, so concurrent requests overlap on the device;
+ * a request's result is the same alone or in any mix (each is solved exactly as if alone). */
+typedef struct smob_server smob_server;
+typedef struct {
+    int device;
+    int max_slots;           /* requests on the GPU at once */
+    double hbm_budget_bytes; /* admission budget (<= 0: 64 GB) */
+    int restart;             /* GMRES restart */
+    int max_iters;           /* GMRES iteration limit per request */
+    int precision;           /* smob_precision of every request */
+    double inner_tol;        /* MIXED inner tolerance (<= 0: library default) */
+} smob_server_opts;
+typedef struct {
+    int state;               /* 0 queued, 1 on the GPU, 2 done */
+    int status;              /* smob_status of the solve (when done) */
+    double t_submit, t_admit, t_done; /* seconds since the server started */
+    double bytes;            /* admission footprint */
+    smob_problem_stats stats;
+} smob_request_info;
+typedef struct {
+    int queued, running;
+    long long completed;
+    double bytes_in_use, peak_bytes, budget_bytes, uptime_s;
+    int peak_running;
+} smob_server_info;
+smob_status smob_server_create(smob_server** server, const smob_server_opts* opts);
+smob_status smob_server_submit(smob_server* server, const smob_geometry* geom, const double* force6n, double tol,
+                               long long* request_id);
+smob_status smob_server_poll(smob_server* server, long long request_id, double* vel6n, smob_request_info* info,
+                             int* done);
+smob_status smob_server_wait(smob_server* server, long long request_id, double timeout_s, double* vel6n,
+                             smob_request_info* info);
+smob_status smob_server_release(smob_server* server, long long request_id);
+smob_status smob_server_stats(smob_server* server, smob_server_info* info);
+smob_status smob_server_destroy(smob_server* server);
+/* admission footprint estimate (bytes of device memory) of one request; host-only arithmetic */
+size_t smob_request_bytes(int n_spheres, const int* orders, int restart);
+
 /* ---- device memory helpers for callers that time resident inputs ---- */
 smob_status smob_device_alloc(smob_ctx* ctx, size_t bytes, void** ptr);
 smob_status smob_device_free(smob_ctx* ctx, void* ptr);

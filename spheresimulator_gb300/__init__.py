@@ -208,6 +208,83 @@ class SphereSTKSHOperator(_Context):
         return out
 
 
+def request_bytes(orders, restart=50):
+    """Device-memory footprint the server uses to admit a request (host arithmetic only)."""
+    o = N.i32(orders).reshape(-1)
+    return int(N.lib().smob_request_bytes(len(o), N.iptr(o), int(restart)))
+
+
+class SolveServer:
+    """Request loop with continuous batching of mobility solves on one GPU (smob_server_*)."""
+
+    def __init__(self, device=0, max_slots=8, hbm_budget_bytes=0.0, restart=50, max_iters=2000,
+                 precision=PREC_MIXED, inner_tol=0.0):
+        self._L = N.lib()
+        opts = N.ServerOpts(int(device), int(max_slots), float(hbm_budget_bytes), int(restart), int(max_iters),
+                            int(precision), float(inner_tol))
+        h = ctypes.c_void_p()
+        N.check(self._L.smob_server_create(ctypes.byref(h), ctypes.byref(opts)))
+        self._h = h
+        self._n = {}
+
+    def submit(self, centers, radii, orders, force, tol=1e-8, quats=None, viscosity=1.0):
+        c = N.f64(centers).reshape(-1, 3)
+        r = N.f64(radii).reshape(-1)
+        o = N.i32(orders).reshape(-1)
+        q = None if quats is None else N.f64(quats).reshape(-1, 4)
+        f = N.f64(force).reshape(-1)
+        geo = N.Geometry(len(r), N.dptr(c), N.dptr(r), N.dptr(q), N.iptr(o), None, float(viscosity))
+        rid = ctypes.c_longlong()
+        N.check(self._L.smob_server_submit(self._h, ctypes.byref(geo), N.dptr(f), float(tol), ctypes.byref(rid)))
+        self._n[rid.value] = len(r)
+        return rid.value
+
+    def poll(self, rid):
+        vel = np.zeros(6 * self._n[rid])
+        info = N.RequestInfo()
+        done = ctypes.c_int()
+        N.check(self._L.smob_server_poll(self._h, rid, N.dptr(vel), ctypes.byref(info), ctypes.byref(done)))
+        return (vel if done.value else None), self._info(info)
+
+    def wait(self, rid, timeout=0.0):
+        vel = np.zeros(6 * self._n[rid])
+        info = N.RequestInfo()
+        code = self._L.smob_server_wait(self._h, rid, float(timeout), N.dptr(vel), ctypes.byref(info))
+        N.check(code, allow=(N.SMOB_ERR_NOT_CONVERGED,))
+        return vel, self._info(info)
+
+    def release(self, rid):
+        N.check(self._L.smob_server_release(self._h, rid))
+        self._n.pop(rid, None)
+
+    def stats(self):
+        s = N.ServerInfo()
+        N.check(self._L.smob_server_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    @staticmethod
+    def _info(i):
+        return {"state": i.state, "status": i.status, "t_submit": i.t_submit, "t_admit": i.t_admit,
+                "t_done": i.t_done, "bytes": i.bytes, "stats": i.stats.as_dict()}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.smob_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class SphereSTKMobMat(SphereSTKSHOperator):
     """Mobility matrix force/torque (6N) -> velocity/angular velocity (6N)
     (BIE/SphereSTKMobMat.cpp:98-286). One context may hold several independent problems

@@ -18,7 +18,7 @@ LIB = os.path.join(LIBDIR, "libsmob.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp", "-I" + INCLUDE, "-I" + CSRC]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-pthread", "-I" + INCLUDE, "-I" + CSRC]
 
 
 def _nvcc():
@@ -67,7 +67,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp%d" % os.getpid()
-    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp", "-lcudart"]
+    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp,-pthread", "-lgomp", "-lcudart"]
     if verbose:
         print(" ".join(link), flush=True)
     r = subprocess.run(link, capture_output=True, text=True)

@@ -51,6 +51,24 @@ class ProblemStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_slots", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double),
+                ("restart", ctypes.c_int), ("max_iters", ctypes.c_int), ("precision", ctypes.c_int),
+                ("inner_tol", ctypes.c_double)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("bytes", ctypes.c_double),
+                ("stats", ProblemStats)]
+
+
+class ServerInfo(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_int), ("running", ctypes.c_int), ("completed", ctypes.c_longlong),
+                ("bytes_in_use", ctypes.c_double), ("peak_bytes", ctypes.c_double), ("budget_bytes", ctypes.c_double),
+                ("uptime_s", ctypes.c_double), ("peak_running", ctypes.c_int)]
+
+
 _lib = None
 _DP = ctypes.POINTER(ctypes.c_double)
 _IP = ctypes.POINTER(ctypes.c_int)
@@ -108,6 +126,15 @@ def lib():
         "smob_flush_l2": (S, [_VP, ctypes.c_size_t]),
         "smob_measure_fma_peaks": (S, [ctypes.c_int, _DP, _DP]),
         "smob_far_traction_noalloc": (S, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_double, _VP, _VP]),
+        "smob_server_create": (S, [ctypes.POINTER(_VP), ctypes.POINTER(ServerOpts)]),
+        "smob_server_submit": (S, [_VP, ctypes.POINTER(Geometry), _DP, ctypes.c_double,
+                                   ctypes.POINTER(ctypes.c_longlong)]),
+        "smob_server_poll": (S, [_VP, ctypes.c_longlong, _DP, ctypes.POINTER(RequestInfo), _IP]),
+        "smob_server_wait": (S, [_VP, ctypes.c_longlong, ctypes.c_double, _DP, ctypes.POINTER(RequestInfo)]),
+        "smob_server_release": (S, [_VP, ctypes.c_longlong]),
+        "smob_server_stats": (S, [_VP, ctypes.POINTER(ServerInfo)]),
+        "smob_server_destroy": (S, [_VP]),
+        "smob_request_bytes": (ctypes.c_size_t, [ctypes.c_int, _IP, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -27,6 +27,10 @@
 
 using namespace smob;
 
+namespace smob {
+smob_status create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank);
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -45,16 +49,28 @@ struct SmobError : std::runtime_error {
         }                                                                                               \
     } while (0)
 
+// Stream that device buffers of the current call are allocated and freed on. Buffers use the
+// stream-ordered allocator (cudaMallocAsync / cudaFreeAsync) so that creating or destroying one
+// context never synchronizes the device: concurrent solves on other streams keep running.
+thread_local cudaStream_t g_alloc_stream = nullptr;
+
+struct AllocStreamScope {
+    cudaStream_t prev;
+    explicit AllocStreamScope(cudaStream_t s) : prev(g_alloc_stream) { g_alloc_stream = s; }
+    ~AllocStreamScope() { g_alloc_stream = prev; }
+};
+
 // device buffer (RAII)
 struct DBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    cudaStream_t s = nullptr;  // stream the buffer was allocated on (freed on the same stream)
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, s);
         p = nullptr;
         bytes = 0;
     }
@@ -62,7 +78,8 @@ struct DBuf {
         if (b <= bytes && p) return;
         release();
         if (b == 0) b = 16;
-        CUDA_OK(cudaMalloc(&p, b));
+        s = g_alloc_stream;
+        CUDA_OK(cudaMallocAsync(&p, b, s));
         bytes = b;
     }
     template <typename T>
@@ -70,7 +87,18 @@ struct DBuf {
     template <typename T>
     void upload(const std::vector<T>& v) {
         alloc(v.size() * sizeof(T));
-        if (!v.empty()) CUDA_OK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!v.empty()) CUDA_OK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+};
+
+// owns the context's stream; declared first in smob_ctx so it is destroyed after every buffer
+struct StreamHolder {
+    cudaStream_t st = nullptr;
+    ~StreamHolder() {
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
     }
 };
 
@@ -85,6 +113,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace smob
 
 struct smob_ctx {
+    StreamHolder sh;  // first member: destroyed last, after all buffers were freed on it
     int device = 0;
     cudaStream_t st = nullptr;
     int N = 0, M = 0, P = 0, pmax = 0;
@@ -168,7 +197,6 @@ struct smob_ctx {
         if (ev_a) cudaEventDestroy(ev_a);
         if (ev_b) cudaEventDestroy(ev_b);
         drop_graphs();
-        if (st) cudaStreamDestroy(st);
     }
 };
 
@@ -1083,6 +1111,15 @@ smob_status smob_version(int* major, int* minor) {
 }
 
 smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
+    return smob::create_context(out, geo, device, -1);
+}
+
+}  // extern "C"
+
+// Context creation with a stream priority: priority_rank 0 is the device's highest stream
+// priority, larger ranks step towards the lowest; -1 keeps the default. The server gives small
+// requests high priority so their kernels are scheduled ahead of large requests' blocks.
+smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank) {
     return guarded([&]() -> smob_status {
         need(out != nullptr && geo != nullptr, "null argument");
         *out = nullptr;
@@ -1098,15 +1135,26 @@ smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
         std::unique_ptr<smob_ctx> c(new smob_ctx);
         c->device = device;
         CUDA_OK(cudaSetDevice(device));
-        CUDA_OK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        if (priority_rank >= 0) {
+            int least = 0, greatest = 0;
+            CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            const int prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
+            CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
+        } else {
+            CUDA_OK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        }
+        c->sh.st = c->st;
+        AllocStreamScope scope(c->st);
         configure_sphere_kernels();
         build_context(c.get(), geo);
         autotune_far32(c.get());
-        CUDA_OK(cudaDeviceSynchronize());
+        CUDA_OK(cudaStreamSynchronize(c->st));
         *out = c.release();
         return SMOB_OK;
     });
 }
+
+extern "C" {
 
 smob_status smob_destroy(smob_ctx* c) {
     if (!c) return SMOB_OK;
@@ -1321,6 +1369,7 @@ smob_status smob_solve_mob_device(smob_ctx* c, const double* d_force, double* d_
         need(c && d_force && d_vel, "null argument");
         check_opts(o);
         set_device(c);
+        AllocStreamScope scope(c->st);
         smob_status s = solve_device(c, d_force, d_vel, d_density, o, stats);
         prof_flush(c);
         return s;
@@ -1333,6 +1382,7 @@ smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double
         need(c && force && vel, "null argument");
         check_opts(o);
         set_device(c);
+        AllocStreamScope scope(c->st);
         for (int i = 0; i < 6 * c->N; ++i)
             if (!std::isfinite(force[i])) throw SmobError(SMOB_ERR_NONFINITE, "force/torque input is not finite");
         ensure_solver(c, std::max(1, o->restart));
@@ -1514,6 +1564,7 @@ smob_status smob_flush_l2(smob_ctx* c, size_t bytes) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
         set_device(c);
+        AllocStreamScope scope(c->st);
         c->d_flush.alloc(bytes);
         CUDA_OK(cudaMemsetAsync(c->d_flush.p, int(c->flush_val++ & 0xff), bytes, c->st));
         CUDA_OK(cudaStreamSynchronize(c->st));
