@@ -81,7 +81,8 @@ typedef struct {
     int status;        /* smob_status of this problem */
     int iterations;    /* GMRES iterations (MIXED: summed over refinement sweeps) */
     int refinements;   /* MIXED: refinement sweeps; FP64: restart cycles */
-    int operator_passes_fp64; /* high-precision operator applications (including b and the final velocity) */
+    int operator_passes_fp64; /* high-precision operator applications (FP64 / float-float: including b and
+                                 the final velocity; MIXED: fused residual + single-layer passes, one each) */
     int operator_passes_fp32; /* FP32 operator applications */
     double relres;     /* final true relative residual |b - A mu|/|b| computed in the high-precision operator */
     double bnorm;      /* |b| */

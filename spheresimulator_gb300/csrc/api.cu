@@ -138,7 +138,7 @@ struct smob_ctx {
     DBuf d_center, d_radius, d_quat, d_order, d_gidx, d_glen, d_coff, d_prob, d_coords, d_norms, d_weights, d_sid;
     DBuf d_pos32, d_nrm32, d_pos32lo, d_nrm32lo, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_nbr_precise, d_near_slot,
         d_slot_sphere, d_problems, d_tabs, d_srcdf;
-    DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_chunks;
+    DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_items_df, d_chunks;
     DBuf d_active;
     // operator workspace
     DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
@@ -146,6 +146,8 @@ struct smob_ctx {
     // solver workspace
     int restart_cap = 0;
     DBuf d_V, d_w, d_r, d_x, d_xlast, d_b, d_rho, d_u, d_force, d_vel;
+    // mixed solve: rho + x, and the single layer of rho + x_hp at the last high-precision residual x_hp
+    DBuf d_dens, d_uhp, d_xhp, d_partial64_sl;
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
     bool have_xlast = false;
 
@@ -570,6 +572,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_map_val_f.upload(mvalf);
     c->d_items32.upload(c->items32);
     c->d_items64.upload(c->items64);
+    c->d_items_df.upload(c->items_tpt[1]);  // float-float far field: 256 targets per CTA, 2 per thread
     c->d_chunks.upload(c->chunks);
     std::vector<unsigned char> act(c->P, 1);
     c->d_active.upload(act);
@@ -748,8 +751,8 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_far_pack_df(g, x, cc, c->d_srcdf.as<float4>(), c->st));
             }
             ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
-            check_launch(c, launch_far_field_df(g, items, nitems, tr, c->d_srcdf.as<float4>(),
-                                                static_cast<double*>(partial), c->st));
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), tr ? 1 : 0,
+                                                c->d_srcdf.as<float4>(), static_cast<double*>(partial), nullptr, c->st));
         } else {
             {
                 ProfScope ps(c, "far_pack");
@@ -770,6 +773,48 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
         ProfScope ps(c, "sphere_self");
         check_launch(c, launch_sphere_op(g, x, out, id ? c_id : 0.0, 0.0, -1, c_lop, nullptr, fp32, c->st));
     }
+}
+
+// High-precision traction and single layer of one density in one pass, on active problems:
+// out_t += c_id*x + c_trac*K[x] and out_s += c_sl*S[x]. Self and near parts in FP64; the far field is
+// one float-float pass that evaluates both kernels per pair (shared r, 1/r, r.f).
+void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, double c_trac, double* out_s,
+                      double c_sl) {
+    const DevGeom& g = c->g;
+    const int nslots = (int)c->slot_sphere.size();
+    c->d_partial64_sl.alloc(sizeof(double) * c->partial64);
+    {
+        ProfScope ps(c, "sphere_self");
+        check_launch(c, launch_sphere_op(g, x, out_t, c_id, c_trac, 3, 0.0, c->d_coef64.p, false, c->st));
+        check_launch(c, launch_sphere_op(g, x, out_s, 0.0, c_sl, 0, 0.0, nullptr, false, c->st));
+    }
+    if (nslots > 0) {
+        for (int k = 0; k < 2; ++k) {
+            const bool tr = k == 0;
+            const long long stride = tr ? c->set_stride_trac : c->set_stride_sl;
+            {
+                ProfScope ps(c, "near_sets");
+                check_launch(c, launch_near_sets(g, c->d_coef64.p, tr, false, c->d_sets64.p, nslots,
+                                                 c->d_slot_sphere.as<int>(), stride, c->st));
+            }
+            ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
+            check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, tr ? c_trac : c_sl, tr ? out_t : out_s,
+                                             c->st, 0));
+        }
+    }
+    {
+        ProfScope ps(c, "far_pack");
+        check_launch(c, launch_far_pack_df(g, x, 1.0, c->d_srcdf.as<float4>(), c->st));
+    }
+    {
+        ProfScope ps(c, "far_both_df");
+        check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
+                                            c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
+                                            c->d_partial64_sl.as<double>(), c->st));
+    }
+    ProfScope ps(c, "far_reduce");
+    check_launch(c, launch_far_reduce(g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), out_t, c->st));
+    check_launch(c, launch_far_reduce(g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), out_s, c->st));
 }
 
 // ---------------------------------------------------------------- solver
@@ -851,12 +896,28 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     CUDA_OK(cudaMemcpyAsync(ks, hks.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
     std::vector<int> passes64(P, 0), cycles(P, 0), passes32x(P, 0);
     std::vector<char> hp_resid_done(P, 0);  // a high-precision residual after a cycle exists
+    // MIXED: beta[p] is a high-precision residual norm (or one updated from it by a small FP32 step);
+    // only such a residual may end a problem's solve
+    std::vector<char> hp_now(P, mixed ? 0 : 1);
+    std::vector<char> x_moved(P, 0);  // MIXED: x changed since the last high-precision residual
+    double *dens = nullptr, *uhp = nullptr, *xhp = nullptr;
+    if (mixed) {
+        c->d_dens.alloc(sizeof(double) * n);
+        c->d_uhp.alloc(sizeof(double) * n);
+        c->d_xhp.alloc(sizeof(double) * n);
+        dens = c->d_dens.as<double>();
+        uhp = c->d_uhp.as<double>();
+        xhp = c->d_xhp.as<double>();
+    }
 
-    // step 1: rigid density; step 2: b = -(I/2 + K) rho  (high precision)
+    // step 1: rigid density; step 2: b = -(I/2 + K) rho. FP64 / float-float: in the solve's precision.
+    // MIXED: with the FP32 operator. b only seeds the first inner cycle and scales the tolerance; every
+    // high-precision residual is formed directly as r = -(I/2 + K)(rho + x) - L x, so b's FP32 error
+    // never reaches a residual that decides convergence.
     check_launch(c, launch_rigid_density(c->g, d_force, rho, st));
     CUDA_OK(cudaMemsetAsync(b, 0, sizeof(double) * n, st));
-    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, hp);
-    for (auto& v : passes64) v++;
+    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, mixed ? OP_FP32 : hp);
+    for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
     std::vector<double> bnorm = seg_norms(c, b, act);
 
     // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution or zero
@@ -865,8 +926,9 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     if (o->warm_start && c->have_xlast) {
         CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
-        for (auto& v : passes64) v++;
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
+        for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
+        if (mixed) std::fill(x_moved.begin(), x_moved.end(), 1);
         check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
         check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
     } else {
@@ -906,7 +968,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         int ncyc = 0;
         for (int p = 0; p < P; ++p) {
             if (done[p]) continue;
-            if (beta[p] / bnorm[p] < tol) {
+            if (beta[p] / bnorm[p] < tol && hp_now[p]) {
                 done[p] = 1;
                 conv[p] = 1;
                 continue;
@@ -985,42 +1047,89 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
         check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, w, st));
         check_launch(c, launch_axpby_seg(L, 1.0, w, 1.0, act, x, st));
-        // Residual. FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos'
-        // restart). MIXED: r = b - A x with the high-precision operator, except once the previous
-        // high-precision residual is below 1e-4 |b|: then r <- r - A32 d, whose FP32 error
-        // ~eps32 * kappa * |r_prev| (<= ~1e-10 |b|) is far below the 1e-8 target, so one
-        // high-precision pass is saved per later refinement sweep.
-        bool upd_all = mixed;
-        for (int p = 0; p < P; ++p)
-            if (cyc[p] && !(hp_resid_done[p] && beta[p] <= 1e-4 * bnorm[p])) upd_all = false;
-        if (upd_all) {
+        // Residual, decided per problem (so a problem takes the same steps alone or in any batch).
+        // FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos' restart).
+        // MIXED, once the previous high-precision residual is below 1e-4 |b|: r <- r - A32 d, whose
+        // FP32 error ~eps32 * kappa * |r_prev| (<= ~1e-10 |b|) is far below the 1e-8 target.
+        // MIXED otherwise: one fused high-precision pass gives r = -(I/2 + K)(rho + x) - L x and the
+        // single layer u_hp = S[rho + x] (the final velocity then needs only S32[x - x_hp]).
+        std::vector<unsigned char> upd(P, 0), hpres(P, 0);
+        bool any_upd = false, any_hp = false;
+        for (int p = 0; p < P; ++p) {
+            if (!cyc[p]) continue;
+            if (mixed && hp_resid_done[p] && beta[p] <= 1e-4 * bnorm[p]) upd[p] = 1, any_upd = true;
+            else hpres[p] = 1, any_hp = true;
+        }
+        if (any_upd) {
+            set_active(c, upd);
             CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
             op_apply(c, w, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
-            for (int p = 0; p < P; ++p)
-                if (cyc[p]) passes32x[p]++;
             check_launch(c, launch_axpby_seg(L, -1.0, u, 1.0, act, r, st));
-        } else {
-            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
             for (int p = 0; p < P; ++p)
-                if (cyc[p]) {
-                    passes64[p]++;
-                    hp_resid_done[p] = 1;
-                }
-            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+                if (upd[p]) passes32x[p]++, x_moved[p] = 1;
         }
+        if (any_hp) {
+            set_active(c, hpres);
+            if (mixed) {
+                CUDA_OK(cudaMemcpyAsync(dens, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+                check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, dens, st));
+                CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+                CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+                op_apply_hp_both(c, dens, u, -0.5, -1.0, w, 1.0);
+                op_apply(c, x, u, 0.0, 0.0, 0.0, -1.0, OP_FP64);  // - L x (per-sphere rigid modes)
+                check_launch(c, launch_axpby_seg(L, 1.0, u, 0.0, act, r, st));
+                check_launch(c, launch_axpby_seg(L, 1.0, w, 0.0, act, uhp, st));
+                check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, xhp, st));
+            } else {
+                CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+                op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
+                check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+                check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+            }
+            for (int p = 0; p < P; ++p)
+                if (hpres[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
+        }
+        set_active(c, cyc);
         std::vector<double> nb = seg_norms(c, r, act);
         for (int p = 0; p < P; ++p)
             if (cyc[p]) beta[p] = nb[p];
     }
 
-    // step 4: rho += mu; u = S[rho] (FP64); rigid averages / viscosity (SphereSTKMobMat.cpp:243-285)
+    // step 4: rho += mu; u = S[rho] (high precision); rigid averages / viscosity (SphereSTKMobMat.cpp:243-285).
+    // MIXED problems with a high-precision residual already hold u_hp = S[rho + x_hp]:
+    // u = u_hp + S32[x - x_hp], the FP32 part acting on the last small correction only.
+    CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+    std::vector<unsigned char> from_hp(P, 0), moved(P, 0), fresh(P, 0);
+    bool any_from_hp = false, any_moved = false, any_fresh = false;
+    for (int p = 0; p < P; ++p) {
+        if (mixed && hp_resid_done[p]) {
+            from_hp[p] = 1, any_from_hp = true;
+            if (x_moved[p]) moved[p] = 1, any_moved = true;
+        } else {
+            fresh[p] = 1, any_fresh = true;
+        }
+    }
+    if (any_from_hp) {
+        set_active(c, from_hp);
+        check_launch(c, launch_axpby_seg(L, 1.0, uhp, 0.0, act, u, st));
+    }
+    if (any_moved) {
+        set_active(c, moved);
+        check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, w, st));
+        check_launch(c, launch_axpby_seg(L, -1.0, xhp, 1.0, act, w, st));
+        op_apply(c, w, u, 0.0, 1.0, 0.0, 0.0, OP_FP32);
+        for (int p = 0; p < P; ++p)
+            if (moved[p]) passes32x[p]++;
+    }
     set_active(c, all);
     check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, rho, st));
-    CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-    op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, hp);
-    for (auto& v : passes64) v++;
+    if (any_fresh) {
+        set_active(c, fresh);
+        op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, hp);
+        for (int p = 0; p < P; ++p)
+            if (fresh[p]) passes64[p]++;
+        set_active(c, all);
+    }
     check_launch(c, launch_rigid_average(c->g, u, 1.0 / c->viscosity, d_vel, st));
     if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     CUDA_OK(cudaMemcpyAsync(c->d_xlast.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -1285,8 +1394,9 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 if (dfar) {
                     check_launch(c, launch_far_pack_df(c->g, din, cc, c->d_srcdf.as<float4>(), c->st));
                     ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
-                    check_launch(c, launch_far_field_df(c->g, items, nitems, tr, c->d_srcdf.as<float4>(),
-                                                        static_cast<double*>(partial), c->st));
+                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(),
+                                                        tr ? 1 : 0, c->d_srcdf.as<float4>(), static_cast<double*>(partial),
+                                                        nullptr, c->st));
                 } else {
                     check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
                     ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));

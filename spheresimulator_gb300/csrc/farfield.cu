@@ -82,6 +82,140 @@ __device__ __forceinline__ bool excluded(const int* __restrict__ nbr_src, int& c
     return cur < end && __ldg(nbr_src + cur) == s;
 }
 
+// ---------------------------------------------------------------- packed FP32x2 far field
+// Blackwell issues two FP32 lanes per FFMA2/FADD2/FMUL2 instruction (__ffma2_rn & co., same
+// per-component rounding as the scalar forms). Targets are packed two per float2; each staged
+// source is stored pre-duplicated, (x,x,y,y) (z,z,fx,fx) (fy,fy,fz,fz), so three 128-bit shared
+// loads give the six broadcast operands. Per pair: ~10 packed instructions + 1 MUFU.RSQ.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+template <bool TRAC>
+__device__ __forceinline__ void pair_x2(const float2& tx, const float2& ty, const float2& tz, const float2& nx,
+                                        const float2& ny, const float2& nz, const float4& A, const float4& B,
+                                        const float4& C, float2& ax, float2& ay, float2& az) {
+    const float2 rx = __fadd2_rn(tx, f2(-A.x, -A.y));
+    const float2 ry = __fadd2_rn(ty, f2(-A.z, -A.w));
+    const float2 rz = __fadd2_rn(tz, f2(-B.x, -B.y));
+    const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __fmul2_rn(rz, rz)));
+    const float2 ri = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+    const float2 rf = __ffma2_rn(rx, f2(B.z, B.w), __ffma2_rn(ry, f2(C.x, C.y), __fmul2_rn(rz, f2(C.z, C.w))));
+    if (TRAC) {
+        const float2 rn = __ffma2_rn(rx, nx, __ffma2_rn(ry, ny, __fmul2_rn(rz, nz)));
+        const float2 ri2 = __fmul2_rn(ri, ri);
+        const float2 k = __fmul2_rn(__fmul2_rn(rf, rn), __fmul2_rn(__fmul2_rn(ri2, ri2), ri));
+        ax = __ffma2_rn(k, rx, ax);
+        ay = __ffma2_rn(k, ry, ay);
+        az = __ffma2_rn(k, rz, az);
+    } else {
+        const float2 k = __fmul2_rn(rf, __fmul2_rn(__fmul2_rn(ri, ri), ri));
+        ax = __ffma2_rn(f2(B.z, B.w), ri, __ffma2_rn(k, rx, ax));
+        ay = __ffma2_rn(f2(C.x, C.y), ri, __ffma2_rn(k, ry, ay));
+        az = __ffma2_rn(f2(C.z, C.w), ri, __ffma2_rn(k, rz, az));
+    }
+}
+
+// NPK float2 packs = 2*NPK targets per thread; a work item covers kFarThreads * 2 * NPK targets
+template <bool TRAC, int NPK>
+__global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarItem* __restrict__ items,
+                                                        const float4* __restrict__ src, float* __restrict__ partial) {
+    constexpr int T = 2 * NPK;
+    const FarItem it = items[blockIdx.x];
+    if (g.active && !g.active[it.problem]) return;
+    __shared__ float4 sA[kFarTile32], sB[kFarTile32], sC[kFarTile32];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 TX[NPK], TY[NPK], TZ[NPK], NX[NPK], NY[NPK], NZ[NPK], AX[NPK], AY[NPK], AZ[NPK];
+    int sid[T], cur[T], end[T];
+    bool val[T];
+#pragma unroll
+    for (int q = 0; q < NPK; ++q) {
+        float4 P[2], Nn[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int u = 2 * q + h;
+            const int t = it.t0 + threadIdx.x + u * kFarThreads;
+            val[u] = t < it.t1;
+            P[h] = val[u] ? g.pos32[t] : z4;
+            Nn[h] = (TRAC && val[u]) ? g.nrm32[t] : z4;
+            sid[u] = val[u] ? __float_as_int(P[h].w) : -1;
+            cur[u] = val[u] ? g.nbr_start[sid[u]] : 0;
+            end[u] = val[u] ? g.nbr_start[sid[u] + 1] : 0;
+        }
+        TX[q] = f2(P[0].x, P[1].x);
+        TY[q] = f2(P[0].y, P[1].y);
+        TZ[q] = f2(P[0].z, P[1].z);
+        NX[q] = f2(Nn[0].x, Nn[1].x);
+        NY[q] = f2(Nn[0].y, Nn[1].y);
+        NZ[q] = f2(Nn[0].z, Nn[1].z);
+        AX[q] = AY[q] = AZ[q] = f2(0.f, 0.f);
+    }
+    for (int s = it.s0; s < it.s1; ++s) {
+        bool sk[T];
+        bool all = true, none = true;
+#pragma unroll
+        for (int u = 0; u < T; ++u) {
+            sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
+            all = all && sk[u];
+            none = none && !sk[u];
+        }
+        if (__syncthreads_and(all)) continue;
+        const int g0 = g.gidx[s], gl = g.glen[s];
+        for (int base = 0; base < gl; base += kFarTile32) {
+            const int n = min(kFarTile32, gl - base);
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += kFarThreads) {
+                const float4 p = g.pos32[g0 + base + k], f = src[g0 + base + k];
+                sA[k] = make_float4(p.x, p.x, p.y, p.y);
+                sB[k] = make_float4(p.z, p.z, f.x, f.x);
+                sC[k] = make_float4(f.y, f.y, f.z, f.z);
+            }
+            __syncthreads();
+            if (none) {
+#pragma unroll 2
+                for (int k = 0; k < n; ++k) {
+                    const float4 A = sA[k], B = sB[k], C = sC[k];
+#pragma unroll
+                    for (int q = 0; q < NPK; ++q)
+                        pair_x2<TRAC>(TX[q], TY[q], TZ[q], NX[q], NY[q], NZ[q], A, B, C, AX[q], AY[q], AZ[q]);
+                }
+            } else {
+                // some targets skip this sphere: compute the packs and keep only the wanted lanes
+                for (int k = 0; k < n; ++k) {
+                    const float4 A = sA[k], B = sB[k], C = sC[k];
+#pragma unroll
+                    for (int q = 0; q < NPK; ++q) {
+                        float2 dx = f2(0.f, 0.f), dy = dx, dz = dx;
+                        pair_x2<TRAC>(TX[q], TY[q], TZ[q], NX[q], NY[q], NZ[q], A, B, C, dx, dy, dz);
+                        if (!sk[2 * q]) {
+                            AX[q].x += dx.x;
+                            AY[q].x += dy.x;
+                            AZ[q].x += dz.x;
+                        }
+                        if (!sk[2 * q + 1]) {
+                            AX[q].y += dx.y;
+                            AY[q].y += dy.y;
+                            AZ[q].y += dz.y;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const Problem pr = g.problems[it.problem];
+    const long long mp = pr.p1 - pr.p0;
+    float* out = partial + pr.poff + 3LL * mp * it.chunk;
+#pragma unroll
+    for (int q = 0; q < NPK; ++q)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int u = 2 * q + h;
+            if (!val[u]) continue;
+            float* o = out + 3LL * (it.t0 + threadIdx.x + u * kFarThreads - pr.p0);
+            o[0] = h ? AX[q].y : AX[q].x;
+            o[1] = h ? AY[q].y : AY[q].x;
+            o[2] = h ? AZ[q].y : AZ[q].x;
+        }
+}
+
 // TPT targets per thread (register blocking: each staged source serves TPT pairs); a work item
 // covers kFarThreads * TPT targets. The tile holds kFarTile32 sources, enough for a whole p=16
 // sphere, so most source spheres cost one staging round and two barriers.
@@ -212,108 +346,161 @@ __global__ void __launch_bounds__(kFarThreads) k_far64(DevGeom g, const FarItem*
 // ---------------------------------------------------------------- float-float (df64) far field
 // Each value is an unevaluated sum hi + lo of two floats (about 48 significant bits). All
 // arithmetic runs on the FP32 pipe (FMA for exact products), which GB300 issues 58x faster than
-// FP64; per traction pair ~190 FP32 instructions. Used for the high-precision passes of the
-// mixed-precision solve (right-hand side, refinement residuals, final single layer).
-struct df {
-    float h, l;
+// FP64. Used for the high-precision passes of the mixed-precision solve. Two targets share a
+// thread as the two lanes of packed FP32x2 instructions (FFMA2/FADD2/FMUL2): every instruction
+// advances two pairs, which halves the issue slots the error-free transformations take.
+// The _rn intrinsics keep every rounding explicit: the compiler may not contract a product into a
+// later addition, which would break the error-free transformations below.
+struct df2 {
+    float2 h, l;
 };
-
-// __fmul_rn/__fadd_rn/__fsub_rn keep every rounding explicit: the compiler may not contract a
-// product into a later addition, which would break the error-free transformations below.
-__device__ __forceinline__ df two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = sub2(s, a);
+    return {s, __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb))};
 }
-__device__ __forceinline__ df quick_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+__device__ __forceinline__ df2 quick_two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    return {s, sub2(b, sub2(s, a))};
 }
-__device__ __forceinline__ df df_add(df a, df b) {
-    const df s = two_sum(a.h, b.h);
-    return quick_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+__device__ __forceinline__ df2 df_add2(df2 a, df2 b) {
+    const df2 s = two_sum2(a.h, b.h);
+    return quick_two_sum2(s.h, __fadd2_rn(s.l, __fadd2_rn(a.l, b.l)));
 }
-__device__ __forceinline__ df df_mul(df a, df b) {
-    const float p = __fmul_rn(a.h, b.h);
-    const float e = fmaf(a.h, b.h, -p);
-    return quick_two_sum(p, fmaf(a.h, b.l, fmaf(a.l, b.h, e)));
+__device__ __forceinline__ df2 df_mul_u2(df2 a, df2 b) {
+    const float2 p = __fmul2_rn(a.h, b.h);
+    const float2 e = __ffma2_rn(a.h, b.h, neg2(p));
+    return {p, __ffma2_rn(a.h, b.l, __ffma2_rn(a.l, b.h, e))};
 }
-// product left unnormalised (|lo| may reach a few ulp of hi): fine as an input to further
-// products and to two_sum-based sums, and 3 instructions cheaper
-__device__ __forceinline__ df df_mul_u(df a, df b) {
-    const float p = __fmul_rn(a.h, b.h);
-    const float e = fmaf(a.h, b.h, -p);
-    return {p, fmaf(a.h, b.l, fmaf(a.l, b.h, e))};
+__device__ __forceinline__ df2 df_mul2(df2 a, df2 b) {
+    const df2 u = df_mul_u2(a, b);
+    return quick_two_sum2(u.h, u.l);
 }
-// a.a for a 3-vector of float-float components
-__device__ __forceinline__ df df_sqr3(df a, df b, df c) {
-    const float p0 = __fmul_rn(a.h, a.h), p1 = __fmul_rn(b.h, b.h), p2 = __fmul_rn(c.h, c.h);
-    float lo = __fadd_rn(__fadd_rn(fmaf(a.h, a.h, -p0), fmaf(b.h, b.h, -p1)), fmaf(c.h, c.h, -p2));
-    lo = fmaf(__fadd_rn(a.h, a.h), a.l, lo);
-    lo = fmaf(__fadd_rn(b.h, b.h), b.l, lo);
-    lo = fmaf(__fadd_rn(c.h, c.h), c.l, lo);
-    const df s01 = two_sum(p0, p1);
-    const df s = two_sum(s01.h, p2);
-    return quick_two_sum(s.h, __fadd_rn(__fadd_rn(s.l, s01.l), lo));
+__device__ __forceinline__ df2 df_dot3_2(df2 a, df2 b, df2 c, df2 d, df2 e, df2 f) {
+    const float2 p0 = __fmul2_rn(a.h, b.h), p1 = __fmul2_rn(c.h, d.h), p2 = __fmul2_rn(e.h, f.h);
+    float2 lo = __fadd2_rn(__fadd2_rn(__ffma2_rn(a.h, b.h, neg2(p0)), __ffma2_rn(c.h, d.h, neg2(p1))),
+                           __ffma2_rn(e.h, f.h, neg2(p2)));
+    lo = __ffma2_rn(a.h, b.l, __ffma2_rn(a.l, b.h, lo));
+    lo = __ffma2_rn(c.h, d.l, __ffma2_rn(c.l, d.h, lo));
+    lo = __ffma2_rn(e.h, f.l, __ffma2_rn(e.l, f.h, lo));
+    const df2 s01 = two_sum2(p0, p1);
+    const df2 s = two_sum2(s01.h, p2);
+    return quick_two_sum2(s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo));
 }
-// a*b + c*d + e*f with one renormalisation
-__device__ __forceinline__ df df_dot3(df a, df b, df c, df d, df e, df f) {
-    const float p0 = __fmul_rn(a.h, b.h), p1 = __fmul_rn(c.h, d.h), p2 = __fmul_rn(e.h, f.h);
-    float lo = __fadd_rn(__fadd_rn(fmaf(a.h, b.h, -p0), fmaf(c.h, d.h, -p1)), fmaf(e.h, f.h, -p2));
-    lo = fmaf(a.h, b.l, fmaf(a.l, b.h, lo));
-    lo = fmaf(c.h, d.l, fmaf(c.l, d.h, lo));
-    lo = fmaf(e.h, f.l, fmaf(e.l, f.h, lo));
-    const df s01 = two_sum(p0, p1);
-    const df s = two_sum(s01.h, p2);
-    return quick_two_sum(s.h, __fadd_rn(__fadd_rn(s.l, s01.l), lo));
+__device__ __forceinline__ df2 df_sqr3_2(df2 a, df2 b, df2 c) {
+    const float2 p0 = __fmul2_rn(a.h, a.h), p1 = __fmul2_rn(b.h, b.h), p2 = __fmul2_rn(c.h, c.h);
+    float2 lo = __fadd2_rn(__fadd2_rn(__ffma2_rn(a.h, a.h, neg2(p0)), __ffma2_rn(b.h, b.h, neg2(p1))),
+                           __ffma2_rn(c.h, c.h, neg2(p2)));
+    lo = __ffma2_rn(__fadd2_rn(a.h, a.h), a.l, lo);
+    lo = __ffma2_rn(__fadd2_rn(b.h, b.h), b.l, lo);
+    lo = __ffma2_rn(__fadd2_rn(c.h, c.h), c.l, lo);
+    const df2 s01 = two_sum2(p0, p1);
+    const df2 s = two_sum2(s01.h, p2);
+    return quick_two_sum2(s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo));
 }
-__device__ __forceinline__ df df_rsqrt(df x) {
-    const float y = rsqrtf(x.h);
-    const float yy = __fmul_rn(y, y);
-    const float yye = fmaf(y, y, -yy);
-    // x*y^2 = 1 - e, evaluated to double-float accuracy; one Newton step squares the error
-    const float p = __fmul_rn(x.h, yy);
-    const float pe = fmaf(x.h, yy, -p);
-    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), fmaf(x.h, yye, __fmul_rn(x.l, yy)));
-    return quick_two_sum(y, __fmul_rn(__fmul_rn(0.5f, y), e));
+__device__ __forceinline__ df2 df_rsqrt2(df2 x) {
+    const float2 y = make_float2(rsqrtf(x.h.x), rsqrtf(x.h.y));
+    const float2 yy = __fmul2_rn(y, y);
+    const float2 yye = __ffma2_rn(y, y, neg2(yy));
+    const float2 p = __fmul2_rn(x.h, yy);
+    const float2 pe = __ffma2_rn(x.h, yy, neg2(p));
+    const float2 one = make_float2(1.0f, 1.0f);
+    const float2 e = sub2(sub2(sub2(one, p), pe), __ffma2_rn(x.h, yye, __fmul2_rn(x.l, yy)));
+    return quick_two_sum2(y, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), y), e));
 }
-__device__ __forceinline__ df df_sub(float4 a_h, float4 a_l, float4 b_h, float4 b_l, int k) {
-    const float ah = k == 0 ? a_h.x : (k == 1 ? a_h.y : a_h.z);
-    const float al = k == 0 ? a_l.x : (k == 1 ? a_l.y : a_l.z);
-    const float bh = k == 0 ? b_h.x : (k == 1 ? b_h.y : b_h.z);
-    const float bl = k == 0 ? b_l.x : (k == 1 ? b_l.y : b_l.z);
-    const df s = two_sum(ah, -bh);
-    return {s.h, __fadd_rn(s.l, __fsub_rn(al, bl))};  // nearly normalised; not renormalised
-}
-// accumulator: hi part by two_sum, lo parts summed and folded in at the end
-__device__ __forceinline__ void df_acc(float& ah, float& al, df v) {
-    const df s = two_sum(ah, v.h);
+__device__ __forceinline__ void df_acc2(float2& ah, float2& al, df2 v) {
+    const df2 s = two_sum2(ah, v.h);
     ah = s.h;
-    al = __fadd_rn(al, __fadd_rn(s.l, v.l));
+    al = __fadd2_rn(al, __fadd2_rn(s.l, v.l));
 }
 
-template <bool TRAC>
-__global__ void __launch_bounds__(kFarThreads) k_far_df(DevGeom g, const FarItem* __restrict__ items,
-                                                       const float4* __restrict__ src, double* __restrict__ partial) {
+// KIND: 0 single layer -> partial; 1 traction -> partial; 2 both from the same sources in one pass
+// (traction -> partial, single layer -> partial_sl), sharing r, 1/r and r.f between the two kernels.
+template <int KIND>
+__global__ void __launch_bounds__(kFarThreads, 3)
+    k_far_dfx2(DevGeom g, const FarItem* __restrict__ items, const float4* __restrict__ src,
+               double* __restrict__ partial, double* __restrict__ partial_sl) {
+    constexpr bool TRAC = KIND != 0, SL = KIND != 1;
     const FarItem it = items[blockIdx.x];
     if (g.active && !g.active[it.problem]) return;
     __shared__ float4 sph[kFarTile], spl[kFarTile], sfh[kFarTile], sfl[kFarTile];
-    const int ta = it.t0 + threadIdx.x;
-    const bool va = ta < it.t1;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 ph = va ? g.pos32[ta] : z4, pl = va ? g.pos32lo[ta] : z4;
-    float4 nh = z4, nl = z4;
-    if (TRAC && va) {
-        nh = g.nrm32[ta];
-        nl = g.nrm32lo[ta];
+    float4 PH[2], PL[2], NH[2], NL[2];
+    int sid[2], cur[2], end[2];
+    bool val[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int t = it.t0 + threadIdx.x + h * kFarThreads;
+        val[h] = t < it.t1;
+        PH[h] = val[h] ? g.pos32[t] : z4;
+        PL[h] = val[h] ? g.pos32lo[t] : z4;
+        NH[h] = (TRAC && val[h]) ? g.nrm32[t] : z4;
+        NL[h] = (TRAC && val[h]) ? g.nrm32lo[t] : z4;
+        sid[h] = val[h] ? __float_as_int(PH[h].w) : -1;
+        cur[h] = val[h] ? g.nbr_start[sid[h]] : 0;
+        end[h] = val[h] ? g.nbr_start[sid[h] + 1] : 0;
     }
-    const df n0{nh.x, nl.x}, n1{nh.y, nl.y}, n2{nh.z, nl.z};
-    const int sa = va ? __float_as_int(ph.w) : -1;
-    int ca = va ? g.nbr_start[sa] : 0, ea = va ? g.nbr_start[sa + 1] : 0;
-    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f, zh = 0.f, zl = 0.f;
+    const df2 tx{f2(PH[0].x, PH[1].x), f2(PL[0].x, PL[1].x)}, ty{f2(PH[0].y, PH[1].y), f2(PL[0].y, PL[1].y)},
+        tz{f2(PH[0].z, PH[1].z), f2(PL[0].z, PL[1].z)};
+    const df2 n0{f2(NH[0].x, NH[1].x), f2(NL[0].x, NL[1].x)}, n1{f2(NH[0].y, NH[1].y), f2(NL[0].y, NL[1].y)},
+        n2{f2(NH[0].z, NH[1].z), f2(NL[0].z, NL[1].z)};
+    float2 xh = f2(0.f, 0.f), xl = xh, yh = xh, yl = xh, zh = xh, zl = xh;     // traction, or SL for KIND 0
+    float2 sxh = xh, sxl = xh, syh = xh, syl = xh, szh = xh, szl = xh;          // single layer for KIND 2
+    // one source against the two packed targets (mx, my, mz); keep scales the source weight per lane
+    auto pair = [&](const df2& mx, const df2& my, const df2& mz, const float4& qh, const float4& ql,
+                    const float4& fh, const float4& fl, bool masked, float2 keep) {
+        const df2 dx = two_sum2(mx.h, f2(-qh.x, -qh.x));
+        const df2 dy = two_sum2(my.h, f2(-qh.y, -qh.y));
+        const df2 dz = two_sum2(mz.h, f2(-qh.z, -qh.z));
+        const df2 rx{dx.h, __fadd2_rn(dx.l, __fadd2_rn(mx.l, f2(-ql.x, -ql.x)))};
+        const df2 ry{dy.h, __fadd2_rn(dy.l, __fadd2_rn(my.l, f2(-ql.y, -ql.y)))};
+        const df2 rz{dz.h, __fadd2_rn(dz.l, __fadd2_rn(mz.l, f2(-ql.z, -ql.z)))};
+        df2 f0{f2(fh.x, fh.x), f2(fl.x, fl.x)}, f1{f2(fh.y, fh.y), f2(fl.y, fl.y)}, fz{f2(fh.z, fh.z), f2(fl.z, fl.z)};
+        if (masked) {
+            f0 = {__fmul2_rn(f0.h, keep), __fmul2_rn(f0.l, keep)};
+            f1 = {__fmul2_rn(f1.h, keep), __fmul2_rn(f1.l, keep)};
+            fz = {__fmul2_rn(fz.h, keep), __fmul2_rn(fz.l, keep)};
+        }
+        const df2 r2 = df_sqr3_2(rx, ry, rz);
+        const df2 ri = df_rsqrt2(r2);
+        const df2 rf = df_dot3_2(rx, f0, ry, f1, rz, fz);
+        const df2 ri2 = df_mul_u2(ri, ri);
+        const df2 ri3 = df_mul_u2(ri2, ri);
+        if (TRAC) {  // (r.f)(r.n) r / r^5
+            const df2 rn = df_dot3_2(rx, n0, ry, n1, rz, n2);
+            const df2 k5 = df_mul2(df_mul_u2(rf, rn), df_mul_u2(ri3, ri2));
+            df_acc2(xh, xl, df_mul_u2(k5, rx));
+            df_acc2(yh, yl, df_mul_u2(k5, ry));
+            df_acc2(zh, zl, df_mul_u2(k5, rz));
+        }
+        if (SL) {  // f / r + (r.f) r / r^3
+            const df2 k3 = df_mul2(rf, ri3);
+            float2& ah = KIND == 2 ? sxh : xh;
+            float2& al = KIND == 2 ? sxl : xl;
+            float2& bh = KIND == 2 ? syh : yh;
+            float2& bl = KIND == 2 ? syl : yl;
+            float2& ch = KIND == 2 ? szh : zh;
+            float2& cl = KIND == 2 ? szl : zl;
+            df_acc2(ah, al, df_add2(df_mul_u2(f0, ri), df_mul_u2(k3, rx)));
+            df_acc2(bh, bl, df_add2(df_mul_u2(f1, ri), df_mul_u2(k3, ry)));
+            df_acc2(ch, cl, df_add2(df_mul_u2(fz, ri), df_mul_u2(k3, rz)));
+        }
+    };
     for (int s = it.s0; s < it.s1; ++s) {
-        const bool ska = !va || excluded(g.nbr_src, ca, ea, sa, s);
-        if (__syncthreads_and(ska)) continue;
+        bool sk[2];
+        sk[0] = !val[0] || excluded(g.nbr_src, cur[0], end[0], sid[0], s);
+        sk[1] = !val[1] || excluded(g.nbr_src, cur[1], end[1], sid[1], s);
+        if (__syncthreads_and(sk[0] && sk[1])) continue;
+        const bool masked = sk[0] || sk[1];
+        // A lane whose target skips this sphere is moved to a point 1e18 away and its source weight
+        // is zeroed: its terms are exact zeros (r^-5 underflows, no 0*inf at r = 0 on its own sphere).
+        const float2 keep = f2(sk[0] ? 0.f : 1.f, sk[1] ? 0.f : 1.f);
+        const float2 far2 = f2(sk[0] ? 1e18f : 0.f, sk[1] ? 1e18f : 0.f);
+        const df2 mx{__fadd2_rn(tx.h, far2), __fmul2_rn(tx.l, keep)};
+        const df2 my{__fadd2_rn(ty.h, far2), __fmul2_rn(ty.l, keep)};
+        const df2 mz{__fadd2_rn(tz.h, far2), __fmul2_rn(tz.l, keep)};
         const int g0 = g.gidx[s], gl = g.glen[s];
         for (int base = 0; base < gl; base += kFarTile) {
             const int n = min(kFarTile, gl - base);
@@ -325,39 +512,29 @@ __global__ void __launch_bounds__(kFarThreads) k_far_df(DevGeom g, const FarItem
                 sfl[k] = src[2 * (g0 + base + k) + 1];
             }
             __syncthreads();
-            if (!ska) {
-                for (int k = 0; k < n; ++k) {
-                    const float4 qh = sph[k], ql = spl[k], fh = sfh[k], fl = sfl[k];
-                    const df rx = df_sub(ph, pl, qh, ql, 0), ry = df_sub(ph, pl, qh, ql, 1),
-                             rz = df_sub(ph, pl, qh, ql, 2);
-                    const df f0{fh.x, fl.x}, f1{fh.y, fl.y}, f2{fh.z, fl.z};
-                    const df r2 = df_sqr3(rx, ry, rz);
-                    const df ri = df_rsqrt(r2);
-                    const df rf = df_dot3(rx, f0, ry, f1, rz, f2);
-                    if (TRAC) {
-                        const df rn = df_dot3(rx, n0, ry, n1, rz, n2);
-                        const df ri2 = df_mul_u(ri, ri);
-                        const df k5 = df_mul(df_mul_u(rf, rn), df_mul_u(df_mul_u(ri2, ri2), ri));
-                        df_acc(xh, xl, df_mul_u(k5, rx));
-                        df_acc(yh, yl, df_mul_u(k5, ry));
-                        df_acc(zh, zl, df_mul_u(k5, rz));
-                    } else {
-                        const df k3 = df_mul(rf, df_mul_u(df_mul_u(ri, ri), ri));
-                        df_acc(xh, xl, df_add(df_mul_u(f0, ri), df_mul_u(k3, rx)));
-                        df_acc(yh, yl, df_add(df_mul_u(f1, ri), df_mul_u(k3, ry)));
-                        df_acc(zh, zl, df_add(df_mul_u(f2, ri), df_mul_u(k3, rz)));
-                    }
-                }
+            if (!masked) {
+                for (int k = 0; k < n; ++k) pair(tx, ty, tz, sph[k], spl[k], sfh[k], sfl[k], false, keep);
+            } else {
+                for (int k = 0; k < n; ++k) pair(mx, my, mz, sph[k], spl[k], sfh[k], sfl[k], true, keep);
             }
         }
     }
     const Problem pr = g.problems[it.problem];
     const long long mp = pr.p1 - pr.p0;
-    if (va) {
-        double* o = partial + pr.poff + 3LL * mp * it.chunk + 3LL * (ta - pr.p0);
-        o[0] = double(xh) + double(xl);
-        o[1] = double(yh) + double(yl);
-        o[2] = double(zh) + double(zl);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (!val[h]) continue;
+        const long long off = pr.poff + 3LL * mp * it.chunk + 3LL * (it.t0 + threadIdx.x + h * kFarThreads - pr.p0);
+        double* o = partial + off;
+        o[0] = h ? double(xh.y) + double(xl.y) : double(xh.x) + double(xl.x);
+        o[1] = h ? double(yh.y) + double(yl.y) : double(yh.x) + double(yl.x);
+        o[2] = h ? double(zh.y) + double(zl.y) : double(zh.x) + double(zl.x);
+        if (KIND == 2) {
+            double* q = partial_sl + off;
+            q[0] = h ? double(sxh.y) + double(sxl.y) : double(sxh.x) + double(sxl.x);
+            q[1] = h ? double(syh.y) + double(syl.y) : double(syh.x) + double(syl.x);
+            q[2] = h ? double(szh.y) + double(szl.y) : double(szh.x) + double(szl.x);
+        }
     }
 }
 
@@ -420,8 +597,14 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 template <int TPT>
 void launch_far32(const DevGeom& g, const FarItem* items, int nitems, bool trac, const float4* src32, float* partial,
                   cudaStream_t st) {
-    if (trac) k_far32<true, TPT><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
-    else k_far32<false, TPT><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
+    if (TPT == 1) {
+        if (trac) k_far32<true, 1><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
+        else k_far32<false, 1><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
+    } else {
+        constexpr int NPK = TPT / 2 > 0 ? TPT / 2 : 1;
+        if (trac) k_far32x2<true, NPK><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
+        else k_far32x2<false, NPK><<<nitems, kFarThreads, 0, st>>>(g, items, src32, partial);
+    }
 }
 
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
@@ -444,11 +627,13 @@ int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2
     return 1;
 }
 
-int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, bool trac, const float4* src2,
-                        double* partial, cudaStream_t st) {
+int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int kind, const float4* src2,
+                        double* partial, double* partial_sl, cudaStream_t st) {
     if (nitems <= 0) return 0;
-    if (trac) k_far_df<true><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial);
-    else k_far_df<false><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial);
+    // items carry 2 * kFarThreads targets each (two packed targets per thread)
+    if (kind == 2) k_far_dfx2<2><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, partial_sl);
+    else if (kind == 1) k_far_dfx2<1><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, nullptr);
+    else k_far_dfx2<0><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, nullptr);
     return 1;
 }
 

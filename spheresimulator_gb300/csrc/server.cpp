@@ -142,8 +142,8 @@ size_t request_bytes(int n, const int* orders, int restart) {
     const size_t chunks = 16;
     size_t b = 0;
     b += size_t(8) * 3 * M * (restart + 1);  // Krylov basis
-    b += size_t(8) * 3 * M * 12;              // solver and staging vectors
-    b += size_t(12) * 3 * M * chunks;         // far-field partial sums (FP32 + FP64)
+    b += size_t(8) * 3 * M * 15;              // solver and staging vectors
+    b += size_t(20) * 3 * M * chunks;         // far-field partial sums (FP32 + 2 x FP64)
     b += size_t(160) * M;                     // point data (FP64 + FP32 + float-float)
     b += size_t(12) * 2 * coef;               // coefficients (FP32 + FP64)
     b += size_t(12) * setsrc * size_t(n);     // near-field sets (upper bound: every sphere a source)

@@ -107,10 +107,12 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
-// float-float far field (hi/lo float pairs on the FP32 pipe); partial sums in FP64 (the FP64 buffer)
+// float-float far field (hi/lo float pairs on the FP32 pipe); partial sums in FP64 (the FP64 buffer).
+// Items cover 2 * kFarThreads targets. kind: 0 single layer, 1 traction (both into partial),
+// 2 traction into partial and single layer into partial_sl from the same sources in one pass.
 int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2, cudaStream_t st);
-int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, bool trac, const float4* src2,
-                        double* partial, cudaStream_t st);
+int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int kind, const float4* src2,
+                        double* partial, double* partial_sl, cudaStream_t st);
 
 // Per-sphere operator: out += c_id*x + c_self*Self[x] + c_lop*L[x]; coefficients of x written to coef
 // (self_kind: -1 none, 0 single layer, 3 traction principal value).

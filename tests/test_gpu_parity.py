@@ -159,6 +159,8 @@ def test_solve_mob_mixed(oracle):
     st = g.last_stats[0]
     assert st["status"] == 0 and st["relres"] < 1e-10
     assert st["operator_passes_fp32"] > 0
+    # b in FP32, then fused high-precision residual + single-layer passes only where refinement needs them
+    assert 1 <= st["operator_passes_fp64"] <= st["refinements"]
     assert rel(vel, ref["vel"]) < 1e-6
 
 
