@@ -38,6 +38,9 @@ RESTART = 50
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = ("cfg2: 64 spheres a=1, seeded RSA in box 20 (min gap 0.1), p=16 (36992 points), "
             "N(0,1) force/torque, GMRES(50) to 1e-8 relative residual")
+# DRAM bytes (read + write) of one FP32 traction far-field launch on this workload, from an ncu capture
+# (GB300, k_far32<1, 1>: 1,897,472 read, 0 written)
+CFG2_FAR32_DRAM_BYTES = 1897472
 
 
 def dist_init():
@@ -257,7 +260,11 @@ def run_native(args, world, rank, local, dist):
                                          / (ms_mixed.mean() / 1e3), 1),
         "roofline": {"kernel": "far_trac_fp32", "bound": "fp32_simt", "achieved": round(achieved, 3) if achieved else None,
                      "peak": round(f32.value, 3), "unit": "TFLOP/s",
-                     "frac": round(achieved / f32.value, 4) if achieved else None, "traffic": None,
+                     "frac": round(achieved / f32.value, 4) if achieved else None,
+                     "traffic": CFG2_FAR32_DRAM_BYTES,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_far32 launch on this "
+                                       "workload (ncu --set full, bench.py --far-once); algorithmic bytes "
+                                       "(positions, normals, sources once) = 1.8 MB",
                      "peak_source": "FP32 FMA issue rate measured in this run (MEASURED_PEAKS.json has no SIMT entry)",
                      "flops_per_launch": 30.0 * pairs, "pairs_per_launch": pairs,
                      "avg_launch_ms": round(avg_s * 1e3, 5), "launches_in_profiled_solve": k_l,
@@ -538,6 +545,19 @@ def run_reference(args, rank):
             "oracle_solve": {"iterations": r["iters"], "relres": r["relres"]}}
 
 
+def far_once():
+    """One far-field pass of each kernel family on the cfg2 workload, with few launches before them."""
+    from spheresimulator_gb300 import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
+    c = configs.cfg2()
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    x = np.random.default_rng(0).standard_normal(3 * g.n_points)
+    a = g.far_field(x, cTrac=1.0, precision=PREC_MIXED)
+    b = g.far_field(x, cSL=1.0, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
+    d = g.far_field(x, cTrac=1.0, precision=PREC_FP64)
+    print(json.dumps({"far_once": "cfg2", "points": int(g.n_points), "finite": bool(np.isfinite(a).all() and
+                      np.isfinite(b).all() and np.isfinite(d).all())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -556,7 +576,13 @@ def main():
     ap.add_argument("--hbm-budget", type=float, default=0.0, help="cfg5: admission budget in bytes (0: 64 GB)")
     ap.add_argument("--fp64-subset", type=int, default=0,
                     help="cfg5: also serve the requests with at most this many spheres in mixed and plain FP64")
+    ap.add_argument("--far-once", action="store_true",
+                    help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
+                         "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
     args = ap.parse_args()
+    if args.far_once:
+        far_once()
+        return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
     world, rank, local, dist = dist_init()

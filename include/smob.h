@@ -218,6 +218,9 @@ smob_status smob_set_graphs(smob_ctx* ctx, int on);
 /* far-field tile shape chosen by the autotuner at smob_create: FP32 targets per thread (1, 2 or 4),
  * the measured milliseconds of the three variants (0 when the choice came from the process cache) */
 smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* variant_ms, int* from_cache);
+/* override the autotuner's choice (1, 2 or 4 FP32 targets per thread); every variant computes each
+ * pair in the same order, so results change only by FP32 rounding in the sums of skipped sources */
+smob_status smob_set_far_tile(smob_ctx* ctx, int targets_per_thread);
 /* CUDA-event interval on the context's stream: mark records a start event; elapsed records an
  * end event, waits for it and returns the milliseconds since the last mark */
 smob_status smob_timer_mark(smob_ctx* ctx);

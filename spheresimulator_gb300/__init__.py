@@ -115,6 +115,17 @@ class _Context:
         """CUDA graphs for the Arnoldi steps of the solves (on by default)."""
         N.check(self._L.smob_set_graphs(self._h, int(on)))
 
+    def set_far_tile(self, targets_per_thread):
+        """Force the FP32 far-field variant (1, 2 or 4 targets per thread) over the autotuner's choice."""
+        N.check(self._L.smob_set_far_tile(self._h, int(targets_per_thread)))
+
+    def tuning(self):
+        """(targets per thread in use, measured ms of the 1/2/4 variants, whether the choice was cached)"""
+        t, c = ctypes.c_int(), ctypes.c_int()
+        ms = np.zeros(3)
+        N.check(self._L.smob_tuning(self._h, ctypes.byref(t), N.dptr(ms), ctypes.byref(c)))
+        return t.value, ms, bool(c.value)
+
     def profile(self, on=True):
         N.check(self._L.smob_profile_enable(self._h, int(on)))
 

@@ -57,6 +57,25 @@ def test_far_field(oracle, seed):
         assert rel(g.far_field(x, cSL=c_sl, cTrac=c_tr, precision=PREC_FLOAT_FLOAT), ref) < 1e-12
 
 
+def test_far_tile_variants(oracle):
+    """Each FP32 far-field variant (1, 2 or 4 targets per thread, scalar or packed FP32x2) matches the
+    oracle; forcing one replaces the autotuner's choice."""
+    cfg = cluster(3, n=7, p=8)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    x = np.random.default_rng(3).standard_normal(3 * g.n_points)
+    ref = o.far_traction(x, 1.0, excl_near=True) + o.far_sl(x, 0.5, excl_near=True)
+    outs = []
+    for tpt in (1, 2, 4):
+        g.set_far_tile(tpt)
+        assert g.tuning()[0] == tpt
+        outs.append(g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED))
+        assert rel(outs[-1], ref) < 2e-5
+    assert rel(outs[1], outs[2]) < 1e-6
+    with pytest.raises(SmobError):
+        g.set_far_tile(3)
+
+
 def test_transforms(oracle):
     cfg = cluster(2, n=3, p=9)
     g = make(cfg)
