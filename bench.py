@@ -545,6 +545,52 @@ def run_reference(args, rank):
             "oracle_solve": {"iterations": r["iters"], "relres": r["relres"]}}
 
 
+def run_multi(args, world, rank, local, dist):
+    """Several right-hand sides on the cfg2 geometry (the columns SphereSTKMobMat::apply solves one
+    by one): K columns in one smob_solve_mob_multi call against K smob_solve_mob calls, host buffers
+    in and out (both timed end to end on the host clock; the calls are synchronous)."""
+    from spheresimulator_gb300 import PREC_MIXED, SphereSTKMobMat, configs
+    cfg = configs.cfg2()
+    mob = SphereSTKMobMat(cfg["centers"], cfg["radii"], cfg["orders"], device=local)
+    k = args.multi
+    F = np.random.default_rng(7).standard_normal((k, 6 * mob.n_spheres))
+    kw = dict(tol=TOL, restart=RESTART, max_iters=1000, precision=PREC_MIXED)
+    auto_tile = mob.tuning()[0]
+
+    def singles():
+        return np.stack([mob.solveMob(F[j], **kw) for j in range(k)])
+
+    for _ in range(max(1, args.warmup)):
+        mob.solveMobMulti(F, **kw)
+        singles()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vm = mob.solveMobMulti(F, **kw)
+    t_multi = allmax(dist, time.perf_counter() - t0)
+    its = [s["iterations"] for s in mob.last_stats]
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vs = singles()
+    t_single = allmax(dist, time.perf_counter() - t0)
+    mob.set_far_tile(1)
+    bitwise = bool(np.array_equal(vm, singles()))
+    err = float(np.linalg.norm(vm - vs) / np.linalg.norm(vs))
+    if rank != 0:
+        return None
+    return {"metric": "mobility solves/s, K right-hand sides on one geometry (cfg2, mixed, 1e-8)",
+            "value": round(world * k * args.steps / t_multi, 4), "unit": "columns/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "dtype": "f32 operator + f64 refinement (mixed)", "data": "synthetic (cfg2 geometry, N(0,1) columns)",
+            "config": {"workload": WORKLOAD, "columns": k, "timing": "host clock around synchronous host-buffer calls"},
+            "ms_per_step": round(1e3 * t_multi / args.steps, 3),
+            "single_solves": {"columns_per_s": round(world * k * args.steps / t_single, 4),
+                              "ms_per_k_columns": round(1e3 * t_single / args.steps, 3), "far_tile": auto_tile},
+            "speedup_vs_single_solves": round(t_single / t_multi, 3),
+            "iterations_per_column": its, "rel_diff_vs_single_autotuned": err,
+            "bitwise_equal_to_single_solves_tile1": bitwise}
+
+
 def far_once():
     """One far-field pass of each kernel family on the cfg2 workload, with few launches before them."""
     from spheresimulator_gb300 import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
@@ -576,6 +622,9 @@ def main():
     ap.add_argument("--hbm-budget", type=float, default=0.0, help="cfg5: admission budget in bytes (0: 64 GB)")
     ap.add_argument("--fp64-subset", type=int, default=0,
                     help="cfg5: also serve the requests with at most this many spheres in mixed and plain FP64")
+    ap.add_argument("--multi", type=int, default=0,
+                    help="cfg2: solve this many right-hand sides together (smob_solve_mob_multi) against as "
+                         "many single solves, and print that line instead of the headline")
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
@@ -588,6 +637,8 @@ def main():
     world, rank, local, dist = dist_init()
     if args.impl == "reference":
         line = run_reference(args, rank)
+    elif args.multi > 0:
+        line = run_multi(args, world, rank, local, dist)
     elif args.config == "cfg5":
         line = run_serving(args, world, rank, local, dist)
     elif args.config != "cfg2":

@@ -149,9 +149,20 @@ smob_status smob_solve_mob(smob_ctx* ctx, const double* force6n, double* vel6n, 
 /* the same with device pointers (inputs already resident; no host copies) */
 smob_status smob_solve_mob_device(smob_ctx* ctx, const double* d_force6n, double* d_vel6n, double* d_density3m,
                                   const smob_solve_opts* opts, smob_problem_stats* stats);
-/* Y = alpha * M X + beta * Y for the mobility matrix M (6N x 6N), n_cols columns (SphereSTKMobMat::apply) */
+/* Y = alpha * M X + beta * Y for the mobility matrix M (6N x 6N), n_cols columns (SphereSTKMobMat::apply,
+ * BIE/SphereSTKMobMat.cpp:98-144); X and Y are [n_cols][6N]. On a one-problem context the columns
+ * are solved together as by smob_solve_mob_multi. */
 smob_status smob_mob_apply(smob_ctx* ctx, const double* X, double* Y, int n_cols, double alpha, double beta,
                            const smob_solve_opts* opts);
+/* Several right-hand sides on one geometry: the columns SphereSTKMobMat::apply solves one after
+ * another with solveMob (BIE/SphereSTKMobMat.cpp:129-143), solved together, each with its own
+ * Krylov space and stopping test. force6n [n_rhs][6N], vel6n [n_rhs][6N], density3m [n_rhs][3M] or
+ * NULL, stats [n_rhs] or NULL. The FP32 far field evaluates each pair's geometry once for all
+ * columns; every column's result equals bit for bit a smob_solve_mob of that column alone with
+ * smob_set_far_tile(ctx, 1). The context must hold one problem. Internal copies of the geometry
+ * are kept on the context per column count (at most 4 counts). */
+smob_status smob_solve_mob_multi(smob_ctx* ctx, int n_rhs, const double* force6n, double* vel6n,
+                                 double* density3m, const smob_solve_opts* opts, smob_problem_stats* stats);
 
 /* ---- serving: a request loop with continuous batching (no counterpart in the reference, which
  * solves one system per time step inside SphereSystem::resolveCollision, SRC/SphereSystem.cpp:403-479).

@@ -323,6 +323,25 @@ class SphereSTKMobMat(SphereSTKSHOperator):
         self.last_stats = [s.as_dict() for s in stats]
         return vel
 
+    def solveMobMulti(self, forces, tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False,
+                      inner_tol=0.0, want_density=False, raise_on_not_converged=True):
+        """forces [K][6N] -> velocities [K][6N]: K right-hand sides on this geometry solved together
+        (the columns SphereSTKMobMat::apply solves one by one, BIE/SphereSTKMobMat.cpp:129-143)."""
+        F = np.ascontiguousarray(N.f64(forces).reshape(-1, 6 * self.n_spheres))
+        k = F.shape[0]
+        vel = np.zeros_like(F)
+        dens = np.zeros((k, 3 * self.n_points)) if want_density else None
+        stats = (N.ProblemStats * k)()
+        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol)
+        code = self._L.smob_solve_mob_multi(self._h, k, N.dptr(F), N.dptr(vel), N.dptr(dens), ctypes.byref(opts),
+                                            stats)
+        allow = () if raise_on_not_converged else (N.SMOB_ERR_NOT_CONVERGED,)
+        N.check(code, allow)
+        self.last_stats = [s.as_dict() for s in stats]
+        if want_density:
+            self._density = dens
+        return vel
+
     def getDensitySolution(self):
         """rho + mu from the last solve (BIE/SphereSTKMobMat.hpp:76)."""
         return self._density

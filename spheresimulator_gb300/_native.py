@@ -108,6 +108,8 @@ def lib():
         "smob_solve_mob_device": (S, [_VP, _VP, _VP, _VP, ctypes.POINTER(SolveOpts), ctypes.POINTER(ProblemStats)]),
         "smob_mob_apply": (S, [_VP, _DP, _DP, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                ctypes.POINTER(SolveOpts)]),
+        "smob_solve_mob_multi": (S, [_VP, ctypes.c_int, _DP, _DP, _DP, ctypes.POINTER(SolveOpts),
+                                     ctypes.POINTER(ProblemStats)]),
         "smob_device_alloc": (S, [_VP, ctypes.c_size_t, ctypes.POINTER(_VP)]),
         "smob_device_free": (S, [_VP, _VP]),
         "smob_memcpy_h2d": (S, [_VP, _VP, _VP, ctypes.c_size_t]),

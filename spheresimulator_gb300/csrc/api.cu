@@ -133,12 +133,18 @@ struct smob_ctx {
     bool tune_cached = false;
     long long partial32 = 0, partial64 = 0;
     std::vector<VecChunk> chunks;
+    // several right-hand sides: this context holds nrep copies of one problem (rep_M points each),
+    // replica 0's FP32 far-field items drive the shared-geometry kernel
+    int nrep = 1, rep_M = 0;
+    std::vector<FarItem> items_rep;
+    std::map<int, smob_ctx*> multi;  // replicated children of a one-problem context, by column count
 
     // device geometry
     DBuf d_center, d_radius, d_quat, d_order, d_gidx, d_glen, d_coff, d_prob, d_coords, d_norms, d_weights, d_sid;
     DBuf d_pos32, d_nrm32, d_pos32lo, d_nrm32lo, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_nbr_precise, d_near_slot,
         d_slot_sphere, d_problems, d_tabs, d_srcdf;
-    DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_items_df, d_chunks;
+    DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_items_df, d_chunks,
+        d_items_rep;
     DBuf d_active;
     // operator workspace
     DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
@@ -192,6 +198,7 @@ struct smob_ctx {
     }
 
     ~smob_ctx() {
+        for (auto& kv : multi) smob_destroy(kv.second);
         for (auto& p : pending) {
             cudaEventDestroy(p.a);
             cudaEventDestroy(p.b);
@@ -765,8 +772,13 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
             }
             ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
-            check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                             c->d_src64.as<double4>(), partial, c->st, c->tpt));
+            if (fp32 && c->nrep > 1)
+                check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
+                                                     c->rep_M, tr, c->d_src32.as<float4>(), static_cast<float*>(partial),
+                                                     c->st));
+            else
+                check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                                 c->d_src64.as<double4>(), partial, c->st, c->tpt));
         }
         {
             ProfScope ps(c, "far_reduce");
@@ -1528,11 +1540,79 @@ smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double
     });
 }
 
+}  // extern "C"
+
+namespace {
+// A child context holding k copies of c's one problem (replica r = problem r), cached per k on c.
+// The copies share c's geometry exactly, so the far field can evaluate each pair once for all of them.
+smob_ctx* replicated(smob_ctx* c, int k) {
+    auto it = c->multi.find(k);
+    if (it != c->multi.end()) return it->second;
+    if (c->multi.size() >= 4) {  // bound the cache for callers that cycle through many column counts
+        for (auto& kv : c->multi) smob_destroy(kv.second);
+        c->multi.clear();
+    }
+    const int N = c->N;
+    std::vector<double> centers, radii, quats;
+    std::vector<int> orders, problem;
+    for (int r = 0; r < k; ++r) {
+        centers.insert(centers.end(), c->centers.begin(), c->centers.end());
+        radii.insert(radii.end(), c->radii.begin(), c->radii.end());
+        quats.insert(quats.end(), c->quats.begin(), c->quats.end());
+        orders.insert(orders.end(), c->orders.begin(), c->orders.end());
+        problem.insert(problem.end(), N, r);
+    }
+    const smob_geometry geo{k * N, centers.data(), radii.data(), quats.data(), orders.data(), problem.data(),
+                            c->viscosity};
+    std::unique_ptr<smob_ctx> r(new smob_ctx);
+    r->device = c->device;
+    CUDA_OK(cudaSetDevice(c->device));
+    CUDA_OK(cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking));
+    r->sh.st = r->st;
+    AllocStreamScope scope(r->st);
+    build_context(r.get(), &geo);
+    r->nrep = k;
+    r->rep_M = c->M;
+    for (const FarItem& f : r->items_tpt[0])
+        if (f.problem == 0) r->items_rep.push_back(f);
+    r->d_items_rep.upload(r->items_rep);
+    r->use_graphs = c->use_graphs;
+    CUDA_OK(cudaStreamSynchronize(r->st));
+    c->multi[k] = r.get();
+    return r.release();
+}
+}  // namespace
+
+extern "C" {
+
+smob_status smob_solve_mob_multi(smob_ctx* c, int n_rhs, const double* force, double* vel, double* density,
+                                 const smob_solve_opts* o, smob_problem_stats* stats) {
+    return guarded([&]() -> smob_status {
+        need(c && force && vel && n_rhs >= 1, "invalid argument");
+        need(c->P == 1 && c->nrep == 1, "several right-hand sides need a context with one problem");
+        check_opts(o);
+        if (n_rhs == 1) return smob_solve_mob(c, force, vel, density, o, stats);
+        set_device(c);
+        AllocStreamScope scope(c->st);
+        smob_ctx* r = replicated(c, n_rhs);
+        return smob_solve_mob(r, force, vel, density, o, stats);
+    });
+}
+
 smob_status smob_mob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, double alpha, double beta,
                            const smob_solve_opts* o) {
     return guarded([&]() -> smob_status {
         need(c && X && Y && n_cols >= 1, "invalid argument");
         const size_t n6 = 6 * (size_t)c->N;
+        if (n_cols > 1 && c->P == 1) {
+            // all columns in one solve, each with its own Krylov space (SphereSTKMobMat.cpp:129-143
+            // solves them one after another)
+            std::vector<double> v(n6 * n_cols);
+            const smob_status s = smob_solve_mob_multi(c, n_cols, X, v.data(), nullptr, o, nullptr);
+            if (s != SMOB_OK && s != SMOB_ERR_NOT_CONVERGED) return s;
+            for (size_t i = 0; i < n6 * n_cols; ++i) Y[i] = (beta == 0.0 ? 0.0 : beta * Y[i]) + alpha * v[i];
+            return s;
+        }
         std::vector<double> v(n6);
         smob_status worst = SMOB_OK;
         for (int col = 0; col < n_cols; ++col) {

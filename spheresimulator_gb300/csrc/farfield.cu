@@ -43,7 +43,7 @@ __device__ __forceinline__ void pair_sl32(const float4& t, const float4& s, cons
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
     const float ri = rsqrtf(r2);
     const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
-    const float k = rf * ri * ri * ri;
+    const float k = rf * (ri * ri * ri);
     ax = fmaf(f.x, ri, fmaf(k, rx, ax));
     ay = fmaf(f.y, ri, fmaf(k, ry, ay));
     az = fmaf(f.z, ri, fmaf(k, rz, az));
@@ -294,6 +294,96 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
         o[0] = ax[u];
         o[1] = ay[u];
         o[2] = az[u];
+    }
+}
+
+// ---------------------------------------------------------------- several right-hand sides, one geometry
+// The context holds nrep identical copies (replicas) of one problem, replica r in problem r with
+// points [r*rep_M, (r+1)*rep_M). Work items are those of replica 0; blockIdx.y selects KB replicas.
+// Per pair the geometry (r, 1/r, r^-5, r.n) is computed once and applied to the KB densities, so
+// a pair-RHS costs 8 FP32 operations + 1 shared load instead of 20 + 2. Per RHS the arithmetic and
+// the summation order are those of k_far32<TRAC, 1>, so every replica's sums equal bit for bit what
+// the one-target-per-thread kernel gives for that density alone.
+template <bool TRAC, int KB>
+__global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarItem* __restrict__ items, int nrep,
+                                                          int rep_M, const float4* __restrict__ src,
+                                                          float* __restrict__ partial) {
+    const FarItem it = items[blockIdx.x];
+    const int r0 = blockIdx.y * KB;
+    const int nr = min(KB, nrep - r0);
+    bool any = g.active == nullptr;
+    for (int r = 0; r < nr && !any; ++r) any = g.active[r0 + r] != 0;
+    if (!any) return;
+    __shared__ float4 sp[kRepTile];
+    __shared__ float4 sf[KB][kRepTile];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int t = it.t0 + threadIdx.x;
+    const bool va = t < it.t1;
+    const float4 tp = va ? g.pos32[t] : z4;
+    const float4 tn = (TRAC && va) ? g.nrm32[t] : z4;
+    const int sa = va ? __float_as_int(tp.w) : -1;
+    int ca = va ? g.nbr_start[sa] : 0;
+    const int ea = va ? g.nbr_start[sa + 1] : 0;
+    float ax[KB], ay[KB], az[KB];
+#pragma unroll
+    for (int r = 0; r < KB; ++r) ax[r] = ay[r] = az[r] = 0.f;
+    for (int s = it.s0; s < it.s1; ++s) {
+        const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s);
+        if (__syncthreads_and(sk)) continue;
+        const int g0 = g.gidx[s], gl = g.glen[s];
+        for (int base = 0; base < gl; base += kRepTile) {
+            const int n = min(kRepTile, gl - base);
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += kFarThreads) {
+                sp[k] = g.pos32[g0 + base + k];
+#pragma unroll
+                for (int r = 0; r < KB; ++r)
+                    sf[r][k] = r < nr ? src[(long long)(r0 + r) * rep_M + g0 + base + k] : z4;
+            }
+            __syncthreads();
+            if (sk) continue;
+            for (int k = 0; k < n; ++k) {
+                const float4 q = sp[k];
+                const float rx = tp.x - q.x, ry = tp.y - q.y, rz = tp.z - q.z;
+                const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                const float ri = rsqrtf(r2);
+                if (TRAC) {
+                    const float ri2 = ri * ri;
+                    const float ri5 = ri2 * ri2 * ri;
+                    const float rn = fmaf(rx, tn.x, fmaf(ry, tn.y, rz * tn.z));
+#pragma unroll
+                    for (int r = 0; r < KB; ++r) {
+                        const float4 f = sf[r][k];
+                        const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
+                        const float kk = (rf * rn) * ri5;
+                        ax[r] = fmaf(kk, rx, ax[r]);
+                        ay[r] = fmaf(kk, ry, ay[r]);
+                        az[r] = fmaf(kk, rz, az[r]);
+                    }
+                } else {
+                    const float ri3 = ri * ri * ri;
+#pragma unroll
+                    for (int r = 0; r < KB; ++r) {
+                        const float4 f = sf[r][k];
+                        const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
+                        const float kk = rf * ri3;
+                        ax[r] = fmaf(f.x, ri, fmaf(kk, rx, ax[r]));
+                        ay[r] = fmaf(f.y, ri, fmaf(kk, ry, ay[r]));
+                        az[r] = fmaf(f.z, ri, fmaf(kk, rz, az[r]));
+                    }
+                }
+            }
+        }
+    }
+    if (!va) return;
+#pragma unroll
+    for (int r = 0; r < KB; ++r) {
+        if (r >= nr) break;
+        const Problem pr = g.problems[r0 + r];
+        float* o = partial + pr.poff + 3LL * (pr.p1 - pr.p0) * it.chunk + 3LL * t;
+        o[0] = ax[r];
+        o[1] = ay[r];
+        o[2] = az[r];
     }
 }
 
@@ -619,6 +709,23 @@ int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool tr
         if (trac) k_far64<true><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
         else k_far64<false><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
     }
+    return 1;
+}
+
+template <int KB>
+void launch_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,
+                const float4* src32, float* partial, cudaStream_t st) {
+    const dim3 grid(nitems, (nrep + KB - 1) / KB);
+    if (trac) k_far32_rep<true, KB><<<grid, kFarThreads, 0, st>>>(g, items, nrep, rep_M, src32, partial);
+    else k_far32_rep<false, KB><<<grid, kFarThreads, 0, st>>>(g, items, nrep, rep_M, src32, partial);
+}
+
+int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,
+                         const float4* src32, float* partial, cudaStream_t st) {
+    if (nitems <= 0 || nrep <= 0) return 0;
+    if (nrep <= 2) launch_rep<2>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
+    else if (nrep <= 4) launch_rep<4>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
+    else launch_rep<8>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
     return 1;
 }
 

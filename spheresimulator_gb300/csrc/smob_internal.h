@@ -23,6 +23,7 @@ constexpr int kFarTargets32 = 256;       // targets per FP32 far-field work item
 constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
 constexpr int kFarTile = 256;            // sources staged per shared-memory tile (FP64 / float-float)
 constexpr int kFarTile32 = 640;          // FP32 tile: a whole p <= 16 sphere (578 points) in one round
+constexpr int kRepTile = 256;            // several-RHS FP32 tile (positions + up to 8 source columns)
 constexpr int kSphereThreads = 256;      // per-sphere transform CTA
 constexpr int kNearThreads = 128;        // near-field CTA (one target point per thread)
 constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
@@ -107,6 +108,10 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
+// FP32 far field of nrep replicas of one problem (replica r = problem r, points [r*rep_M, (r+1)*rep_M)):
+// items are replica 0's (kFarThreads targets each); each pair's geometry serves all replicas
+int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,
+                         const float4* src32, float* partial, cudaStream_t st);
 // float-float far field (hi/lo float pairs on the FP32 pipe); partial sums in FP64 (the FP64 buffer).
 // Items cover 2 * kFarThreads targets. kind: 0 single layer, 1 traction (both into partial),
 // 2 traction into partial and single layer into partial_sl from the same sources in one pass.
