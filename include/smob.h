@@ -154,6 +154,34 @@ smob_status smob_solve_mob_device(smob_ctx* ctx, const double* d_force6n, double
  * are solved together as by smob_solve_mob_multi. */
 smob_status smob_mob_apply(smob_ctx* ctx, const double* X, double* Y, int n_cols, double alpha, double beta,
                            const smob_solve_opts* opts);
+/* ---- time stepping: the geometry update between mobility solves of a time loop
+ * (SphereSystem::moveEuler -> Sphere::stepEuler, SRC/SphereSystem.cpp:386-398, Sphere/Sphere.cpp:367-373).
+ * centre += v dt; orientation rotated by omega dt (rotation by |omega| dt about omega, composed on the
+ * left, normalised). The context is rebuilt in place for the new geometry: grid points, normals and the
+ * far-field copies on the device, near pairs and their metadata on the host (O(N) data). The previous
+ * solution stays as the warm start of the next solve (smob_solve_opts.warm_start, SphereSTKMobMat.cpp:222).
+ * vel6n: [N][6] (v, omega) as the solve returns it. Spheres of one problem that would overlap give
+ * SMOB_ERR_ARG and leave the context unchanged. Every kernel result after an update equals, bit for
+ * bit, that of a context created from the updated geometry. */
+smob_status smob_step_euler(smob_ctx* ctx, const double* vel6n, double dt);
+/* the same with the velocities in device memory (e.g. the output of smob_solve_mob_device) */
+smob_status smob_step_euler_device(smob_ctx* ctx, const double* d_vel6n, double dt);
+/* new centres [3N] and orientations [4N] (NULL: unchanged) for the same spheres, rebuilt as above */
+smob_status smob_set_geometry(smob_ctx* ctx, const double* centers, const double* quats);
+/* current centres [3N] and orientations [4N] (either may be NULL) */
+smob_status smob_get_geometry(const smob_ctx* ctx, double* centers, double* quats);
+
+/* ---- output files in the reference's formats
+ * A density (3M host values, e.g. getDensitySolution) on every sphere's grid with both poles added,
+ * one VTK XML piece per sphere (Sphere::writeVTU / writePVTU, Sphere/Sphere.cpp:322-365; Shexp::writeVTU,
+ * Sphere/Shexp.cpp:96-204): <prefix>Sphere_<name>_r0_<postfix>.vtu and <prefix>Sphere_<name>_<postfix>.pvtu.
+ * Pole values are the density's expansion at theta = 1e-6 and pi - 1e-6 (weight 0 there). */
+smob_status smob_write_vtu(smob_ctx* ctx, const char* prefix, const char* postfix, const char* name,
+                           const double* density3m);
+/* sphere centres and radii as XYZ (SphereSystem::writeXYZ, SRC/SphereSystem.cpp:158-179); gids: N ids
+ * or NULL for 0..N-1 */
+smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, double time);
+
 /* Several right-hand sides on one geometry: the columns SphereSTKMobMat::apply solves one after
  * another with solveMob (BIE/SphereSTKMobMat.cpp:129-143), solved together, each with its own
  * Krylov space and stopping test. force6n [n_rhs][6N], vel6n [n_rhs][6N], density3m [n_rhs][3M] or

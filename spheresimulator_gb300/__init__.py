@@ -79,6 +79,51 @@ class _Context:
     def __exit__(self, *a):
         self.close()
 
+    # ---- time stepping (Sphere::stepEuler, Sphere/Sphere.cpp:367-373): the context is rebuilt in place
+    def _refresh(self):
+        c = np.zeros((self.n_spheres, 3))
+        q = np.zeros((self.n_spheres, 4))
+        N.check(self._L.smob_get_geometry(self._h, N.dptr(c), N.dptr(q)))
+        self.centers, self.quats = c, q
+        nnp = ctypes.c_int()
+        N.check(self._L.smob_get_sizes(self._h, None, None, None, ctypes.byref(nnp)))
+        self.n_near_pairs = nnp.value
+
+    def geometry(self):
+        """(centres [N,3], unit quaternions [N,4]) of the current geometry."""
+        return self.centers.copy(), self.quats.copy()
+
+    def step_euler(self, vel, dt):
+        """Advance every sphere by its velocity/angular velocity (6N, as solveMob returns) over dt."""
+        v = N.f64(vel).reshape(-1)
+        if v.shape[0] != 6 * self.n_spheres:
+            raise ValueError("expected 6N velocities")
+        N.check(self._L.smob_step_euler(self._h, N.dptr(v), float(dt)))
+        self._refresh()
+
+    def set_geometry(self, centers, quats=None):
+        """New centres (and orientations) for the same spheres."""
+        c = N.f64(centers).reshape(-1)
+        q = None if quats is None else N.f64(quats).reshape(-1)
+        if c.shape[0] != 3 * self.n_spheres or (q is not None and q.shape[0] != 4 * self.n_spheres):
+            raise ValueError("expected 3N centres and 4N quaternions")
+        N.check(self._L.smob_set_geometry(self._h, N.dptr(c), N.dptr(q)))
+        self._refresh()
+
+    # ---- output files (Sphere::writeVTU/writePVTU, SphereSystem::writeXYZ)
+    def writeVTU(self, prefix, postfix, density, name="stkmob"):
+        """Density (3M) on every sphere's grid with poles: <prefix>Sphere_<name>_r0_<postfix>.vtu + .pvtu."""
+        d = N.f64(density).reshape(-1)
+        if d.shape[0] != 3 * self.n_points:
+            raise ValueError("expected 3M density values")
+        N.check(self._L.smob_write_vtu(self._h, str(prefix).encode(), str(postfix).encode(), str(name).encode(),
+                                       N.dptr(d)))
+
+    def writeXYZ(self, path, time=0.0, gids=None):
+        """Sphere centres and radii, one 'S gid radius x y z' line per sphere."""
+        g = None if gids is None else N.i32(gids).reshape(-1)
+        N.check(self._L.smob_write_xyz(self._h, str(path).encode(), N.iptr(g), float(time)))
+
     # grid getters (SphereSTKSHOperator.hpp:218-223)
     def _grid(self):
         c = np.zeros((self.n_points, 3))

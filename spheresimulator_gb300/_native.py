@@ -110,6 +110,12 @@ def lib():
                                ctypes.POINTER(SolveOpts)]),
         "smob_solve_mob_multi": (S, [_VP, ctypes.c_int, _DP, _DP, _DP, ctypes.POINTER(SolveOpts),
                                      ctypes.POINTER(ProblemStats)]),
+        "smob_write_vtu": (S, [_VP, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _DP]),
+        "smob_write_xyz": (S, [_VP, ctypes.c_char_p, _IP, ctypes.c_double]),
+        "smob_step_euler": (S, [_VP, _DP, ctypes.c_double]),
+        "smob_step_euler_device": (S, [_VP, _VP, ctypes.c_double]),
+        "smob_set_geometry": (S, [_VP, _DP, _DP]),
+        "smob_get_geometry": (S, [_VP, _DP, _DP]),
         "smob_device_alloc": (S, [_VP, ctypes.c_size_t, ctypes.POINTER(_VP)]),
         "smob_device_free": (S, [_VP, _VP]),
         "smob_memcpy_h2d": (S, [_VP, _VP, _VP, ctypes.c_size_t]),

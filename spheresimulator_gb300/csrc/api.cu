@@ -118,11 +118,15 @@ struct smob_ctx {
     cudaStream_t st = nullptr;
     int N = 0, M = 0, P = 0, pmax = 0;
     double viscosity = 1.0;
-    std::vector<double> centers, radii, quats, coords, norms, weights;
+    std::vector<double> centers, radii, quats, weights;
+    mutable std::vector<double> coords, norms;  // host copies, refreshed on demand after a geometry update
     std::vector<int> orders, prob, gidx, glen, coff, sid;
     std::vector<Problem> problems;
     std::vector<int> nbr_start, nbr_src, near_src_slot, slot_sphere;
     std::vector<unsigned char> nbr_precise;
+    std::vector<double> org;         // per-problem origin of the relative (far-field) coordinates
+    std::vector<char> map_orders;    // orders whose near maps are on the device
+    mutable bool host_grid_stale = false;  // coords/norms changed on the device (geometry update)
     int n_precise = 0;
     int ncoef_total = 0;  // complex numbers
     long long set_stride_trac = 0, set_stride_sl = 0;
@@ -142,7 +146,7 @@ struct smob_ctx {
     // device geometry
     DBuf d_center, d_radius, d_quat, d_order, d_gidx, d_glen, d_coff, d_prob, d_coords, d_norms, d_weights, d_sid;
     DBuf d_pos32, d_nrm32, d_pos32lo, d_nrm32lo, d_pos64, d_nrm64, d_nbr_start, d_nbr_src, d_nbr_precise, d_near_slot,
-        d_slot_sphere, d_problems, d_tabs, d_srcdf;
+        d_slot_sphere, d_problems, d_tabs, d_srcdf, d_org;
     DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_items_df, d_chunks,
         d_items_rep;
     DBuf d_active;
@@ -252,17 +256,73 @@ void check_launch(smob_ctx* c, int n) {
     if (e != cudaSuccess) throw SmobError(SMOB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
 }
 
-inline void qrot_h(const double* q, const double* v, double* o) {
-    const double w = q[0], x = q[1], y = q[2], z = q[3];
-    const double tx = 2 * (y * v[2] - z * v[1]);
-    const double ty = 2 * (z * v[0] - x * v[2]);
-    const double tz = 2 * (x * v[1] - y * v[0]);
-    o[0] = v[0] + w * tx + (y * tz - z * ty);
-    o[1] = v[1] + w * ty + (z * tx - x * tz);
-    o[2] = v[2] + w * tz + (x * ty - y * tx);
+// unit quaternion of sphere i from a caller's orientation: normalised, except that one already of
+// unit norm (to 1e-15) is kept bit for bit, so a geometry read back and passed in again is reproduced
+void unit_quat(const double* q, double* out, int i) {
+    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    const double nq = std::sqrt(n2);
+    if (!(nq > 0) || !std::isfinite(nq))
+        throw SmobError(SMOB_ERR_ARG, "quaternion of sphere " + std::to_string(i) + " is zero or not finite");
+    for (int k = 0; k < 4; ++k) out[k] = std::fabs(n2 - 1.0) <= 1e-15 ? q[k] : q[k] / nq;
 }
 
 // ---------------------------------------------------------------- context set-up
+// spheres of one problem must not overlap or touch (centres in `centers`, radii of the context)
+void check_overlap(const smob_ctx* c, const std::vector<double>& centers) {
+    for (const auto& pr : c->problems)
+        for (int t = pr.s0; t < pr.s1; ++t)
+            for (int s = t + 1; s < pr.s1; ++s) {
+                double r2 = 0;
+                for (int k = 0; k < 3; ++k) {
+                    const double d = centers[3 * s + k] - centers[3 * t + k];
+                    r2 += d * d;
+                }
+                if (std::sqrt(r2) <= c->radii[s] + c->radii[t])
+                    throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(s) +
+                                                      " overlap or touch");
+            }
+}
+
+// near pairs (MPI/NearInteraction.txx:430-447; Rad = 1.5*radius, SphereSTKSHOperator.cpp:547),
+// within each problem, sorted by target then source; near-singular flags; near-source slots
+void build_near(smob_ctx* c) {
+    const int N = c->N;
+    c->nbr_start.assign(N + 1, 0);
+    c->nbr_src.clear();
+    c->nbr_precise.clear();
+    for (const auto& pr : c->problems)
+        for (int t = pr.s0; t < pr.s1; ++t) {
+            for (int s = pr.s0; s < pr.s1; ++s) {
+                double r2 = 0;
+                for (int k = 0; k < 3; ++k) {
+                    const double d = c->centers[3 * s + k] - c->centers[3 * t + k];
+                    r2 += d * d;
+                }
+                const double Rn = 1.5 * c->radii[s] + 1.5 * c->radii[t];
+                if (r2 > 0 && r2 < Rn * Rn) {
+                    c->nbr_src.push_back(s);
+                    const double gap = std::sqrt(r2) - c->radii[s] - c->radii[t];
+                    c->nbr_precise.push_back(gap < 0.1 * std::min(c->radii[s], c->radii[t]) ? 1 : 0);
+                }
+            }
+            c->nbr_start[t + 1] = (int)c->nbr_src.size();
+        }
+    c->near_src_slot.assign(N, -1);
+    c->slot_sphere.clear();
+    for (int s : c->nbr_src)
+        if (c->near_src_slot[s] < 0) {
+            c->near_src_slot[s] = (int)c->slot_sphere.size();
+            c->slot_sphere.push_back(s);
+        }
+    std::sort(c->slot_sphere.begin(), c->slot_sphere.end());
+    for (size_t k = 0; k < c->slot_sphere.size(); ++k) c->near_src_slot[c->slot_sphere[k]] = (int)k;
+}
+
+void problem_origins(smob_ctx* c);
+void upload_near(smob_ctx* c);
+void build_tables(smob_ctx* c);
+void bind_geom(smob_ctx* c);
+
 void build_context(smob_ctx* c, const smob_geometry* geo) {
     const int N = geo->n_spheres;
     c->N = N;
@@ -273,10 +333,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->quats.resize(4 * N);
     for (int i = 0; i < N; ++i) {
         if (geo->quats) {
-            const double* q = geo->quats + 4 * i;
-            const double nq = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-            if (!(nq > 0) || !std::isfinite(nq)) throw SmobError(SMOB_ERR_ARG, "quaternion of sphere " + std::to_string(i) + " is zero or not finite");
-            for (int k = 0; k < 4; ++k) c->quats[4 * i + k] = q[k] / nq;
+            unit_quat(geo->quats + 4 * i, &c->quats[4 * i], i);
         } else {
             c->quats[4 * i] = 1;
             c->quats[4 * i + 1] = c->quats[4 * i + 2] = c->quats[4 * i + 3] = 0;
@@ -316,8 +373,11 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     }
     c->M = off;
     c->ncoef_total = coffs;
+    // grid points and normals are built on the device (launch_regrid, below) from the centres and
+    // orientations, at creation and after every geometry update alike; the host copies follow on demand
     c->coords.resize(3 * off);
     c->norms.resize(3 * off);
+    c->host_grid_stale = true;
     c->weights.resize(off);
     c->sid.resize(off);
     for (int i = 0; i < N; ++i) {
@@ -326,13 +386,6 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
         for (int j = 0; j < T.nt; ++j)
             for (int k = 0; k < T.nphi; ++k) {
                 const int id = c->gidx[i] + j * T.nphi + k;
-                const double v[3] = {T.st[j] * T.cph[k], T.st[j] * T.sph[k], T.ct[j]};
-                double o[3];
-                qrot_h(&c->quats[4 * i], v, o);
-                for (int d = 0; d < 3; ++d) {
-                    c->norms[3 * id + d] = o[d];
-                    c->coords[3 * id + d] = a * o[d] + c->centers[3 * i + d];
-                }
                 c->weights[id] = a * a * T.wq[j];
                 c->sid[id] = i;
             }
@@ -356,40 +409,8 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
         pr.v1 = 3 * pr.p1;
     }
 
-    // near pairs (MPI/NearInteraction.txx:430-447; Rad = 1.5*radius, SphereSTKSHOperator.cpp:547),
-    // within each problem, sorted by target then source; overlapping spheres are rejected
-    c->nbr_start.assign(N + 1, 0);
-    c->nbr_src.clear();
-    c->nbr_precise.clear();
-    for (const auto& pr : c->problems)
-        for (int t = pr.s0; t < pr.s1; ++t) {
-            for (int s = pr.s0; s < pr.s1; ++s) {
-                double r2 = 0;
-                for (int k = 0; k < 3; ++k) {
-                    const double d = c->centers[3 * s + k] - c->centers[3 * t + k];
-                    r2 += d * d;
-                }
-                if (s != t && std::sqrt(r2) <= c->radii[s] + c->radii[t])
-                    throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(s) +
-                                                      " overlap or touch");
-                const double Rn = 1.5 * c->radii[s] + 1.5 * c->radii[t];
-                if (r2 > 0 && r2 < Rn * Rn) {
-                    c->nbr_src.push_back(s);
-                    const double gap = std::sqrt(r2) - c->radii[s] - c->radii[t];
-                    c->nbr_precise.push_back(gap < 0.1 * std::min(c->radii[s], c->radii[t]) ? 1 : 0);
-                }
-            }
-            c->nbr_start[t + 1] = (int)c->nbr_src.size();
-        }
-    c->near_src_slot.assign(N, -1);
-    c->slot_sphere.clear();
-    for (int s : c->nbr_src)
-        if (c->near_src_slot[s] < 0) {
-            c->near_src_slot[s] = (int)c->slot_sphere.size();
-            c->slot_sphere.push_back(s);
-        }
-    std::sort(c->slot_sphere.begin(), c->slot_sphere.end());
-    for (size_t k = 0; k < c->slot_sphere.size(); ++k) c->near_src_slot[c->slot_sphere[k]] = (int)k;
+    check_overlap(c, c->centers);
+    build_near(c);
     const int ndmax = ncoef(c->pmax + 3);
     c->set_stride_trac = 2LL * kNearSetsTrac * ndmax;
     c->set_stride_sl = 2LL * kNearSetsSL * ndmax;
@@ -448,7 +469,95 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
         pr.c1 = (int)c->chunks.size();
     }
 
-    // tables per order present (and p+1 synthesis tables are host-only)
+    build_tables(c);
+
+    // point data: FP64 lab-frame grid and the far-field copies relative to each problem's origin
+    // (centre of its sphere bounding box), all written by the regrid kernel below
+    problem_origins(c);
+    c->d_center.upload(c->centers);
+    c->d_radius.upload(c->radii);
+    c->d_quat.upload(c->quats);
+    c->d_order.upload(c->orders);
+    c->d_gidx.upload(c->gidx);
+    c->d_glen.upload(c->glen);
+    c->d_coff.upload(c->coff);
+    c->d_prob.upload(c->prob);
+    c->d_coords.alloc(sizeof(double) * 3 * c->M);
+    c->d_norms.alloc(sizeof(double) * 3 * c->M);
+    c->d_weights.upload(c->weights);
+    c->d_sid.upload(c->sid);
+    c->d_pos32.alloc(sizeof(float4) * c->M);
+    c->d_nrm32.alloc(sizeof(float4) * c->M);
+    c->d_pos32lo.alloc(sizeof(float4) * c->M);
+    c->d_nrm32lo.alloc(sizeof(float4) * c->M);
+    c->d_pos64.alloc(sizeof(double4) * c->M);
+    c->d_nrm64.alloc(sizeof(double4) * c->M);
+    c->d_org.upload(c->org);
+    c->d_problems.upload(c->problems);
+    c->d_items32.upload(c->items32);
+    c->d_items64.upload(c->items64);
+    c->d_items_df.upload(c->items_tpt[1]);  // float-float far field: 256 targets per CTA, 2 per thread
+    c->d_chunks.upload(c->chunks);
+    std::vector<unsigned char> act(c->P, 1);
+    c->d_active.upload(act);
+
+    // operator workspace
+    c->d_src32.alloc(sizeof(float4) * c->M);
+    c->d_src64.alloc(sizeof(double4) * c->M);
+    c->d_srcdf.alloc(sizeof(float4) * 2 * c->M);
+    c->d_partial32.alloc(sizeof(float) * c->partial32);
+    c->d_partial64.alloc(sizeof(double) * c->partial64);
+    c->d_coef32.alloc(sizeof(float) * 2 * c->ncoef_total);
+    c->d_coef64.alloc(sizeof(double) * 2 * c->ncoef_total);
+    c->d_in.alloc(sizeof(double) * 3 * c->M);
+    c->d_out.alloc(sizeof(double) * 3 * c->M);
+    c->d_tmp.alloc(sizeof(double) * 3 * c->M);
+    c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * 2);
+    upload_near(c);
+    bind_geom(c);
+    check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
+}
+
+// ---------------------------------------------------------------- tables, near metadata, bindings
+// per-problem origin for the relative point coordinates: centre of the problem's sphere bounding box
+void problem_origins(smob_ctx* c) {
+    c->org.assign(3 * c->P, 0.0);
+    for (int pi = 0; pi < c->P; ++pi) {
+        const Problem& pr = c->problems[pi];
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int s = pr.s0; s < pr.s1; ++s)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], c->centers[3 * s + k]);
+                hi[k] = std::max(hi[k], c->centers[3 * s + k]);
+            }
+        for (int k = 0; k < 3; ++k) c->org[3 * pi + k] = 0.5 * (lo[k] + hi[k]);
+    }
+}
+
+// near lists, slots and the near-set workspace to the device; near lanes for this geometry
+void upload_near(smob_ctx* c) {
+    c->d_nbr_start.upload(c->nbr_start);
+    c->d_nbr_src.upload(c->nbr_src);
+    c->d_nbr_precise.upload(c->nbr_precise);
+    c->n_precise = 0;
+    for (unsigned char v : c->nbr_precise) c->n_precise += v;
+    c->d_near_slot.upload(c->near_src_slot);
+    c->d_slot_sphere.upload(c->slot_sphere);
+    const size_t nsl = c->slot_sphere.size();
+    c->d_sets32.alloc(sizeof(float) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
+    c->d_sets64.alloc(sizeof(double) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
+    // near-field lanes per target: enough threads to fill the GPU (~152 SMs x 2048 threads) when few
+    // target points have near pairs, one lane (no repeated recurrence) when many do; the lane count
+    // does not change any result (each set is summed by one lane in a fixed order)
+    long long tpts = 0;
+    for (int t = 0; t < c->N; ++t)
+        if (c->nbr_start[t + 1] > c->nbr_start[t]) tpts += c->glen[t];
+    const double want = 152.0 * 2048.0 / double(std::max<long long>(tpts, 1));
+    c->g.near_lanes = want >= 8 ? 8 : (want >= 4 ? 4 : (want >= 2 ? 2 : 1));
+}
+
+// transform tables of every order present, near maps of the orders of near-source spheres
+void build_tables(smob_ctx* c) {
     std::vector<OrderTables> tabs(kMaxOrder + 1);
     std::vector<double> tab;
     std::vector<int> rowptr, col;
@@ -512,62 +621,6 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->g.th_diag = (int)tab.size();
     tab.insert(tab.end(), dg.begin(), dg.end());
 
-    // FP32/FP64 point data relative to each problem's origin (centre of its sphere bounding box)
-    std::vector<float4> pos32(c->M), nrm32(c->M), pos32lo(c->M), nrm32lo(c->M);
-    std::vector<double4> pos64(c->M), nrm64(c->M);
-    for (const auto& pr : c->problems) {
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (int s = pr.s0; s < pr.s1; ++s)
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = std::min(lo[k], c->centers[3 * s + k]);
-                hi[k] = std::max(hi[k], c->centers[3 * s + k]);
-            }
-        double org[3];
-        for (int k = 0; k < 3; ++k) org[k] = 0.5 * (lo[k] + hi[k]);
-        for (int i = pr.p0; i < pr.p1; ++i) {
-            int sidbits = c->sid[i];
-            float fs;
-            std::memcpy(&fs, &sidbits, 4);
-            const double x = c->coords[3 * i] - org[0], y = c->coords[3 * i + 1] - org[1], z = c->coords[3 * i + 2] - org[2];
-            pos32[i] = make_float4(float(x), float(y), float(z), fs);
-            nrm32[i] = make_float4(float(c->norms[3 * i]), float(c->norms[3 * i + 1]), float(c->norms[3 * i + 2]), 0.f);
-            pos32lo[i] = make_float4(float(x - double(pos32[i].x)), float(y - double(pos32[i].y)),
-                                     float(z - double(pos32[i].z)), 0.f);
-            nrm32lo[i] = make_float4(float(c->norms[3 * i] - double(nrm32[i].x)),
-                                     float(c->norms[3 * i + 1] - double(nrm32[i].y)),
-                                     float(c->norms[3 * i + 2] - double(nrm32[i].z)), 0.f);
-            pos64[i] = make_double4(x, y, z, 0.0);
-            nrm64[i] = make_double4(c->norms[3 * i], c->norms[3 * i + 1], c->norms[3 * i + 2], 0.0);
-        }
-    }
-
-    // upload
-    c->d_center.upload(c->centers);
-    c->d_radius.upload(c->radii);
-    c->d_quat.upload(c->quats);
-    c->d_order.upload(c->orders);
-    c->d_gidx.upload(c->gidx);
-    c->d_glen.upload(c->glen);
-    c->d_coff.upload(c->coff);
-    c->d_prob.upload(c->prob);
-    c->d_coords.upload(c->coords);
-    c->d_norms.upload(c->norms);
-    c->d_weights.upload(c->weights);
-    c->d_sid.upload(c->sid);
-    c->d_pos32.upload(pos32);
-    c->d_nrm32.upload(nrm32);
-    c->d_pos32lo.upload(pos32lo);
-    c->d_nrm32lo.upload(nrm32lo);
-    c->d_pos64.upload(pos64);
-    c->d_nrm64.upload(nrm64);
-    c->d_nbr_start.upload(c->nbr_start);
-    c->d_nbr_src.upload(c->nbr_src);
-    c->d_nbr_precise.upload(c->nbr_precise);
-    c->n_precise = 0;
-    for (unsigned char v : c->nbr_precise) c->n_precise += v;
-    c->d_near_slot.upload(c->near_src_slot);
-    c->d_slot_sphere.upload(c->slot_sphere);
-    c->d_problems.upload(c->problems);
     c->d_tabs.upload(tabs);
     c->d_tab_d.upload(tab);
     std::vector<float> tabf(tab.begin(), tab.end());
@@ -577,43 +630,16 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_map_val_d.upload(mval);
     std::vector<float> mvalf(mval.begin(), mval.end());
     c->d_map_val_f.upload(mvalf);
-    c->d_items32.upload(c->items32);
-    c->d_items64.upload(c->items64);
-    c->d_items_df.upload(c->items_tpt[1]);  // float-float far field: 256 targets per CTA, 2 per thread
-    c->d_chunks.upload(c->chunks);
-    std::vector<unsigned char> act(c->P, 1);
-    c->d_active.upload(act);
+    c->map_orders = near_p;
+}
 
-    // operator workspace
-    c->d_src32.alloc(sizeof(float4) * c->M);
-    c->d_src64.alloc(sizeof(double4) * c->M);
-    c->d_srcdf.alloc(sizeof(float4) * 2 * c->M);
-    c->d_partial32.alloc(sizeof(float) * c->partial32);
-    c->d_partial64.alloc(sizeof(double) * c->partial64);
-    c->d_coef32.alloc(sizeof(float) * 2 * c->ncoef_total);
-    c->d_coef64.alloc(sizeof(double) * 2 * c->ncoef_total);
-    const size_t nsl = c->slot_sphere.size();
-    c->d_sets32.alloc(sizeof(float) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
-    c->d_sets64.alloc(sizeof(double) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
-    c->d_in.alloc(sizeof(double) * 3 * c->M);
-    c->d_out.alloc(sizeof(double) * 3 * c->M);
-    c->d_tmp.alloc(sizeof(double) * 3 * c->M);
-    c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * 2);
-
+// device pointers and sizes of the geometry, as the kernels receive them
+void bind_geom(smob_ctx* c) {
     DevGeom& g = c->g;
     g.N = c->N;
     g.M = c->M;
     g.P = c->P;
     g.pmax = c->pmax;
-    // near-field lanes per target: enough threads to fill the GPU (~152 SMs x 2048 threads) when few
-    // target points have near pairs, one lane (no repeated recurrence) when many do
-    {
-        long long tpts = 0;
-        for (int t = 0; t < c->N; ++t)
-            if (c->nbr_start[t + 1] > c->nbr_start[t]) tpts += c->glen[t];
-        const double want = 152.0 * 2048.0 / double(std::max<long long>(tpts, 1));
-        g.near_lanes = want >= 8 ? 8 : (want >= 4 ? 4 : (want >= 2 ? 2 : 1));
-    }
     g.center = c->d_center.as<double>();
     g.radius = c->d_radius.as<double>();
     g.quat = c->d_quat.as<double>();
@@ -1200,6 +1226,68 @@ void need(bool cond, const char* msg) {
 
 void set_device(const smob_ctx* c) { CUDA_OK(cudaSetDevice(c->device)); }
 
+// the last geometry update rebuilt the grid on the device only: bring the host copy up to date
+void refresh_host_grid(const smob_ctx* c) {
+    if (!c->host_grid_stale) return;
+    set_device(c);
+    CUDA_OK(cudaMemcpyAsync(c->coords.data(), c->d_coords.p, sizeof(double) * c->coords.size(), cudaMemcpyDeviceToHost,
+                            c->st));
+    CUDA_OK(cudaMemcpyAsync(c->norms.data(), c->d_norms.p, sizeof(double) * c->norms.size(), cudaMemcpyDeviceToHost,
+                            c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    c->host_grid_stale = false;
+}
+
+// Orientation after a time step (Sphere::stepEuler, Sphere/Sphere.cpp:367-373, through SimToolbox's
+// EquatnHelper::rotateEquatn, which is absent): the rotation by angle |w| dt about w (a lab-frame
+// angular velocity) composed on the left, q <- (cos(|w|dt/2), sin(|w|dt/2) w/|w|) q, normalised.
+void quat_step(const double* q, const double* w, double dt, double* out) {
+    const double wn = std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    if (!(wn * std::fabs(dt) > 0)) {
+        std::copy(q, q + 4, out);
+        return;
+    }
+    const double h = 0.5 * wn * dt, sh = std::sin(h) / wn;
+    const double a0 = std::cos(h), a[3] = {w[0] * sh, w[1] * sh, w[2] * sh};
+    // Hamilton product (a0, a) (q0, qv)
+    double r[4];
+    r[0] = a0 * q[0] - (a[0] * q[1] + a[1] * q[2] + a[2] * q[3]);
+    r[1] = a0 * q[1] + q[0] * a[0] + (a[1] * q[3] - a[2] * q[2]);
+    r[2] = a0 * q[2] + q[0] * a[1] + (a[2] * q[1] - a[0] * q[3]);
+    r[3] = a0 * q[3] + q[0] * a[2] + (a[0] * q[2] - a[1] * q[1]);
+    const double n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3]);
+    for (int k = 0; k < 4; ++k) out[k] = r[k] / n;
+}
+
+// New centres and orientations for the same spheres: near lists and their metadata on the host
+// (O(N) data), grid points and far-field copies rebuilt on the device (no host round trip of the
+// O(M) arrays). Throws (context unchanged) if spheres of a problem would overlap. The warm-start
+// solution is kept; captured graphs and several-RHS copies of the old geometry are dropped.
+void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std::vector<double>& quats) {
+    check_overlap(c, centers);
+    c->centers = centers;
+    c->quats = quats;
+    build_near(c);
+    std::vector<char> near_p(kMaxOrder + 1, 0);
+    for (int s : c->slot_sphere) near_p[c->orders[s]] = 1;
+    bool new_map = false;
+    for (int p = 1; p <= kMaxOrder; ++p)
+        if (near_p[p] && !(p < (int)c->map_orders.size() && c->map_orders[p])) new_map = true;
+    if (new_map) build_tables(c);
+    problem_origins(c);
+    c->d_center.upload(c->centers);
+    c->d_quat.upload(c->quats);
+    c->d_org.upload(c->org);
+    upload_near(c);
+    bind_geom(c);
+    check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
+    c->host_grid_stale = true;
+    c->drop_graphs();
+    for (auto& kv : c->multi) smob_destroy(kv.second);
+    c->multi.clear();
+    CUDA_OK(cudaStreamSynchronize(c->st));
+}
+
 // copy a host 3M vector in, run f(d_in, d_out) with d_out preloaded from host out, copy back
 template <typename F>
 void host_io(smob_ctx* c, const double* in, double* out, bool load_out, F&& f) {
@@ -1225,6 +1313,21 @@ void all_active(smob_ctx* c) {
 }
 
 }  // namespace
+
+smob::HostSpheres smob::host_spheres(const smob_ctx* c) {
+    refresh_host_grid(c);
+    HostSpheres h;
+    h.N = c->N;
+    h.M = c->M;
+    h.centers = c->centers.data();
+    h.radii = c->radii.data();
+    h.quats = c->quats.data();
+    h.coords = c->coords.data();
+    h.weights = c->weights.data();
+    h.orders = c->orders.data();
+    h.gidx = c->gidx.data();
+    return h;
+}
 
 // ================================================================ C ABI
 extern "C" {
@@ -1305,10 +1408,65 @@ smob_status smob_get_sizes(const smob_ctx* c, int* n_spheres, int* n_points, int
 smob_status smob_get_grid(const smob_ctx* c, double* coords, double* norms, double* weights) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
+        if (coords || norms) refresh_host_grid(c);
         if (coords) std::copy(c->coords.begin(), c->coords.end(), coords);
         if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
         if (weights) std::copy(c->weights.begin(), c->weights.end(), weights);
         return SMOB_OK;
+    });
+}
+
+smob_status smob_set_geometry(smob_ctx* c, const double* centers, const double* quats) {
+    return guarded([&]() -> smob_status {
+        need(c && centers, "null argument");
+        need(c->nrep == 1, "not a user context");
+        std::vector<double> ce(centers, centers + 3 * c->N);
+        for (double v : ce) need(std::isfinite(v), "centre is not finite");
+        std::vector<double> q = c->quats;
+        if (quats)
+            for (int i = 0; i < c->N; ++i) unit_quat(quats + 4 * i, &q[4 * i], i);
+        set_device(c);
+        AllocStreamScope scope(c->st);
+        update_geometry(c, ce, q);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_step_euler(smob_ctx* c, const double* vel6n, double dt) {
+    return guarded([&]() -> smob_status {
+        need(c && vel6n, "null argument");
+        need(c->nrep == 1, "not a user context");
+        need(std::isfinite(dt), "dt is not finite");
+        for (int i = 0; i < 6 * c->N; ++i) need(std::isfinite(vel6n[i]), "velocity is not finite");
+        std::vector<double> ce(c->centers), q(c->quats);
+        for (int i = 0; i < c->N; ++i) {
+            for (int k = 0; k < 3; ++k) ce[3 * i + k] += vel6n[6 * i + k] * dt;
+            quat_step(&c->quats[4 * i], vel6n + 6 * i + 3, dt, &q[4 * i]);
+        }
+        set_device(c);
+        AllocStreamScope scope(c->st);
+        update_geometry(c, ce, q);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_get_geometry(const smob_ctx* c, double* centers, double* quats) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (centers) std::copy(c->centers.begin(), c->centers.end(), centers);
+        if (quats) std::copy(c->quats.begin(), c->quats.end(), quats);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_step_euler_device(smob_ctx* c, const double* d_vel6n, double dt) {
+    return guarded([&]() -> smob_status {
+        need(c && d_vel6n, "null argument");
+        set_device(c);
+        std::vector<double> v(6 * (size_t)c->N);
+        CUDA_OK(cudaMemcpyAsync(v.data(), d_vel6n, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return smob_step_euler(c, v.data(), dt);
     });
 }
 

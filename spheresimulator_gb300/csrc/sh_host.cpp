@@ -91,6 +91,38 @@ void synth(const HostOrderTables& T, int pc, const cd* c, double* g) {
     }
 }
 
+}  // namespace
+
+// the VSH expansion of degree <= p at one body-frame direction (theta, phi), Cartesian body-frame
+// output; the same basis and sums as synth (0 < theta < pi)
+void vsh_eval_point(int p, const std::complex<double>* c, double theta, double phi, double* out) {
+    const int nc = ncoef(p);
+    std::vector<double> P(nc), dP(nc), Ps(nc);
+    const double t = std::cos(theta), s = std::sin(theta);
+    legendre_ring(p, t, s, P.data(), dP.data(), Ps.data());
+    double vr = 0, vt = 0, vp = 0;
+    for (int m = 0; m <= p; ++m) {
+        cd r(0, 0), th(0, 0), q(0, 0);
+        for (int n = m; n <= p; ++n) {
+            const int id = cidx(n, m);
+            const cd im(0, m * Ps[id]);
+            r += c[id] * P[id];
+            th += c[nc + id] * dP[id] - im * c[2 * nc + id];
+            q += im * c[nc + id] + c[2 * nc + id] * dP[id];
+        }
+        const double e = m == 0 ? 1.0 : 2.0, c0 = std::cos(m * phi), s0 = std::sin(m * phi);
+        vr += e * (r.real() * c0 - r.imag() * s0);
+        vt += e * (th.real() * c0 - th.imag() * s0);
+        vp += e * (q.real() * c0 - q.imag() * s0);
+    }
+    const double cp = std::cos(phi), sp = std::sin(phi);
+    out[0] = vr * s * cp + vt * t * cp - vp * sp;
+    out[1] = vr * s * sp + vt * t * sp + vp * cp;
+    out[2] = vr * t - vt * s;
+}
+
+namespace {
+
 void scalar_analysis(const HostOrderTables& T, const double* f, int stride, cd* out) {
     const int pd = T.p;
     std::fill(out, out + ncoef(pd), cd(0, 0));

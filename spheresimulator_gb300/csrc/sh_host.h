@@ -4,6 +4,7 @@
 // sphere's vector-SH coefficients to the coefficient sets of its exterior Laplace
 // potentials (used by the near-field evaluation).
 #pragma once
+#include <complex>
 #include <vector>
 
 namespace smob {
@@ -26,6 +27,9 @@ struct SparseMap {
 };
 
 const HostOrderTables& host_tables(int p);
+// VSH coefficients (3 blocks of ncoef(p) complex values) evaluated at one body-frame direction
+// (0 < theta < pi); Cartesian body-frame vector out[3]
+void vsh_eval_point(int p, const std::complex<double>* c, double theta, double phi, double* out);
 void gauss_legendre_nodes(int n, std::vector<double>& x, std::vector<double>& w);
 // trac = true: 25 sets (div L, Hessians of L_x, L_y, L_z, L_r); false: 15 sets (L_j, grad L_j, grad L_r)
 const SparseMap& near_map(int p, bool trac);

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+struct smob_ctx;
+
 namespace smob {
 
 constexpr int kMaxOrder = 32;
@@ -135,9 +137,22 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
                      cudaStream_t st, int pair_filter = 0);
 
+// Geometry update: grid points, normals and far-field copies from the current centres/orientations
+// (org: 3 per problem); writes the buffers that g's read-only views point to
+int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st);
+
 // Rigid-body pieces of the mobility solve
 int launch_rigid_density(const DevGeom& g, const double* force6n, double* rho, cudaStream_t st);
 int launch_rigid_average(const DevGeom& g, const double* u, double inv_visc, double* vel6n, cudaStream_t st);
+
+// Host view of a context's spheres and grid for the file writers (the grid is refreshed from the
+// device first if a geometry update changed it)
+struct HostSpheres {
+    int N = 0, M = 0;
+    const double *centers = nullptr, *radii = nullptr, *quats = nullptr, *coords = nullptr, *weights = nullptr;
+    const int *orders = nullptr, *gidx = nullptr;
+};
+HostSpheres host_spheres(const ::smob_ctx* c);
 
 
 }  // namespace smob

@@ -350,6 +350,56 @@ __global__ void k_rigid_density(DevGeom g, const double* __restrict__ f6, double
     rho[3 * i + 2] = F[2] * fa + B[0] * r[1] - B[1] * r[0];
 }
 
+// Grid points, normals and the far-field copies of every point from the spheres' current centres and
+// orientations (Shexp::getGridWithPole without the poles, Sphere/Shexp.cpp:206-271). The one builder
+// of the grid, at context creation and after every geometry update, so an updated context equals a
+// newly created one bit for bit; explicit round-to-nearest operations keep the result independent
+// of the compiler's FMA contraction.
+__device__ __forceinline__ void qrot_rn(const double* q, const double* v, double* o) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double tx = __dmul_rn(2.0, __dsub_rn(__dmul_rn(y, v[2]), __dmul_rn(z, v[1])));
+    const double ty = __dmul_rn(2.0, __dsub_rn(__dmul_rn(z, v[0]), __dmul_rn(x, v[2])));
+    const double tz = __dmul_rn(2.0, __dsub_rn(__dmul_rn(x, v[1]), __dmul_rn(y, v[0])));
+    o[0] = __dadd_rn(__dadd_rn(v[0], __dmul_rn(w, tx)), __dsub_rn(__dmul_rn(y, tz), __dmul_rn(z, ty)));
+    o[1] = __dadd_rn(__dadd_rn(v[1], __dmul_rn(w, ty)), __dsub_rn(__dmul_rn(z, tx), __dmul_rn(x, tz)));
+    o[2] = __dadd_rn(__dadd_rn(v[2], __dmul_rn(w, tz)), __dsub_rn(__dmul_rn(x, ty), __dmul_rn(y, tx)));
+}
+
+__global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __restrict__ coords,
+                         double* __restrict__ norms, float4* __restrict__ pos32, float4* __restrict__ nrm32,
+                         float4* __restrict__ pos32lo, float4* __restrict__ nrm32lo, double4* __restrict__ pos64,
+                         double4* __restrict__ nrm64) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.M) return;
+    const int s = g.sid[i];
+    const OrderTables T = g.tabs[g.order[s]];
+    const int l = i - g.gidx[s], j = l / T.nphi, k = l - j * T.nphi;
+    const double ct = g.tab_d[T.ring + j], st = g.tab_d[T.ring + T.nt + j];
+    const double cp = g.tab_d[T.cph + k], sp = g.tab_d[T.cph + T.nphi + k];
+    const double v[3] = {__dmul_rn(st, cp), __dmul_rn(st, sp), ct};
+    double n[3];
+    qrot_rn(g.quat + 4 * s, v, n);
+    const double a = g.radius[s];
+    const double* o = org + 3 * g.prob[s];
+    double x[3], r[3];
+    for (int d = 0; d < 3; ++d) {
+        x[d] = __dadd_rn(__dmul_rn(a, n[d]), g.center[3 * s + d]);
+        r[d] = __dsub_rn(x[d], o[d]);
+        coords[3 * i + d] = x[d];
+        norms[3 * i + d] = n[d];
+    }
+    const float4 p = make_float4(float(r[0]), float(r[1]), float(r[2]), __int_as_float(s));
+    const float4 q = make_float4(float(n[0]), float(n[1]), float(n[2]), 0.f);
+    pos32[i] = p;
+    nrm32[i] = q;
+    pos32lo[i] = make_float4(float(__dsub_rn(r[0], double(p.x))), float(__dsub_rn(r[1], double(p.y))),
+                             float(__dsub_rn(r[2], double(p.z))), 0.f);
+    nrm32lo[i] = make_float4(float(__dsub_rn(n[0], double(q.x))), float(__dsub_rn(n[1], double(q.y))),
+                             float(__dsub_rn(n[2], double(q.z))), 0.f);
+    pos64[i] = make_double4(r[0], r[1], r[2], 0.0);
+    nrm64[i] = make_double4(n[0], n[1], n[2], 0.0);
+}
+
 __global__ void k_rigid_average(DevGeom g, const double* __restrict__ u, double inv_visc, double* __restrict__ vel) {
     const int s = blockIdx.x;
     if (g.active && !g.active[g.prob[s]]) return;
@@ -401,6 +451,14 @@ int launch_sh_g2s(const DevGeom& g, const double* grid, double* coef, cudaStream
 int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream_t st) {
     SphereArgs a{nullptr, coef, grid, 0, 0, 0, -1, 2, nullptr};
     return launch_sphere<double>(g, a, st);
+}
+
+int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st) {
+    k_regrid<<<(g.M + 255) / 256, 256, 0, st>>>(g, org, const_cast<double*>(g.coords), const_cast<double*>(g.norms),
+                                                const_cast<float4*>(g.pos32), const_cast<float4*>(g.nrm32),
+                                                const_cast<float4*>(g.pos32lo), const_cast<float4*>(g.nrm32lo),
+                                                const_cast<double4*>(g.pos64), const_cast<double4*>(g.nrm64));
+    return 1;
 }
 
 int launch_rigid_density(const DevGeom& g, const double* force6n, double* rho, cudaStream_t st) {
