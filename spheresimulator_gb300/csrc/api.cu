@@ -113,9 +113,11 @@ void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace smob
 
 struct smob_ctx {
-    StreamHolder sh;  // first member: destroyed last, after all buffers were freed on it
+    StreamHolder sh;   // first member: destroyed last, after all buffers were freed on it
+    StreamHolder sh2;  // side stream of the operator passes (far field beside sphere/near kernels)
     int device = 0;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr, st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int N = 0, M = 0, P = 0, pmax = 0;
     double viscosity = 1.0;
     std::vector<double> centers, radii, quats, weights;
@@ -209,6 +211,8 @@ struct smob_ctx {
         }
         if (ev_a) cudaEventDestroy(ev_a);
         if (ev_b) cudaEventDestroy(ev_b);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
         drop_graphs();
     }
 };
@@ -219,18 +223,41 @@ namespace {
 struct ProfScope {
     smob_ctx* c;
     const char* name;
+    cudaStream_t s;
     cudaEvent_t a{}, b{};
-    ProfScope(smob_ctx* ctx, const char* n) : c(ctx), name(n) {
+    ProfScope(smob_ctx* ctx, const char* n, cudaStream_t st = nullptr) : c(ctx), name(n), s(st ? st : ctx->st) {
         if (c->prof) {
             cudaEventCreate(&a);
             cudaEventCreate(&b);
-            cudaEventRecord(a, c->st);
+            cudaEventRecord(a, s);
         }
     }
     ~ProfScope() {
         if (c->prof) {
-            cudaEventRecord(b, c->st);
+            cudaEventRecord(b, s);
             c->pending.push_back({name, a, b});
+        }
+    }
+};
+
+// Fork/join of one operator pass: the far field runs on the side stream while the sphere and near
+// kernels run on the main stream (they touch disjoint buffers until the far-field reduction, which
+// follows the join). Serial when profiling, so each kernel's CUDA-event time stays its own.
+struct PassFork {
+    smob_ctx* c;
+    bool on;
+    explicit PassFork(smob_ctx* ctx) : c(ctx), on(ctx->st2 != nullptr && !ctx->prof) {
+        if (on) {
+            CUDA_OK(cudaEventRecord(c->ev_fork, c->st));
+            CUDA_OK(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
+        }
+    }
+    cudaStream_t far() const { return on ? c->st2 : c->st; }
+    void join() {
+        if (on) {
+            CUDA_OK(cudaEventRecord(c->ev_join, c->st2));
+            CUDA_OK(cudaStreamWaitEvent(c->st, c->ev_join, 0));
+            on = false;
         }
     }
 };
@@ -758,6 +785,32 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
     const FarItem* items = fp32 ? c->d_items32.as<FarItem>() : c->d_items64.as<FarItem>();
     const int nitems = (int)(fp32 ? c->items32.size() : c->items64.size());
     auto kind_pass = [&](bool tr, double cc, bool with_id_lop) {
+        PassFork fork(c);
+        const cudaStream_t fs = fork.far();
+        // far field: side stream
+        if (dfar) {
+            {
+                ProfScope ps(c, "far_pack", fs);
+                check_launch(c, launch_far_pack_df(g, x, cc, c->d_srcdf.as<float4>(), fs));
+            }
+            ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df", fs);
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), tr ? 1 : 0,
+                                                c->d_srcdf.as<float4>(), static_cast<double*>(partial), nullptr, fs));
+        } else {
+            {
+                ProfScope ps(c, "far_pack", fs);
+                check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, fs));
+            }
+            ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"), fs);
+            if (fp32 && c->nrep > 1)
+                check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
+                                                     c->rep_M, tr, c->d_src32.as<float4>(), static_cast<float*>(partial),
+                                                     fs));
+            else
+                check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                                 c->d_src64.as<double4>(), partial, fs, c->tpt));
+        }
+        // sphere self and near field: main stream
         {
             ProfScope ps(c, "sphere_self");
             check_launch(c, launch_sphere_op(g, x, out, with_id_lop && id ? c_id : 0.0, cc, tr ? 3 : 0,
@@ -784,28 +837,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, cc, out, c->st, 2));
             }
         }
-        if (dfar) {
-            {
-                ProfScope ps(c, "far_pack");
-                check_launch(c, launch_far_pack_df(g, x, cc, c->d_srcdf.as<float4>(), c->st));
-            }
-            ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
-            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), tr ? 1 : 0,
-                                                c->d_srcdf.as<float4>(), static_cast<double*>(partial), nullptr, c->st));
-        } else {
-            {
-                ProfScope ps(c, "far_pack");
-                check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
-            }
-            ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
-            if (fp32 && c->nrep > 1)
-                check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
-                                                     c->rep_M, tr, c->d_src32.as<float4>(), static_cast<float*>(partial),
-                                                     c->st));
-            else
-                check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                 c->d_src64.as<double4>(), partial, c->st, c->tpt));
-        }
+        fork.join();
         {
             ProfScope ps(c, "far_reduce");
             check_launch(c, launch_far_reduce(g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), out, c->st));
@@ -827,6 +859,18 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
     const DevGeom& g = c->g;
     const int nslots = (int)c->slot_sphere.size();
     c->d_partial64_sl.alloc(sizeof(double) * c->partial64);
+    PassFork fork(c);
+    const cudaStream_t fs = fork.far();
+    {
+        ProfScope ps(c, "far_pack", fs);
+        check_launch(c, launch_far_pack_df(g, x, 1.0, c->d_srcdf.as<float4>(), fs));
+    }
+    {
+        ProfScope ps(c, "far_both_df", fs);
+        check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
+                                            c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
+                                            c->d_partial64_sl.as<double>(), fs));
+    }
     {
         ProfScope ps(c, "sphere_self");
         check_launch(c, launch_sphere_op(g, x, out_t, c_id, c_trac, 3, 0.0, c->d_coef64.p, false, c->st));
@@ -846,16 +890,7 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
                                              c->st, 0));
         }
     }
-    {
-        ProfScope ps(c, "far_pack");
-        check_launch(c, launch_far_pack_df(g, x, 1.0, c->d_srcdf.as<float4>(), c->st));
-    }
-    {
-        ProfScope ps(c, "far_both_df");
-        check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
-                                            c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
-                                            c->d_partial64_sl.as<double>(), c->st));
-    }
+    fork.join();
     ProfScope ps(c, "far_reduce");
     check_launch(c, launch_far_reduce(g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), out_t, c->st));
     check_launch(c, launch_far_reduce(g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), out_s, c->st));
@@ -1226,6 +1261,17 @@ void need(bool cond, const char* msg) {
 
 void set_device(const smob_ctx* c) { CUDA_OK(cudaSetDevice(c->device)); }
 
+// the context's main and side streams (non-blocking, priority prio: 0 is the default) and the
+// fork/join events of the operator passes
+void create_streams(smob_ctx* c, int prio) {
+    CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
+    c->sh.st = c->st;
+    CUDA_OK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, prio));
+    c->sh2.st = c->st2;
+    CUDA_OK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CUDA_OK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+}
+
 // the last geometry update rebuilt the grid on the device only: bring the host copy up to date
 void refresh_host_grid(const smob_ctx* c) {
     if (!c->host_grid_stale) return;
@@ -1365,15 +1411,13 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
         std::unique_ptr<smob_ctx> c(new smob_ctx);
         c->device = device;
         CUDA_OK(cudaSetDevice(device));
+        int prio = 0;
         if (priority_rank >= 0) {
             int least = 0, greatest = 0;
             CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-            const int prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
-            CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
-        } else {
-            CUDA_OK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+            prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
         }
-        c->sh.st = c->st;
+        create_streams(c.get(), prio);
         AllocStreamScope scope(c->st);
         configure_sphere_kernels();
         build_context(c.get(), geo);
@@ -1725,8 +1769,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
     CUDA_OK(cudaSetDevice(c->device));
-    CUDA_OK(cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking));
-    r->sh.st = r->st;
+    create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
     build_context(r.get(), &geo);
     r->nrep = k;
