@@ -23,15 +23,28 @@ namespace smob {
 
 namespace {
 
+// One MUFU instruction each (PTX rsqrt/rcp .approx.ftz): plain rsqrtf adds a fix-up for denormal
+// arguments, which a squared pair distance never is. 1/r^2 from its own MUFU spares the FMA pipes
+// the ri*ri product that the pair would otherwise spend on it.
+__device__ __forceinline__ float rsqrt_mufu(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_mufu(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void pair_trac32(const float4& t, const float4& n, const float4& s, const float4& f,
                                             float& ax, float& ay, float& az) {
     const float rx = t.x - s.x, ry = t.y - s.y, rz = t.z - s.z;
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float ri = rsqrtf(r2);
-    const float ri2 = ri * ri;
+    const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
     const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
     const float rn = fmaf(rx, n.x, fmaf(ry, n.y, rz * n.z));
-    const float k = (rf * rn) * (ri2 * ri2 * ri);
+    const float k = (rf * rn) * (q * q * ri);
     ax = fmaf(k, rx, ax);
     ay = fmaf(k, ry, ay);
     az = fmaf(k, rz, az);
@@ -41,9 +54,9 @@ __device__ __forceinline__ void pair_sl32(const float4& t, const float4& s, cons
                                           float& az) {
     const float rx = t.x - s.x, ry = t.y - s.y, rz = t.z - s.z;
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float ri = rsqrtf(r2);
+    const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
     const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
-    const float k = rf * (ri * ri * ri);
+    const float k = rf * (q * ri);
     ax = fmaf(f.x, ri, fmaf(k, rx, ax));
     ay = fmaf(f.y, ri, fmaf(k, ry, ay));
     az = fmaf(f.z, ri, fmaf(k, rz, az));
@@ -86,7 +99,7 @@ __device__ __forceinline__ bool excluded(const int* __restrict__ nbr_src, int& c
 // Blackwell issues two FP32 lanes per FFMA2/FADD2/FMUL2 instruction (__ffma2_rn & co., same
 // per-component rounding as the scalar forms). Targets are packed two per float2; each staged
 // source is stored pre-duplicated, (x,x,y,y) (z,z,fx,fx) (fy,fy,fz,fz), so three 128-bit shared
-// loads give the six broadcast operands. Per pair: ~10 packed instructions + 1 MUFU.RSQ.
+// loads give the six broadcast operands. Per pair: ~10 packed instructions + MUFU.RSQ and MUFU.RCP.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
 template <bool TRAC>
@@ -97,17 +110,16 @@ __device__ __forceinline__ void pair_x2(const float2& tx, const float2& ty, cons
     const float2 ry = __fadd2_rn(ty, f2(-A.z, -A.w));
     const float2 rz = __fadd2_rn(tz, f2(-B.x, -B.y));
     const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __fmul2_rn(rz, rz)));
-    const float2 ri = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+    const float2 ri = f2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y)), q = f2(rcp_mufu(r2.x), rcp_mufu(r2.y));
     const float2 rf = __ffma2_rn(rx, f2(B.z, B.w), __ffma2_rn(ry, f2(C.x, C.y), __fmul2_rn(rz, f2(C.z, C.w))));
     if (TRAC) {
         const float2 rn = __ffma2_rn(rx, nx, __ffma2_rn(ry, ny, __fmul2_rn(rz, nz)));
-        const float2 ri2 = __fmul2_rn(ri, ri);
-        const float2 k = __fmul2_rn(__fmul2_rn(rf, rn), __fmul2_rn(__fmul2_rn(ri2, ri2), ri));
+        const float2 k = __fmul2_rn(__fmul2_rn(rf, rn), __fmul2_rn(__fmul2_rn(q, q), ri));
         ax = __ffma2_rn(k, rx, ax);
         ay = __ffma2_rn(k, ry, ay);
         az = __ffma2_rn(k, rz, az);
     } else {
-        const float2 k = __fmul2_rn(rf, __fmul2_rn(__fmul2_rn(ri, ri), ri));
+        const float2 k = __fmul2_rn(rf, __fmul2_rn(q, ri));
         ax = __ffma2_rn(f2(B.z, B.w), ri, __ffma2_rn(k, rx, ax));
         ay = __ffma2_rn(f2(C.x, C.y), ri, __ffma2_rn(k, ry, ay));
         az = __ffma2_rn(f2(C.z, C.w), ri, __ffma2_rn(k, rz, az));
@@ -343,13 +355,12 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
             __syncthreads();
             if (sk) continue;
             for (int k = 0; k < n; ++k) {
-                const float4 q = sp[k];
-                const float rx = tp.x - q.x, ry = tp.y - q.y, rz = tp.z - q.z;
+                const float4 sq = sp[k];
+                const float rx = tp.x - sq.x, ry = tp.y - sq.y, rz = tp.z - sq.z;
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                const float ri = rsqrtf(r2);
+                const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
                 if (TRAC) {
-                    const float ri2 = ri * ri;
-                    const float ri5 = ri2 * ri2 * ri;
+                    const float ri5 = q * q * ri;
                     const float rn = fmaf(rx, tn.x, fmaf(ry, tn.y, rz * tn.z));
 #pragma unroll
                     for (int r = 0; r < KB; ++r) {
@@ -361,7 +372,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
                         az[r] = fmaf(kk, rz, az[r]);
                     }
                 } else {
-                    const float ri3 = ri * ri * ri;
+                    const float ri3 = q * ri;
 #pragma unroll
                     for (int r = 0; r < KB; ++r) {
                         const float4 f = sf[r][k];
@@ -378,12 +389,13 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
     if (!va) return;
 #pragma unroll
     for (int r = 0; r < KB; ++r) {
-        if (r >= nr) break;
-        const Problem pr = g.problems[r0 + r];
-        float* o = partial + pr.poff + 3LL * (pr.p1 - pr.p0) * it.chunk + 3LL * t;
-        o[0] = ax[r];
-        o[1] = ay[r];
-        o[2] = az[r];
+        if (r < nr) {
+            const Problem pr = g.problems[r0 + r];
+            float* o = partial + pr.poff + 3LL * (pr.p1 - pr.p0) * it.chunk + 3LL * t;
+            o[0] = ax[r];
+            o[1] = ay[r];
+            o[2] = az[r];
+        }
     }
 }
 
@@ -491,7 +503,7 @@ __device__ __forceinline__ df2 df_sqr3_2(df2 a, df2 b, df2 c) {
     return quick_two_sum2(s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo));
 }
 __device__ __forceinline__ df2 df_rsqrt2(df2 x) {
-    const float2 y = make_float2(rsqrtf(x.h.x), rsqrtf(x.h.y));
+    const float2 y = make_float2(rsqrt_mufu(x.h.x), rsqrt_mufu(x.h.y));
     const float2 yy = __fmul2_rn(y, y);
     const float2 yye = __ffma2_rn(y, y, neg2(yy));
     const float2 p = __fmul2_rn(x.h, yy);
