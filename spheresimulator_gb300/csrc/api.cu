@@ -1091,10 +1091,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         };
         // Steps run in blocks of kGraphBlock; with graphs on, each block is captured once per context
         // (per block start, cycle precision and restart length) and replayed, and the host looks at
-        // the active flags only between blocks.
+        // the active flags only between blocks (steps after every problem stopped inside a block
+        // launch kernels that return at once). A profiled solve checks after every step, so each
+        // kernel it times did its full work.
         const bool graphs = c->use_graphs && !c->prof;
-        for (int j0 = 0; j0 < m; j0 += kGraphBlock) {
-            const int cnt = std::min(kGraphBlock, m - j0);
+        const int blk = c->prof ? 1 : kGraphBlock;
+        for (int j0 = 0; j0 < m; j0 += blk) {
+            const int cnt = std::min(blk, m - j0);
             if (graphs) {
                 const long long key = ((long long)cyc_prec * 4096 + m) * 4096 + j0;
                 auto it = c->graphs.find(key);

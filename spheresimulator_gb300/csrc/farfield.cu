@@ -463,22 +463,14 @@ __device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
     const float2 bb = sub2(s, a);
     return {s, __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb))};
 }
-__device__ __forceinline__ df2 quick_two_sum2(float2 a, float2 b) {
-    const float2 s = __fadd2_rn(a, b);
-    return {s, sub2(b, sub2(s, a))};
-}
-__device__ __forceinline__ df2 df_add2(df2 a, df2 b) {
-    const df2 s = two_sum2(a.h, b.h);
-    return quick_two_sum2(s.h, __fadd2_rn(s.l, __fadd2_rn(a.l, b.l)));
-}
+// Products, dot products, squares and the reciprocal square root return unnormalised pairs
+// (|lo| up to a few ulp of hi instead of half an ulp): every result feeds further products or the
+// two_sum accumulators, whose error bounds this leaves at ~2^-44 relative, far below the 1e-10 the
+// refinement residuals need, and each skipped renormalisation saves three instructions.
 __device__ __forceinline__ df2 df_mul_u2(df2 a, df2 b) {
     const float2 p = __fmul2_rn(a.h, b.h);
     const float2 e = __ffma2_rn(a.h, b.h, neg2(p));
     return {p, __ffma2_rn(a.h, b.l, __ffma2_rn(a.l, b.h, e))};
-}
-__device__ __forceinline__ df2 df_mul2(df2 a, df2 b) {
-    const df2 u = df_mul_u2(a, b);
-    return quick_two_sum2(u.h, u.l);
 }
 __device__ __forceinline__ df2 df_dot3_2(df2 a, df2 b, df2 c, df2 d, df2 e, df2 f) {
     const float2 p0 = __fmul2_rn(a.h, b.h), p1 = __fmul2_rn(c.h, d.h), p2 = __fmul2_rn(e.h, f.h);
@@ -489,7 +481,7 @@ __device__ __forceinline__ df2 df_dot3_2(df2 a, df2 b, df2 c, df2 d, df2 e, df2 
     lo = __ffma2_rn(e.h, f.l, __ffma2_rn(e.l, f.h, lo));
     const df2 s01 = two_sum2(p0, p1);
     const df2 s = two_sum2(s01.h, p2);
-    return quick_two_sum2(s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo));
+    return {s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo)};
 }
 __device__ __forceinline__ df2 df_sqr3_2(df2 a, df2 b, df2 c) {
     const float2 p0 = __fmul2_rn(a.h, a.h), p1 = __fmul2_rn(b.h, b.h), p2 = __fmul2_rn(c.h, c.h);
@@ -500,7 +492,7 @@ __device__ __forceinline__ df2 df_sqr3_2(df2 a, df2 b, df2 c) {
     lo = __ffma2_rn(__fadd2_rn(c.h, c.h), c.l, lo);
     const df2 s01 = two_sum2(p0, p1);
     const df2 s = two_sum2(s01.h, p2);
-    return quick_two_sum2(s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo));
+    return {s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo)};
 }
 __device__ __forceinline__ df2 df_rsqrt2(df2 x) {
     const float2 y = make_float2(rsqrt_mufu(x.h.x), rsqrt_mufu(x.h.y));
@@ -510,7 +502,7 @@ __device__ __forceinline__ df2 df_rsqrt2(df2 x) {
     const float2 pe = __ffma2_rn(x.h, yy, neg2(p));
     const float2 one = make_float2(1.0f, 1.0f);
     const float2 e = sub2(sub2(sub2(one, p), pe), __ffma2_rn(x.h, yye, __fmul2_rn(x.l, yy)));
-    return quick_two_sum2(y, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), y), e));
+    return {y, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), y), e)};
 }
 __device__ __forceinline__ void df_acc2(float2& ah, float2& al, df2 v) {
     const df2 s = two_sum2(ah, v.h);
@@ -572,22 +564,25 @@ __global__ void __launch_bounds__(kFarThreads, 3)
         const df2 ri3 = df_mul_u2(ri2, ri);
         if (TRAC) {  // (r.f)(r.n) r / r^5
             const df2 rn = df_dot3_2(rx, n0, ry, n1, rz, n2);
-            const df2 k5 = df_mul2(df_mul_u2(rf, rn), df_mul_u2(ri3, ri2));
+            const df2 k5 = df_mul_u2(df_mul_u2(rf, rn), df_mul_u2(ri3, ri2));
             df_acc2(xh, xl, df_mul_u2(k5, rx));
             df_acc2(yh, yl, df_mul_u2(k5, ry));
             df_acc2(zh, zl, df_mul_u2(k5, rz));
         }
         if (SL) {  // f / r + (r.f) r / r^3
-            const df2 k3 = df_mul2(rf, ri3);
+            const df2 k3 = df_mul_u2(rf, ri3);
             float2& ah = KIND == 2 ? sxh : xh;
             float2& al = KIND == 2 ? sxl : xl;
             float2& bh = KIND == 2 ? syh : yh;
             float2& bl = KIND == 2 ? syl : yl;
             float2& ch = KIND == 2 ? szh : zh;
             float2& cl = KIND == 2 ? szl : zl;
-            df_acc2(ah, al, df_add2(df_mul_u2(f0, ri), df_mul_u2(k3, rx)));
-            df_acc2(bh, bl, df_add2(df_mul_u2(f1, ri), df_mul_u2(k3, ry)));
-            df_acc2(ch, cl, df_add2(df_mul_u2(fz, ri), df_mul_u2(k3, rz)));
+            df_acc2(ah, al, df_mul_u2(f0, ri));
+            df_acc2(ah, al, df_mul_u2(k3, rx));
+            df_acc2(bh, bl, df_mul_u2(f1, ri));
+            df_acc2(bh, bl, df_mul_u2(k3, ry));
+            df_acc2(ch, cl, df_mul_u2(fz, ri));
+            df_acc2(ch, cl, df_mul_u2(k3, rz));
         }
     };
     for (int s = it.s0; s < it.s1; ++s) {
