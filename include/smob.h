@@ -75,6 +75,9 @@ typedef struct {
     int precision;     /* smob_precision */
     int warm_start;    /* nonzero: start from the previous solution of each problem (SphereSTKMobMat.cpp:222) */
     double inner_tol;  /* MIXED only: relative tolerance of each FP32 inner solve (<= 0: library default 1e-5) */
+    int precond;       /* 0: none (the reference's unpreconditioned GMRES); 1: right preconditioner that inverts
+                          every sphere's own I/2 + K_PV + L exactly (block diagonal in the spherical-harmonic
+                          basis). Same solution to the tolerance, fewer iterations, different Krylov path. */
 } smob_solve_opts;
 
 typedef struct {

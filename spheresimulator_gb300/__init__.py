@@ -31,10 +31,12 @@ def spectral_dof(p):
     return 3 * (p + 1) * (p + 2)
 
 
-def solve_opts(tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False, inner_tol=0.0):
-    """GMRES settings (mobilitySolver.yaml:3-16 names: Convergence Tolerance, Num Blocks, Maximum Iterations)."""
+def solve_opts(tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False, inner_tol=0.0,
+               precond=0):
+    """GMRES settings (mobilitySolver.yaml:3-16 names: Convergence Tolerance, Num Blocks, Maximum Iterations);
+    precond=1 adds the block-diagonal right preconditioner (each sphere's own operator inverted)."""
     return N.SolveOpts(float(tol), int(restart), int(max_iters), int(precision), int(bool(warm_start)),
-                       float(inner_tol))
+                       float(inner_tol), int(precond))
 
 
 class _Context:
@@ -352,7 +354,7 @@ class SphereSTKMobMat(SphereSTKSHOperator):
         self.last_stats = None
 
     def solveMob(self, force, tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False,
-                 inner_tol=0.0, want_density=True, raise_on_not_converged=True):
+                 inner_tol=0.0, want_density=True, raise_on_not_converged=True, precond=0):
         """force (6N) -> velocity (6N); also keeps rho+mu (getDensitySolution)."""
         force = N.f64(force).reshape(-1)
         if force.shape[0] != 6 * self.n_spheres:
@@ -360,7 +362,7 @@ class SphereSTKMobMat(SphereSTKSHOperator):
         vel = np.zeros(6 * self.n_spheres)
         dens = np.zeros(3 * self.n_points) if want_density else None
         stats = (N.ProblemStats * self.n_problems)()
-        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol)
+        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol, precond)
         code = self._L.smob_solve_mob(self._h, N.dptr(force), N.dptr(vel), N.dptr(dens), ctypes.byref(opts), stats)
         allow = () if raise_on_not_converged else (N.SMOB_ERR_NOT_CONVERGED,)
         N.check(code, allow)
@@ -369,7 +371,7 @@ class SphereSTKMobMat(SphereSTKSHOperator):
         return vel
 
     def solveMobMulti(self, forces, tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False,
-                      inner_tol=0.0, want_density=False, raise_on_not_converged=True):
+                      inner_tol=0.0, want_density=False, raise_on_not_converged=True, precond=0):
         """forces [K][6N] -> velocities [K][6N]: K right-hand sides on this geometry solved together
         (the columns SphereSTKMobMat::apply solves one by one, BIE/SphereSTKMobMat.cpp:129-143)."""
         F = np.ascontiguousarray(N.f64(forces).reshape(-1, 6 * self.n_spheres))
@@ -377,7 +379,7 @@ class SphereSTKMobMat(SphereSTKSHOperator):
         vel = np.zeros_like(F)
         dens = np.zeros((k, 3 * self.n_points)) if want_density else None
         stats = (N.ProblemStats * k)()
-        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol)
+        opts = solve_opts(tol, restart, max_iters, precision, warm_start, inner_tol, precond)
         code = self._L.smob_solve_mob_multi(self._h, k, N.dptr(F), N.dptr(vel), N.dptr(dens), ctypes.byref(opts),
                                             stats)
         allow = () if raise_on_not_converged else (N.SMOB_ERR_NOT_CONVERGED,)

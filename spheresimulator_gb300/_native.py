@@ -39,7 +39,8 @@ class Geometry(ctypes.Structure):
 
 class SolveOpts(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("restart", ctypes.c_int), ("max_iters", ctypes.c_int),
-                ("precision", ctypes.c_int), ("warm_start", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+                ("precision", ctypes.c_int), ("warm_start", ctypes.c_int), ("inner_tol", ctypes.c_double),
+                ("precond", ctypes.c_int)]
 
 
 class ProblemStats(ctypes.Structure):

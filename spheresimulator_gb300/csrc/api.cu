@@ -160,6 +160,7 @@ struct smob_ctx {
     DBuf d_V, d_w, d_r, d_x, d_xlast, d_b, d_rho, d_u, d_force, d_vel;
     // mixed solve: rho + x, and the single layer of rho + x_hp at the last high-precision residual x_hp
     DBuf d_dens, d_uhp, d_xhp, d_partial64_sl;
+    DBuf d_pz;  // preconditioned vector P v
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
     bool have_xlast = false;
 
@@ -967,6 +968,19 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     unsigned char* act = c->d_active.as<unsigned char>();
     unsigned char* incyc = c->d_incycle.as<unsigned char>();
     KrylovState* ks = c->d_ks.as<KrylovState>();
+    // Optional right preconditioner P: per sphere the exact inverse of its own I/2 + K_PV + L
+    // (block diagonal, one sphere-kernel pass in the cycle precision). GMRES then builds its
+    // Krylov space for A P while every residual stays that of A x = b.
+    const bool pc = o->precond != 0;
+    double* pz = nullptr;
+    if (pc) {
+        c->d_pz.alloc(sizeof(double) * n);
+        pz = c->d_pz.as<double>();
+    }
+    auto apply_precond = [&](const double* in, double* out) {
+        CUDA_OK(cudaMemsetAsync(out, 0, sizeof(double) * n, st));
+        check_launch(c, launch_sphere_op(c->g, in, out, 2.0, 1.0, 4, 0.0, nullptr, cyc_prec == OP_FP32, st));
+    };
 
     std::vector<unsigned char> all(P, 1);
     set_active(c, all);
@@ -1075,6 +1089,10 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         // later work through the active flags)
         auto step = [&](int j) {
             const double* Vj = V + n * j;
+            if (pc) {  // right preconditioning: w = A P V_j
+                apply_precond(Vj, pz);
+                Vj = pz;
+            }
             CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
             op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, cyc_prec);
             double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
@@ -1099,7 +1117,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         for (int j0 = 0; j0 < m; j0 += blk) {
             const int cnt = std::min(blk, m - j0);
             if (graphs) {
-                const long long key = ((long long)cyc_prec * 4096 + m) * 4096 + j0;
+                const long long key = (((long long)cyc_prec * 2 + (pc ? 1 : 0)) * 4096 + m) * 4096 + j0;
                 auto it = c->graphs.find(key);
                 if (it == c->graphs.end()) {
                     const long long before = c->launches;
@@ -1128,7 +1146,12 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         set_active(c, cyc);
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
         check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, w, st));
-        check_launch(c, launch_axpby_seg(L, 1.0, w, 1.0, act, x, st));
+        double* dx = w;  // the correction of this cycle: V y, or P V y when preconditioned
+        if (pc) {
+            apply_precond(w, pz);
+            dx = pz;
+        }
+        check_launch(c, launch_axpby_seg(L, 1.0, dx, 1.0, act, x, st));
         // Residual, decided per problem (so a problem takes the same steps alone or in any batch).
         // FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos' restart).
         // MIXED, once the previous high-precision residual is below 1e-4 |b|: r <- r - A32 d, whose
@@ -1145,7 +1168,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         if (any_upd) {
             set_active(c, upd);
             CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-            op_apply(c, w, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
+            op_apply(c, dx, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
             check_launch(c, launch_axpby_seg(L, -1.0, u, 1.0, act, r, st));
             for (int p = 0; p < P; ++p)
                 if (upd[p]) passes32x[p]++, x_moved[p] = 1;
@@ -1707,6 +1730,7 @@ static smob_status check_opts(const smob_solve_opts* o) {
     if (!(o->tol > 0) || o->restart < 1 || o->max_iters < 1) throw SmobError(SMOB_ERR_ARG, "invalid solve options");
     if (o->precision != SMOB_PREC_FP64 && o->precision != SMOB_PREC_MIXED && o->precision != SMOB_PREC_FLOAT_FLOAT)
         throw SmobError(SMOB_ERR_ARG, "unknown precision");
+    if (o->precond != 0 && o->precond != 1) throw SmobError(SMOB_ERR_ARG, "unknown preconditioner");
     return SMOB_OK;
 }
 

@@ -122,7 +122,8 @@ int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int 
                         double* partial, double* partial_sl, cudaStream_t st);
 
 // Per-sphere operator: out += c_id*x + c_self*Self[x] + c_lop*L[x]; coefficients of x written to coef
-// (self_kind: -1 none, 0 single layer, 3 traction principal value).
+// (self_kind: -1 none, 0 single layer, 3 traction principal value, 4 inverse of the sphere's own
+// I/2 + K_PV + L minus 2 I, used with c_id = 2 as the block-diagonal preconditioner).
 int launch_sphere_op(const DevGeom& g, const double* x, double* out, double c_id, double c_self, int self_kind,
                      double c_lop, void* coef, bool fp32, cudaStream_t st);
 void configure_sphere_kernels();

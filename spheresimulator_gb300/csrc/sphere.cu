@@ -65,7 +65,7 @@ struct SphereArgs {
     const double* coef_in;  // coefficient input (S2G), double complex
     double* out;            // grid output
     double c_id, c_self, c_lop;
-    int self_kind;          // -1 none, 0 single layer, 3 traction PV
+    int self_kind;          // -1 none, 0 single layer, 3 traction PV, 4 block-diagonal preconditioner
     int mode;               // 0 OP, 1 G2S, 2 S2G
     void* coef_out;         // coefficient output (Real complex in OP, double in G2S), may be null
 };
@@ -219,6 +219,17 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
                     lh = dn / ((2 * dn + 1) * (2 * dn + 3));
                     lg = (dn + 1) / ((2 * dn - 1) * (2 * dn + 1));
                     lx = Real(1) / (2 * dn + 1);
+                } else if (a.self_kind == 4) {
+                    // block-diagonal preconditioner: the inverse of the sphere's own I/2 + K_PV + L,
+                    // minus the 2 I that c_id = 2 adds on the grid (that 2 I also inverts the I/2 the
+                    // operator applies to the part of a grid field beyond degree p). L is the identity
+                    // on the rigid modes (n = 1 G: translations, n = 1 X: rotations), zero elsewhere.
+                    const Real dh = Real(0.5) + Real(3) / (2 * (2 * dn + 1) * (2 * dn + 3));
+                    const Real dg = n == 1 ? Real(1) : Real(0.5) - Real(3) / (2 * (2 * dn - 1) * (2 * dn + 1));
+                    const Real dx = n == 1 ? Real(1) : Real(0.5) - Real(3) / (2 * (2 * dn + 1));
+                    lh = Real(1) / dh - 2;
+                    lg = Real(1) / dg - 2;
+                    lx = Real(1) / dx - 2;
                 } else {
                     lh = Real(3) / (2 * (2 * dn + 1) * (2 * dn + 3));
                     lg = Real(-3) / (2 * (2 * dn - 1) * (2 * dn + 1));

@@ -71,5 +71,5 @@ def test_structures_match_header():
     """ctypes mirrors of smob_geometry / smob_solve_opts / smob_problem_stats have the C layout."""
     from spheresimulator_gb300 import _native as N
     assert ctypes.sizeof(N.Geometry) == 56
-    assert ctypes.sizeof(N.SolveOpts) == 32
+    assert ctypes.sizeof(N.SolveOpts) == 40
     assert ctypes.sizeof(N.ProblemStats) == 40
