@@ -547,7 +547,8 @@ def run_reference(args, rank):
            "sample": "per step: one FP64 operator pass (0.5I+K+L) of the full cfg2 workload, times %d passes "
                      "(iterations + b + restart residual + final single layer of one full oracle solve at 1e-8)"
                      % passes}
-    return {"metric": METRIC, "value": round(value, 6), "unit": "solves/s", "impl": "reference", "n_gpus": 0,
+    return {"metric": METRIC, "value": round(value, 6), "unit": "solves/s", "impl": "reference",
+            "n_gpus": args.gpus, "cpu_threads": nthreads,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(ts.mean() * 1e3), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded RSA packing, N(0,1) forces)",

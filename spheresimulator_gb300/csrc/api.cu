@@ -868,9 +868,14 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
     }
     {
         ProfScope ps(c, "far_both_df", fs);
-        check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
-                                            c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
-                                            c->d_partial64_sl.as<double>(), fs));
+        if (c->nrep > 1)
+            check_launch(c, launch_far_field_df_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
+                                                    c->rep_M, c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
+                                                    c->d_partial64_sl.as<double>(), fs));
+        else
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
+                                                c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
+                                                c->d_partial64_sl.as<double>(), fs));
     }
     {
         ProfScope ps(c, "sphere_self");

@@ -453,61 +453,86 @@ __global__ void __launch_bounds__(kFarThreads) k_far64(DevGeom g, const FarItem*
 // advances two pairs, which halves the issue slots the error-free transformations take.
 // The _rn intrinsics keep every rounding explicit: the compiler may not contract a product into a
 // later addition, which would break the error-free transformations below.
-struct df2 {
-    float2 h, l;
+// Elementwise primitives on one float or on two packed lanes (float2 -> FP32x2 instructions), every
+// rounding explicit; a lane of a packed operation rounds exactly like the scalar one, so the scalar
+// and packed forms of each helper below agree bit for bit per lane.
+__device__ __forceinline__ float v_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float v_neg(float a) { return -a; }
+__device__ __forceinline__ float v_sub(float a, float b) { return __fadd_rn(a, -b); }
+__device__ __forceinline__ float v_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float v_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float v_rsqrt(float a) { return rsqrt_mufu(a); }
+__device__ __forceinline__ float v_c(float, float c) { return c; }
+__device__ __forceinline__ float2 v_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 v_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 v_sub(float2 a, float2 b) { return __fadd2_rn(a, v_neg(b)); }
+__device__ __forceinline__ float2 v_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 v_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 v_rsqrt(float2 a) { return make_float2(rsqrt_mufu(a.x), rsqrt_mufu(a.y)); }
+__device__ __forceinline__ float2 v_c(float2, float c) { return make_float2(c, c); }
+
+template <typename T>
+struct dfv {
+    T h, l;
 };
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
-__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
-    const float2 s = __fadd2_rn(a, b);
-    const float2 bb = sub2(s, a);
-    return {s, __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb))};
+using df2 = dfv<float2>;
+using df1 = dfv<float>;
+
+template <typename T>
+__device__ __forceinline__ dfv<T> two_sum(T a, T b) {
+    const T s = v_add(a, b);
+    const T bb = v_sub(s, a);
+    return {s, v_add(v_sub(a, v_sub(s, bb)), v_sub(b, bb))};
 }
 // Products, dot products, squares and the reciprocal square root return unnormalised pairs
 // (|lo| up to a few ulp of hi instead of half an ulp): every result feeds further products or the
 // two_sum accumulators, whose error bounds this leaves at ~2^-44 relative, far below the 1e-10 the
 // refinement residuals need, and each skipped renormalisation saves three instructions.
-__device__ __forceinline__ df2 df_mul_u2(df2 a, df2 b) {
-    const float2 p = __fmul2_rn(a.h, b.h);
-    const float2 e = __ffma2_rn(a.h, b.h, neg2(p));
-    return {p, __ffma2_rn(a.h, b.l, __ffma2_rn(a.l, b.h, e))};
+template <typename T>
+__device__ __forceinline__ dfv<T> df_mul_u(dfv<T> a, dfv<T> b) {
+    const T p = v_mul(a.h, b.h);
+    const T e = v_fma(a.h, b.h, v_neg(p));
+    return {p, v_fma(a.h, b.l, v_fma(a.l, b.h, e))};
 }
-__device__ __forceinline__ df2 df_dot3_2(df2 a, df2 b, df2 c, df2 d, df2 e, df2 f) {
-    const float2 p0 = __fmul2_rn(a.h, b.h), p1 = __fmul2_rn(c.h, d.h), p2 = __fmul2_rn(e.h, f.h);
-    float2 lo = __fadd2_rn(__fadd2_rn(__ffma2_rn(a.h, b.h, neg2(p0)), __ffma2_rn(c.h, d.h, neg2(p1))),
-                           __ffma2_rn(e.h, f.h, neg2(p2)));
-    lo = __ffma2_rn(a.h, b.l, __ffma2_rn(a.l, b.h, lo));
-    lo = __ffma2_rn(c.h, d.l, __ffma2_rn(c.l, d.h, lo));
-    lo = __ffma2_rn(e.h, f.l, __ffma2_rn(e.l, f.h, lo));
-    const df2 s01 = two_sum2(p0, p1);
-    const df2 s = two_sum2(s01.h, p2);
-    return {s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo)};
+template <typename T>
+__device__ __forceinline__ dfv<T> df_dot3(dfv<T> a, dfv<T> b, dfv<T> c, dfv<T> d, dfv<T> e, dfv<T> f) {
+    const T p0 = v_mul(a.h, b.h), p1 = v_mul(c.h, d.h), p2 = v_mul(e.h, f.h);
+    T lo = v_add(v_add(v_fma(a.h, b.h, v_neg(p0)), v_fma(c.h, d.h, v_neg(p1))), v_fma(e.h, f.h, v_neg(p2)));
+    lo = v_fma(a.h, b.l, v_fma(a.l, b.h, lo));
+    lo = v_fma(c.h, d.l, v_fma(c.l, d.h, lo));
+    lo = v_fma(e.h, f.l, v_fma(e.l, f.h, lo));
+    const dfv<T> s01 = two_sum(p0, p1);
+    const dfv<T> s = two_sum(s01.h, p2);
+    return {s.h, v_add(v_add(s.l, s01.l), lo)};
 }
-__device__ __forceinline__ df2 df_sqr3_2(df2 a, df2 b, df2 c) {
-    const float2 p0 = __fmul2_rn(a.h, a.h), p1 = __fmul2_rn(b.h, b.h), p2 = __fmul2_rn(c.h, c.h);
-    float2 lo = __fadd2_rn(__fadd2_rn(__ffma2_rn(a.h, a.h, neg2(p0)), __ffma2_rn(b.h, b.h, neg2(p1))),
-                           __ffma2_rn(c.h, c.h, neg2(p2)));
-    lo = __ffma2_rn(__fadd2_rn(a.h, a.h), a.l, lo);
-    lo = __ffma2_rn(__fadd2_rn(b.h, b.h), b.l, lo);
-    lo = __ffma2_rn(__fadd2_rn(c.h, c.h), c.l, lo);
-    const df2 s01 = two_sum2(p0, p1);
-    const df2 s = two_sum2(s01.h, p2);
-    return {s.h, __fadd2_rn(__fadd2_rn(s.l, s01.l), lo)};
+template <typename T>
+__device__ __forceinline__ dfv<T> df_sqr3(dfv<T> a, dfv<T> b, dfv<T> c) {
+    const T p0 = v_mul(a.h, a.h), p1 = v_mul(b.h, b.h), p2 = v_mul(c.h, c.h);
+    T lo = v_add(v_add(v_fma(a.h, a.h, v_neg(p0)), v_fma(b.h, b.h, v_neg(p1))), v_fma(c.h, c.h, v_neg(p2)));
+    lo = v_fma(v_add(a.h, a.h), a.l, lo);
+    lo = v_fma(v_add(b.h, b.h), b.l, lo);
+    lo = v_fma(v_add(c.h, c.h), c.l, lo);
+    const dfv<T> s01 = two_sum(p0, p1);
+    const dfv<T> s = two_sum(s01.h, p2);
+    return {s.h, v_add(v_add(s.l, s01.l), lo)};
 }
-__device__ __forceinline__ df2 df_rsqrt2(df2 x) {
-    const float2 y = make_float2(rsqrt_mufu(x.h.x), rsqrt_mufu(x.h.y));
-    const float2 yy = __fmul2_rn(y, y);
-    const float2 yye = __ffma2_rn(y, y, neg2(yy));
-    const float2 p = __fmul2_rn(x.h, yy);
-    const float2 pe = __ffma2_rn(x.h, yy, neg2(p));
-    const float2 one = make_float2(1.0f, 1.0f);
-    const float2 e = sub2(sub2(sub2(one, p), pe), __ffma2_rn(x.h, yye, __fmul2_rn(x.l, yy)));
-    return {y, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), y), e)};
+template <typename T>
+__device__ __forceinline__ dfv<T> df_rsqrt(dfv<T> x) {
+    const T y = v_rsqrt(x.h);
+    const T yy = v_mul(y, y);
+    const T yye = v_fma(y, y, v_neg(yy));
+    // x*y^2 = 1 - e, evaluated to double-float accuracy; one Newton step squares the error
+    const T p = v_mul(x.h, yy);
+    const T pe = v_fma(x.h, yy, v_neg(p));
+    const T e = v_sub(v_sub(v_sub(v_c(y, 1.0f), p), pe), v_fma(x.h, yye, v_mul(x.l, yy)));
+    return {y, v_mul(v_mul(v_c(y, 0.5f), y), e)};
 }
-__device__ __forceinline__ void df_acc2(float2& ah, float2& al, df2 v) {
-    const df2 s = two_sum2(ah, v.h);
+// accumulator: hi part by two_sum, lo parts summed and folded in at the end
+template <typename T>
+__device__ __forceinline__ void df_acc(T& ah, T& al, dfv<T> v) {
+    const dfv<T> s = two_sum(ah, v.h);
     ah = s.h;
-    al = __fadd2_rn(al, __fadd2_rn(s.l, v.l));
+    al = v_add(al, v_add(s.l, v.l));
 }
 
 // KIND: 0 single layer -> partial; 1 traction -> partial; 2 both from the same sources in one pass
@@ -545,9 +570,9 @@ __global__ void __launch_bounds__(kFarThreads, 3)
     // one source against the two packed targets (mx, my, mz); keep scales the source weight per lane
     auto pair = [&](const df2& mx, const df2& my, const df2& mz, const float4& qh, const float4& ql,
                     const float4& fh, const float4& fl, bool masked, float2 keep) {
-        const df2 dx = two_sum2(mx.h, f2(-qh.x, -qh.x));
-        const df2 dy = two_sum2(my.h, f2(-qh.y, -qh.y));
-        const df2 dz = two_sum2(mz.h, f2(-qh.z, -qh.z));
+        const df2 dx = two_sum(mx.h, f2(-qh.x, -qh.x));
+        const df2 dy = two_sum(my.h, f2(-qh.y, -qh.y));
+        const df2 dz = two_sum(mz.h, f2(-qh.z, -qh.z));
         const df2 rx{dx.h, __fadd2_rn(dx.l, __fadd2_rn(mx.l, f2(-ql.x, -ql.x)))};
         const df2 ry{dy.h, __fadd2_rn(dy.l, __fadd2_rn(my.l, f2(-ql.y, -ql.y)))};
         const df2 rz{dz.h, __fadd2_rn(dz.l, __fadd2_rn(mz.l, f2(-ql.z, -ql.z)))};
@@ -557,32 +582,32 @@ __global__ void __launch_bounds__(kFarThreads, 3)
             f1 = {__fmul2_rn(f1.h, keep), __fmul2_rn(f1.l, keep)};
             fz = {__fmul2_rn(fz.h, keep), __fmul2_rn(fz.l, keep)};
         }
-        const df2 r2 = df_sqr3_2(rx, ry, rz);
-        const df2 ri = df_rsqrt2(r2);
-        const df2 rf = df_dot3_2(rx, f0, ry, f1, rz, fz);
-        const df2 ri2 = df_mul_u2(ri, ri);
-        const df2 ri3 = df_mul_u2(ri2, ri);
+        const df2 r2 = df_sqr3(rx, ry, rz);
+        const df2 ri = df_rsqrt(r2);
+        const df2 rf = df_dot3(rx, f0, ry, f1, rz, fz);
+        const df2 ri2 = df_mul_u(ri, ri);
+        const df2 ri3 = df_mul_u(ri2, ri);
         if (TRAC) {  // (r.f)(r.n) r / r^5
-            const df2 rn = df_dot3_2(rx, n0, ry, n1, rz, n2);
-            const df2 k5 = df_mul_u2(df_mul_u2(rf, rn), df_mul_u2(ri3, ri2));
-            df_acc2(xh, xl, df_mul_u2(k5, rx));
-            df_acc2(yh, yl, df_mul_u2(k5, ry));
-            df_acc2(zh, zl, df_mul_u2(k5, rz));
+            const df2 rn = df_dot3(rx, n0, ry, n1, rz, n2);
+            const df2 k5 = df_mul_u(df_mul_u(rf, rn), df_mul_u(ri3, ri2));
+            df_acc(xh, xl, df_mul_u(k5, rx));
+            df_acc(yh, yl, df_mul_u(k5, ry));
+            df_acc(zh, zl, df_mul_u(k5, rz));
         }
         if (SL) {  // f / r + (r.f) r / r^3
-            const df2 k3 = df_mul_u2(rf, ri3);
+            const df2 k3 = df_mul_u(rf, ri3);
             float2& ah = KIND == 2 ? sxh : xh;
             float2& al = KIND == 2 ? sxl : xl;
             float2& bh = KIND == 2 ? syh : yh;
             float2& bl = KIND == 2 ? syl : yl;
             float2& ch = KIND == 2 ? szh : zh;
             float2& cl = KIND == 2 ? szl : zl;
-            df_acc2(ah, al, df_mul_u2(f0, ri));
-            df_acc2(ah, al, df_mul_u2(k3, rx));
-            df_acc2(bh, bl, df_mul_u2(f1, ri));
-            df_acc2(bh, bl, df_mul_u2(k3, ry));
-            df_acc2(ch, cl, df_mul_u2(fz, ri));
-            df_acc2(ch, cl, df_mul_u2(k3, rz));
+            df_acc(ah, al, df_mul_u(f0, ri));
+            df_acc(ah, al, df_mul_u(k3, rx));
+            df_acc(bh, bl, df_mul_u(f1, ri));
+            df_acc(bh, bl, df_mul_u(k3, ry));
+            df_acc(ch, cl, df_mul_u(fz, ri));
+            df_acc(ch, cl, df_mul_u(k3, rz));
         }
     };
     for (int s = it.s0; s < it.s1; ++s) {
@@ -631,6 +656,103 @@ __global__ void __launch_bounds__(kFarThreads, 3)
             q[0] = h ? double(sxh.y) + double(sxl.y) : double(sxh.x) + double(sxl.x);
             q[1] = h ? double(syh.y) + double(syl.y) : double(syh.x) + double(syl.x);
             q[2] = h ? double(szh.y) + double(szl.y) : double(szh.x) + double(szl.x);
+        }
+    }
+}
+
+// Float-float traction and single layer (the fused high-precision pass) for nrep replicas of one
+// problem (see k_far32_rep): one target per thread, replica 0's work items, KB columns per CTA.
+// The pair geometry (r, r^2, 1/r, r^-3, r^-5, r.n) is evaluated once and serves the KB columns;
+// per column the arithmetic and the source order are those of k_far_dfx2<2>, so each column's
+// sums equal bit for bit the single-problem pass on that column.
+template <int KB>
+__global__ void __launch_bounds__(kFarThreads) k_far_df_rep(DevGeom g, const FarItem* __restrict__ items, int nrep,
+                                                           int rep_M, const float4* __restrict__ src,
+                                                           double* __restrict__ partial,
+                                                           double* __restrict__ partial_sl) {
+    const FarItem it = items[blockIdx.x];
+    const int r0 = blockIdx.y * KB;
+    const int nr = min(KB, nrep - r0);
+    bool any = g.active == nullptr;
+    for (int r = 0; r < nr && !any; ++r) any = g.active[r0 + r] != 0;
+    if (!any) return;
+    __shared__ float4 sph[kRepTileDF], spl[kRepTileDF];
+    __shared__ float4 sfh[KB][kRepTileDF], sfl[KB][kRepTileDF];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int t = it.t0 + threadIdx.x;
+    const bool va = t < it.t1;
+    const float4 PH = va ? g.pos32[t] : z4, PL = va ? g.pos32lo[t] : z4;
+    const float4 NH = va ? g.nrm32[t] : z4, NL = va ? g.nrm32lo[t] : z4;
+    const int sa = va ? __float_as_int(PH.w) : -1;
+    int ca = va ? g.nbr_start[sa] : 0;
+    const int ea = va ? g.nbr_start[sa + 1] : 0;
+    const df1 n0{NH.x, NL.x}, n1{NH.y, NL.y}, n2{NH.z, NL.z};
+    float th[KB][3], tl[KB][3], sh[KB][3], sl[KB][3];
+#pragma unroll
+    for (int r = 0; r < KB; ++r)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) th[r][d] = tl[r][d] = sh[r][d] = sl[r][d] = 0.f;
+    for (int s = it.s0; s < it.s1; ++s) {
+        const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s);
+        if (__syncthreads_and(sk)) continue;
+        const int g0 = g.gidx[s], gl = g.glen[s];
+        for (int base = 0; base < gl; base += kRepTileDF) {
+            const int n = min(kRepTileDF, gl - base);
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += kFarThreads) {
+                sph[k] = g.pos32[g0 + base + k];
+                spl[k] = g.pos32lo[g0 + base + k];
+#pragma unroll
+                for (int r = 0; r < KB; ++r) {
+                    const long long i = (long long)(r0 + r) * rep_M + g0 + base + k;
+                    sfh[r][k] = r < nr ? src[2 * i] : z4;
+                    sfl[r][k] = r < nr ? src[2 * i + 1] : z4;
+                }
+            }
+            __syncthreads();
+            if (sk) continue;
+            for (int k = 0; k < n; ++k) {
+                const float4 qh = sph[k], ql = spl[k];
+                const df1 dx = two_sum(PH.x, -qh.x), dy = two_sum(PH.y, -qh.y), dz = two_sum(PH.z, -qh.z);
+                const df1 rx{dx.h, v_add(dx.l, v_add(PL.x, -ql.x))};
+                const df1 ry{dy.h, v_add(dy.l, v_add(PL.y, -ql.y))};
+                const df1 rz{dz.h, v_add(dz.l, v_add(PL.z, -ql.z))};
+                const df1 ri = df_rsqrt(df_sqr3(rx, ry, rz));
+                const df1 ri2 = df_mul_u(ri, ri);
+                const df1 ri3 = df_mul_u(ri2, ri);
+                const df1 rn = df_dot3(rx, n0, ry, n1, rz, n2);
+                const df1 ri5 = df_mul_u(ri3, ri2);
+#pragma unroll
+                for (int r = 0; r < KB; ++r) {
+                    const float4 fh = sfh[r][k], fl = sfl[r][k];
+                    const df1 f0{fh.x, fl.x}, f1{fh.y, fl.y}, fz{fh.z, fl.z};
+                    const df1 rf = df_dot3(rx, f0, ry, f1, rz, fz);
+                    const df1 k5 = df_mul_u(df_mul_u(rf, rn), ri5);
+                    df_acc(th[r][0], tl[r][0], df_mul_u(k5, rx));
+                    df_acc(th[r][1], tl[r][1], df_mul_u(k5, ry));
+                    df_acc(th[r][2], tl[r][2], df_mul_u(k5, rz));
+                    const df1 k3 = df_mul_u(rf, ri3);
+                    df_acc(sh[r][0], sl[r][0], df_mul_u(f0, ri));
+                    df_acc(sh[r][0], sl[r][0], df_mul_u(k3, rx));
+                    df_acc(sh[r][1], sl[r][1], df_mul_u(f1, ri));
+                    df_acc(sh[r][1], sl[r][1], df_mul_u(k3, ry));
+                    df_acc(sh[r][2], sl[r][2], df_mul_u(fz, ri));
+                    df_acc(sh[r][2], sl[r][2], df_mul_u(k3, rz));
+                }
+            }
+        }
+    }
+    if (!va) return;
+#pragma unroll
+    for (int r = 0; r < KB; ++r) {
+        if (r < nr) {
+            const Problem pr = g.problems[r0 + r];
+            const long long off = pr.poff + 3LL * (pr.p1 - pr.p0) * it.chunk + 3LL * t;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                partial[off + d] = double(th[r][d]) + double(tl[r][d]);
+                partial_sl[off + d] = double(sh[r][d]) + double(sl[r][d]);
+            }
         }
     }
 }
@@ -733,6 +855,18 @@ int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int
     if (nrep <= 2) launch_rep<2>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
     else if (nrep <= 4) launch_rep<4>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
     else launch_rep<8>(g, items, nitems, nrep, rep_M, trac, src32, partial, st);
+    return 1;
+}
+
+int launch_far_field_df_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M,
+                            const float4* src2, double* partial, double* partial_sl, cudaStream_t st) {
+    if (nitems <= 0 || nrep <= 0) return 0;
+    if (nrep <= 2) {
+        k_far_df_rep<2><<<dim3(nitems, 1), kFarThreads, 0, st>>>(g, items, nrep, rep_M, src2, partial, partial_sl);
+    } else {
+        k_far_df_rep<4><<<dim3(nitems, (nrep + 3) / 4), kFarThreads, 0, st>>>(g, items, nrep, rep_M, src2, partial,
+                                                                            partial_sl);
+    }
     return 1;
 }
 

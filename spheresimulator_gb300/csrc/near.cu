@@ -60,12 +60,17 @@ __global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real
     }
 }
 
-template <typename Real, int NS>
-__device__ __forceinline__ void contract(const Real* __restrict__ set, int idx, Real tr, Real ti, Real* acc) {
-    const Real* c = set + 2 * NS * idx;
-#pragma unroll
-    for (int k = 0; k < NS; ++k) acc[k] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[k]));
-}
+// (re, im) of one coefficient as one 8- or 16-byte load (the sets of a harmonic are (re, im) pairs)
+template <typename Real>
+struct Cplx;
+template <>
+struct Cplx<float> {
+    using T = float2;
+};
+template <>
+struct Cplx<double> {
+    using T = double2;
+};
 
 // One target point per group of LANES lanes. Every lane runs the (cheap) harmonic recurrence;
 // lane l contracts only the coefficient sets k = l, l + LANES, ..., so the lanes of a group read
@@ -78,11 +83,14 @@ __device__ __forceinline__ void contract(const Real* __restrict__ set, int idx, 
 template <typename Real, int NS, int LANES>
 __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, Real tr, Real ti,
                                               Real* acc) {
-    const Real* c = set + 2 * NS * idx;
+    const typename Cplx<Real>::T* c = reinterpret_cast<const typename Cplx<Real>::T*>(set + 2 * NS * idx);
 #pragma unroll
     for (int s = 0; s < (NS + LANES - 1) / LANES; ++s) {
         const int k = lane + LANES * s;
-        if (k < NS) acc[s] = fma(__ldg(c + 2 * k), tr, fma(-__ldg(c + 2 * k + 1), ti, acc[s]));
+        if (k < NS) {
+            const typename Cplx<Real>::T v = __ldg(c + k);
+            acc[s] = fma(v.x, tr, fma(-v.y, ti, acc[s]));
+        }
     }
 }
 

@@ -26,6 +26,7 @@ constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
 constexpr int kFarTile = 256;            // sources staged per shared-memory tile (FP64 / float-float)
 constexpr int kFarTile32 = 640;          // FP32 tile: a whole p <= 16 sphere (578 points) in one round
 constexpr int kRepTile = 256;            // several-RHS FP32 tile (positions + up to 8 source columns)
+constexpr int kRepTileDF = 128;          // several-RHS float-float tile (hi/lo positions + up to 4 columns)
 constexpr int kSphereThreads = 256;      // per-sphere transform CTA
 constexpr int kNearThreads = 128;        // near-field CTA (one target point per thread)
 constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
@@ -120,6 +121,10 @@ int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int
 int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2, cudaStream_t st);
 int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int kind, const float4* src2,
                         double* partial, double* partial_sl, cudaStream_t st);
+// the fused float-float pass (traction -> partial, single layer -> partial_sl) for nrep replicas of one
+// problem; items are replica 0's (kFarThreads targets each)
+int launch_far_field_df_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M,
+                            const float4* src2, double* partial, double* partial_sl, cudaStream_t st);
 
 // Per-sphere operator: out += c_id*x + c_self*Self[x] + c_lop*L[x]; coefficients of x written to coef
 // (self_kind: -1 none, 0 single layer, 3 traction principal value, 4 inverse of the sphere's own
