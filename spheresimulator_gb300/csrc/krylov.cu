@@ -61,6 +61,11 @@ __global__ void k_chunk_finalize(const Problem* __restrict__ probs, int P, const
     }
 }
 
+// Elementwise kernels: grid (chunk, kElemBlocks), one element per thread, so a small problem's
+// few chunks still spread over the whole GPU. Per element the arithmetic is independent of the grid.
+constexpr int kElemThreads = 256;
+constexpr int kElemBlocks = kVecChunk / kElemThreads;
+
 // w[l] += sign * sum_{i < n_p} h[p*hstride + i] * V[i*ldv + l]
 __global__ void k_chunk_update(const VecChunk* __restrict__ chunks, const double* __restrict__ V, long long ldv,
                                int nvec, const int* __restrict__ nvec_p, const double* __restrict__ h,
@@ -68,13 +73,13 @@ __global__ void k_chunk_update(const VecChunk* __restrict__ chunks, const double
                                double* __restrict__ w) {
     const VecChunk ch = chunks[blockIdx.x];
     if (active && !active[ch.problem]) return;
+    const long long l = ch.l0 + (long long)blockIdx.y * kElemThreads + threadIdx.x;
+    if (l >= ch.l1) return;
     const int n = nvec_p ? nvec_p[ch.problem] : nvec;
     const double* hp = h + hstride * ch.problem;
-    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) {
-        double s = 0;
-        for (int i = 0; i < n; ++i) s = fma(hp[i], V[ldv * i + l], s);
-        w[l] = fma(sign, s, w[l]);
-    }
+    double s = 0;
+    for (int i = 0; i < n; ++i) s = fma(hp[i], V[ldv * i + l], s);
+    w[l] = fma(sign, s, w[l]);
 }
 
 // dst[l] = src[l] * f(p) with f = 1/val[p] (invert) or val[p]
@@ -83,9 +88,11 @@ __global__ void k_chunk_scale(const VecChunk* __restrict__ chunks, const double*
                               const unsigned char* __restrict__ active, double* __restrict__ dst) {
     const VecChunk ch = chunks[blockIdx.x];
     if (active && !active[ch.problem]) return;
+    const long long l = ch.l0 + (long long)blockIdx.y * kElemThreads + threadIdx.x;
+    if (l >= ch.l1) return;
     double f = val[vstride * ch.problem];
     if (invert) f = f != 0 ? 1.0 / f : 0.0;
-    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) dst[l] = src[l] * f;
+    dst[l] = src[l] * f;
 }
 
 // y = a*x + b*y on active problems (b == 0 overwrites)
@@ -93,8 +100,9 @@ __global__ void k_chunk_axpby(const VecChunk* __restrict__ chunks, double a, con
                               const unsigned char* __restrict__ active, double* __restrict__ y) {
     const VecChunk ch = chunks[blockIdx.x];
     if (active && !active[ch.problem]) return;
-    for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x)
-        y[l] = (b == 0.0) ? a * x[l] : fma(a, x[l], b * y[l]);
+    const long long l = ch.l0 + (long long)blockIdx.y * kElemThreads + threadIdx.x;
+    if (l >= ch.l1) return;
+    y[l] = (b == 0.0) ? a * x[l] : fma(a, x[l], b * y[l]);
 }
 
 __global__ void k_cycle_init(int P, int m, const unsigned char* __restrict__ in_cycle, const double* __restrict__ beta,
@@ -181,19 +189,21 @@ int launch_dots(const KrylovLaunch& L, const double* A, long long lda, int nvec,
 
 int launch_update(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const int* nvec_p, const double* h,
                   long long hstride, double sign, const unsigned char* active, double* w, cudaStream_t st) {
-    k_chunk_update<<<L.nchunks, 256, 0, st>>>(L.chunks, V, ldv, nvec, nvec_p, h, hstride, sign, active, w);
+    k_chunk_update<<<dim3(L.nchunks, kElemBlocks), kElemThreads, 0, st>>>(L.chunks, V, ldv, nvec, nvec_p, h, hstride,
+                                                                          sign, active, w);
     return 1;
 }
 
 int launch_scale(const KrylovLaunch& L, const double* src, const double* val, long long vstride, bool invert,
                  const unsigned char* active, double* dst, cudaStream_t st) {
-    k_chunk_scale<<<L.nchunks, 256, 0, st>>>(L.chunks, src, val, vstride, invert ? 1 : 0, active, dst);
+    k_chunk_scale<<<dim3(L.nchunks, kElemBlocks), kElemThreads, 0, st>>>(L.chunks, src, val, vstride, invert ? 1 : 0,
+                                                                         active, dst);
     return 1;
 }
 
 int launch_axpby_seg(const KrylovLaunch& L, double a, const double* x, double b, const unsigned char* active, double* y,
                      cudaStream_t st) {
-    k_chunk_axpby<<<L.nchunks, 256, 0, st>>>(L.chunks, a, x, b, active, y);
+    k_chunk_axpby<<<dim3(L.nchunks, kElemBlocks), kElemThreads, 0, st>>>(L.chunks, a, x, b, active, y);
     return 1;
 }
 
