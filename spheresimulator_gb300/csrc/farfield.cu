@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
             }
             __syncthreads();
             if (none) {
-#pragma unroll 2
+#pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const float4 A = sA[k], B = sB[k], C = sC[k];
 #pragma unroll
