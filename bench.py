@@ -619,6 +619,19 @@ def far_once():
                       np.isfinite(b).all() and np.isfinite(d).all())}))
 
 
+def near_once():
+    """One near-field pass (FP32 traction, then FP64 traction) on the first 64 problems of cfg4: the
+    batched shape, where every target point has near pairs and the kernel runs one lane per target."""
+    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
+    c = configs.cfg4(n_problems=64)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"], problem=c["problem"])
+    x = np.random.default_rng(0).standard_normal(3 * g.n_points)
+    a = g.near_field(x, cTrac=1.0, precision=PREC_MIXED)
+    b = g.near_field(x, cTrac=1.0, precision=PREC_FP64)
+    print(json.dumps({"near_once": "cfg4[:64]", "points": int(g.n_points), "near_pairs": int(g.n_near_pairs),
+                      "rel_diff_fp32_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b))}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -643,9 +656,14 @@ def main():
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
+    ap.add_argument("--near-once", action="store_true",
+                    help="one near-field pass (FP32, FP64) on 64 problems of cfg4 and exit; a short program for ncu")
     args = ap.parse_args()
     if args.far_once:
         far_once()
+        return
+    if args.near_once:
+        near_once()
         return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3

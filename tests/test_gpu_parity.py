@@ -155,6 +155,25 @@ def test_apply_cfg2_scale(oracle):
     assert rel(g.apply(x, precision=PREC_MIXED), ref) < 2e-5
 
 
+def test_mobility_properties_cfg2_scale():
+    """Cfg 2 (64 spheres, p=16, the bench workload) through size-independent properties of the
+    mobility matrix M: reciprocity F1.M F2 = F2.M F1 (M is symmetric), positive dissipation F.M F > 0,
+    and linearity M(a F1 + b F2) = a M F1 + b M F2, all to the solve tolerance, mixed precision; the
+    several-column solve gives the single solves' columns."""
+    cfg = configs.cfg2()
+    mob = make(cfg, SphereSTKMobMat)
+    rng = np.random.default_rng(5)
+    F1, F2 = rng.standard_normal((2, 6 * mob.n_spheres))
+    kw = dict(tol=1e-10, precision=PREC_MIXED, want_density=False)
+    V1, V2 = mob.solveMob(F1, **kw), mob.solveMob(F2, **kw)
+    assert abs(F1 @ V2 - F2 @ V1) < 1e-8 * np.linalg.norm(F1) * np.linalg.norm(V2)
+    assert F1 @ V1 > 0 and F2 @ V2 > 0
+    V12 = mob.solveMob(0.3 * F1 - 1.7 * F2, **kw)
+    assert rel(V12, 0.3 * V1 - 1.7 * V2) < 1e-8
+    Vm = mob.solveMobMulti(np.stack([F1, F2]), tol=1e-10, precision=PREC_MIXED)
+    assert rel(Vm[0], V1) < 1e-8 and rel(Vm[1], V2) < 1e-8
+
+
 @pytest.mark.parametrize("which", ["cfg1", "cluster"])
 def test_solve_mob_fp64(oracle, which):
     cfg = configs.cfg1() if which == "cfg1" else cluster(8, n=6, p=8)
