@@ -11,9 +11,11 @@
 // remaining smooth-quadrature part.
 //
 // Work decomposition: one CTA per work item = (block of targets of one problem) x (chunk of
-// source spheres of the same problem). Sources are staged per sphere in shared memory as
-// float4 (x,y,z,sphere-id) + float4 (f,0); each thread owns two targets (FP32) or one (FP64).
-// A per-thread merge cursor over the sorted near-pair list decides per source sphere whether
+// source spheres of the same problem). Sources are staged per sphere in shared memory; each thread
+// owns 1, 2 or 4 targets in FP32 (scalar, or packed FP32x2 lanes; the autotuner picks), 2 in
+// float-float (packed) and 1 in FP64. The several-right-hand-side kernels run one problem's work
+// items for up to 8 (FP32) or 4 (float-float) copies of it at once, evaluating each pair's geometry
+// once. A per-thread merge cursor over the sorted near-pair list decides per source sphere whether
 // the thread's target skips it; a CTA-wide vote skips the staging when every target does.
 // Partial sums go to [problem][chunk][point][3] and a second kernel reduces the chunks in
 // fixed order, so results do not depend on scheduling or on other problems in the batch.

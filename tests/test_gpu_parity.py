@@ -155,6 +155,26 @@ def test_apply_cfg2_scale(oracle):
     assert rel(g.apply(x, precision=PREC_MIXED), ref) < 2e-5
 
 
+def test_high_orders(oracle):
+    """Orders up to the library maximum p = 32 (Cfg 5 draws p = 24) with near pairs between spheres of
+    different orders: the operator and a solve match the oracle."""
+    rng = np.random.default_rng(23)
+    q = rng.standard_normal((3, 4))
+    cfg = dict(centers=np.array([[0.0, 0, 0], [2.2, 0, 0], [4.4, 0.4, 0]]), radii=np.array([1.0, 1.0, 0.9]),
+               orders=np.array([24, 32, 20]), quats=q / np.linalg.norm(q, axis=1)[:, None],
+               force=rng.standard_normal(18))
+    g = make(cfg)
+    assert g.n_near_pairs > 0
+    o = oracle_op(oracle, cfg)
+    x = np.random.default_rng(23).standard_normal(3 * g.n_points)
+    ref = o.apply(x)
+    assert rel(g.apply(x), ref) < 1e-11
+    assert rel(g.apply(x, precision=PREC_MIXED), ref) < 2e-5
+    mob = make(cfg, SphereSTKMobMat)
+    vel = mob.solveMob(cfg["force"], tol=1e-11)
+    assert rel(vel, o.solve_mob(cfg["force"], tol=1e-12)["vel"]) < 1e-8
+
+
 def test_mobility_properties_cfg2_scale():
     """Cfg 2 (64 spheres, p=16, the bench workload) through size-independent properties of the
     mobility matrix M: reciprocity F1.M F2 = F2.M F1 (M is symmetric), positive dissipation F.M F > 0,
