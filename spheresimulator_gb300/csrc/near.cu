@@ -97,18 +97,21 @@ __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int 
 template <typename Real, bool TRAC, int LANES>
 __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride,
                                                             const Real* __restrict__ th, int th_c1, int th_c2,
-                                                            int th_diag, double c, int pair_filter,
+                                                            int th_diag, double c, int pair_filter, int tile_major,
                                                             double* __restrict__ out) {
     constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
     constexpr int kNearLanes = LANES;
-    const int t = blockIdx.x;
+    // tile-major grid: the tiles of one target sphere are adjacent in launch order, so they run
+    // together and share its sources' coefficient sets through L2 instead of each fetching them
+    const int t = tile_major ? blockIdx.y : blockIdx.x;
+    const int tile = tile_major ? blockIdx.x : blockIdx.y;
     if (g.active && !g.active[g.prob[t]]) return;
     const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
     if (e0 == e1) return;
     const int lane = threadIdx.x % kNearLanes;
-    const int j = blockIdx.y * (kNearThreads / kNearLanes) + threadIdx.x / kNearLanes;
+    const int j = tile * (kNearThreads / kNearLanes) + threadIdx.x / kNearLanes;
     const int ng = g.glen[t];
-    if (blockIdx.y * (kNearThreads / kNearLanes) >= ng) return;  // whole CTA past the sphere
+    if (tile * (kNearThreads / kNearLanes) >= ng) return;  // whole CTA past the sphere
     const bool valid = j < ng;                                   // lanes stay for the shuffles
     const int i = g.gidx[t] + (valid ? j : 0);
     const double X[3] = {g.coords[3 * i], g.coords[3 * i + 1], g.coords[3 * i + 2]};
@@ -223,23 +226,25 @@ void launch_near_eval_l(const DevGeom& g, const void* sets, long long stride, bo
                         double* out, cudaStream_t st, int pair_filter) {
     const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
     const int per_cta = kNearThreads / LANES;
-    dim3 grid(g.N, (gmax + per_cta - 1) / per_cta);
+    const int tiles = (gmax + per_cta - 1) / per_cta;
+    const int tm = g.N <= 65535 ? 1 : 0;  // grid y is limited to 65535
+    const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
     if (fp32) {
         const float* s = static_cast<const float*>(sets);
         if (trac)
             k_near_eval<float, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
-                                                                           g.th_diag, c, pair_filter, out);
+                                                                           g.th_diag, c, pair_filter, tm, out);
         else
             k_near_eval<float, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
-                                                                            g.th_diag, c, pair_filter, out);
+                                                                            g.th_diag, c, pair_filter, tm, out);
     } else {
         const double* s = static_cast<const double*>(sets);
         if (trac)
             k_near_eval<double, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
-                                                                            g.th_diag, c, pair_filter, out);
+                                                                            g.th_diag, c, pair_filter, tm, out);
         else
             k_near_eval<double, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
-                                                                             g.th_diag, c, pair_filter, out);
+                                                                             g.th_diag, c, pair_filter, tm, out);
     }
 }
 
