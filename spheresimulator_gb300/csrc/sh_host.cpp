@@ -343,6 +343,10 @@ const SparseMap& near_map(int p, bool trac) {
             fill[e.first]++;
         }
     std::lock_guard<std::mutex> lk(mu);
+    // another thread (e.g. a second server worker) may have built the same map meanwhile: keep the
+    // first one, whose address earlier callers already hold
+    auto it = cache.find(key);
+    if (it != cache.end()) return *it->second;
     auto& ref = *M;
     cache[key] = std::move(M);
     return ref;

@@ -29,6 +29,22 @@ def test_server_results_equal_solo_solves():
         assert np.array_equal(vel, v)
 
 
+def test_concurrent_first_use_of_an_order():
+    """Four requests of one order that no earlier context used (p = 13) start together, so the
+    workers build that order's host tables and near maps concurrently; every result equals its solo
+    solve bit for bit."""
+    reqs = [configs.small_cluster(seed=70 + k, n=5, p=13, gap=0.15, quats=True) for k in range(4)]
+    with SolveServer(max_slots=4, precision=PREC_MIXED) as srv:
+        ids = [srv.submit(r["centers"], r["radii"], r["orders"], r["force"], tol=1e-8, quats=r["quats"])
+               for r in reqs]
+        out = [srv.wait(i, timeout=600) for i in ids]
+    for r, (vel, info) in zip(reqs, out):
+        assert info["status"] == 0
+        solo = SphereSTKMobMat(r["centers"], r["radii"], r["orders"], quats=r["quats"])
+        assert np.array_equal(vel, solo.solveMob(r["force"], tol=1e-8, restart=50, max_iters=2000,
+                                                  precision=PREC_MIXED))
+
+
 def test_server_admission_respects_budget():
     """With a budget that fits one request at a time, requests run one after another."""
     from spheresimulator_gb300 import request_bytes
