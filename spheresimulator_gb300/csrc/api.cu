@@ -1631,6 +1631,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
     return guarded([&]() -> smob_status {
         need(c && in && out, "null argument");
         set_device(c);
+        AllocStreamScope scope(c->st);  // the fused float-float path allocates its second partial buffer
         all_active(c);
         const bool fp32 = precision == SMOB_PREC_MIXED;
         const bool dfar = precision == SMOB_PREC_FLOAT_FLOAT;

@@ -254,8 +254,11 @@ smob_status smob_server_wait(smob_server* s, long long id, double timeout_s, dou
         smob::set_last_error("unknown request id");
         return SMOB_ERR_ARG;
     }
-    Request* r = it->second.get();
-    const auto pred = [&] { return r->state == 2; };
+    // look the request up again on every wake-up: another thread may release it meanwhile
+    const auto pred = [&] {
+        auto f = s->reqs.find(id);
+        return f == s->reqs.end() || f->second->state == 2;
+    };
     if (timeout_s > 0) {
         if (!s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) {
             smob::set_last_error("timed out waiting for the request");
@@ -264,6 +267,12 @@ smob_status smob_server_wait(smob_server* s, long long id, double timeout_s, dou
     } else {
         s->done_cv.wait(lk, pred);
     }
+    it = s->reqs.find(id);
+    if (it == s->reqs.end()) {
+        smob::set_last_error("request was released while waiting for it");
+        return SMOB_ERR_STATE;
+    }
+    const Request* r = it->second.get();
     fill_info(r, info);
     if (vel6n && !r->vel.empty()) std::copy(r->vel.begin(), r->vel.end(), vel6n);
     if (r->status != SMOB_OK) smob::set_last_error(r->error.c_str());
