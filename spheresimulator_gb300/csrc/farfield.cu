@@ -38,15 +38,24 @@ __device__ __forceinline__ float rcp_mufu(float x) {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+// r^-5 of a squared distance as 2^(-2.5 log2 r^2): two MUFU instructions and one multiply, where
+// rsqrt, rcp and q*q*ri take two MUFU and two multiplies (the traction pair needs no plain 1/r).
+// Relative error ~5e-7 (lg2.approx's absolute error times 2.5 ln 2, plus ex2.approx's 2 ulp).
+__device__ __forceinline__ float rpow5_mufu(float r2) {
+    float l, y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l) : "f"(r2));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-2.5f * l));
+    return y;
+}
 
 __device__ __forceinline__ void pair_trac32(const float4& t, const float4& n, const float4& s, const float4& f,
                                             float& ax, float& ay, float& az) {
     const float rx = t.x - s.x, ry = t.y - s.y, rz = t.z - s.z;
     const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-    const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
+    const float ri5 = rpow5_mufu(r2);
     const float rf = fmaf(rx, f.x, fmaf(ry, f.y, rz * f.z));
     const float rn = fmaf(rx, n.x, fmaf(ry, n.y, rz * n.z));
-    const float k = (rf * rn) * (q * q * ri);
+    const float k = (rf * rn) * ri5;
     ax = fmaf(k, rx, ax);
     ay = fmaf(k, ry, ay);
     az = fmaf(k, rz, az);
@@ -101,7 +110,7 @@ __device__ __forceinline__ bool excluded(const int* __restrict__ nbr_src, int& c
 // Blackwell issues two FP32 lanes per FFMA2/FADD2/FMUL2 instruction (__ffma2_rn & co., same
 // per-component rounding as the scalar forms). Targets are packed two per float2; each staged
 // source is stored pre-duplicated, (x,x,y,y) (z,z,fx,fx) (fy,fy,fz,fz), so three 128-bit shared
-// loads give the six broadcast operands. Per pair: ~10 packed instructions + MUFU.RSQ and MUFU.RCP.
+// loads give the six broadcast operands. Per pair: ~10 packed instructions + two MUFU instructions.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
 template <bool TRAC>
@@ -112,15 +121,16 @@ __device__ __forceinline__ void pair_x2(const float2& tx, const float2& ty, cons
     const float2 ry = __fadd2_rn(ty, f2(-A.z, -A.w));
     const float2 rz = __fadd2_rn(tz, f2(-B.x, -B.y));
     const float2 r2 = __ffma2_rn(rx, rx, __ffma2_rn(ry, ry, __fmul2_rn(rz, rz)));
-    const float2 ri = f2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y)), q = f2(rcp_mufu(r2.x), rcp_mufu(r2.y));
     const float2 rf = __ffma2_rn(rx, f2(B.z, B.w), __ffma2_rn(ry, f2(C.x, C.y), __fmul2_rn(rz, f2(C.z, C.w))));
     if (TRAC) {
+        const float2 ri5 = f2(rpow5_mufu(r2.x), rpow5_mufu(r2.y));
         const float2 rn = __ffma2_rn(rx, nx, __ffma2_rn(ry, ny, __fmul2_rn(rz, nz)));
-        const float2 k = __fmul2_rn(__fmul2_rn(rf, rn), __fmul2_rn(__fmul2_rn(q, q), ri));
+        const float2 k = __fmul2_rn(__fmul2_rn(rf, rn), ri5);
         ax = __ffma2_rn(k, rx, ax);
         ay = __ffma2_rn(k, ry, ay);
         az = __ffma2_rn(k, rz, az);
     } else {
+        const float2 ri = f2(rsqrt_mufu(r2.x), rsqrt_mufu(r2.y)), q = f2(rcp_mufu(r2.x), rcp_mufu(r2.y));
         const float2 k = __fmul2_rn(rf, __fmul2_rn(q, ri));
         ax = __ffma2_rn(f2(B.z, B.w), ri, __ffma2_rn(k, rx, ax));
         ay = __ffma2_rn(f2(C.x, C.y), ri, __ffma2_rn(k, ry, ay));
@@ -360,9 +370,8 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
                 const float4 sq = sp[k];
                 const float rx = tp.x - sq.x, ry = tp.y - sq.y, rz = tp.z - sq.z;
                 const float r2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
                 if (TRAC) {
-                    const float ri5 = q * q * ri;
+                    const float ri5 = rpow5_mufu(r2);
                     const float rn = fmaf(rx, tn.x, fmaf(ry, tn.y, rz * tn.z));
 #pragma unroll
                     for (int r = 0; r < KB; ++r) {
@@ -374,6 +383,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
                         az[r] = fmaf(kk, rz, az[r]);
                     }
                 } else {
+                    const float ri = rsqrt_mufu(r2), q = rcp_mufu(r2);
                     const float ri3 = q * ri;
 #pragma unroll
                     for (int r = 0; r < KB; ++r) {
