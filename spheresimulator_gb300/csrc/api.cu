@@ -1690,16 +1690,25 @@ smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c
             void* sets = fp32 ? c->d_sets32.p : c->d_sets64.p;
             // coefficients only: a sphere pass with no self term and no output contribution
             CUDA_OK(cudaMemsetAsync(c->d_tmp.p, 0, sizeof(double) * 3 * c->M, c->st));
-            check_launch(c, launch_sphere_op(c->g, din, c->d_tmp.as<double>(), 0.0, 0.0, 3, 0.0, coef, fp32, c->st));
+            {
+                ProfScope ps(c, "sphere_self");
+                check_launch(c, launch_sphere_op(c->g, din, c->d_tmp.as<double>(), 0.0, 0.0, 3, 0.0, coef, fp32, c->st));
+            }
             for (int k = 0; k < 2; ++k) {
                 const bool tr = k == 0;
                 const double cc = tr ? c_trac : c_sl;
                 if (cc == 0.0) continue;
                 const long long stride = tr ? c->set_stride_trac : c->set_stride_sl;
-                check_launch(c, launch_near_sets(c->g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(), stride, c->st));
+                {
+                    ProfScope ps(c, "near_sets");
+                    check_launch(c, launch_near_sets(c->g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(),
+                                                     stride, c->st));
+                }
+                ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
                 check_launch(c, launch_near_eval(c->g, sets, stride, tr, fp32, cc, dout, c->st));
             }
         });
+        prof_flush(c);
         return SMOB_OK;
     });
 }

@@ -80,27 +80,37 @@ struct Cplx<double> {
 // target points that have near pairs.
 // pair_filter: 0 every pair, 1 only pairs with gap >= 0.1 min radius, 2 only the
 // near-singular pairs (gap < 0.1 min radius).
-template <typename Real, int NS, int LANES>
-__device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, Real tr, Real ti,
-                                              Real* acc) {
+// PPT target points per thread share every coefficient load (one load, PPT complex multiply-adds).
+template <typename Real, int NS, int LANES, int PPT>
+__device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, const Real* tr,
+                                              const Real* ti, Real (*acc)[(NS + LANES - 1) / LANES]) {
     const typename Cplx<Real>::T* c = reinterpret_cast<const typename Cplx<Real>::T*>(set + 2 * NS * idx);
 #pragma unroll
     for (int s = 0; s < (NS + LANES - 1) / LANES; ++s) {
         const int k = lane + LANES * s;
         if (k < NS) {
             const typename Cplx<Real>::T v = __ldg(c + k);
-            acc[s] = fma(v.x, tr, fma(-v.y, ti, acc[s]));
+#pragma unroll
+            for (int p = 0; p < PPT; ++p) acc[p][s] = fma(v.x, tr[p], fma(-v.y, ti[p], acc[p][s]));
         }
     }
 }
 
+// Target points per thread: two in FP32 when one lane serves a target (many targets, e.g. batches),
+// so each coefficient load feeds two points and the two recurrences run side by side; one otherwise
+// (the FP64 variant would spill at the register budget that keeps 4 CTAs per SM).
+template <typename Real, int LANES>
+__host__ __device__ constexpr int near_ppt() { return (LANES == 1 && sizeof(Real) == 4) ? 2 : 1; }
+
 template <typename Real, bool TRAC, int LANES>
-__global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride,
-                                                            const Real* __restrict__ th, int th_c1, int th_c2,
-                                                            int th_diag, double c, int pair_filter, int tile_major,
-                                                            double* __restrict__ out) {
+// registers: two-point FP32 at 3 CTAs per SM (168 without spills), one-lane FP64 at 4 CTAs per SM
+__global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3 : (LANES == 1 ? 4 : 1))
+    k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride, const Real* __restrict__ th, int th_c1,
+                int th_c2, int th_diag, double c, int pair_filter, int tile_major, double* __restrict__ out) {
     constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
     constexpr int kNearLanes = LANES;
+    constexpr int PPT = near_ppt<Real, LANES>();
+    constexpr int GROUPS = kNearThreads / kNearLanes;  // target groups per CTA and per point slot
     // tile-major grid: the tiles of one target sphere are adjacent in launch order, so they run
     // together and share its sources' coefficient sets through L2 instead of each fetching them
     const int t = tile_major ? blockIdx.y : blockIdx.x;
@@ -109,17 +119,25 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
     const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
     if (e0 == e1) return;
     const int lane = threadIdx.x % kNearLanes;
-    const int j = tile * (kNearThreads / kNearLanes) + threadIdx.x / kNearLanes;
     const int ng = g.glen[t];
-    if (tile * (kNearThreads / kNearLanes) >= ng) return;  // whole CTA past the sphere
-    const bool valid = j < ng;                                   // lanes stay for the shuffles
-    const int i = g.gidx[t] + (valid ? j : 0);
-    const double X[3] = {g.coords[3 * i], g.coords[3 * i + 1], g.coords[3 * i + 2]};
-    const double Nl[3] = {g.norms[3 * i], g.norms[3 * i + 1], g.norms[3 * i + 2]};
+    if (tile * GROUPS * PPT >= ng) return;  // whole CTA past the sphere
+    bool valid[PPT];
+    int i[PPT];
+    double X[PPT][3], Nl[PPT][3], res[PPT][3];
+#pragma unroll
+    for (int p = 0; p < PPT; ++p) {
+        const int j = (tile * PPT + p) * GROUPS + threadIdx.x / kNearLanes;
+        valid[p] = j < ng;  // lanes of an invalid point stay for the shuffles
+        i[p] = g.gidx[t] + (valid[p] ? j : 0);
+        for (int d = 0; d < 3; ++d) {
+            X[p][d] = g.coords[3 * i[p] + d];
+            Nl[p][d] = g.norms[3 * i[p] + d];
+            res[p][d] = 0;
+        }
+    }
     const Real* c1 = th + th_c1;
     const Real* c2 = th + th_c2;
     const Real* dg = th + th_diag;
-    double res[3] = {0, 0, 0};
     for (int e = e0; e < e1; ++e) {
         if (pair_filter == 1 && g.nbr_precise[e]) continue;
         if (pair_filter == 2 && !g.nbr_precise[e]) continue;
@@ -130,80 +148,103 @@ __global__ void __launch_bounds__(kNearThreads) k_near_eval(DevGeom g, const Rea
         const double q[4] = {g.quat[4 * s], g.quat[4 * s + 1], g.quat[4 * s + 2], g.quat[4 * s + 3]};
         const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
         const double a = g.radius[s];
-        const double rel[3] = {X[0] - g.center[3 * s], X[1] - g.center[3 * s + 1], X[2] - g.center[3 * s + 2]};
-        double xb[3], nb[3];
-        qrot(qc, rel, xb);
-        qrot(qc, Nl, nb);
-        const Real x = Real(xb[0] / a), y = Real(xb[1] / a), z = Real(xb[2] / a);
-        const Real r2 = x * x + y * y + z * z;
-        const Real ir2 = Real(1) / r2;
         constexpr int NL = (NS + kNearLanes - 1) / kNearLanes;
-        Real accl[NL];
+        Real x[PPT], y[PPT], z[PPT], ir2[PPT], dr[PPT], di[PPT];
+        double nb[PPT][3];
+        Real accl[PPT][NL];
 #pragma unroll
-        for (int k = 0; k < NL; ++k) accl[k] = 0;
-        Real dr = Real(1) / sqrt(r2), di = 0;  // Th_0^0
+        for (int p = 0; p < PPT; ++p) {
+            const double rel[3] = {X[p][0] - g.center[3 * s], X[p][1] - g.center[3 * s + 1],
+                                   X[p][2] - g.center[3 * s + 2]};
+            double xb[3];
+            qrot(qc, rel, xb);
+            qrot(qc, Nl[p], nb[p]);
+            x[p] = Real(xb[0] / a);
+            y[p] = Real(xb[1] / a);
+            z[p] = Real(xb[2] / a);
+            const Real r2 = x[p] * x[p] + y[p] * y[p] + z[p] * z[p];
+            ir2[p] = Real(1) / r2;
+            dr[p] = Real(1) / sqrt(r2);  // Th_0^0
+            di[p] = 0;
+#pragma unroll
+            for (int k = 0; k < NL; ++k) accl[p][k] = 0;
+        }
         for (int m = 0; m <= Nd; ++m) {
-            if (m > 0) {
-                const Real f = -dg[m] * ir2;
-                const Real nr = f * (x * dr - y * di);
-                const Real ni = f * (x * di + y * dr);
-                dr = nr;
-                di = ni;
+            Real pr[PPT], pi[PPT], cr[PPT], ci[PPT];
+#pragma unroll
+            for (int p = 0; p < PPT; ++p) {
+                if (m > 0) {
+                    const Real f = -dg[m] * ir2[p];
+                    const Real nr = f * (x[p] * dr[p] - y[p] * di[p]);
+                    const Real ni = f * (x[p] * di[p] + y[p] * dr[p]);
+                    dr[p] = nr;
+                    di[p] = ni;
+                }
+                pr[p] = 0;
+                pi[p] = 0;
+                cr[p] = dr[p];
+                ci[p] = di[p];
             }
-            Real pr = 0, pi = 0, cr = dr, ci = di;
             for (int n = m; n <= Nd; ++n) {
                 const int idx = n * (n + 1) / 2 + m;
-                contract_lane<Real, NS, LANES>(S, idx, lane, cr, ci, accl);
+                contract_lane<Real, NS, LANES, PPT>(S, idx, lane, cr, ci, accl);
                 if (n < Nd) {
                     const Real a1 = c1[idx], a2 = c2[idx];
-                    const Real nr = -(a1 * z * cr + a2 * pr) * ir2;
-                    const Real ni = -(a1 * z * ci + a2 * pi) * ir2;
-                    pr = cr;
-                    pi = ci;
-                    cr = nr;
-                    ci = ni;
-                }
-            }
-        }
-        // gather the NS sets from their owning lanes (set k lives in lane k % kNearLanes, slot k / kNearLanes)
-        Real acc[NS];
 #pragma unroll
-        for (int k = 0; k < NS; ++k) acc[k] = __shfl_sync(0xffffffffu, accl[k / kNearLanes], k % kNearLanes, kNearLanes);
-        double vb[3];
-        if (TRAC) {
-            const double n0 = nb[0], n1 = nb[1], n2 = nb[2];
-            const double xs[3] = {double(x), double(y), double(z)};
-            // symmetric index s(i,k): 00,11,22,01,02,12 -> 0..5
-            const int S3[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
-            const double nn[3] = {n0, n1, n2};
-            for (int ii = 0; ii < 3; ++ii) {
-                double v = nn[ii] * double(acc[0]);
-                for (int kk = 0; kk < 3; ++kk) {
-                    double h = double(acc[19 + S3[ii][kk]]);
-                    for (int jj = 0; jj < 3; ++jj) h -= xs[jj] * double(acc[1 + 6 * jj + S3[ii][kk]]);
-                    v += nn[kk] * h;
+                    for (int p = 0; p < PPT; ++p) {
+                        const Real nr = -(a1 * z[p] * cr[p] + a2 * pr[p]) * ir2[p];
+                        const Real ni = -(a1 * z[p] * ci[p] + a2 * pi[p]) * ir2[p];
+                        pr[p] = cr[p];
+                        pi[p] = ci[p];
+                        cr[p] = nr;
+                        ci[p] = ni;
+                    }
                 }
-                vb[ii] = v / (4 * kPi);
-            }
-        } else {
-            const double xs[3] = {double(x), double(y), double(z)};
-            for (int ii = 0; ii < 3; ++ii) {
-                double v = double(acc[ii]) + double(acc[12 + ii]);
-                for (int jj = 0; jj < 3; ++jj) v -= xs[jj] * double(acc[3 + 3 * jj + ii]);
-                vb[ii] = a * v / (8 * kPi);
             }
         }
-        double vl[3];
-        qrot(q, vb, vl);
-        res[0] += vl[0];
-        res[1] += vl[1];
-        res[2] += vl[2];
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) {
+            // gather the NS sets from their owning lanes (set k lives in lane k % kNearLanes, slot k / kNearLanes)
+            Real acc[NS];
+#pragma unroll
+            for (int k = 0; k < NS; ++k)
+                acc[k] = __shfl_sync(0xffffffffu, accl[p][k / kNearLanes], k % kNearLanes, kNearLanes);
+            double vb[3];
+            const double xs[3] = {double(x[p]), double(y[p]), double(z[p])};
+            if (TRAC) {
+                // symmetric index s(i,k): 00,11,22,01,02,12 -> 0..5
+                const int S3[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+                const double* nn = nb[p];
+                for (int ii = 0; ii < 3; ++ii) {
+                    double v = nn[ii] * double(acc[0]);
+                    for (int kk = 0; kk < 3; ++kk) {
+                        double h = double(acc[19 + S3[ii][kk]]);
+                        for (int jj = 0; jj < 3; ++jj) h -= xs[jj] * double(acc[1 + 6 * jj + S3[ii][kk]]);
+                        v += nn[kk] * h;
+                    }
+                    vb[ii] = v / (4 * kPi);
+                }
+            } else {
+                for (int ii = 0; ii < 3; ++ii) {
+                    double v = double(acc[ii]) + double(acc[12 + ii]);
+                    for (int jj = 0; jj < 3; ++jj) v -= xs[jj] * double(acc[3 + 3 * jj + ii]);
+                    vb[ii] = a * v / (8 * kPi);
+                }
+            }
+            double vl[3];
+            qrot(q, vb, vl);
+            res[p][0] += vl[0];
+            res[p][1] += vl[1];
+            res[p][2] += vl[2];
+        }
     }
-    if (valid && lane == 0) {
-        out[3 * i] += c * res[0];
-        out[3 * i + 1] += c * res[1];
-        out[3 * i + 2] += c * res[2];
-    }
+#pragma unroll
+    for (int p = 0; p < PPT; ++p)
+        if (valid[p] && lane == 0) {
+            out[3 * i[p]] += c * res[p][0];
+            out[3 * i[p] + 1] += c * res[p][1];
+            out[3 * i[p] + 2] += c * res[p][2];
+        }
 }
 
 }  // namespace
@@ -225,7 +266,7 @@ template <int LANES>
 void launch_near_eval_l(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c,
                         double* out, cudaStream_t st, int pair_filter) {
     const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
-    const int per_cta = kNearThreads / LANES;
+    const int per_cta = kNearThreads / LANES * (fp32 ? near_ppt<float, LANES>() : 1);
     const int tiles = (gmax + per_cta - 1) / per_cta;
     const int tm = g.N <= 65535 ? 1 : 0;  // grid y is limited to 65535
     const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
