@@ -606,6 +606,80 @@ def run_multi(args, world, rank, local, dist):
             "bitwise_equal_to_single_solves_tile1": bitwise}
 
 
+def contact_forces(centers, n_contacts, n_solves, seed):
+    """Forces of a collision solver's iterations on one configuration: F = D gamma, the columns of D
+    equal and opposite unit forces along the centre line of the n_contacts closest sphere pairs
+    (the constraint directions of SphereSystem::resolveCollision), gamma >= 0 new every iteration."""
+    c = np.asarray(centers)
+    n = len(c)
+    d = np.linalg.norm(c[:, None] - c[None], axis=-1) + np.eye(n) * 1e9
+    pairs = sorted((d[i, j], i, j) for i in range(n) for j in range(i + 1, n))[:n_contacts]
+    D = np.zeros((6 * n, len(pairs)))
+    for k, (_, i, j) in enumerate(pairs):
+        e = (c[j] - c[i]) / np.linalg.norm(c[j] - c[i])
+        D[6 * i:6 * i + 3, k] = -e
+        D[6 * j:6 * j + 3, k] = e
+    g = np.random.default_rng(seed).uniform(0.0, 1.0, (n_solves, len(pairs)))
+    return [D @ gk for gk in g]
+
+
+def run_sequence(args, world, rank, local, dist):
+    """A sequence of mobility solves on the cfg2 geometry, as the collision solver issues them: forces
+    F = D gamma on --contacts contact directions with new gamma every solve (or, with --contacts 0,
+    forces drifting by --drift per solve). Three initial guesses: zero; the reference's previous
+    solution (xLast, BIE/SphereSTKMobMat.cpp:222); recycled solutions (warm_start "recycle"). Host
+    buffers in and out, host clock around synchronous calls."""
+    from spheresimulator_gb300 import PREC_MIXED, SphereSTKMobMat, configs
+    cfg = configs.cfg2()
+    k = args.sequence
+    rng = np.random.default_rng(11)
+    if args.contacts > 0:
+        F = contact_forces(cfg["centers"], args.contacts, k, seed=11)
+        model = "F = D gamma: %d contact directions (closest sphere pairs), gamma ~ U(0,1) new per solve" % \
+            args.contacts
+    else:
+        F = [cfg["force"]]
+        for _ in range(k - 1):
+            f = F[-1]
+            F.append(f + args.drift * np.linalg.norm(f) / np.sqrt(f.size) * rng.standard_normal(f.shape))
+        model = "force k+1 = force k + %g |F|/sqrt(6N) N(0,1) per component" % args.drift
+    kw = dict(tol=TOL, restart=RESTART, max_iters=1000, precision=PREC_MIXED)
+    arms = {}
+    for name in ("cold", "last", "recycle"):
+        mob = SphereSTKMobMat(cfg["centers"], cfg["radii"], cfg["orders"], device=local)
+        for _ in range(max(1, args.warmup)):
+            mob.solveMob(rng.standard_normal(F[0].shape), **kw)
+        mob.recycle_clear()
+        vel, its = [], []
+        barrier(dist)
+        t0 = time.perf_counter()
+        for j in range(k):
+            ws = {"cold": False, "last": j > 0, "recycle": "recycle"}[name]
+            vel.append(mob.solveMob(F[j], warm_start=ws, **kw))
+            its.append(mob.last_stats[0]["iterations"])
+        t = allmax(dist, time.perf_counter() - t0)
+        arms[name] = {"solves_per_s": round(world * k / t, 4), "ms_per_solve": round(1e3 * t / k, 3),
+                      "iterations": its, "vel": vel}
+    err = max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(arms["recycle"]["vel"],
+                                                                                arms["cold"]["vel"]))
+    for a in arms.values():
+        a.pop("vel")
+    if rank != 0:
+        return None
+    return {"metric": "mobility solves/s, a sequence of collision-solver forces on one geometry (cfg2, mixed, 1e-8)",
+            "value": arms["recycle"]["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": k,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "dtype": "f32 operator + f64 refinement (mixed)",
+            "data": "synthetic (cfg2 geometry; %s)" % model,
+            "config": {"workload": WORKLOAD, "solves": k, "forces": model,
+                       "timing": "host clock around synchronous host-buffer calls"},
+            "ms_per_step": arms["recycle"]["ms_per_solve"], "arms": arms,
+            "speedup_vs_previous_solution_warm_start": round(arms["last"]["ms_per_solve"] /
+                                                             arms["recycle"]["ms_per_solve"], 3),
+            "speedup_vs_cold": round(arms["cold"]["ms_per_solve"] / arms["recycle"]["ms_per_solve"], 3),
+            "max_rel_diff_recycle_vs_cold": err}
+
+
 def far_once():
     """One far-field pass of each kernel family on the cfg2 workload, with few launches before them."""
     from spheresimulator_gb300 import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
@@ -653,6 +727,13 @@ def main():
     ap.add_argument("--multi", type=int, default=0,
                     help="cfg2: solve this many right-hand sides together (smob_solve_mob_multi) against as "
                          "many single solves, and print that line instead of the headline")
+    ap.add_argument("--sequence", type=int, default=0,
+                    help="cfg2: a sequence of this many solves with drifting forces, zero / previous-solution / "
+                         "recycled initial guesses; print that line instead of the headline")
+    ap.add_argument("--contacts", type=int, default=12,
+                    help="--sequence: contact directions spanning the forces (0: drifting forces instead)")
+    ap.add_argument("--drift", type=float, default=0.05,
+                    help="--sequence --contacts 0: relative force change per solve")
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
@@ -672,6 +753,8 @@ def main():
         line = run_reference(args, rank)
     elif args.multi > 0:
         line = run_multi(args, world, rank, local, dist)
+    elif args.sequence > 0:
+        line = run_sequence(args, world, rank, local, dist)
     elif args.config == "cfg5":
         line = run_serving(args, world, rank, local, dist)
     elif args.config != "cfg2":

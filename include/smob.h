@@ -68,12 +68,22 @@ typedef struct {
     double viscosity;       /* fluid viscosity (same for all problems), > 0 */
 } smob_geometry;
 
+/* initial guess of a mobility solve (smob_solve_opts.warm_start) */
+typedef enum {
+    SMOB_WARM_NONE = 0,
+    SMOB_WARM_LAST = 1,    /* the previous solution (the reference's xLast) */
+    SMOB_WARM_RECYCLE = 2  /* the combination of up to 16 earlier solutions on this geometry that fits the new
+                              force best (exact for a force in their span); the solve adds its own
+                              solution to them (smob_recycle_info) */
+} smob_warm_start;
+
 typedef struct {
     double tol;        /* relative residual |b - A mu| / |b| target (mobilitySolver.yaml "Convergence Tolerance") */
     int restart;       /* Krylov vectors per cycle ("Num Blocks") */
     int max_iters;     /* total GMRES iterations ("Maximum Iterations") */
     int precision;     /* smob_precision */
-    int warm_start;    /* nonzero: start from the previous solution of each problem (SphereSTKMobMat.cpp:222) */
+    int warm_start;    /* smob_warm_start: 0 zero initial guess; 1 the previous solution of each problem
+                          (SphereSTKMobMat.cpp:222); 2 recycled solutions (smob_recycle_info) */
     double inner_tol;  /* MIXED only: relative tolerance of each FP32 inner solve (<= 0: library default 1e-5) */
     int precond;       /* 0: none (the reference's unpreconditioned GMRES); 1: right preconditioner that inverts
                           every sphere's own I/2 + K_PV + L exactly (block diagonal in the spherical-harmonic
@@ -192,6 +202,22 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * columns; every column's result equals bit for bit a smob_solve_mob of that column alone with
  * smob_set_far_tile(ctx, 1). The context must hold one problem. Internal copies of the geometry
  * are kept on the context per column count (at most 4 counts). */
+/* Recycled solutions for a sequence of solves on one geometry, e.g. the collision solver's repeated
+ * mobility solves, whose forces are combinations of a few contact forces (the reference keeps its
+ * Krylov solver between solves for this, BIE/SphereSTKMobMat.cpp:232). A solve with warm_start
+ * SMOB_WARM_RECYCLE starts from mu0 = U Q^T F: the columns of Q are the forces of earlier such solves,
+ * orthonormalised per problem, and U holds their density corrections transformed alike. The
+ * correction is linear in the force, so a force in the span of earlier ones (a repeated force, a
+ * combination of contact forces already seen) starts at the tolerance of those solves; otherwise mu0
+ * is the least-squares fit. The solve then adds its own (F, mu). At most 16 pairs are kept (then the
+ * space starts again from the newest); a geometry update, or a solve of another precision, empties it.
+ * MIXED columns also hold the solve's final residual and high-precision single layer (linear in the
+ * force as well), so a MIXED solve whose force lies in the span knows its residual without an
+ * operator pass and needs only FP32 work. count: pairs held; capacity: 16.
+ * smob_recycle_clear forgets the recycled pairs and the previous solution (warm_start 1). */
+smob_status smob_recycle_info(const smob_ctx* ctx, int* count, int* capacity);
+smob_status smob_recycle_clear(smob_ctx* ctx);
+
 smob_status smob_solve_mob_multi(smob_ctx* ctx, int n_rhs, const double* force6n, double* vel6n,
                                  double* density3m, const smob_solve_opts* opts, smob_problem_stats* stats);
 

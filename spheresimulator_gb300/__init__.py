@@ -31,11 +31,26 @@ def spectral_dof(p):
     return 3 * (p + 1) * (p + 2)
 
 
+WARM_NONE, WARM_LAST, WARM_RECYCLE = 0, 1, 2
+
+
+def _warm_code(warm_start):
+    if isinstance(warm_start, str):
+        if warm_start != "recycle":
+            raise ValueError("warm_start: False, True (previous solution) or 'recycle'")
+        return WARM_RECYCLE
+    if isinstance(warm_start, (bool, np.bool_)):
+        return WARM_LAST if warm_start else WARM_NONE
+    return int(warm_start)
+
+
 def solve_opts(tol=1e-10, restart=50, max_iters=500, precision=PREC_FP64, warm_start=False, inner_tol=0.0,
                precond=0):
     """GMRES settings (mobilitySolver.yaml:3-16 names: Convergence Tolerance, Num Blocks, Maximum Iterations);
+    warm_start: False (zero), True (previous solution, SphereSTKMobMat.cpp:222) or "recycle" (the closest
+    combination of earlier solutions on this geometry, which the solve then joins);
     precond=1 adds the block-diagonal right preconditioner (each sphere's own operator inverted)."""
-    return N.SolveOpts(float(tol), int(restart), int(max_iters), int(precision), int(bool(warm_start)),
+    return N.SolveOpts(float(tol), int(restart), int(max_iters), int(precision), _warm_code(warm_start),
                        float(inner_tol), int(precond))
 
 
@@ -165,6 +180,15 @@ class _Context:
     def set_far_tile(self, targets_per_thread):
         """Force the FP32 far-field variant (1, 2 or 4 targets per thread) over the autotuner's choice."""
         N.check(self._L.smob_set_far_tile(self._h, int(targets_per_thread)))
+
+    def recycle_info(self):
+        """(recycled solutions held, capacity) for warm_start="recycle"."""
+        k, cap = ctypes.c_int(), ctypes.c_int()
+        N.check(self._L.smob_recycle_info(self._h, ctypes.byref(k), ctypes.byref(cap)))
+        return k.value, cap.value
+
+    def recycle_clear(self):
+        N.check(self._L.smob_recycle_clear(self._h))
 
     def tuning(self):
         """(targets per thread in use, measured ms of the 1/2/4 variants, whether the choice was cached)"""

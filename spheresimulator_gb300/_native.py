@@ -131,6 +131,8 @@ def lib():
         "smob_tuning": (S, [_VP, _IP, _DP, _IP]),
         "smob_set_graphs": (S, [_VP, ctypes.c_int]),
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
+        "smob_recycle_info": (S, [_VP, _IP, _IP]),
+        "smob_recycle_clear": (S, [_VP]),
         "smob_timer_mark": (S, [_VP]),
         "smob_timer_elapsed": (S, [_VP, _DP]),
         "smob_flush_l2": (S, [_VP, ctypes.c_size_t]),

@@ -104,6 +104,16 @@ struct StreamHolder {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host check of the stop flags
+// recycled solutions (warm_start 2): pairs (force_i, mu_i) of earlier solves kept per context, with
+// the forces orthonormalised per problem; a force closer than this (relative) to their span adds nothing
+constexpr int kRecycleMax = 16;
+constexpr double kRecycleDrop = 1e-10;
+// parts of a recycled solve state: mu; and from MIXED solves the final residual r, the single layer
+// u_hp at the last high-precision residual and that residual's mu (x_hp), all linear in the force
+constexpr int kRecycleParts = 4;
+// MIXED: a recycled guess whose residual is estimated below this (relative) is checked with the
+// high-precision pass at once (it may already meet the tolerance), not with an FP32 residual
+constexpr double kRecycleHpFirst = 1e-3;
 
 }  // namespace
 
@@ -161,6 +171,12 @@ struct smob_ctx {
     // mixed solve: rho + x, and the single layer of rho + x_hp at the last high-precision residual x_hp
     DBuf d_dens, d_uhp, d_xhp, d_partial64_sl;
     DBuf d_pz;  // preconditioned vector P v
+    // recycled solutions: rq (host, orthonormal forces per problem, [kRecycleMax][6N]) and d_ru
+    // (device, [kRecycleMax][kRecycleParts][3M]) the solve states transformed alike; rk columns of
+    // each, all from solves of precision rprec
+    std::vector<double> rq;
+    DBuf d_ru, d_rcoef, d_rscale;
+    int rk = 0, rprec = -1;
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
     bool have_xlast = false;
 
@@ -945,6 +961,119 @@ std::vector<double> seg_norms(smob_ctx* c, const double* v, const unsigned char*
     return h;
 }
 
+// Recycled solutions for a sequence of solves on one geometry (the caller the reference prepares
+// for at BIE/SphereSTKMobMat.cpp:232: the collision solver's repeated mobility solves, whose forces
+// are combinations of a few contact forces). Every solve with warm_start 2 adds its pair (F, mu),
+// A mu = b(F) to the tolerance. The forces are kept orthonormal per problem (classical Gram-Schmidt,
+// twice, on the host: 6N values each) and the mu's transformed with the same coefficients on the
+// device, so each kept mu column solves the system of its force column. b, rho and mu are linear
+// in F, so a new solve starts from mu0 = U h, h = Q^T F: exact (to the tolerance of the earlier
+// solves) when F lies in their span, the least-squares fit otherwise. When full, the space starts
+// again from the newest pair.
+
+// parts[k] = U_k Q^T F (k < nparts, null parts skipped) on every problem; returns per problem
+// |F - Q Q^T F| / |F|
+std::vector<double> recycle_guess(smob_ctx* c, const std::vector<double>& f, double* const* parts, int nparts) {
+    const size_t n = 3 * (size_t)c->M;
+    const size_t n6 = 6 * (size_t)c->N;
+    const int P = c->P;
+    std::vector<double> h((size_t)P * kRecycleMax, 0.0), fn2(P, 0.0);
+    for (int s = 0; s < c->N; ++s) {
+        const int p = c->prob[s];
+        for (int i = 6 * s; i < 6 * s + 6; ++i) {
+            fn2[p] += f[i] * f[i];
+            for (int j = 0; j < c->rk; ++j) h[(size_t)p * kRecycleMax + j] += c->rq[n6 * j + i] * f[i];
+        }
+    }
+    // |F - Q h| from the vector itself (|F|^2 - |h|^2 would lose everything below ~1e-8)
+    std::vector<double> res2(P, 0.0), est(P, 1.0);
+    for (int s = 0; s < c->N; ++s) {
+        const int p = c->prob[s];
+        for (int i = 6 * s; i < 6 * s + 6; ++i) {
+            double e = f[i];
+            for (int j = 0; j < c->rk; ++j) e -= h[(size_t)p * kRecycleMax + j] * c->rq[n6 * j + i];
+            res2[p] += e * e;
+        }
+    }
+    for (int p = 0; p < P; ++p)
+        if (fn2[p] > 0) est[p] = std::sqrt(res2[p] / fn2[p]);
+    KrylovLaunch L = c->kl();
+    CUDA_OK(cudaMemcpyAsync(c->d_rcoef.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, c->st));
+    for (int k = 0; k < nparts; ++k) {
+        if (!parts[k]) continue;
+        CUDA_OK(cudaMemsetAsync(parts[k], 0, sizeof(double) * n, c->st));
+        check_launch(c, launch_update(L, c->d_ru.as<double>() + n * k, (long long)(n * kRecycleParts), c->rk, nullptr,
+                                      c->d_rcoef.as<double>(), kRecycleMax, 1.0, c->d_active.as<unsigned char>(),
+                                      parts[k], c->st));
+    }
+    CUDA_OK(cudaStreamSynchronize(c->st));  // h must outlive its copy
+    return est;
+}
+
+// add (F, parts) of the problems in keep (converged, nonzero forcing) as a new column; the other
+// problems (and problems whose force is already in the span) get zero columns. A solve of another
+// precision than the stored columns' starts the space again.
+void recycle_add(smob_ctx* c, const std::vector<double>& f, const double* const* parts, int nparts, int prec,
+                 const std::vector<unsigned char>& keep) {
+    if (std::none_of(keep.begin(), keep.end(), [](unsigned char k) { return k != 0; })) return;
+    const size_t n = 3 * (size_t)c->M;
+    const size_t n6 = 6 * (size_t)c->N;
+    const int P = c->P;
+    cudaStream_t st = c->st;
+    if (!c->d_ru.p) {
+        c->d_ru.alloc(sizeof(double) * n * kRecycleParts * kRecycleMax);
+        c->d_rcoef.alloc(sizeof(double) * P * kRecycleMax);
+        c->d_rscale.alloc(sizeof(double) * P);
+        c->rq.assign(n6 * kRecycleMax, 0.0);
+    }
+    if (c->rk == kRecycleMax || prec != c->rprec) c->rk = 0;
+    c->rprec = prec;
+    const int k = c->rk;
+    // host: q = F - Q coef (two classical Gram-Schmidt passes), per problem
+    std::vector<double> q(n6, 0.0), coef((size_t)P * kRecycleMax, 0.0), fn2(P, 0.0), nu2(P, 0.0);
+    for (int s = 0; s < c->N; ++s)
+        if (keep[c->prob[s]])
+            for (int i = 6 * s; i < 6 * s + 6; ++i) q[i] = f[i], fn2[c->prob[s]] += f[i] * f[i];
+    for (int pass = 0; pass < 2 && k > 0; ++pass) {
+        std::vector<double> d((size_t)P * kRecycleMax, 0.0);
+        for (int s = 0; s < c->N; ++s)
+            for (int i = 6 * s; i < 6 * s + 6; ++i)
+                for (int j = 0; j < k; ++j) d[(size_t)c->prob[s] * kRecycleMax + j] += c->rq[n6 * j + i] * q[i];
+        for (int s = 0; s < c->N; ++s)
+            for (int i = 6 * s; i < 6 * s + 6; ++i)
+                for (int j = 0; j < k; ++j) q[i] -= d[(size_t)c->prob[s] * kRecycleMax + j] * c->rq[n6 * j + i];
+        for (size_t i = 0; i < d.size(); ++i) coef[i] += d[i];
+    }
+    for (int s = 0; s < c->N; ++s)
+        for (int i = 6 * s; i < 6 * s + 6; ++i) nu2[c->prob[s]] += q[i] * q[i];
+    std::vector<double> sc(P, 0.0);
+    for (int p = 0; p < P; ++p) {
+        const double nu = std::sqrt(nu2[p]);
+        if (keep[p] && std::isfinite(nu) && nu > kRecycleDrop * std::sqrt(fn2[p])) sc[p] = 1.0 / nu;
+    }
+    for (int s = 0; s < c->N; ++s)
+        for (int i = 6 * s; i < 6 * s + 6; ++i) c->rq[n6 * k + i] = q[i] * sc[c->prob[s]];
+    // device: part_k = (v_k - U_k coef) / nu with the same coefficients
+    KrylovLaunch L = c->kl();
+    const unsigned char* act = c->d_active.as<unsigned char>();
+    CUDA_OK(cudaMemcpyAsync(c->d_rcoef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, st));
+    CUDA_OK(cudaMemcpyAsync(c->d_rscale.p, sc.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
+    set_active(c, keep);
+    for (int m = 0; m < kRecycleParts; ++m) {
+        double* base = c->d_ru.as<double>() + n * m;
+        double* u = base + n * kRecycleParts * k;
+        CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        if (m >= nparts || !parts[m]) continue;
+        check_launch(c, launch_axpby_seg(L, 1.0, parts[m], 0.0, act, u, st));
+        if (k > 0)
+            check_launch(c, launch_update(L, base, (long long)(n * kRecycleParts), k, nullptr, c->d_rcoef.as<double>(),
+                                          kRecycleMax, -1.0, act, u, st));
+        check_launch(c, launch_scale(L, u, c->d_rscale.as<double>(), 1, false, act, u, st));
+    }
+    CUDA_OK(cudaStreamSynchronize(st));  // coef and sc must outlive their copies
+    if (std::any_of(sc.begin(), sc.end(), [](double v) { return v != 0.0; })) c->rk++;
+}
+
 // the mobility solve on device pointers (SphereSTKMobMat::solveMob, BIE/SphereSTKMobMat.cpp:146-286)
 smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, double* d_density,
                          const smob_solve_opts* o, smob_problem_stats* stats) {
@@ -1007,6 +1136,22 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         uhp = c->d_uhp.as<double>();
         xhp = c->d_xhp.as<double>();
     }
+    // MIXED: one fused high-precision pass on the problems in mask gives r = -(I/2 + K)(rho + x) - L x
+    // and the single layer u_hp = S[rho + x] (the final velocity then needs only S32[x - x_hp])
+    auto hp_residual = [&](const std::vector<unsigned char>& mask) {
+        set_active(c, mask);
+        CUDA_OK(cudaMemcpyAsync(dens, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, dens, st));
+        CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        op_apply_hp_both(c, dens, u, -0.5, -1.0, w, 1.0);
+        op_apply(c, x, u, 0.0, 0.0, 0.0, -1.0, OP_FP64);  // - L x (per-sphere rigid modes)
+        check_launch(c, launch_axpby_seg(L, 1.0, u, 0.0, act, r, st));
+        check_launch(c, launch_axpby_seg(L, 1.0, w, 0.0, act, uhp, st));
+        check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, xhp, st));
+        for (int p = 0; p < P; ++p)
+            if (mask[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
+    };
 
     // step 1: rigid density; step 2: b = -(I/2 + K) rho. FP64 / float-float: in the solve's precision.
     // MIXED: with the FP32 operator. b only seeds the first inner cycle and scales the tolerance; every
@@ -1018,10 +1163,43 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
     std::vector<double> bnorm = seg_norms(c, b, act);
 
-    // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution or zero
+    // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution, zero, or
+    // (warm_start 2) the combination of recycled earlier solutions closest to this b
     std::vector<char> done(P, 0), conv(P, 0);
     std::vector<double> beta(P, 0.0);
-    if (o->warm_start && c->have_xlast) {
+    const bool recycle = o->warm_start == 2;
+    std::vector<double> hforce;
+    if (recycle) {
+        hforce.resize(6 * (size_t)c->N);
+        CUDA_OK(cudaMemcpyAsync(hforce.data(), d_force, sizeof(double) * hforce.size(), cudaMemcpyDeviceToHost, st));
+        CUDA_OK(cudaStreamSynchronize(st));
+    }
+    if (recycle && c->rk > 0) {
+        // MIXED from MIXED columns: a force in the span (to far below the tolerance) takes the
+        // combined residual, u_hp and x_hp as well, which are those of the combined solution (every
+        // part is linear in the force): no operator pass is needed to know where it stands
+        const bool state = mixed && c->rprec == SMOB_PREC_MIXED;
+        double* parts[kRecycleParts] = {x, state ? r : nullptr, state ? uhp : nullptr, state ? xhp : nullptr};
+        const std::vector<double> est = recycle_guess(c, hforce, parts, kRecycleParts);
+        std::vector<unsigned char> good(P, 0), poor(P, 0);
+        bool any_good = false, any_poor = false;
+        for (int p = 0; p < P; ++p) {
+            if (state && est[p] <= 1e-2 * tol) hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 1;
+            else if (mixed && est[p] <= kRecycleHpFirst) good[p] = 1, any_good = true;
+            else poor[p] = 1, any_poor = true;
+        }
+        if (any_poor) {
+            set_active(c, poor);
+            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
+            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+            for (int p = 0; p < P; ++p)
+                if (poor[p]) (mixed ? passes32x[p] : passes64[p])++, x_moved[p] = mixed ? 1 : 0;
+        }
+        if (any_good) hp_residual(good);
+        set_active(c, all);
+    } else if (o->warm_start && c->have_xlast) {
         CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
         op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
@@ -1178,24 +1356,14 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             for (int p = 0; p < P; ++p)
                 if (upd[p]) passes32x[p]++, x_moved[p] = 1;
         }
-        if (any_hp) {
+        if (any_hp && mixed) {
+            hp_residual(hpres);
+        } else if (any_hp) {
             set_active(c, hpres);
-            if (mixed) {
-                CUDA_OK(cudaMemcpyAsync(dens, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-                check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, dens, st));
-                CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-                CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-                op_apply_hp_both(c, dens, u, -0.5, -1.0, w, 1.0);
-                op_apply(c, x, u, 0.0, 0.0, 0.0, -1.0, OP_FP64);  // - L x (per-sphere rigid modes)
-                check_launch(c, launch_axpby_seg(L, 1.0, u, 0.0, act, r, st));
-                check_launch(c, launch_axpby_seg(L, 1.0, w, 0.0, act, uhp, st));
-                check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, xhp, st));
-            } else {
-                CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-                op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
-                check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-                check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
-            }
+            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
+            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
             for (int p = 0; p < P; ++p)
                 if (hpres[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
         }
@@ -1244,6 +1412,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     CUDA_OK(cudaMemcpyAsync(c->d_xlast.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     c->have_xlast = true;
+    if (recycle) {
+        std::vector<unsigned char> keep(P, 0);
+        for (int p = 0; p < P; ++p) keep[p] = conv[p] && std::isfinite(bnorm[p]) && bnorm[p] >= 1e-5 ? 1 : 0;
+        const double* parts[kRecycleParts] = {x, mixed ? r : nullptr, uhp, xhp};
+        recycle_add(c, hforce, parts, kRecycleParts, o->precision, keep);
+        set_active(c, all);
+    }
     CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
     CUDA_OK(cudaStreamSynchronize(st));
 
@@ -1360,6 +1535,7 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
     c->host_grid_stale = true;
     c->drop_graphs();
+    c->rk = 0;  // recycled solutions belong to the old operator
     for (auto& kv : c->multi) smob_destroy(kv.second);
     c->multi.clear();
     CUDA_OK(cudaStreamSynchronize(c->st));
@@ -1746,7 +1922,26 @@ static smob_status check_opts(const smob_solve_opts* o) {
     if (o->precision != SMOB_PREC_FP64 && o->precision != SMOB_PREC_MIXED && o->precision != SMOB_PREC_FLOAT_FLOAT)
         throw SmobError(SMOB_ERR_ARG, "unknown precision");
     if (o->precond != 0 && o->precond != 1) throw SmobError(SMOB_ERR_ARG, "unknown preconditioner");
+    if (o->warm_start < 0 || o->warm_start > 2) throw SmobError(SMOB_ERR_ARG, "unknown warm start");
     return SMOB_OK;
+}
+
+smob_status smob_recycle_info(const smob_ctx* c, int* count, int* capacity) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (count) *count = c->rk;
+        if (capacity) *capacity = kRecycleMax;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_recycle_clear(smob_ctx* c) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        c->rk = 0;
+        c->have_xlast = false;
+        return SMOB_OK;
+    });
 }
 
 smob_status smob_solve_mob_device(smob_ctx* c, const double* d_force, double* d_vel, double* d_density,

@@ -73,3 +73,22 @@ def test_structures_match_header():
     assert ctypes.sizeof(N.Geometry) == 56
     assert ctypes.sizeof(N.SolveOpts) == 40
     assert ctypes.sizeof(N.ProblemStats) == 40
+
+
+def test_warm_start_codes():
+    """warm_start maps to smob_warm_start: False 0, True 1 (previous solution), "recycle" 2."""
+    from spheresimulator_gb300 import WARM_LAST, WARM_NONE, WARM_RECYCLE, solve_opts
+    assert (WARM_NONE, WARM_LAST, WARM_RECYCLE) == (0, 1, 2)
+    assert solve_opts(warm_start=False).warm_start == 0
+    assert solve_opts(warm_start=True).warm_start == 1
+    assert solve_opts(warm_start="recycle").warm_start == 2
+    with pytest.raises(ValueError):
+        solve_opts(warm_start="sometimes")
+    hdr = open(os.path.join(ROOT, "include", "smob.h")).read()
+    for name, v in (("SMOB_WARM_NONE", 0), ("SMOB_WARM_LAST", 1), ("SMOB_WARM_RECYCLE", 2)):
+        assert re.search(r"%s\s*=\s*%d" % (name, v), hdr)
+    from spheresimulator_gb300 import _native as N
+    L = N.lib()
+    k = ctypes.c_int()
+    assert L.smob_recycle_info(None, ctypes.byref(k), None) == N.SMOB_ERR_ARG
+    assert L.smob_recycle_clear(None) == N.SMOB_ERR_ARG
