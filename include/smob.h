@@ -202,6 +202,21 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * columns; every column's result equals bit for bit a smob_solve_mob of that column alone with
  * smob_set_far_tile(ctx, 1). The context must hold one problem. Internal copies of the geometry
  * are kept on the context per column count (at most 4 counts). */
+/* FP32 far field from coarse equivalent sources. Inside the FP32 operator passes (SMOB_PREC_MIXED:
+ * the inner solves and the final velocity correction) the far field of a well-separated source sphere
+ * is evaluated from equivalent sources on a coarser grid of the same sphere: its grid sources projected
+ * onto the spherical harmonics of degree <= pe and re-weighted with the order-pe quadrature, which
+ * reproduces the far field to ~(a_s / r_min)^(pe+1) relative (r_min: distance from the source centre to
+ * the nearest target point). Each source sphere gets the coarse orders its far targets need for eps
+ * (relative to the sphere's own contribution); near pairs, the own sphere and every FP64 and float-float
+ * pass keep the direct sum over the grid points, so the high-precision residuals that decide
+ * convergence, and the plain FP64 solve, are those of the reference's smooth quadrature. The reference
+ * evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).
+ * eps <= 0 turns it off (the direct sum everywhere); default 1e-7. */
+smob_status smob_set_far_compression(smob_ctx* ctx, double eps);
+/* current eps, coarse points held and (sphere, level) entries */
+smob_status smob_far_compression_info(const smob_ctx* ctx, double* eps, int* coarse_points, int* entries);
+
 /* Recycled solutions for a sequence of solves on one geometry, e.g. the collision solver's repeated
  * mobility solves, whose forces are combinations of a few contact forces (the reference keeps its
  * Krylov solver between solves for this, BIE/SphereSTKMobMat.cpp:232). A solve with warm_start

@@ -181,6 +181,17 @@ class _Context:
         """Force the FP32 far-field variant (1, 2 or 4 targets per thread) over the autotuner's choice."""
         N.check(self._L.smob_set_far_tile(self._h, int(targets_per_thread)))
 
+    def set_far_compression(self, eps):
+        """Tolerance of the FP32 far field's coarse equivalent sources for well-separated sphere pairs
+        (relative to each source sphere's contribution); eps <= 0 evaluates every pair directly."""
+        N.check(self._L.smob_set_far_compression(self._h, float(eps)))
+
+    def far_compression_info(self):
+        """(eps, coarse points held, (sphere, level) entries)"""
+        e, pts, ent = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        N.check(self._L.smob_far_compression_info(self._h, ctypes.byref(e), ctypes.byref(pts), ctypes.byref(ent)))
+        return e.value, pts.value, ent.value
+
     def recycle_info(self):
         """(recycled solutions held, capacity) for warm_start="recycle"."""
         k, cap = ctypes.c_int(), ctypes.c_int()

@@ -132,6 +132,8 @@ def lib():
         "smob_set_graphs": (S, [_VP, ctypes.c_int]),
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
         "smob_recycle_info": (S, [_VP, _IP, _IP]),
+        "smob_set_far_compression": (S, [_VP, ctypes.c_double]),
+        "smob_far_compression_info": (S, [_VP, _DP, _IP, _IP]),
         "smob_recycle_clear": (S, [_VP]),
         "smob_timer_mark": (S, [_VP]),
         "smob_timer_elapsed": (S, [_VP, _DP]),

@@ -104,6 +104,11 @@ struct StreamHolder {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host check of the stop flags
+// FP32 far field from coarse equivalent sources: per-pair tolerance (relative to the source sphere's
+// contribution) and the coarse orders a sphere may use, ascending
+constexpr double kCoarseEpsDefault = 1e-7;
+constexpr double kCoarseMargin = 1.0;  // orders added to log(eps) / log(a_s / r_min) (measured, p = 16)
+constexpr int kCoarseLadder[] = {3, 4, 5, 6, 8, 10, 12, 14, 16, 20, 24, 28};
 // recycled solutions (warm_start 2): pairs (force_i, mu_i) of earlier solves kept per context, with
 // the forces orthonormalised per problem; a force closer than this (relative) to their span adds nothing
 constexpr int kRecycleMax = 16;
@@ -164,6 +169,12 @@ struct smob_ctx {
     DBuf d_active;
     // operator workspace
     DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
+    // FP32 far field from coarse equivalent sources (far_eps <= 0: off)
+    double far_eps = kCoarseEpsDefault;
+    std::vector<int4> clev;
+    std::vector<int2> cent;
+    int ncoarse = 0;
+    DBuf d_clev, d_cent, d_cpos32, d_csrc, d_cmap, d_cnode, d_cnode_off;
     DBuf d_in, d_out, d_tmp;  // host-pointer API staging
     // solver workspace
     int restart_cap = 0;
@@ -366,6 +377,7 @@ void problem_origins(smob_ctx* c);
 void upload_near(smob_ctx* c);
 void build_tables(smob_ctx* c);
 void bind_geom(smob_ctx* c);
+void build_coarse(smob_ctx* c);
 
 void build_context(smob_ctx* c, const smob_geometry* geo) {
     const int N = geo->n_spheres;
@@ -558,8 +570,10 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_tmp.alloc(sizeof(double) * 3 * c->M);
     c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * 2);
     upload_near(c);
+    build_coarse(c);
     bind_geom(c);
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
+    check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
 }
 
 // ---------------------------------------------------------------- tables, near metadata, bindings
@@ -678,6 +692,82 @@ void build_tables(smob_ctx* c) {
 }
 
 // device pointers and sizes of the geometry, as the kernels receive them
+// Coarse levels of every source sphere for this geometry: for each far pair (t, s) of a problem the
+// coarsest ladder order pe < p_s with pe >= log(eps) / log(a_s / r_min) + margin, r_min = |c_t - c_s| - a_t
+// (the FP32 kernels recompute this per target and use the coarsest level built that satisfies it);
+// at most kCoarseLevels orders per sphere (the finest kept). Maps are shared per (p, pe).
+void build_coarse(smob_ctx* c) {
+    const int N = c->N;
+    c->clev.assign((size_t)N * kCoarseLevels, make_int4(0, 0, 0, 0));
+    c->cent.clear();
+    c->ncoarse = 0;
+    std::vector<float> maps;
+    std::map<int, int> map_off;                 // p * 64 + pe -> offset in maps
+    std::vector<double> nodes;
+    std::vector<int> node_off(kMaxOrder + 1, 0);
+    std::vector<char> have_nodes(kMaxOrder + 1, 0);
+    if (c->far_eps > 0 && c->nrep == 1) {
+        const double leps = std::log(c->far_eps);
+        for (int pi = 0; pi < c->P; ++pi) {
+            const Problem& pr = c->problems[pi];
+            for (int s = pr.s0; s < pr.s1; ++s) {
+                const int ps = c->orders[s];
+                const double as = c->radii[s];
+                std::vector<char> used(sizeof(kCoarseLadder) / sizeof(int), 0);
+                for (int t = pr.s0; t < pr.s1; ++t) {
+                    if (t == s) continue;
+                    double d2 = 0;
+                    for (int k = 0; k < 3; ++k) {
+                        const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
+                        d2 += dk * dk;
+                    }
+                    const double d = std::sqrt(d2);
+                    if (d < 1.5 * (as + c->radii[t])) continue;  // near pair: spectral, not far field
+                    const double rmin = d - c->radii[t];
+                    if (!(rmin > as)) continue;
+                    const double need = leps / std::log(as / rmin) + kCoarseMargin;
+                    for (size_t l = 0; l < used.size(); ++l)
+                        if (kCoarseLadder[l] >= need) {
+                            if (kCoarseLadder[l] < ps) used[l] = 1;
+                            break;
+                        }
+                }
+                std::vector<int> pes;
+                for (size_t l = 0; l < used.size(); ++l)
+                    if (used[l]) pes.push_back(kCoarseLadder[l]);
+                if ((int)pes.size() > kCoarseLevels) pes.erase(pes.begin(), pes.end() - kCoarseLevels);
+                for (int l = 0; l < (int)pes.size(); ++l) {
+                    const int pe = pes[l];
+                    const int key = ps * 64 + pe;
+                    if (!map_off.count(key)) {
+                        const std::vector<float>& m = coarse_map(ps, pe);
+                        map_off[key] = (int)maps.size();
+                        maps.insert(maps.end(), m.begin(), m.end());
+                    }
+                    if (!have_nodes[pe]) {
+                        std::vector<double> nv;
+                        unit_nodes(pe, nv);
+                        node_off[pe] = (int)(nodes.size() / 3);
+                        nodes.insert(nodes.end(), nv.begin(), nv.end());
+                        have_nodes[pe] = 1;
+                    }
+                    const int cnt = (pe + 1) * (2 * pe + 2);
+                    c->clev[(size_t)s * kCoarseLevels + l] = make_int4(pe, c->ncoarse, cnt, map_off[key]);
+                    c->cent.push_back(make_int2(s, l));
+                    c->ncoarse += cnt;
+                }
+            }
+        }
+    }
+    c->d_clev.upload(c->clev);
+    c->d_cent.upload(c->cent);
+    c->d_cmap.upload(maps);
+    c->d_cnode.upload(nodes);
+    c->d_cnode_off.upload(node_off);
+    c->d_cpos32.alloc(sizeof(float4) * std::max(c->ncoarse, 1));
+    c->d_csrc.alloc(sizeof(float4) * std::max(c->ncoarse, 1));
+}
+
 void bind_geom(smob_ctx* c) {
     DevGeom& g = c->g;
     g.N = c->N;
@@ -715,6 +805,16 @@ void bind_geom(smob_ctx* c) {
     g.map_val_d = c->d_map_val_d.as<double>();
     g.map_val_f = c->d_map_val_f.as<float>();
     g.active = c->d_active.as<unsigned char>();
+    g.ncent = (int)c->cent.size();
+    g.clog_eps = c->far_eps > 0 ? float(std::log(c->far_eps)) : 0.f;
+    g.cmargin = float(kCoarseMargin);
+    g.clev = c->d_clev.as<int4>();
+    g.cent = c->d_cent.as<int2>();
+    g.cpos32 = c->d_cpos32.as<float4>();
+    g.cmap = c->d_cmap.as<float>();
+    g.cnode = c->d_cnode.as<double>();
+    g.cnode_off = c->d_cnode_off.as<int>();
+    g.csrc = c->d_csrc.as<float4>();
 }
 
 // Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on
@@ -1531,8 +1631,10 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
     c->d_quat.upload(c->quats);
     c->d_org.upload(c->org);
     upload_near(c);
+    build_coarse(c);
     bind_geom(c);
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
+    check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
     c->host_grid_stale = true;
     c->drop_graphs();
     c->rk = 0;  // recycled solutions belong to the old operator
@@ -2005,6 +2107,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
                             c->viscosity};
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
+    r->far_eps = 0.0;  // the several-column kernels read every column's own grid sources
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
@@ -2178,6 +2281,32 @@ smob_status smob_tuning(const smob_ctx* c, int* targets_per_thread, double* vari
         if (variant_ms)
             for (int k = 0; k < 3; ++k) variant_ms[k] = c->tune_ms[k];
         if (from_cache) *from_cache = c->tune_cached ? 1 : 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_far_compression(smob_ctx* c, double eps) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        need(std::isfinite(eps) && eps < 1e-3, "far-field tolerance must be below 1e-3 (<= 0: off)");
+        set_device(c);
+        AllocStreamScope as(c->st);
+        c->drop_graphs();  // captured blocks hold the old coarse tables
+        c->far_eps = eps > 0 ? eps : 0.0;
+        build_coarse(c);
+        bind_geom(c);
+        check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_far_compression_info(const smob_ctx* c, double* eps, int* coarse_points, int* entries) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (eps) *eps = c->far_eps;
+        if (coarse_points) *coarse_points = c->ncoarse;
+        if (entries) *entries = (int)c->cent.size();
         return SMOB_OK;
     });
 }

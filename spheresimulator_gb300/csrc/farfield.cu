@@ -106,6 +106,91 @@ __device__ __forceinline__ bool excluded(const int* __restrict__ nbr_src, int& c
     return cur < end && __ldg(nbr_src + cur) == s;
 }
 
+// ---------------------------------------------------------------- coarse equivalent sources (FP32)
+// For a well-separated pair of spheres the far field of the source sphere's grid sources equals that
+// of equivalent sources on a coarser grid of the same sphere (order pe: the sources projected onto
+// the harmonics of degree <= pe and re-weighted with the coarse quadrature) to ~(a_s / r_min)^(pe+1)
+// relative, r_min the distance from the source centre to the nearest target point. Each target votes
+// per source sphere for the coarsest level within the tolerance; the CTA takes the finest vote, or
+// the fine sources (with the exclusions) when a target skips the sphere.
+constexpr unsigned kBitFine = 1u << kCoarseLevels;  // the sphere's own grid sources
+constexpr unsigned kBitSkip = 2u << kCoarseLevels;  // own sphere or near pair of some target
+
+__device__ __forceinline__ unsigned level_bit(const DevGeom& g, int t, int s) {
+    if (g.ncent == 0) return kBitFine;
+    const int4* L = g.clev + s * kCoarseLevels;
+    if (__ldg(&L[0].x) == 0) return kBitFine;
+    const float dx = float(__ldg(g.center + 3 * t) - __ldg(g.center + 3 * s));
+    const float dy = float(__ldg(g.center + 3 * t + 1) - __ldg(g.center + 3 * s + 1));
+    const float dz = float(__ldg(g.center + 3 * t + 2) - __ldg(g.center + 3 * s + 2));
+    const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - float(__ldg(g.radius + t));
+    const float as = float(__ldg(g.radius + s));
+    if (!(rmin > as)) return kBitFine;
+    const float need = g.clog_eps / __logf(as / rmin) + g.cmargin;
+#pragma unroll 1
+    for (int l = 0; l < kCoarseLevels; ++l) {
+        const int pe = __ldg(&L[l].x);
+        if (pe == 0) break;
+        if (float(pe) >= need) return 1u << l;
+    }
+    return kBitFine;
+}
+
+// CTA-wide OR of one vote per thread (per-warp slots, double-buffered by parity: one barrier)
+__device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[kFarThreads / 32], int parity) {
+    v = __reduce_or_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) slots[parity][threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned r = 0;
+#pragma unroll
+    for (int w = 0; w < kFarThreads / 32; ++w) r |= slots[parity][w];
+    return r;
+}
+
+// the CTA's source range for sphere s from its votes: fine grid points or one coarse level
+__device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned votes, const float4* src,
+                                             const float4*& P, const float4*& F, int& g0, int& gl) {
+    const bool coarse = !(votes & (kBitSkip | kBitFine));
+    if (coarse) {
+        const int4 L = g.clev[s * kCoarseLevels + (31 - __clz(votes))];
+        P = g.cpos32;
+        F = g.csrc;
+        g0 = L.y;
+        gl = L.z;
+    } else {
+        P = g.pos32;
+        F = src;
+        g0 = g.gidx[s];
+        gl = g.glen[s];
+    }
+    return coarse;
+}
+
+// f_e = coarse map x weighted sources, one (sphere, level) entry per CTA
+__global__ void __launch_bounds__(128) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
+    const int2 e = g.cent[blockIdx.x];
+    const int s = e.x;
+    if (g.active && !g.active[g.prob[s]]) return;
+    const int4 L = g.clev[s * kCoarseLevels + e.y];
+    const int g0 = g.gidx[s], ng = g.glen[s];
+    extern __shared__ float4 sfine[];
+    for (int j = threadIdx.x; j < ng; j += blockDim.x) sfine[j] = src[g0 + j];
+    __syncthreads();
+    const float* __restrict__ Mt = g.cmap + L.w;
+    for (int k = threadIdx.x; k < L.z; k += blockDim.x) {
+        float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < ng; ++j) {
+            const float m = __ldg(Mt + (long long)j * L.z + k);
+            const float4 f = sfine[j];
+            ax = fmaf(m, f.x, ax);
+            ay = fmaf(m, f.y, ay);
+            az = fmaf(m, f.z, az);
+        }
+        g.csrc[L.y + k] = make_float4(ax, ay, az, 0.f);
+    }
+}
+
 // ---------------------------------------------------------------- packed FP32x2 far field
 // Blackwell issues two FP32 lanes per FFMA2/FADD2/FMUL2 instruction (__ffma2_rn & co., same
 // per-component rounding as the scalar forms). Targets are packed two per float2; each staged
@@ -146,6 +231,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
     const FarItem it = items[blockIdx.x];
     if (g.active && !g.active[it.problem]) return;
     __shared__ float4 sA[kFarTile32], sB[kFarTile32], sC[kFarTile32];
+    __shared__ unsigned votes_buf[2][kFarThreads / 32];
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float2 TX[NPK], TY[NPK], TZ[NPK], NX[NPK], NY[NPK], NZ[NPK], AX[NPK], AY[NPK], AZ[NPK];
     int sid[T], cur[T], end[T];
@@ -172,28 +258,33 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
         NZ[q] = f2(Nn[0].z, Nn[1].z);
         AX[q] = AY[q] = AZ[q] = f2(0.f, 0.f);
     }
-    for (int s = it.s0; s < it.s1; ++s) {
+    int parity = 0;
+    for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
         bool sk[T];
-        bool all = true, none = true;
+        bool none = true;
+        unsigned vote = 0;
 #pragma unroll
         for (int u = 0; u < T; ++u) {
             sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
-            all = all && sk[u];
             none = none && !sk[u];
+            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, sid[u], s);
         }
-        if (__syncthreads_and(all)) continue;
-        const int g0 = g.gidx[s], gl = g.glen[s];
+        const unsigned votes = cta_or(vote, votes_buf, parity);
+        if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
+        const float4 *SP, *SF;
+        int g0, gl;
+        const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
         for (int base = 0; base < gl; base += kFarTile32) {
             const int n = min(kFarTile32, gl - base);
             __syncthreads();
             for (int k = threadIdx.x; k < n; k += kFarThreads) {
-                const float4 p = g.pos32[g0 + base + k], f = src[g0 + base + k];
+                const float4 p = SP[g0 + base + k], f = SF[g0 + base + k];
                 sA[k] = make_float4(p.x, p.x, p.y, p.y);
                 sB[k] = make_float4(p.z, p.z, f.x, f.x);
                 sC[k] = make_float4(f.y, f.y, f.z, f.z);
             }
             __syncthreads();
-            if (none) {
+            if (none || coarse) {
 #pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const float4 A = sA[k], B = sB[k], C = sC[k];
@@ -250,6 +341,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
     if (g.active && !g.active[it.problem]) return;
     __shared__ float4 sp[kFarTile32];
     __shared__ float4 sf[kFarTile32];
+    __shared__ unsigned votes_buf[2][kFarThreads / 32];
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 P[TPT], Nn[TPT];
     int sid[TPT], cur[TPT], end[TPT];
@@ -266,26 +358,31 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
         end[u] = val[u] ? g.nbr_start[sid[u] + 1] : 0;
         ax[u] = ay[u] = az[u] = 0.f;
     }
-    for (int s = it.s0; s < it.s1; ++s) {
+    int parity = 0;
+    for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
         bool sk[TPT];
-        bool all = true, none = true;
+        bool none = true;
+        unsigned vote = 0;
 #pragma unroll
         for (int u = 0; u < TPT; ++u) {
             sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
-            all = all && sk[u];
             none = none && !sk[u];
+            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, sid[u], s);
         }
-        if (__syncthreads_and(all)) continue;
-        const int g0 = g.gidx[s], gl = g.glen[s];
+        const unsigned votes = cta_or(vote, votes_buf, parity);
+        if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
+        const float4 *SP, *SF;
+        int g0, gl;
+        const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
         for (int base = 0; base < gl; base += kFarTile32) {
             const int n = min(kFarTile32, gl - base);
             __syncthreads();
             for (int k = threadIdx.x; k < n; k += kFarThreads) {
-                sp[k] = g.pos32[g0 + base + k];
-                sf[k] = src[g0 + base + k];
+                sp[k] = SP[g0 + base + k];
+                sf[k] = SF[g0 + base + k];
             }
             __syncthreads();
-            if (none) {
+            if (none || coarse) {
 #pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const float4 q = sp[k], f = sf[k];
@@ -841,7 +938,14 @@ void launch_far32(const DevGeom& g, const FarItem* items, int nitems, bool trac,
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt) {
     if (nitems <= 0) return 0;
+    int n = 1;
     if (fp32) {
+        if (g.ncent > 0) {
+            // coarse strengths of this pass first (every FP32 far-field kernel may read them)
+            const size_t sm = sizeof(float4) * (g.pmax + 1) * (2 * g.pmax + 2);
+            k_coarse_src<<<g.ncent, 128, sm, st>>>(g, src32);
+            ++n;
+        }
         float* pf = static_cast<float*>(partial);
         if (tpt == 1) launch_far32<1>(g, items, nitems, trac, src32, pf, st);
         else if (tpt == 4) launch_far32<4>(g, items, nitems, trac, src32, pf, st);
@@ -850,7 +954,7 @@ int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool tr
         if (trac) k_far64<true><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
         else k_far64<false><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
     }
-    return 1;
+    return n;
 }
 
 template <int KB>

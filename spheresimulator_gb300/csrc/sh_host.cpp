@@ -352,6 +352,62 @@ const SparseMap& near_map(int p, bool trac) {
     return ref;
 }
 
+void unit_nodes(int p, std::vector<double>& xyz) {
+    const HostOrderTables& T = host_tables(p);
+    xyz.resize(3 * size_t(T.nt) * T.nphi);
+    for (int j = 0; j < T.nt; ++j)
+        for (int k = 0; k < T.nphi; ++k) {
+            double* v = &xyz[3 * (size_t(j) * T.nphi + k)];
+            v[0] = T.st[j] * T.cph[k];
+            v[1] = T.st[j] * T.sph[k];
+            v[2] = T.ct[j];
+        }
+}
+
+// Equivalent sources on the order-pe grid of the same sphere: f_e[k] = W_pe[k] sum_j K(k, j) f[j],
+// K(k, j) = sum_{n <= pe} (2n+1)/(4 pi) P_n(nu_k . nu_j) (the addition theorem: the reproducing kernel
+// of the harmonics of degree <= pe). f are weighted grid sources (w_j x_j), so with the order-p
+// quadrature exact to degree 2p+1 this is the order-p projection of x onto degree <= pe, sampled at
+// the coarse nodes and weighted with the coarse quadrature.
+const std::vector<float>& coarse_map(int p, int pe) {
+    static std::mutex mu;
+    static std::map<int, std::unique_ptr<std::vector<float>>> cache;
+    const int key = p * 64 + pe;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return *it->second;
+    }
+    const HostOrderTables& Te = host_tables(pe);
+    std::vector<double> nf, nc;
+    unit_nodes(p, nf);
+    unit_nodes(pe, nc);
+    const int ng = int(nf.size() / 3), ne = int(nc.size() / 3);
+    auto M = std::make_unique<std::vector<float>>(size_t(ng) * ne);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < ng; ++j)
+        for (int k = 0; k < ne; ++k) {
+            const double x = std::max(-1.0, std::min(1.0, nf[3 * j] * nc[3 * k] + nf[3 * j + 1] * nc[3 * k + 1] +
+                                                              nf[3 * j + 2] * nc[3 * k + 2]));
+            // Legendre recurrence P_{n+1} = ((2n+1) x P_n - n P_{n-1}) / (n+1)
+            double p0 = 1.0, p1 = x, sum = 1.0 + 3.0 * x;
+            if (pe == 0) sum = 1.0;
+            for (int n = 1; n < pe; ++n) {
+                const double p2 = ((2.0 * n + 1) * x * p1 - n * p0) / (n + 1);
+                p0 = p1;
+                p1 = p2;
+                sum += (2.0 * (n + 1) + 1) * p2;
+            }
+            (*M)[size_t(j) * ne + k] = float(Te.wq[k / Te.nphi] * sum / (4 * PI));
+        }
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return *it->second;
+    auto& ref = *M;
+    cache[key] = std::move(M);
+    return ref;
+}
+
 void theta_recurrence(int nmax, std::vector<double>& c1, std::vector<double>& c2, std::vector<double>& diag) {
     c1.assign(ncoef(nmax), 0.0);
     c2.assign(ncoef(nmax), 0.0);

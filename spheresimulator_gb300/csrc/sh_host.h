@@ -33,6 +33,11 @@ void vsh_eval_point(int p, const std::complex<double>* c, double theta, double p
 void gauss_legendre_nodes(int n, std::vector<double>& x, std::vector<double>& w);
 // trac = true: 25 sets (div L, Hessians of L_x, L_y, L_z, L_r); false: 15 sets (L_j, grad L_j, grad L_r)
 const SparseMap& near_map(int p, bool trac);
+// unit-sphere grid nodes of order p (ring-major, as the sphere grids): [node][3]
+void unit_nodes(int p, std::vector<double>& xyz);
+// FP32 map from the weighted grid sources of an order-p sphere to equivalent sources on its order-pe
+// grid (pe < p), transposed: [j (fine node)][k (coarse node)]
+const std::vector<float>& coarse_map(int p, int pe);
 // recurrence coefficients of the irregular solid harmonics up to degree nmax:
 // c1[cidx(n,m)] = (2n+1)/sqrt((n+1)^2-m^2), c2[cidx(n,m)] = sqrt((n^2-m^2)/((n+1)^2-m^2)), diag[m] = sqrt((2m-1)/(2m))
 void theta_recurrence(int nmax, std::vector<double>& c1, std::vector<double>& c2, std::vector<double>& diag);

@@ -32,6 +32,7 @@ constexpr int kNearThreads = 128;        // near-field CTA (one target point per
 constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
 constexpr int kNearSetsTrac = 25;        // div L, Hessians of L_x,L_y,L_z,L_r
 constexpr int kNearSetsSL = 15;          // L_j, grad L_j, grad L_r
+constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per sphere (FP32 far field)
 
 __host__ __device__ inline int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
 __host__ __device__ inline int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
@@ -100,6 +101,18 @@ struct DevGeom {
     const double* map_val_d;
     const float* map_val_f;
     const unsigned char* active;  // per problem: operator work enabled
+    // FP32 far field from coarse equivalent sources for well-separated sphere pairs (ncent = 0: off).
+    // A source sphere s has up to kCoarseLevels coarse orders pe, ascending; a target sphere t may use
+    // the coarsest with pe >= clog_eps / log(a_s / (|c_t - c_s| - a_t)) + cmargin.
+    int ncent;                 // (sphere, level) entries
+    float clog_eps, cmargin;
+    const int4* clev;          // [N][kCoarseLevels] {pe (0: unused), first coarse point, count, map offset}
+    const int2* cent;          // [ncent] {sphere, level}
+    const float4* cpos32;      // coarse points: x, y, z relative to the problem origin, w = sphere id bits
+    const float* cmap;         // coarse maps, [fine node][coarse node] per (p, pe)
+    const double* cnode;       // unit nodes of the coarse orders, [node][3]
+    const int* cnode_off;      // [kMaxOrder + 1] first node of order pe in cnode
+    float4* csrc;              // coarse source strengths of the current FP32 pass (workspace)
 };
 
 // ---------------------------------------------------------------- kernels (launch wrappers)
@@ -111,6 +124,8 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
+// coarse points of every (sphere, level) entry, relative to the problem origins (after launch_regrid)
+int launch_coarse_grid(const DevGeom& g, const double* org, float4* cpos32, cudaStream_t st);
 // FP32 far field of nrep replicas of one problem (replica r = problem r, points [r*rep_M, (r+1)*rep_M)):
 // items are replica 0's (kFarThreads targets each); each pair's geometry serves all replicas
 int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,

@@ -411,6 +411,24 @@ __global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __re
     nrm64[i] = make_double4(n[0], n[1], n[2], 0.0);
 }
 
+// coarse points of one (sphere, level) entry per CTA: the order-pe unit nodes placed like the sphere's
+// own grid (k_regrid), relative to the problem origin in FP32
+__global__ void k_coarse_grid(DevGeom g, const double* __restrict__ org, float4* __restrict__ cpos32) {
+    const int2 e = g.cent[blockIdx.x];
+    const int s = e.x;
+    const int4 L = g.clev[s * kCoarseLevels + e.y];
+    const double* nodes = g.cnode + 3LL * g.cnode_off[L.x];
+    const double a = g.radius[s];
+    const double* o = org + 3 * g.prob[s];
+    for (int k = threadIdx.x; k < L.z; k += blockDim.x) {
+        double n[3];
+        qrot_rn(g.quat + 4 * s, nodes + 3 * k, n);
+        float r[3];
+        for (int d = 0; d < 3; ++d) r[d] = float(__dsub_rn(__dadd_rn(__dmul_rn(a, n[d]), g.center[3 * s + d]), o[d]));
+        cpos32[L.y + k] = make_float4(r[0], r[1], r[2], __int_as_float(s));
+    }
+}
+
 __global__ void k_rigid_average(DevGeom g, const double* __restrict__ u, double inv_visc, double* __restrict__ vel) {
     const int s = blockIdx.x;
     if (g.active && !g.active[g.prob[s]]) return;
@@ -469,6 +487,12 @@ int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st) {
                                                 const_cast<float4*>(g.pos32), const_cast<float4*>(g.nrm32),
                                                 const_cast<float4*>(g.pos32lo), const_cast<float4*>(g.nrm32lo),
                                                 const_cast<double4*>(g.pos64), const_cast<double4*>(g.nrm64));
+    return 1;
+}
+
+int launch_coarse_grid(const DevGeom& g, const double* org, float4* cpos32, cudaStream_t st) {
+    if (g.ncent <= 0) return 0;
+    k_coarse_grid<<<g.ncent, 128, 0, st>>>(g, org, cpos32);
     return 1;
 }
 

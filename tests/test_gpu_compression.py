@@ -1,0 +1,99 @@
+"""FP32 far field from coarse equivalent sources for well-separated sphere pairs: accuracy against
+the direct sum and the FP64 oracle, tolerance control, solves that equal the direct-sum solves to
+the tolerance, and batches and geometry updates."""
+import numpy as np
+import pytest
+
+from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKMobMat, SphereSTKSHOperator, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _spread(seed=0, n=24, p=12, box=22.0):
+    """Spheres spread in a box, so most pairs are well separated."""
+    rng = np.random.default_rng(seed)
+    radii = rng.uniform(0.8, 1.2, n)
+    return dict(centers=configs.rsa(rng, n, radii, box, 0.3), radii=radii, orders=np.full(n, p))
+
+
+def test_far_field_matches_direct_sum():
+    c = _spread()
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    eps, pts, ent = g.far_compression_info()
+    assert eps == 1e-7 and ent > 0 and pts > 0
+    x = np.random.default_rng(1).standard_normal(3 * g.n_points)
+    fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
+    comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
+    g.set_far_compression(0)
+    assert g.far_compression_info()[1:] == (0, 0)
+    direct = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
+    # the compression error sits at the FP32 rounding level of the direct sum
+    assert _rel(direct, fp64) < 2e-5
+    assert _rel(comp, fp64) < 2e-5
+    assert _rel(comp, direct) < 2e-6
+
+
+def test_tolerance_controls_the_error():
+    c = _spread(seed=2)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    x = np.random.default_rng(2).standard_normal(3 * g.n_points)
+    ref = g.far_field(x, cTrac=1.0, precision=PREC_FP64)
+    errs = []
+    for eps in (1e-3 * 0.99, 1e-5, 1e-8):
+        g.set_far_compression(eps)
+        assert g.far_compression_info()[2] > 0
+        errs.append(_rel(g.far_field(x, cTrac=1.0, precision=PREC_MIXED), ref))
+    # the loose tolerance shows; the tight one is at the FP32 rounding level of the direct sum
+    assert errs[0] > 3 * errs[2] and errs[0] < 1e-3 and errs[2] < 2e-6
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_mixed_solve_equals_direct_sum_solve(precond):
+    c = _spread(seed=3, n=20, p=10, box=16.0)
+    F = np.random.default_rng(3).standard_normal(6 * 20)
+    g = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    assert g.far_compression_info()[2] > 0
+    v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED, precond=precond)
+    s = g.last_stats[0]
+    d = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    d.set_far_compression(0)
+    vd = d.solveMob(F, tol=1e-10, precision=PREC_MIXED, precond=precond)
+    ref = d.solveMob(F, tol=1e-11, precision=PREC_FP64)
+    assert s["status"] == 0 and s["relres"] < 1e-10
+    assert _rel(v, vd) < 1e-9 and _rel(v, ref) < 1e-9
+    assert s["iterations"] <= d.last_stats[0]["iterations"] + 2
+
+
+def test_batch_equals_problems_alone_and_update_equals_fresh():
+    a, b = _spread(seed=4, n=10, p=8, box=14.0), _spread(seed=5, n=14, p=8, box=16.0)
+    centers = np.vstack([a["centers"], b["centers"] + 200.0])
+    radii = np.concatenate([a["radii"], b["radii"]])
+    orders = np.concatenate([a["orders"], b["orders"]])
+    prob = np.array([0] * 10 + [1] * 14, dtype=np.int32)
+    F = np.random.default_rng(6).standard_normal(6 * 24)
+    g = SphereSTKMobMat(centers, radii, orders, problem=prob)
+    v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED)
+    for sl, pts, cc, rr, oo in ((slice(0, 60), slice(0, 10), a["centers"], a["radii"], a["orders"]),
+                                (slice(60, 144), slice(10, 24), b["centers"] + 200.0, b["radii"], b["orders"])):
+        alone = SphereSTKMobMat(cc, rr, oo)
+        assert np.array_equal(alone.solveMob(F[sl], tol=1e-10, precision=PREC_MIXED), v[sl])
+    moved = centers + np.random.default_rng(7).uniform(-0.05, 0.05, centers.shape)
+    g.set_geometry(moved)
+    fresh = SphereSTKMobMat(moved, radii, orders, problem=prob)
+    assert g.far_compression_info() == fresh.far_compression_info()
+    assert np.array_equal(g.solveMob(F, tol=1e-10, precision=PREC_MIXED),
+                          fresh.solveMob(F, tol=1e-10, precision=PREC_MIXED))
+
+
+def test_invalid_tolerance_is_rejected():
+    c = _spread(seed=8, n=3, p=4)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    from spheresimulator_gb300 import SmobError
+    with pytest.raises(SmobError):
+        g.set_far_compression(0.1)
+    with pytest.raises(SmobError):
+        g.set_far_compression(float("nan"))

@@ -254,11 +254,12 @@ def test_batched_equals_alone():
 @pytest.mark.parametrize("k", [2, 3, 6])
 def test_multi_rhs_equals_single_solves(k):
     """K right-hand sides solved together (shared-geometry FP32 far field) give bit for bit the
-    solves of each column alone with the one-target-per-thread FP32 kernel; the Tpetra-style apply
-    with K columns uses the same path."""
+    solves of each column alone with the one-target-per-thread FP32 kernel and the direct far field
+    (no coarse equivalent sources); the Tpetra-style apply with K columns uses the same path."""
     cfg = cluster(19, n=6, p=8, gap=0.1)
     mob = make(cfg, SphereSTKMobMat)
     mob.set_far_tile(1)
+    mob.set_far_compression(0)
     F = np.random.default_rng(k).standard_normal((k, 6 * mob.n_spheres))
     for prec in (PREC_MIXED, PREC_FP64):
         V = mob.solveMobMulti(F, tol=1e-10, precision=prec, want_density=True)
