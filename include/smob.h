@@ -216,6 +216,10 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
 smob_status smob_set_far_compression(smob_ctx* ctx, double eps);
 /* current eps, coarse points held and (sphere, level) entries */
 smob_status smob_far_compression_info(const smob_ctx* ctx, double* eps, int* coarse_points, int* entries);
+/* target-source pairs of one FP32 far-field pass with the current tile: the direct sum's (every far
+ * pair), the evaluated ones (fine or coarse sources, as the kernels choose them per CTA), and the
+ * multiply-adds of the coarse strengths per pass */
+smob_status smob_far_pairs(const smob_ctx* ctx, long long* direct, long long* evaluated, long long* coarse_macs);
 
 /* Recycled solutions for a sequence of solves on one geometry, e.g. the collision solver's repeated
  * mobility solves, whose forces are combinations of a few contact forces (the reference keeps its

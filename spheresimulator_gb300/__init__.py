@@ -192,6 +192,12 @@ class _Context:
         N.check(self._L.smob_far_compression_info(self._h, ctypes.byref(e), ctypes.byref(pts), ctypes.byref(ent)))
         return e.value, pts.value, ent.value
 
+    def far_pairs(self):
+        """(direct-sum pairs, evaluated pairs, coarse-strength multiply-adds) of one FP32 far-field pass"""
+        d, e, m = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        N.check(self._L.smob_far_pairs(self._h, ctypes.byref(d), ctypes.byref(e), ctypes.byref(m)))
+        return d.value, e.value, m.value
+
     def recycle_info(self):
         """(recycled solutions held, capacity) for warm_start="recycle"."""
         k, cap = ctypes.c_int(), ctypes.c_int()

@@ -134,6 +134,8 @@ def lib():
         "smob_recycle_info": (S, [_VP, _IP, _IP]),
         "smob_set_far_compression": (S, [_VP, ctypes.c_double]),
         "smob_far_compression_info": (S, [_VP, _DP, _IP, _IP]),
+        "smob_far_pairs": (S, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                               ctypes.POINTER(ctypes.c_longlong)]),
         "smob_recycle_clear": (S, [_VP]),
         "smob_timer_mark": (S, [_VP]),
         "smob_timer_elapsed": (S, [_VP, _DP]),

@@ -174,7 +174,9 @@ struct smob_ctx {
     std::vector<int4> clev;
     std::vector<int2> cent;
     int ncoarse = 0;
-    DBuf d_clev, d_cent, d_cpos32, d_csrc, d_cmap, d_cnode, d_cnode_off;
+    std::vector<int4> cdesc, cgrp;
+    std::vector<int2> gent;
+    DBuf d_clev, d_cent, d_cpos32, d_csrc, d_cmap, d_cnode, d_cnode_off, d_cdesc, d_cgrp, d_gent;
     DBuf d_in, d_out, d_tmp;  // host-pointer API staging
     // solver workspace
     int restart_cap = 0;
@@ -759,8 +761,37 @@ void build_coarse(smob_ctx* c) {
             }
         }
     }
+    // GEMM tiles of the per-pass strengths: entries grouped by map (p, pe), 8 spheres x 64 nodes per CTA
+    c->cdesc.clear();
+    c->cgrp.clear();
+    c->gent.clear();
+    struct MapGroup {
+        int ng = 0, cnt = 0;
+        std::vector<int2> ents;  // {sphere, first coarse point}
+    };
+    std::map<int, MapGroup> by_map;  // by map offset
+    for (const int2& e : c->cent) {
+        const int4 L = c->clev[(size_t)e.x * kCoarseLevels + e.y];
+        MapGroup& mg = by_map[L.w];
+        mg.ng = c->glen[e.x];
+        mg.cnt = L.z;
+        mg.ents.push_back(make_int2(e.x, L.y));
+    }
+    for (auto& kv : by_map) {
+        const MapGroup& mg = kv.second;
+        const int grp = (int)c->cgrp.size();
+        c->cgrp.push_back(make_int4(kv.first, mg.ng, mg.cnt, 0));
+        const int first = (int)c->gent.size();
+        c->gent.insert(c->gent.end(), mg.ents.begin(), mg.ents.end());
+        for (int e = 0; e < (int)mg.ents.size(); e += 8)
+            for (int k0 = 0; k0 < mg.cnt; k0 += 64)
+                c->cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
+    }
     c->d_clev.upload(c->clev);
     c->d_cent.upload(c->cent);
+    c->d_cdesc.upload(c->cdesc);
+    c->d_cgrp.upload(c->cgrp);
+    c->d_gent.upload(c->gent);
     c->d_cmap.upload(maps);
     c->d_cnode.upload(nodes);
     c->d_cnode_off.upload(node_off);
@@ -815,6 +846,10 @@ void bind_geom(smob_ctx* c) {
     g.cnode = c->d_cnode.as<double>();
     g.cnode_off = c->d_cnode_off.as<int>();
     g.csrc = c->d_csrc.as<float4>();
+    g.ncdesc = (int)c->cdesc.size();
+    g.cdesc = c->d_cdesc.as<int4>();
+    g.cgrp = c->d_cgrp.as<int4>();
+    g.gent = c->d_gent.as<int2>();
 }
 
 // Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on
@@ -835,6 +870,7 @@ void autotune_far32(smob_ctx* c) {
         CUDA_OK(cudaEventCreate(&a));
         CUDA_OK(cudaEventCreate(&b));
         CUDA_OK(cudaMemsetAsync(c->d_src32.p, 0, sizeof(float4) * c->M, c->st));
+        check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
         DBuf items[3];
         for (int k = 0; k < 3; ++k) items[k].upload(c->items_tpt[k]);
         auto run = [&](int k) {
@@ -917,6 +953,10 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
             {
                 ProfScope ps(c, "far_pack", fs);
                 check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, fs));
+            }
+            if (fp32 && c->nrep == 1 && g.ncent > 0) {
+                ProfScope ps(c, "far_coarse", fs);
+                check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
             }
             ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"), fs);
             if (fp32 && c->nrep > 1)
@@ -1943,6 +1983,10 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                                                         nullptr, c->st));
                 } else {
                     check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
+                    if (fp32 && c->g.ncent > 0) {
+                        ProfScope ps(c, "far_coarse");
+                        check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
+                    }
                     ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
                     check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
                                                      c->d_src64.as<double4>(), partial, c->st, c->tpt));
@@ -2307,6 +2351,67 @@ smob_status smob_far_compression_info(const smob_ctx* c, double* eps, int* coars
         if (eps) *eps = c->far_eps;
         if (coarse_points) *coarse_points = c->ncoarse;
         if (entries) *entries = (int)c->cent.size();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* evaluated, long long* coarse_macs) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        // the FP32 kernels' per-CTA choice replayed on the host for the current work items: a source
+        // sphere is skipped when every target skips it, read from its grid points when some target
+        // skips it or needs them, else from the finest coarse level any target votes for
+        const double leps = c->far_eps > 0 ? std::log(c->far_eps) : 0.0;
+        long long dir = 0, ev = 0;
+        std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
+        for (const FarItem& it : c->items32) {
+            tsph.clear();
+            for (int t = it.t0; t < it.t1; ++t) {
+                const int ts = c->sid[t];
+                if (tsph.empty() || tsph.back().first != ts) tsph.push_back({ts, 0});
+                tsph.back().second++;
+            }
+            for (int s = it.s0; s < it.s1; ++s) {
+                int keep = 0, all = 0, fine = 0, lvmax = -1;
+                for (auto& ts : tsph) {
+                    const int t = ts.first;
+                    all += ts.second;
+                    bool skip = t == s;
+                    for (int e = c->nbr_start[t]; e < c->nbr_start[t + 1] && !skip; ++e) skip = c->nbr_src[e] == s;
+                    if (skip) continue;
+                    keep += ts.second;
+                    int lv = -1;
+                    const int4* L = &c->clev[(size_t)s * kCoarseLevels];
+                    if (!c->cent.empty() && L[0].x != 0) {
+                        double d2 = 0;
+                        for (int k = 0; k < 3; ++k) {
+                            const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
+                            d2 += dk * dk;
+                        }
+                        const double rmin = std::sqrt(d2) - c->radii[t];
+                        if (rmin > c->radii[s]) {
+                            const double need = leps / std::log(c->radii[s] / rmin) + kCoarseMargin;
+                            for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l)
+                                if (L[l].x >= need) {
+                                    lv = l;
+                                    break;
+                                }
+                        }
+                    }
+                    if (lv < 0) fine = 1;
+                    else lvmax = std::max(lvmax, lv);
+                }
+                dir += (long long)keep * c->glen[s];
+                if (keep == 0) continue;
+                if (fine || keep < all) ev += (long long)keep * c->glen[s];
+                else ev += (long long)all * c->clev[(size_t)s * kCoarseLevels + lvmax].z;
+            }
+        }
+        long long macs = 0;
+        for (const int2& e : c->cent) macs += 3LL * c->glen[e.x] * c->clev[(size_t)e.x * kCoarseLevels + e.y].z;
+        if (direct) *direct = dir;
+        if (evaluated) *evaluated = ev;
+        if (coarse_macs) *coarse_macs = macs;
         return SMOB_OK;
     });
 }

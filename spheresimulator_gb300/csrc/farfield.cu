@@ -166,28 +166,69 @@ __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned v
     return coarse;
 }
 
-// f_e = coarse map x weighted sources, one (sphere, level) entry per CTA
+// f_e = coarse map x weighted sources: per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per sphere]. A CTA
+// computes 64 coarse nodes of up to 8 spheres, staging 32 fine nodes of the map and of the spheres'
+// sources per step; thread (sphere t / 16, nodes t % 16 + 16 i) keeps 4 x 3 accumulators.
+constexpr int kCgNodes = 64, kCgSph = 8, kCgK = 32;
 __global__ void __launch_bounds__(128) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
-    const int2 e = g.cent[blockIdx.x];
-    const int s = e.x;
-    if (g.active && !g.active[g.prob[s]]) return;
-    const int4 L = g.clev[s * kCoarseLevels + e.y];
-    const int g0 = g.gidx[s], ng = g.glen[s];
-    extern __shared__ float4 sfine[];
-    for (int j = threadIdx.x; j < ng; j += blockDim.x) sfine[j] = src[g0 + j];
-    __syncthreads();
-    const float* __restrict__ Mt = g.cmap + L.w;
-    for (int k = threadIdx.x; k < L.z; k += blockDim.x) {
-        float ax = 0.f, ay = 0.f, az = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < ng; ++j) {
-            const float m = __ldg(Mt + (long long)j * L.z + k);
-            const float4 f = sfine[j];
-            ax = fmaf(m, f.x, ax);
-            ay = fmaf(m, f.y, ay);
-            az = fmaf(m, f.z, az);
+    const int4 d = g.cdesc[blockIdx.x];
+    const int4 G = g.cgrp[d.x];
+    const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
+    __shared__ float Ms[kCgK][kCgNodes];
+    __shared__ float4 Fs[kCgK][kCgSph];
+    __shared__ int sbase[kCgSph], sout[kCgSph];
+    __shared__ unsigned char sact[kCgSph];
+    const int t = threadIdx.x;
+    if (t < kCgSph) {
+        int sb = 0, so = 0;
+        unsigned char a = 0;
+        if (t < ne) {
+            const int2 e = g.gent[d.z + t];
+            sb = g.gidx[e.x];
+            so = e.y;
+            a = (g.active && !g.active[g.prob[e.x]]) ? 0 : 1;
         }
-        g.csrc[L.y + k] = make_float4(ax, ay, az, 0.f);
+        sbase[t] = sb;
+        sout[t] = so;
+        sact[t] = a;
+    }
+    __syncthreads();
+    const int si = t >> 4, ni = t & 15;
+    float acc[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
+    const float* __restrict__ map = g.cmap + G.x;
+    for (int j0 = 0; j0 < ng; j0 += kCgK) {
+#pragma unroll
+        for (int r = 0; r < kCgK * kCgNodes / 128; ++r) {
+            const int idx = t + 128 * r, jj = idx / kCgNodes, kk = idx % kCgNodes;
+            Ms[jj][kk] = (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk) : 0.f;
+        }
+#pragma unroll
+        for (int r = 0; r < kCgK * kCgSph / 128; ++r) {
+            const int idx = t + 128 * r, jj = idx / kCgSph, ss = idx % kCgSph;
+            Fs[jj][ss] = (j0 + jj < ng && ss < ne) ? src[sbase[ss] + j0 + jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int jj = 0; jj < kCgK; ++jj) {
+            const float4 f = Fs[jj][si];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float m = Ms[jj][ni + 16 * i];
+                acc[i][0] = fmaf(m, f.x, acc[i][0]);
+                acc[i][1] = fmaf(m, f.y, acc[i][1]);
+                acc[i][2] = fmaf(m, f.z, acc[i][2]);
+            }
+        }
+        __syncthreads();
+    }
+    if (si < ne && sact[si]) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int k = k0 + ni + 16 * i;
+            if (k < cnt) g.csrc[sout[si] + k] = make_float4(acc[i][0], acc[i][1], acc[i][2], 0.f);
+        }
     }
 }
 
@@ -938,14 +979,7 @@ void launch_far32(const DevGeom& g, const FarItem* items, int nitems, bool trac,
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt) {
     if (nitems <= 0) return 0;
-    int n = 1;
     if (fp32) {
-        if (g.ncent > 0) {
-            // coarse strengths of this pass first (every FP32 far-field kernel may read them)
-            const size_t sm = sizeof(float4) * (g.pmax + 1) * (2 * g.pmax + 2);
-            k_coarse_src<<<g.ncent, 128, sm, st>>>(g, src32);
-            ++n;
-        }
         float* pf = static_cast<float*>(partial);
         if (tpt == 1) launch_far32<1>(g, items, nitems, trac, src32, pf, st);
         else if (tpt == 4) launch_far32<4>(g, items, nitems, trac, src32, pf, st);
@@ -954,7 +988,13 @@ int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool tr
         if (trac) k_far64<true><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
         else k_far64<false><<<nitems, kFarThreads, 0, st>>>(g, items, src64, static_cast<double*>(partial));
     }
-    return n;
+    return 1;
+}
+
+int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st) {
+    if (g.ncent <= 0 || g.ncdesc <= 0) return 0;
+    k_coarse_src<<<g.ncdesc, 128, 0, st>>>(g, src32);
+    return 1;
 }
 
 template <int KB>

@@ -113,6 +113,11 @@ struct DevGeom {
     const double* cnode;       // unit nodes of the coarse orders, [node][3]
     const int* cnode_off;      // [kMaxOrder + 1] first node of order pe in cnode
     float4* csrc;              // coarse source strengths of the current FP32 pass (workspace)
+    // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of 64 coarse nodes x 8 spheres
+    int ncdesc;
+    const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
+    const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
+    const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
 };
 
 // ---------------------------------------------------------------- kernels (launch wrappers)
@@ -120,6 +125,9 @@ struct DevGeom {
 // Far field: out[3M] += sum over far sources of c_sl*S + c_trac*K(dot n_target).
 int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4* src64, bool fp32,
                     cudaStream_t st);
+// coarse equivalent-source strengths of this pass from the FP32 grid sources (before every FP32
+// launch_far_field when g.ncent > 0)
+int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
