@@ -611,7 +611,7 @@ def run_multi(args, world, rank, local, dist):
         vs = singles()
     t_single = allmax(dist, time.perf_counter() - t0)
     mob.set_far_tile(1)
-    bitwise = bool(np.array_equal(vm, singles()))
+    bitwise = bool(np.array_equal(mob.solveMobMulti(F, **kw), singles()))
     err = float(np.linalg.norm(vm - vs) / np.linalg.norm(vs))
     if rank != 0:
         return None

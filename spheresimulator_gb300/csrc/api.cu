@@ -708,7 +708,7 @@ void build_coarse(smob_ctx* c) {
     std::vector<double> nodes;
     std::vector<int> node_off(kMaxOrder + 1, 0);
     std::vector<char> have_nodes(kMaxOrder + 1, 0);
-    if (c->far_eps > 0 && c->nrep == 1) {
+    if (c->far_eps > 0) {
         const double leps = std::log(c->far_eps);
         for (int pi = 0; pi < c->P; ++pi) {
             const Problem& pr = c->problems[pi];
@@ -846,6 +846,7 @@ void bind_geom(smob_ctx* c) {
     g.cnode = c->d_cnode.as<double>();
     g.cnode_off = c->d_cnode_off.as<int>();
     g.csrc = c->d_csrc.as<float4>();
+    g.crep = c->nrep > 1 ? c->ncoarse / c->nrep : c->ncoarse;
     g.ncdesc = (int)c->cdesc.size();
     g.cdesc = c->d_cdesc.as<int4>();
     g.cgrp = c->d_cgrp.as<int4>();
@@ -954,7 +955,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 ProfScope ps(c, "far_pack", fs);
                 check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, fs));
             }
-            if (fp32 && c->nrep == 1 && g.ncent > 0) {
+            if (fp32 && g.ncent > 0) {
                 ProfScope ps(c, "far_coarse", fs);
                 check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
             }
@@ -2151,13 +2152,14 @@ smob_ctx* replicated(smob_ctx* c, int k) {
                             c->viscosity};
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
-    r->far_eps = 0.0;  // the several-column kernels read every column's own grid sources
+    r->far_eps = c->far_eps;  // replicas share the levels; each column's coarse strengths are its own
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
     build_context(r.get(), &geo);
     r->nrep = k;
     r->rep_M = c->M;
+    bind_geom(r.get());  // coarse points per replica
     for (const FarItem& f : r->items_tpt[0])
         if (f.problem == 0) r->items_rep.push_back(f);
     r->d_items_rep.upload(r->items_rep);
@@ -2336,6 +2338,8 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps) {
         set_device(c);
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old coarse tables
+        for (auto& kv : c->multi) smob_destroy(kv.second);  // several-RHS copies follow the new tolerance
+        c->multi.clear();
         c->far_eps = eps > 0 ? eps : 0.0;
         build_coarse(c);
         bind_geom(c);

@@ -167,30 +167,33 @@ __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned v
 }
 
 // f_e = coarse map x weighted sources: per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per sphere]. A CTA
-// computes 64 coarse nodes of up to 8 spheres, staging 32 fine nodes of the map and of the spheres'
-// sources per step; thread (sphere t / 16, nodes t % 16 + 16 i) keeps 4 x 3 accumulators.
-constexpr int kCgNodes = 64, kCgSph = 8, kCgK = 32;
-__global__ void __launch_bounds__(128) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
+// computes 64 coarse nodes of up to 8 spheres; its 4 groups of 128 threads take interleaved slices of
+// 16 fine nodes (map rows and the spheres' sources staged in shared memory), thread (sphere t / 16,
+// nodes t % 16 + 16 i) of a group keeps 4 x 3 accumulators, and the groups' sums are added in a fixed
+// order at the end.
+constexpr int kCgNodes = 64, kCgSph = 8, kCgK = 16, kCgGroups = 4;
+__global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
     const int4 d = g.cdesc[blockIdx.x];
     const int4 G = g.cgrp[d.x];
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
-    __shared__ float Ms[kCgK][kCgNodes];
-    __shared__ float4 Fs[kCgK][kCgSph];
+    __shared__ float Ms[kCgGroups][kCgK][kCgNodes];
+    __shared__ float4 Fs[kCgGroups][kCgK][kCgSph];
+    __shared__ float red[kCgGroups - 1][12][128];
     __shared__ int sbase[kCgSph], sout[kCgSph];
     __shared__ unsigned char sact[kCgSph];
-    const int t = threadIdx.x;
-    if (t < kCgSph) {
+    const int grp = threadIdx.x >> 7, t = threadIdx.x & 127;
+    if (threadIdx.x < kCgSph) {
         int sb = 0, so = 0;
         unsigned char a = 0;
-        if (t < ne) {
-            const int2 e = g.gent[d.z + t];
+        if (threadIdx.x < ne) {
+            const int2 e = g.gent[d.z + threadIdx.x];
             sb = g.gidx[e.x];
             so = e.y;
             a = (g.active && !g.active[g.prob[e.x]]) ? 0 : 1;
         }
-        sbase[t] = sb;
-        sout[t] = so;
-        sact[t] = a;
+        sbase[threadIdx.x] = sb;
+        sout[threadIdx.x] = so;
+        sact[threadIdx.x] = a;
     }
     __syncthreads();
     const int si = t >> 4, ni = t & 15;
@@ -198,24 +201,25 @@ __global__ void __launch_bounds__(128) k_coarse_src(DevGeom g, const float4* __r
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
     const float* __restrict__ map = g.cmap + G.x;
-    for (int j0 = 0; j0 < ng; j0 += kCgK) {
+    for (int jb = 0; jb < ng; jb += kCgK * kCgGroups) {
+        const int j0 = jb + grp * kCgK;  // this group's slice
 #pragma unroll
         for (int r = 0; r < kCgK * kCgNodes / 128; ++r) {
             const int idx = t + 128 * r, jj = idx / kCgNodes, kk = idx % kCgNodes;
-            Ms[jj][kk] = (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk) : 0.f;
+            Ms[grp][jj][kk] =
+                (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk) : 0.f;
         }
-#pragma unroll
-        for (int r = 0; r < kCgK * kCgSph / 128; ++r) {
-            const int idx = t + 128 * r, jj = idx / kCgSph, ss = idx % kCgSph;
-            Fs[jj][ss] = (j0 + jj < ng && ss < ne) ? src[sbase[ss] + j0 + jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t < kCgK * kCgSph) {
+            const int jj = t / kCgSph, ss = t % kCgSph;
+            Fs[grp][jj][ss] = (j0 + jj < ng && ss < ne) ? src[sbase[ss] + j0 + jj] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         __syncthreads();
-#pragma unroll 8
+#pragma unroll
         for (int jj = 0; jj < kCgK; ++jj) {
-            const float4 f = Fs[jj][si];
+            const float4 f = Fs[grp][jj][si];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float m = Ms[jj][ni + 16 * i];
+                const float m = Ms[grp][jj][ni + 16 * i];
                 acc[i][0] = fmaf(m, f.x, acc[i][0]);
                 acc[i][1] = fmaf(m, f.y, acc[i][1]);
                 acc[i][2] = fmaf(m, f.z, acc[i][2]);
@@ -223,9 +227,20 @@ __global__ void __launch_bounds__(128) k_coarse_src(DevGeom g, const float4* __r
         }
         __syncthreads();
     }
-    if (si < ne && sact[si]) {
+    if (grp > 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = acc[i][c];
+    }
+    __syncthreads();
+    if (grp == 0 && si < ne && sact[si]) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
+#pragma unroll
+            for (int q = 0; q < kCgGroups - 1; ++q)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[i][c] += red[q][3 * i + c][t];
             const int k = k0 + ni + 16 * i;
             if (k < cnt) g.csrc[sout[si] + k] = make_float4(acc[i][0], acc[i][1], acc[i][2], 0.f);
         }
@@ -478,6 +493,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
     if (!any) return;
     __shared__ float4 sp[kRepTile];
     __shared__ float4 sf[KB][kRepTile];
+    __shared__ unsigned votes_buf[2][kFarThreads / 32];
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const int t = it.t0 + threadIdx.x;
     const bool va = t < it.t1;
@@ -489,18 +505,23 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
     float ax[KB], ay[KB], az[KB];
 #pragma unroll
     for (int r = 0; r < KB; ++r) ax[r] = ay[r] = az[r] = 0.f;
-    for (int s = it.s0; s < it.s1; ++s) {
+    int parity = 0;
+    for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
         const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s);
-        if (__syncthreads_and(sk)) continue;
-        const int g0 = g.gidx[s], gl = g.glen[s];
+        // the same per-CTA choice as k_far32<TRAC, 1> over the same targets (replica 0's items)
+        const unsigned votes = cta_or(va ? (sk ? kBitSkip : level_bit(g, sa, s)) : 0u, votes_buf, parity);
+        if (!(votes & ~kBitSkip)) continue;
+        const float4 *SP, *SF;
+        int g0, gl;
+        const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
+        const long long rstride = coarse ? (long long)g.crep : (long long)rep_M;  // replica r's sources
         for (int base = 0; base < gl; base += kRepTile) {
             const int n = min(kRepTile, gl - base);
             __syncthreads();
             for (int k = threadIdx.x; k < n; k += kFarThreads) {
-                sp[k] = g.pos32[g0 + base + k];
+                sp[k] = SP[g0 + base + k];
 #pragma unroll
-                for (int r = 0; r < KB; ++r)
-                    sf[r][k] = r < nr ? src[(long long)(r0 + r) * rep_M + g0 + base + k] : z4;
+                for (int r = 0; r < KB; ++r) sf[r][k] = r < nr ? SF[(r0 + r) * rstride + g0 + base + k] : z4;
             }
             __syncthreads();
             if (sk) continue;
@@ -993,7 +1014,7 @@ int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool tr
 
 int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st) {
     if (g.ncent <= 0 || g.ncdesc <= 0) return 0;
-    k_coarse_src<<<g.ncdesc, 128, 0, st>>>(g, src32);
+    k_coarse_src<<<g.ncdesc, 128 * kCgGroups, 0, st>>>(g, src32);
     return 1;
 }
 

@@ -113,6 +113,7 @@ struct DevGeom {
     const double* cnode;       // unit nodes of the coarse orders, [node][3]
     const int* cnode_off;      // [kMaxOrder + 1] first node of order pe in cnode
     float4* csrc;              // coarse source strengths of the current FP32 pass (workspace)
+    int crep;                  // coarse points of one replica (several-RHS contexts; else all of them)
     // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of 64 coarse nodes x 8 spheres
     int ncdesc;
     const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
