@@ -192,13 +192,14 @@ def run_native(args, world, rank, local, dist):
 
     # ---- the same mixed solve with every FP32 far-field pair summed directly (no coarse equivalent sources)
     eps_default = mob.far_compression_info()[0]
-    mob.set_far_compression(0)
+    eps_hp_default = mob.far_compression_info(hp=True)[0]
+    mob.set_far_compression(0, 0)
     solve_dev(PREC_MIXED)
     ms_dir, st_dir = timed(PREC_MIXED, args.steps)
     vel_dir = np.zeros(n6)
     N.check(L.smob_memcpy_d2h(h, vel_dir.ctypes.data_as(ctypes.c_void_p), d_vel, 8 * n6))
     dir_total = allmax(dist, ms_dir.sum() / 1e3)
-    mob.set_far_compression(eps_default)
+    mob.set_far_compression(eps_default, eps_hp_default)
     solve_dev(PREC_MIXED)
 
     # ---- end to end through the host-pointer API
@@ -245,6 +246,7 @@ def run_native(args, world, rank, local, dist):
     achieved = 30.0 * evaluated / avg_s / 1e12 if avg_s > 0 else None
     c_l, c_ms = prof.get("far_coarse", (0, 0.0))
     eps, cpts, cent = mob.far_compression_info()
+    eps_hp, cpts_hp, cent_hp = mob.far_compression_info(hp=True)
     tot_prof = sum(v[1] for v in prof.values())
 
     # ---- CPU baseline: one FP64 operator pass of the oracle, times the FP64 solve's pass count
@@ -290,8 +292,8 @@ def run_native(args, world, rank, local, dist):
             "iterations": st_dir["iterations"], "passes_fp32": st_dir["operator_passes_fp32"],
             "relres": st_dir["relres"],
             "rel_err_vs_fp64": float(np.linalg.norm(vel_dir - vel_fp64) / np.linalg.norm(vel_fp64)),
-            "note": "the headline solve with the FP32 far field summed over every grid source pair "
-                    "(smob_set_far_compression(ctx, 0))"},
+            "note": "the headline solve with the far field summed over every grid source pair in every pass "
+                    "(smob_set_far_compression(ctx, 0, 0))"},
         "rel_err_mixed_vs_fp64": float(np.linalg.norm(vel_mixed - vel_fp64) / np.linalg.norm(vel_fp64)),
         "pair_interactions_per_s": round(pairs * (st_mixed["operator_passes_fp32"] + st_mixed["operator_passes_fp64"])
                                          / (ms_mixed.mean() / 1e3), 1),
@@ -302,7 +304,9 @@ def run_native(args, world, rank, local, dist):
                             "evaluated_pairs_per_pass": evaluated,
                             "evaluated_fraction": round(evaluated / direct, 4) if direct else None,
                             "coarse_strength_macs_per_pass": coarse_macs,
-                            "coarse_strength_ms_per_pass": round(c_ms / max(c_l, 1), 5)},
+                            "coarse_strength_ms_per_pass": round(c_ms / max(c_l, 1), 5),
+                            "eps_float_float": eps_hp, "coarse_points_float_float": cpts_hp,
+                            "entries_float_float": cent_hp},
         "roofline": {"kernel": "far_trac_fp32", "bound": "fp32_simt", "achieved": round(achieved, 3) if achieved else None,
                      "peak": round(f32.value, 3), "unit": "TFLOP/s",
                      "frac": round(achieved / f32.value, 4) if achieved else None,
@@ -404,6 +408,7 @@ def run_config(args, world, rank, local, dist):
     achieved = 30.0 * evaluated / avg_s / 1e12 if avg_s > 0 else None
     c_l, c_ms = prof.get("far_coarse", (0, 0.0))
     eps, cpts, cent = mob.far_compression_info()
+    eps_hp, cpts_hp, cent_hp = mob.far_compression_info(hp=True)
     its = [s["iterations"] for s in sts]
     # CPU restatement: pair rate measured on cfg2 (one FP64 operator pass), scaled to this workload
     c2 = configs.cfg2()
@@ -438,7 +443,9 @@ def run_config(args, world, rank, local, dist):
                             "evaluated_pairs_per_pass": evaluated,
                             "evaluated_fraction": round(evaluated / direct, 4) if direct else None,
                             "coarse_strength_macs_per_pass": coarse_macs,
-                            "coarse_strength_ms_per_pass": round(c_ms / max(c_l, 1), 5)},
+                            "coarse_strength_ms_per_pass": round(c_ms / max(c_l, 1), 5),
+                            "eps_float_float": eps_hp, "coarse_points_float_float": cpts_hp,
+                            "entries_float_float": cent_hp},
         "roofline": {"kernel": "far_trac_fp32", "bound": "fp32_simt", "achieved": round(achieved, 3) if achieved else None,
                      "peak": round(f32.value, 3), "unit": "TFLOP/s",
                      "frac": round(achieved / f32.value, 4) if achieved else None, "traffic": None,
@@ -630,7 +637,10 @@ def run_multi(args, world, rank, local, dist):
         vs = singles()
     t_single = allmax(dist, time.perf_counter() - t0)
     mob.set_far_tile(1)
+    eps32, eps_hp = mob.far_compression_info()[0], mob.far_compression_info(hp=True)[0]
+    mob.set_far_compression(eps32, 0)  # the several-column float-float pass sums every grid-point pair
     bitwise = bool(np.array_equal(mob.solveMobMulti(F, **kw), singles()))
+    mob.set_far_compression(eps32, eps_hp)
     err = float(np.linalg.norm(vm - vs) / np.linalg.norm(vs))
     if rank != 0:
         return None
@@ -644,6 +654,8 @@ def run_multi(args, world, rank, local, dist):
                               "ms_per_k_columns": round(1e3 * t_single / args.steps, 3), "far_tile": auto_tile},
             "speedup_vs_single_solves": round(t_single / t_multi, 3),
             "iterations_per_column": its, "rel_diff_vs_single_autotuned": err,
+            "bitwise_note": "with the FP32 coarse sources on and the float-float ones off (the several-column "
+                            "float-float kernel sums every grid-point pair)",
             "bitwise_equal_to_single_solves_tile1": bitwise}
 
 

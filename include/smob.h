@@ -202,20 +202,22 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * columns; every column's result equals bit for bit a smob_solve_mob of that column alone with
  * smob_set_far_tile(ctx, 1). The context must hold one problem. Internal copies of the geometry
  * are kept on the context per column count (at most 4 counts). */
-/* FP32 far field from coarse equivalent sources. Inside the FP32 operator passes (SMOB_PREC_MIXED:
- * the inner solves and the final velocity correction) the far field of a well-separated source sphere
- * is evaluated from equivalent sources on a coarser grid of the same sphere: its grid sources projected
- * onto the spherical harmonics of degree <= pe and re-weighted with the order-pe quadrature, which
- * reproduces the far field to ~(a_s / r_min)^(pe+1) relative (r_min: distance from the source centre to
- * the nearest target point). Each source sphere gets the coarse orders its far targets need for eps
- * (relative to the sphere's own contribution); near pairs, the own sphere and every FP64 and float-float
- * pass keep the direct sum over the grid points, so the high-precision residuals that decide
- * convergence, and the plain FP64 solve, are those of the reference's smooth quadrature. The reference
- * evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).
- * eps <= 0 turns it off (the direct sum everywhere); default 1e-7. */
-smob_status smob_set_far_compression(smob_ctx* ctx, double eps);
-/* current eps, coarse points held and (sphere, level) entries */
-smob_status smob_far_compression_info(const smob_ctx* ctx, double* eps, int* coarse_points, int* entries);
+/* Far field from coarse equivalent sources. For a well-separated pair of spheres the far field of the
+ * source sphere's grid sources is evaluated from equivalent sources on a coarser grid of the same
+ * sphere: its grid sources projected onto the spherical harmonics of degree <= pe and re-weighted with
+ * the order-pe quadrature, which reproduces the far field to ~(a_s / r_min)^(pe+1) relative (r_min:
+ * distance from the source centre to the nearest target point). Each source sphere gets the coarse
+ * orders its far targets need for the tolerance (relative to the sphere's own contribution). eps sets
+ * it for the FP32 operator passes (SMOB_PREC_MIXED inner solves and final velocity correction; default
+ * 1e-7), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
+ * layer, SMOB_PREC_FLOAT_FLOAT; default 1e-12). Near pairs, the own sphere and every FP64 pass keep the
+ * direct sum over the grid points: the plain FP64 solve is the reference's smooth quadrature. The
+ * reference evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).
+ * A tolerance <= 0 turns that set off (the direct sum). */
+smob_status smob_set_far_compression(smob_ctx* ctx, double eps, double eps_hp);
+/* the tolerance, coarse points held and (sphere, level) entries of the FP32 set (hp = 0) or the
+ * float-float set (hp = 1) */
+smob_status smob_far_compression_info(const smob_ctx* ctx, int hp, double* eps, int* coarse_points, int* entries);
 /* target-source pairs of one FP32 far-field pass with the current tile: the direct sum's (every far
  * pair), the evaluated ones (fine or coarse sources, as the kernels choose them per CTA), and the
  * multiply-adds of the coarse strengths per pass */

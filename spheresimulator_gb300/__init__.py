@@ -181,15 +181,19 @@ class _Context:
         """Force the FP32 far-field variant (1, 2 or 4 targets per thread) over the autotuner's choice."""
         N.check(self._L.smob_set_far_tile(self._h, int(targets_per_thread)))
 
-    def set_far_compression(self, eps):
-        """Tolerance of the FP32 far field's coarse equivalent sources for well-separated sphere pairs
-        (relative to each source sphere's contribution); eps <= 0 evaluates every pair directly."""
-        N.check(self._L.smob_set_far_compression(self._h, float(eps)))
+    def set_far_compression(self, eps, eps_hp=None):
+        """Tolerances of the far field's coarse equivalent sources for well-separated sphere pairs
+        (relative to each source sphere's contribution): eps for the FP32 passes, eps_hp for the
+        float-float passes (None: unchanged); <= 0 evaluates every pair directly."""
+        if eps_hp is None:
+            eps_hp = self.far_compression_info(hp=True)[0]
+        N.check(self._L.smob_set_far_compression(self._h, float(eps), float(eps_hp)))
 
-    def far_compression_info(self):
-        """(eps, coarse points held, (sphere, level) entries)"""
+    def far_compression_info(self, hp=False):
+        """(eps, coarse points held, (sphere, level) entries) of the FP32 set, or of the float-float set"""
         e, pts, ent = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
-        N.check(self._L.smob_far_compression_info(self._h, ctypes.byref(e), ctypes.byref(pts), ctypes.byref(ent)))
+        N.check(self._L.smob_far_compression_info(self._h, int(bool(hp)), ctypes.byref(e), ctypes.byref(pts),
+                                                  ctypes.byref(ent)))
         return e.value, pts.value, ent.value
 
     def far_pairs(self):

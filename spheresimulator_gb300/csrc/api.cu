@@ -107,6 +107,7 @@ constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host c
 // FP32 far field from coarse equivalent sources: per-pair tolerance (relative to the source sphere's
 // contribution) and the coarse orders a sphere may use, ascending
 constexpr double kCoarseEpsDefault = 1e-7;
+constexpr double kCoarseEpsHpDefault = 1e-12;  // float-float passes (refinement residuals, u_hp)
 constexpr double kCoarseMargin = 1.0;  // orders added to log(eps) / log(a_s / r_min) (measured, p = 16)
 constexpr int kCoarseLadder[] = {3, 4, 5, 6, 8, 10, 12, 14, 16, 20, 24, 28};
 // recycled solutions (warm_start 2): pairs (force_i, mu_i) of earlier solves kept per context, with
@@ -169,14 +170,24 @@ struct smob_ctx {
     DBuf d_active;
     // operator workspace
     DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
-    // FP32 far field from coarse equivalent sources (far_eps <= 0: off)
-    double far_eps = kCoarseEpsDefault;
-    std::vector<int4> clev;
-    std::vector<int2> cent;
-    int ncoarse = 0;
-    std::vector<int4> cdesc, cgrp;
-    std::vector<int2> gent;
-    DBuf d_clev, d_cent, d_cpos32, d_csrc, d_cmap, d_cnode, d_cnode_off, d_cdesc, d_cgrp, d_gent;
+    // far field from coarse equivalent sources: the FP32 set and the float-float set (eps <= 0: off)
+    struct CoarseHost {
+        double eps = 0;
+        bool hp = false;  // float-float set: FP64 maps, hi/lo points and strengths
+        std::vector<int4> clev;
+        std::vector<int2> cent;
+        int ncoarse = 0;
+        std::vector<int4> cdesc, cgrp;
+        std::vector<int2> gent;
+        DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent;
+    };
+    CoarseHost c32, chp;
+    DBuf d_cnode, d_cnode_off;
+    smob_ctx() {
+        c32.eps = kCoarseEpsDefault;
+        chp.eps = kCoarseEpsHpDefault;
+        chp.hp = true;
+    }
     DBuf d_in, d_out, d_tmp;  // host-pointer API staging
     // solver workspace
     int restart_cap = 0;
@@ -380,6 +391,7 @@ void upload_near(smob_ctx* c);
 void build_tables(smob_ctx* c);
 void bind_geom(smob_ctx* c);
 void build_coarse(smob_ctx* c);
+void coarse_grids(smob_ctx* c);
 
 void build_context(smob_ctx* c, const smob_geometry* geo) {
     const int N = geo->n_spheres;
@@ -575,7 +587,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     build_coarse(c);
     bind_geom(c);
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
-    check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
+    coarse_grids(c);
 }
 
 // ---------------------------------------------------------------- tables, near metadata, bindings
@@ -694,22 +706,21 @@ void build_tables(smob_ctx* c) {
 }
 
 // device pointers and sizes of the geometry, as the kernels receive them
-// Coarse levels of every source sphere for this geometry: for each far pair (t, s) of a problem the
-// coarsest ladder order pe < p_s with pe >= log(eps) / log(a_s / r_min) + margin, r_min = |c_t - c_s| - a_t
-// (the FP32 kernels recompute this per target and use the coarsest level built that satisfies it);
-// at most kCoarseLevels orders per sphere (the finest kept). Maps are shared per (p, pe).
-void build_coarse(smob_ctx* c) {
+// Coarse levels of every source sphere for this geometry and one tolerance: for each far pair (t, s) of
+// a problem the coarsest ladder order pe < p_s with pe >= log(eps) / log(a_s / r_min) + margin,
+// r_min = |c_t - c_s| - a_t (the kernels recompute this per target and use the coarsest level built that
+// satisfies it); at most kCoarseLevels orders per sphere (the finest kept). Maps are shared per (p, pe).
+void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>& nodes, std::vector<int>& node_off,
+                      std::vector<char>& have_nodes) {
     const int N = c->N;
-    c->clev.assign((size_t)N * kCoarseLevels, make_int4(0, 0, 0, 0));
-    c->cent.clear();
-    c->ncoarse = 0;
+    h.clev.assign((size_t)N * kCoarseLevels, make_int4(0, 0, 0, 0));
+    h.cent.clear();
+    h.ncoarse = 0;
     std::vector<float> maps;
-    std::map<int, int> map_off;                 // p * 64 + pe -> offset in maps
-    std::vector<double> nodes;
-    std::vector<int> node_off(kMaxOrder + 1, 0);
-    std::vector<char> have_nodes(kMaxOrder + 1, 0);
-    if (c->far_eps > 0) {
-        const double leps = std::log(c->far_eps);
+    std::vector<double> mapsd;
+    std::map<int, int> map_off;  // p * 64 + pe -> offset in the maps
+    if (h.eps > 0) {
+        const double leps = std::log(h.eps);
         for (int pi = 0; pi < c->P; ++pi) {
             const Problem& pr = c->problems[pi];
             for (int s = pr.s0; s < pr.s1; ++s) {
@@ -742,9 +753,15 @@ void build_coarse(smob_ctx* c) {
                     const int pe = pes[l];
                     const int key = ps * 64 + pe;
                     if (!map_off.count(key)) {
-                        const std::vector<float>& m = coarse_map(ps, pe);
-                        map_off[key] = (int)maps.size();
-                        maps.insert(maps.end(), m.begin(), m.end());
+                        if (h.hp) {
+                            const std::vector<double>& m = coarse_map_d(ps, pe);
+                            map_off[key] = (int)mapsd.size();
+                            mapsd.insert(mapsd.end(), m.begin(), m.end());
+                        } else {
+                            const std::vector<float>& m = coarse_map(ps, pe);
+                            map_off[key] = (int)maps.size();
+                            maps.insert(maps.end(), m.begin(), m.end());
+                        }
                     }
                     if (!have_nodes[pe]) {
                         std::vector<double> nv;
@@ -754,24 +771,24 @@ void build_coarse(smob_ctx* c) {
                         have_nodes[pe] = 1;
                     }
                     const int cnt = (pe + 1) * (2 * pe + 2);
-                    c->clev[(size_t)s * kCoarseLevels + l] = make_int4(pe, c->ncoarse, cnt, map_off[key]);
-                    c->cent.push_back(make_int2(s, l));
-                    c->ncoarse += cnt;
+                    h.clev[(size_t)s * kCoarseLevels + l] = make_int4(pe, h.ncoarse, cnt, map_off[key]);
+                    h.cent.push_back(make_int2(s, l));
+                    h.ncoarse += cnt;
                 }
             }
         }
     }
     // GEMM tiles of the per-pass strengths: entries grouped by map (p, pe), 8 spheres x 64 nodes per CTA
-    c->cdesc.clear();
-    c->cgrp.clear();
-    c->gent.clear();
+    h.cdesc.clear();
+    h.cgrp.clear();
+    h.gent.clear();
     struct MapGroup {
         int ng = 0, cnt = 0;
         std::vector<int2> ents;  // {sphere, first coarse point}
     };
     std::map<int, MapGroup> by_map;  // by map offset
-    for (const int2& e : c->cent) {
-        const int4 L = c->clev[(size_t)e.x * kCoarseLevels + e.y];
+    for (const int2& e : h.cent) {
+        const int4 L = h.clev[(size_t)e.x * kCoarseLevels + e.y];
         MapGroup& mg = by_map[L.w];
         mg.ng = c->glen[e.x];
         mg.cnt = L.z;
@@ -779,24 +796,43 @@ void build_coarse(smob_ctx* c) {
     }
     for (auto& kv : by_map) {
         const MapGroup& mg = kv.second;
-        const int grp = (int)c->cgrp.size();
-        c->cgrp.push_back(make_int4(kv.first, mg.ng, mg.cnt, 0));
-        const int first = (int)c->gent.size();
-        c->gent.insert(c->gent.end(), mg.ents.begin(), mg.ents.end());
+        const int grp = (int)h.cgrp.size();
+        h.cgrp.push_back(make_int4(kv.first, mg.ng, mg.cnt, 0));
+        const int first = (int)h.gent.size();
+        h.gent.insert(h.gent.end(), mg.ents.begin(), mg.ents.end());
         for (int e = 0; e < (int)mg.ents.size(); e += 8)
             for (int k0 = 0; k0 < mg.cnt; k0 += 64)
-                c->cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
+                h.cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
     }
-    c->d_clev.upload(c->clev);
-    c->d_cent.upload(c->cent);
-    c->d_cdesc.upload(c->cdesc);
-    c->d_cgrp.upload(c->cgrp);
-    c->d_gent.upload(c->gent);
-    c->d_cmap.upload(maps);
+    h.d_clev.upload(h.clev);
+    h.d_cent.upload(h.cent);
+    h.d_cdesc.upload(h.cdesc);
+    h.d_cgrp.upload(h.cgrp);
+    h.d_gent.upload(h.gent);
+    if (h.hp) h.d_cmap.upload(mapsd);
+    else h.d_cmap.upload(maps);
+    const size_t np = std::max(h.ncoarse, 1);
+    h.d_cpos32.alloc(sizeof(float4) * np);
+    if (h.hp) h.d_cpos32lo.alloc(sizeof(float4) * np);
+    h.d_csrc.alloc(sizeof(float4) * np * (h.hp ? 2 : 1));
+}
+
+void build_coarse(smob_ctx* c) {
+    std::vector<double> nodes;
+    std::vector<int> node_off(kMaxOrder + 1, 0);
+    std::vector<char> have_nodes(kMaxOrder + 1, 0);
+    build_coarse_set(c, c->c32, nodes, node_off, have_nodes);
+    build_coarse_set(c, c->chp, nodes, node_off, have_nodes);
     c->d_cnode.upload(nodes);
     c->d_cnode_off.upload(node_off);
-    c->d_cpos32.alloc(sizeof(float4) * std::max(c->ncoarse, 1));
-    c->d_csrc.alloc(sizeof(float4) * std::max(c->ncoarse, 1));
+}
+
+// coarse points of both sets (after the grid; geometry-dependent)
+void coarse_grids(smob_ctx* c) {
+    check_launch(c, launch_coarse_grid(c->g, c->g.cs32, c->d_org.as<double>(), c->c32.d_cpos32.as<float4>(), nullptr,
+                                       c->st));
+    check_launch(c, launch_coarse_grid(c->g, c->g.cshp, c->d_org.as<double>(), c->chp.d_cpos32.as<float4>(),
+                                       c->chp.d_cpos32lo.as<float4>(), c->st));
 }
 
 void bind_geom(smob_ctx* c) {
@@ -836,21 +872,27 @@ void bind_geom(smob_ctx* c) {
     g.map_val_d = c->d_map_val_d.as<double>();
     g.map_val_f = c->d_map_val_f.as<float>();
     g.active = c->d_active.as<unsigned char>();
-    g.ncent = (int)c->cent.size();
-    g.clog_eps = c->far_eps > 0 ? float(std::log(c->far_eps)) : 0.f;
-    g.cmargin = float(kCoarseMargin);
-    g.clev = c->d_clev.as<int4>();
-    g.cent = c->d_cent.as<int2>();
-    g.cpos32 = c->d_cpos32.as<float4>();
-    g.cmap = c->d_cmap.as<float>();
+    auto bind_set = [&](const smob_ctx::CoarseHost& h, CoarseSet& cs) {
+        cs.ncent = (int)h.cent.size();
+        cs.clog_eps = h.eps > 0 ? float(std::log(h.eps)) : 0.f;
+        cs.cmargin = float(kCoarseMargin);
+        cs.clev = h.d_clev.as<int4>();
+        cs.cent = h.d_cent.as<int2>();
+        cs.cpos32 = h.d_cpos32.as<float4>();
+        cs.cpos32lo = h.hp ? h.d_cpos32lo.as<float4>() : nullptr;
+        cs.cmap = h.hp ? nullptr : h.d_cmap.as<float>();
+        cs.cmapd = h.hp ? h.d_cmap.as<double>() : nullptr;
+        cs.csrc = h.d_csrc.as<float4>();
+        cs.crep = c->nrep > 1 ? h.ncoarse / c->nrep : h.ncoarse;
+        cs.ncdesc = (int)h.cdesc.size();
+        cs.cdesc = h.d_cdesc.as<int4>();
+        cs.cgrp = h.d_cgrp.as<int4>();
+        cs.gent = h.d_gent.as<int2>();
+    };
+    bind_set(c->c32, g.cs32);
+    bind_set(c->chp, g.cshp);
     g.cnode = c->d_cnode.as<double>();
     g.cnode_off = c->d_cnode_off.as<int>();
-    g.csrc = c->d_csrc.as<float4>();
-    g.crep = c->nrep > 1 ? c->ncoarse / c->nrep : c->ncoarse;
-    g.ncdesc = (int)c->cdesc.size();
-    g.cdesc = c->d_cdesc.as<int4>();
-    g.cgrp = c->d_cgrp.as<int4>();
-    g.gent = c->d_gent.as<int2>();
 }
 
 // Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on
@@ -946,6 +988,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
             {
                 ProfScope ps(c, "far_pack", fs);
                 check_launch(c, launch_far_pack_df(g, x, cc, c->d_srcdf.as<float4>(), fs));
+                check_launch(c, launch_coarse_src_df(g, c->d_srcdf.as<float4>(), fs));
             }
             ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df", fs);
             check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), tr ? 1 : 0,
@@ -955,7 +998,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 ProfScope ps(c, "far_pack", fs);
                 check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, fs));
             }
-            if (fp32 && g.ncent > 0) {
+            if (fp32 && g.cs32.ncent > 0) {
                 ProfScope ps(c, "far_coarse", fs);
                 check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
             }
@@ -1022,6 +1065,7 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
     {
         ProfScope ps(c, "far_pack", fs);
         check_launch(c, launch_far_pack_df(g, x, 1.0, c->d_srcdf.as<float4>(), fs));
+        if (c->nrep == 1) check_launch(c, launch_coarse_src_df(g, c->d_srcdf.as<float4>(), fs));
     }
     {
         ProfScope ps(c, "far_both_df", fs);
@@ -1675,7 +1719,7 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
     build_coarse(c);
     bind_geom(c);
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
-    check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
+    coarse_grids(c);
     c->host_grid_stale = true;
     c->drop_graphs();
     c->rk = 0;  // recycled solutions belong to the old operator
@@ -1962,6 +2006,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 // both kernels from one float-float pass over the pairs (the mixed solve's fused pass)
                 c->d_partial64_sl.alloc(sizeof(double) * c->partial64);
                 check_launch(c, launch_far_pack_df(c->g, din, 1.0, c->d_srcdf.as<float4>(), c->st));
+                check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                 {
                     ProfScope ps(c, "far_both_df");
                     check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
@@ -1978,13 +2023,14 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 if (cc == 0.0) continue;
                 if (dfar) {
                     check_launch(c, launch_far_pack_df(c->g, din, cc, c->d_srcdf.as<float4>(), c->st));
+                    check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                     ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
                     check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(),
                                                         tr ? 1 : 0, c->d_srcdf.as<float4>(), static_cast<double*>(partial),
                                                         nullptr, c->st));
                 } else {
                     check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
-                    if (fp32 && c->g.ncent > 0) {
+                    if (fp32 && c->g.cs32.ncent > 0) {
                         ProfScope ps(c, "far_coarse");
                         check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
                     }
@@ -2152,7 +2198,8 @@ smob_ctx* replicated(smob_ctx* c, int k) {
                             c->viscosity};
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
-    r->far_eps = c->far_eps;  // replicas share the levels; each column's coarse strengths are its own
+    r->c32.eps = c->c32.eps;  // replicas share the levels; each column's coarse strengths are its own
+    r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
@@ -2331,30 +2378,33 @@ smob_status smob_tuning(const smob_ctx* c, int* targets_per_thread, double* vari
     });
 }
 
-smob_status smob_set_far_compression(smob_ctx* c, double eps) {
+smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
         need(std::isfinite(eps) && eps < 1e-3, "far-field tolerance must be below 1e-3 (<= 0: off)");
+        need(std::isfinite(eps_hp) && eps_hp < 1e-9, "float-float far-field tolerance must be below 1e-9 (<= 0: off)");
         set_device(c);
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old coarse tables
         for (auto& kv : c->multi) smob_destroy(kv.second);  // several-RHS copies follow the new tolerance
         c->multi.clear();
-        c->far_eps = eps > 0 ? eps : 0.0;
+        c->c32.eps = eps > 0 ? eps : 0.0;
+        c->chp.eps = eps_hp > 0 ? eps_hp : 0.0;
         build_coarse(c);
         bind_geom(c);
-        check_launch(c, launch_coarse_grid(c->g, c->d_org.as<double>(), c->d_cpos32.as<float4>(), c->st));
+        coarse_grids(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
 }
 
-smob_status smob_far_compression_info(const smob_ctx* c, double* eps, int* coarse_points, int* entries) {
+smob_status smob_far_compression_info(const smob_ctx* c, int hp, double* eps, int* coarse_points, int* entries) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        if (eps) *eps = c->far_eps;
-        if (coarse_points) *coarse_points = c->ncoarse;
-        if (entries) *entries = (int)c->cent.size();
+        const smob_ctx::CoarseHost& h = hp ? c->chp : c->c32;
+        if (eps) *eps = h.eps;
+        if (coarse_points) *coarse_points = h.ncoarse;
+        if (entries) *entries = (int)h.cent.size();
         return SMOB_OK;
     });
 }
@@ -2365,7 +2415,8 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
         // the FP32 kernels' per-CTA choice replayed on the host for the current work items: a source
         // sphere is skipped when every target skips it, read from its grid points when some target
         // skips it or needs them, else from the finest coarse level any target votes for
-        const double leps = c->far_eps > 0 ? std::log(c->far_eps) : 0.0;
+        const smob_ctx::CoarseHost& h = c->c32;
+        const double leps = h.eps > 0 ? std::log(h.eps) : 0.0;
         long long dir = 0, ev = 0;
         std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
         for (const FarItem& it : c->items32) {
@@ -2385,8 +2436,8 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
                     if (skip) continue;
                     keep += ts.second;
                     int lv = -1;
-                    const int4* L = &c->clev[(size_t)s * kCoarseLevels];
-                    if (!c->cent.empty() && L[0].x != 0) {
+                    const int4* L = &h.clev[(size_t)s * kCoarseLevels];
+                    if (!h.cent.empty() && L[0].x != 0) {
                         double d2 = 0;
                         for (int k = 0; k < 3; ++k) {
                             const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
@@ -2408,11 +2459,11 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
                 dir += (long long)keep * c->glen[s];
                 if (keep == 0) continue;
                 if (fine || keep < all) ev += (long long)keep * c->glen[s];
-                else ev += (long long)all * c->clev[(size_t)s * kCoarseLevels + lvmax].z;
+                else ev += (long long)all * h.clev[(size_t)s * kCoarseLevels + lvmax].z;
             }
         }
         long long macs = 0;
-        for (const int2& e : c->cent) macs += 3LL * c->glen[e.x] * c->clev[(size_t)e.x * kCoarseLevels + e.y].z;
+        for (const int2& e : h.cent) macs += 3LL * c->glen[e.x] * h.clev[(size_t)e.x * kCoarseLevels + e.y].z;
         if (direct) *direct = dir;
         if (evaluated) *evaluated = ev;
         if (coarse_macs) *coarse_macs = macs;

@@ -116,9 +116,9 @@ __device__ __forceinline__ bool excluded(const int* __restrict__ nbr_src, int& c
 constexpr unsigned kBitFine = 1u << kCoarseLevels;  // the sphere's own grid sources
 constexpr unsigned kBitSkip = 2u << kCoarseLevels;  // own sphere or near pair of some target
 
-__device__ __forceinline__ unsigned level_bit(const DevGeom& g, int t, int s) {
-    if (g.ncent == 0) return kBitFine;
-    const int4* L = g.clev + s * kCoarseLevels;
+__device__ __forceinline__ unsigned level_bit(const DevGeom& g, const CoarseSet& cs, int t, int s) {
+    if (cs.ncent == 0) return kBitFine;
+    const int4* L = cs.clev + s * kCoarseLevels;
     if (__ldg(&L[0].x) == 0) return kBitFine;
     const float dx = float(__ldg(g.center + 3 * t) - __ldg(g.center + 3 * s));
     const float dy = float(__ldg(g.center + 3 * t + 1) - __ldg(g.center + 3 * s + 1));
@@ -126,7 +126,7 @@ __device__ __forceinline__ unsigned level_bit(const DevGeom& g, int t, int s) {
     const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - float(__ldg(g.radius + t));
     const float as = float(__ldg(g.radius + s));
     if (!(rmin > as)) return kBitFine;
-    const float need = g.clog_eps / __logf(as / rmin) + g.cmargin;
+    const float need = cs.clog_eps / __logf(as / rmin) + cs.cmargin;
 #pragma unroll 1
     for (int l = 0; l < kCoarseLevels; ++l) {
         const int pe = __ldg(&L[l].x);
@@ -147,14 +147,14 @@ __device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[kFarThr
     return r;
 }
 
-// the CTA's source range for sphere s from its votes: fine grid points or one coarse level
+// the CTA's source range for sphere s from its votes: fine grid points or one coarse level (FP32 set)
 __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned votes, const float4* src,
                                              const float4*& P, const float4*& F, int& g0, int& gl) {
     const bool coarse = !(votes & (kBitSkip | kBitFine));
     if (coarse) {
-        const int4 L = g.clev[s * kCoarseLevels + (31 - __clz(votes))];
-        P = g.cpos32;
-        F = g.csrc;
+        const int4 L = g.cs32.clev[s * kCoarseLevels + (31 - __clz(votes))];
+        P = g.cs32.cpos32;
+        F = g.cs32.csrc;
         g0 = L.y;
         gl = L.z;
     } else {
@@ -173,8 +173,9 @@ __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned v
 // order at the end.
 constexpr int kCgNodes = 64, kCgSph = 8, kCgK = 16, kCgGroups = 4;
 __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
-    const int4 d = g.cdesc[blockIdx.x];
-    const int4 G = g.cgrp[d.x];
+    const CoarseSet& cs = g.cs32;
+    const int4 d = cs.cdesc[blockIdx.x];
+    const int4 G = cs.cgrp[d.x];
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
     __shared__ float Ms[kCgGroups][kCgK][kCgNodes];
     __shared__ float4 Fs[kCgGroups][kCgK][kCgSph];
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
         int sb = 0, so = 0;
         unsigned char a = 0;
         if (threadIdx.x < ne) {
-            const int2 e = g.gent[d.z + threadIdx.x];
+            const int2 e = cs.gent[d.z + threadIdx.x];
             sb = g.gidx[e.x];
             so = e.y;
             a = (g.active && !g.active[g.prob[e.x]]) ? 0 : 1;
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
     float acc[4][3];
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
-    const float* __restrict__ map = g.cmap + G.x;
+    const float* __restrict__ map = cs.cmap + G.x;
     for (int jb = 0; jb < ng; jb += kCgK * kCgGroups) {
         const int j0 = jb + grp * kCgK;  // this group's slice
 #pragma unroll
@@ -242,7 +243,96 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
 #pragma unroll
                 for (int c = 0; c < 3; ++c) acc[i][c] += red[q][3 * i + c][t];
             const int k = k0 + ni + 16 * i;
-            if (k < cnt) g.csrc[sout[si] + k] = make_float4(acc[i][0], acc[i][1], acc[i][2], 0.f);
+            if (k < cnt) cs.csrc[sout[si] + k] = make_float4(acc[i][0], acc[i][1], acc[i][2], 0.f);
+        }
+    }
+}
+
+// The float-float set's strengths: the same GEMM tiles in FP64 (maps in FP64, sources hi + lo), two
+// split-K groups of 128 threads; each strength is stored as a hi/lo float pair like the grid sources.
+constexpr int kCgGroupsD = 2;
+__global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, const float4* __restrict__ src2) {
+    const CoarseSet& cs = g.cshp;
+    const int4 d = cs.cdesc[blockIdx.x];
+    const int4 G = cs.cgrp[d.x];
+    const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
+    __shared__ double Ms[kCgGroupsD][kCgK][kCgNodes];
+    __shared__ double4 Fs[kCgGroupsD][kCgK][kCgSph];
+    __shared__ double red[kCgGroupsD - 1][12][128];
+    __shared__ int sbase[kCgSph], sout[kCgSph];
+    __shared__ unsigned char sact[kCgSph];
+    const int grp = threadIdx.x >> 7, t = threadIdx.x & 127;
+    if (threadIdx.x < kCgSph) {
+        int sb = 0, so = 0;
+        unsigned char a = 0;
+        if (threadIdx.x < ne) {
+            const int2 e = cs.gent[d.z + threadIdx.x];
+            sb = g.gidx[e.x];
+            so = e.y;
+            a = (g.active && !g.active[g.prob[e.x]]) ? 0 : 1;
+        }
+        sbase[threadIdx.x] = sb;
+        sout[threadIdx.x] = so;
+        sact[threadIdx.x] = a;
+    }
+    __syncthreads();
+    const int si = t >> 4, ni = t & 15;
+    double acc[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
+    const double* __restrict__ map = cs.cmapd + G.x;
+    for (int jb = 0; jb < ng; jb += kCgK * kCgGroupsD) {
+        const int j0 = jb + grp * kCgK;
+#pragma unroll
+        for (int r = 0; r < kCgK * kCgNodes / 128; ++r) {
+            const int idx = t + 128 * r, jj = idx / kCgNodes, kk = idx % kCgNodes;
+            Ms[grp][jj][kk] =
+                (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk) : 0.0;
+        }
+        if (t < kCgK * kCgSph) {
+            const int jj = t / kCgSph, ss = t % kCgSph;
+            double4 f = make_double4(0, 0, 0, 0);
+            if (j0 + jj < ng && ss < ne) {
+                const float4 h = src2[2LL * (sbase[ss] + j0 + jj)], l = src2[2LL * (sbase[ss] + j0 + jj) + 1];
+                f = make_double4(double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z), 0.0);
+            }
+            Fs[grp][jj][ss] = f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int jj = 0; jj < kCgK; ++jj) {
+            const double4 f = Fs[grp][jj][si];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double m = Ms[grp][jj][ni + 16 * i];
+                acc[i][0] = fma(m, f.x, acc[i][0]);
+                acc[i][1] = fma(m, f.y, acc[i][1]);
+                acc[i][2] = fma(m, f.z, acc[i][2]);
+            }
+        }
+        __syncthreads();
+    }
+    if (grp > 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = acc[i][c];
+    }
+    __syncthreads();
+    if (grp == 0 && si < ne && sact[si]) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+            for (int q = 0; q < kCgGroupsD - 1; ++q)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[i][c] += red[q][3 * i + c][t];
+            const int k = k0 + ni + 16 * i;
+            if (k < cnt) {
+                const float hx = float(acc[i][0]), hy = float(acc[i][1]), hz = float(acc[i][2]);
+                cs.csrc[2LL * (sout[si] + k)] = make_float4(hx, hy, hz, 0.f);
+                cs.csrc[2LL * (sout[si] + k) + 1] = make_float4(float(acc[i][0] - double(hx)), float(acc[i][1] - double(hy)),
+                                                                float(acc[i][2] - double(hz)), 0.f);
+            }
         }
     }
 }
@@ -323,7 +413,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
         for (int u = 0; u < T; ++u) {
             sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
             none = none && !sk[u];
-            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, sid[u], s);
+            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, g.cs32, sid[u], s);
         }
         const unsigned votes = cta_or(vote, votes_buf, parity);
         if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
@@ -423,7 +513,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
         for (int u = 0; u < TPT; ++u) {
             sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
             none = none && !sk[u];
-            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, sid[u], s);
+            if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, g.cs32, sid[u], s);
         }
         const unsigned votes = cta_or(vote, votes_buf, parity);
         if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
@@ -509,12 +599,12 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
     for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
         const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s);
         // the same per-CTA choice as k_far32<TRAC, 1> over the same targets (replica 0's items)
-        const unsigned votes = cta_or(va ? (sk ? kBitSkip : level_bit(g, sa, s)) : 0u, votes_buf, parity);
+        const unsigned votes = cta_or(va ? (sk ? kBitSkip : level_bit(g, g.cs32, sa, s)) : 0u, votes_buf, parity);
         if (!(votes & ~kBitSkip)) continue;
         const float4 *SP, *SF;
         int g0, gl;
         const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
-        const long long rstride = coarse ? (long long)g.crep : (long long)rep_M;  // replica r's sources
+        const long long rstride = coarse ? (long long)g.cs32.crep : (long long)rep_M;  // replica r's sources
         for (int base = 0; base < gl; base += kRepTile) {
             const int n = min(kRepTile, gl - base);
             __syncthreads();
@@ -738,6 +828,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
         n2{f2(NH[0].z, NH[1].z), f2(NL[0].z, NL[1].z)};
     float2 xh = f2(0.f, 0.f), xl = xh, yh = xh, yl = xh, zh = xh, zl = xh;     // traction, or SL for KIND 0
     float2 sxh = xh, sxl = xh, syh = xh, syl = xh, szh = xh, szl = xh;          // single layer for KIND 2
+    __shared__ unsigned votes_buf[2][kFarThreads / 32];
     // one source against the two packed targets (mx, my, mz); keep scales the source weight per lane
     auto pair = [&](const df2& mx, const df2& my, const df2& mz, const float4& qh, const float4& ql,
                     const float4& fh, const float4& fl, bool masked, float2 keep) {
@@ -781,11 +872,29 @@ __global__ void __launch_bounds__(kFarThreads, 3)
             df_acc(ch, cl, df_mul_u(k3, rz));
         }
     };
-    for (int s = it.s0; s < it.s1; ++s) {
+    int parity = 0;
+    for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
         bool sk[2];
         sk[0] = !val[0] || excluded(g.nbr_src, cur[0], end[0], sid[0], s);
         sk[1] = !val[1] || excluded(g.nbr_src, cur[1], end[1], sid[1], s);
-        if (__syncthreads_and(sk[0] && sk[1])) continue;
+        unsigned vote = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (val[h]) vote |= sk[h] ? kBitSkip : level_bit(g, g.cshp, sid[h], s);
+        const unsigned votes = cta_or(vote, votes_buf, parity);
+        if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
+        // coarse level of the float-float set, or the grid sources
+        const bool coarse = !(votes & (kBitSkip | kBitFine));
+        const float4 *QH = g.pos32, *QL = g.pos32lo, *QF = src;
+        int g0 = g.gidx[s], gl = g.glen[s];
+        if (coarse) {
+            const int4 L = g.cshp.clev[s * kCoarseLevels + (31 - __clz(votes))];
+            QH = g.cshp.cpos32;
+            QL = g.cshp.cpos32lo;
+            QF = g.cshp.csrc;
+            g0 = L.y;
+            gl = L.z;
+        }
         const bool masked = sk[0] || sk[1];
         // A lane whose target skips this sphere is moved to a point 1e18 away and its source weight
         // is zeroed: its terms are exact zeros (r^-5 underflows, no 0*inf at r = 0 on its own sphere).
@@ -794,15 +903,14 @@ __global__ void __launch_bounds__(kFarThreads, 3)
         const df2 mx{__fadd2_rn(tx.h, far2), __fmul2_rn(tx.l, keep)};
         const df2 my{__fadd2_rn(ty.h, far2), __fmul2_rn(ty.l, keep)};
         const df2 mz{__fadd2_rn(tz.h, far2), __fmul2_rn(tz.l, keep)};
-        const int g0 = g.gidx[s], gl = g.glen[s];
         for (int base = 0; base < gl; base += kFarTile) {
             const int n = min(kFarTile, gl - base);
             __syncthreads();
             for (int k = threadIdx.x; k < n; k += kFarThreads) {
-                sph[k] = g.pos32[g0 + base + k];
-                spl[k] = g.pos32lo[g0 + base + k];
-                sfh[k] = src[2 * (g0 + base + k)];
-                sfl[k] = src[2 * (g0 + base + k) + 1];
+                sph[k] = QH[g0 + base + k];
+                spl[k] = QL[g0 + base + k];
+                sfh[k] = QF[2 * (g0 + base + k)];
+                sfl[k] = QF[2 * (g0 + base + k) + 1];
             }
             __syncthreads();
             if (!masked) {
@@ -1012,9 +1120,15 @@ int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool tr
     return 1;
 }
 
+int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st) {
+    if (g.cshp.ncent <= 0 || g.cshp.ncdesc <= 0) return 0;
+    k_coarse_src_df<<<g.cshp.ncdesc, 128 * kCgGroupsD, 0, st>>>(g, src2);
+    return 1;
+}
+
 int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st) {
-    if (g.ncent <= 0 || g.ncdesc <= 0) return 0;
-    k_coarse_src<<<g.ncdesc, 128 * kCgGroups, 0, st>>>(g, src32);
+    if (g.cs32.ncent <= 0 || g.cs32.ncdesc <= 0) return 0;
+    k_coarse_src<<<g.cs32.ncdesc, 128 * kCgGroups, 0, st>>>(g, src32);
     return 1;
 }
 

@@ -364,14 +364,14 @@ void unit_nodes(int p, std::vector<double>& xyz) {
         }
 }
 
-// Equivalent sources on the order-pe grid of the same sphere: f_e[k] = W_pe[k] sum_j K(k, j) f[j],
+// Equivalent sources on the order-pe grid of the same sphere (FP64 map; coarse_map is its FP32 copy): f_e[k] = W_pe[k] sum_j K(k, j) f[j],
 // K(k, j) = sum_{n <= pe} (2n+1)/(4 pi) P_n(nu_k . nu_j) (the addition theorem: the reproducing kernel
 // of the harmonics of degree <= pe). f are weighted grid sources (w_j x_j), so with the order-p
 // quadrature exact to degree 2p+1 this is the order-p projection of x onto degree <= pe, sampled at
 // the coarse nodes and weighted with the coarse quadrature.
-const std::vector<float>& coarse_map(int p, int pe) {
+const std::vector<double>& coarse_map_d(int p, int pe) {
     static std::mutex mu;
-    static std::map<int, std::unique_ptr<std::vector<float>>> cache;
+    static std::map<int, std::unique_ptr<std::vector<double>>> cache;
     const int key = p * 64 + pe;
     {
         std::lock_guard<std::mutex> lk(mu);
@@ -383,7 +383,7 @@ const std::vector<float>& coarse_map(int p, int pe) {
     unit_nodes(p, nf);
     unit_nodes(pe, nc);
     const int ng = int(nf.size() / 3), ne = int(nc.size() / 3);
-    auto M = std::make_unique<std::vector<float>>(size_t(ng) * ne);
+    auto M = std::make_unique<std::vector<double>>(size_t(ng) * ne);
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < ng; ++j)
         for (int k = 0; k < ne; ++k) {
@@ -398,8 +398,27 @@ const std::vector<float>& coarse_map(int p, int pe) {
                 p1 = p2;
                 sum += (2.0 * (n + 1) + 1) * p2;
             }
-            (*M)[size_t(j) * ne + k] = float(Te.wq[k / Te.nphi] * sum / (4 * PI));
+            (*M)[size_t(j) * ne + k] = Te.wq[k / Te.nphi] * sum / (4 * PI);
         }
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return *it->second;
+    auto& ref = *M;
+    cache[key] = std::move(M);
+    return ref;
+}
+
+const std::vector<float>& coarse_map(int p, int pe) {
+    static std::mutex mu;
+    static std::map<int, std::unique_ptr<std::vector<float>>> cache;
+    const int key = p * 64 + pe;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return *it->second;
+    }
+    const std::vector<double>& d = coarse_map_d(p, pe);
+    auto M = std::make_unique<std::vector<float>>(d.begin(), d.end());
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) return *it->second;

@@ -38,6 +38,7 @@ void unit_nodes(int p, std::vector<double>& xyz);
 // FP32 map from the weighted grid sources of an order-p sphere to equivalent sources on its order-pe
 // grid (pe < p), transposed: [j (fine node)][k (coarse node)]
 const std::vector<float>& coarse_map(int p, int pe);
+const std::vector<double>& coarse_map_d(int p, int pe);
 // recurrence coefficients of the irregular solid harmonics up to degree nmax:
 // c1[cidx(n,m)] = (2n+1)/sqrt((n+1)^2-m^2), c2[cidx(n,m)] = sqrt((n^2-m^2)/((n+1)^2-m^2)), diag[m] = sqrt((2m-1)/(2m))
 void theta_recurrence(int nmax, std::vector<double>& c1, std::vector<double>& c2, std::vector<double>& diag);

@@ -65,6 +65,25 @@ struct Problem {
     int c0, c1;      // reduction chunk range (segmented dots)
 };
 
+// coarse equivalent sources of one tolerance (see DevGeom)
+struct CoarseSet {
+    int ncent;                 // (sphere, level) entries
+    float clog_eps, cmargin;
+    const int4* clev;          // [N][kCoarseLevels] {pe (0: unused), first coarse point, count, map offset}
+    const int2* cent;          // [ncent] {sphere, level}
+    const float4* cpos32;      // coarse points: x, y, z relative to the problem origin, w = sphere id bits
+    const float4* cpos32lo;    // float-float set: the coordinates' low parts
+    const float* cmap;         // FP32 set: coarse maps, [fine node][coarse node] per (p, pe)
+    const double* cmapd;       // float-float set: the same maps in FP64
+    float4* csrc;              // strengths of the current pass (float-float set: hi, lo interleaved)
+    int crep;                  // coarse points of one replica (several-RHS contexts; else all of them)
+    // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of 64 coarse nodes x 8 spheres
+    int ncdesc;
+    const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
+    const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
+    const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
+};
+
 struct DevGeom {
     int N, M, P;
     int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
@@ -101,24 +120,13 @@ struct DevGeom {
     const double* map_val_d;
     const float* map_val_f;
     const unsigned char* active;  // per problem: operator work enabled
-    // FP32 far field from coarse equivalent sources for well-separated sphere pairs (ncent = 0: off).
-    // A source sphere s has up to kCoarseLevels coarse orders pe, ascending; a target sphere t may use
-    // the coarsest with pe >= clog_eps / log(a_s / (|c_t - c_s| - a_t)) + cmargin.
-    int ncent;                 // (sphere, level) entries
-    float clog_eps, cmargin;
-    const int4* clev;          // [N][kCoarseLevels] {pe (0: unused), first coarse point, count, map offset}
-    const int2* cent;          // [ncent] {sphere, level}
-    const float4* cpos32;      // coarse points: x, y, z relative to the problem origin, w = sphere id bits
-    const float* cmap;         // coarse maps, [fine node][coarse node] per (p, pe)
+    // Far field from coarse equivalent sources for well-separated sphere pairs: one set for the FP32
+    // passes and one, with a tighter tolerance, for the float-float passes (ncent = 0: off). A source
+    // sphere s has up to kCoarseLevels coarse orders pe, ascending; a target sphere t may use the
+    // coarsest with pe >= clog_eps / log(a_s / (|c_t - c_s| - a_t)) + cmargin.
+    CoarseSet cs32, cshp;
     const double* cnode;       // unit nodes of the coarse orders, [node][3]
     const int* cnode_off;      // [kMaxOrder + 1] first node of order pe in cnode
-    float4* csrc;              // coarse source strengths of the current FP32 pass (workspace)
-    int crep;                  // coarse points of one replica (several-RHS contexts; else all of them)
-    // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of 64 coarse nodes x 8 spheres
-    int ncdesc;
-    const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
-    const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
-    const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
 };
 
 // ---------------------------------------------------------------- kernels (launch wrappers)
@@ -129,12 +137,16 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 // coarse equivalent-source strengths of this pass from the FP32 grid sources (before every FP32
 // launch_far_field when g.ncent > 0)
 int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st);
+// the float-float set's strengths (hi, lo) from the float-float grid sources of launch_far_pack_df
+int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
-// coarse points of every (sphere, level) entry, relative to the problem origins (after launch_regrid)
-int launch_coarse_grid(const DevGeom& g, const double* org, float4* cpos32, cudaStream_t st);
+// coarse points of every (sphere, level) entry of a set, relative to the problem origins (after
+// launch_regrid); cpos32lo (may be null) receives the low parts
+int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org, float4* cpos32, float4* cpos32lo,
+                       cudaStream_t st);
 // FP32 far field of nrep replicas of one problem (replica r = problem r, points [r*rep_M, (r+1)*rep_M)):
 // items are replica 0's (kFarThreads targets each); each pair's geometry serves all replicas
 int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,

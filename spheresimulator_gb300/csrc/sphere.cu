@@ -412,20 +412,24 @@ __global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __re
 }
 
 // coarse points of one (sphere, level) entry per CTA: the order-pe unit nodes placed like the sphere's
-// own grid (k_regrid), relative to the problem origin in FP32
-__global__ void k_coarse_grid(DevGeom g, const double* __restrict__ org, float4* __restrict__ cpos32) {
-    const int2 e = g.cent[blockIdx.x];
+// own grid (k_regrid), relative to the problem origin in FP32 (and the low parts when asked)
+__global__ void k_coarse_grid(DevGeom g, CoarseSet cs, const double* __restrict__ org, float4* __restrict__ cpos32,
+                              float4* __restrict__ cpos32lo) {
+    const int2 e = cs.cent[blockIdx.x];
     const int s = e.x;
-    const int4 L = g.clev[s * kCoarseLevels + e.y];
+    const int4 L = cs.clev[s * kCoarseLevels + e.y];
     const double* nodes = g.cnode + 3LL * g.cnode_off[L.x];
     const double a = g.radius[s];
     const double* o = org + 3 * g.prob[s];
     for (int k = threadIdx.x; k < L.z; k += blockDim.x) {
-        double n[3];
+        double n[3], r[3];
         qrot_rn(g.quat + 4 * s, nodes + 3 * k, n);
-        float r[3];
-        for (int d = 0; d < 3; ++d) r[d] = float(__dsub_rn(__dadd_rn(__dmul_rn(a, n[d]), g.center[3 * s + d]), o[d]));
-        cpos32[L.y + k] = make_float4(r[0], r[1], r[2], __int_as_float(s));
+        for (int d = 0; d < 3; ++d) r[d] = __dsub_rn(__dadd_rn(__dmul_rn(a, n[d]), g.center[3 * s + d]), o[d]);
+        const float4 p = make_float4(float(r[0]), float(r[1]), float(r[2]), __int_as_float(s));
+        cpos32[L.y + k] = p;
+        if (cpos32lo)
+            cpos32lo[L.y + k] = make_float4(float(__dsub_rn(r[0], double(p.x))), float(__dsub_rn(r[1], double(p.y))),
+                                            float(__dsub_rn(r[2], double(p.z))), 0.f);
     }
 }
 
@@ -490,9 +494,10 @@ int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st) {
     return 1;
 }
 
-int launch_coarse_grid(const DevGeom& g, const double* org, float4* cpos32, cudaStream_t st) {
-    if (g.ncent <= 0) return 0;
-    k_coarse_grid<<<g.ncent, 128, 0, st>>>(g, org, cpos32);
+int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org, float4* cpos32, float4* cpos32lo,
+                       cudaStream_t st) {
+    if (cs.ncent <= 0) return 0;
+    k_coarse_grid<<<cs.ncent, 128, 0, st>>>(g, cs, org, cpos32, cpos32lo);
     return 1;
 }
 

@@ -4,7 +4,7 @@ the tolerance, and batches and geometry updates."""
 import numpy as np
 import pytest
 
-from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKMobMat, SphereSTKSHOperator, configs
+from spheresimulator_gb300 import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SphereSTKMobMat, SphereSTKSHOperator, configs
 
 pytestmark = pytest.mark.gpu
 
@@ -29,12 +29,29 @@ def test_far_field_matches_direct_sum():
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
     comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
     g.set_far_compression(0)
-    assert g.far_compression_info()[1:] == (0, 0)
+    assert g.far_compression_info()[1:] == (0, 0) and g.far_compression_info(hp=True)[2] > 0
     direct = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
     # the compression error sits at the FP32 rounding level of the direct sum
     assert _rel(direct, fp64) < 2e-5
     assert _rel(comp, fp64) < 2e-5
     assert _rel(comp, direct) < 2e-6
+
+
+def test_float_float_far_field_with_coarse_sources():
+    """The float-float set (tolerance 1e-12) against the direct float-float sum and the FP64 sum."""
+    c = _spread(seed=9, n=24, p=12, box=26.0)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    eps_hp, pts, ent = g.far_compression_info(hp=True)
+    assert eps_hp == 1e-12 and ent > 0 and pts > 0
+    x = np.random.default_rng(9).standard_normal(3 * g.n_points)
+    fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
+    comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
+    g.set_far_compression(1e-7, 0)
+    assert g.far_compression_info(hp=True)[1:] == (0, 0)
+    direct = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
+    # float-float sums carry ~1e-12 relative rounding on this size; the coarse sources add below 1e-11
+    assert _rel(direct, fp64) < 1e-11
+    assert _rel(comp, fp64) < 2e-11 and _rel(comp, direct) < 2e-11
 
 
 def test_tolerance_controls_the_error():
@@ -60,7 +77,7 @@ def test_mixed_solve_equals_direct_sum_solve(precond):
     v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED, precond=precond)
     s = g.last_stats[0]
     d = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
-    d.set_far_compression(0)
+    d.set_far_compression(0, 0)
     vd = d.solveMob(F, tol=1e-10, precision=PREC_MIXED, precond=precond)
     ref = d.solveMob(F, tol=1e-11, precision=PREC_FP64)
     assert s["status"] == 0 and s["relres"] < 1e-10
@@ -97,3 +114,5 @@ def test_invalid_tolerance_is_rejected():
         g.set_far_compression(0.1)
     with pytest.raises(SmobError):
         g.set_far_compression(float("nan"))
+    with pytest.raises(SmobError):
+        g.set_far_compression(1e-7, 1e-8)

@@ -255,13 +255,16 @@ def test_batched_equals_alone():
 def test_multi_rhs_equals_single_solves(k):
     """K right-hand sides solved together (shared-geometry FP32 far field) give bit for bit the
     solves of each column alone with the one-target-per-thread FP32 kernel, with and without coarse
-    equivalent sources; the Tpetra-style apply with K columns uses the same path."""
+    equivalent sources in the FP32 passes (the several-column float-float pass sums every grid-point
+    pair, so the single solves' float-float set is off here); the Tpetra-style apply with K columns
+    uses the same path."""
     rng = np.random.default_rng(19)
     radii = rng.uniform(0.8, 1.2, 12)
     cfg = dict(centers=configs.rsa(rng, 12, radii, 24.0, 0.1), radii=radii, orders=np.full(12, 10))
     mob = make(cfg, SphereSTKMobMat)
     mob.set_far_tile(1)
-    assert mob.far_compression_info()[2] > 0 and mob.n_near_pairs >= 0
+    mob.set_far_compression(1e-7, 0)
+    assert mob.far_compression_info()[2] > 0
     F = np.random.default_rng(k).standard_normal((k, 6 * mob.n_spheres))
     for prec in (PREC_MIXED, PREC_FP64):
         V = mob.solveMobMulti(F, tol=1e-10, precision=prec, want_density=True)
@@ -272,7 +275,7 @@ def test_multi_rhs_equals_single_solves(k):
             assert np.array_equal(V[j], v)
             assert np.array_equal(dens[j], mob.getDensitySolution())
             assert stats[j]["iterations"] == mob.last_stats[0]["iterations"]
-    mob.set_far_compression(0)
+    mob.set_far_compression(0, 0)
     V = mob.solveMobMulti(F, tol=1e-10, precision=PREC_MIXED)
     for j in range(k):
         assert np.array_equal(V[j], mob.solveMob(F[j], tol=1e-10, precision=PREC_MIXED))
