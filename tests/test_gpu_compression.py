@@ -24,7 +24,7 @@ def test_far_field_matches_direct_sum():
     c = _spread()
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
     eps, pts, ent = g.far_compression_info()
-    assert eps == 1e-7 and ent > 0 and pts > 0
+    assert eps == 1e-6 and ent > 0 and pts > 0
     x = np.random.default_rng(1).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
     comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
