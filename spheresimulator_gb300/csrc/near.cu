@@ -52,7 +52,7 @@ __global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real
     const int base = trac ? T.trac_map : T.sl_map;
     const int rows = trac ? T.trac_rows : T.sl_rows;
     Real* out = sets + stride * slot;
-    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    for (int r = blockIdx.y * blockDim.x + threadIdx.x; r < rows; r += gridDim.y * blockDim.x) {
         const int e0 = g.map_rowptr[base + r], e1 = g.map_rowptr[base + r + 1];
         Real acc = 0;
         for (int e = e0; e < e1; ++e) acc += mapval[e] * cin[g.map_col[e]];
@@ -253,12 +253,16 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
                      const int* slot_sphere, long long stride, cudaStream_t st) {
     if (nslots <= 0) return 0;
     const size_t sm = size_t(6 * ncoef(g.pmax)) * (fp32 ? sizeof(float) : sizeof(double));
+    // each slot's rows (2 x sets x ncoef(p+3), ~10^4) split over kSetSplit CTAs: few near-source spheres
+    // still give the GPU enough CTAs
+    constexpr int kSetSplit = 8;
+    const dim3 grid(nslots, kSetSplit);
     if (fp32)
-        k_near_sets<float><<<nslots, 256, sm, st>>>(g, static_cast<const float*>(coef), g.map_val_f, trac, slot_sphere,
-                                                    stride, static_cast<float*>(sets));
+        k_near_sets<float><<<grid, 256, sm, st>>>(g, static_cast<const float*>(coef), g.map_val_f, trac, slot_sphere,
+                                                  stride, static_cast<float*>(sets));
     else
-        k_near_sets<double><<<nslots, 256, sm, st>>>(g, static_cast<const double*>(coef), g.map_val_d, trac,
-                                                     slot_sphere, stride, static_cast<double*>(sets));
+        k_near_sets<double><<<grid, 256, sm, st>>>(g, static_cast<const double*>(coef), g.map_val_d, trac,
+                                                   slot_sphere, stride, static_cast<double*>(sets));
     return 1;
 }
 

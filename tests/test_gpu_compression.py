@@ -38,20 +38,22 @@ def test_far_field_matches_direct_sum():
 
 
 def test_float_float_far_field_with_coarse_sources():
-    """The float-float set (tolerance 1e-12) against the direct float-float sum and the FP64 sum."""
+    """The float-float set (tolerance 1e-10) against the direct float-float sum and the FP64 sum."""
     c = _spread(seed=9, n=24, p=12, box=26.0)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
     eps_hp, pts, ent = g.far_compression_info(hp=True)
-    assert eps_hp == 1e-12 and ent > 0 and pts > 0
+    assert eps_hp == 1e-10 and ent > 0 and pts > 0
     x = np.random.default_rng(9).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
     comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
     g.set_far_compression(1e-7, 0)
     assert g.far_compression_info(hp=True)[1:] == (0, 0)
     direct = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
-    # float-float sums carry ~1e-12 relative rounding on this size; the coarse sources add below 1e-11
+    # float-float sums carry ~1e-12 relative rounding on this size; the coarse sources add below 1e-10
     assert _rel(direct, fp64) < 1e-11
-    assert _rel(comp, fp64) < 2e-11 and _rel(comp, direct) < 2e-11
+    assert _rel(comp, fp64) < 1e-10 and _rel(comp, direct) < 1e-10
+    g.set_far_compression(1e-6, 1e-12)
+    assert _rel(g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT), direct) < 2e-11
 
 
 def test_tolerance_controls_the_error():
