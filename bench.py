@@ -39,8 +39,8 @@ L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = ("cfg2: 64 spheres a=1, seeded RSA in box 20 (min gap 0.1), p=16 (36992 points), "
             "N(0,1) force/torque, GMRES(50) to 1e-8 relative residual")
 # DRAM bytes (read + write) of one FP32 traction far-field launch on this workload, from an ncu capture
-# (GB300, k_far32<1, 1>: 1,897,472 read, 0 written)
-CFG2_FAR32_DRAM_BYTES = 1897472
+# (GB300, k_far32<1, 1> with coarse equivalent sources: 4,226,304 read, 0 written)
+CFG2_FAR32_DRAM_BYTES = 4226304
 
 
 def dist_init():
@@ -314,7 +314,8 @@ def run_native(args, world, rank, local, dist):
                      "traffic": CFG2_FAR32_DRAM_BYTES,
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_far32 launch on this "
                                        "workload (ncu --set full, bench.py --far-once); algorithmic bytes "
-                                       "(positions, normals, sources once) = 1.8 MB",
+                                       "(grid positions, normals, sources 1.8 MB and coarse points and "
+                                       "strengths 2.3 MB, each once) = 4.1 MB",
                      "peak_source": "FP32 FMA issue rate measured in this run (MEASURED_PEAKS.json has no SIMT entry)",
                      "flops_per_launch": 30.0 * evaluated, "pairs_per_launch": evaluated,
                      "pairs_note": "pairs the kernel evaluates per launch (fine grid sources, or coarse equivalent "
