@@ -188,7 +188,7 @@ struct smob_ctx {
         DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent;
     };
     CoarseHost c32, chp;
-    DBuf d_cnode, d_cnode_off;
+    DBuf d_cnode, d_cnode_off, d_sph32;
     smob_ctx() {
         c32.eps = kCoarseEpsDefault;
         chp.eps = kCoarseEpsHpDefault;
@@ -833,6 +833,14 @@ void build_coarse(smob_ctx* c) {
     build_coarse_set(c, c->chp, nodes, node_off, have_nodes);
     c->d_cnode.upload(nodes);
     c->d_cnode_off.upload(node_off);
+    // sphere centres relative to their problem's origin and radii, FP32, for the kernels' level votes
+    std::vector<float4> sph(c->N);
+    for (int i = 0; i < c->N; ++i) {
+        const double* o = &c->org[3 * c->prob[i]];
+        sph[i] = make_float4(float(c->centers[3 * i] - o[0]), float(c->centers[3 * i + 1] - o[1]),
+                             float(c->centers[3 * i + 2] - o[2]), float(c->radii[i]));
+    }
+    c->d_sph32.upload(sph);
 }
 
 // coarse points of both sets (after the grid; geometry-dependent)
@@ -901,6 +909,7 @@ void bind_geom(smob_ctx* c) {
     bind_set(c->chp, g.cshp);
     g.cnode = c->d_cnode.as<double>();
     g.cnode_off = c->d_cnode_off.as<int>();
+    g.sph32 = c->d_sph32.as<float4>();
 }
 
 // Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on

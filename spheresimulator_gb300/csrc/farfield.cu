@@ -120,11 +120,10 @@ __device__ __forceinline__ unsigned level_bit(const DevGeom& g, const CoarseSet&
     if (cs.ncent == 0) return kBitFine;
     const int4* L = cs.clev + s * kCoarseLevels;
     if (__ldg(&L[0].x) == 0) return kBitFine;
-    const float dx = float(__ldg(g.center + 3 * t) - __ldg(g.center + 3 * s));
-    const float dy = float(__ldg(g.center + 3 * t + 1) - __ldg(g.center + 3 * s + 1));
-    const float dz = float(__ldg(g.center + 3 * t + 2) - __ldg(g.center + 3 * s + 2));
-    const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - float(__ldg(g.radius + t));
-    const float as = float(__ldg(g.radius + s));
+    const float4 ct = __ldg(g.sph32 + t), cs4 = __ldg(g.sph32 + s);
+    const float dx = ct.x - cs4.x, dy = ct.y - cs4.y, dz = ct.z - cs4.z;
+    const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - ct.w;
+    const float as = cs4.w;
     if (!(rmin > as)) return kBitFine;
     const float need = cs.clog_eps / __logf(as / rmin) + cs.cmargin;
 #pragma unroll 1

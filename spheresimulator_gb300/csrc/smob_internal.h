@@ -125,6 +125,7 @@ struct DevGeom {
     // sphere s has up to kCoarseLevels coarse orders pe, ascending; a target sphere t may use the
     // coarsest with pe >= clog_eps / log(a_s / (|c_t - c_s| - a_t)) + cmargin.
     CoarseSet cs32, cshp;
+    const float4* sph32;       // per sphere: centre relative to the problem origin (FP32), radius
     const double* cnode;       // unit nodes of the coarse orders, [node][3]
     const int* cnode_off;      // [kMaxOrder + 1] first node of order pe in cnode
 };
