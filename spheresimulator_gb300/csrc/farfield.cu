@@ -1,7 +1,7 @@
 // farfield.cu — all-pairs Stokes single-layer / traction far field.
 //
 // Replaces the STKFMM far-field evaluations of BIE/SphereSTKSHOperator.cpp:273-303 (PVel)
-// and :354-446 (Traction, dotted with the target normal) by direct summation:
+// and :354-446 (Traction, dotted with the target normal) by summation over all pairs:
 //   SL:        u(x) = 1/(8 pi) sum_y [ f/r + (r.f) r / r^3 ]
 //   traction:  t(x) = -3/(4 pi) sum_y r (r.f)(r.n_x) / r^5,      r = x - y, f = w_y * density_y * c
 // Sources on the target's own sphere are skipped (the reference adds then subtracts them,
@@ -16,7 +16,9 @@
 // float-float (packed) and 1 in FP64. The several-right-hand-side kernels run one problem's work
 // items for up to 8 (FP32) or 4 (float-float) copies of it at once, evaluating each pair's geometry
 // once. A per-thread merge cursor over the sorted near-pair list decides per source sphere whether
-// the thread's target skips it; a CTA-wide vote skips the staging when every target does.
+// the thread's target skips it. The FP32 and float-float kernels also vote per source sphere for its
+// coarse equivalent sources when every target of the CTA is far enough (see the coarse section
+// below); the CTA stages the grid sources, one coarse level, or nothing when every target skips.
 // Partial sums go to [problem][chunk][point][3] and a second kernel reduces the chunks in
 // fixed order, so results do not depend on scheduling or on other problems in the batch.
 #include "smob_internal.h"
