@@ -1831,6 +1831,7 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
         create_streams(c.get(), prio);
         AllocStreamScope scope(c->st);
         configure_sphere_kernels();
+        configure_near_kernels();
         build_context(c.get(), geo);
         autotune_far32(c.get());
         CUDA_OK(cudaStreamSynchronize(c->st));

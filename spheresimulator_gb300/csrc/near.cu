@@ -81,7 +81,8 @@ struct Cplx<double> {
 // pair_filter: 0 every pair, 1 only pairs with gap >= 0.1 min radius, 2 only the
 // near-singular pairs (gap < 0.1 min radius).
 // PPT target points per thread share every coefficient load (one load, PPT complex multiply-adds).
-template <typename Real, int NS, int LANES, int PPT>
+// SMEM: the sets are staged in shared memory (plain loads) instead of read through the read-only cache.
+template <typename Real, int NS, int LANES, int PPT, bool SMEM>
 __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int idx, int lane, const Real* tr,
                                               const Real* ti, Real (*acc)[(NS + LANES - 1) / LANES]) {
     const typename Cplx<Real>::T* c = reinterpret_cast<const typename Cplx<Real>::T*>(set + 2 * NS * idx);
@@ -89,7 +90,7 @@ __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int 
     for (int s = 0; s < (NS + LANES - 1) / LANES; ++s) {
         const int k = lane + LANES * s;
         if (k < NS) {
-            const typename Cplx<Real>::T v = __ldg(c + k);
+            const typename Cplx<Real>::T v = SMEM ? c[k] : __ldg(c + k);
 #pragma unroll
             for (int p = 0; p < PPT; ++p) acc[p][s] = fma(v.x, tr[p], fma(-v.y, ti[p], acc[p][s]));
         }
@@ -102,7 +103,10 @@ __device__ __forceinline__ void contract_lane(const Real* __restrict__ set, int 
 template <typename Real, int LANES>
 __host__ __device__ constexpr int near_ppt() { return (LANES == 1 && sizeof(Real) == 4) ? 2 : 1; }
 
-template <typename Real, bool TRAC, int LANES>
+// STAGE: each source's coefficient sets (NS x ncoef(p+3) complex values) and the recurrence tables are
+// staged in dynamic shared memory, so the contraction reads shared memory instead of L1/L2; the
+// arithmetic and its order are those of the unstaged kernel.
+template <typename Real, bool TRAC, int LANES, bool STAGE>
 // registers: two-point FP32 at 3 CTAs per SM (168 without spills), one-lane FP64 at 4 CTAs per SM
 __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3 : (LANES == 1 ? 4 : 1))
     k_near_eval(DevGeom g, const Real* __restrict__ sets, long long stride, const Real* __restrict__ th, int th_c1,
@@ -138,13 +142,40 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
     const Real* c1 = th + th_c1;
     const Real* c2 = th + th_c2;
     const Real* dg = th + th_diag;
+    // staged layout: [sets: 2 NS ncoef(pmax+3)][c1: ncoef][c2: ncoef][diag: pmax+4]
+    extern __shared__ __align__(16) unsigned char near_smem[];
+    Real* sS = reinterpret_cast<Real*>(near_smem);
+    if (STAGE) {
+        const int ncd = ncoef(g.pmax + 3);
+        Real* t1 = sS + 2 * NS * ncd;
+        for (int k = threadIdx.x; k < ncd; k += blockDim.x) {
+            t1[k] = c1[k];
+            t1[ncd + k] = c2[k];
+        }
+        for (int k = threadIdx.x; k < g.pmax + 4; k += blockDim.x) t1[2 * ncd + k] = dg[k];
+        c1 = t1;
+        c2 = t1 + ncd;
+        dg = t1 + 2 * ncd;
+    }
     for (int e = e0; e < e1; ++e) {
-        if (pair_filter == 1 && g.nbr_precise[e]) continue;
+        if (pair_filter == 1 && g.nbr_precise[e]) continue;  // (uniform over the CTA)
         if (pair_filter == 2 && !g.nbr_precise[e]) continue;
         const int s = g.nbr_src[e];
         const int slot = g.near_src_slot[s];
         const Real* S = sets + stride * slot;
         const int Nd = g.order[s] + 3;
+        if (STAGE) {
+            // the previous source's sets are done; copy this source's, one complex value (8 or 16 bytes,
+            // the slot stride's alignment) per load
+            __syncthreads();
+            using CT = typename Cplx<Real>::T;
+            const int nv = NS * ncoef(Nd);
+            const CT* srcv = reinterpret_cast<const CT*>(S);
+            CT* dstv = reinterpret_cast<CT*>(sS);
+            for (int k = threadIdx.x; k < nv; k += blockDim.x) dstv[k] = __ldg(srcv + k);
+            __syncthreads();
+            S = sS;
+        }
         const double q[4] = {g.quat[4 * s], g.quat[4 * s + 1], g.quat[4 * s + 2], g.quat[4 * s + 3]};
         const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
         const double a = g.radius[s];
@@ -187,7 +218,7 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
             }
             for (int n = m; n <= Nd; ++n) {
                 const int idx = n * (n + 1) / 2 + m;
-                contract_lane<Real, NS, LANES, PPT>(S, idx, lane, cr, ci, accl);
+                contract_lane<Real, NS, LANES, PPT, STAGE>(S, idx, lane, cr, ci, accl);
                 if (n < Nd) {
                     const Real a1 = c1[idx], a2 = c2[idx];
 #pragma unroll
@@ -266,6 +297,26 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
     return 1;
 }
 
+// dynamic shared memory of the staged near kernel: sets of one source, c1, c2, diag
+template <typename Real>
+size_t near_stage_bytes(int pmax, bool trac) {
+    const size_t ncd = ncoef(pmax + 3);
+    return (2 * (trac ? kNearSetsTrac : kNearSetsSL) * ncd + 2 * ncd + pmax + 4) * sizeof(Real);
+}
+constexpr size_t kNearStageMax = 160 * 1024;  // larger set blocks (FP64 at high orders) read through L1/L2
+
+template <typename Real, bool TRAC, int LANES>
+void launch_near_typed(const DevGeom& g, dim3 grid, const Real* s, const Real* tab, long long stride, double c,
+                       int pair_filter, int tm, double* out, cudaStream_t st) {
+    const size_t sm = near_stage_bytes<Real>(g.pmax, TRAC);
+    if (sm <= kNearStageMax)
+        k_near_eval<Real, TRAC, LANES, true><<<grid, kNearThreads, sm, st>>>(g, s, stride, tab, g.th_c1, g.th_c2,
+                                                                            g.th_diag, c, pair_filter, tm, out);
+    else
+        k_near_eval<Real, TRAC, LANES, false><<<grid, kNearThreads, 0, st>>>(g, s, stride, tab, g.th_c1, g.th_c2,
+                                                                            g.th_diag, c, pair_filter, tm, out);
+}
+
 template <int LANES>
 void launch_near_eval_l(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c,
                         double* out, cudaStream_t st, int pair_filter) {
@@ -276,21 +327,28 @@ void launch_near_eval_l(const DevGeom& g, const void* sets, long long stride, bo
     const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
     if (fp32) {
         const float* s = static_cast<const float*>(sets);
-        if (trac)
-            k_near_eval<float, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
-                                                                           g.th_diag, c, pair_filter, tm, out);
-        else
-            k_near_eval<float, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_f, g.th_c1, g.th_c2,
-                                                                            g.th_diag, c, pair_filter, tm, out);
+        if (trac) launch_near_typed<float, true, LANES>(g, grid, s, g.tab_f, stride, c, pair_filter, tm, out, st);
+        else launch_near_typed<float, false, LANES>(g, grid, s, g.tab_f, stride, c, pair_filter, tm, out, st);
     } else {
         const double* s = static_cast<const double*>(sets);
-        if (trac)
-            k_near_eval<double, true, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
-                                                                            g.th_diag, c, pair_filter, tm, out);
-        else
-            k_near_eval<double, false, LANES><<<grid, kNearThreads, 0, st>>>(g, s, stride, g.tab_d, g.th_c1, g.th_c2,
-                                                                             g.th_diag, c, pair_filter, tm, out);
+        if (trac) launch_near_typed<double, true, LANES>(g, grid, s, g.tab_d, stride, c, pair_filter, tm, out, st);
+        else launch_near_typed<double, false, LANES>(g, grid, s, g.tab_d, stride, c, pair_filter, tm, out, st);
     }
+}
+
+template <typename Real, bool TRAC>
+void configure_near_typed() {
+    cudaFuncSetAttribute(k_near_eval<Real, TRAC, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+    cudaFuncSetAttribute(k_near_eval<Real, TRAC, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+    cudaFuncSetAttribute(k_near_eval<Real, TRAC, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+    cudaFuncSetAttribute(k_near_eval<Real, TRAC, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+}
+
+void configure_near_kernels() {
+    configure_near_typed<float, true>();
+    configure_near_typed<float, false>();
+    configure_near_typed<double, true>();
+    configure_near_typed<double, false>();
 }
 
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,

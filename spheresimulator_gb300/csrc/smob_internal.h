@@ -169,6 +169,7 @@ int launch_far_field_df_rep(const DevGeom& g, const FarItem* items, int nitems, 
 int launch_sphere_op(const DevGeom& g, const double* x, double* out, double c_id, double c_self, int self_kind,
                      double c_lop, void* coef, bool fp32, cudaStream_t st);
 void configure_sphere_kernels();
+void configure_near_kernels();  // shared-memory limits of the staged near-field kernels
 // Transforms only: coef (double) from grid (g2s), or grid from coef (s2g, overwrite)
 int launch_sh_g2s(const DevGeom& g, const double* grid, double* coef, cudaStream_t st);
 int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream_t st);
