@@ -209,7 +209,7 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * distance from the source centre to the nearest target point). Each source sphere gets the coarse
  * orders its far targets need for the tolerance (relative to the sphere's own contribution). eps sets
  * it for the FP32 operator passes (SMOB_PREC_MIXED inner solves and final velocity correction; default
- * 1e-6), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
+ * 1e-5), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
  * layer, SMOB_PREC_FLOAT_FLOAT; default 1e-10). Near pairs, the own sphere and every FP64 pass keep the
  * direct sum over the grid points: the plain FP64 solve is the reference's smooth quadrature. The
  * reference evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).

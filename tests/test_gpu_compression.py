@@ -24,17 +24,18 @@ def test_far_field_matches_direct_sum():
     c = _spread()
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
     eps, pts, ent = g.far_compression_info()
-    assert eps == 1e-6 and ent > 0 and pts > 0
+    assert eps == 1e-5 and ent > 0 and pts > 0
     x = np.random.default_rng(1).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
     comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
     g.set_far_compression(0)
     assert g.far_compression_info()[1:] == (0, 0) and g.far_compression_info(hp=True)[2] > 0
     direct = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
-    # the compression error sits at the FP32 rounding level of the direct sum
+    # the compression error stays a few times the FP32 rounding level, well below the 1e-5 the
+    # inner solves stop at
     assert _rel(direct, fp64) < 2e-5
     assert _rel(comp, fp64) < 2e-5
-    assert _rel(comp, direct) < 2e-6
+    assert _rel(comp, direct) < 1e-5
 
 
 def test_float_float_far_field_with_coarse_sources():
