@@ -626,15 +626,15 @@ void upload_near(smob_ctx* c) {
     const size_t nsl = c->slot_sphere.size();
     c->d_sets32.alloc(sizeof(float) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
     c->d_sets64.alloc(sizeof(double) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
-    // near-field lanes per target: ~152 x 512 threads when few target points have near pairs (the
+    // near-field lanes per target: ~152 x 256 threads when few target points have near pairs (the
     // kernel runs beside the far field, which fills the rest of the GPU; more lanes repeat the
-    // recurrence for little gain: 8 lanes were 4% slower per cfg2 solve than 4), one lane (no repeated
-    // recurrence) when many do; the lane count does not change any result (each set is summed by one
-    // lane in a fixed order)
+    // recurrence: with the sets in shared memory, cfg2 solves take 20.5 ms with 2 lanes, 21.0 with 4,
+    // 21.4 with 8 and 22.1 with 1), one lane (no repeated recurrence) when many do; the lane count does
+    // not change any result (each set is summed by one lane in a fixed order)
     long long tpts = 0;
     for (int t = 0; t < c->N; ++t)
         if (c->nbr_start[t + 1] > c->nbr_start[t]) tpts += c->glen[t];
-    const double want = 152.0 * 512.0 / double(std::max<long long>(tpts, 1));
+    const double want = 152.0 * 256.0 / double(std::max<long long>(tpts, 1));
     c->g.near_lanes = want >= 8 ? 8 : (want >= 4 ? 4 : (want >= 2 ? 2 : 1));
 }
 
