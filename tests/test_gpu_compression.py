@@ -119,3 +119,22 @@ def test_invalid_tolerance_is_rejected():
         g.set_far_compression(float("nan"))
     with pytest.raises(SmobError):
         g.set_far_compression(1e-7, 1e-8)
+
+
+def test_high_orders_use_fine_coarse_levels():
+    """Orders up to 32 spread apart: coarse orders up to 28 (several shared-memory tiles per coarse
+    sphere, the largest maps); the far field and a mixed solve match the direct sum and the FP64 solve."""
+    rng = np.random.default_rng(21)
+    centers = np.array([[0.0, 0, 0], [9.0, 0, 0], [0, 11.0, 0], [0, 0, 13.0], [8.0, 9.0, 7.0]])
+    radii = np.array([1.0, 1.1, 0.9, 1.0, 1.2])
+    orders = np.array([32, 24, 20, 16, 28])
+    g = SphereSTKMobMat(centers, radii, orders)
+    assert g.far_compression_info()[2] > 0 and g.far_compression_info(hp=True)[2] > 0
+    x = rng.standard_normal(3 * g.n_points)
+    fp64 = g.far_field(x, cSL=0.4, cTrac=1.0, precision=PREC_FP64)
+    assert _rel(g.far_field(x, cSL=0.4, cTrac=1.0, precision=PREC_MIXED), fp64) < 2e-5
+    assert _rel(g.far_field(x, cSL=0.4, cTrac=1.0, precision=PREC_FLOAT_FLOAT), fp64) < 1e-10
+    F = rng.standard_normal(30)
+    v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED)
+    assert g.last_stats[0]["status"] == 0
+    assert _rel(v, g.solveMob(F, tol=1e-12, precision=PREC_FP64)) < 1e-9
