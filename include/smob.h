@@ -126,7 +126,9 @@ smob_status smob_apply_lop(smob_ctx* ctx, const double* in, double* out, double 
 smob_status smob_project_null_space(smob_ctx* ctx, double* inout);
 
 /* ---- kernel-level pieces for parity tests (host pointers, add-into) ---- */
-/* far field over all sources except the target's own sphere and its near-pair source spheres */
+/* far field over all sources except the target's own sphere and its near-pair source spheres; FP64
+ * sums every pair, SMOB_PREC_MIXED (FP32) and SMOB_PREC_FLOAT_FLOAT read coarse equivalent sources for
+ * well-separated sphere pairs at the context's tolerances (smob_set_far_compression) */
 smob_status smob_far_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
 /* spectral evaluation of the near-pair source spheres at their targets (no direct subtraction) */
 smob_status smob_near_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
