@@ -147,7 +147,8 @@ size_t request_bytes(int n, const int* orders, int restart) {
     b += size_t(160) * M;                     // point data (FP64 + FP32 + float-float)
     b += size_t(12) * 2 * coef;               // coefficients (FP32 + FP64)
     b += size_t(12) * setsrc * size_t(n);     // near-field sets (upper bound: every sphere a source)
-    b += size_t(8) << 20;                     // tables and small arrays
+    b += size_t(96) * M;                      // coarse equivalent sources: points and strengths of both sets
+    b += size_t(56) << 20;                    // tables, coarse maps and small arrays
     return b;
 }
 
