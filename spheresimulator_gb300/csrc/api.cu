@@ -788,7 +788,8 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
             }
         }
     }
-    // GEMM tiles of the per-pass strengths: entries grouped by map (p, pe), 8 spheres x 64 nodes per CTA
+    // GEMM tiles of the per-pass strengths: entries grouped by map (p, pe), 8 spheres x kCoarseTileNodes
+    // coarse nodes per CTA
     h.cdesc.clear();
     h.cgrp.clear();
     h.gent.clear();
@@ -811,7 +812,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         const int first = (int)h.gent.size();
         h.gent.insert(h.gent.end(), mg.ents.begin(), mg.ents.end());
         for (int e = 0; e < (int)mg.ents.size(); e += 8)
-            for (int k0 = 0; k0 < mg.cnt; k0 += 64)
+            for (int k0 = 0; k0 < mg.cnt; k0 += kCoarseTileNodes)
                 h.cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
     }
     h.d_clev.upload(h.clev);

@@ -168,11 +168,12 @@ __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned v
 }
 
 // f_e = coarse map x weighted sources: per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per sphere]. A CTA
-// computes 64 coarse nodes of up to 8 spheres; its 4 groups of 128 threads take interleaved slices of
-// 16 fine nodes (map rows and the spheres' sources staged in shared memory), thread (sphere t / 16,
-// nodes t % 16 + 16 i) of a group keeps 4 x 3 accumulators, and the groups' sums are added in a fixed
-// order at the end.
-constexpr int kCgNodes = 64, kCgSph = 8, kCgK = 16, kCgGroups = 4;
+// computes kCoarseTileNodes coarse nodes of up to 8 spheres; its 4 groups of 128 threads take interleaved
+// slices of 16 fine nodes (map rows and the spheres' sources staged in shared memory), thread (sphere
+// t / 16, nodes t % 16 + 16 i) of a group keeps kCgNi x 3 accumulators, and the groups' sums are added
+// in a fixed order at the end.
+constexpr int kCgNodes = kCoarseTileNodes, kCgSph = 8, kCgK = 16, kCgGroups = 4;
+constexpr int kCgNi = kCgNodes / 16;  // coarse nodes per thread
 __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const float4* __restrict__ src) {
     const CoarseSet& cs = g.cs32;
     const int4 d = cs.cdesc[blockIdx.x];
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
     __shared__ float Ms[kCgGroups][kCgK][kCgNodes];
     __shared__ float4 Fs[kCgGroups][kCgK][kCgSph];
-    __shared__ float red[kCgGroups - 1][12][128];
+    __shared__ float red[kCgGroups - 1][3 * kCgNi][128];
     __shared__ int sbase[kCgSph], sout[kCgSph];
     __shared__ unsigned char sact[kCgSph];
     const int grp = threadIdx.x >> 7, t = threadIdx.x & 127;
@@ -199,9 +200,9 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
     }
     __syncthreads();
     const int si = t >> 4, ni = t & 15;
-    float acc[4][3];
+    float acc[kCgNi][3];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
+    for (int i = 0; i < kCgNi; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
     const float* __restrict__ map = cs.cmap + G.x;
     for (int jb = 0; jb < ng; jb += kCgK * kCgGroups) {
         const int j0 = jb + grp * kCgK;  // this group's slice
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
         for (int jj = 0; jj < kCgK; ++jj) {
             const float4 f = Fs[grp][jj][si];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < kCgNi; ++i) {
                 const float m = Ms[grp][jj][ni + 16 * i];
                 acc[i][0] = fmaf(m, f.x, acc[i][0]);
                 acc[i][1] = fmaf(m, f.y, acc[i][1]);
@@ -231,14 +232,14 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
     }
     if (grp > 0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < kCgNi; ++i)
 #pragma unroll
             for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = acc[i][c];
     }
     __syncthreads();
     if (grp == 0 && si < ne && sact[si]) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < kCgNi; ++i) {
 #pragma unroll
             for (int q = 0; q < kCgGroups - 1; ++q)
 #pragma unroll
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
     __shared__ double Ms[kCgGroupsD][kCgK][kCgNodes];
     __shared__ double4 Fs[kCgGroupsD][kCgK][kCgSph];
-    __shared__ double red[kCgGroupsD - 1][12][128];
+    __shared__ double red[kCgGroupsD - 1][3 * kCgNi][128];
     __shared__ int sbase[kCgSph], sout[kCgSph];
     __shared__ unsigned char sact[kCgSph];
     const int grp = threadIdx.x >> 7, t = threadIdx.x & 127;
@@ -278,9 +279,9 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
     }
     __syncthreads();
     const int si = t >> 4, ni = t & 15;
-    double acc[4][3];
+    double acc[kCgNi][3];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
+    for (int i = 0; i < kCgNi; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
     const double* __restrict__ map = cs.cmapd + G.x;
     for (int jb = 0; jb < ng; jb += kCgK * kCgGroupsD) {
         const int j0 = jb + grp * kCgK;
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
         for (int jj = 0; jj < kCgK; ++jj) {
             const double4 f = Fs[grp][jj][si];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
+            for (int i = 0; i < kCgNi; ++i) {
                 const double m = Ms[grp][jj][ni + 16 * i];
                 acc[i][0] = fma(m, f.x, acc[i][0]);
                 acc[i][1] = fma(m, f.y, acc[i][1]);
@@ -315,14 +316,14 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
     }
     if (grp > 0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < kCgNi; ++i)
 #pragma unroll
             for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = acc[i][c];
     }
     __syncthreads();
     if (grp == 0 && si < ne && sact[si]) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < kCgNi; ++i) {
 #pragma unroll
             for (int q = 0; q < kCgGroupsD - 1; ++q)
 #pragma unroll

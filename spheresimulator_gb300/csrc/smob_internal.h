@@ -33,6 +33,7 @@ constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements)
 constexpr int kNearSetsTrac = 25;        // div L, Hessians of L_x,L_y,L_z,L_r
 constexpr int kNearSetsSL = 15;          // L_j, grad L_j, grad L_r
 constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per sphere (FP32 far field)
+constexpr int kCoarseTileNodes = 32;     // coarse nodes per CTA of the coarse-strength GEMMs (multiple of 16)
 
 __host__ __device__ inline int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
 __host__ __device__ inline int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
@@ -77,7 +78,7 @@ struct CoarseSet {
     const double* cmapd;       // float-float set: the same maps in FP64
     float4* csrc;              // strengths of the current pass (float-float set: hi, lo interleaved)
     int crep;                  // coarse points of one replica (several-RHS contexts; else all of them)
-    // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of 64 coarse nodes x 8 spheres
+    // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of kCoarseTileNodes coarse nodes x 8 spheres
     int ncdesc;
     const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
     const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
