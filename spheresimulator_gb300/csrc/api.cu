@@ -568,8 +568,8 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_nrm32.alloc(sizeof(float4) * c->M);
     c->d_pos32lo.alloc(sizeof(float4) * c->M);
     c->d_nrm32lo.alloc(sizeof(float4) * c->M);
-    c->d_pos64.alloc(sizeof(double4) * c->M);
-    c->d_nrm64.alloc(sizeof(double4) * c->M);
+    c->d_pos64.alloc(sizeof(double4_32a) * c->M);
+    c->d_nrm64.alloc(sizeof(double4_32a) * c->M);
     c->d_org.upload(c->org);
     c->d_problems.upload(c->problems);
     c->d_items32.upload(c->items32);
@@ -581,7 +581,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
 
     // operator workspace
     c->d_src32.alloc(sizeof(float4) * c->M);
-    c->d_src64.alloc(sizeof(double4) * c->M);
+    c->d_src64.alloc(sizeof(double4_32a) * c->M);
     c->d_srcdf.alloc(sizeof(float4) * 2 * c->M);
     c->d_partial32.alloc(sizeof(float) * c->partial32);
     c->d_partial64.alloc(sizeof(double) * c->partial64);
@@ -876,8 +876,8 @@ void bind_geom(smob_ctx* c) {
     g.nrm32 = c->d_nrm32.as<float4>();
     g.pos32lo = c->d_pos32lo.as<float4>();
     g.nrm32lo = c->d_nrm32lo.as<float4>();
-    g.pos64 = c->d_pos64.as<double4>();
-    g.nrm64 = c->d_nrm64.as<double4>();
+    g.pos64 = c->d_pos64.as<double4_32a>();
+    g.nrm64 = c->d_nrm64.as<double4_32a>();
     g.nbr_start = c->d_nbr_start.as<int>();
     g.nbr_src = c->d_nbr_src.as<int>();
     g.nbr_precise = c->d_nbr_precise.as<unsigned char>();
@@ -1016,7 +1016,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
         } else {
             {
                 ProfScope ps(c, "far_pack", fs);
-                check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, fs));
+                check_launch(c, launch_far_pack(g, x, cc, c->d_src32.as<float4>(), c->d_src64.as<double4_32a>(), fp32, fs));
             }
             if (fp32 && g.cs32.ncent > 0) {
                 ProfScope ps(c, "far_coarse", fs);
@@ -1029,7 +1029,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                                                      fs));
             else
                 check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                 c->d_src64.as<double4>(), partial, fs, c->tpt));
+                                                 c->d_src64.as<double4_32a>(), partial, fs, c->tpt));
         }
         // sphere self and near field: main stream
         {
@@ -2050,14 +2050,14 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                                                         tr ? 1 : 0, c->d_srcdf.as<float4>(), static_cast<double*>(partial),
                                                         nullptr, c->st));
                 } else {
-                    check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4>(), fp32, c->st));
+                    check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4_32a>(), fp32, c->st));
                     if (fp32 && c->g.cs32.ncent > 0) {
                         ProfScope ps(c, "far_coarse");
                         check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
                     }
                     ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
                     check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                     c->d_src64.as<double4>(), partial, c->st, c->tpt));
+                                                     c->d_src64.as<double4_32a>(), partial, c->st, c->tpt));
                 }
                 check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st));
             }

@@ -75,7 +75,7 @@ __device__ __forceinline__ void pair_sl32(const float4& t, const float4& s, cons
     az = fmaf(f.z, ri, fmaf(k, rz, az));
 }
 
-__device__ __forceinline__ void pair_trac64(const double4& t, const double4& n, const double4& s, const double4& f,
+__device__ __forceinline__ void pair_trac64(const double4_32a& t, const double4_32a& n, const double4_32a& s, const double4_32a& f,
                                             double& ax, double& ay, double& az) {
     const double rx = t.x - s.x, ry = t.y - s.y, rz = t.z - s.z;
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
@@ -89,7 +89,7 @@ __device__ __forceinline__ void pair_trac64(const double4& t, const double4& n, 
     az = fma(k, rz, az);
 }
 
-__device__ __forceinline__ void pair_sl64(const double4& t, const double4& s, const double4& f, double& ax,
+__device__ __forceinline__ void pair_sl64(const double4_32a& t, const double4_32a& s, const double4_32a& f, double& ax,
                                           double& ay, double& az) {
     const double rx = t.x - s.x, ry = t.y - s.y, rz = t.z - s.z;
     const double r2 = fma(rx, rx, fma(ry, ry, rz * rz));
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
     const int4 G = cs.cgrp[d.x];
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
     __shared__ double Ms[kCgGroupsD][kCgK][kCgNodes];
-    __shared__ double4 Fs[kCgGroupsD][kCgK][kCgSph];
+    __shared__ double4_32a Fs[kCgGroupsD][kCgK][kCgSph];
     __shared__ double red[kCgGroupsD - 1][3 * kCgNi][128];
     __shared__ int sbase[kCgSph], sout[kCgSph];
     __shared__ unsigned char sact[kCgSph];
@@ -293,17 +293,17 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
         }
         if (t < kCgK * kCgSph) {
             const int jj = t / kCgSph, ss = t % kCgSph;
-            double4 f = make_double4(0, 0, 0, 0);
+            double4_32a f = make_double4_32a(0, 0, 0, 0);
             if (j0 + jj < ng && ss < ne) {
                 const float4 h = src2[2LL * (sbase[ss] + j0 + jj)], l = src2[2LL * (sbase[ss] + j0 + jj) + 1];
-                f = make_double4(double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z), 0.0);
+                f = make_double4_32a(double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z), 0.0);
             }
             Fs[grp][jj][ss] = f;
         }
         __syncthreads();
 #pragma unroll 4
         for (int jj = 0; jj < kCgK; ++jj) {
-            const double4 f = Fs[grp][jj][si];
+            const double4_32a f = Fs[grp][jj][si];
 #pragma unroll
             for (int i = 0; i < kCgNi; ++i) {
                 const double m = Ms[grp][jj][ni + 16 * i];
@@ -664,16 +664,16 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
 
 template <bool TRAC>
 __global__ void __launch_bounds__(kFarThreads) k_far64(DevGeom g, const FarItem* __restrict__ items,
-                                                      const double4* __restrict__ src, double* __restrict__ partial) {
+                                                      const double4_32a* __restrict__ src, double* __restrict__ partial) {
     const FarItem it = items[blockIdx.x];
     if (g.active && !g.active[it.problem]) return;
-    __shared__ double4 sp[kFarTile];
-    __shared__ double4 sf[kFarTile];
+    __shared__ double4_32a sp[kFarTile];
+    __shared__ double4_32a sf[kFarTile];
     const int ta = it.t0 + threadIdx.x;
     const bool va = ta < it.t1;
-    const double4 z4 = make_double4(0, 0, 0, 0);
-    const double4 pa = va ? g.pos64[ta] : z4;
-    const double4 na = (TRAC && va) ? g.nrm64[ta] : z4;
+    const double4_32a z4 = make_double4_32a(0, 0, 0, 0);
+    const double4_32a pa = va ? g.pos64[ta] : z4;
+    const double4_32a na = (TRAC && va) ? g.nrm64[ta] : z4;
     const int sa = va ? g.sid[ta] : -1;
     int ca = va ? g.nbr_start[sa] : 0, ea = va ? g.nbr_start[sa + 1] : 0;
     double xa = 0, ya = 0, za = 0;
@@ -1055,14 +1055,14 @@ __global__ void k_far_pack_df(DevGeom g, const double* __restrict__ x, double c,
 }
 
 __global__ void k_far_pack(DevGeom g, const double* __restrict__ x, double c, float4* __restrict__ s32,
-                           double4* __restrict__ s64) {
+                           double4_32a* __restrict__ s64) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.M) return;
     if (g.active && !g.active[g.prob[g.sid[i]]]) return;
     const double w = g.weights[i] * c;
     const double fx = x[3 * i] * w, fy = x[3 * i + 1] * w, fz = x[3 * i + 2] * w;
     if (s32) s32[i] = make_float4(float(fx), float(fy), float(fz), 0.f);
-    if (s64) s64[i] = make_double4(fx, fy, fz, 0.0);
+    if (s64) s64[i] = make_double4_32a(fx, fy, fz, 0.0);
 }
 
 template <typename Real>
@@ -1088,7 +1088,7 @@ __global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double
 
 }  // namespace
 
-int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4* src64, bool fp32,
+int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4_32a* src64, bool fp32,
                     cudaStream_t st) {
     k_far_pack<<<(g.M + 255) / 256, 256, 0, st>>>(g, x, c, fp32 ? src32 : nullptr, fp32 ? nullptr : src64);
     return 1;
@@ -1108,7 +1108,7 @@ void launch_far32(const DevGeom& g, const FarItem* items, int nitems, bool trac,
 }
 
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
-                     const double4* src64, void* partial, cudaStream_t st, int tpt) {
+                     const double4_32a* src64, void* partial, cudaStream_t st, int tpt) {
     if (nitems <= 0) return 0;
     if (fp32) {
         float* pf = static_cast<float*>(partial);

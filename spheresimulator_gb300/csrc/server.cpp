@@ -117,7 +117,7 @@ struct smob_server {
         const int rank = pairs < 1e9 ? 0 : (pairs < 3e10 ? 1 : 2);
         smob_status s = smob::create_context(&ctx, &g, opts.device, rank);
         if (s == SMOB_OK) {
-            smob_solve_opts o{r->tol, opts.restart, opts.max_iters, opts.precision, 0, opts.inner_tol};
+            smob_solve_opts o{r->tol, opts.restart, opts.max_iters, opts.precision, SMOB_WARM_NONE, opts.inner_tol, 0};
             r->vel.assign(6 * r->n, 0.0);
             s = smob_solve_mob(ctx, r->force.data(), r->vel.data(), nullptr, &o, &r->stats);
         }

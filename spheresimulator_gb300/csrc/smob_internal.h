@@ -5,7 +5,7 @@
 //              coff (coefficient offset, complex units), prob[N]
 //   points   : coords/norms[3M] (FP64 lab frame), weights[M], sid[M];
 //              pos32/nrm32 float4 (x,y,z relative to the problem's origin, w = sphere id bits);
-//              pos64/nrm64 double4 (same, FP64)
+//              pos64/nrm64 double4_32a (same, FP64)
 //   near     : CSR by target sphere (nbr_start[N+1], nbr_src[pairs], sorted by source)
 //   far field: work items (target block x source-sphere chunk) and a partial-sum buffer
 //              laid out per problem as [chunk][point][3] (deterministic fixed-order reduction)
@@ -106,8 +106,8 @@ struct DevGeom {
     const float4* nrm32;
     const float4* pos32lo;  // float-float low parts: coordinate - float(coordinate), normal likewise
     const float4* nrm32lo;
-    const double4* pos64;
-    const double4* nrm64;
+    const double4_32a* pos64;
+    const double4_32a* nrm64;
     const int* nbr_start;
     const int* nbr_src;
     const unsigned char* nbr_precise;  // per pair: surface gap < 0.1 * min radius (evaluated in FP64 in mixed mode)
@@ -134,7 +134,7 @@ struct DevGeom {
 // ---------------------------------------------------------------- kernels (launch wrappers)
 // Every wrapper launches on `st` and returns the number of kernels it launched.
 // Far field: out[3M] += sum over far sources of c_sl*S + c_trac*K(dot n_target).
-int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4* src64, bool fp32,
+int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, double4_32a* src64, bool fp32,
                     cudaStream_t st);
 // coarse equivalent-source strengths of this pass from the FP32 grid sources (before every FP32
 // launch_far_field when g.ncent > 0)
@@ -143,7 +143,7 @@ int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st);
 int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
-                     const double4* src64, void* partial, cudaStream_t st, int tpt = 2);
+                     const double4_32a* src64, void* partial, cudaStream_t st, int tpt = 2);
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
 // coarse points of every (sphere, level) entry of a set, relative to the problem origins (after
 // launch_regrid); cpos32lo (may be null) receives the low parts

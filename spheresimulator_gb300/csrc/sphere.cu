@@ -378,8 +378,8 @@ __device__ __forceinline__ void qrot_rn(const double* q, const double* v, double
 
 __global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __restrict__ coords,
                          double* __restrict__ norms, float4* __restrict__ pos32, float4* __restrict__ nrm32,
-                         float4* __restrict__ pos32lo, float4* __restrict__ nrm32lo, double4* __restrict__ pos64,
-                         double4* __restrict__ nrm64) {
+                         float4* __restrict__ pos32lo, float4* __restrict__ nrm32lo, double4_32a* __restrict__ pos64,
+                         double4_32a* __restrict__ nrm64) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.M) return;
     const int s = g.sid[i];
@@ -407,8 +407,8 @@ __global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __re
                              float(__dsub_rn(r[2], double(p.z))), 0.f);
     nrm32lo[i] = make_float4(float(__dsub_rn(n[0], double(q.x))), float(__dsub_rn(n[1], double(q.y))),
                              float(__dsub_rn(n[2], double(q.z))), 0.f);
-    pos64[i] = make_double4(r[0], r[1], r[2], 0.0);
-    nrm64[i] = make_double4(n[0], n[1], n[2], 0.0);
+    pos64[i] = make_double4_32a(r[0], r[1], r[2], 0.0);
+    nrm64[i] = make_double4_32a(n[0], n[1], n[2], 0.0);
 }
 
 // coarse points of one (sphere, level) entry per CTA: the order-pe unit nodes placed like the sphere's
@@ -490,7 +490,7 @@ int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st) {
     k_regrid<<<(g.M + 255) / 256, 256, 0, st>>>(g, org, const_cast<double*>(g.coords), const_cast<double*>(g.norms),
                                                 const_cast<float4*>(g.pos32), const_cast<float4*>(g.nrm32),
                                                 const_cast<float4*>(g.pos32lo), const_cast<float4*>(g.nrm32lo),
-                                                const_cast<double4*>(g.pos64), const_cast<double4*>(g.nrm64));
+                                                const_cast<double4_32a*>(g.pos64), const_cast<double4_32a*>(g.nrm64));
     return 1;
 }
 
