@@ -215,7 +215,8 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * layer, SMOB_PREC_FLOAT_FLOAT; default 1e-10). Near pairs, the own sphere and every FP64 pass keep the
  * direct sum over the grid points: the plain FP64 solve is the reference's smooth quadrature. The
  * reference evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).
- * A tolerance <= 0 turns that set off (the direct sum). */
+ * A tolerance <= 0 turns that set off (the direct sum). Setting the tolerances empties the recycled
+ * solutions (smob_recycle_info) and drops the several-column copies of the context. */
 smob_status smob_set_far_compression(smob_ctx* ctx, double eps, double eps_hp);
 /* the tolerance, coarse points held and (sphere, level) entries of the FP32 set (hp = 0) or the
  * float-float set (hp = 1) */

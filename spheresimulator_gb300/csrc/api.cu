@@ -2411,6 +2411,7 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
         c->multi.clear();
         c->c32.eps = eps > 0 ? eps : 0.0;
         c->chp.eps = eps_hp > 0 ? eps_hp : 0.0;
+        c->rk = 0;  // recycled residuals belong to the old operators
         build_coarse(c);
         bind_geom(c);
         coarse_grids(c);
