@@ -209,7 +209,8 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * sphere: its grid sources projected onto the spherical harmonics of degree <= pe and re-weighted with
  * the order-pe quadrature, which reproduces the far field to ~(a_s / r_min)^(pe+1) relative (r_min:
  * distance from the source centre to the nearest target point). Each source sphere gets the coarse
- * orders its far targets need for the tolerance (relative to the sphere's own contribution). eps sets
+ * orders its far targets need for the tolerance (relative to the sphere's own contribution; the
+ * measured error stays within a small factor of it, below 3.4 eps over orders 8-24). eps sets
  * it for the FP32 operator passes (SMOB_PREC_MIXED inner solves and final velocity correction; default
  * 1e-5), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
  * layer, SMOB_PREC_FLOAT_FLOAT; default 1e-10). Near pairs, the own sphere and every FP64 pass keep the
