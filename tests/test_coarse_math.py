@@ -68,7 +68,7 @@ def test_far_field_error_follows_the_level_rule():
             val = far(trg, tg, nc, coarse_map(p, pe) @ f, trac)
             err = np.abs(val - ref).max() / np.abs(ref).max()
             assert err < 4 * eps, (trac, R, pe, err)
-            # one order coarser is visibly worse than the finest level, so the rule is not slack by orders
+            # three orders coarser is worse, so the rule does not overshoot by orders
             if pe > 3:
                 nc2, _ = grid(pe - 3)
                 worse = np.abs(far(trg, tg, nc2, coarse_map(p, pe - 3) @ f, trac) - ref).max() / np.abs(ref).max()
