@@ -574,7 +574,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_problems.upload(c->problems);
     c->d_items32.upload(c->items32);
     c->d_items64.upload(c->items64);
-    c->d_items_df.upload(c->items_tpt[1]);  // float-float far field: 256 targets per CTA, 2 per thread
+    c->d_items_df.upload(c->items_tpt[0]);  // float-float far field: 128 targets per CTA, 2 per thread
     c->d_chunks.upload(c->chunks);
     std::vector<unsigned char> act(c->P, 1);
     c->d_active.upload(act);
@@ -1011,7 +1011,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_coarse_src_df(g, c->d_srcdf.as<float4>(), fs));
             }
             ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df", fs);
-            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), tr ? 1 : 0,
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), tr ? 1 : 0,
                                                 c->d_srcdf.as<float4>(), static_cast<double*>(partial), nullptr, fs));
         } else {
             {
@@ -1094,7 +1094,7 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
                                                     c->rep_M, c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                     c->d_partial64_sl.as<double>(), fs));
         else
-            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), 2,
                                                 c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                 c->d_partial64_sl.as<double>(), fs));
     }
@@ -2030,7 +2030,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                 {
                     ProfScope ps(c, "far_both_df");
-                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(), 2,
+                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), 2,
                                                         c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                         c->d_partial64_sl.as<double>(), c->st));
                 }
@@ -2046,7 +2046,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                     check_launch(c, launch_far_pack_df(c->g, din, cc, c->d_srcdf.as<float4>(), c->st));
                     check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                     ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
-                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[1].size(),
+                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(),
                                                         tr ? 1 : 0, c->d_srcdf.as<float4>(), static_cast<double*>(partial),
                                                         nullptr, c->st));
                 } else {

@@ -137,14 +137,15 @@ __device__ __forceinline__ unsigned level_bit(const DevGeom& g, const CoarseSet&
     return kBitFine;
 }
 
-// CTA-wide OR of one vote per thread (per-warp slots, double-buffered by parity: one barrier)
-__device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[kFarThreads / 32], int parity) {
+// CTA-wide OR of one vote per thread (per-warp slots, double-buffered by parity: one barrier); NT threads
+template <int NT = kFarThreads>
+__device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[NT / 32], int parity) {
     v = __reduce_or_sync(0xffffffffu, v);
     if ((threadIdx.x & 31) == 0) slots[parity][threadIdx.x >> 5] = v;
     __syncthreads();
     unsigned r = 0;
 #pragma unroll
-    for (int w = 0; w < kFarThreads / 32; ++w) r |= slots[parity][w];
+    for (int w = 0; w < NT / 32; ++w) r |= slots[parity][w];
     return r;
 }
 
@@ -801,10 +802,11 @@ __device__ __forceinline__ void df_acc(T& ah, T& al, dfv<T> v) {
 // KIND: 0 single layer -> partial; 1 traction -> partial; 2 both from the same sources in one pass
 // (traction -> partial, single layer -> partial_sl), sharing r, 1/r and r.f between the two kernels.
 template <int KIND>
-__global__ void __launch_bounds__(kFarThreads, 3)
+__global__ void __launch_bounds__(kFarThreadsDF, 6)
     k_far_dfx2(DevGeom g, const FarItem* __restrict__ items, const float4* __restrict__ src,
                double* __restrict__ partial, double* __restrict__ partial_sl) {
     constexpr bool TRAC = KIND != 0, SL = KIND != 1;
+    constexpr int NT = kFarThreadsDF;
     const FarItem it = items[blockIdx.x];
     if (g.active && !g.active[it.problem]) return;
     __shared__ float4 sph[kFarTile], spl[kFarTile], sfh[kFarTile], sfl[kFarTile];
@@ -814,7 +816,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
     bool val[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const int t = it.t0 + threadIdx.x + h * kFarThreads;
+        const int t = it.t0 + threadIdx.x + h * NT;
         val[h] = t < it.t1;
         PH[h] = val[h] ? g.pos32[t] : z4;
         PL[h] = val[h] ? g.pos32lo[t] : z4;
@@ -830,7 +832,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
         n2{f2(NH[0].z, NH[1].z), f2(NL[0].z, NL[1].z)};
     float2 xh = f2(0.f, 0.f), xl = xh, yh = xh, yl = xh, zh = xh, zl = xh;     // traction, or SL for KIND 0
     float2 sxh = xh, sxl = xh, syh = xh, syl = xh, szh = xh, szl = xh;          // single layer for KIND 2
-    __shared__ unsigned votes_buf[2][kFarThreads / 32];
+    __shared__ unsigned votes_buf[2][NT / 32];
     // one source against the two packed targets (mx, my, mz); keep scales the source weight per lane
     auto pair = [&](const df2& mx, const df2& my, const df2& mz, const float4& qh, const float4& ql,
                     const float4& fh, const float4& fl, bool masked, float2 keep) {
@@ -883,7 +885,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
 #pragma unroll
         for (int h = 0; h < 2; ++h)
             if (val[h]) vote |= sk[h] ? kBitSkip : level_bit(g, g.cshp, sid[h], s);
-        const unsigned votes = cta_or(vote, votes_buf, parity);
+        const unsigned votes = cta_or<NT>(vote, votes_buf, parity);
         if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
         // coarse level of the float-float set, or the grid sources
         const bool coarse = !(votes & (kBitSkip | kBitFine));
@@ -908,7 +910,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
         for (int base = 0; base < gl; base += kFarTile) {
             const int n = min(kFarTile, gl - base);
             __syncthreads();
-            for (int k = threadIdx.x; k < n; k += kFarThreads) {
+            for (int k = threadIdx.x; k < n; k += NT) {
                 sph[k] = QH[g0 + base + k];
                 spl[k] = QL[g0 + base + k];
                 sfh[k] = QF[2 * (g0 + base + k)];
@@ -927,7 +929,7 @@ __global__ void __launch_bounds__(kFarThreads, 3)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         if (!val[h]) continue;
-        const long long off = pr.poff + 3LL * mp * it.chunk + 3LL * (it.t0 + threadIdx.x + h * kFarThreads - pr.p0);
+        const long long off = pr.poff + 3LL * mp * it.chunk + 3LL * (it.t0 + threadIdx.x + h * NT - pr.p0);
         double* o = partial + off;
         o[0] = h ? double(xh.y) + double(xl.y) : double(xh.x) + double(xl.x);
         o[1] = h ? double(yh.y) + double(yl.y) : double(yh.x) + double(yl.x);
@@ -1171,10 +1173,10 @@ int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2
 int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int kind, const float4* src2,
                         double* partial, double* partial_sl, cudaStream_t st) {
     if (nitems <= 0) return 0;
-    // items carry 2 * kFarThreads targets each (two packed targets per thread)
-    if (kind == 2) k_far_dfx2<2><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, partial_sl);
-    else if (kind == 1) k_far_dfx2<1><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, nullptr);
-    else k_far_dfx2<0><<<nitems, kFarThreads, 0, st>>>(g, items, src2, partial, nullptr);
+    // items carry 2 * kFarThreadsDF targets each (two packed targets per thread)
+    if (kind == 2) k_far_dfx2<2><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, partial_sl);
+    else if (kind == 1) k_far_dfx2<1><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
+    else k_far_dfx2<0><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
     return 1;
 }
 

@@ -20,7 +20,8 @@ struct smob_ctx;
 namespace smob {
 
 constexpr int kMaxOrder = 32;
-constexpr int kFarThreads = 128;         // far-field CTA size (FP32: 2 targets per thread)
+constexpr int kFarThreads = 128;         // far-field CTA size (FP32: 1, 2 or 4 targets per thread)
+constexpr int kFarThreadsDF = 64;        // float-float far-field CTA (2 packed targets per thread: 128 targets)
 constexpr int kFarTargets32 = 256;       // targets per FP32 far-field work item
 constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
 constexpr int kFarTile = 256;            // sources staged per shared-memory tile (FP64 / float-float)
@@ -154,7 +155,7 @@ int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org,
 int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,
                          const float4* src32, float* partial, cudaStream_t st);
 // float-float far field (hi/lo float pairs on the FP32 pipe); partial sums in FP64 (the FP64 buffer).
-// Items cover 2 * kFarThreads targets. kind: 0 single layer, 1 traction (both into partial),
+// Items cover 2 * kFarThreadsDF targets. kind: 0 single layer, 1 traction (both into partial),
 // 2 traction into partial and single layer into partial_sl from the same sources in one pass.
 int launch_far_pack_df(const DevGeom& g, const double* x, double c, float4* src2, cudaStream_t st);
 int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int kind, const float4* src2,
