@@ -158,6 +158,7 @@ struct smob_ctx {
     long long set_stride_trac = 0, set_stride_sl = 0;
     std::vector<FarItem> items32, items64;
     std::vector<FarItem> items_tpt[3];  // FP32 item lists for 1, 2, 4 targets per thread
+    std::vector<FarItem> items_df;      // float-float items: 2 * kFarThreadsDF targets
     int tpt = 2;                         // FP32 targets per thread chosen by the autotuner
     double tune_ms[3] = {0, 0, 0};
     bool tune_cached = false;
@@ -524,6 +525,10 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     // both item lists share the chunking rule, so Problem.nchunks/poff are the same for both
     make_items(kFarTargets64, c->items64, c->partial64);
     for (int k = 0; k < 3; ++k) make_items(kFarThreads << k, c->items_tpt[k], c->partial32);
+    {
+        long long unused = 0;
+        make_items(2 * kFarThreadsDF, c->items_df, unused);
+    }
     c->items32 = c->items_tpt[1];
     // heavier problems first helps the tail of uneven batches
     auto by_cost = [&](std::vector<FarItem>& items) {
@@ -535,6 +540,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     };
     by_cost(c->items32);
     by_cost(c->items64);
+    by_cost(c->items_df);
     for (auto& v : c->items_tpt) by_cost(v);
 
     // reduction chunks for the Krylov vectors
@@ -574,7 +580,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_problems.upload(c->problems);
     c->d_items32.upload(c->items32);
     c->d_items64.upload(c->items64);
-    c->d_items_df.upload(c->items_tpt[0]);  // float-float far field: 128 targets per CTA, 2 per thread
+    c->d_items_df.upload(c->items_df);  // float-float far field: 2 targets per thread
     c->d_chunks.upload(c->chunks);
     std::vector<unsigned char> act(c->P, 1);
     c->d_active.upload(act);
@@ -1011,7 +1017,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 check_launch(c, launch_coarse_src_df(g, c->d_srcdf.as<float4>(), fs));
             }
             ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df", fs);
-            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), tr ? 1 : 0,
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(), tr ? 1 : 0,
                                                 c->d_srcdf.as<float4>(), static_cast<double*>(partial), nullptr, fs));
         } else {
             {
@@ -1094,7 +1100,7 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
                                                     c->rep_M, c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                     c->d_partial64_sl.as<double>(), fs));
         else
-            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), 2,
+            check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(), 2,
                                                 c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                 c->d_partial64_sl.as<double>(), fs));
     }
@@ -2030,7 +2036,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                 {
                     ProfScope ps(c, "far_both_df");
-                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(), 2,
+                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(), 2,
                                                         c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                         c->d_partial64_sl.as<double>(), c->st));
                 }
@@ -2046,7 +2052,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                     check_launch(c, launch_far_pack_df(c->g, din, cc, c->d_srcdf.as<float4>(), c->st));
                     check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
                     ProfScope ps(c, tr ? "far_trac_df" : "far_sl_df");
-                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_tpt[0].size(),
+                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(),
                                                         tr ? 1 : 0, c->d_srcdf.as<float4>(), static_cast<double*>(partial),
                                                         nullptr, c->st));
                 } else {

@@ -802,7 +802,7 @@ __device__ __forceinline__ void df_acc(T& ah, T& al, dfv<T> v) {
 // KIND: 0 single layer -> partial; 1 traction -> partial; 2 both from the same sources in one pass
 // (traction -> partial, single layer -> partial_sl), sharing r, 1/r and r.f between the two kernels.
 template <int KIND>
-__global__ void __launch_bounds__(kFarThreadsDF, 6)
+__global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     k_far_dfx2(DevGeom g, const FarItem* __restrict__ items, const float4* __restrict__ src,
                double* __restrict__ partial, double* __restrict__ partial_sl) {
     constexpr bool TRAC = KIND != 0, SL = KIND != 1;

@@ -21,7 +21,7 @@ namespace smob {
 
 constexpr int kMaxOrder = 32;
 constexpr int kFarThreads = 128;         // far-field CTA size (FP32: 1, 2 or 4 targets per thread)
-constexpr int kFarThreadsDF = 64;        // float-float far-field CTA (2 packed targets per thread: 128 targets)
+constexpr int kFarThreadsDF = 32;        // float-float far-field CTA (2 packed targets per thread: 64 targets)
 constexpr int kFarTargets32 = 256;       // targets per FP32 far-field work item
 constexpr int kFarTargets64 = 128;       // targets per FP64 far-field work item
 constexpr int kFarTile = 256;            // sources staged per shared-memory tile (FP64 / float-float)
