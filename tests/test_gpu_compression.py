@@ -138,3 +138,18 @@ def test_high_orders_use_fine_coarse_levels():
     v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED)
     assert g.last_stats[0]["status"] == 0
     assert _rel(v, g.solveMob(F, tol=1e-12, precision=PREC_FP64)) < 1e-9
+
+
+def test_far_pairs_replay():
+    """The host replay of the kernels' per-CTA choices: the direct count is every far pair, the
+    evaluated count drops with coarse sources and equals the direct count without them."""
+    c = _spread(seed=12, n=16, p=10, box=18.0)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    ng = (c["orders"] + 1) * (2 * c["orders"] + 2)
+    t, s = g.near_pairs()
+    direct = int(ng.sum() ** 2 - (ng ** 2).sum() - (ng[t] * ng[s]).sum())
+    d, e, macs = g.far_pairs()
+    assert d == direct and 0 < e < d and macs > 0
+    g.set_far_compression(0, 0)
+    d0, e0, m0 = g.far_pairs()
+    assert d0 == direct and e0 == direct and m0 == 0
