@@ -189,6 +189,11 @@ class _Context:
             eps_hp = self.far_compression_info(hp=True)[0]
         N.check(self._L.smob_set_far_compression(self._h, float(eps), float(eps_hp)))
 
+    def set_far_coarse_targets(self, on):
+        """Coarse targets of the FP32 set (default on): the far field of a well-separated source sphere
+        evaluated at a coarse grid of the target sphere and interpolated to its grid."""
+        N.check(self._L.smob_set_far_coarse_targets(self._h, int(bool(on))))
+
     def far_compression_info(self, hp=False):
         """(eps, coarse points held, (sphere, level) entries) of the FP32 set, or of the float-float set"""
         e, pts, ent = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
@@ -197,7 +202,8 @@ class _Context:
         return e.value, pts.value, ent.value
 
     def far_pairs(self):
-        """(direct-sum pairs, evaluated pairs, coarse-strength multiply-adds) of one FP32 far-field pass"""
+        """(direct-sum pairs, evaluated pairs, coarse multiply-adds: strengths and target interpolation) of one
+        FP32 far-field pass"""
         d, e, m = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
         N.check(self._L.smob_far_pairs(self._h, ctypes.byref(d), ctypes.byref(e), ctypes.byref(m)))
         return d.value, e.value, m.value

@@ -133,6 +133,7 @@ def lib():
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
         "smob_recycle_info": (S, [_VP, _IP, _IP]),
         "smob_set_far_compression": (S, [_VP, ctypes.c_double, ctypes.c_double]),
+        "smob_set_far_coarse_targets": (S, [_VP, ctypes.c_int]),
         "smob_far_compression_info": (S, [_VP, ctypes.c_int, _DP, _IP, _IP]),
         "smob_far_pairs": (S, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                ctypes.POINTER(ctypes.c_longlong)]),

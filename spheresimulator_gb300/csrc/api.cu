@@ -117,6 +117,9 @@ constexpr double kCoarseEpsDefault = 1e-5;
 // residual moves by 3e-14
 constexpr double kCoarseEpsHpDefault = 1e-10;
 constexpr double kCoarseMargin = 1.0;  // orders added to log(eps) / log(a_s / r_min) (measured, p = 16)
+// coarse targets: one order more (the traction's target normal raises the field's degree by one;
+// with it the interpolated traction stays within the sources' error, measured in numpy over p = 12-24)
+constexpr double kCoarseTargetMargin = 2.0;
 constexpr int kCoarseLadder[] = {3, 4, 5, 6, 8, 10, 12, 14, 16, 20, 24, 28};
 // recycled solutions (warm_start 2): pairs (force_i, mu_i) of earlier solves kept per context, with
 // the forces orthonormalised per problem; a force closer than this (relative) to their span adds nothing
@@ -189,11 +192,23 @@ struct smob_ctx {
         std::vector<int4> cdesc, cgrp;
         std::vector<int2> gent;
         DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent;
+        // coarse targets: listed entries with their candidate sources, work items, partial sums and
+        // the interpolation side
+        bool ctgt = false;
+        std::vector<CtEnt> ctent;
+        std::vector<int> ctsrc, ctused;
+        std::vector<CtWork> ct_work;
+        std::vector<CtITile> ctitile;
+        std::vector<int> ctient;
+        long long ct_partial = 0;
+        DBuf d_ctent, d_ctsrc, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32, d_ctu, d_ctitile,
+            d_ctient;
     };
     CoarseHost c32, chp;
     DBuf d_cnode, d_cnode_off, d_sph32;
     smob_ctx() {
         c32.eps = kCoarseEpsDefault;
+        c32.ctgt = true;
         chp.eps = kCoarseEpsHpDefault;
         chp.hp = true;
     }
@@ -402,6 +417,25 @@ void bind_geom(smob_ctx* c);
 void build_coarse(smob_ctx* c);
 void coarse_grids(smob_ctx* c);
 
+// source-sphere chunks of a problem's far-field work items: consecutive spheres of about
+// max(2048, M_problem / 16) grid points; depends only on the problem itself, so its sums are the
+// same alone or inside any batch
+std::vector<std::pair<int, int>> source_chunks(const smob_ctx* c, const Problem& pr) {
+    const int mp = pr.p1 - pr.p0;
+    const int ch = std::max(2048, (mp + 15) / 16);
+    std::vector<std::pair<int, int>> chunks;
+    int cs = pr.s0, acc = 0;
+    for (int s = pr.s0; s < pr.s1; ++s) {
+        acc += c->glen[s];
+        if (acc >= ch || s + 1 == pr.s1) {
+            chunks.push_back({cs, s + 1});
+            cs = s + 1;
+            acc = 0;
+        }
+    }
+    return chunks;
+}
+
 void build_context(smob_ctx* c, const smob_geometry* geo) {
     const int N = geo->n_spheres;
     c->N = N;
@@ -502,17 +536,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
         for (int pi = 0; pi < c->P; ++pi) {
             Problem& pr = c->problems[pi];
             const int mp = pr.p1 - pr.p0;
-            const int ch = std::max(2048, (mp + 15) / 16);
-            std::vector<std::pair<int, int>> chunks;
-            int cs = pr.s0, acc = 0;
-            for (int s = pr.s0; s < pr.s1; ++s) {
-                acc += c->glen[s];
-                if (acc >= ch || s + 1 == pr.s1) {
-                    chunks.push_back({cs, s + 1});
-                    cs = s + 1;
-                    acc = 0;
-                }
-            }
+            const std::vector<std::pair<int, int>> chunks = source_chunks(c, pr);
             pr.nchunks = (int)chunks.size();
             pr.poff = poff;
             poff += 3LL * mp * pr.nchunks;
@@ -732,7 +756,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.clev.assign((size_t)N * kCoarseLevels, make_int4(0, 0, 0, 0));
     h.cent.clear();
     h.ncoarse = 0;
-    std::vector<float> maps;
+    std::vector<float> maps, mapsT;
     std::vector<double> mapsd;
     std::map<int, int> map_off;  // p * 64 + pe -> offset in the maps
     if (h.eps > 0) {
@@ -760,6 +784,18 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                             if (kCoarseLadder[l] < ps) used[l] = 1;
                             break;
                         }
+                    // s as the target of t: the same ratio a_s / (|c_t - c_s| - a_t), its own margin,
+                    // and a level only if it has at most kCoarseTargetNum / kCoarseTargetDen of the grid
+                    if (h.ctgt) {
+                        const double need_t = leps / std::log(as / rmin) + kCoarseTargetMargin;
+                        for (size_t l = 0; l < used.size(); ++l)
+                            if (kCoarseLadder[l] >= need_t) {
+                                const int pe = kCoarseLadder[l];
+                                if (pe < ps && (pe + 1) * (2 * pe + 2) * kCoarseTargetDen <= c->glen[s] * kCoarseTargetNum)
+                                    used[l] = 1;
+                                break;
+                            }
+                    }
                 }
                 std::vector<int> pes;
                 for (size_t l = 0; l < used.size(); ++l)
@@ -769,6 +805,9 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                     const int pe = pes[l];
                     const int key = ps * 64 + pe;
                     if (!map_off.count(key)) {
+                        // the map [fine j][coarse k] and (FP32 set) at the same offset its transpose
+                        // [k][j] (the coarse targets' interpolation)
+                        const int ngf = (ps + 1) * (2 * ps + 2), nec = (pe + 1) * (2 * pe + 2);
                         if (h.hp) {
                             const std::vector<double>& m = coarse_map_d(ps, pe);
                             map_off[key] = (int)mapsd.size();
@@ -777,6 +816,10 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                             const std::vector<float>& m = coarse_map(ps, pe);
                             map_off[key] = (int)maps.size();
                             maps.insert(maps.end(), m.begin(), m.end());
+                            mapsT.resize(maps.size());
+                            for (int j = 0; j < ngf; ++j)
+                                for (int k = 0; k < nec; ++k)
+                                    mapsT[map_off[key] + (size_t)k * ngf + j] = m[(size_t)j * nec + k];
                         }
                     }
                     if (!have_nodes[pe]) {
@@ -821,6 +864,133 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
             for (int k0 = 0; k0 < mg.cnt; k0 += kCoarseTileNodes)
                 h.cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
     }
+    // Coarse targets: for every sphere t and level l small enough to serve as its targets, the source
+    // spheres whose pair may take that level (tgt_level on the device, in FP32 from FP32 centres:
+    // listed here in FP64 with a margin of kCtRuleSlack orders on both sides of each level boundary,
+    // so a pair near a boundary is a candidate of both levels and the device check picks one). Work
+    // items: node blocks of 128, 64 or 32 threads x candidate ranges of about kCtSrcPoints source points.
+    constexpr double kCtRuleSlack = 1e-3;
+    constexpr int kCtSrcPoints = 512;
+    h.ctent.clear();
+    h.ctsrc.clear();
+    h.ct_work.clear();
+    h.ctitile.clear();
+    h.ctient.clear();
+    std::vector<double> work_cost;
+    h.ctused.assign((size_t)std::max(N, 1) * kCoarseLevels, 0);
+    h.ct_partial = 0;
+    if (h.ctgt && !h.cent.empty()) {
+        const double leps = std::log(h.eps);
+        auto dist = [&](int t, int s) {
+            double d2 = 0;
+            for (int k = 0; k < 3; ++k) {
+                const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
+                d2 += dk * dk;
+            }
+            return std::sqrt(d2);
+        };
+        // source points a candidate will likely be read from (its coarse level for t, or its grid)
+        auto src_points = [&](int t, int s, double d) {
+            const int4* L = &h.clev[(size_t)s * kCoarseLevels];
+            const double rmin = d - c->radii[t];
+            if (L[0].x != 0 && rmin > c->radii[s]) {
+                const double need = leps / std::log(c->radii[s] / rmin) + kCoarseMargin;
+                for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l)
+                    if (L[l].x >= need) return L[l].z;
+            }
+            return c->glen[s];
+        };
+        std::vector<std::vector<int>> cand(kCoarseLevels), pts(kCoarseLevels);
+        for (int pi = 0; pi < c->P; ++pi) {
+            const Problem& pr = c->problems[pi];
+            for (int t = pr.s0; t < pr.s1; ++t) {
+                const int4* L = &h.clev[(size_t)t * kCoarseLevels];
+                if (L[0].x == 0) continue;
+                for (auto& v : cand) v.clear();
+                for (auto& v : pts) v.clear();
+                for (int s = pr.s0; s < pr.s1; ++s) {
+                    if (s == t) continue;
+                    bool nearp = false;
+                    for (int e = c->nbr_start[t]; e < c->nbr_start[t + 1] && !nearp; ++e) nearp = c->nbr_src[e] == s;
+                    if (nearp) continue;
+                    const double d = dist(t, s);
+                    const double rmin = d - c->radii[s];
+                    if (!(rmin > c->radii[t])) continue;
+                    const double need = leps / std::log(c->radii[t] / rmin) + kCoarseTargetMargin;
+                    for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l) {
+                        if (L[l].z * kCoarseTargetDen > c->glen[t] * kCoarseTargetNum) break;  // and every finer
+                        if (L[l].x >= need - kCtRuleSlack && (l == 0 || L[l - 1].x < need + kCtRuleSlack)) {
+                            cand[l].push_back(s);
+                            pts[l].push_back(src_points(t, s, d));
+                        }
+                    }
+                }
+                for (int l = 0; l < kCoarseLevels; ++l) {
+                    if (cand[l].empty()) continue;
+                    CtEnt e{};
+                    e.t = t;
+                    e.l = l;
+                    e.q0 = L[l].y;
+                    e.n = L[l].z;
+                    e.src0 = (int)h.ctsrc.size();
+                    e.nsrc = (int)cand[l].size();
+                    e.problem = pi;
+                    e.poff = h.ct_partial;
+                    std::vector<std::pair<int, int>> chunks;
+                    std::vector<int> chunk_pts;
+                    for (int a = 0, acc = 0, i = 0; i < e.nsrc; ++i) {
+                        acc += pts[l][i];
+                        if (acc >= kCtSrcPoints || i + 1 == e.nsrc) {
+                            chunks.push_back({e.src0 + a, e.src0 + i + 1});
+                            chunk_pts.push_back(acc);
+                            a = i + 1;
+                            acc = 0;
+                        }
+                    }
+                    e.nchunks = (int)chunks.size();
+                    h.ct_partial += 3LL * e.n * e.nchunks;
+                    h.ctsrc.insert(h.ctsrc.end(), cand[l].begin(), cand[l].end());
+                    const int ei = (int)h.ctent.size();
+                    h.ctent.push_back(e);
+                    h.ctused[(size_t)t * kCoarseLevels + l] = 1;
+                    for (int k0 = 0, rem = e.n; rem > 0;) {
+                        const int w = rem > 96 ? 128 : (rem > 32 ? 64 : 32);
+                        const int nb = std::min(w, rem);
+                        for (int ci = 0; ci < e.nchunks; ++ci) {
+                            h.ct_work.push_back(CtWork{ei, k0, nb, w, chunks[ci].first, chunks[ci].second, ci, 0});
+                            // the CTA's time: its source points over its slices
+                            work_cost.push_back((double)chunk_pts[ci] * w / kFarThreads);
+                        }
+                        k0 += nb;
+                        rem -= nb;
+                    }
+                }
+            }
+        }
+        // longest items first (the tail of the one wave they usually fill)
+        std::vector<int> order(h.ct_work.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work_cost[a] > work_cost[b]; });
+        std::vector<CtWork> sorted(order.size());
+        for (size_t i = 0; i < order.size(); ++i) sorted[i] = h.ct_work[order[i]];
+        h.ct_work.swap(sorted);
+        // interpolation tiles: listed entries grouped by map, 8 entries x 128 grid points per CTA
+        std::map<int, std::vector<int>> by_map;
+        for (int i = 0; i < (int)h.ctent.size(); ++i) {
+            const CtEnt& e = h.ctent[i];
+            by_map[h.clev[(size_t)e.t * kCoarseLevels + e.l].w].push_back(i);
+        }
+        for (auto& kv : by_map) {
+            const CtEnt& e0 = h.ctent[kv.second[0]];
+            const int ng = c->glen[e0.t], n = e0.n;
+            for (size_t a = 0; a < kv.second.size(); a += 8) {
+                const int first = (int)h.ctient.size();
+                const int ne = (int)std::min<size_t>(8, kv.second.size() - a);
+                h.ctient.insert(h.ctient.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
+                for (int j0 = 0; j0 < ng; j0 += 128) h.ctitile.push_back(CtITile{kv.first, ng, n, first, ne, j0, 0, 0});
+            }
+        }
+    }
     h.d_clev.upload(h.clev);
     h.d_cent.upload(h.cent);
     h.d_cdesc.upload(h.cdesc);
@@ -832,6 +1002,19 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.d_cpos32.alloc(sizeof(float4) * np);
     if (h.hp) h.d_cpos32lo.alloc(sizeof(float4) * np);
     h.d_csrc.alloc(sizeof(float4) * np * (h.hp ? 2 : 1));
+    if (!h.ctent.empty()) {
+        h.d_ctent.upload(h.ctent);
+        h.d_ctsrc.upload(h.ctsrc);
+        h.d_ctused.upload(h.ctused);
+        h.d_ct_work.upload(h.ct_work);
+        h.d_ctitile.upload(h.ctitile);
+        h.d_ctient.upload(h.ctient);
+        h.d_ct_partial.alloc(sizeof(float) * (size_t)h.ct_partial);
+        h.d_ctinterp.alloc(sizeof(float) * 3 * (size_t)kCoarseLevels * (size_t)std::max(c->M, 1));
+        h.d_cmapT.upload(mapsT);
+        h.d_cnrm32.alloc(sizeof(float4) * np);
+        h.d_ctu.alloc(sizeof(float4) * np);
+    }
 }
 
 void build_coarse(smob_ctx* c) {
@@ -855,9 +1038,10 @@ void build_coarse(smob_ctx* c) {
 // coarse points of both sets (after the grid; geometry-dependent)
 void coarse_grids(smob_ctx* c) {
     check_launch(c, launch_coarse_grid(c->g, c->g.cs32, c->d_org.as<double>(), c->c32.d_cpos32.as<float4>(), nullptr,
+                                       c->c32.ctent.empty() ? nullptr : c->c32.d_cnrm32.as<float4>(), nullptr,
                                        c->st));
     check_launch(c, launch_coarse_grid(c->g, c->g.cshp, c->d_org.as<double>(), c->chp.d_cpos32.as<float4>(),
-                                       c->chp.d_cpos32lo.as<float4>(), c->st));
+                                       c->chp.d_cpos32lo.as<float4>(), nullptr, nullptr, c->st));
 }
 
 void bind_geom(smob_ctx* c) {
@@ -913,6 +1097,20 @@ void bind_geom(smob_ctx* c) {
         cs.cdesc = h.d_cdesc.as<int4>();
         cs.cgrp = h.d_cgrp.as<int4>();
         cs.gent = h.d_gent.as<int2>();
+        const bool ct = !h.ctent.empty();
+        cs.ctgt = ct ? 1 : 0;
+        cs.ctmargin = float(kCoarseTargetMargin);
+        cs.cnrm32 = ct ? h.d_cnrm32.as<float4>() : nullptr;
+        cs.cmapT = ct ? h.d_cmapT.as<float>() : nullptr;
+        cs.ctused = ct ? h.d_ctused.as<int>() : nullptr;
+        cs.nctent = ct ? (int)h.ctent.size() : 0;
+        cs.ctent = ct ? h.d_ctent.as<CtEnt>() : nullptr;
+        cs.ctsrc = ct ? h.d_ctsrc.as<int>() : nullptr;
+        cs.ctinterp = ct ? h.d_ctinterp.as<float>() : nullptr;
+        cs.nctitile = ct ? (int)h.ctitile.size() : 0;
+        cs.ctitile = ct ? h.d_ctitile.as<CtITile>() : nullptr;
+        cs.ctient = ct ? h.d_ctient.as<int>() : nullptr;
+        cs.ctu = ct ? h.d_ctu.as<float4>() : nullptr;
     };
     bind_set(c->c32, g.cs32);
     bind_set(c->chp, g.cshp);
@@ -993,6 +1191,14 @@ void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
 // kernels with the far field in float-float (the high-precision operator of the mixed solve)
 enum OpPrec { OP_FP64 = 0, OP_FP32 = 1, OP_DF = 2 };
 
+// FP32 far field at the coarse targets (after the pass's coarse strengths, on the far stream)
+void far_ct(smob_ctx* c, bool trac, cudaStream_t st) {
+    if (c->c32.ctent.empty()) return;
+    ProfScope ps(c, "far_ct", st);
+    check_launch(c, launch_far_ct(c->g, c->c32.d_ct_work.as<CtWork>(), (int)c->c32.ct_work.size(), trac,
+                                  c->d_src32.as<float4>(), c->c32.d_ct_partial.as<float>(), st));
+}
+
 // out (device) += c_id*x + c_sl*S[x] + c_trac*K[x] + c_lop*L[x] on active problems
 void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_sl, double c_trac, double c_lop,
               int prec) {
@@ -1028,6 +1234,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 ProfScope ps(c, "far_coarse", fs);
                 check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
             }
+            if (fp32) far_ct(c, tr, fs);
             ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"), fs);
             if (fp32 && c->nrep > 1)
                 check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
@@ -1067,7 +1274,8 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
         fork.join();
         {
             ProfScope ps(c, "far_reduce");
-            check_launch(c, launch_far_reduce(g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), out, c->st));
+            check_launch(c, launch_far_reduce(g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), out, c->st,
+                                              fp32 && !c->c32.ctent.empty() ? 1 : 0));
         }
     };
     if (trac) kind_pass(true, c_trac, true);
@@ -2061,11 +2269,13 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                         ProfScope ps(c, "far_coarse");
                         check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
                     }
+                    if (fp32) far_ct(c, tr, c->st);
                     ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
                     check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
                                                      c->d_src64.as<double4_32a>(), partial, c->st, c->tpt));
                 }
-                check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st));
+                check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st,
+                                                  fp32 && !c->c32.ctent.empty() ? 1 : 0));
             }
         });
         prof_flush(c);
@@ -2226,6 +2436,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
     r->c32.eps = c->c32.eps;  // replicas share the levels; each column's coarse strengths are its own
+    r->c32.ctgt = c->c32.ctgt;  // coarse targets per replica (the replicas are problems of the copy)
     r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
@@ -2426,6 +2637,24 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
     });
 }
 
+smob_status smob_set_far_coarse_targets(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        AllocStreamScope as(c->st);
+        c->drop_graphs();  // captured blocks hold the old coarse tables
+        for (auto& kv : c->multi) smob_destroy(kv.second);
+        c->multi.clear();
+        c->c32.ctgt = on != 0;
+        c->rk = 0;
+        build_coarse(c);
+        bind_geom(c);
+        coarse_grids(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
 smob_status smob_far_compression_info(const smob_ctx* c, int hp, double* eps, int* coarse_points, int* entries) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
@@ -2440,12 +2669,50 @@ smob_status smob_far_compression_info(const smob_ctx* c, int hp, double* eps, in
 smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* evaluated, long long* coarse_macs) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        // the FP32 kernels' per-CTA choice replayed on the host for the current work items: a source
-        // sphere is skipped when every target skips it, read from its grid points when some target
-        // skips it or needs them, else from the finest coarse level any target votes for
+        // the FP32 kernels' choices replayed on the host for the current work items: a pair whose
+        // target sphere has a coarse-target level for it goes to the coarse targets (their nodes
+        // against the source's level for that target sphere, or its grid); on the grid targets a
+        // source sphere is skipped when every target skips it, read from its grid points when some
+        // target needs them, else from the finest coarse level any target votes for
         const smob_ctx::CoarseHost& h = c->c32;
         const double leps = h.eps > 0 ? std::log(h.eps) : 0.0;
-        long long dir = 0, ev = 0;
+        auto dist = [&](int t, int s) {
+            double d2 = 0;
+            for (int k = 0; k < 3; ++k) {
+                const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
+                d2 += dk * dk;
+            }
+            return std::sqrt(d2);
+        };
+        auto near_pair = [&](int t, int s) {
+            if (t == s) return true;
+            for (int e = c->nbr_start[t]; e < c->nbr_start[t + 1]; ++e)
+                if (c->nbr_src[e] == s) return true;
+            return false;
+        };
+        // level index of the source side (nodes on t's surface), -1: grid sources
+        auto src_level = [&](int t, int s) {
+            const int4* L = &h.clev[(size_t)s * kCoarseLevels];
+            if (h.cent.empty() || L[0].x == 0) return -1;
+            const double rmin = dist(t, s) - c->radii[t];
+            if (!(rmin > c->radii[s])) return -1;
+            const double need = leps / std::log(c->radii[s] / rmin) + kCoarseMargin;
+            for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l)
+                if (L[l].x >= need) return l;
+            return -1;
+        };
+        // coarse-target level of t for s, -1: grid targets
+        auto tgt_lev = [&](int t, int s) {
+            const int4* L = &h.clev[(size_t)t * kCoarseLevels];
+            if (h.ctent.empty() || L[0].x == 0) return -1;
+            const double rmin = dist(t, s) - c->radii[s];
+            if (!(rmin > c->radii[t])) return -1;
+            const double need = leps / std::log(c->radii[t] / rmin) + kCoarseTargetMargin;
+            for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l)
+                if (L[l].x >= need) return L[l].z * kCoarseTargetDen <= c->glen[t] * kCoarseTargetNum ? l : -1;
+            return -1;
+        };
+        long long dir = 0, ev = 0, macs = 0;
         std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
         for (const FarItem& it : c->items32) {
             tsph.clear();
@@ -2455,42 +2722,32 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
                 tsph.back().second++;
             }
             for (int s = it.s0; s < it.s1; ++s) {
-                int keep = 0, all = 0, fine = 0, lvmax = -1;
+                int keep = 0, fine = 0, lvmax = -1;
                 for (auto& ts : tsph) {
                     const int t = ts.first;
-                    all += ts.second;
-                    bool skip = t == s;
-                    for (int e = c->nbr_start[t]; e < c->nbr_start[t + 1] && !skip; ++e) skip = c->nbr_src[e] == s;
-                    if (skip) continue;
+                    if (near_pair(t, s)) continue;
+                    dir += (long long)ts.second * c->glen[s];
+                    if (tgt_lev(t, s) >= 0) continue;
                     keep += ts.second;
-                    int lv = -1;
-                    const int4* L = &h.clev[(size_t)s * kCoarseLevels];
-                    if (!h.cent.empty() && L[0].x != 0) {
-                        double d2 = 0;
-                        for (int k = 0; k < 3; ++k) {
-                            const double dk = c->centers[3 * t + k] - c->centers[3 * s + k];
-                            d2 += dk * dk;
-                        }
-                        const double rmin = std::sqrt(d2) - c->radii[t];
-                        if (rmin > c->radii[s]) {
-                            const double need = leps / std::log(c->radii[s] / rmin) + kCoarseMargin;
-                            for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l)
-                                if (L[l].x >= need) {
-                                    lv = l;
-                                    break;
-                                }
-                        }
-                    }
+                    const int lv = src_level(t, s);
                     if (lv < 0) fine = 1;
                     else lvmax = std::max(lvmax, lv);
                 }
-                dir += (long long)keep * c->glen[s];
                 if (keep == 0) continue;
-                if (fine || keep < all) ev += (long long)keep * c->glen[s];
-                else ev += (long long)all * h.clev[(size_t)s * kCoarseLevels + lvmax].z;
+                ev += (long long)keep * (fine ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lvmax].z);
             }
         }
-        long long macs = 0;
+        // coarse-target work items: a candidate counts if its pair takes the entry's level
+        for (const CtWork& w : h.ct_work) {
+            const CtEnt& e = h.ctent[w.ent];
+            for (int i = w.sa; i < w.sb; ++i) {
+                const int s = h.ctsrc[i];
+                if (tgt_lev(e.t, s) != e.l) continue;
+                const int lv = src_level(e.t, s);
+                ev += (long long)w.nb * (lv < 0 ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lv].z);
+            }
+        }
+        for (const CtEnt& e : h.ctent) macs += 3LL * c->glen[e.t] * e.n;  // interpolation to the grid
         for (const int2& e : h.cent) macs += 3LL * c->glen[e.x] * h.clev[(size_t)e.x * kCoarseLevels + e.y].z;
         if (direct) *direct = dir;
         if (evaluated) *evaluated = ev;

@@ -137,6 +137,32 @@ __device__ __forceinline__ unsigned level_bit(const DevGeom& g, const CoarseSet&
     return kBitFine;
 }
 
+// Coarse-target level of the far pair (target sphere t, source sphere s): the index of the coarsest
+// built level of t with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s)) + ctmargin, if that level has
+// at most kCoarseTargetNum / kCoarseTargetDen of t's grid points; else -1 (grid targets). The grid
+// kernels skip exactly the pairs for which this is >= 0 and the coarse-target kernel evaluates exactly
+// those (both call this function on the same arguments). Near pairs and t == s are excluded by the
+// callers.
+__device__ __forceinline__ int tgt_level(const DevGeom& g, const CoarseSet& cs, int t, int s) {
+    if (!cs.ctgt || cs.ncent == 0) return -1;
+    const int4* L = cs.clev + t * kCoarseLevels;
+    if (__ldg(&L[0].x) == 0) return -1;
+    const float4 ct = __ldg(g.sph32 + t), cs4 = __ldg(g.sph32 + s);
+    const float dx = ct.x - cs4.x, dy = ct.y - cs4.y, dz = ct.z - cs4.z;
+    const float rmin = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - cs4.w;
+    const float at = ct.w;
+    if (!(rmin > at)) return -1;
+    const float need = cs.clog_eps / __logf(at / rmin) + cs.ctmargin;
+    const int cap = __ldg(g.glen + t) * kCoarseTargetNum;
+#pragma unroll 1
+    for (int l = 0; l < kCoarseLevels; ++l) {
+        const int4 Ll = __ldg(&L[l]);
+        if (Ll.x == 0) break;
+        if (float(Ll.x) >= need) return Ll.z * kCoarseTargetDen <= cap ? l : -1;
+    }
+    return -1;
+}
+
 // CTA-wide OR of one vote per thread (per-warp slots, double-buffered by parity: one barrier); NT threads
 template <int NT = kFarThreads>
 __device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[NT / 32], int parity) {
@@ -149,12 +175,14 @@ __device__ __forceinline__ unsigned cta_or(unsigned v, unsigned (*slots)[NT / 32
     return r;
 }
 
-// the CTA's source range for sphere s from its votes: fine grid points or one coarse level (FP32 set)
+// the CTA's source range for sphere s from its votes: fine grid points or one coarse level (FP32 set);
+// targets that skip the sphere do not vote, and the others may take coarse sources (a masked loop)
 __device__ __forceinline__ bool pick_sources(const DevGeom& g, int s, unsigned votes, const float4* src,
                                              const float4*& P, const float4*& F, int& g0, int& gl) {
-    const bool coarse = !(votes & (kBitSkip | kBitFine));
+    const unsigned lv = votes & ~kBitSkip;
+    const bool coarse = !(lv & kBitFine);
     if (coarse) {
-        const int4 L = g.cs32.clev[s * kCoarseLevels + (31 - __clz(votes))];
+        const int4 L = g.cs32.clev[s * kCoarseLevels + (31 - __clz(lv))];
         P = g.cs32.cpos32;
         F = g.cs32.csrc;
         g0 = L.y;
@@ -414,7 +442,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
         unsigned vote = 0;
 #pragma unroll
         for (int u = 0; u < T; ++u) {
-            sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
+            sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s) || tgt_level(g, g.cs32, sid[u], s) >= 0;
             none = none && !sk[u];
             if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, g.cs32, sid[u], s);
         }
@@ -422,7 +450,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
         if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
         const float4 *SP, *SF;
         int g0, gl;
-        const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
+        pick_sources(g, s, votes, src, SP, SF, g0, gl);
         for (int base = 0; base < gl; base += kFarTile32) {
             const int n = min(kFarTile32, gl - base);
             __syncthreads();
@@ -433,7 +461,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32x2(DevGeom g, const FarIte
                 sC[k] = make_float4(f.y, f.y, f.z, f.z);
             }
             __syncthreads();
-            if (none || coarse) {
+            if (none) {
 #pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const float4 A = sA[k], B = sB[k], C = sC[k];
@@ -514,7 +542,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
         unsigned vote = 0;
 #pragma unroll
         for (int u = 0; u < TPT; ++u) {
-            sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s);
+            sk[u] = !val[u] || excluded(g.nbr_src, cur[u], end[u], sid[u], s) || tgt_level(g, g.cs32, sid[u], s) >= 0;
             none = none && !sk[u];
             if (val[u]) vote |= sk[u] ? kBitSkip : level_bit(g, g.cs32, sid[u], s);
         }
@@ -522,7 +550,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
         if (!(votes & ~kBitSkip)) continue;  // every target skips this sphere
         const float4 *SP, *SF;
         int g0, gl;
-        const bool coarse = pick_sources(g, s, votes, src, SP, SF, g0, gl);
+        pick_sources(g, s, votes, src, SP, SF, g0, gl);
         for (int base = 0; base < gl; base += kFarTile32) {
             const int n = min(kFarTile32, gl - base);
             __syncthreads();
@@ -531,7 +559,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32(DevGeom g, const FarItem*
                 sf[k] = SF[g0 + base + k];
             }
             __syncthreads();
-            if (none || coarse) {
+            if (none) {
 #pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const float4 q = sp[k], f = sf[k];
@@ -600,7 +628,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
     for (int r = 0; r < KB; ++r) ax[r] = ay[r] = az[r] = 0.f;
     int parity = 0;
     for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
-        const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s);
+        const bool sk = !va || excluded(g.nbr_src, ca, ea, sa, s) || tgt_level(g, g.cs32, sa, s) >= 0;
         // the same per-CTA choice as k_far32<TRAC, 1> over the same targets (replica 0's items)
         const unsigned votes = cta_or(va ? (sk ? kBitSkip : level_bit(g, g.cs32, sa, s)) : 0u, votes_buf, parity);
         if (!(votes & ~kBitSkip)) continue;
@@ -660,6 +688,164 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
             o[1] = ay[r];
             o[2] = az[r];
         }
+    }
+}
+
+// ---------------------------------------------------------------- coarse targets (FP32)
+// One CTA per work item: nodes [k0, k0 + nb) of a listed entry (target sphere t, level l) against a
+// range of its candidate source spheres. A candidate counts only if tgt_level(t, s) == l (the rule
+// the grid kernels skip by, evaluated here on the same arguments; CTA-uniform), and is read from its
+// coarse level for t (level_bit: the nodes lie on t's surface) or its grid. The CTA's threads form
+// 128 / w slices of w threads: thread (node, slice) takes every (128 / w)-th staged pair of source
+// points, so small entries keep every thread busy. A thread's target sits duplicated in both FP32x2
+// lanes and the sources are staged two to a pack, (x1,x2,y1,y2) (z1,z2,fx1,fx2) (fy1,fy2,fz1,fz2):
+// one packed pair_x2 evaluates two pairs (an odd tile ends with a zero-strength point 1e18 away).
+// The lanes' and slices' sums are added in a fixed order.
+template <bool TRAC>
+__global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWork* __restrict__ works,
+                                                         const float4* __restrict__ src, float* __restrict__ partial) {
+    const CtWork w = works[blockIdx.x];
+    const CoarseSet& cs = g.cs32;
+    const CtEnt e = cs.ctent[w.ent];
+    if (g.active && !g.active[e.problem]) return;
+    constexpr int kPk = kFarTile32 / 2;
+    __shared__ float4 sA[kPk], sB[kPk], sC[kPk];
+    __shared__ float red[3][kFarThreads];
+    const int nslice = kFarThreads / w.w;
+    const int node = threadIdx.x % w.w, slice = threadIdx.x / w.w;
+    const bool val = node < w.nb;
+    const int cn = e.q0 + w.k0 + node;
+    // an empty slot sits 1e18 away: its terms are finite (and not written)
+    const float4 P = val ? cs.cpos32[cn] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+    const float4 Nn = (TRAC && val) ? cs.cnrm32[cn] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 TX = f2(P.x, P.x), TY = f2(P.y, P.y), TZ = f2(P.z, P.z);
+    const float2 NX = f2(Nn.x, Nn.x), NY = f2(Nn.y, Nn.y), NZ = f2(Nn.z, Nn.z);
+    float2 AX = f2(0.f, 0.f), AY = AX, AZ = AX;
+    for (int i = w.sa; i < w.sb; ++i) {
+        const int s = cs.ctsrc[i];
+        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of the neighbouring level
+        const float4 *SP, *SF;
+        int g0, gl;
+        pick_sources(g, s, level_bit(g, cs, e.t, s), src, SP, SF, g0, gl);
+        for (int base = 0; base < gl; base += kFarTile32) {
+            const int n = min(kFarTile32, gl - base);
+            const int np = (n + 1) >> 1;
+            __syncthreads();
+            for (int k = threadIdx.x; k < np; k += kFarThreads) {
+                const int k1 = 2 * k, k2 = 2 * k + 1;
+                const float4 p1 = SP[g0 + base + k1], f1 = SF[g0 + base + k1];
+                const float4 p2 = k2 < n ? SP[g0 + base + k2] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+                const float4 q2 = k2 < n ? SF[g0 + base + k2] : make_float4(0.f, 0.f, 0.f, 0.f);
+                sA[k] = make_float4(p1.x, p2.x, p1.y, p2.y);
+                sB[k] = make_float4(p1.z, p2.z, f1.x, q2.x);
+                sC[k] = make_float4(f1.y, q2.y, f1.z, q2.z);
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int k = slice; k < np; k += nslice)
+                pair_x2<TRAC>(TX, TY, TZ, NX, NY, NZ, sA[k], sB[k], sC[k], AX, AY, AZ);
+        }
+    }
+    red[0][threadIdx.x] = AX.x + AX.y;
+    red[1][threadIdx.x] = AY.x + AY.y;
+    red[2][threadIdx.x] = AZ.x + AZ.y;
+    __syncthreads();
+    if (slice == 0 && val) {
+        float x = 0.f, y = 0.f, z = 0.f;
+        for (int sl = 0; sl < nslice; ++sl) {
+            x += red[0][node + sl * w.w];
+            y += red[1][node + sl * w.w];
+            z += red[2][node + sl * w.w];
+        }
+        float* o = partial + e.poff + 3LL * ((long long)w.chunk * e.n + w.k0 + node);
+        o[0] = x;
+        o[1] = y;
+        o[2] = z;
+    }
+}
+
+// the chunks' sums of every listed entry's nodes, in fixed order, into ctu
+__global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
+    const CoarseSet& cs = g.cs32;
+    const CtEnt e = cs.ctent[blockIdx.x];
+    if (g.active && !g.active[e.problem]) return;
+    for (int k = threadIdx.x; k < e.n; k += blockDim.x) {
+        float x = 0.f, y = 0.f, z = 0.f;
+        for (int c = 0; c < e.nchunks; ++c) {
+            const float* o = partial + e.poff + 3LL * ((long long)c * e.n + k);
+            x += o[0];
+            y += o[1];
+            z += o[2];
+        }
+        cs.ctu[e.q0 + k] = make_float4(x, y, z, 0.f);
+    }
+}
+
+// Interpolation of the listed entries' node values to their spheres' grids: u(nu_j) = sum_k w_k
+// K_pe(nu_j . nu_k) u_k (the transposed coarse map, exact for fields of degree <= pe on the sphere).
+// A small GEMM per map (order p, level pe): CTA tile = 128 grid points x up to 8 entries of that
+// map; each map element read (coalesced, [node][grid point]) serves the 8 entries' 3 components,
+// whose node values are staged kCiK nodes at a time in shared memory. Each entry's result goes to
+// its level slot of ctinterp.
+constexpr int kCiEnt = 8, kCiK = 32;
+__global__ void __launch_bounds__(128) k_ct_interp(DevGeom g) {
+    const CoarseSet& cs = g.cs32;
+    const CtITile d = cs.ctitile[blockIdx.x];
+    __shared__ float4 U[kCiK][kCiEnt];
+    __shared__ int eq0[kCiEnt], eon[kCiEnt];
+    __shared__ long long ebase[kCiEnt];
+    if (threadIdx.x < kCiEnt) {
+        const int e = threadIdx.x;
+        eon[e] = 0;
+        eq0[e] = 0;
+        ebase[e] = 0;
+        if (e < d.ne) {
+            const CtEnt en = cs.ctent[cs.ctient[d.e0 + e]];
+            eon[e] = !g.active || g.active[en.problem];
+            eq0[e] = en.q0;
+            ebase[e] = (long long)en.l * g.M + g.gidx[en.t];
+        }
+    }
+    __syncthreads();
+    const int j = d.j0 + threadIdx.x;
+    const bool val = j < d.ng;
+    const float* MT = cs.cmapT + d.mapoff + (val ? j : 0);
+    float acc[kCiEnt][3];
+#pragma unroll
+    for (int e = 0; e < kCiEnt; ++e) acc[e][0] = acc[e][1] = acc[e][2] = 0.f;
+    for (int k0 = 0; k0 < d.n; k0 += kCiK) {
+        const int nk = min(kCiK, d.n - k0);
+        // the chunk's map column in registers first: kCiK independent loads in flight per thread
+        float mk[kCiK];
+#pragma unroll
+        for (int kk = 0; kk < kCiK; ++kk) mk[kk] = (val && kk < nk) ? __ldg(MT + (long long)(k0 + kk) * d.ng) : 0.f;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kCiK * kCiEnt; idx += 128) {
+            const int kk = idx / kCiEnt, e = idx % kCiEnt;
+            U[kk][e] = (kk < nk && eon[e]) ? cs.ctu[eq0[e] + k0 + kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+        // rows past nk hold zeros in both operands
+#pragma unroll
+        for (int kk = 0; kk < kCiK; ++kk) {
+            const float m = mk[kk];
+#pragma unroll
+            for (int e = 0; e < kCiEnt; ++e) {
+                const float4 u = U[kk][e];
+                acc[e][0] = fmaf(m, u.x, acc[e][0]);
+                acc[e][1] = fmaf(m, u.y, acc[e][1]);
+                acc[e][2] = fmaf(m, u.z, acc[e][2]);
+            }
+        }
+    }
+    if (!val) return;
+#pragma unroll
+    for (int e = 0; e < kCiEnt; ++e) {
+        if (e >= d.ne || !eon[e]) continue;
+        float* o = cs.ctinterp + 3LL * (ebase[e] + j);
+        o[0] = acc[e][0];
+        o[1] = acc[e][1];
+        o[2] = acc[e][2];
     }
 }
 
@@ -1067,11 +1253,16 @@ __global__ void k_far_pack(DevGeom g, const double* __restrict__ x, double c, fl
     if (s64) s64[i] = make_double4_32a(fx, fy, fz, 0.0);
 }
 
+// Chunk sums in fixed order, then (ct != 0) the coarse-target values of every used entry of the
+// point's sphere interpolated to the point: u(nu_j) = sum_k w_k K_pe(nu_j . nu_k) u_k, the transposed
+// coarse map (exact for fields of degree <= pe on the sphere), read coalesced as [coarse][fine].
 template <typename Real>
-__global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double pre, double* __restrict__ out) {
+__global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double pre, double* __restrict__ out,
+                             int ct) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.M) return;
-    const int pb = g.prob[g.sid[i]];
+    const int sph = g.sid[i];
+    const int pb = g.prob[sph];
     if (g.active && !g.active[pb]) return;
     const Problem pr = g.problems[pb];
     const long long mp = pr.p1 - pr.p0;
@@ -1082,6 +1273,17 @@ __global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double
         sx += double(q[0]);
         sy += double(q[1]);
         sz += double(q[2]);
+    }
+    if (ct) {
+        // the listed coarse-target entries of the point's sphere, by level
+        const CoarseSet& cs = g.cs32;
+        for (int l = 0; l < kCoarseLevels; ++l) {
+            if (!cs.ctused[sph * kCoarseLevels + l]) continue;
+            const float* o = cs.ctinterp + 3LL * ((long long)l * g.M + i);
+            sx += double(o[0]);
+            sy += double(o[1]);
+            sz += double(o[2]);
+        }
     }
     out[3 * i] += pre * sx;
     out[3 * i + 1] += pre * sy;
@@ -1180,11 +1382,22 @@ int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int 
     return 1;
 }
 
-int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st) {
+int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st,
+                      int ct) {
     const int blocks = (g.M + 255) / 256;
-    if (fp32) k_far_reduce<float><<<blocks, 256, 0, st>>>(g, static_cast<const float*>(partial), pre, out);
-    else k_far_reduce<double><<<blocks, 256, 0, st>>>(g, static_cast<const double*>(partial), pre, out);
+    if (fp32) k_far_reduce<float><<<blocks, 256, 0, st>>>(g, static_cast<const float*>(partial), pre, out, ct);
+    else k_far_reduce<double><<<blocks, 256, 0, st>>>(g, static_cast<const double*>(partial), pre, out, ct);
     return 1;
+}
+
+int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
+                  cudaStream_t st) {
+    if (nworks <= 0 || g.cs32.nctent <= 0) return 0;
+    if (trac) k_far32_ct<true><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
+    else k_far32_ct<false><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
+    k_ct_sum<<<g.cs32.nctent, 128, 0, st>>>(g, partial);
+    k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
+    return 3;
 }
 
 }  // namespace smob

@@ -84,6 +84,53 @@ struct CoarseSet {
     const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
     const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
     const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
+    // Coarse targets (FP32 set): a target sphere t takes the far field of a well-separated source
+    // sphere s at the nodes of one of its own coarse levels and interpolates it to its grid (the
+    // transposed map); level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s))
+    // + ctmargin, if it has at most kCoarseTargetNum / kCoarseTargetDen of the sphere's grid points
+    // (else the pair stays on the grid targets).
+    int ctgt;                  // 1: coarse targets on
+    float ctmargin;
+    const float4* cnrm32;      // coarse node normals, w = level index bits
+    const float* cmapT;        // the maps transposed, [coarse node][fine node], at the maps' offsets
+    const int* ctused;         // [N][kCoarseLevels]: the entry is a listed coarse-target entry (CtEnt)
+    int nctent;
+    const struct CtEnt* ctent; // listed entries: those with candidate source spheres
+    const int* ctsrc;          // the entries' candidate source spheres
+    float4* ctu;               // far field at the coarse targets of the current pass
+    float* ctinterp;           // interpolated to the grid, [level slot][M][3] (listed entries)
+    int nctitile;              // interpolation tiles (CtITile) and their entry lists
+    const struct CtITile* ctitile;
+    const int* ctient;
+};
+
+// coarse targets of a sphere: at most 7/10 of its grid points (interpolation plus coarse evaluation
+// must undercut the grid evaluation)
+constexpr int kCoarseTargetNum = 7, kCoarseTargetDen = 10;
+
+// A listed coarse-target entry (sphere t, level l): its nodes are the coarse points [q0, q0 + n) of
+// the set, its candidate sources ctsrc[src0, src0 + nsrc) (every s with tgt_level(t, s) == l and
+// neighbours of the level boundary; the kernels check the rule per pair); partial sums at poff as
+// [chunk][node][3].
+struct CtEnt {
+    int t, l, q0, n;
+    int src0, nsrc, nchunks, problem;
+    long long poff;
+    long long pad;
+};
+
+// one coarse-target work item: nodes [k0, k0 + nb) of entry ent with w threads per slice (32, 64 or
+// 128; 128 / w slices share the sources) against candidates [sa, sb) of the entry, partial chunk
+struct CtWork {
+    int ent, k0, nb, w;
+    int sa, sb, chunk, pad;
+};
+
+// one interpolation tile: grid points [j0, j0 + 128) of up to 8 listed entries sharing one map
+// (order p, level pe): entries ctient[e0, e0 + ne), map at mapoff ([n][ng])
+struct CtITile {
+    int mapoff, ng, n, e0;
+    int ne, j0, pad0, pad1;
 };
 
 struct DevGeom {
@@ -145,11 +192,20 @@ int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4_32a* src64, void* partial, cudaStream_t st, int tpt = 2);
-int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st);
+// ct: 0 no coarse targets, 1 the FP32 set's (ctu), 2 the float-float set's traction (ctud), 3 its
+// single layer (ctud_sl): the coarse-target values of every used entry are interpolated to the grid and
+// added with the chunks' sums
+int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st,
+                      int ct = 0);
+// FP32 far field at the coarse targets of the listed entries (after launch_coarse_src): the work items
+// into partial (CtEnt layout), their chunks summed into cs32.ctu, and the interpolation of every
+// listed entry to its sphere's grid into cs32.ctinterp (launch_far_reduce with ct = 1 adds it)
+int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
+                  cudaStream_t st);
 // coarse points of every (sphere, level) entry of a set, relative to the problem origins (after
 // launch_regrid); cpos32lo (may be null) receives the low parts
 int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org, float4* cpos32, float4* cpos32lo,
-                       cudaStream_t st);
+                       float4* cnrm32, float4* cnrm32lo, cudaStream_t st);
 // FP32 far field of nrep replicas of one problem (replica r = problem r, points [r*rep_M, (r+1)*rep_M)):
 // items are replica 0's (kFarThreads targets each); each pair's geometry serves all replicas
 int launch_far_field_rep(const DevGeom& g, const FarItem* items, int nitems, int nrep, int rep_M, bool trac,

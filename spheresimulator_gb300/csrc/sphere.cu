@@ -414,7 +414,7 @@ __global__ void k_regrid(DevGeom g, const double* __restrict__ org, double* __re
 // coarse points of one (sphere, level) entry per CTA: the order-pe unit nodes placed like the sphere's
 // own grid (k_regrid), relative to the problem origin in FP32 (and the low parts when asked)
 __global__ void k_coarse_grid(DevGeom g, CoarseSet cs, const double* __restrict__ org, float4* __restrict__ cpos32,
-                              float4* __restrict__ cpos32lo) {
+                              float4* __restrict__ cpos32lo, float4* __restrict__ cnrm32, float4* __restrict__ cnrm32lo) {
     const int2 e = cs.cent[blockIdx.x];
     const int s = e.x;
     const int4 L = cs.clev[s * kCoarseLevels + e.y];
@@ -430,6 +430,13 @@ __global__ void k_coarse_grid(DevGeom g, CoarseSet cs, const double* __restrict_
         if (cpos32lo)
             cpos32lo[L.y + k] = make_float4(float(__dsub_rn(r[0], double(p.x))), float(__dsub_rn(r[1], double(p.y))),
                                             float(__dsub_rn(r[2], double(p.z))), 0.f);
+        if (cnrm32) {
+            const float4 q = make_float4(float(n[0]), float(n[1]), float(n[2]), __int_as_float(e.y));
+            cnrm32[L.y + k] = q;
+            if (cnrm32lo)
+                cnrm32lo[L.y + k] = make_float4(float(__dsub_rn(n[0], double(q.x))), float(__dsub_rn(n[1], double(q.y))),
+                                                float(__dsub_rn(n[2], double(q.z))), 0.f);
+        }
     }
 }
 
@@ -495,9 +502,9 @@ int launch_regrid(const DevGeom& g, const double* org, cudaStream_t st) {
 }
 
 int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org, float4* cpos32, float4* cpos32lo,
-                       cudaStream_t st) {
+                       float4* cnrm32, float4* cnrm32lo, cudaStream_t st) {
     if (cs.ncent <= 0) return 0;
-    k_coarse_grid<<<cs.ncent, 128, 0, st>>>(g, cs, org, cpos32, cpos32lo);
+    k_coarse_grid<<<cs.ncent, 128, 0, st>>>(g, cs, org, cpos32, cpos32lo, cnrm32, cnrm32lo);
     return 1;
 }
 

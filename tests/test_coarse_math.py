@@ -73,3 +73,56 @@ def test_far_field_error_follows_the_level_rule():
                 nc2, _ = grid(pe - 3)
                 worse = np.abs(far(trg, tg, nc2, coarse_map(p, pe - 3) @ f, trac) - ref).max() / np.abs(ref).max()
                 assert worse > err
+
+
+def test_target_interpolation_is_exact_to_degree_pe():
+    """The transposed map interpolates a field sampled at the order-pe nodes to the order-p grid:
+    u(nu_j) = sum_k w_k K_pe(nu_j . nu_k) u(nu_k), exact for degree <= pe."""
+    p, pe = 12, 5
+    nf, _ = grid(p)
+    nc, _ = grid(pe)
+    M = coarse_map(p, pe)
+    for field in (lambda n: n @ np.array([0.3, -1.2, 0.7]),
+                  lambda n: n[:, 0] * n[:, 1] * n[:, 2] ** 3 - 0.4 * n[:, 2] ** 5):  # degrees 1 and 5
+        assert np.allclose(M.T @ field(nc), field(nf), atol=1e-13)
+
+
+def test_coarse_targets_and_sources_follow_the_level_rules():
+    """Both sides compressed: the far field of the source sphere's coarse sources (level from
+    a_s / (d - a_t), margin 1) at the target sphere's coarse nodes (level from a_t / (d - a_s),
+    margin 2: the traction's target normal adds a degree), interpolated to the target grid, stays
+    within 10 eps of the direct sum relative to the pair's largest value."""
+    rng = np.random.default_rng(5)
+    ladder = (3, 4, 5, 6, 8, 10, 12, 14)
+
+    def level(ratio, eps, p, margin):
+        need = np.log(eps) / np.log(ratio) + margin
+        for pe in ladder:
+            if pe >= p:
+                return None
+            if pe >= need:
+                return pe
+        return None
+
+    p = 16
+    nf, wf = grid(p)
+    checked = 0
+    for _ in range(12):
+        at, a_s = rng.uniform(0.8, 1.2, 2)
+        d = rng.uniform(1.5 * (at + a_s), 14.0)
+        u = rng.standard_normal(3)
+        u /= np.linalg.norm(u)
+        f = (wf * a_s ** 2)[:, None] * rng.standard_normal((len(nf), 3))
+        for eps in (1e-5, 1e-10):
+            lt = level(at / (d - a_s), eps, p, 2.0)
+            if lt is None:
+                continue
+            ls = level(a_s / (d - at), eps, p, 1.0)
+            src, fs = (d * u + a_s * nf, f) if ls is None else (d * u + a_s * grid(ls)[0], coarse_map(p, ls) @ f)
+            nc, _ = grid(lt)
+            for trac in (True, False):
+                ref = far(at * nf, nf, d * u + a_s * nf, f, trac)
+                val = coarse_map(p, lt).T @ far(at * nc, nc, src, fs, trac)
+                assert np.abs(val - ref).max() / np.abs(ref).max() < 10 * eps, (trac, d, eps, lt, ls)
+                checked += 1
+    assert checked > 10

@@ -153,3 +153,46 @@ def test_far_pairs_replay():
     g.set_far_compression(0, 0)
     d0, e0, m0 = g.far_pairs()
     assert d0 == direct and e0 == direct and m0 == 0
+
+
+def test_coarse_targets_match_direct_sum():
+    """Coarse targets (far fields at a target sphere's coarse nodes, interpolated to its grid) on a
+    spread geometry: fewer evaluated pairs, the same accuracy class as the sources alone, and at a
+    tight tolerance the FP32 rounding level of the direct sum."""
+    c = _spread(seed=31, n=40, p=14, box=40.0)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
+    x = np.random.default_rng(31).standard_normal(3 * g.n_points)
+    fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
+    d_on, e_on, _ = g.far_pairs()
+    on = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
+    g.set_far_coarse_targets(False)
+    d_off, e_off, _ = g.far_pairs()
+    off = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
+    assert d_on == d_off and e_on < 0.7 * e_off
+    assert _rel(off, fp64) < 2e-5 and _rel(on, fp64) < 2e-5
+    for trac, sl in ((1.0, 0.0), (0.0, 1.0)):
+        ref = g.far_field(x, cSL=sl, cTrac=trac, precision=PREC_FP64)
+        g.set_far_coarse_targets(True)
+        g.set_far_compression(1e-8)
+        assert _rel(g.far_field(x, cSL=sl, cTrac=trac, precision=PREC_MIXED), ref) < 2e-6
+        g.set_far_compression(1e-5)
+        assert _rel(g.far_field(x, cSL=sl, cTrac=trac, precision=PREC_MIXED), ref) < 2e-5
+        g.set_far_coarse_targets(False)
+
+
+def test_coarse_targets_in_batches_and_mixed_solves():
+    """Coarse targets inside a batch of two problems: each problem's solve equals its solve alone bit
+    for bit, and equals the solve without coarse targets to the solve tolerance."""
+    a, b = _spread(seed=32, n=16, p=10, box=30.0), _spread(seed=33, n=12, p=12, box=30.0)
+    centers = np.vstack([a["centers"], b["centers"] + 300.0])
+    radii = np.concatenate([a["radii"], b["radii"]])
+    orders = np.concatenate([a["orders"], b["orders"]])
+    prob = np.array([0] * 16 + [1] * 12, dtype=np.int32)
+    F = np.random.default_rng(34).standard_normal(6 * 28)
+    g = SphereSTKMobMat(centers, radii, orders, problem=prob)
+    v = g.solveMob(F, tol=1e-10, precision=PREC_MIXED)
+    assert all(s["status"] == 0 for s in g.last_stats)
+    alone = SphereSTKMobMat(a["centers"], a["radii"], a["orders"])
+    assert np.array_equal(alone.solveMob(F[:96], tol=1e-10, precision=PREC_MIXED), v[:96])
+    g.set_far_coarse_targets(False)
+    assert _rel(g.solveMob(F, tol=1e-10, precision=PREC_MIXED), v) < 1e-9
