@@ -900,12 +900,52 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
             }
             return c->glen[s];
         };
-        std::vector<std::vector<int>> cand(kCoarseLevels), pts(kCoarseLevels);
+        // slot kCoarseLevels: the grid entry's candidates (pairs that stay on the grid targets)
+        std::vector<std::vector<int>> cand(kCoarseLevels + 1), pts(kCoarseLevels + 1);
+        auto add_entry = [&](int t, int l, int q0, int n, int pi) {
+            const int slot = l < 0 ? kCoarseLevels : l;
+            CtEnt e{};
+            e.t = t;
+            e.l = l;
+            e.q0 = q0;
+            e.n = n;
+            e.src0 = (int)h.ctsrc.size();
+            e.nsrc = (int)cand[slot].size();
+            e.problem = pi;
+            e.poff = h.ct_partial;
+            std::vector<std::pair<int, int>> chunks;
+            std::vector<int> chunk_pts;
+            for (int a = 0, acc = 0, i = 0; i < e.nsrc; ++i) {
+                acc += pts[slot][i];
+                if (acc >= kCtSrcPoints || i + 1 == e.nsrc) {
+                    chunks.push_back({e.src0 + a, e.src0 + i + 1});
+                    chunk_pts.push_back(acc);
+                    a = i + 1;
+                    acc = 0;
+                }
+            }
+            e.nchunks = (int)chunks.size();  // 0: no candidates, the sums are zeros
+            h.ct_partial += 3LL * e.n * e.nchunks;
+            h.ctsrc.insert(h.ctsrc.end(), cand[slot].begin(), cand[slot].end());
+            const int ei = (int)h.ctent.size();
+            h.ctent.push_back(e);
+            if (l >= 0) h.ctused[(size_t)t * kCoarseLevels + l] = 1;
+            for (int k0 = 0, rem = e.n; rem > 0 && e.nchunks > 0;) {
+                const int w = rem > 96 ? 128 : (rem > 32 ? 64 : 32);
+                const int nb = std::min(w, rem);
+                for (int ci = 0; ci < e.nchunks; ++ci) {
+                    h.ct_work.push_back(CtWork{ei, k0, nb, w, chunks[ci].first, chunks[ci].second, ci, 0});
+                    // the CTA's time: its source points over its slices
+                    work_cost.push_back((double)chunk_pts[ci] * w / kFarThreads);
+                }
+                k0 += nb;
+                rem -= nb;
+            }
+        };
         for (int pi = 0; pi < c->P; ++pi) {
             const Problem& pr = c->problems[pi];
             for (int t = pr.s0; t < pr.s1; ++t) {
                 const int4* L = &h.clev[(size_t)t * kCoarseLevels];
-                if (L[0].x == 0) continue;
                 for (auto& v : cand) v.clear();
                 for (auto& v : pts) v.clear();
                 for (int s = pr.s0; s < pr.s1; ++s) {
@@ -915,56 +955,28 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                     if (nearp) continue;
                     const double d = dist(t, s);
                     const double rmin = d - c->radii[s];
-                    if (!(rmin > c->radii[t])) continue;
-                    const double need = leps / std::log(c->radii[t] / rmin) + kCoarseTargetMargin;
-                    for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l) {
-                        if (L[l].z * kCoarseTargetDen > c->glen[t] * kCoarseTargetNum) break;  // and every finer
-                        if (L[l].x >= need - kCtRuleSlack && (l == 0 || L[l - 1].x < need + kCtRuleSlack)) {
-                            cand[l].push_back(s);
-                            pts[l].push_back(src_points(t, s, d));
+                    // the grid entry keeps every pair not certainly taken by one coarse-target level
+                    bool certain = false;
+                    if (L[0].x != 0 && rmin > c->radii[t]) {
+                        const double need = leps / std::log(c->radii[t] / rmin) + kCoarseTargetMargin;
+                        for (int l = 0; l < kCoarseLevels && L[l].x != 0; ++l) {
+                            if (L[l].z * kCoarseTargetDen > c->glen[t] * kCoarseTargetNum) break;  // and every finer
+                            if (L[l].x >= need - kCtRuleSlack && (l == 0 || L[l - 1].x < need + kCtRuleSlack)) {
+                                cand[l].push_back(s);
+                                pts[l].push_back(src_points(t, s, d));
+                                if (L[l].x >= need + kCtRuleSlack && (l == 0 || L[l - 1].x < need - kCtRuleSlack))
+                                    certain = true;
+                            }
                         }
+                    }
+                    if (!certain) {
+                        cand[kCoarseLevels].push_back(s);
+                        pts[kCoarseLevels].push_back(src_points(t, s, d));
                     }
                 }
-                for (int l = 0; l < kCoarseLevels; ++l) {
-                    if (cand[l].empty()) continue;
-                    CtEnt e{};
-                    e.t = t;
-                    e.l = l;
-                    e.q0 = L[l].y;
-                    e.n = L[l].z;
-                    e.src0 = (int)h.ctsrc.size();
-                    e.nsrc = (int)cand[l].size();
-                    e.problem = pi;
-                    e.poff = h.ct_partial;
-                    std::vector<std::pair<int, int>> chunks;
-                    std::vector<int> chunk_pts;
-                    for (int a = 0, acc = 0, i = 0; i < e.nsrc; ++i) {
-                        acc += pts[l][i];
-                        if (acc >= kCtSrcPoints || i + 1 == e.nsrc) {
-                            chunks.push_back({e.src0 + a, e.src0 + i + 1});
-                            chunk_pts.push_back(acc);
-                            a = i + 1;
-                            acc = 0;
-                        }
-                    }
-                    e.nchunks = (int)chunks.size();
-                    h.ct_partial += 3LL * e.n * e.nchunks;
-                    h.ctsrc.insert(h.ctsrc.end(), cand[l].begin(), cand[l].end());
-                    const int ei = (int)h.ctent.size();
-                    h.ctent.push_back(e);
-                    h.ctused[(size_t)t * kCoarseLevels + l] = 1;
-                    for (int k0 = 0, rem = e.n; rem > 0;) {
-                        const int w = rem > 96 ? 128 : (rem > 32 ? 64 : 32);
-                        const int nb = std::min(w, rem);
-                        for (int ci = 0; ci < e.nchunks; ++ci) {
-                            h.ct_work.push_back(CtWork{ei, k0, nb, w, chunks[ci].first, chunks[ci].second, ci, 0});
-                            // the CTA's time: its source points over its slices
-                            work_cost.push_back((double)chunk_pts[ci] * w / kFarThreads);
-                        }
-                        k0 += nb;
-                        rem -= nb;
-                    }
-                }
+                add_entry(t, -1, c->gidx[t], c->glen[t], pi);
+                for (int l = 0; l < kCoarseLevels; ++l)
+                    if (!cand[l].empty()) add_entry(t, l, L[l].y, L[l].z, pi);
             }
         }
         // longest items first (the tail of the one wave they usually fill)
@@ -978,7 +990,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         std::map<int, std::vector<int>> by_map;
         for (int i = 0; i < (int)h.ctent.size(); ++i) {
             const CtEnt& e = h.ctent[i];
-            by_map[h.clev[(size_t)e.t * kCoarseLevels + e.l].w].push_back(i);
+            if (e.l >= 0) by_map[h.clev[(size_t)e.t * kCoarseLevels + e.l].w].push_back(i);
         }
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
@@ -1010,7 +1022,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         h.d_ctitile.upload(h.ctitile);
         h.d_ctient.upload(h.ctient);
         h.d_ct_partial.alloc(sizeof(float) * (size_t)h.ct_partial);
-        h.d_ctinterp.alloc(sizeof(float) * 3 * (size_t)kCoarseLevels * (size_t)std::max(c->M, 1));
+        h.d_ctinterp.alloc(sizeof(float) * 3 * (size_t)(kCoarseLevels + 1) * (size_t)std::max(c->M, 1));
         h.d_cmapT.upload(mapsT);
         h.d_cnrm32.alloc(sizeof(float4) * np);
         h.d_ctu.alloc(sizeof(float4) * np);
@@ -1191,10 +1203,11 @@ void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
 // kernels with the far field in float-float (the high-precision operator of the mixed solve)
 enum OpPrec { OP_FP64 = 0, OP_FP32 = 1, OP_DF = 2 };
 
-// FP32 far field at the coarse targets (after the pass's coarse strengths, on the far stream)
+// FP32 far field with coarse targets: the listed and grid entries (after the pass's coarse strengths,
+// on the far stream); replaces launch_far_field for FP32 passes when the set has entries
+bool far_ct_on(const smob_ctx* c) { return !c->c32.ctent.empty(); }
 void far_ct(smob_ctx* c, bool trac, cudaStream_t st) {
-    if (c->c32.ctent.empty()) return;
-    ProfScope ps(c, "far_ct", st);
+    ProfScope ps(c, trac ? "far_trac_fp32" : "far_sl_fp32", st);
     check_launch(c, launch_far_ct(c->g, c->c32.d_ct_work.as<CtWork>(), (int)c->c32.ct_work.size(), trac,
                                   c->d_src32.as<float4>(), c->c32.d_ct_partial.as<float>(), st));
 }
@@ -1234,15 +1247,19 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
                 ProfScope ps(c, "far_coarse", fs);
                 check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
             }
-            if (fp32) far_ct(c, tr, fs);
-            ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"), fs);
-            if (fp32 && c->nrep > 1)
-                check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
-                                                     c->rep_M, tr, c->d_src32.as<float4>(), static_cast<float*>(partial),
-                                                     fs));
-            else
-                check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                 c->d_src64.as<double4_32a>(), partial, fs, c->tpt));
+            if (fp32 && far_ct_on(c)) {
+                far_ct(c, tr, fs);
+            } else {
+                ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"),
+                             fs);
+                if (fp32 && c->nrep > 1)
+                    check_launch(c, launch_far_field_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(),
+                                                         c->nrep, c->rep_M, tr, c->d_src32.as<float4>(),
+                                                         static_cast<float*>(partial), fs));
+                else
+                    check_launch(c, launch_far_field(g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                                     c->d_src64.as<double4_32a>(), partial, fs, c->tpt));
+            }
         }
         // sphere self and near field: main stream
         {
@@ -1275,7 +1292,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
         {
             ProfScope ps(c, "far_reduce");
             check_launch(c, launch_far_reduce(g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), out, c->st,
-                                              fp32 && !c->c32.ctent.empty() ? 1 : 0));
+                                              fp32 && far_ct_on(c) ? 1 : 0));
         }
     };
     if (trac) kind_pass(true, c_trac, true);
@@ -2269,13 +2286,16 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                         ProfScope ps(c, "far_coarse");
                         check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
                     }
-                    if (fp32) far_ct(c, tr, c->st);
-                    ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
-                    check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
-                                                     c->d_src64.as<double4_32a>(), partial, c->st, c->tpt));
+                    if (fp32 && far_ct_on(c)) {
+                        far_ct(c, tr, c->st);
+                    } else {
+                        ProfScope ps(c, fp32 ? (tr ? "far_trac_fp32" : "far_sl_fp32") : (tr ? "far_trac_fp64" : "far_sl_fp64"));
+                        check_launch(c, launch_far_field(c->g, items, nitems, tr, fp32, c->d_src32.as<float4>(),
+                                                         c->d_src64.as<double4_32a>(), partial, c->st, c->tpt));
+                    }
                 }
                 check_launch(c, launch_far_reduce(c->g, partial, fp32, tr ? -3.0 / (4 * kPi) : 1.0 / (8 * kPi), dout, c->st,
-                                                  fp32 && !c->c32.ctent.empty() ? 1 : 0));
+                                                  fp32 && far_ct_on(c) ? 1 : 0));
             }
         });
         prof_flush(c);
@@ -2436,7 +2456,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
     r->c32.eps = c->c32.eps;  // replicas share the levels; each column's coarse strengths are its own
-    r->c32.ctgt = c->c32.ctgt;  // coarse targets per replica (the replicas are problems of the copy)
+    r->c32.ctgt = false;      // the several-column kernels evaluate the grid targets of every far pair
     r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
@@ -2669,11 +2689,12 @@ smob_status smob_far_compression_info(const smob_ctx* c, int hp, double* eps, in
 smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* evaluated, long long* coarse_macs) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        // the FP32 kernels' choices replayed on the host for the current work items: a pair whose
-        // target sphere has a coarse-target level for it goes to the coarse targets (their nodes
-        // against the source's level for that target sphere, or its grid); on the grid targets a
-        // source sphere is skipped when every target skips it, read from its grid points when some
-        // target needs them, else from the finest coarse level any target votes for
+        // the FP32 kernels' choices replayed on the host for the current work items. With coarse
+        // targets, every entry's work items: a candidate counts if its pair takes the entry's level
+        // (coarse nodes or the grid points) and is read from the source's level for that target sphere
+        // or its grid. Without, the grid items: a source sphere is skipped when every target skips it,
+        // read from its grid points when some target needs them, else from the finest coarse level
+        // any target votes for.
         const smob_ctx::CoarseHost& h = c->c32;
         const double leps = h.eps > 0 ? std::log(h.eps) : 0.0;
         auto dist = [&](int t, int s) {
@@ -2713,41 +2734,48 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
             return -1;
         };
         long long dir = 0, ev = 0, macs = 0;
-        std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
-        for (const FarItem& it : c->items32) {
-            tsph.clear();
-            for (int t = it.t0; t < it.t1; ++t) {
-                const int ts = c->sid[t];
-                if (tsph.empty() || tsph.back().first != ts) tsph.push_back({ts, 0});
-                tsph.back().second++;
-            }
-            for (int s = it.s0; s < it.s1; ++s) {
-                int keep = 0, fine = 0, lvmax = -1;
-                for (auto& ts : tsph) {
-                    const int t = ts.first;
-                    if (near_pair(t, s)) continue;
-                    dir += (long long)ts.second * c->glen[s];
-                    if (tgt_lev(t, s) >= 0) continue;
-                    keep += ts.second;
-                    const int lv = src_level(t, s);
-                    if (lv < 0) fine = 1;
-                    else lvmax = std::max(lvmax, lv);
+        if (!h.ctent.empty()) {
+            for (const Problem& pr : c->problems)
+                for (int t = pr.s0; t < pr.s1; ++t)
+                    for (int s = pr.s0; s < pr.s1; ++s)
+                        if (!near_pair(t, s)) dir += (long long)c->glen[t] * c->glen[s];
+            // work items of the listed and grid entries: a candidate counts if its pair takes the entry's level
+            for (const CtWork& w : h.ct_work) {
+                const CtEnt& e = h.ctent[w.ent];
+                for (int i = w.sa; i < w.sb; ++i) {
+                    const int s = h.ctsrc[i];
+                    if (tgt_lev(e.t, s) != e.l) continue;
+                    const int lv = src_level(e.t, s);
+                    ev += (long long)w.nb * (lv < 0 ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lv].z);
                 }
-                if (keep == 0) continue;
-                ev += (long long)keep * (fine ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lvmax].z);
+            }
+            for (const CtEnt& e : h.ctent)
+                if (e.l >= 0) macs += 3LL * c->glen[e.t] * e.n;  // interpolation to the grid
+        } else {
+            std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
+            for (const FarItem& it : c->items32) {
+                tsph.clear();
+                for (int t = it.t0; t < it.t1; ++t) {
+                    const int ts = c->sid[t];
+                    if (tsph.empty() || tsph.back().first != ts) tsph.push_back({ts, 0});
+                    tsph.back().second++;
+                }
+                for (int s = it.s0; s < it.s1; ++s) {
+                    int keep = 0, fine = 0, lvmax = -1;
+                    for (auto& ts : tsph) {
+                        const int t = ts.first;
+                        if (near_pair(t, s)) continue;
+                        dir += (long long)ts.second * c->glen[s];
+                        keep += ts.second;
+                        const int lv = src_level(t, s);
+                        if (lv < 0) fine = 1;
+                        else lvmax = std::max(lvmax, lv);
+                    }
+                    if (keep == 0) continue;
+                    ev += (long long)keep * (fine ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lvmax].z);
+                }
             }
         }
-        // coarse-target work items: a candidate counts if its pair takes the entry's level
-        for (const CtWork& w : h.ct_work) {
-            const CtEnt& e = h.ctent[w.ent];
-            for (int i = w.sa; i < w.sb; ++i) {
-                const int s = h.ctsrc[i];
-                if (tgt_lev(e.t, s) != e.l) continue;
-                const int lv = src_level(e.t, s);
-                ev += (long long)w.nb * (lv < 0 ? c->glen[s] : h.clev[(size_t)s * kCoarseLevels + lv].z);
-            }
-        }
-        for (const CtEnt& e : h.ctent) macs += 3LL * c->glen[e.t] * e.n;  // interpolation to the grid
         for (const int2& e : h.cent) macs += 3LL * c->glen[e.x] * h.clev[(size_t)e.x * kCoarseLevels + e.y].z;
         if (direct) *direct = dir;
         if (evaluated) *evaluated = ev;

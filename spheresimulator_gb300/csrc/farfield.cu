@@ -692,10 +692,10 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
 }
 
 // ---------------------------------------------------------------- coarse targets (FP32)
-// One CTA per work item: nodes [k0, k0 + nb) of a listed entry (target sphere t, level l) against a
-// range of its candidate source spheres. A candidate counts only if tgt_level(t, s) == l (the rule
-// the grid kernels skip by, evaluated here on the same arguments; CTA-uniform), and is read from its
-// coarse level for t (level_bit: the nodes lie on t's surface) or its grid. The CTA's threads form
+// One CTA per work item: nodes [k0, k0 + nb) of an entry (target sphere t, level l, or its grid
+// points for l = -1) against a range of its candidate source spheres. A candidate counts only if
+// tgt_level(t, s) == l (CTA-uniform; the host lists boundary cases under both sides), and is read from
+// its coarse level for t (level_bit: the nodes lie on t's surface) or its grid. The CTA's threads form
 // 128 / w slices of w threads: thread (node, slice) takes every (128 / w)-th staged pair of source
 // points, so small entries keep every thread busy. A thread's target sits duplicated in both FP32x2
 // lanes and the sources are staged two to a pack, (x1,x2,y1,y2) (z1,z2,fx1,fx2) (fy1,fy2,fz1,fz2):
@@ -715,15 +715,16 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWor
     const int node = threadIdx.x % w.w, slice = threadIdx.x / w.w;
     const bool val = node < w.nb;
     const int cn = e.q0 + w.k0 + node;
+    const bool grid = e.l < 0;  // the sphere's grid points (CTA-uniform)
     // an empty slot sits 1e18 away: its terms are finite (and not written)
-    const float4 P = val ? cs.cpos32[cn] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
-    const float4 Nn = (TRAC && val) ? cs.cnrm32[cn] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 P = val ? (grid ? g.pos32[cn] : cs.cpos32[cn]) : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+    const float4 Nn = (TRAC && val) ? (grid ? g.nrm32[cn] : cs.cnrm32[cn]) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 TX = f2(P.x, P.x), TY = f2(P.y, P.y), TZ = f2(P.z, P.z);
     const float2 NX = f2(Nn.x, Nn.x), NY = f2(Nn.y, Nn.y), NZ = f2(Nn.z, Nn.z);
     float2 AX = f2(0.f, 0.f), AY = AX, AZ = AX;
     for (int i = w.sa; i < w.sb; ++i) {
         const int s = cs.ctsrc[i];
-        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of the neighbouring level
+        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of a neighbouring level
         const float4 *SP, *SF;
         int g0, gl;
         pick_sources(g, s, level_bit(g, cs, e.t, s), src, SP, SF, g0, gl);
@@ -764,7 +765,7 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWor
     }
 }
 
-// the chunks' sums of every listed entry's nodes, in fixed order, into ctu
+// the chunks' sums of every entry's nodes, in fixed order, into ctu (listed) or the grid slot (grid)
 __global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
     const CoarseSet& cs = g.cs32;
     const CtEnt e = cs.ctent[blockIdx.x];
@@ -777,7 +778,13 @@ __global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
             y += o[1];
             z += o[2];
         }
-        cs.ctu[e.q0 + k] = make_float4(x, y, z, 0.f);
+        if (e.l >= 0) cs.ctu[e.q0 + k] = make_float4(x, y, z, 0.f);
+        else {
+            float* o = cs.ctinterp + 3LL * ((long long)kCoarseLevels * g.M + e.q0 + k);
+            o[0] = x;
+            o[1] = y;
+            o[2] = z;
+        }
     }
 }
 
@@ -1268,18 +1275,23 @@ __global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double
     const long long mp = pr.p1 - pr.p0;
     const Real* base = partial + pr.poff + 3LL * (i - pr.p0);
     double sx = 0, sy = 0, sz = 0;
-    for (int c = 0; c < pr.nchunks; ++c) {
-        const Real* q = base + 3LL * mp * c;
-        sx += double(q[0]);
-        sy += double(q[1]);
-        sz += double(q[2]);
-    }
-    if (ct) {
-        // the listed coarse-target entries of the point's sphere, by level
+    if (!ct) {
+        for (int c = 0; c < pr.nchunks; ++c) {
+            const Real* q = base + 3LL * mp * c;
+            sx += double(q[0]);
+            sy += double(q[1]);
+            sz += double(q[2]);
+        }
+    } else {
+        // the grid entry's sums, then the listed coarse-target entries of the point's sphere by level
         const CoarseSet& cs = g.cs32;
+        const float* o = cs.ctinterp + 3LL * ((long long)kCoarseLevels * g.M + i);
+        sx = double(o[0]);
+        sy = double(o[1]);
+        sz = double(o[2]);
         for (int l = 0; l < kCoarseLevels; ++l) {
             if (!cs.ctused[sph * kCoarseLevels + l]) continue;
-            const float* o = cs.ctinterp + 3LL * ((long long)l * g.M + i);
+            o = cs.ctinterp + 3LL * ((long long)l * g.M + i);
             sx += double(o[0]);
             sy += double(o[1]);
             sz += double(o[2]);
@@ -1392,12 +1404,20 @@ int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double p
 
 int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
                   cudaStream_t st) {
-    if (nworks <= 0 || g.cs32.nctent <= 0) return 0;
-    if (trac) k_far32_ct<true><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
-    else k_far32_ct<false><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
+    if (g.cs32.nctent <= 0) return 0;
+    int n = 0;
+    if (nworks > 0) {  // entries without candidates have no items: their sums are zeros
+        if (trac) k_far32_ct<true><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
+        else k_far32_ct<false><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
+        ++n;
+    }
     k_ct_sum<<<g.cs32.nctent, 128, 0, st>>>(g, partial);
-    k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
-    return 3;
+    ++n;
+    if (g.cs32.nctitile > 0) {  // grid entries only: nothing to interpolate
+        k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
+        ++n;
+    }
+    return n;
 }
 
 }  // namespace smob

@@ -98,7 +98,8 @@ struct CoarseSet {
     const struct CtEnt* ctent; // listed entries: those with candidate source spheres
     const int* ctsrc;          // the entries' candidate source spheres
     float4* ctu;               // far field at the coarse targets of the current pass
-    float* ctinterp;           // interpolated to the grid, [level slot][M][3] (listed entries)
+    float* ctinterp;           // [kCoarseLevels + 1][M][3]: listed entries interpolated to the grid by
+                               // level slot, and the grid entries' sums
     int nctitile;              // interpolation tiles (CtITile) and their entry lists
     const struct CtITile* ctitile;
     const int* ctient;
@@ -111,7 +112,9 @@ constexpr int kCoarseTargetNum = 7, kCoarseTargetDen = 10;
 // A listed coarse-target entry (sphere t, level l): its nodes are the coarse points [q0, q0 + n) of
 // the set, its candidate sources ctsrc[src0, src0 + nsrc) (every s with tgt_level(t, s) == l and
 // neighbours of the level boundary; the kernels check the rule per pair); partial sums at poff as
-// [chunk][node][3].
+// [chunk][node][3]. A grid entry (l = -1, one per sphere) has the sphere's grid points [q0, q0 + n)
+// as nodes and the sources whose pair stays on the grid targets (tgt_level == -1) as candidates;
+// its sums go to slot kCoarseLevels of ctinterp.
 struct CtEnt {
     int t, l, q0, n;
     int src0, nsrc, nchunks, problem;
@@ -192,14 +195,14 @@ int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4_32a* src64, void* partial, cudaStream_t st, int tpt = 2);
-// ct: 0 no coarse targets, 1 the FP32 set's (ctu), 2 the float-float set's traction (ctud), 3 its
-// single layer (ctud_sl): the coarse-target values of every used entry are interpolated to the grid and
-// added with the chunks' sums
+// ct: 0 the chunks' sums of partial; 1 (FP32 with coarse targets) the grid entries' sums and the
+// listed entries' interpolated values from cs32.ctinterp instead (partial is not read)
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st,
                       int ct = 0);
-// FP32 far field at the coarse targets of the listed entries (after launch_coarse_src): the work items
-// into partial (CtEnt layout), their chunks summed into cs32.ctu, and the interpolation of every
-// listed entry to its sphere's grid into cs32.ctinterp (launch_far_reduce with ct = 1 adds it)
+// FP32 far field with coarse targets (after launch_coarse_src): the work items of the listed and the
+// grid entries into partial (CtEnt layout), their chunks summed into cs32.ctu (listed) and the grid
+// slot of cs32.ctinterp (grid entries), and the listed entries interpolated to their spheres' grids
+// into their level slots (launch_far_reduce with ct = 1 adds the slots)
 int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
                   cudaStream_t st);
 // coarse points of every (sphere, level) entry of a set, relative to the problem origins (after

@@ -256,7 +256,8 @@ def test_multi_rhs_equals_single_solves(k):
     """K right-hand sides solved together (shared-geometry FP32 far field) give bit for bit the
     solves of each column alone with the one-target-per-thread FP32 kernel, with and without coarse
     equivalent sources in the FP32 passes (the several-column float-float pass sums every grid-point
-    pair, so the single solves' float-float set is off here); the Tpetra-style apply with K columns
+    pair and the several-column FP32 kernel evaluates the grid targets of every far pair, so the single
+    solves' float-float set and coarse targets are off here); the Tpetra-style apply with K columns
     uses the same path."""
     rng = np.random.default_rng(19)
     radii = rng.uniform(0.8, 1.2, 12)
@@ -264,6 +265,7 @@ def test_multi_rhs_equals_single_solves(k):
     mob = make(cfg, SphereSTKMobMat)
     mob.set_far_tile(1)
     mob.set_far_compression(1e-7, 0)
+    mob.set_far_coarse_targets(False)
     assert mob.far_compression_info()[2] > 0
     F = np.random.default_rng(k).standard_normal((k, 6 * mob.n_spheres))
     for prec in (PREC_MIXED, PREC_FP64):
