@@ -219,12 +219,14 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * A tolerance <= 0 turns that set off (the direct sum). Setting the tolerances empties the recycled
  * solutions (smob_recycle_info) and drops the several-column copies of the context. */
 smob_status smob_set_far_compression(smob_ctx* ctx, double eps, double eps_hp);
-/* Coarse targets (on by default for the FP32 set): the target side of a well-separated pair
- * compressed the same way. The far field of the source sphere (its coarse or grid sources) is
- * evaluated at the nodes of a coarse order pt of the target sphere and interpolated to its grid with
- * the same reproducing kernel (exact for fields of degree <= pt on the sphere), pt chosen like pe with
- * the target radius and one order more (the target normal of the traction), and only where pt's grid
- * has at most 7/10 of the sphere's points. Same empties and drops as smob_set_far_compression. */
+/* Coarse targets (on by default): the target side of a well-separated pair compressed the same way.
+ * The far field of the source sphere (its coarse or grid sources) is evaluated at the nodes of a
+ * coarse order pt of the target sphere and interpolated to its grid with the same reproducing kernel
+ * (exact for fields of degree <= pt on the sphere), pt chosen like pe with the target radius and one
+ * order more (the target normal of the traction), and only where pt's grid has at most 7/10 of the
+ * sphere's points. Applies to the FP32 passes (tolerance eps) and to the MIXED solve's fused
+ * float-float pass (eps_hp); the several-column solves keep grid targets. Same empties and drops as
+ * smob_set_far_compression. */
 smob_status smob_set_far_coarse_targets(smob_ctx* ctx, int on);
 /* the tolerance, coarse points held and (sphere, level) entries of the FP32 set (hp = 0) or the
  * float-float set (hp = 1) */

@@ -201,8 +201,8 @@ struct smob_ctx {
         std::vector<CtITile> ctitile;
         std::vector<int> ctient;
         long long ct_partial = 0;
-        DBuf d_ctent, d_ctsrc, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32, d_ctu, d_ctitile,
-            d_ctient;
+        DBuf d_ctent, d_ctsrc, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32, d_cnrm32lo, d_ctu,
+            d_ctitile, d_ctient;
     };
     CoarseHost c32, chp;
     DBuf d_cnode, d_cnode_off, d_sph32;
@@ -211,6 +211,7 @@ struct smob_ctx {
         c32.ctgt = true;
         chp.eps = kCoarseEpsHpDefault;
         chp.hp = true;
+        chp.ctgt = true;
     }
     DBuf d_in, d_out, d_tmp;  // host-pointer API staging
     // solver workspace
@@ -757,7 +758,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.cent.clear();
     h.ncoarse = 0;
     std::vector<float> maps, mapsT;
-    std::vector<double> mapsd;
+    std::vector<double> mapsd, mapsTd;
     std::map<int, int> map_off;  // p * 64 + pe -> offset in the maps
     if (h.eps > 0) {
         const double leps = std::log(h.eps);
@@ -805,13 +806,17 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                     const int pe = pes[l];
                     const int key = ps * 64 + pe;
                     if (!map_off.count(key)) {
-                        // the map [fine j][coarse k] and (FP32 set) at the same offset its transpose
-                        // [k][j] (the coarse targets' interpolation)
+                        // the map [fine j][coarse k] and, at the same offset, its transpose [k][j]
+                        // (the coarse targets' interpolation)
                         const int ngf = (ps + 1) * (2 * ps + 2), nec = (pe + 1) * (2 * pe + 2);
                         if (h.hp) {
                             const std::vector<double>& m = coarse_map_d(ps, pe);
                             map_off[key] = (int)mapsd.size();
                             mapsd.insert(mapsd.end(), m.begin(), m.end());
+                            mapsTd.resize(mapsd.size());
+                            for (int j = 0; j < ngf; ++j)
+                                for (int k = 0; k < nec; ++k)
+                                    mapsTd[map_off[key] + (size_t)k * ngf + j] = m[(size_t)j * nec + k];
                         } else {
                             const std::vector<float>& m = coarse_map(ps, pe);
                             map_off[key] = (int)maps.size();
@@ -925,13 +930,14 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                 }
             }
             e.nchunks = (int)chunks.size();  // 0: no candidates, the sums are zeros
-            h.ct_partial += 3LL * e.n * e.nchunks;
+            h.ct_partial += (h.hp ? 6LL : 3LL) * e.n * e.nchunks;
             h.ctsrc.insert(h.ctsrc.end(), cand[slot].begin(), cand[slot].end());
             const int ei = (int)h.ctent.size();
             h.ctent.push_back(e);
             if (l >= 0) h.ctused[(size_t)t * kCoarseLevels + l] = 1;
             for (int k0 = 0, rem = e.n; rem > 0 && e.nchunks > 0;) {
-                const int w = rem > 96 ? 128 : (rem > 32 ? 64 : 32);
+                // float-float set: 64 nodes per CTA (two per thread of kFarThreadsDF)
+                const int w = h.hp ? 2 * kFarThreadsDF : (rem > 96 ? 128 : (rem > 32 ? 64 : 32));
                 const int nb = std::min(w, rem);
                 for (int ci = 0; ci < e.nchunks; ++ci) {
                     h.ct_work.push_back(CtWork{ei, k0, nb, w, chunks[ci].first, chunks[ci].second, ci, 0});
@@ -995,7 +1001,8 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
             const int ng = c->glen[e0.t], n = e0.n;
-            for (size_t a = 0; a < kv.second.size(); a += 8) {
+            const size_t per = h.hp ? 4 : 8;  // entries per tile (the kernels' kCiEntD / kCiEnt)
+            for (size_t a = 0; a < kv.second.size(); a += per) {
                 const int first = (int)h.ctient.size();
                 const int ne = (int)std::min<size_t>(8, kv.second.size() - a);
                 h.ctient.insert(h.ctient.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
@@ -1021,11 +1028,20 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         h.d_ct_work.upload(h.ct_work);
         h.d_ctitile.upload(h.ctitile);
         h.d_ctient.upload(h.ctient);
-        h.d_ct_partial.alloc(sizeof(float) * (size_t)h.ct_partial);
-        h.d_ctinterp.alloc(sizeof(float) * 3 * (size_t)(kCoarseLevels + 1) * (size_t)std::max(c->M, 1));
-        h.d_cmapT.upload(mapsT);
+        const size_t slots = (size_t)(kCoarseLevels + 1) * (size_t)std::max(c->M, 1);
         h.d_cnrm32.alloc(sizeof(float4) * np);
-        h.d_ctu.alloc(sizeof(float4) * np);
+        if (h.hp) {
+            h.d_ct_partial.alloc(sizeof(double) * (size_t)h.ct_partial);
+            h.d_ctinterp.alloc(sizeof(double) * 6 * slots);
+            h.d_cmapT.upload(mapsTd);
+            h.d_cnrm32lo.alloc(sizeof(float4) * np);
+            h.d_ctu.alloc(sizeof(double) * 6 * np);
+        } else {
+            h.d_ct_partial.alloc(sizeof(float) * (size_t)h.ct_partial);
+            h.d_ctinterp.alloc(sizeof(float) * 3 * slots);
+            h.d_cmapT.upload(mapsT);
+            h.d_ctu.alloc(sizeof(float4) * np);
+        }
     }
 }
 
@@ -1052,8 +1068,10 @@ void coarse_grids(smob_ctx* c) {
     check_launch(c, launch_coarse_grid(c->g, c->g.cs32, c->d_org.as<double>(), c->c32.d_cpos32.as<float4>(), nullptr,
                                        c->c32.ctent.empty() ? nullptr : c->c32.d_cnrm32.as<float4>(), nullptr,
                                        c->st));
+    const bool hpct = !c->chp.ctent.empty();
     check_launch(c, launch_coarse_grid(c->g, c->g.cshp, c->d_org.as<double>(), c->chp.d_cpos32.as<float4>(),
-                                       c->chp.d_cpos32lo.as<float4>(), nullptr, nullptr, c->st));
+                                       c->chp.d_cpos32lo.as<float4>(), hpct ? c->chp.d_cnrm32.as<float4>() : nullptr,
+                                       hpct ? c->chp.d_cnrm32lo.as<float4>() : nullptr, c->st));
 }
 
 void bind_geom(smob_ctx* c) {
@@ -1113,16 +1131,20 @@ void bind_geom(smob_ctx* c) {
         cs.ctgt = ct ? 1 : 0;
         cs.ctmargin = float(kCoarseTargetMargin);
         cs.cnrm32 = ct ? h.d_cnrm32.as<float4>() : nullptr;
-        cs.cmapT = ct ? h.d_cmapT.as<float>() : nullptr;
+        cs.cnrm32lo = ct && h.hp ? h.d_cnrm32lo.as<float4>() : nullptr;
+        cs.cmapT = ct && !h.hp ? h.d_cmapT.as<float>() : nullptr;
+        cs.cmapTd = ct && h.hp ? h.d_cmapT.as<double>() : nullptr;
         cs.ctused = ct ? h.d_ctused.as<int>() : nullptr;
         cs.nctent = ct ? (int)h.ctent.size() : 0;
         cs.ctent = ct ? h.d_ctent.as<CtEnt>() : nullptr;
         cs.ctsrc = ct ? h.d_ctsrc.as<int>() : nullptr;
-        cs.ctinterp = ct ? h.d_ctinterp.as<float>() : nullptr;
+        cs.ctinterp = ct && !h.hp ? h.d_ctinterp.as<float>() : nullptr;
+        cs.ctinterpd = ct && h.hp ? h.d_ctinterp.as<double>() : nullptr;
         cs.nctitile = ct ? (int)h.ctitile.size() : 0;
         cs.ctitile = ct ? h.d_ctitile.as<CtITile>() : nullptr;
         cs.ctient = ct ? h.d_ctient.as<int>() : nullptr;
-        cs.ctu = ct ? h.d_ctu.as<float4>() : nullptr;
+        cs.ctu = ct && !h.hp ? h.d_ctu.as<float4>() : nullptr;
+        cs.ctud = ct && h.hp ? h.d_ctu.as<double>() : nullptr;
     };
     bind_set(c->c32, g.cs32);
     bind_set(c->chp, g.cshp);
@@ -1202,6 +1224,13 @@ void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
 // operator precisions: every kernel in FP64; every kernel in FP32; or FP64 sphere and near
 // kernels with the far field in float-float (the high-precision operator of the mixed solve)
 enum OpPrec { OP_FP64 = 0, OP_FP32 = 1, OP_DF = 2 };
+
+// the fused float-float pass with the float-float set's coarse targets (after its coarse strengths)
+bool far_df_ct_on(const smob_ctx* c) { return c->nrep == 1 && !c->chp.ctent.empty(); }
+void far_df_ct(smob_ctx* c, cudaStream_t st) {
+    check_launch(c, launch_far_df_ct(c->g, c->chp.d_ct_work.as<CtWork>(), (int)c->chp.ct_work.size(),
+                                     c->d_srcdf.as<float4>(), c->chp.d_ct_partial.as<double>(), st));
+}
 
 // FP32 far field with coarse targets: the listed and grid entries (after the pass's coarse strengths,
 // on the far stream); replaces launch_far_field for FP32 passes when the set has entries
@@ -1318,12 +1347,15 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
         check_launch(c, launch_far_pack_df(g, x, 1.0, c->d_srcdf.as<float4>(), fs));
         if (c->nrep == 1) check_launch(c, launch_coarse_src_df(g, c->d_srcdf.as<float4>(), fs));
     }
+    const bool hpct = far_df_ct_on(c);
     {
         ProfScope ps(c, "far_both_df", fs);
         if (c->nrep > 1)
             check_launch(c, launch_far_field_df_rep(g, c->d_items_rep.as<FarItem>(), (int)c->items_rep.size(), c->nrep,
                                                     c->rep_M, c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
                                                     c->d_partial64_sl.as<double>(), fs));
+        else if (hpct)
+            far_df_ct(c, fs);
         else
             check_launch(c, launch_far_field_df(g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(), 2,
                                                 c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
@@ -1350,8 +1382,9 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
     }
     fork.join();
     ProfScope ps(c, "far_reduce");
-    check_launch(c, launch_far_reduce(g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), out_t, c->st));
-    check_launch(c, launch_far_reduce(g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), out_s, c->st));
+    check_launch(c, launch_far_reduce(g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), out_t, c->st,
+                                      hpct ? 2 : 0));
+    check_launch(c, launch_far_reduce(g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), out_s, c->st, hpct ? 3 : 0));
 }
 
 // ---------------------------------------------------------------- solver
@@ -2259,14 +2292,20 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                 c->d_partial64_sl.alloc(sizeof(double) * c->partial64);
                 check_launch(c, launch_far_pack_df(c->g, din, 1.0, c->d_srcdf.as<float4>(), c->st));
                 check_launch(c, launch_coarse_src_df(c->g, c->d_srcdf.as<float4>(), c->st));
+                const bool hpct = far_df_ct_on(c);
                 {
                     ProfScope ps(c, "far_both_df");
-                    check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(), 2,
-                                                        c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
-                                                        c->d_partial64_sl.as<double>(), c->st));
+                    if (hpct)
+                        far_df_ct(c, c->st);
+                    else
+                        check_launch(c, launch_far_field_df(c->g, c->d_items_df.as<FarItem>(), (int)c->items_df.size(),
+                                                            2, c->d_srcdf.as<float4>(), c->d_partial64.as<double>(),
+                                                            c->d_partial64_sl.as<double>(), c->st));
                 }
-                check_launch(c, launch_far_reduce(c->g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), dout, c->st));
-                check_launch(c, launch_far_reduce(c->g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), dout, c->st));
+                check_launch(c, launch_far_reduce(c->g, c->d_partial64.p, false, c_trac * (-3.0 / (4 * kPi)), dout, c->st,
+                                                  hpct ? 2 : 0));
+                check_launch(c, launch_far_reduce(c->g, c->d_partial64_sl.p, false, c_sl / (8 * kPi), dout, c->st,
+                                                  hpct ? 3 : 0));
                 return;
             }
             for (int k = 0; k < 2; ++k) {
@@ -2458,6 +2497,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     r->c32.eps = c->c32.eps;  // replicas share the levels; each column's coarse strengths are its own
     r->c32.ctgt = false;      // the several-column kernels evaluate the grid targets of every far pair
     r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
+    r->chp.ctgt = false;
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
@@ -2666,6 +2706,7 @@ smob_status smob_set_far_coarse_targets(smob_ctx* c, int on) {
         for (auto& kv : c->multi) smob_destroy(kv.second);
         c->multi.clear();
         c->c32.ctgt = on != 0;
+        c->chp.ctgt = on != 0;
         c->rk = 0;
         build_coarse(c);
         bind_geom(c);

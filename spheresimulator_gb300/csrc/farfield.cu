@@ -992,13 +992,68 @@ __device__ __forceinline__ void df_acc(T& ah, T& al, dfv<T> v) {
     al = v_add(al, v_add(s.l, v.l));
 }
 
+// packed float-float accumulators of two targets: traction (or the single layer for KIND 0) and, for
+// KIND 2, the single layer
+struct DfAcc {
+    float2 xh, xl, yh, yl, zh, zl;
+    float2 sxh, sxl, syh, syl, szh, szl;
+};
+
+// one source (qh + ql, strength fh + fl) against the two packed targets (mx, my, mz) with normals
+// (n0, n1, n2); masked: keep scales the source weight per lane
+template <int KIND>
+__device__ __forceinline__ void df_pair(const df2& mx, const df2& my, const df2& mz, const df2& n0, const df2& n1,
+                                        const df2& n2, const float4& qh, const float4& ql, const float4& fh,
+                                        const float4& fl, bool masked, float2 keep, DfAcc& a) {
+    constexpr bool TRAC = KIND != 0, SL = KIND != 1;
+    const df2 dx = two_sum(mx.h, f2(-qh.x, -qh.x));
+    const df2 dy = two_sum(my.h, f2(-qh.y, -qh.y));
+    const df2 dz = two_sum(mz.h, f2(-qh.z, -qh.z));
+    const df2 rx{dx.h, __fadd2_rn(dx.l, __fadd2_rn(mx.l, f2(-ql.x, -ql.x)))};
+    const df2 ry{dy.h, __fadd2_rn(dy.l, __fadd2_rn(my.l, f2(-ql.y, -ql.y)))};
+    const df2 rz{dz.h, __fadd2_rn(dz.l, __fadd2_rn(mz.l, f2(-ql.z, -ql.z)))};
+    df2 f0{f2(fh.x, fh.x), f2(fl.x, fl.x)}, f1{f2(fh.y, fh.y), f2(fl.y, fl.y)}, fz{f2(fh.z, fh.z), f2(fl.z, fl.z)};
+    if (masked) {
+        f0 = {__fmul2_rn(f0.h, keep), __fmul2_rn(f0.l, keep)};
+        f1 = {__fmul2_rn(f1.h, keep), __fmul2_rn(f1.l, keep)};
+        fz = {__fmul2_rn(fz.h, keep), __fmul2_rn(fz.l, keep)};
+    }
+    const df2 r2 = df_sqr3(rx, ry, rz);
+    const df2 ri = df_rsqrt(r2);
+    const df2 rf = df_dot3(rx, f0, ry, f1, rz, fz);
+    const df2 ri2 = df_mul_u(ri, ri);
+    const df2 ri3 = df_mul_u(ri2, ri);
+    if (TRAC) {  // (r.f)(r.n) r / r^5
+        const df2 rn = df_dot3(rx, n0, ry, n1, rz, n2);
+        const df2 k5 = df_mul_u(df_mul_u(rf, rn), df_mul_u(ri3, ri2));
+        df_acc(a.xh, a.xl, df_mul_u(k5, rx));
+        df_acc(a.yh, a.yl, df_mul_u(k5, ry));
+        df_acc(a.zh, a.zl, df_mul_u(k5, rz));
+    }
+    if (SL) {  // f / r + (r.f) r / r^3
+        const df2 k3 = df_mul_u(rf, ri3);
+        float2& ah = KIND == 2 ? a.sxh : a.xh;
+        float2& al = KIND == 2 ? a.sxl : a.xl;
+        float2& bh = KIND == 2 ? a.syh : a.yh;
+        float2& bl = KIND == 2 ? a.syl : a.yl;
+        float2& ch = KIND == 2 ? a.szh : a.zh;
+        float2& cl = KIND == 2 ? a.szl : a.zl;
+        df_acc(ah, al, df_mul_u(f0, ri));
+        df_acc(ah, al, df_mul_u(k3, rx));
+        df_acc(bh, bl, df_mul_u(f1, ri));
+        df_acc(bh, bl, df_mul_u(k3, ry));
+        df_acc(ch, cl, df_mul_u(fz, ri));
+        df_acc(ch, cl, df_mul_u(k3, rz));
+    }
+}
+
 // KIND: 0 single layer -> partial; 1 traction -> partial; 2 both from the same sources in one pass
 // (traction -> partial, single layer -> partial_sl), sharing r, 1/r and r.f between the two kernels.
 template <int KIND>
 __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     k_far_dfx2(DevGeom g, const FarItem* __restrict__ items, const float4* __restrict__ src,
                double* __restrict__ partial, double* __restrict__ partial_sl) {
-    constexpr bool TRAC = KIND != 0, SL = KIND != 1;
+    constexpr bool TRAC = KIND != 0;
     constexpr int NT = kFarThreadsDF;
     const FarItem it = items[blockIdx.x];
     if (g.active && !g.active[it.problem]) return;
@@ -1023,51 +1078,13 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
         tz{f2(PH[0].z, PH[1].z), f2(PL[0].z, PL[1].z)};
     const df2 n0{f2(NH[0].x, NH[1].x), f2(NL[0].x, NL[1].x)}, n1{f2(NH[0].y, NH[1].y), f2(NL[0].y, NL[1].y)},
         n2{f2(NH[0].z, NH[1].z), f2(NL[0].z, NL[1].z)};
-    float2 xh = f2(0.f, 0.f), xl = xh, yh = xh, yl = xh, zh = xh, zl = xh;     // traction, or SL for KIND 0
-    float2 sxh = xh, sxl = xh, syh = xh, syl = xh, szh = xh, szl = xh;          // single layer for KIND 2
+    DfAcc acc;
+    acc.xh = acc.xl = acc.yh = acc.yl = acc.zh = acc.zl = f2(0.f, 0.f);
+    acc.sxh = acc.sxl = acc.syh = acc.syl = acc.szh = acc.szl = f2(0.f, 0.f);
     __shared__ unsigned votes_buf[2][NT / 32];
-    // one source against the two packed targets (mx, my, mz); keep scales the source weight per lane
     auto pair = [&](const df2& mx, const df2& my, const df2& mz, const float4& qh, const float4& ql,
                     const float4& fh, const float4& fl, bool masked, float2 keep) {
-        const df2 dx = two_sum(mx.h, f2(-qh.x, -qh.x));
-        const df2 dy = two_sum(my.h, f2(-qh.y, -qh.y));
-        const df2 dz = two_sum(mz.h, f2(-qh.z, -qh.z));
-        const df2 rx{dx.h, __fadd2_rn(dx.l, __fadd2_rn(mx.l, f2(-ql.x, -ql.x)))};
-        const df2 ry{dy.h, __fadd2_rn(dy.l, __fadd2_rn(my.l, f2(-ql.y, -ql.y)))};
-        const df2 rz{dz.h, __fadd2_rn(dz.l, __fadd2_rn(mz.l, f2(-ql.z, -ql.z)))};
-        df2 f0{f2(fh.x, fh.x), f2(fl.x, fl.x)}, f1{f2(fh.y, fh.y), f2(fl.y, fl.y)}, fz{f2(fh.z, fh.z), f2(fl.z, fl.z)};
-        if (masked) {
-            f0 = {__fmul2_rn(f0.h, keep), __fmul2_rn(f0.l, keep)};
-            f1 = {__fmul2_rn(f1.h, keep), __fmul2_rn(f1.l, keep)};
-            fz = {__fmul2_rn(fz.h, keep), __fmul2_rn(fz.l, keep)};
-        }
-        const df2 r2 = df_sqr3(rx, ry, rz);
-        const df2 ri = df_rsqrt(r2);
-        const df2 rf = df_dot3(rx, f0, ry, f1, rz, fz);
-        const df2 ri2 = df_mul_u(ri, ri);
-        const df2 ri3 = df_mul_u(ri2, ri);
-        if (TRAC) {  // (r.f)(r.n) r / r^5
-            const df2 rn = df_dot3(rx, n0, ry, n1, rz, n2);
-            const df2 k5 = df_mul_u(df_mul_u(rf, rn), df_mul_u(ri3, ri2));
-            df_acc(xh, xl, df_mul_u(k5, rx));
-            df_acc(yh, yl, df_mul_u(k5, ry));
-            df_acc(zh, zl, df_mul_u(k5, rz));
-        }
-        if (SL) {  // f / r + (r.f) r / r^3
-            const df2 k3 = df_mul_u(rf, ri3);
-            float2& ah = KIND == 2 ? sxh : xh;
-            float2& al = KIND == 2 ? sxl : xl;
-            float2& bh = KIND == 2 ? syh : yh;
-            float2& bl = KIND == 2 ? syl : yl;
-            float2& ch = KIND == 2 ? szh : zh;
-            float2& cl = KIND == 2 ? szl : zl;
-            df_acc(ah, al, df_mul_u(f0, ri));
-            df_acc(ah, al, df_mul_u(k3, rx));
-            df_acc(bh, bl, df_mul_u(f1, ri));
-            df_acc(bh, bl, df_mul_u(k3, ry));
-            df_acc(ch, cl, df_mul_u(fz, ri));
-            df_acc(ch, cl, df_mul_u(k3, rz));
-        }
+        df_pair<KIND>(mx, my, mz, n0, n1, n2, qh, ql, fh, fl, masked, keep, acc);
     };
     int parity = 0;
     for (int s = it.s0; s < it.s1; ++s, parity ^= 1) {
@@ -1124,15 +1141,170 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
         if (!val[h]) continue;
         const long long off = pr.poff + 3LL * mp * it.chunk + 3LL * (it.t0 + threadIdx.x + h * NT - pr.p0);
         double* o = partial + off;
-        o[0] = h ? double(xh.y) + double(xl.y) : double(xh.x) + double(xl.x);
-        o[1] = h ? double(yh.y) + double(yl.y) : double(yh.x) + double(yl.x);
-        o[2] = h ? double(zh.y) + double(zl.y) : double(zh.x) + double(zl.x);
+        o[0] = h ? double(acc.xh.y) + double(acc.xl.y) : double(acc.xh.x) + double(acc.xl.x);
+        o[1] = h ? double(acc.yh.y) + double(acc.yl.y) : double(acc.yh.x) + double(acc.yl.x);
+        o[2] = h ? double(acc.zh.y) + double(acc.zl.y) : double(acc.zh.x) + double(acc.zl.x);
         if (KIND == 2) {
             double* q = partial_sl + off;
-            q[0] = h ? double(sxh.y) + double(sxl.y) : double(sxh.x) + double(sxl.x);
-            q[1] = h ? double(syh.y) + double(syl.y) : double(syh.x) + double(syl.x);
-            q[2] = h ? double(szh.y) + double(szl.y) : double(szh.x) + double(szl.x);
+            q[0] = h ? double(acc.sxh.y) + double(acc.sxl.y) : double(acc.sxh.x) + double(acc.sxl.x);
+            q[1] = h ? double(acc.syh.y) + double(acc.syl.y) : double(acc.syh.x) + double(acc.syl.x);
+            q[2] = h ? double(acc.szh.y) + double(acc.szl.y) : double(acc.szh.x) + double(acc.szl.x);
         }
+    }
+}
+
+// The fused float-float pass with the float-float set's coarse targets: one CTA of kFarThreadsDF
+// threads per work item, nodes [k0, k0 + 64) of an entry (coarse nodes of level l, or the sphere's
+// grid points for l = -1), two per thread as the packed lanes of df_pair, against the entry's
+// candidates; a candidate counts only if tgt_level(t, s) == l (CTA-uniform) and is read from its
+// float-float coarse level for t or its grid. Partial sums [chunk][node][6] (traction, single layer).
+__global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
+    k_far_df_ct(DevGeom g, const CtWork* __restrict__ works, const float4* __restrict__ src,
+                double* __restrict__ partial) {
+    constexpr int NT = kFarThreadsDF;
+    const CtWork w = works[blockIdx.x];
+    const CoarseSet& cs = g.cshp;
+    const CtEnt e = cs.ctent[w.ent];
+    if (g.active && !g.active[e.problem]) return;
+    __shared__ float4 sph[kFarTile], spl[kFarTile], sfh[kFarTile], sfl[kFarTile];
+    const bool grid = e.l < 0;  // CTA-uniform
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 PH[2], PL[2], NH[2], NL[2];
+    bool val[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int node = threadIdx.x + h * NT;
+        val[h] = node < w.nb;
+        const int cn = e.q0 + w.k0 + node;
+        // an empty slot sits 1e18 away: its terms are finite (and not written)
+        PH[h] = val[h] ? (grid ? g.pos32[cn] : cs.cpos32[cn]) : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        PL[h] = val[h] ? (grid ? g.pos32lo[cn] : cs.cpos32lo[cn]) : z4;
+        NH[h] = val[h] ? (grid ? g.nrm32[cn] : cs.cnrm32[cn]) : z4;
+        NL[h] = val[h] ? (grid ? g.nrm32lo[cn] : cs.cnrm32lo[cn]) : z4;
+    }
+    const df2 tx{f2(PH[0].x, PH[1].x), f2(PL[0].x, PL[1].x)}, ty{f2(PH[0].y, PH[1].y), f2(PL[0].y, PL[1].y)},
+        tz{f2(PH[0].z, PH[1].z), f2(PL[0].z, PL[1].z)};
+    const df2 n0{f2(NH[0].x, NH[1].x), f2(NL[0].x, NL[1].x)}, n1{f2(NH[0].y, NH[1].y), f2(NL[0].y, NL[1].y)},
+        n2{f2(NH[0].z, NH[1].z), f2(NL[0].z, NL[1].z)};
+    DfAcc acc;
+    acc.xh = acc.xl = acc.yh = acc.yl = acc.zh = acc.zl = f2(0.f, 0.f);
+    acc.sxh = acc.sxl = acc.syh = acc.syl = acc.szh = acc.szl = f2(0.f, 0.f);
+    const float2 one = f2(1.f, 1.f);
+    for (int i = w.sa; i < w.sb; ++i) {
+        const int s = cs.ctsrc[i];
+        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of a neighbouring level
+        const unsigned b = level_bit(g, cs, e.t, s);
+        const float4 *QH = g.pos32, *QL = g.pos32lo, *QF = src;
+        int g0 = g.gidx[s], gl = g.glen[s];
+        if (!(b & kBitFine)) {
+            const int4 L = cs.clev[s * kCoarseLevels + (31 - __clz(b))];
+            QH = cs.cpos32;
+            QL = cs.cpos32lo;
+            QF = cs.csrc;
+            g0 = L.y;
+            gl = L.z;
+        }
+        for (int base = 0; base < gl; base += kFarTile) {
+            const int n = min(kFarTile, gl - base);
+            __syncthreads();
+            for (int k = threadIdx.x; k < n; k += NT) {
+                sph[k] = QH[g0 + base + k];
+                spl[k] = QL[g0 + base + k];
+                sfh[k] = QF[2 * (g0 + base + k)];
+                sfl[k] = QF[2 * (g0 + base + k) + 1];
+            }
+            __syncthreads();
+            for (int k = 0; k < n; ++k) df_pair<2>(tx, ty, tz, n0, n1, n2, sph[k], spl[k], sfh[k], sfl[k], false, one, acc);
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (!val[h]) continue;
+        double* o = partial + e.poff + 6LL * ((long long)w.chunk * e.n + w.k0 + threadIdx.x + h * NT);
+        o[0] = h ? double(acc.xh.y) + double(acc.xl.y) : double(acc.xh.x) + double(acc.xl.x);
+        o[1] = h ? double(acc.yh.y) + double(acc.yl.y) : double(acc.yh.x) + double(acc.yl.x);
+        o[2] = h ? double(acc.zh.y) + double(acc.zl.y) : double(acc.zh.x) + double(acc.zl.x);
+        o[3] = h ? double(acc.sxh.y) + double(acc.sxl.y) : double(acc.sxh.x) + double(acc.sxl.x);
+        o[4] = h ? double(acc.syh.y) + double(acc.syl.y) : double(acc.syh.x) + double(acc.syl.x);
+        o[5] = h ? double(acc.szh.y) + double(acc.szl.y) : double(acc.szh.x) + double(acc.szl.x);
+    }
+}
+
+// the chunks' sums of every float-float entry's nodes, in fixed order, into ctud (listed) or the grid
+// slot of ctinterpd (grid entries)
+__global__ void k_ct_sum_df(DevGeom g, const double* __restrict__ partial) {
+    const CoarseSet& cs = g.cshp;
+    const CtEnt e = cs.ctent[blockIdx.x];
+    if (g.active && !g.active[e.problem]) return;
+    for (int k = threadIdx.x; k < e.n; k += blockDim.x) {
+        double v[6] = {0, 0, 0, 0, 0, 0};
+        for (int c = 0; c < e.nchunks; ++c) {
+            const double* o = partial + e.poff + 6LL * ((long long)c * e.n + k);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) v[q] += o[q];
+        }
+        double* d = e.l >= 0 ? cs.ctud + 6LL * (e.q0 + k) : cs.ctinterpd + 6LL * ((long long)kCoarseLevels * g.M + e.q0 + k);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) d[q] = v[q];
+    }
+}
+
+// The float-float set's interpolation in FP64 (k_ct_interp's tiling with 4 entries x 6 components per
+// grid point; the map column batched in registers, the entries' node values staged in shared memory).
+constexpr int kCiEntD = 4, kCiKD = 16;
+__global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
+    const CoarseSet& cs = g.cshp;
+    const CtITile d = cs.ctitile[blockIdx.x];
+    __shared__ double U[kCiKD][kCiEntD][6];
+    __shared__ int eq0[kCiEntD], eon[kCiEntD];
+    __shared__ long long ebase[kCiEntD];
+    if (threadIdx.x < kCiEntD) {
+        const int e = threadIdx.x;
+        eon[e] = 0;
+        eq0[e] = 0;
+        ebase[e] = 0;
+        if (e < d.ne) {
+            const CtEnt en = cs.ctent[cs.ctient[d.e0 + e]];
+            eon[e] = !g.active || g.active[en.problem];
+            eq0[e] = en.q0;
+            ebase[e] = (long long)en.l * g.M + g.gidx[en.t];
+        }
+    }
+    __syncthreads();
+    const int j = d.j0 + threadIdx.x;
+    const bool val = j < d.ng;
+    const double* MT = cs.cmapTd + d.mapoff + (val ? j : 0);
+    double acc[kCiEntD][6];
+#pragma unroll
+    for (int e = 0; e < kCiEntD; ++e)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc[e][q] = 0.0;
+    for (int k0 = 0; k0 < d.n; k0 += kCiKD) {
+        const int nk = min(kCiKD, d.n - k0);
+        double mk[kCiKD];
+#pragma unroll
+        for (int kk = 0; kk < kCiKD; ++kk) mk[kk] = (val && kk < nk) ? __ldg(MT + (long long)(k0 + kk) * d.ng) : 0.0;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kCiKD * kCiEntD * 6; idx += 128) {
+            const int q = idx % 6, e = (idx / 6) % kCiEntD, kk = idx / (6 * kCiEntD);
+            U[kk][e][q] = (kk < nk && eon[e]) ? cs.ctud[6LL * (eq0[e] + k0 + kk) + q] : 0.0;
+        }
+        __syncthreads();
+        // rows past nk hold zeros in both operands
+#pragma unroll
+        for (int kk = 0; kk < kCiKD; ++kk)
+#pragma unroll
+            for (int e = 0; e < kCiEntD; ++e)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc[e][q] = fma(mk[kk], U[kk][e][q], acc[e][q]);
+    }
+    if (!val) return;
+#pragma unroll
+    for (int e = 0; e < kCiEntD; ++e) {
+        if (e >= d.ne || !eon[e]) continue;
+        double* o = cs.ctinterpd + 6LL * (ebase[e] + j);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) o[q] = acc[e][q];
     }
 }
 
@@ -1282,7 +1454,7 @@ __global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double
             sy += double(q[1]);
             sz += double(q[2]);
         }
-    } else {
+    } else if (ct == 1) {
         // the grid entry's sums, then the listed coarse-target entries of the point's sphere by level
         const CoarseSet& cs = g.cs32;
         const float* o = cs.ctinterp + 3LL * ((long long)kCoarseLevels * g.M + i);
@@ -1295,6 +1467,21 @@ __global__ void k_far_reduce(DevGeom g, const Real* __restrict__ partial, double
             sx += double(o[0]);
             sy += double(o[1]);
             sz += double(o[2]);
+        }
+    } else {
+        // the float-float set's slots: traction (ct 2) or single layer (ct 3) components
+        const CoarseSet& cs = g.cshp;
+        const int q = ct == 2 ? 0 : 3;
+        const double* o = cs.ctinterpd + 6LL * ((long long)kCoarseLevels * g.M + i) + q;
+        sx = o[0];
+        sy = o[1];
+        sz = o[2];
+        for (int l = 0; l < kCoarseLevels; ++l) {
+            if (!cs.ctused[sph * kCoarseLevels + l]) continue;
+            o = cs.ctinterpd + 6LL * ((long long)l * g.M + i) + q;
+            sx += o[0];
+            sy += o[1];
+            sz += o[2];
         }
     }
     out[3 * i] += pre * sx;
@@ -1392,6 +1579,23 @@ int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int 
     else if (kind == 1) k_far_dfx2<1><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
     else k_far_dfx2<0><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
     return 1;
+}
+
+int launch_far_df_ct(const DevGeom& g, const CtWork* works, int nworks, const float4* src2, double* partial,
+                     cudaStream_t st) {
+    if (g.cshp.nctent <= 0) return 0;
+    int n = 0;
+    if (nworks > 0) {
+        k_far_df_ct<<<nworks, kFarThreadsDF, 0, st>>>(g, works, src2, partial);
+        ++n;
+    }
+    k_ct_sum_df<<<g.cshp.nctent, 128, 0, st>>>(g, partial);
+    ++n;
+    if (g.cshp.nctitile > 0) {
+        k_ct_interp_df<<<g.cshp.nctitile, 128, 0, st>>>(g);
+        ++n;
+    }
+    return n;
 }
 
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st,

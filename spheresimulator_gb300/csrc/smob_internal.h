@@ -84,22 +84,27 @@ struct CoarseSet {
     const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
     const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
     const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
-    // Coarse targets (FP32 set): a target sphere t takes the far field of a well-separated source
-    // sphere s at the nodes of one of its own coarse levels and interpolates it to its grid (the
-    // transposed map); level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s))
-    // + ctmargin, if it has at most kCoarseTargetNum / kCoarseTargetDen of the sphere's grid points
-    // (else the pair stays on the grid targets).
+    // Coarse targets: a target sphere t takes the far field of a well-separated source sphere s at the
+    // nodes of one of its own coarse levels and interpolates it to its grid (the transposed map);
+    // level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s)) + ctmargin, if
+    // it has at most kCoarseTargetNum / kCoarseTargetDen of the sphere's grid points (else the pair
+    // stays on the grid targets). FP32 set: FP32 passes; float-float set: the fused float-float pass
+    // (traction and single layer).
     int ctgt;                  // 1: coarse targets on
     float ctmargin;
-    const float4* cnrm32;      // coarse node normals, w = level index bits
-    const float* cmapT;        // the maps transposed, [coarse node][fine node], at the maps' offsets
+    const float4* cnrm32;      // coarse node normals, w = level index bits (float-float set: high parts)
+    const float4* cnrm32lo;    // float-float set: the normals' low parts
+    const float* cmapT;        // FP32 set: the maps transposed, [coarse node][fine node], at the maps' offsets
+    const double* cmapTd;      // float-float set: the same in FP64
     const int* ctused;         // [N][kCoarseLevels]: the entry is a listed coarse-target entry (CtEnt)
     int nctent;
-    const struct CtEnt* ctent; // listed entries: those with candidate source spheres
+    const struct CtEnt* ctent; // listed and grid entries
     const int* ctsrc;          // the entries' candidate source spheres
-    float4* ctu;               // far field at the coarse targets of the current pass
-    float* ctinterp;           // [kCoarseLevels + 1][M][3]: listed entries interpolated to the grid by
-                               // level slot, and the grid entries' sums
+    float4* ctu;               // FP32 set: far field at the coarse targets of the current pass
+    float* ctinterp;           // FP32 set: [kCoarseLevels + 1][M][3]: listed entries interpolated to the
+                               // grid by level slot, and the grid entries' sums
+    double* ctud;              // float-float set: traction and single layer at the coarse targets [6]
+    double* ctinterpd;         // float-float set: as ctinterp with [6] per point
     int nctitile;              // interpolation tiles (CtITile) and their entry lists
     const struct CtITile* ctitile;
     const int* ctient;
@@ -123,14 +128,15 @@ struct CtEnt {
 };
 
 // one coarse-target work item: nodes [k0, k0 + nb) of entry ent with w threads per slice (32, 64 or
-// 128; 128 / w slices share the sources) against candidates [sa, sb) of the entry, partial chunk
+// 128; 128 / w slices share the sources; float-float set: 64 nodes, two per thread) against candidates
+// [sa, sb) of the entry, partial chunk
 struct CtWork {
     int ent, k0, nb, w;
     int sa, sb, chunk, pad;
 };
 
-// one interpolation tile: grid points [j0, j0 + 128) of up to 8 listed entries sharing one map
-// (order p, level pe): entries ctient[e0, e0 + ne), map at mapoff ([n][ng])
+// one interpolation tile: grid points [j0, j0 + 128) of up to 8 (float-float set: 4) listed entries
+// sharing one map (order p, level pe): entries ctient[e0, e0 + ne), map at mapoff ([n][ng])
 struct CtITile {
     int mapoff, ng, n, e0;
     int ne, j0, pad0, pad1;
@@ -196,7 +202,8 @@ int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 int launch_far_field(const DevGeom& g, const FarItem* items, int nitems, bool trac, bool fp32, const float4* src32,
                      const double4_32a* src64, void* partial, cudaStream_t st, int tpt = 2);
 // ct: 0 the chunks' sums of partial; 1 (FP32 with coarse targets) the grid entries' sums and the
-// listed entries' interpolated values from cs32.ctinterp instead (partial is not read)
+// listed entries' interpolated values from cs32.ctinterp instead (partial is not read); 2 / 3 the same
+// from cshp.ctinterpd, traction / single layer (the fused float-float pass)
 int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double pre, double* out, cudaStream_t st,
                       int ct = 0);
 // FP32 far field with coarse targets (after launch_coarse_src): the work items of the listed and the
@@ -205,6 +212,11 @@ int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double p
 // into their level slots (launch_far_reduce with ct = 1 adds the slots)
 int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
                   cudaStream_t st);
+// the fused float-float pass (traction and single layer) with the float-float set's coarse targets
+// (after launch_coarse_src_df): as launch_far_ct, into cshp.ctud / ctinterpd (launch_far_reduce with
+// ct = 2 and 3 adds the slots)
+int launch_far_df_ct(const DevGeom& g, const CtWork* works, int nworks, const float4* src2, double* partial,
+                     cudaStream_t st);
 // coarse points of every (sphere, level) entry of a set, relative to the problem origins (after
 // launch_regrid); cpos32lo (may be null) receives the low parts
 int launch_coarse_grid(const DevGeom& g, const CoarseSet& cs, const double* org, float4* cpos32, float4* cpos32lo,

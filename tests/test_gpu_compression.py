@@ -196,3 +196,21 @@ def test_coarse_targets_in_batches_and_mixed_solves():
     assert np.array_equal(alone.solveMob(F[:96], tol=1e-10, precision=PREC_MIXED), v[:96])
     g.set_far_coarse_targets(False)
     assert _rel(g.solveMob(F, tol=1e-10, precision=PREC_MIXED), v) < 1e-9
+
+
+def test_float_float_coarse_targets():
+    """The fused float-float pass with coarse targets (its 1e-10 set): against the same pass with grid
+    targets and the FP64 sum, and a mixed solve against the FP64 solve."""
+    c = _spread(seed=35, n=16, p=16, box=60.0)
+    g = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    x = np.random.default_rng(35).standard_normal(3 * g.n_points)
+    fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
+    on = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
+    F = np.random.default_rng(36).standard_normal(6 * 16)
+    v_on = g.solveMob(F, tol=1e-10, precision=PREC_MIXED)
+    assert g.last_stats[0]["status"] == 0
+    g.set_far_coarse_targets(False)
+    off = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
+    assert _rel(off, fp64) < 1e-10 and _rel(on, fp64) < 1e-10 and _rel(on, off) < 1e-10
+    ref = g.solveMob(F, tol=1e-12, precision=PREC_FP64)
+    assert _rel(v_on, ref) < 1e-9
