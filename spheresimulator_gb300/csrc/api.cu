@@ -201,8 +201,8 @@ struct smob_ctx {
         std::vector<CtITile> ctitile;
         std::vector<int> ctient;
         long long ct_partial = 0;
-        DBuf d_ctent, d_ctsrc, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32, d_cnrm32lo, d_ctu,
-            d_ctitile, d_ctient;
+        DBuf d_ctent, d_ctsrc, d_ctcand, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32,
+            d_cnrm32lo, d_ctu, d_ctitile, d_ctient;
     };
     CoarseHost c32, chp;
     DBuf d_cnode, d_cnode_off, d_sph32;
@@ -1024,6 +1024,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     if (!h.ctent.empty()) {
         h.d_ctent.upload(h.ctent);
         h.d_ctsrc.upload(h.ctsrc);
+        h.d_ctcand.alloc(sizeof(int2) * std::max<size_t>(h.ctsrc.size(), 1));
         h.d_ctused.upload(h.ctused);
         h.d_ct_work.upload(h.ct_work);
         h.d_ctitile.upload(h.ctitile);
@@ -1072,6 +1073,9 @@ void coarse_grids(smob_ctx* c) {
     check_launch(c, launch_coarse_grid(c->g, c->g.cshp, c->d_org.as<double>(), c->chp.d_cpos32.as<float4>(),
                                        c->chp.d_cpos32lo.as<float4>(), hpct ? c->chp.d_cnrm32.as<float4>() : nullptr,
                                        hpct ? c->chp.d_cnrm32lo.as<float4>() : nullptr, c->st));
+    // the coarse-target candidates of this geometry
+    check_launch(c, launch_ct_classify(c->g, c->g.cs32, c->st));
+    check_launch(c, launch_ct_classify(c->g, c->g.cshp, c->st));
 }
 
 void bind_geom(smob_ctx* c) {
@@ -1138,6 +1142,7 @@ void bind_geom(smob_ctx* c) {
         cs.nctent = ct ? (int)h.ctent.size() : 0;
         cs.ctent = ct ? h.d_ctent.as<CtEnt>() : nullptr;
         cs.ctsrc = ct ? h.d_ctsrc.as<int>() : nullptr;
+        cs.ctcand = ct ? h.d_ctcand.as<int2>() : nullptr;
         cs.ctinterp = ct && !h.hp ? h.d_ctinterp.as<float>() : nullptr;
         cs.ctinterpd = ct && h.hp ? h.d_ctinterp.as<double>() : nullptr;
         cs.nctitile = ct ? (int)h.ctitile.size() : 0;

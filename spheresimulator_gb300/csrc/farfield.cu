@@ -693,9 +693,9 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
 
 // ---------------------------------------------------------------- coarse targets (FP32)
 // One CTA per work item: nodes [k0, k0 + nb) of an entry (target sphere t, level l, or its grid
-// points for l = -1) against a range of its candidate source spheres. A candidate counts only if
-// tgt_level(t, s) == l (CTA-uniform; the host lists boundary cases under both sides), and is read from
-// its coarse level for t (level_bit: the nodes lie on t's surface) or its grid. The CTA's threads form
+// points for l = -1) against a range of its candidate source spheres, each resolved per geometry
+// (k_ct_classify: counted only if tgt_level(t, s) == l, the host listing boundary cases under both
+// levels; read from its coarse level for t, the nodes lying on t's surface, or its grid). The CTA's threads form
 // 128 / w slices of w threads: thread (node, slice) takes every (128 / w)-th staged pair of source
 // points, so small entries keep every thread busy. A thread's target sits duplicated in both FP32x2
 // lanes and the sources are staged two to a pack, (x1,x2,y1,y2) (z1,z2,fx1,fx2) (fy1,fy2,fz1,fz2):
@@ -723,11 +723,12 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWor
     const float2 NX = f2(Nn.x, Nn.x), NY = f2(Nn.y, Nn.y), NZ = f2(Nn.z, Nn.z);
     float2 AX = f2(0.f, 0.f), AY = AX, AZ = AX;
     for (int i = w.sa; i < w.sb; ++i) {
-        const int s = cs.ctsrc[i];
-        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of a neighbouring level
-        const float4 *SP, *SF;
-        int g0, gl;
-        pick_sources(g, s, level_bit(g, cs, e.t, s), src, SP, SF, g0, gl);
+        const int2 cc = cs.ctcand[i];  // CTA-uniform
+        if (cc.y == 0) continue;       // a boundary candidate of a neighbouring level
+        const bool coarse = cc.y < 0;
+        const float4* SP = coarse ? cs.cpos32 : g.pos32;
+        const float4* SF = coarse ? cs.csrc : src;
+        const int g0 = cc.x, gl = coarse ? -cc.y : cc.y;
         for (int base = 0; base < gl; base += kFarTile32) {
             const int n = min(kFarTile32, gl - base);
             const int np = (n + 1) >> 1;
@@ -762,6 +763,27 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWor
         o[0] = x;
         o[1] = y;
         o[2] = z;
+    }
+}
+
+// Per geometry: each entry's candidates resolved once. A candidate s of entry (t, l) counts if
+// tgt_level(t, s) == l (the same rule for the listed and the grid entries, so every far pair lands in
+// exactly one entry) and is read from its coarse level for t (level_bit) or its grid points.
+__global__ void k_ct_classify(DevGeom g, CoarseSet cs) {
+    const CtEnt e = cs.ctent[blockIdx.x];
+    for (int i = threadIdx.x; i < e.nsrc; i += blockDim.x) {
+        const int s = cs.ctsrc[e.src0 + i];
+        int2 cc = make_int2(0, 0);
+        if (tgt_level(g, cs, e.t, s) == e.l) {
+            const unsigned b = level_bit(g, cs, e.t, s);
+            if (b & kBitFine) {
+                cc = make_int2(g.gidx[s], g.glen[s]);
+            } else {
+                const int4 L = cs.clev[s * kCoarseLevels + (31 - __clz(b))];
+                cc = make_int2(L.y, -L.z);
+            }
+        }
+        cs.ctcand[e.src0 + i] = cc;
     }
 }
 
@@ -1156,8 +1178,8 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
 // The fused float-float pass with the float-float set's coarse targets: one CTA of kFarThreadsDF
 // threads per work item, nodes [k0, k0 + 64) of an entry (coarse nodes of level l, or the sphere's
 // grid points for l = -1), two per thread as the packed lanes of df_pair, against the entry's
-// candidates; a candidate counts only if tgt_level(t, s) == l (CTA-uniform) and is read from its
-// float-float coarse level for t or its grid. Partial sums [chunk][node][6] (traction, single layer).
+// candidates as k_ct_classify resolved them (float-float coarse level or grid). Partial sums
+// [chunk][node][6] (traction, single layer).
 __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     k_far_df_ct(DevGeom g, const CtWork* __restrict__ works, const float4* __restrict__ src,
                 double* __restrict__ partial) {
@@ -1191,19 +1213,13 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     acc.sxh = acc.sxl = acc.syh = acc.syl = acc.szh = acc.szl = f2(0.f, 0.f);
     const float2 one = f2(1.f, 1.f);
     for (int i = w.sa; i < w.sb; ++i) {
-        const int s = cs.ctsrc[i];
-        if (tgt_level(g, cs, e.t, s) != e.l) continue;  // a boundary candidate of a neighbouring level
-        const unsigned b = level_bit(g, cs, e.t, s);
-        const float4 *QH = g.pos32, *QL = g.pos32lo, *QF = src;
-        int g0 = g.gidx[s], gl = g.glen[s];
-        if (!(b & kBitFine)) {
-            const int4 L = cs.clev[s * kCoarseLevels + (31 - __clz(b))];
-            QH = cs.cpos32;
-            QL = cs.cpos32lo;
-            QF = cs.csrc;
-            g0 = L.y;
-            gl = L.z;
-        }
+        const int2 cc = cs.ctcand[i];  // CTA-uniform
+        if (cc.y == 0) continue;       // a boundary candidate of a neighbouring level
+        const bool coarse = cc.y < 0;
+        const float4* QH = coarse ? cs.cpos32 : g.pos32;
+        const float4* QL = coarse ? cs.cpos32lo : g.pos32lo;
+        const float4* QF = coarse ? cs.csrc : src;
+        const int g0 = cc.x, gl = coarse ? -cc.y : cc.y;
         for (int base = 0; base < gl; base += kFarTile) {
             const int n = min(kFarTile, gl - base);
             __syncthreads();
@@ -1578,6 +1594,12 @@ int launch_far_field_df(const DevGeom& g, const FarItem* items, int nitems, int 
     if (kind == 2) k_far_dfx2<2><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, partial_sl);
     else if (kind == 1) k_far_dfx2<1><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
     else k_far_dfx2<0><<<nitems, kFarThreadsDF, 0, st>>>(g, items, src2, partial, nullptr);
+    return 1;
+}
+
+int launch_ct_classify(const DevGeom& g, const CoarseSet& cs, cudaStream_t st) {
+    if (cs.nctent <= 0) return 0;
+    k_ct_classify<<<cs.nctent, 128, 0, st>>>(g, cs);
     return 1;
 }
 

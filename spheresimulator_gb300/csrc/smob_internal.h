@@ -100,6 +100,9 @@ struct CoarseSet {
     int nctent;
     const struct CtEnt* ctent; // listed and grid entries
     const int* ctsrc;          // the entries' candidate source spheres
+    int2* ctcand;              // per candidate, from the geometry (launch_ct_classify): the first point and
+                               // count of the sources it is read from (count < 0: coarse points, -count of
+                               // them; 0: not this entry's pair)
     float4* ctu;               // FP32 set: far field at the coarse targets of the current pass
     float* ctinterp;           // FP32 set: [kCoarseLevels + 1][M][3]: listed entries interpolated to the
                                // grid by level slot, and the grid entries' sums
@@ -212,6 +215,9 @@ int launch_far_reduce(const DevGeom& g, const void* partial, bool fp32, double p
 // into their level slots (launch_far_reduce with ct = 1 adds the slots)
 int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, const float4* src32, float* partial,
                   cudaStream_t st);
+// per geometry (after launch_coarse_grid): every entry's candidates resolved by tgt_level and level_bit
+// into cs.ctcand, which the target kernels read instead of evaluating the rules per pass
+int launch_ct_classify(const DevGeom& g, const CoarseSet& cs, cudaStream_t st);
 // the fused float-float pass (traction and single layer) with the float-float set's coarse targets
 // (after launch_coarse_src_df): as launch_far_ct, into cshp.ctud / ctinterpd (launch_far_reduce with
 // ct = 2 and 3 adds the slots)
