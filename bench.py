@@ -40,7 +40,7 @@ WORKLOAD = ("cfg2: 64 spheres a=1, seeded RSA in box 20 (min gap 0.1), p=16 (369
             "N(0,1) force/torque, GMRES(50) to 1e-8 relative residual")
 # DRAM bytes (read + write) of one FP32 traction far-field launch on this workload, from an ncu capture
 # (GB300, k_far32<1, 1> with coarse equivalent sources: 4,226,304 read, 0 written)
-CFG2_FAR32_DRAM_BYTES = 4226304
+CFG2_FAR32_DRAM_BYTES = 4346112
 
 
 def dist_init():
@@ -312,14 +312,17 @@ def run_native(args, world, rank, local, dist):
                      "peak": round(f32.value, 3), "unit": "TFLOP/s",
                      "frac": round(achieved / f32.value, 4) if achieved else None,
                      "traffic": CFG2_FAR32_DRAM_BYTES,
-                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_far32 launch on this "
-                                       "workload (ncu --set full, bench.py --far-once); algorithmic bytes "
-                                       "(grid positions, normals, sources 1.8 MB and coarse points and "
-                                       "strengths 2.3 MB, each once) = 4.1 MB",
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_far32_ct launch (the "
+                                       "FP32 entry kernel) on this workload (ncu --set full, bench.py --far-once); "
+                                       "algorithmic bytes (grid positions, normals, sources 1.8 MB, coarse points, "
+                                       "normals and strengths 3.3 MB, candidate table 0.1 MB, each once; partial "
+                                       "sums stay in L2) = 5.2 MB upper bound",
                      "peak_source": "FP32 FMA issue rate measured in this run (MEASURED_PEAKS.json has no SIMT entry)",
                      "flops_per_launch": 30.0 * evaluated, "pairs_per_launch": evaluated,
-                     "pairs_note": "pairs the kernel evaluates per launch (fine grid sources, or coarse equivalent "
-                                   "sources for well-separated sphere pairs), 30 flop each",
+                     "pairs_note": "pairs one FP32 far-field pass evaluates (grid targets or a target sphere's coarse "
+                                   "nodes, against grid sources or coarse equivalent sources, for well-separated "
+                                   "sphere pairs), 30 flop each; the time is the pass's entry kernel, chunk sums "
+                                   "and interpolation together",
                      "avg_launch_ms": round(avg_s * 1e3, 5), "launches_in_profiled_solve": k_l,
                      "share_of_kernel_time": round(k_ms / tot_prof, 4) if tot_prof else None,
                      "fp64_fma_peak_tflops": round(f64.value, 4)},

@@ -792,7 +792,8 @@ __global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
     const CoarseSet& cs = g.cs32;
     const CtEnt e = cs.ctent[blockIdx.x];
     if (g.active && !g.active[e.problem]) return;
-    for (int k = threadIdx.x; k < e.n; k += blockDim.x) {
+    // CTA (entry, block of blockDim.x nodes)
+    for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < e.n; k += blockDim.x * gridDim.y) {
         float x = 0.f, y = 0.f, z = 0.f;
         for (int c = 0; c < e.nchunks; ++c) {
             const float* o = partial + e.poff + 3LL * ((long long)c * e.n + k);
@@ -1252,7 +1253,8 @@ __global__ void k_ct_sum_df(DevGeom g, const double* __restrict__ partial) {
     const CoarseSet& cs = g.cshp;
     const CtEnt e = cs.ctent[blockIdx.x];
     if (g.active && !g.active[e.problem]) return;
-    for (int k = threadIdx.x; k < e.n; k += blockDim.x) {
+    // CTA (entry, block of blockDim.x nodes)
+    for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < e.n; k += blockDim.x * gridDim.y) {
         double v[6] = {0, 0, 0, 0, 0, 0};
         for (int c = 0; c < e.nchunks; ++c) {
             const double* o = partial + e.poff + 6LL * ((long long)c * e.n + k);
@@ -1611,7 +1613,8 @@ int launch_far_df_ct(const DevGeom& g, const CtWork* works, int nworks, const fl
         k_far_df_ct<<<nworks, kFarThreadsDF, 0, st>>>(g, works, src2, partial);
         ++n;
     }
-    k_ct_sum_df<<<g.cshp.nctent, 128, 0, st>>>(g, partial);
+    const int nblk = ((g.pmax + 1) * (2 * g.pmax + 2) + 127) / 128;  // the largest entry: a grid entry
+    k_ct_sum_df<<<dim3(g.cshp.nctent, nblk), 128, 0, st>>>(g, partial);
     ++n;
     if (g.cshp.nctitile > 0) {
         k_ct_interp_df<<<g.cshp.nctitile, 128, 0, st>>>(g);
@@ -1637,7 +1640,8 @@ int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, 
         else k_far32_ct<false><<<nworks, kFarThreads, 0, st>>>(g, works, src32, partial);
         ++n;
     }
-    k_ct_sum<<<g.cs32.nctent, 128, 0, st>>>(g, partial);
+    const int nblk = ((g.pmax + 1) * (2 * g.pmax + 2) + 127) / 128;  // the largest entry: a grid entry
+    k_ct_sum<<<dim3(g.cs32.nctent, nblk), 128, 0, st>>>(g, partial);
     ++n;
     if (g.cs32.nctitile > 0) {  // grid entries only: nothing to interpolate
         k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
