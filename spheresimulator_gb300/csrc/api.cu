@@ -992,7 +992,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         std::vector<CtWork> sorted(order.size());
         for (size_t i = 0; i < order.size(); ++i) sorted[i] = h.ct_work[order[i]];
         h.ct_work.swap(sorted);
-        // interpolation tiles: listed entries grouped by map, 8 entries x 128 grid points per CTA
+        // interpolation tiles: listed entries grouped by map, 2 (float-float: 4) entries x 128 grid points
         std::map<int, std::vector<int>> by_map;
         for (int i = 0; i < (int)h.ctent.size(); ++i) {
             const CtEnt& e = h.ctent[i];
@@ -1001,7 +1001,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
             const int ng = c->glen[e0.t], n = e0.n;
-            const size_t per = h.hp ? 4 : 8;  // entries per tile (the kernels' kCiEntD / kCiEnt)
+            const size_t per = h.hp ? 4 : 2;  // entries per tile (the kernels' kCiEntD / kCiEnt)
             for (size_t a = 0; a < kv.second.size(); a += per) {
                 const int first = (int)h.ctient.size();
                 const int ne = (int)std::min<size_t>(8, kv.second.size() - a);

@@ -813,11 +813,12 @@ __global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
 
 // Interpolation of the listed entries' node values to their spheres' grids: u(nu_j) = sum_k w_k
 // K_pe(nu_j . nu_k) u_k (the transposed coarse map, exact for fields of degree <= pe on the sphere).
-// A small GEMM per map (order p, level pe): CTA tile = 128 grid points x up to 8 entries of that
-// map; each map element read (coalesced, [node][grid point]) serves the 8 entries' 3 components,
-// whose node values are staged kCiK nodes at a time in shared memory. Each entry's result goes to
-// its level slot of ctinterp.
-constexpr int kCiEnt = 8, kCiK = 32;
+// A small GEMM per map (order p, level pe): CTA tile = 128 grid points x up to kCiEnt entries of that
+// map; each map element read (coalesced, [node][grid point]) serves the entries' 3 components, whose
+// node values are staged kCiK nodes at a time in shared memory. Two entries per tile: the map stays in
+// L2 and more CTAs hide its latency (one CTA per SM with 8 entries on cfg2). Each entry's result goes
+// to its level slot of ctinterp.
+constexpr int kCiEnt = 2, kCiK = 32;
 __global__ void __launch_bounds__(128) k_ct_interp(DevGeom g) {
     const CoarseSet& cs = g.cs32;
     const CtITile d = cs.ctitile[blockIdx.x];

@@ -1,9 +1,11 @@
-"""The mathematics of the coarse equivalent sources, restated in numpy (CPU): for a sphere's grid
-sources f_j, equivalent sources f_e = W_pe K_pe f on the order-pe grid of the same sphere, with
-K_pe(k, j) = sum_{n <= pe} (2n+1)/(4 pi) P_n(nu_k . nu_j), reproduce the sphere's Stokes single-layer
-and traction far fields to ~(a / r_min)^(pe+1) relative; the library's level rule
+"""The mathematics of the coarse equivalent sources and coarse targets, restated in numpy (CPU): for
+a sphere's grid sources f_j, equivalent sources f_e = W_pe K_pe f on the order-pe grid of the same
+sphere, with K_pe(k, j) = sum_{n <= pe} (2n+1)/(4 pi) P_n(nu_k . nu_j), reproduce the sphere's Stokes
+single-layer and traction far fields to ~(a / r_min)^(pe+1) relative; the library's level rule
 pe >= log(eps) / log(a / r_min) + 1 keeps the error near eps (below 3.4 eps over p = 8-24,
-a / r_min = 0.05-0.4, both kernels and eps = 1e-5-1e-10; below eps with a margin of 2)."""
+a / r_min = 0.05-0.4, both kernels and eps = 1e-5-1e-10; below eps with a margin of 2). On the target
+side the transposed map interpolates a field sampled at a sphere's order-pt nodes to its grid, exact
+for degree <= pt; with the target rule's margin of 2 both sides together stay within 10 eps."""
 import numpy as np
 from numpy.polynomial.legendre import leggauss, legval
 
