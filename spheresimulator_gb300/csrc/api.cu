@@ -992,7 +992,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         std::vector<CtWork> sorted(order.size());
         for (size_t i = 0; i < order.size(); ++i) sorted[i] = h.ct_work[order[i]];
         h.ct_work.swap(sorted);
-        // interpolation tiles: listed entries grouped by map, 2 (float-float: 4) entries x 128 grid points
+        // interpolation tiles: listed entries grouped by map, 2 entries x 128 (float-float: 256) grid points
         std::map<int, std::vector<int>> by_map;
         for (int i = 0; i < (int)h.ctent.size(); ++i) {
             const CtEnt& e = h.ctent[i];
@@ -1001,12 +1001,13 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
             const int ng = c->glen[e0.t], n = e0.n;
-            const size_t per = h.hp ? 4 : 2;  // entries per tile (the kernels' kCiEntD / kCiEnt)
+            const size_t per = 2;                // entries per tile (the kernels' kCiEnt / kCiEntD)
+            const int pts = h.hp ? 256 : 128;    // grid points per tile
             for (size_t a = 0; a < kv.second.size(); a += per) {
                 const int first = (int)h.ctient.size();
                 const int ne = (int)std::min<size_t>(8, kv.second.size() - a);
                 h.ctient.insert(h.ctient.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
-                for (int j0 = 0; j0 < ng; j0 += 128) h.ctitile.push_back(CtITile{kv.first, ng, n, first, ne, j0, 0, 0});
+                for (int j0 = 0; j0 < ng; j0 += pts) h.ctitile.push_back(CtITile{kv.first, ng, n, first, ne, j0, 0, 0});
             }
         }
     }
@@ -1034,7 +1035,13 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         if (h.hp) {
             h.d_ct_partial.alloc(sizeof(double) * (size_t)h.ct_partial);
             h.d_ctinterp.alloc(sizeof(double) * 6 * slots);
-            h.d_cmapT.upload(mapsTd);
+            // (hi, lo) float pairs of the FP64 transposed maps (the float-float interpolation)
+            std::vector<float2> mapsTdf(mapsTd.size());
+            for (size_t i = 0; i < mapsTd.size(); ++i) {
+                const float hi = float(mapsTd[i]);
+                mapsTdf[i] = make_float2(hi, float(mapsTd[i] - double(hi)));
+            }
+            h.d_cmapT.upload(mapsTdf);
             h.d_cnrm32lo.alloc(sizeof(float4) * np);
             h.d_ctu.alloc(sizeof(double) * 6 * np);
         } else {
@@ -1137,7 +1144,7 @@ void bind_geom(smob_ctx* c) {
         cs.cnrm32 = ct ? h.d_cnrm32.as<float4>() : nullptr;
         cs.cnrm32lo = ct && h.hp ? h.d_cnrm32lo.as<float4>() : nullptr;
         cs.cmapT = ct && !h.hp ? h.d_cmapT.as<float>() : nullptr;
-        cs.cmapTd = ct && h.hp ? h.d_cmapT.as<double>() : nullptr;
+        cs.cmapTdf = ct && h.hp ? h.d_cmapT.as<float2>() : nullptr;
         cs.ctused = ct ? h.d_ctused.as<int>() : nullptr;
         cs.nctent = ct ? (int)h.ctent.size() : 0;
         cs.ctent = ct ? h.d_ctent.as<CtEnt>() : nullptr;

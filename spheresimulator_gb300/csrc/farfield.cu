@@ -1268,13 +1268,15 @@ __global__ void k_ct_sum_df(DevGeom g, const double* __restrict__ partial) {
     }
 }
 
-// The float-float set's interpolation in FP64 (k_ct_interp's tiling with 4 entries x 6 components per
-// grid point; the map column batched in registers, the entries' node values staged in shared memory).
-constexpr int kCiEntD = 4, kCiKD = 16;
+// The float-float set's interpolation in float-float arithmetic on the FP32 pipes (the FP64 pipe is
+// 1/58 of them): maps stored as (hi, lo) float pairs, the entries' node values split into (hi, lo) in
+// shared memory, products by df_mul_u and sums by df_acc (~2^-44 relative to the sum of |terms|).
+// CTA tile: 256 grid points (two per thread, the packed lanes) x kCiEntD entries x 6 components.
+constexpr int kCiEntD = 2, kCiKD = 8;
 __global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
     const CoarseSet& cs = g.cshp;
     const CtITile d = cs.ctitile[blockIdx.x];
-    __shared__ double U[kCiKD][kCiEntD][6];
+    __shared__ float2 U[kCiKD][kCiEntD][6];
     __shared__ int eq0[kCiEntD], eon[kCiEntD];
     __shared__ long long ebase[kCiEntD];
     if (threadIdx.x < kCiEntD) {
@@ -1290,32 +1292,42 @@ __global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
         }
     }
     __syncthreads();
-    const int j = d.j0 + threadIdx.x;
+    // grid points j, j + 1 (ng is even, so both or neither exist); (hi, lo) pairs of both in one float4
+    const int j = d.j0 + 2 * threadIdx.x;
     const bool val = j < d.ng;
-    const double* MT = cs.cmapTd + d.mapoff + (val ? j : 0);
-    double acc[kCiEntD][6];
+    const float4* MT = reinterpret_cast<const float4*>(cs.cmapTdf + d.mapoff + (val ? j : 0));
+    const long long row = d.ng / 2;  // float4 per map row
+    float2 ah[kCiEntD][6], al[kCiEntD][6];
 #pragma unroll
     for (int e = 0; e < kCiEntD; ++e)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc[e][q] = 0.0;
+        for (int q = 0; q < 6; ++q) ah[e][q] = al[e][q] = f2(0.f, 0.f);
     for (int k0 = 0; k0 < d.n; k0 += kCiKD) {
         const int nk = min(kCiKD, d.n - k0);
-        double mk[kCiKD];
+        float4 mk[kCiKD];
 #pragma unroll
-        for (int kk = 0; kk < kCiKD; ++kk) mk[kk] = (val && kk < nk) ? __ldg(MT + (long long)(k0 + kk) * d.ng) : 0.0;
+        for (int kk = 0; kk < kCiKD; ++kk)
+            mk[kk] = (val && kk < nk) ? __ldg(MT + (long long)(k0 + kk) * row) : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
         for (int idx = threadIdx.x; idx < kCiKD * kCiEntD * 6; idx += 128) {
             const int q = idx % 6, e = (idx / 6) % kCiEntD, kk = idx / (6 * kCiEntD);
-            U[kk][e][q] = (kk < nk && eon[e]) ? cs.ctud[6LL * (eq0[e] + k0 + kk) + q] : 0.0;
+            const double u = (kk < nk && eon[e]) ? cs.ctud[6LL * (eq0[e] + k0 + kk) + q] : 0.0;
+            const float h = float(u);
+            U[kk][e][q] = f2(h, float(u - double(h)));
         }
         __syncthreads();
         // rows past nk hold zeros in both operands
 #pragma unroll
-        for (int kk = 0; kk < kCiKD; ++kk)
+        for (int kk = 0; kk < kCiKD; ++kk) {
+            const df2 m{f2(mk[kk].x, mk[kk].z), f2(mk[kk].y, mk[kk].w)};
 #pragma unroll
             for (int e = 0; e < kCiEntD; ++e)
 #pragma unroll
-                for (int q = 0; q < 6; ++q) acc[e][q] = fma(mk[kk], U[kk][e][q], acc[e][q]);
+                for (int q = 0; q < 6; ++q) {
+                    const float2 u = U[kk][e][q];
+                    df_acc(ah[e][q], al[e][q], df_mul_u(m, df2{f2(u.x, u.x), f2(u.y, u.y)}));
+                }
+        }
     }
     if (!val) return;
 #pragma unroll
@@ -1323,7 +1335,10 @@ __global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
         if (e >= d.ne || !eon[e]) continue;
         double* o = cs.ctinterpd + 6LL * (ebase[e] + j);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) o[q] = acc[e][q];
+        for (int q = 0; q < 6; ++q) {
+            o[q] = double(ah[e][q].x) + double(al[e][q].x);
+            o[6 + q] = double(ah[e][q].y) + double(al[e][q].y);
+        }
     }
 }
 

@@ -95,7 +95,7 @@ struct CoarseSet {
     const float4* cnrm32;      // coarse node normals, w = level index bits (float-float set: high parts)
     const float4* cnrm32lo;    // float-float set: the normals' low parts
     const float* cmapT;        // FP32 set: the maps transposed, [coarse node][fine node], at the maps' offsets
-    const double* cmapTd;      // float-float set: the same in FP64
+    const float2* cmapTdf;     // float-float set: the same from the FP64 maps as (hi, lo) float pairs
     const int* ctused;         // [N][kCoarseLevels]: the entry is a listed coarse-target entry (CtEnt)
     int nctent;
     const struct CtEnt* ctent; // listed and grid entries
@@ -138,7 +138,7 @@ struct CtWork {
     int sa, sb, chunk, pad;
 };
 
-// one interpolation tile: grid points [j0, j0 + 128) of up to 2 (float-float set: 4) listed entries
+// one interpolation tile: grid points [j0, j0 + 128) (float-float set: 256) of up to 2 listed entries
 // sharing one map (order p, level pe): entries ctient[e0, e0 + ne), map at mapoff ([n][ng])
 struct CtITile {
     int mapoff, ng, n, e0;
