@@ -227,6 +227,8 @@ struct smob_ctx {
     DBuf d_ru, d_rcoef, d_rscale;
     int rk = 0, rprec = -1;
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
+    DBuf d_red_count;     // per (problem, vector) counters of the fused dot reductions
+    int red_cstride = 0;  // counters per problem
     bool have_xlast = false;
 
     DevGeom g{};
@@ -266,6 +268,8 @@ struct smob_ctx {
         L.problems = d_problems.as<Problem>();
         L.P = P;
         L.partial = d_partial_red.as<double>();
+        L.counters = d_red_count.as<unsigned>();
+        L.cstride = red_cstride;
         return L;
     }
 
@@ -344,9 +348,17 @@ void prof_flush(smob_ctx* c) {
 }
 
 void check_launch(smob_ctx* c, int n) {
+    if (n < 0) throw SmobError(SMOB_ERR_STATE, "kernel launch refused: more vectors than the work buffers hold");
     c->launches += n;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw SmobError(SMOB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+}
+
+// counters of the fused dot reductions: nvec per problem, zeroed (the kernels leave them zero)
+void alloc_red_counters(smob_ctx* c, int nvec) {
+    c->d_red_count.alloc(sizeof(unsigned) * (size_t)std::max(c->P, 1) * nvec);
+    CUDA_OK(cudaMemsetAsync(c->d_red_count.p, 0, sizeof(unsigned) * (size_t)std::max(c->P, 1) * nvec, c->st));
+    c->red_cstride = nvec;
 }
 
 // unit quaternion of sphere i from a caller's orientation: normalised, except that one already of
@@ -622,6 +634,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_out.alloc(sizeof(double) * 3 * c->M);
     c->d_tmp.alloc(sizeof(double) * 3 * c->M);
     c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * 2);
+    alloc_red_counters(c, 2);
     upload_near(c);
     build_coarse(c);
     bind_geom(c);
@@ -1411,6 +1424,7 @@ void ensure_solver(smob_ctx* c, int m) {
         c->d_sn.alloc(sizeof(double) * c->P * m);
         c->d_y.alloc(sizeof(double) * c->P * m);
         c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * (m + 1));
+        alloc_red_counters(c, m + 1);
         c->restart_cap = m;
     }
     c->d_w.alloc(sizeof(double) * n);

@@ -26,9 +26,17 @@ __device__ __forceinline__ double block_reduce(double v, double* red) {
     return s;
 }
 
+// Chunk dot products <A_i, b> with the final sum fused in: every CTA writes its chunk's partial, and
+// the last CTA of a (problem, vector) to finish (a counter per pair, after a memory fence) adds that
+// problem's partials in chunk order and writes out[p*ostride + ooff + i] (+)= sum (sqrt if take_sqrt;
+// optionally also out2), then resets the counter. The order of the final sum is fixed, so the result
+// does not depend on which CTA finishes last.
 __global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* __restrict__ A, long long lda,
                              const double* __restrict__ b, const unsigned char* __restrict__ active,
-                             double* __restrict__ partial, int nchunks) {
+                             double* __restrict__ partial, int nchunks, const Problem* __restrict__ probs,
+                             unsigned* __restrict__ counters, int cstride, double* out, long long ostride,
+                             long long ooff, int accumulate, int take_sqrt, double* out2, long long ostride2,
+                             int accumulate2) {
     __shared__ double red[32];
     const VecChunk ch = chunks[blockIdx.x];
     if (active && !active[ch.problem]) return;
@@ -37,27 +45,22 @@ __global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* 
     double s = 0;
     for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) s = fma(a[l], b[l], s);
     s = block_reduce(s, red);
-    if (threadIdx.x == 0) partial[(long long)i * nchunks + blockIdx.x] = s;
-}
-
-// out[p*ostride + ooff + i] (+)= sum over the problem's chunks, i < nvec; optionally also into out2
-__global__ void k_chunk_finalize(const Problem* __restrict__ probs, int P, const double* __restrict__ partial,
-                                 int nchunks, int nvec, const unsigned char* __restrict__ active, double* out,
-                                 long long ostride, long long ooff, int accumulate, int take_sqrt, double* out2,
-                                 long long ostride2, int accumulate2) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P * nvec) return;
-    const int p = t / nvec, i = t - p * nvec;
-    if (active && !active[p]) return;
-    const Problem pr = probs[p];
-    double s = 0;
-    for (int c = pr.c0; c < pr.c1; ++c) s += partial[(long long)i * nchunks + c];
-    if (take_sqrt) s = sqrt(s);
-    double* o = out + ostride * p + ooff + i;
-    *o = accumulate ? *o + s : s;
+    if (threadIdx.x != 0) return;
+    partial[(long long)i * nchunks + blockIdx.x] = s;
+    __threadfence();
+    const Problem pr = probs[ch.problem];
+    unsigned* cnt = counters + (long long)ch.problem * cstride + i;
+    if (atomicAdd(cnt, 1u) != (unsigned)(pr.c1 - pr.c0 - 1)) return;
+    // the last chunk of this (problem, vector): every partial is written
+    double t = 0;
+    for (int c = pr.c0; c < pr.c1; ++c) t += __ldcg(partial + (long long)i * nchunks + c);
+    *cnt = 0u;
+    if (take_sqrt) t = sqrt(t);
+    double* o = out + ostride * ch.problem + ooff + i;
+    *o = accumulate ? *o + t : t;
     if (out2) {
-        double* o2 = out2 + ostride2 * p + i;
-        *o2 = accumulate2 ? *o2 + s : s;
+        double* o2 = out2 + ostride2 * ch.problem + i;
+        *o2 = accumulate2 ? *o2 + t : t;
     }
 }
 
@@ -178,13 +181,12 @@ __global__ void k_kcount(int P, const KrylovState* __restrict__ ks, int* __restr
 int launch_dots(const KrylovLaunch& L, const double* A, long long lda, int nvec, const double* b,
                 const unsigned char* active, double* out, long long ostride, long long ooff, bool accumulate,
                 bool take_sqrt, cudaStream_t st, double* out2, long long ostride2, bool accumulate2) {
+    if (nvec > L.cstride) return -1;  // more vectors than counters per problem
     dim3 grid(L.nchunks, nvec);
-    k_chunk_dots<<<grid, 256, 0, st>>>(L.chunks, A, lda, b, active, L.partial, L.nchunks);
-    const int n = L.P * nvec;
-    k_chunk_finalize<<<(n + 127) / 128, 128, 0, st>>>(L.problems, L.P, L.partial, L.nchunks, nvec, active, out, ostride,
-                                                      ooff, accumulate ? 1 : 0, take_sqrt ? 1 : 0, out2, ostride2,
-                                                      accumulate2 ? 1 : 0);
-    return 2;
+    k_chunk_dots<<<grid, 256, 0, st>>>(L.chunks, A, lda, b, active, L.partial, L.nchunks, L.problems, L.counters,
+                                       L.cstride, out, ostride, ooff, accumulate ? 1 : 0, take_sqrt ? 1 : 0, out2,
+                                       ostride2, accumulate2 ? 1 : 0);
+    return 1;
 }
 
 int launch_update(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const int* nvec_p, const double* h,

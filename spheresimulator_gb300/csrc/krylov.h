@@ -27,6 +27,8 @@ struct KrylovLaunch {
     const Problem* problems;
     int P;
     double* partial;  // nchunks * max_nvec
+    unsigned* counters;  // P * cstride, zero between launches (launch_dots' last chunk of each sum resets it)
+    int cstride;         // counters per problem (the most vectors one launch_dots may take)
 };
 
 // out[p*ostride + ooff + i] (+)= <A_i, b> over problem p's segment for i < nvec (sqrt if take_sqrt);
