@@ -1005,7 +1005,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         std::vector<CtWork> sorted(order.size());
         for (size_t i = 0; i < order.size(); ++i) sorted[i] = h.ct_work[order[i]];
         h.ct_work.swap(sorted);
-        // interpolation tiles: listed entries grouped by map, 2 entries x 128 (float-float: 256) grid points
+        // interpolation tiles: listed entries grouped by map, 2 entries x 128 grid points (float-float: 1 x 256)
         std::map<int, std::vector<int>> by_map;
         for (int i = 0; i < (int)h.ctent.size(); ++i) {
             const CtEnt& e = h.ctent[i];
@@ -1014,7 +1014,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
             const int ng = c->glen[e0.t], n = e0.n;
-            const size_t per = 2;                // entries per tile (the kernels' kCiEnt / kCiEntD)
+            const size_t per = h.hp ? 1 : 2;     // entries per tile (the kernels' kCiEntD / kCiEnt)
             const int pts = h.hp ? 256 : 128;    // grid points per tile
             for (size_t a = 0; a < kv.second.size(); a += per) {
                 const int first = (int)h.ctient.size();

@@ -1272,7 +1272,7 @@ __global__ void k_ct_sum_df(DevGeom g, const double* __restrict__ partial) {
 // 1/58 of them): maps stored as (hi, lo) float pairs, the entries' node values split into (hi, lo) in
 // shared memory, products by df_mul_u and sums by df_acc (~2^-44 relative to the sum of |terms|).
 // CTA tile: 256 grid points (two per thread, the packed lanes) x kCiEntD entries x 6 components.
-constexpr int kCiEntD = 2, kCiKD = 8;
+constexpr int kCiEntD = 1, kCiKD = 8;  // one entry per tile: 2x the CTAs of two (177 on cfg2, 152 SMs)
 __global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
     const CoarseSet& cs = g.cshp;
     const CtITile d = cs.ctitile[blockIdx.x];

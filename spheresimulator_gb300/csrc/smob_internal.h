@@ -138,7 +138,7 @@ struct CtWork {
     int sa, sb, chunk, pad;
 };
 
-// one interpolation tile: grid points [j0, j0 + 128) (float-float set: 256) of up to 2 listed entries
+// one interpolation tile: grid points [j0, j0 + 128) of up to 2 listed entries (float-float set: 256, 1)
 // sharing one map (order p, level pe): entries ctient[e0, e0 + ne), map at mapoff ([n][ng])
 struct CtITile {
     int mapoff, ng, n, e0;
