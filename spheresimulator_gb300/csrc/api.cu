@@ -760,10 +760,13 @@ void build_tables(smob_ctx* c) {
 }
 
 // device pointers and sizes of the geometry, as the kernels receive them
-// Coarse levels of every source sphere for this geometry and one tolerance: for each far pair (t, s) of
-// a problem the coarsest ladder order pe < p_s with pe >= log(eps) / log(a_s / r_min) + margin,
-// r_min = |c_t - c_s| - a_t (the kernels recompute this per target and use the coarsest level built that
-// satisfies it); at most kCoarseLevels orders per sphere (the finest kept). Maps are shared per (p, pe).
+// Coarse levels of every sphere for this geometry and one tolerance: for each far pair (t, s) of a
+// problem the coarsest ladder order pe < p_s with pe >= log(eps) / log(a_s / r_min) + margin,
+// r_min = |c_t - c_s| - a_t (s as the source; the kernels use the coarsest level built that satisfies
+// it) and, with coarse targets, the same with the target margin for s as the target of t (if that
+// level has at most kCoarseTargetNum / kCoarseTargetDen of s's grid points); at most kCoarseLevels
+// orders per sphere (the finest kept). Maps (and their transposes) are shared per (p, pe). Then the
+// coarse-target entries, their candidates, work items and interpolation tiles.
 void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>& nodes, std::vector<int>& node_off,
                       std::vector<char>& have_nodes) {
     const int N = c->N;
