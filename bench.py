@@ -328,7 +328,10 @@ def run_native(args, world, rank, local, dist):
                      "fp64_fma_peak_tflops": round(f64.value, 4)},
         "kernel_ms_profiled_solve": {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items())},
         "autotune": {"fp32_targets_per_thread": tpt.value, "variant_ms_tpt_1_2_4": [round(v, 4) for v in tms],
-                     "from_cache": bool(tcache.value)},
+                     "from_cache": bool(tcache.value),
+                     "note": "tile of the FP32 grid kernels, tuned when a context first runs them (here the "
+                             "direct-sum arm, coarse sources off); with coarse targets on (the default) the "
+                             "FP32 passes run the entry kernel and do not use it"},
         "cpu_baseline": cpu,
         "e2e": {"value": round(world * args.steps / e2e_total, 4), "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * n6, "d2h_bytes_per_step": 8 * n6,

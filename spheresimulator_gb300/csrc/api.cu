@@ -163,6 +163,7 @@ struct smob_ctx {
     std::vector<FarItem> items_tpt[3];  // FP32 item lists for 1, 2, 4 targets per thread
     std::vector<FarItem> items_df;      // float-float items: 2 * kFarThreadsDF targets
     int tpt = 2;                         // FP32 targets per thread chosen by the autotuner
+    bool tuned = false;                  // autotuner run (or the tile set by the caller)
     double tune_ms[3] = {0, 0, 0};
     bool tune_cached = false;
     long long partial32 = 0, partial64 = 0;
@@ -1269,6 +1270,14 @@ void far_ct(smob_ctx* c, bool trac, cudaStream_t st) {
                                   c->d_src32.as<float4>(), c->c32.d_ct_partial.as<float>(), st));
 }
 
+// The FP32 grid kernels' tile is tuned when a context first runs them: with coarse targets on, its
+// FP32 passes use the entry kernel instead and need no tuning.
+void ensure_tuned(smob_ctx* c) {
+    if (c->tuned || far_ct_on(c)) return;
+    autotune_far32(c);
+    c->tuned = true;
+}
+
 // out (device) += c_id*x + c_sl*S[x] + c_trac*K[x] + c_lop*L[x] on active problems
 void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_sl, double c_trac, double c_lop,
               int prec) {
@@ -2034,6 +2043,7 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
     coarse_grids(c);
     c->host_grid_stale = true;
+    ensure_tuned(c);  // the new geometry may have no coarse targets: its FP32 passes run the grid kernels
     c->drop_graphs();
     c->rk = 0;  // recycled solutions belong to the old operator
     for (auto& kv : c->multi) smob_destroy(kv.second);
@@ -2129,7 +2139,7 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
         configure_sphere_kernels();
         configure_near_kernels();
         build_context(c.get(), geo);
-        autotune_far32(c.get());
+        ensure_tuned(c.get());
         CUDA_OK(cudaStreamSynchronize(c->st));
         *out = c.release();
         return SMOB_OK;
@@ -2721,6 +2731,7 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
         build_coarse(c);
         bind_geom(c);
         coarse_grids(c);
+        ensure_tuned(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
@@ -2740,6 +2751,7 @@ smob_status smob_set_far_coarse_targets(smob_ctx* c, int on) {
         build_coarse(c);
         bind_geom(c);
         coarse_grids(c);
+        ensure_tuned(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
@@ -2863,6 +2875,7 @@ smob_status smob_set_far_tile(smob_ctx* c, int targets_per_thread) {
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old item list and kernel variant
         c->tpt = targets_per_thread;
+        c->tuned = true;  // the caller's choice stands
         c->items32 = c->items_tpt[k];
         c->d_items32.upload(c->items32);
         CUDA_OK(cudaStreamSynchronize(c->st));
