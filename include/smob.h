@@ -144,13 +144,16 @@ smob_status smob_coeff_offsets(const smob_ctx* ctx, int* offsets /* N+1, in doub
  * synchronizes the device). Everything is passed as device pointers: coords/norms/density (3n),
  * weights (n), sphere id per point (n); out (3n) += -3/(4 pi) * sum over points j on other spheres
  * of r (r . f_j)(r . n_i)/r^5 with f_j = c * weights[j] * density[j], r = x_i - x_j (near-pair
- * spheres are not excluded). stream: a cudaStream_t, or NULL for the default stream.
+ * spheres are not excluded; a point of another sphere that coincides with the target, r = 0, adds
+ * nothing). stream: a cudaStream_t, or NULL for the default stream.
  * Limit: 1 <= n_points <= 40960, otherwise SMOB_ERR_ARG. The scratch (per-chunk partial sums) is
  * a fixed 7.5 MiB __device__ array that every GPU loading the library keeps until exit; all calls
  * on a device share it and it keeps the last call's contents, so calls that overlap on the GPU
- * (different streams, or host threads) race. The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that first call before any
- * stream capture. */
+ * (different streams, or host threads) race. The array's device address belongs to the CUDA context
+ * of the current device: a call made outside stream capture looks it up (cudaGetSymbolAddress) for
+ * the current context, so a device reset or a non-primary context is followed; a call made while
+ * its stream is being captured uses the address that an earlier call in the same context looked up,
+ * so make the first call in each context before any stream capture (otherwise SMOB_ERR_STATE). */
 smob_status smob_far_traction_noalloc(const double* d_coords, const double* d_norms, const double* d_weights,
                                       const double* d_density, const int* d_sphere, int n_points, double c,
                                       double* d_out, void* stream);
@@ -236,6 +239,10 @@ smob_status smob_far_compression_info(const smob_ctx* ctx, int hp, double* eps, 
  * choose them), and the multiply-adds of the coarse strengths and the coarse targets' interpolation
  * per pass */
 smob_status smob_far_pairs(const smob_ctx* ctx, long long* direct, long long* evaluated, long long* coarse_macs);
+/* the same for the FP32 set (hp = 0, what smob_far_pairs reports) or for the float-float set (hp = 1: the
+ * pairs one fused float-float pass of a MIXED solve evaluates, each for both kernels) */
+smob_status smob_far_pairs_set(const smob_ctx* ctx, int hp, long long* direct, long long* evaluated,
+                               long long* coarse_macs);
 
 /* Recycled solutions for a sequence of solves on one geometry, e.g. the collision solver's repeated
  * mobility solves, whose forces are combinations of a few contact forces (the reference keeps its

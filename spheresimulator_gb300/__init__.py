@@ -201,11 +201,12 @@ class _Context:
                                                   ctypes.byref(ent)))
         return e.value, pts.value, ent.value
 
-    def far_pairs(self):
+    def far_pairs(self, hp=False):
         """(direct-sum pairs, evaluated pairs, coarse multiply-adds: strengths and target interpolation) of one
-        FP32 far-field pass"""
+        FP32 far-field pass, or (hp=True) of one fused float-float pass"""
         d, e, m = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
-        N.check(self._L.smob_far_pairs(self._h, ctypes.byref(d), ctypes.byref(e), ctypes.byref(m)))
+        N.check(self._L.smob_far_pairs_set(self._h, int(bool(hp)), ctypes.byref(d), ctypes.byref(e),
+                                           ctypes.byref(m)))
         return d.value, e.value, m.value
 
     def recycle_info(self):

@@ -137,6 +137,8 @@ def lib():
         "smob_far_compression_info": (S, [_VP, ctypes.c_int, _DP, _IP, _IP]),
         "smob_far_pairs": (S, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                ctypes.POINTER(ctypes.c_longlong)]),
+        "smob_far_pairs_set": (S, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong),
+                                   ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
         "smob_recycle_clear": (S, [_VP]),
         "smob_timer_mark": (S, [_VP]),
         "smob_timer_elapsed": (S, [_VP, _DP]),

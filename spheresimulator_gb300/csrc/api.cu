@@ -1018,11 +1018,11 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (auto& kv : by_map) {
             const CtEnt& e0 = h.ctent[kv.second[0]];
             const int ng = c->glen[e0.t], n = e0.n;
-            const size_t per = h.hp ? 1 : 2;     // entries per tile (the kernels' kCiEntD / kCiEnt)
-            const int pts = h.hp ? 256 : 128;    // grid points per tile
+            const size_t per = h.hp ? kCiEntD : kCiEnt;  // entries per tile (what the kernels read)
+            const int pts = h.hp ? kCiPtsD : kCiPts;        // grid points per tile
             for (size_t a = 0; a < kv.second.size(); a += per) {
                 const int first = (int)h.ctient.size();
-                const int ne = (int)std::min<size_t>(8, kv.second.size() - a);
+                const int ne = (int)std::min<size_t>(per, kv.second.size() - a);
                 h.ctient.insert(h.ctient.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
                 for (int j0 = 0; j0 < ng; j0 += pts) h.ctitile.push_back(CtITile{kv.first, ng, n, first, ne, j0, 0, 0});
             }
@@ -1272,8 +1272,13 @@ void far_ct(smob_ctx* c, bool trac, cudaStream_t st) {
 
 // The FP32 grid kernels' tile is tuned when a context first runs them: with coarse targets on, its
 // FP32 passes use the entry kernel instead and need no tuning.
+// Tile tuning of the FP32 grid kernels, run when a context first needs them: at creation, and
+// lazily at the next solve or operator call after a geometry or tolerance change left the FP32
+// passes without coarse targets (so that an update never runs the ~30 ms timed warm-up itself and
+// stays all-or-nothing). The choice is cached per (largest order, size bucket) for the process.
 void ensure_tuned(smob_ctx* c) {
     if (c->tuned || far_ct_on(c)) return;
+    AllocStreamScope scope(c->st);  // the tuner's item lists live on the context's stream
     autotune_far32(c);
     c->tuned = true;
 }
@@ -1594,6 +1599,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     const bool ffar = o->precision == SMOB_PREC_FLOAT_FLOAT;
     const int hp = (mixed || ffar) ? OP_DF : OP_FP64;
     const int cyc_prec = mixed ? OP_FP32 : hp;
+    ensure_tuned(c);  // before any capture: the tuner synchronizes
     ensure_solver(c, m);
     const size_t n = 3 * (size_t)c->M;
     const int P = c->P;
@@ -2043,7 +2049,8 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
     check_launch(c, launch_regrid(c->g, c->d_org.as<double>(), c->st));
     coarse_grids(c);
     c->host_grid_stale = true;
-    ensure_tuned(c);  // the new geometry may have no coarse targets: its FP32 passes run the grid kernels
+    // (the new geometry may have no coarse targets, so that its FP32 passes run the grid kernels: their
+    // tile is tuned by the next solve or operator call, not inside the update)
     c->drop_graphs();
     c->rk = 0;  // recycled solutions belong to the old operator
     for (auto& kv : c->multi) smob_destroy(kv.second);
@@ -2260,6 +2267,7 @@ smob_status smob_apply_p2p(smob_ctx* c, const double* in, double* out, double c_
         need(c && in && out, "null argument");
         set_device(c);
         all_active(c);
+        ensure_tuned(c);
         host_io(c, in, out, true, [&](const double* din, double* dout) {
             op_apply(c, din, dout, c_id, c_sl, c_trac, 0.0, op_prec(precision));
         });
@@ -2285,6 +2293,7 @@ smob_status smob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, doub
         need(c && X && Y && n_cols >= 1, "invalid argument");
         set_device(c);
         all_active(c);
+        ensure_tuned(c);
         const size_t n = 3 * (size_t)c->M;
         std::vector<double> tmp(n);
         for (int col = 0; col < n_cols; ++col) {
@@ -2320,6 +2329,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
         set_device(c);
         AllocStreamScope scope(c->st);  // the fused float-float path allocates its second partial buffer
         all_active(c);
+        ensure_tuned(c);
         const bool fp32 = precision == SMOB_PREC_MIXED;
         const bool dfar = precision == SMOB_PREC_FLOAT_FLOAT;
         host_io(c, in, out, true, [&](const double* din, double* dout) {
@@ -2731,7 +2741,6 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
         build_coarse(c);
         bind_geom(c);
         coarse_grids(c);
-        ensure_tuned(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
@@ -2751,7 +2760,6 @@ smob_status smob_set_far_coarse_targets(smob_ctx* c, int on) {
         build_coarse(c);
         bind_geom(c);
         coarse_grids(c);
-        ensure_tuned(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
@@ -2769,15 +2777,22 @@ smob_status smob_far_compression_info(const smob_ctx* c, int hp, double* eps, in
 }
 
 smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* evaluated, long long* coarse_macs) {
+    return smob_far_pairs_set(c, 0, direct, evaluated, coarse_macs);
+}
+
+smob_status smob_far_pairs_set(const smob_ctx* c, int hp, long long* direct, long long* evaluated,
+                               long long* coarse_macs) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
+        need(hp == 0 || hp == 1, "hp must be 0 (FP32 set) or 1 (float-float set)");
         // the FP32 kernels' choices replayed on the host for the current work items. With coarse
         // targets, every entry's work items: a candidate counts if its pair takes the entry's level
         // (coarse nodes or the grid points) and is read from the source's level for that target sphere
         // or its grid. Without, the grid items: a source sphere is skipped when every target skips it,
         // read from its grid points when some target needs them, else from the finest coarse level
-        // any target votes for.
-        const smob_ctx::CoarseHost& h = c->c32;
+        // any target votes for. The float-float set (hp = 1) replays the fused float-float pass the same
+        // way (its entries, or without coarse targets its votes over items_df).
+        const smob_ctx::CoarseHost& h = hp ? c->chp : c->c32;
         const double leps = h.eps > 0 ? std::log(h.eps) : 0.0;
         auto dist = [&](int t, int s) {
             double d2 = 0;
@@ -2835,7 +2850,7 @@ smob_status smob_far_pairs(const smob_ctx* c, long long* direct, long long* eval
                 if (e.l >= 0) macs += 3LL * c->glen[e.t] * e.n;  // interpolation to the grid
         } else {
             std::vector<std::pair<int, int>> tsph;  // (target sphere, targets of it in the item)
-            for (const FarItem& it : c->items32) {
+            for (const FarItem& it : (hp ? c->items_df : c->items32)) {
                 tsph.clear();
                 for (int t = it.t0; t < it.t1; ++t) {
                     const int ts = c->sid[t];

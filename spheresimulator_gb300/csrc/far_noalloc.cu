@@ -39,8 +39,17 @@ constexpr int kNoAllocMaxDevices = 64;
 // needs to start at zero: each call writes every entry it later reads (all chunks x all targets).
 static __device__ __align__(256) double g_far_noalloc_scratch[kNoAllocChunks * kNoAllocMaxPoints * 3];
 
+// Scratch addresses looked up so far, one per (device, CUDA context): the address of a __device__
+// array belongs to the context that loaded the module, so a non-primary context on the same device,
+// or the primary context created again after cudaDeviceReset, has its own.
+struct ScratchAddr {
+    int dev;
+    void* ctx;
+    double* addr;
+};
 std::mutex g_setup_mu;
-double* g_scratch_addr[kNoAllocMaxDevices] = {};
+ScratchAddr g_scratch_addr[kNoAllocMaxDevices] = {};
+int g_scratch_count = 0;
 
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_far_noalloc_partial(const double* __restrict__ coords, const double* __restrict__ norms,
@@ -85,6 +94,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
                 if (ss[k] == sid) continue;
                 const double rx = tx - sp[3 * k], ry = ty - sp[3 * k + 1], rz = tz - sp[3 * k + 2];
                 const double r2 = rx * rx + ry * ry + rz * rz;
+                if (r2 == 0) continue;  // a point of another sphere at the target itself adds nothing
                 const double ri = rsqrt(r2);
                 const double ri2 = ri * ri;
                 const double rf = rx * sf[3 * k] + ry * sf[3 * k + 1] + rz * sf[3 * k + 2];
@@ -119,17 +129,51 @@ __global__ void k_far_noalloc_reduce(const double* __restrict__ partial, int n, 
     out[3 * t + 2] += pre * sz;
 }
 
-// Device address of the scratch array for the current device. Host code cannot use the symbol
-// itself as a pointer (it names a host-side shadow); the address is looked up once per device.
-smob_status scratch_for_current_device(double** ptr) {
+// The current CUDA context (driver cuCtxGetCurrent, reached through the runtime so that the library
+// does not link libcuda); nullptr if it cannot be queried.
+void* current_context() {
+    using Fn = int (*)(void**);
+    static Fn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<Fn>(f);
+    }();
+    void* ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of the scratch array in the current context. Host code cannot use the symbol
+// itself as a pointer (it names a host-side shadow). Outside stream capture the address is looked
+// up with cudaGetSymbolAddress on every call (a lookup in the runtime's table once the module is
+// loaded), so a reset device or another context gets its own address; during capture, where that
+// call may have to load the module, the address cached for the current (device, context) is used,
+// and a context without one is refused.
+smob_status scratch_for_call(cudaStream_t st, double** ptr) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
         cudaGetLastError();
         smob::set_last_error("smob_far_traction_noalloc: no usable current CUDA device");
         return SMOB_ERR_NO_DEVICE;
     }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    bool capturing = false;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        capturing = true;  // the legacy stream while another thread captures: treat as capture
+    } else {
+        capturing = cs != cudaStreamCaptureStatusNone;
+    }
+    void* ctx = current_context();
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    ScratchAddr* slot = nullptr;
+    for (int i = 0; i < g_scratch_count; ++i)
+        if (g_scratch_addr[i].dev == dev && g_scratch_addr[i].ctx == ctx) slot = &g_scratch_addr[i];
+    if (!capturing) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_far_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
@@ -137,9 +181,19 @@ smob_status scratch_for_current_device(double** ptr) {
             smob::set_last_error("smob_far_traction_noalloc: cudaGetSymbolAddress of the scratch array failed");
             return SMOB_ERR_CUDA;
         }
-        g_scratch_addr[dev] = static_cast<double*>(p);
+        if (!slot) {
+            // full table (more contexts than kNoAllocMaxDevices): reuse the oldest entry
+            slot = &g_scratch_addr[g_scratch_count < kNoAllocMaxDevices ? g_scratch_count++ : 0];
+            slot->dev = dev;
+            slot->ctx = ctx;
+        }
+        slot->addr = static_cast<double*>(p);
+    } else if (!slot) {
+        smob::set_last_error("smob_far_traction_noalloc: the first call in a CUDA context must come before any "
+                             "stream capture (it looks up the scratch array's device address)");
+        return SMOB_ERR_STATE;
     }
-    *ptr = g_scratch_addr[dev];
+    *ptr = slot->addr;
     return SMOB_OK;
 }
 
@@ -157,9 +211,9 @@ extern "C" smob_status smob_far_traction_noalloc(const double* d_coords, const d
         return SMOB_ERR_ARG;
     }
     double* scratch = nullptr;
-    const smob_status s = scratch_for_current_device(&scratch);
-    if (s != SMOB_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const smob_status s = scratch_for_call(st, &scratch);
+    if (s != SMOB_OK) return s;
     const dim3 grid((n_points + kNoAllocThreads - 1) / kNoAllocThreads, kNoAllocChunks);
     k_far_noalloc_partial<<<grid, kNoAllocThreads, 0, st>>>(d_coords, d_norms, d_weights, d_density, d_sphere, n_points,
                                                             c, scratch);

@@ -818,7 +818,8 @@ __global__ void k_ct_sum(DevGeom g, const float* __restrict__ partial) {
 // node values are staged kCiK nodes at a time in shared memory. Two entries per tile: the map stays in
 // L2 and more CTAs hide its latency (one CTA per SM with 8 entries on cfg2). Each entry's result goes
 // to its level slot of ctinterp.
-constexpr int kCiEnt = 2, kCiK = 32;
+constexpr int kCiK = 32;  // entries per tile: kCiEnt; grid points per tile: kCiPts (one per thread)
+static_assert(kCiPts == 128, "k_ct_interp runs one grid point per thread of 128");
 __global__ void __launch_bounds__(128) k_ct_interp(DevGeom g) {
     const CoarseSet& cs = g.cs32;
     const CtITile d = cs.ctitile[blockIdx.x];
@@ -1272,7 +1273,8 @@ __global__ void k_ct_sum_df(DevGeom g, const double* __restrict__ partial) {
 // 1/58 of them): maps stored as (hi, lo) float pairs, the entries' node values split into (hi, lo) in
 // shared memory, products by df_mul_u and sums by df_acc (~2^-44 relative to the sum of |terms|).
 // CTA tile: 256 grid points (two per thread, the packed lanes) x kCiEntD entries x 6 components.
-constexpr int kCiEntD = 1, kCiKD = 8;  // one entry per tile: 2x the CTAs of two (177 on cfg2, 152 SMs)
+constexpr int kCiKD = 8;  // kCiEntD = 1 entry per tile: 2x the CTAs of two (177 on cfg2, 152 SMs)
+static_assert(kCiPtsD == 2 * 128, "k_ct_interp_df runs two grid points per thread of 128");
 __global__ void __launch_bounds__(128) k_ct_interp_df(DevGeom g) {
     const CoarseSet& cs = g.cshp;
     const CtITile d = cs.ctitile[blockIdx.x];

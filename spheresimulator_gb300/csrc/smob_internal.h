@@ -35,6 +35,11 @@ constexpr int kNearSetsTrac = 25;        // div L, Hessians of L_x,L_y,L_z,L_r
 constexpr int kNearSetsSL = 15;          // L_j, grad L_j, grad L_r
 constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per sphere (FP32 far field)
 constexpr int kCoarseTileNodes = 32;     // coarse nodes per CTA of the coarse-strength GEMMs (multiple of 16)
+// interpolation tiles of the coarse targets (the host lists at most this many entries per tile; the
+// kernels k_ct_interp / k_ct_interp_df read exactly these): FP32 set 2 entries x 128 grid points,
+// float-float set 1 entry x 256 grid points (two per thread)
+constexpr int kCiEnt = 2, kCiPts = 128;
+constexpr int kCiEntD = 1, kCiPtsD = 256;
 
 __host__ __device__ inline int ncoef(int p) { return (p + 1) * (p + 2) / 2; }
 __host__ __device__ inline int cidx(int n, int m) { return n * (n + 1) / 2 + m; }

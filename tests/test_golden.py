@@ -61,3 +61,37 @@ def test_cuda_matches_golden():
     assert rel(op.apply(c["x"]), c["apply"]) < 1e-11
     mob = SphereSTKMobMat(c["centers"], c["radii"], c["orders"], quats=c["quats"])
     assert rel(mob.solveMob(c["force"], tol=1e-12), c["vel"]) < 1e-9
+
+
+def test_scale_fixtures_match_their_generators():
+    """The at-scale solve fixtures (tests/golden/make_golden.py --scale) hold the inputs that the
+    seeded generators still produce, and their oracle answers are finite and physically sized."""
+    import sys
+    sys.path.insert(0, HERE)
+    import make_golden as M
+    from spheresimulator_gb300 import configs
+    c2 = load("golden_cfg2_solve.npz")
+    ref = configs.cfg2()
+    assert np.array_equal(c2["centers"], ref["centers"]) and np.array_equal(c2["force"], ref["force"])
+    c3 = load("golden_poly48.npz")
+    ref = configs.cfg3(seed=38, n=48, box=14.0)
+    assert np.array_equal(c3["centers"], ref["centers"]) and np.array_equal(c3["radii"], ref["radii"])
+    b = load("golden_batch6.npz")
+    ref = configs.cfg4(seed=41, n_problems=6, nmax=24)
+    assert np.array_equal(b["centers"], ref["centers"]) and np.array_equal(b["problem"], ref["problem"])
+    q = load("golden_p24.npz")
+    ref = configs.cfg5_request(np.random.default_rng(24), nmin=20, nmax=20, orders=(24,))
+    assert np.array_equal(q["centers"], ref["centers"]) and np.array_equal(q["force"], ref["force"])
+    s = load("golden_seq12.npz")
+    cl, cols, in_span, fresh, vstep, dt, c1, q1 = M.seq12()
+    assert np.array_equal(s["cols"], cols) and np.array_equal(s["centers_moved"], c1)
+    assert np.array_equal(s["quats_moved"], q1)
+    # linearity of the oracle's solutions: the in-span force's velocity is the same combination
+    combo = 0.6 * s["v_cols"][0] - 1.3 * s["v_cols"][1] + 0.25 * s["v_cols"][2]
+    assert rel(combo, s["v_span"]) < 1e-10
+    for f in (c2, c3, b, q):
+        V = f["vel"].reshape(-1, 6)
+        F = f["force"].reshape(-1, 6)
+        assert np.all(np.isfinite(V))
+        # dissipation: the mobility matrix is positive definite, F . V > 0
+        assert float((F * V).sum()) > 0

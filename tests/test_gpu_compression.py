@@ -150,9 +150,13 @@ def test_far_pairs_replay():
     direct = int(ng.sum() ** 2 - (ng ** 2).sum() - (ng[t] * ng[s]).sum())
     d, e, macs = g.far_pairs()
     assert d == direct and 0 < e < d and macs > 0
+    # the fused float-float pass's set: the same direct pairs, at most as many evaluated
+    dh, eh, mh = g.far_pairs(hp=True)
+    assert dh == direct and 0 < eh <= dh
     g.set_far_compression(0, 0)
     d0, e0, m0 = g.far_pairs()
     assert d0 == direct and e0 == direct and m0 == 0
+    assert g.far_pairs(hp=True)[:2] == (direct, direct)
 
 
 def test_coarse_targets_match_direct_sum():
