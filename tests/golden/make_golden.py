@@ -24,7 +24,7 @@ GPU solves at 1e-8 / 1e-6 are checked against), written by --scale:
                          right-hand sides), a force in their span and a new one (recycling), and a
                          time step (prescribed v, omega, dt) with the oracle solve on the moved geometry
 
-Run:  python tests/golden/make_golden.py [--scale]
+Run:  python tests/golden/make_golden.py [--scale [cfg2 poly48 batch6 p24 seq12]]
 """
 import os
 import sys
@@ -92,62 +92,73 @@ def seq12():
     cols = rng.standard_normal((3, 6 * 12))
     in_span = 0.6 * cols[0] - 1.3 * cols[1] + 0.25 * cols[2]
     fresh = rng.standard_normal(6 * 12)
-    vstep = 0.3 * rng.standard_normal((12, 6))
+    vstep = 0.1 * rng.standard_normal((12, 6))
     dt = 0.25
     c1 = cl["centers"] + vstep[:, :3] * dt
+    d = np.linalg.norm(c1[:, None] - c1[None], axis=-1) - cl["radii"][:, None] - cl["radii"][None]
+    assert d[~np.eye(12, dtype=bool)].min() > 0.1, "the step brings two spheres within 0.1 of each other"
     q1 = np.array([quat_step(cl["quats"][i], vstep[i, 3:], dt) for i in range(12)])
     return cl, cols, in_span, fresh, vstep, dt, c1, q1
 
 
-def scale():
+def scale(only=None):
+    """Writes the at-scale solve fixtures (all, or those named in `only`)."""
+    def want(name):
+        return not only or name in only
+
     def solve(centers, radii, orders, force, quats=None):
         op = O.Operator(centers, radii, orders, quats=quats)
         r = op.solve_mob(force, tol=1e-12, restart=50, maxit=2000)
         assert r["status"] == 0 and r["relres"] < 1e-12, (r["status"], r["relres"])
         return r
 
-    c2 = configs.cfg2()
-    r = solve(c2["centers"], c2["radii"], c2["orders"], c2["force"])
-    np.savez_compressed(os.path.join(HERE, "golden_cfg2_solve.npz"), centers=c2["centers"], radii=c2["radii"],
-                        orders=c2["orders"], force=c2["force"], vel=r["vel"], iters=r["iters"])
-    print("cfg2", r["iters"], r["relres"], flush=True)
+    if want("cfg2"):
+        c2 = configs.cfg2()
+        r = solve(c2["centers"], c2["radii"], c2["orders"], c2["force"])
+        np.savez_compressed(os.path.join(HERE, "golden_cfg2_solve.npz"), centers=c2["centers"], radii=c2["radii"],
+                            orders=c2["orders"], force=c2["force"], vel=r["vel"], iters=r["iters"])
+        print("cfg2", r["iters"], r["relres"], flush=True)
 
-    c3 = configs.cfg3(seed=38, n=48, box=14.0)
-    r = solve(c3["centers"], c3["radii"], c3["orders"], c3["force"])
-    np.savez_compressed(os.path.join(HERE, "golden_poly48.npz"), centers=c3["centers"], radii=c3["radii"],
-                        orders=c3["orders"], force=c3["force"], vel=r["vel"], iters=r["iters"])
-    print("poly48", r["iters"], r["relres"], flush=True)
+    if want("poly48"):
+        c3 = configs.cfg3(seed=38, n=48, box=14.0)
+        r = solve(c3["centers"], c3["radii"], c3["orders"], c3["force"])
+        np.savez_compressed(os.path.join(HERE, "golden_poly48.npz"), centers=c3["centers"], radii=c3["radii"],
+                            orders=c3["orders"], force=c3["force"], vel=r["vel"], iters=r["iters"])
+        print("poly48", r["iters"], r["relres"], flush=True)
 
-    b = configs.cfg4(seed=41, n_problems=6, nmax=24)
-    vel = np.zeros_like(b["force"])
-    for k in range(6):
-        m = b["problem"] == k
-        m6 = np.repeat(m, 6)
-        vel[m6] = solve(b["centers"][m], b["radii"][m], b["orders"][m], b["force"][m6])["vel"]
-    np.savez_compressed(os.path.join(HERE, "golden_batch6.npz"), centers=b["centers"], radii=b["radii"],
-                        orders=b["orders"], problem=b["problem"], force=b["force"], vel=vel)
-    print("batch6", flush=True)
+    if want("batch6"):
+        b = configs.cfg4(seed=41, n_problems=6, nmax=24)
+        vel = np.zeros_like(b["force"])
+        for k in range(6):
+            m = b["problem"] == k
+            m6 = np.repeat(m, 6)
+            vel[m6] = solve(b["centers"][m], b["radii"][m], b["orders"][m], b["force"][m6])["vel"]
+        np.savez_compressed(os.path.join(HERE, "golden_batch6.npz"), centers=b["centers"], radii=b["radii"],
+                            orders=b["orders"], problem=b["problem"], force=b["force"], vel=vel)
+        print("batch6", flush=True)
 
-    q = configs.cfg5_request(np.random.default_rng(24), nmin=20, nmax=20, orders=(24,))
-    r = solve(q["centers"], q["radii"], q["orders"], q["force"])
-    np.savez_compressed(os.path.join(HERE, "golden_p24.npz"), centers=q["centers"], radii=q["radii"],
-                        orders=q["orders"], force=q["force"], vel=r["vel"], iters=r["iters"])
-    print("p24", r["iters"], r["relres"], flush=True)
+    if want("p24"):
+        q = configs.cfg5_request(np.random.default_rng(24), nmin=20, nmax=20, orders=(24,))
+        r = solve(q["centers"], q["radii"], q["orders"], q["force"])
+        np.savez_compressed(os.path.join(HERE, "golden_p24.npz"), centers=q["centers"], radii=q["radii"],
+                            orders=q["orders"], force=q["force"], vel=r["vel"], iters=r["iters"])
+        print("p24", r["iters"], r["relres"], flush=True)
 
-    cl, cols, in_span, fresh, vstep, dt, c1, q1 = seq12()
-    v_cols = np.stack([solve(cl["centers"], cl["radii"], cl["orders"], f, cl["quats"])["vel"] for f in cols])
-    v_span = solve(cl["centers"], cl["radii"], cl["orders"], in_span, cl["quats"])["vel"]
-    v_fresh = solve(cl["centers"], cl["radii"], cl["orders"], fresh, cl["quats"])["vel"]
-    v_moved = solve(c1, cl["radii"], cl["orders"], cols[0], q1)["vel"]
-    np.savez_compressed(os.path.join(HERE, "golden_seq12.npz"), centers=cl["centers"], radii=cl["radii"],
-                        orders=cl["orders"], quats=cl["quats"], cols=cols, v_cols=v_cols, in_span=in_span,
-                        v_span=v_span, fresh=fresh, v_fresh=v_fresh, vstep=vstep, dt=dt, centers_moved=c1,
-                        quats_moved=q1, v_moved=v_moved)
-    print("seq12", flush=True)
+    if want("seq12"):
+        cl, cols, in_span, fresh, vstep, dt, c1, q1 = seq12()
+        v_cols = np.stack([solve(cl["centers"], cl["radii"], cl["orders"], f, cl["quats"])["vel"] for f in cols])
+        v_span = solve(cl["centers"], cl["radii"], cl["orders"], in_span, cl["quats"])["vel"]
+        v_fresh = solve(cl["centers"], cl["radii"], cl["orders"], fresh, cl["quats"])["vel"]
+        v_moved = solve(c1, cl["radii"], cl["orders"], cols[0], q1)["vel"]
+        np.savez_compressed(os.path.join(HERE, "golden_seq12.npz"), centers=cl["centers"], radii=cl["radii"],
+                            orders=cl["orders"], quats=cl["quats"], cols=cols, v_cols=v_cols, in_span=in_span,
+                            v_span=v_span, fresh=fresh, v_fresh=v_fresh, vstep=vstep, dt=dt, centers_moved=c1,
+                            quats_moved=q1, v_moved=v_moved)
+        print("seq12", flush=True)
 
 
 if __name__ == "__main__":
     if "--scale" in sys.argv:
-        scale()
+        scale([a for a in sys.argv[1:] if not a.startswith("--")])
     else:
         main()
