@@ -237,6 +237,19 @@ def run_native(args, world, rank, local, dist):
     mob.profile_reset()
     solve_dev(PREC_MIXED)
     prof = mob.profile_table()
+    # the same solve with the other FP32 near-field kernel, then the other FP32 sphere-operator kernel
+    # (tensor cores vs SIMT pipes), each against the defaults
+    near_tc0, sph_tc0 = mob.near_tc(), mob.sphere_tc()
+    mob.set_near_tc(not near_tc0)
+    mob.profile_reset()
+    solve_dev(PREC_MIXED)
+    prof_near_alt = mob.profile_table()
+    mob.set_near_tc(near_tc0)
+    mob.set_sphere_tc(not sph_tc0)
+    mob.profile_reset()
+    solve_dev(PREC_MIXED)
+    prof_sph_alt = mob.profile_table()
+    mob.set_sphere_tc(sph_tc0)
     mob.profile(False)
     f32, f64 = ctypes.c_double(), ctypes.c_double()
     N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
@@ -368,6 +381,15 @@ def run_native(args, world, rank, local, dist):
             "avg_launch_ms": round(avg_df * 1e3, 5), "launches_in_profiled_solve": d_l,
             "share_of_kernel_time": round(d_ms / tot_prof, 4) if tot_prof else None},
         "kernel_ms_profiled_solve": {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items())},
+        "tensor_cores": {
+            "near_eval_trac_ms_tc_simt": [round((prof if near_tc0 else prof_near_alt).get("near_eval_trac", (0, 0.0))[1], 4),
+                                          round((prof_near_alt if near_tc0 else prof).get("near_eval_trac", (0, 0.0))[1], 4)],
+            "sphere_self_ms_tc_simt": [round((prof if sph_tc0 else prof_sph_alt).get("sphere_self", (0, 0.0))[1], 4),
+                                       round((prof_sph_alt if sph_tc0 else prof).get("sphere_self", (0, 0.0))[1], 4)],
+            "default_near_tc": near_tc0, "default_sphere_tc": sph_tc0,
+            "note": "per profiled mixed solve (serialised CUDA-event times), tcgen05 kernels vs SIMT kernels: the "
+                    "FP32 near-field contraction as a TF32 GEMM (k_near_eval_tc) and the FP32 sphere operator "
+                    "with its Legendre stage as TF32 GEMMs (k_legendre_tc), 3xTF32 split"},
         "autotune": {"fp32_targets_per_thread": tpt.value, "variant_ms_tpt_1_2_4": [round(v, 4) for v in tms],
                      "from_cache": bool(tcache.value),
                      "note": "tile of the FP32 grid kernels, tuned when a context first runs them (here the "
@@ -806,16 +828,20 @@ def far_once():
 
 
 def near_once():
-    """One near-field pass (FP32 traction, then FP64 traction) on the first 64 problems of cfg4: the
-    batched shape, where every target point has near pairs and the kernel runs one lane per target."""
+    """One near-field pass (FP32 traction on the tensor cores, FP64 traction, FP32 traction on the SIMT
+    pipes) on the first 64 problems of cfg4: the batched shape, where every target point has near pairs."""
     from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
     c = configs.cfg4(n_problems=64)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"], problem=c["problem"])
     x = np.random.default_rng(0).standard_normal(3 * g.n_points)
     a = g.near_field(x, cTrac=1.0, precision=PREC_MIXED)
     b = g.near_field(x, cTrac=1.0, precision=PREC_FP64)
+    g.set_near_tc(False)
+    g.set_sphere_tc(False)
+    c = g.near_field(x, cTrac=1.0, precision=PREC_MIXED)  # the SIMT kernels, for the launch list
     print(json.dumps({"near_once": "cfg4[:64]", "points": int(g.n_points), "near_pairs": int(g.n_near_pairs),
-                      "rel_diff_fp32_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b))}))
+                      "rel_diff_fp32_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                      "rel_diff_simt_fp64": float(np.linalg.norm(c - b) / np.linalg.norm(b))}))
 
 
 def main():

@@ -328,6 +328,19 @@ smob_status smob_set_graphs(smob_ctx* ctx, int on);
 /* far-field tile shape chosen by the autotuner at smob_create: FP32 targets per thread (1, 2 or 4),
  * the measured milliseconds of the three variants (0 when the choice came from the process cache) */
 smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* variant_ms, int* from_cache);
+/* FP32 near field on the tensor cores (default 1): the contraction of each target point's solid
+ * harmonics with a near source sphere's coefficient sets runs as a tcgen05 TF32 GEMM (3xTF32 split,
+ * ~FP32 accuracy); 0 selects the SIMT kernel (same mathematics, FP32 multiply-adds). FP64 and
+ * near-singular pairs always use the FP64 SIMT kernel. */
+smob_status smob_set_near_tc(smob_ctx* ctx, int on);
+/* FP32 sphere operator (self terms of the FP32 passes) with the Legendre stage of its transforms on the
+ * tensor cores: per order and m, the forward and inverse Legendre sums of up to 21 spheres as tcgen05
+ * TF32 GEMMs (3xTF32 split), between per-sphere phi-DFT kernels (three launches per pass). Default 0:
+ * the single SIMT kernel per sphere, which is faster at these sizes (the Legendre sums are a small part
+ * of it). FP64 passes always use the FP64 SIMT kernel. */
+smob_status smob_set_sphere_tc(smob_ctx* ctx, int on);
+/* the current choices of smob_set_near_tc and smob_set_sphere_tc (either pointer may be NULL) */
+smob_status smob_tc_info(const smob_ctx* ctx, int* near_tc, int* sphere_tc);
 /* override the autotuner's choice (1, 2 or 4 FP32 targets per thread); every variant computes each
  * pair in the same order, so results change only by FP32 rounding in the sums of skipped sources */
 smob_status smob_set_far_tile(smob_ctx* ctx, int targets_per_thread);

@@ -15,7 +15,11 @@ def build(force=False, verbose=False):
             os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "smob_oracle.h"))):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fno-math-errno", "-fPIC", "-shared", "-o", tmp, SRC]
+    # -ffp-contract=off: every product and sum rounded as written, on x86 and on Arm alike (GCC fuses
+    # them into FMAs by default where the target has FMA), so boundary decisions such as the near-pair
+    # rule are the IEEE evaluation of the expression
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fno-math-errno", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", tmp, SRC]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

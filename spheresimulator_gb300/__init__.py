@@ -107,8 +107,11 @@ class _Context:
         self.n_near_pairs = nnp.value
 
     def geometry(self):
-        """(centres [N,3], unit quaternions [N,4]) of the current geometry."""
-        return self.centers.copy(), self.quats.copy()
+        """(centres [N,3], unit quaternions [N,4]) of the current geometry, as the library holds it."""
+        c = np.zeros((self.n_spheres, 3))
+        q = np.zeros((self.n_spheres, 4))
+        N.check(self._L.smob_get_geometry(self._h, N.dptr(c), N.dptr(q)))
+        return c, q
 
     def step_euler(self, vel, dt):
         """Advance every sphere by its velocity/angular velocity (6N, as solveMob returns) over dt."""
@@ -176,6 +179,26 @@ class _Context:
     def set_graphs(self, on=True):
         """CUDA graphs for the Arnoldi steps of the solves (on by default)."""
         N.check(self._L.smob_set_graphs(self._h, int(on)))
+
+    def near_tc(self):
+        """True if the FP32 near field runs on the tensor cores"""
+        v = ctypes.c_int()
+        N.check(self._L.smob_tc_info(self._h, ctypes.byref(v), None))
+        return bool(v.value)
+
+    def sphere_tc(self):
+        """True if the FP32 sphere operator runs its Legendre stage on the tensor cores"""
+        v = ctypes.c_int()
+        N.check(self._L.smob_tc_info(self._h, None, ctypes.byref(v)))
+        return bool(v.value)
+
+    def set_sphere_tc(self, on=True):
+        """FP32 sphere operator with its Legendre stage on the tensor cores (default) or the SIMT kernel"""
+        N.check(self._L.smob_set_sphere_tc(self._h, int(bool(on))))
+
+    def set_near_tc(self, on=True):
+        """FP32 near field on the tensor cores (default) or on the SIMT pipes"""
+        N.check(self._L.smob_set_near_tc(self._h, int(bool(on))))
 
     def set_far_tile(self, targets_per_thread):
         """Force the FP32 far-field variant (1, 2 or 4 targets per thread) over the autotuner's choice."""

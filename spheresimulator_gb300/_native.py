@@ -131,6 +131,9 @@ def lib():
         "smob_tuning": (S, [_VP, _IP, _DP, _IP]),
         "smob_set_graphs": (S, [_VP, ctypes.c_int]),
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
+        "smob_set_near_tc": (S, [_VP, ctypes.c_int]),
+        "smob_set_sphere_tc": (S, [_VP, ctypes.c_int]),
+        "smob_tc_info": (S, [_VP, _IP, _IP]),
         "smob_recycle_info": (S, [_VP, _IP, _IP]),
         "smob_set_far_compression": (S, [_VP, ctypes.c_double, ctypes.c_double]),
         "smob_set_far_coarse_targets": (S, [_VP, ctypes.c_int]),

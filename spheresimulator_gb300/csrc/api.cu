@@ -181,6 +181,14 @@ struct smob_ctx {
     DBuf d_tab_d, d_tab_f, d_map_rowptr, d_map_col, d_map_val_d, d_map_val_f, d_items32, d_items64, d_items_df, d_chunks,
         d_items_rep;
     DBuf d_active;
+    DBuf d_err;            // device error word (DevGeom::err)
+    bool near_tc = true;   // FP32 near field on the tensor cores
+    // FP32 sphere operator with the Legendre stage on the tensor cores: off by default, measured slower
+    // than the single-kernel SIMT operator (three launches per pass against one; cfg2 2.1 vs 1.1 ms per
+    // solve, a 64-problem batch 0.54 vs 0.21 ms per pass)
+    bool sph_tc = false;
+    int n_leg_tiles = 0;
+    DBuf d_leg_tiles, d_leg_sph, d_leg_tab, d_leg_off, d_fgbuf, d_lopbuf;
     // operator workspace
     DBuf d_src32, d_src64, d_partial32, d_partial64, d_coef32, d_coef64, d_sets32, d_sets64;
     // far field from coarse equivalent sources: the FP32 set and the float-float set (eps <= 0: off)
@@ -373,60 +381,75 @@ void unit_quat(const double* q, double* out, int i) {
 }
 
 // ---------------------------------------------------------------- context set-up
-// spheres of one problem must not overlap or touch (centres in `centers`, radii of the context)
-void check_overlap(const smob_ctx* c, const std::vector<double>& centers) {
-    for (const auto& pr : c->problems)
-        for (int t = pr.s0; t < pr.s1; ++t)
-            for (int s = t + 1; s < pr.s1; ++s) {
-                double r2 = 0;
-                for (int k = 0; k < 3; ++k) {
-                    const double d = centers[3 * s + k] - centers[3 * t + k];
-                    r2 += d * d;
-                }
-                if (std::sqrt(r2) <= c->radii[s] + c->radii[t])
-                    throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(s) +
-                                                      " overlap or touch");
-            }
+// Spheres of one problem must not overlap or touch: checked on the device (k_overlap) for the
+// centres d_centers with the context's radii and problems (d_radius, d_prob, d_problems uploaded);
+// throws with the first such pair in (t, s) order and changes nothing.
+void check_overlap(smob_ctx* c, const double* d_centers) {
+    DBuf first;
+    first.alloc(sizeof(unsigned long long));
+    CUDA_OK(cudaMemsetAsync(first.p, 0xff, sizeof(unsigned long long), c->st));
+    check_launch(c, launch_overlap_check(d_centers, c->d_radius.as<double>(), c->d_prob.as<int>(),
+                                         c->d_problems.as<Problem>(), c->N, first.as<unsigned long long>(), c->st));
+    unsigned long long h = 0;
+    CUDA_OK(cudaMemcpyAsync(&h, first.p, sizeof(h), cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    if (h != ~0ULL) {
+        const long long t = (long long)(h / (unsigned long long)c->N), sp = (long long)(h % (unsigned long long)c->N);
+        throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(sp) +
+                                          " overlap or touch");
+    }
 }
 
-// near pairs (MPI/NearInteraction.txx:430-447; Rad = 1.5*radius, SphereSTKSHOperator.cpp:547),
-// within each problem, sorted by target then source; near-singular flags; near-source slots
+// Near pairs (MPI/NearInteraction.txx:430-447; Rad = 1.5*radius, SphereSTKSHOperator.cpp:547) within
+// each problem, built on the device from d_center (nbrlist.cu): CSR by target with sources ascending,
+// near-singular flags, near-source slots in sphere order. The host keeps a copy of these O(N + pairs)
+// arrays for the bookkeeping that reads them (near maps per order, coarse-level candidates, counts).
 void build_near(smob_ctx* c) {
     const int N = c->N;
-    c->nbr_start.assign(N + 1, 0);
-    c->nbr_src.clear();
-    c->nbr_precise.clear();
-    for (const auto& pr : c->problems)
-        for (int t = pr.s0; t < pr.s1; ++t) {
-            for (int s = pr.s0; s < pr.s1; ++s) {
-                double r2 = 0;
-                for (int k = 0; k < 3; ++k) {
-                    const double d = c->centers[3 * s + k] - c->centers[3 * t + k];
-                    r2 += d * d;
-                }
-                const double Rn = 1.5 * c->radii[s] + 1.5 * c->radii[t];
-                if (r2 > 0 && r2 < Rn * Rn) {
-                    c->nbr_src.push_back(s);
-                    const double gap = std::sqrt(r2) - c->radii[s] - c->radii[t];
-                    c->nbr_precise.push_back(gap < 0.1 * std::min(c->radii[s], c->radii[t]) ? 1 : 0);
-                }
-            }
-            c->nbr_start[t + 1] = (int)c->nbr_src.size();
-        }
-    c->near_src_slot.assign(N, -1);
-    c->slot_sphere.clear();
-    for (int s : c->nbr_src)
-        if (c->near_src_slot[s] < 0) {
-            c->near_src_slot[s] = (int)c->slot_sphere.size();
-            c->slot_sphere.push_back(s);
-        }
-    std::sort(c->slot_sphere.begin(), c->slot_sphere.end());
-    for (size_t k = 0; k < c->slot_sphere.size(); ++k) c->near_src_slot[c->slot_sphere[k]] = (int)k;
+    DBuf count, totals;
+    count.alloc(sizeof(int) * std::max(N, 1));
+    totals.alloc(2 * sizeof(int));
+    c->d_nbr_start.alloc(sizeof(int) * (N + 1));
+    c->d_near_slot.alloc(sizeof(int) * std::max(N, 1));
+    const double* ctr = c->d_center.as<double>();
+    const double* rad = c->d_radius.as<double>();
+    check_launch(c, launch_nbr_count(ctr, rad, c->d_prob.as<int>(), c->d_problems.as<Problem>(), N, count.as<int>(),
+                                     c->st));
+    check_launch(c, launch_nbr_scan(count.as<int>(), N, c->d_nbr_start.as<int>(), c->d_near_slot.as<int>(),
+                                    totals.as<int>(), c->st));
+    int tot[2] = {0, 0};
+    CUDA_OK(cudaMemcpyAsync(tot, totals.p, sizeof(tot), cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    c->d_nbr_src.alloc(sizeof(int) * std::max(tot[0], 1));
+    c->d_nbr_precise.alloc(std::max(tot[0], 1));
+    c->d_slot_sphere.alloc(sizeof(int) * std::max(tot[1], 1));
+    check_launch(c, launch_nbr_fill(ctr, rad, c->d_prob.as<int>(), c->d_problems.as<Problem>(), N,
+                                    c->d_nbr_start.as<int>(), c->d_near_slot.as<int>(), c->d_nbr_src.as<int>(),
+                                    c->d_nbr_precise.as<unsigned char>(), c->d_slot_sphere.as<int>(), c->st));
+    c->nbr_start.resize(N + 1);
+    c->nbr_src.resize(tot[0]);
+    c->nbr_precise.resize(tot[0]);
+    c->near_src_slot.resize(N);
+    c->slot_sphere.resize(tot[1]);
+    CUDA_OK(cudaMemcpyAsync(c->nbr_start.data(), c->d_nbr_start.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost,
+                            c->st));
+    if (tot[0] > 0) {
+        CUDA_OK(cudaMemcpyAsync(c->nbr_src.data(), c->d_nbr_src.p, sizeof(int) * tot[0], cudaMemcpyDeviceToHost, c->st));
+        CUDA_OK(cudaMemcpyAsync(c->nbr_precise.data(), c->d_nbr_precise.p, tot[0], cudaMemcpyDeviceToHost, c->st));
+    }
+    if (N > 0)
+        CUDA_OK(cudaMemcpyAsync(c->near_src_slot.data(), c->d_near_slot.p, sizeof(int) * N, cudaMemcpyDeviceToHost,
+                                c->st));
+    if (tot[1] > 0)
+        CUDA_OK(cudaMemcpyAsync(c->slot_sphere.data(), c->d_slot_sphere.p, sizeof(int) * tot[1],
+                                cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
 }
 
 void problem_origins(smob_ctx* c);
 void upload_near(smob_ctx* c);
 void build_tables(smob_ctx* c);
+void build_leg(smob_ctx* c);
 void bind_geom(smob_ctx* c);
 void build_coarse(smob_ctx* c);
 void coarse_grids(smob_ctx* c);
@@ -536,7 +559,13 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
         pr.v1 = 3 * pr.p1;
     }
 
-    check_overlap(c, c->centers);
+    // what the device neighbour list and overlap check read (the problems are uploaded again below,
+    // with their far-field and reduction fields)
+    c->d_center.upload(c->centers);
+    c->d_radius.upload(c->radii);
+    c->d_prob.upload(c->prob);
+    c->d_problems.upload(c->problems);
+    check_overlap(c, c->d_center.as<double>());
     build_near(c);
     const int ndmax = ncoef(c->pmax + 3);
     c->set_stride_trac = 2LL * kNearSetsTrac * ndmax;
@@ -592,6 +621,7 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     }
 
     build_tables(c);
+    build_leg(c);
 
     // point data: FP64 lab-frame grid and the far-field copies relative to each problem's origin
     // (centre of its sphere bounding box), all written by the regrid kernel below
@@ -622,6 +652,8 @@ void build_context(smob_ctx* c, const smob_geometry* geo) {
     c->d_chunks.upload(c->chunks);
     std::vector<unsigned char> act(c->P, 1);
     c->d_active.upload(act);
+    c->d_err.alloc(sizeof(int));
+    CUDA_OK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->st));
 
     // operator workspace
     c->d_src32.alloc(sizeof(float4) * c->M);
@@ -659,17 +691,18 @@ void problem_origins(smob_ctx* c) {
     }
 }
 
-// near lists, slots and the near-set workspace to the device; near lanes for this geometry
+// the near-set workspace for this geometry's near sources; near lanes of the SIMT near kernel
 void upload_near(smob_ctx* c) {
-    c->d_nbr_start.upload(c->nbr_start);
-    c->d_nbr_src.upload(c->nbr_src);
-    c->d_nbr_precise.upload(c->nbr_precise);
+    // (the lists themselves were built on the device by build_near)
     c->n_precise = 0;
     for (unsigned char v : c->nbr_precise) c->n_precise += v;
-    c->d_near_slot.upload(c->near_src_slot);
-    c->d_slot_sphere.upload(c->slot_sphere);
     const size_t nsl = c->slot_sphere.size();
-    c->d_sets32.alloc(sizeof(float) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
+    // FP32 sets: [idx][set] for the SIMT kernel or the tiles of the tensor-core kernel, whose padding
+    // must read as zero (cleared here, on every geometry update and when the near kernel is switched)
+    const long long s32 = std::max({c->set_stride_trac, c->set_stride_sl, near_tile_stride(c->pmax, true),
+                                    near_tile_stride(c->pmax, false)});
+    c->d_sets32.alloc(sizeof(float) * std::max<size_t>(nsl, 1) * s32);
+    CUDA_OK(cudaMemsetAsync(c->d_sets32.p, 0, c->d_sets32.bytes, c->st));
     c->d_sets64.alloc(sizeof(double) * nsl * std::max(c->set_stride_trac, c->set_stride_sl));
     // near-field lanes per target: ~152 x 256 threads when few target points have near pairs (the
     // kernel runs beside the far field, which fills the rest of the GPU; more lanes repeat the
@@ -758,6 +791,66 @@ void build_tables(smob_ctx* c) {
     std::vector<float> mvalf(mval.begin(), mval.end());
     c->d_map_val_f.upload(mvalf);
     c->map_orders = near_p;
+}
+
+// Tensor-core Legendre stage of the FP32 sphere operator (k_legendre_tc): tiles of up to 21 spheres of
+// one order, and per present order p and m the B operand tables in the tc_sm100.h operand layout,
+// chunks of 32 K values: forward rows n = m..p (padded to 16), K = (block b, ring j) -> w_j times P, dP
+// or m Ps at (j, n, m); inverse rows j = 0..p (padded to 16), K = (block b, n - m) -> the same tables
+// unweighted. Depends only on the orders.
+void build_leg(smob_ctx* c) {
+    constexpr int kSpt = 21, kK = 32;
+    std::vector<int4> tiles;
+    std::vector<int> sph;
+    std::vector<float> tab;
+    std::vector<int> off(2 * (kMaxOrder + 1) * (kMaxOrder + 1), 0);
+    auto kmaj = [](int r, int k) { return ((r >> 3) * (kK >> 2) + (k >> 2)) * 32 + (r & 7) * 4 + (k & 3); };
+    for (int p = 1; p <= kMaxOrder; ++p) {
+        std::vector<int> list;
+        for (int i = 0; i < c->N; ++i)
+            if (c->orders[i] == p) list.push_back(i);
+        if (list.empty()) continue;
+        for (size_t a = 0; a < list.size(); a += kSpt)
+            tiles.push_back(make_int4(p, (int)(sph.size() + a), (int)std::min<size_t>(kSpt, list.size() - a), 0));
+        sph.insert(sph.end(), list.begin(), list.end());
+        const HostOrderTables& T = host_tables(p);
+        const int nt = p + 1, nc = T.nc;
+        const int KP = kK * ((3 * nt + kK - 1) / kK), nch = KP / kK;
+        for (int m = 0; m <= p; ++m) {
+            const int nn = p + 1 - m;
+            for (int dir = 0; dir < 2; ++dir) {
+                const int rows = dir == 0 ? nn : nt, NR = 16 * ((rows + 15) / 16);
+                off[2 * (p * (kMaxOrder + 1) + m) + dir] = (int)tab.size();
+                const size_t base = tab.size();
+                tab.resize(base + (size_t)nch * NR * kK, 0.f);
+                for (int r = 0; r < rows; ++r)
+                    for (int k = 0; k < 3 * nt; ++k) {
+                        const int b = k / nt, q = k - b * nt;
+                        int j, n;
+                        if (dir == 0) {
+                            n = m + r;
+                            j = q;
+                        } else {
+                            j = r;
+                            n = m + q;
+                            if (n > p) continue;
+                        }
+                        const int id = cidx(n, m);
+                        double v = b == 0 ? T.P[j * nc + id] : (b == 1 ? T.dP[j * nc + id] : m * T.Ps[j * nc + id]);
+                        if (dir == 0) v *= T.wq[j];
+                        tab[base + (size_t)(k / kK) * NR * kK + kmaj(r, k % kK)] = float(v);
+                    }
+            }
+        }
+    }
+    c->n_leg_tiles = (int)tiles.size();
+    c->d_leg_tiles.upload(tiles);
+    c->d_leg_sph.upload(sph);
+    c->d_leg_tab.upload(tab);
+    c->d_leg_off.upload(off);
+    const long long stride = 6LL * (c->pmax + 1) * (c->pmax + 1);
+    c->d_fgbuf.alloc(sizeof(float) * stride * std::max(c->N, 1));
+    c->d_lopbuf.alloc(sizeof(double) * 6 * std::max(c->N, 1));
 }
 
 // device pointers and sizes of the geometry, as the kernels receive them
@@ -1139,6 +1232,17 @@ void bind_geom(smob_ctx* c) {
     g.map_val_d = c->d_map_val_d.as<double>();
     g.map_val_f = c->d_map_val_f.as<float>();
     g.active = c->d_active.as<unsigned char>();
+    g.near_tc = c->near_tc ? 1 : 0;
+    g.err = c->d_err.as<int>();
+    g.sph_tc = c->sph_tc ? 1 : 0;
+    g.n_leg_tiles = c->n_leg_tiles;
+    g.leg_tiles = c->d_leg_tiles.as<int4>();
+    g.leg_sph = c->d_leg_sph.as<int>();
+    g.leg_tab = c->d_leg_tab.as<float>();
+    g.leg_off = c->d_leg_off.as<int>();
+    g.fgbuf = c->d_fgbuf.as<float>();
+    g.fg_stride = 6LL * (c->pmax + 1) * (c->pmax + 1);
+    g.lopbuf = c->d_lopbuf.as<double>();
     auto bind_set = [&](const smob_ctx::CoarseHost& h, CoarseSet& cs) {
         cs.ncent = (int)h.cent.size();
         cs.clog_eps = h.eps > 0 ? float(std::log(h.eps)) : 0.f;
@@ -1933,7 +2037,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         set_active(c, all);
     }
     CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
+    int dev_err = 0;
+    CUDA_OK(cudaMemcpyAsync(&dev_err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_OK(cudaStreamSynchronize(st));
+    if (dev_err != 0) {
+        CUDA_OK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), st));
+        throw SmobError(SMOB_ERR_CUDA, "a tensor-core near-field kernel gave up waiting for its MMAs (results void)");
+    }
 
     smob_status worst = SMOB_OK;
     for (int p = 0; p < P; ++p) {
@@ -1956,6 +2066,18 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     if (worst == SMOB_ERR_NONFINITE) g_err = "non-finite values in the mobility solve";
     else if (worst == SMOB_ERR_NOT_CONVERGED) g_err = "GMRES stopped at its iteration limit";
     return worst;
+}
+
+// Reads and clears the device error word (DevGeom::err) after the stream's work so far; a kernel
+// that gave up a bounded wait (tensor-core near field) wrote nothing, so the call's results are void.
+void check_device_error(smob_ctx* c) {
+    int h = 0;
+    CUDA_OK(cudaMemcpyAsync(&h, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    if (h != 0) {
+        CUDA_OK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->st));
+        throw SmobError(SMOB_ERR_CUDA, "a tensor-core near-field kernel gave up waiting for its MMAs (results void)");
+    }
 }
 
 template <typename F>
@@ -2029,9 +2151,14 @@ void quat_step(const double* q, const double* w, double dt, double* out) {
 // O(M) arrays). Throws (context unchanged) if spheres of a problem would overlap. The warm-start
 // solution is kept; captured graphs and several-RHS copies of the old geometry are dropped.
 void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std::vector<double>& quats) {
-    check_overlap(c, centers);
+    {
+        DBuf dc;
+        dc.upload(centers);
+        check_overlap(c, dc.as<double>());  // throws before anything changed
+    }
     c->centers = centers;
     c->quats = quats;
+    c->d_center.upload(c->centers);
     build_near(c);
     std::vector<char> near_p(kMaxOrder + 1, 0);
     for (int s : c->slot_sphere) near_p[c->orders[s]] = 1;
@@ -2067,7 +2194,7 @@ void host_io(smob_ctx* c, const double* in, double* out, bool load_out, F&& f) {
     else CUDA_OK(cudaMemsetAsync(c->d_out.p, 0, bytes, c->st));
     f(c->d_in.as<double>(), c->d_out.as<double>());
     CUDA_OK(cudaMemcpyAsync(out, c->d_out.p, bytes, cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    check_device_error(c);  // synchronizes the stream
 }
 
 int op_prec(int precision) {
@@ -2547,6 +2674,8 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     r->c32.ctgt = false;      // the several-column kernels evaluate the grid targets of every far pair
     r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
     r->chp.ctgt = false;
+    r->near_tc = c->near_tc;  // the same near and sphere kernels as the single solves (results equal column
+    r->sph_tc = c->sph_tc;    // by column)
     CUDA_OK(cudaSetDevice(c->device));
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
@@ -2877,6 +3006,42 @@ smob_status smob_far_pairs_set(const smob_ctx* c, int hp, long long* direct, lon
         if (direct) *direct = dir;
         if (evaluated) *evaluated = ev;
         if (coarse_macs) *coarse_macs = macs;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_tc_info(const smob_ctx* c, int* near_tc, int* sphere_tc) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (near_tc) *near_tc = c->near_tc ? 1 : 0;
+        if (sphere_tc) *sphere_tc = c->sph_tc ? 1 : 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_sphere_tc(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        c->drop_graphs();  // captured blocks hold the other kernels
+        for (auto& kv : c->multi) smob_set_sphere_tc(kv.second, on);
+        c->sph_tc = on != 0;
+        c->g.sph_tc = c->sph_tc ? 1 : 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_near_tc(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        set_device(c);
+        c->drop_graphs();  // captured blocks hold the other kernel
+        for (auto& kv : c->multi) smob_set_near_tc(kv.second, on);
+        c->near_tc = on != 0;
+        c->g.near_tc = c->near_tc ? 1 : 0;
+        // the tile padding must read as zero again after the SIMT layout used the buffer
+        CUDA_OK(cudaMemsetAsync(c->d_sets32.p, 0, c->d_sets32.bytes, c->st));
+        CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
     });
 }

@@ -18,6 +18,7 @@
 //       8 pi u_i = L_i - x_j d_i L_j + d_i L_r                             (single layer, x radius)
 //     and rotates back into the lab frame. Accumulation per target point is in a fixed order.
 #include "smob_internal.h"
+#include "tc_sm100.h"
 
 namespace smob {
 
@@ -25,19 +26,81 @@ namespace {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 
-__device__ __forceinline__ void qrot(const double* q, const double* v, double* o) {
-    const double w = q[0], x = q[1], y = q[2], z = q[3];
-    const double tx = 2 * (y * v[2] - z * v[1]);
-    const double ty = 2 * (z * v[0] - x * v[2]);
-    const double tz = 2 * (x * v[1] - y * v[0]);
+template <typename T>
+__device__ __forceinline__ void qrot(const T* q, const T* v, T* o) {
+    const T w = q[0], x = q[1], y = q[2], z = q[3];
+    const T tx = 2 * (y * v[2] - z * v[1]);
+    const T ty = 2 * (z * v[0] - x * v[2]);
+    const T tz = 2 * (x * v[1] - y * v[0]);
     o[0] = v[0] + w * tx + (y * tz - z * ty);
     o[1] = v[1] + w * ty + (z * tx - x * tz);
     o[2] = v[2] + w * tz + (x * ty - y * tx);
 }
 
+// Per near pair and target: the target in the source's body frame scaled to the unit sphere, and the
+// target normal in the body frame. E is the arithmetic of this set-up and of the assembly below: FP32
+// in the FP32 passes (the FP64 pipe of this GPU runs at 1/58 of the FP32 rate, and ~190 FP64 operations
+// per pair cost more than the contraction itself), FP64 in the FP64 passes. The difference from the
+// source centre is taken in FP64 either way (target and centre are large, their difference small).
+template <typename E>
+__device__ __forceinline__ void near_frame(const DevGeom& g, int s, const double* X, const E* nl, E* xs, E* nb) {
+    const E q[4] = {E(g.quat[4 * s]), E(-g.quat[4 * s + 1]), E(-g.quat[4 * s + 2]), E(-g.quat[4 * s + 3])};
+    const E rel[3] = {E(X[0] - g.center[3 * s]), E(X[1] - g.center[3 * s + 1]), E(X[2] - g.center[3 * s + 2])};
+    E xb[3];
+    qrot(q, rel, xb);
+    qrot(q, nl, nb);
+    const E a = E(g.radius[s]);
+    if (sizeof(E) == 4) {
+        const E ia = E(1) / a;
+        for (int d = 0; d < 3; ++d) xs[d] = xb[d] * ia;
+    } else {
+        for (int d = 0; d < 3; ++d) xs[d] = xb[d] / a;
+    }
+}
+
+// The traction (TRAC) or single-layer velocity at one target from its NS contracted sets, rotated back
+// to the lab frame: 4 pi t_i = n_i div L - x_j n_k d_i d_k L_j + n_k d_i d_k L_r,
+// 8 pi u_i = a (L_i - x_j d_i L_j + d_i L_r).
+template <bool TRAC, typename E, typename A>
+__device__ __forceinline__ void near_assemble(const DevGeom& g, int s, const A* acc, const E* xs, const E* nn,
+                                              E* vl) {
+    E vb[3];
+    if (TRAC) {
+        // symmetric index s(i,k): 00,11,22,01,02,12 -> 0..5
+        const int S3[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+        for (int ii = 0; ii < 3; ++ii) {
+            E v = nn[ii] * E(acc[0]);
+            for (int kk = 0; kk < 3; ++kk) {
+                E h = E(acc[19 + S3[ii][kk]]);
+                for (int jj = 0; jj < 3; ++jj) h -= xs[jj] * E(acc[1 + 6 * jj + S3[ii][kk]]);
+                v += nn[kk] * h;
+            }
+            vb[ii] = sizeof(E) == 4 ? v * E(1.0 / (4 * kPi)) : v / E(4 * kPi);
+        }
+    } else {
+        const E a = E(g.radius[s]);
+        for (int ii = 0; ii < 3; ++ii) {
+            E v = E(acc[ii]) + E(acc[12 + ii]);
+            for (int jj = 0; jj < 3; ++jj) v -= xs[jj] * E(acc[3 + 3 * jj + ii]);
+            vb[ii] = sizeof(E) == 4 ? a * v * E(1.0 / (8 * kPi)) : a * v / E(8 * kPi);
+        }
+    }
+    const E q[4] = {E(g.quat[4 * s]), E(g.quat[4 * s + 1]), E(g.quat[4 * s + 2]), E(g.quat[4 * s + 3])};
+    qrot(q, vb, vl);
+}
+
+// Position of harmonic (n, m) in the recurrence order of degree Nd (m = 0..Nd outer, n = m..Nd inner),
+// the K order of the tensor-core contraction.
+__host__ __device__ __forceinline__ int rec_pos(int n, int m, int Nd) { return m * (Nd + 1) - m * (m - 1) / 2 + (n - m); }
+
+// tiled: write the sets as the B operand of k_near_eval_tc instead of [idx][set] complex: per chunk of
+// kNearTcChunk harmonics (in recurrence order) an NN x 2 kNearTcChunk FP32 tile in the K-major
+// core-matrix layout of tc_sm100.h (row = set, K = (Re, -Im) of each harmonic); the padding (sets
+// >= NS, harmonics past ncoef(p + 3)) stays as cleared at allocation.
 template <typename Real>
 __global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real* __restrict__ mapval, bool trac,
-                            const int* __restrict__ slot_sphere, long long stride, Real* __restrict__ sets) {
+                            const int* __restrict__ slot_sphere, long long stride, Real* __restrict__ sets,
+                            int tiled) {
     const int slot = blockIdx.x;
     const int s = slot_sphere[slot];
     if (g.active && !g.active[g.prob[s]]) return;
@@ -52,11 +115,24 @@ __global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real
     const int base = trac ? T.trac_map : T.sl_map;
     const int rows = trac ? T.trac_rows : T.sl_rows;
     Real* out = sets + stride * slot;
+    const int NS = trac ? kNearSetsTrac : kNearSetsSL;
+    const int NN = trac ? 32 : 16;
+    const int Nd = p + 3;
     for (int r = blockIdx.y * blockDim.x + threadIdx.x; r < rows; r += gridDim.y * blockDim.x) {
         const int e0 = g.map_rowptr[base + r], e1 = g.map_rowptr[base + r + 1];
         Real acc = 0;
         for (int e = e0; e < e1; ++e) acc += mapval[e] * cin[g.map_col[e]];
-        out[r] = acc;
+        if (!tiled) {
+            out[r] = acc;
+            continue;
+        }
+        // row r = (idx, set, re/im) of the [idx][set] complex layout
+        const int idx = r / (2 * NS), rem = r - idx * 2 * NS, set = rem >> 1, im = rem & 1;
+        int n = 0;
+        while ((n + 1) * (n + 2) / 2 <= idx) ++n;
+        const int pos = rec_pos(n, idx - n * (n + 1) / 2, Nd);
+        const int ch = pos / kNearTcChunk, k = 2 * (pos - ch * kNearTcChunk) + im;
+        out[(long long)ch * NN * (2 * kNearTcChunk) + tc::kmajor_offset(set, k, 2 * kNearTcChunk) / 4] = im ? -acc : acc;
     }
 }
 
@@ -127,7 +203,8 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
     if (tile * GROUPS * PPT >= ng) return;  // whole CTA past the sphere
     bool valid[PPT];
     int i[PPT];
-    double X[PPT][3], Nl[PPT][3], res[PPT][3];
+    double X[PPT][3], res[PPT][3];
+    Real Nl[PPT][3];
 #pragma unroll
     for (int p = 0; p < PPT; ++p) {
         const int j = (tile * PPT + p) * GROUPS + threadIdx.x / kNearLanes;
@@ -135,7 +212,7 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
         i[p] = g.gidx[t] + (valid[p] ? j : 0);
         for (int d = 0; d < 3; ++d) {
             X[p][d] = g.coords[3 * i[p] + d];
-            Nl[p][d] = g.norms[3 * i[p] + d];
+            Nl[p][d] = Real(g.norms[3 * i[p] + d]);
             res[p][d] = 0;
         }
     }
@@ -176,23 +253,17 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
             __syncthreads();
             S = sS;
         }
-        const double q[4] = {g.quat[4 * s], g.quat[4 * s + 1], g.quat[4 * s + 2], g.quat[4 * s + 3]};
-        const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
-        const double a = g.radius[s];
         constexpr int NL = (NS + kNearLanes - 1) / kNearLanes;
         Real x[PPT], y[PPT], z[PPT], ir2[PPT], dr[PPT], di[PPT];
-        double nb[PPT][3];
+        Real nb[PPT][3];
         Real accl[PPT][NL];
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
-            const double rel[3] = {X[p][0] - g.center[3 * s], X[p][1] - g.center[3 * s + 1],
-                                   X[p][2] - g.center[3 * s + 2]};
-            double xb[3];
-            qrot(qc, rel, xb);
-            qrot(qc, Nl[p], nb[p]);
-            x[p] = Real(xb[0] / a);
-            y[p] = Real(xb[1] / a);
-            z[p] = Real(xb[2] / a);
+            Real xs[3];
+            near_frame<Real>(g, s, X[p], Nl[p], xs, nb[p]);
+            x[p] = xs[0];
+            y[p] = xs[1];
+            z[p] = xs[2];
             const Real r2 = x[p] * x[p] + y[p] * y[p] + z[p] * z[p];
             ir2[p] = Real(1) / r2;
             dr[p] = Real(1) / sqrt(r2);  // Th_0^0
@@ -240,33 +311,12 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
 #pragma unroll
             for (int k = 0; k < NS; ++k)
                 acc[k] = __shfl_sync(0xffffffffu, accl[p][k / kNearLanes], k % kNearLanes, kNearLanes);
-            double vb[3];
-            const double xs[3] = {double(x[p]), double(y[p]), double(z[p])};
-            if (TRAC) {
-                // symmetric index s(i,k): 00,11,22,01,02,12 -> 0..5
-                const int S3[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
-                const double* nn = nb[p];
-                for (int ii = 0; ii < 3; ++ii) {
-                    double v = nn[ii] * double(acc[0]);
-                    for (int kk = 0; kk < 3; ++kk) {
-                        double h = double(acc[19 + S3[ii][kk]]);
-                        for (int jj = 0; jj < 3; ++jj) h -= xs[jj] * double(acc[1 + 6 * jj + S3[ii][kk]]);
-                        v += nn[kk] * h;
-                    }
-                    vb[ii] = v / (4 * kPi);
-                }
-            } else {
-                for (int ii = 0; ii < 3; ++ii) {
-                    double v = double(acc[ii]) + double(acc[12 + ii]);
-                    for (int jj = 0; jj < 3; ++jj) v -= xs[jj] * double(acc[3 + 3 * jj + ii]);
-                    vb[ii] = a * v / (8 * kPi);
-                }
-            }
-            double vl[3];
-            qrot(q, vb, vl);
-            res[p][0] += vl[0];
-            res[p][1] += vl[1];
-            res[p][2] += vl[2];
+            const Real xs[3] = {x[p], y[p], z[p]};
+            Real vl[3];
+            near_assemble<TRAC, Real, Real>(g, s, acc, xs, nb[p], vl);
+            res[p][0] += double(vl[0]);
+            res[p][1] += double(vl[1]);
+            res[p][2] += double(vl[2]);
         }
     }
 #pragma unroll
@@ -276,6 +326,229 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
             out[3 * i[p] + 1] += c * res[p][1];
             out[3 * i[p] + 2] += c * res[p][2];
         }
+}
+
+// ---------------------------------------------------------------- tensor-core near field (FP32 passes)
+// The contraction of k_near_eval as a GEMM on the tcgen05 tensor cores. One CTA = 256 target points of
+// one target sphere, one per thread, as two MMA tiles of M = 128 rows (threads 0-127, 128-255); for
+// each near source sphere:
+//   A [256 x K]: the targets' irregular solid harmonics, K = 2 ncoef(p_s + 3) real values (Re, Im of
+//     each harmonic) in the recurrence order (m outer, n inner), generated by the threads
+//     kNearTcChunk harmonics at a time (the FP32 recurrence of k_near_eval) into shared memory;
+//   B [NN x K]: the source's coefficient sets as (Re, -Im) (tiled by k_near_sets), NN = 32 traction
+//     (25 sets) or 16 single layer (15 sets), one chunk shared by both tiles;
+//   D [128 x NN] per tile in tensor memory (tile 0 at column 0, tile 1 at column 32), FP32: row i holds
+//     target i's NS contractions.
+// Products in 3xTF32 (a_hi b_hi + a_hi b_lo + a_lo b_hi, the split made as the operands are staged).
+// One operand stage per CTA (~72 KB, three CTAs per SM): the threads fill the chunk, one thread issues
+// the MMAs, commits them to an mbarrier and waits for them (bounded) while the other warps sleep at the
+// barrier and the other CTAs of the SM generate their chunks. After a source's last chunk each warp
+// loads its 32 rows (tcgen05.ld) and assembles the traction or velocity in FP32. On a wait timeout the
+// CTA records it in err, writes nothing and releases its tensor memory.
+constexpr int kTcK = 2 * kNearTcChunk;          // K per chunk (TF32 elements)
+constexpr int kTcABytes = 128 * kTcK * 4;       // one A operand tile chunk (16 KB)
+constexpr int kTcThreads = 256;                 // two M tiles
+constexpr long long kTcWaitPolls = 1LL << 22;
+
+template <bool TRAC>
+__host__ __device__ constexpr int tc_nn() { return TRAC ? 32 : 16; }
+// A hi, A lo for two tiles, then B hi, B lo
+template <bool TRAC>
+__host__ __device__ constexpr int tc_stage_bytes() { return 4 * kTcABytes + 2 * tc_nn<TRAC>() * kTcK * 4; }
+
+template <bool TRAC>
+__global__ void __launch_bounds__(kTcThreads, 2)
+    k_near_eval_tc(DevGeom g, const float* __restrict__ tiles, long long tstride, const float* __restrict__ th,
+                   int th_c1, int th_c2, int th_diag, double c, int pair_filter, int tile_major, double* __restrict__ out,
+                   int* __restrict__ err) {
+    constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
+    constexpr int NN = tc_nn<TRAC>();
+    constexpr int BBYTES = NN * kTcK * 4;
+    const int t = tile_major ? blockIdx.y : blockIdx.x;
+    const int tile = tile_major ? blockIdx.x : blockIdx.y;
+    if (g.active && !g.active[g.prob[t]]) return;
+    const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
+    const int ng = g.glen[t];
+    if (e0 == e1 || tile * kTcThreads >= ng) return;
+    bool any = false;  // (uniform over the CTA)
+    for (int e = e0; e < e1; ++e)
+        if (!(pair_filter == 1 && g.nbr_precise[e]) && !(pair_filter == 2 && !g.nbr_precise[e])) any = true;
+    if (!any) return;
+
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, mt = tid >> 7, row = tid & 127;
+    unsigned char* sA = tc_smem + mt * 2 * kTcABytes;  // this thread's tile: hi, then lo
+    unsigned char* sB = tc_smem + 4 * kTcABytes;       // hi, then lo
+    // recurrence tables after the stage: (c1, c2) pairs, then the diagonal factors
+    const int ncd = ncoef(g.pmax + 3);
+    float2* t12 = reinterpret_cast<float2*>(tc_smem + tc_stage_bytes<TRAC>());
+    float* dg = reinterpret_cast<float*>(t12 + ncd);
+    for (int k = tid; k < ncd; k += kTcThreads) t12[k] = make_float2(th[th_c1 + k], th[th_c2 + k]);
+    for (int k = tid; k < g.pmax + 4; k += kTcThreads) dg[k] = th[th_diag + k];
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, 64);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+        s_fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, NN);
+
+    const int j = tile * kTcThreads + tid;
+    const bool valid = j < ng;
+    const int i = g.gidx[t] + (valid ? j : 0);
+    double X[3], res[3] = {0, 0, 0};
+    float Nl[3];
+    for (int d = 0; d < 3; ++d) {
+        X[d] = g.coords[3 * i + d];
+        Nl[d] = float(g.norms[3 * i + d]);
+    }
+    unsigned phase = 0;
+    bool failed = false;
+    for (int e = e0; e < e1 && !failed; ++e) {
+        if (pair_filter == 1 && g.nbr_precise[e]) continue;
+        if (pair_filter == 2 && !g.nbr_precise[e]) continue;
+        const int s = g.nbr_src[e];
+        const float* T = tiles + tstride * g.near_src_slot[s];
+        const int Nd = g.order[s] + 3;
+        const int nck = (ncoef(Nd) + kNearTcChunk - 1) / kNearTcChunk;
+        float xs3[3], nb[3];
+        near_frame<float>(g, s, X, Nl, xs3, nb);
+        const float x = xs3[0], y = xs3[1], z = xs3[2];
+        const float r2 = x * x + y * y + z * z;
+        const float ir2 = 1.f / r2;
+        // recurrence state: the harmonic (n, m) to emit next is (cr, ci); past the last one (m > Nd) all zero
+        float dr = 1.f / sqrtf(r2), di = 0.f;  // Th_m^m
+        int m = 0, n = 0, idx = 0;              // idx = n (n + 1) / 2 + m
+        float pr = 0.f, pi = 0.f, cr = dr, ci = di;
+        const float zi = z * ir2;
+        for (int ch = 0; ch < nck; ++ch) {
+            // B chunk (one float4 per thread for NN = 32): copy and split
+            const float4* gB = reinterpret_cast<const float4*>(T + (long long)ch * NN * kTcK);
+            for (int v = tid; v < NN * kTcK / 4; v += kTcThreads) {
+                const float4 b = __ldg(gB + v);
+                float4 h, l;
+                tc::tf32_split(b.x, h.x, l.x);
+                tc::tf32_split(b.y, h.y, l.y);
+                tc::tf32_split(b.z, h.z, l.z);
+                tc::tf32_split(b.w, h.w, l.w);
+                reinterpret_cast<float4*>(sB)[v] = h;
+                reinterpret_cast<float4*>(sB + BBYTES)[v] = l;
+            }
+            // A chunk: the next kNearTcChunk harmonics of this thread's target, 4 K values at a time
+#pragma unroll
+            for (int qd = 0; qd < kTcK / 4; ++qd) {
+                float v4[4];
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    v4[2 * h2] = cr;
+                    v4[2 * h2 + 1] = ci;
+                    if (n < Nd) {
+                        // Th_{n+1}^m = -(c1 z Th_n^m + c2 Th_{n-1}^m) / r^2
+                        const float2 a12 = t12[idx];
+                        const float nr = -(a12.x * zi * cr + a12.y * ir2 * pr);
+                        const float ni = -(a12.x * zi * ci + a12.y * ir2 * pi);
+                        pr = cr;
+                        pi = ci;
+                        cr = nr;
+                        ci = ni;
+                        idx += n + 1;
+                        ++n;
+                    } else if (m < Nd) {
+                        // next column: Th_{m+1}^{m+1} = -d_{m+1} (x + i y) Th_m^m / r^2
+                        ++m;
+                        const float f = -dg[m] * ir2;
+                        const float nr = f * (x * dr - y * di);
+                        const float ni = f * (x * di + y * dr);
+                        dr = nr;
+                        di = ni;
+                        pr = 0.f;
+                        pi = 0.f;
+                        cr = dr;
+                        ci = di;
+                        n = m;
+                        idx = m * (m + 1) / 2 + m;
+                    } else {
+                        cr = 0.f;
+                        ci = 0.f;
+                    }
+                }
+                float4 h, l;
+                tc::tf32_split(v4[0], h.x, l.x);
+                tc::tf32_split(v4[1], h.y, l.y);
+                tc::tf32_split(v4[2], h.z, l.z);
+                tc::tf32_split(v4[3], h.w, l.w);
+                const uint32_t off = tc::kmajor_offset(row, 4 * qd, kTcK);
+                *reinterpret_cast<float4*>(sA + off) = h;
+                *reinterpret_cast<float4*>(sA + kTcABytes + off) = l;
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t b0 = tc::smem_u32(sB), bl0 = b0 + BBYTES;
+#pragma unroll
+                for (int tt = 0; tt < 2; ++tt) {
+                    const uint32_t a0 = tc::smem_u32(tc_smem + tt * 2 * kTcABytes), al0 = a0 + kTcABytes;
+#pragma unroll
+                    for (int ks = 0; ks < kTcK / 8; ++ks) {
+                        const uint32_t o = ks * 256;
+                        const uint64_t ah = tc::sdesc(a0 + o, 128, (kTcK / 4) * 128);
+                        const uint64_t al = tc::sdesc(al0 + o, 128, (kTcK / 4) * 128);
+                        const uint64_t bh = tc::sdesc(b0 + o, 128, (kTcK / 4) * 128);
+                        const uint64_t bl = tc::sdesc(bl0 + o, 128, (kTcK / 4) * 128);
+                        const uint32_t d = tmem + 32 * tt;
+                        tc::mma_tf32(d, ah, bh, idesc, ch > 0 || ks > 0);
+                        tc::mma_tf32(d, ah, bl, idesc, true);
+                        tc::mma_tf32(d, al, bh, idesc, true);
+                    }
+                }
+                tc::mma_commit(&mbar);
+                // one thread waits for the chunk's MMAs; the others sleep at the barrier below
+                if (!tc::mbar_wait_bounded(&mbar, phase, kTcWaitPolls)) s_fail = 1;
+            }
+            phase ^= 1;
+            __syncthreads();
+            if (s_fail) {
+                failed = true;
+                break;
+            }
+        }
+        if (failed) break;
+        tc::fence_after_sync();
+        float acc[32];
+        tc::tmem_ld_32x32b_x32(tmem + 32 * mt + (uint32_t((warp & 3) * 32) << 16), acc);
+        tc::fence_before_sync();  // the next source's first MMA overwrites D after the next barrier
+        (void)NS;
+        float vl[3];
+        near_assemble<TRAC, float, float>(g, s, acc, xs3, nb, vl);
+        res[0] += double(vl[0]);
+        res[1] += double(vl[1]);
+        res[2] += double(vl[2]);
+    }
+    if (failed) {
+        if (tid == 0) atomicExch(err, 1);
+    } else if (valid) {
+        out[3 * i] += c * res[0];
+        out[3 * i + 1] += c * res[1];
+        out[3 * i + 2] += c * res[2];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 64);
+    }
 }
 
 }  // namespace
@@ -288,12 +561,15 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
     // still give the GPU enough CTAs
     constexpr int kSetSplit = 8;
     const dim3 grid(nslots, kSetSplit);
-    if (fp32)
+    if (fp32) {
+        const bool tiled = g.near_tc != 0;
         k_near_sets<float><<<grid, 256, sm, st>>>(g, static_cast<const float*>(coef), g.map_val_f, trac, slot_sphere,
-                                                  stride, static_cast<float*>(sets));
-    else
+                                                  tiled ? near_tile_stride(g.pmax, trac) : stride,
+                                                  static_cast<float*>(sets), tiled ? 1 : 0);
+    } else {
         k_near_sets<double><<<grid, 256, sm, st>>>(g, static_cast<const double*>(coef), g.map_val_d, trac,
-                                                   slot_sphere, stride, static_cast<double*>(sets));
+                                                   slot_sphere, stride, static_cast<double*>(sets), 0);
+    }
     return 1;
 }
 
@@ -344,7 +620,17 @@ void configure_near_typed() {
     cudaFuncSetAttribute(k_near_eval<Real, TRAC, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
 }
 
+// dynamic shared memory of the tensor-core near kernel: the operand stage and the recurrence tables
+template <bool TRAC>
+size_t near_tc_smem(int pmax) {
+    return size_t(tc_stage_bytes<TRAC>()) + size_t(2 * ncoef(pmax + 3) + pmax + 4) * sizeof(float);
+}
+
 void configure_near_kernels() {
+    cudaFuncSetAttribute(k_near_eval_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<true>(kMaxOrder)));
+    cudaFuncSetAttribute(k_near_eval_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<false>(kMaxOrder)));
     configure_near_typed<float, true>();
     configure_near_typed<float, false>();
     configure_near_typed<double, true>();
@@ -353,6 +639,23 @@ void configure_near_kernels() {
 
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
                      cudaStream_t st, int pair_filter) {
+    if (fp32 && g.near_tc) {
+        // one CTA per (target sphere, 256 of its grid points); tile-major (the tiles of a sphere adjacent)
+        const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
+        const int tiles = (gmax + kTcThreads - 1) / kTcThreads;
+        const int tm = g.N <= 65535 ? 1 : 0;
+        const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
+        const float* tl = static_cast<const float*>(sets);
+        if (trac)
+            k_near_eval_tc<true><<<grid, kTcThreads, near_tc_smem<true>(g.pmax), st>>>(
+                g, tl, near_tile_stride(g.pmax, true), g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out,
+                g.err);
+        else
+            k_near_eval_tc<false><<<grid, kTcThreads, near_tc_smem<false>(g.pmax), st>>>(
+                g, tl, near_tile_stride(g.pmax, false), g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm,
+                out, g.err);
+        return 1;
+    }
     switch (g.near_lanes) {
         case 1: launch_near_eval_l<1>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;
         case 2: launch_near_eval_l<2>(g, sets, stride, trac, fp32, c, out, st, pair_filter); break;

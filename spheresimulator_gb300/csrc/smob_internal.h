@@ -33,6 +33,13 @@ constexpr int kNearThreads = 128;        // near-field CTA (one target point per
 constexpr int kVecChunk = 4096;          // segmented reduction chunk (elements), never crosses a problem
 constexpr int kNearSetsTrac = 25;        // div L, Hessians of L_x,L_y,L_z,L_r
 constexpr int kNearSetsSL = 15;          // L_j, grad L_j, grad L_r
+constexpr int kNearTcChunk = 16;         // harmonics (complex) per K chunk of the tensor-core near field
+// floats per near-source slot of the tiled FP32 sets (the B operand of the tensor-core near field):
+// chunks of kNearTcChunk harmonics up to degree pmax + 3, each a (32 or 16) x 2 kNearTcChunk tile
+inline long long near_tile_stride(int pmax, bool trac) {
+    const int nck = ((pmax + 4) * (pmax + 5) / 2 + kNearTcChunk - 1) / kNearTcChunk;
+    return (long long)nck * (trac ? 32 : 16) * 2 * kNearTcChunk;
+}
 constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per sphere (FP32 far field)
 constexpr int kCoarseTileNodes = 32;     // coarse nodes per CTA of the coarse-strength GEMMs (multiple of 16)
 // interpolation tiles of the coarse targets (the host lists at most this many entries per tile; the
@@ -154,6 +161,21 @@ struct DevGeom {
     int N, M, P;
     int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
     int near_lanes;       // lanes per target point in the near-field kernel (1, 2, 4 or 8)
+    int near_tc;          // FP32 near field on the tensor cores (k_near_eval_tc, tiled sets); 0: SIMT kernel
+    // FP32 sphere operator with the Legendre stage on the tensor cores (k_legendre_tc; 0: one SIMT kernel):
+    // tiles {order p, first entry of leg_sph, spheres (<= 21), 0} of spheres of one order; B operand
+    // tables per (p, m), forward and inverse, at leg_off[2 (p (kMaxOrder + 1) + m) + {0, 1}] floats into
+    // leg_tab; per-sphere workspaces fgbuf (fg_stride floats: [3][p+1][p+1] complex) and lopbuf (6 doubles)
+    int sph_tc;
+    int n_leg_tiles;
+    const int4* leg_tiles;
+    const int* leg_sph;
+    const float* leg_tab;
+    const int* leg_off;
+    float* fgbuf;
+    long long fg_stride;
+    double* lopbuf;
+    int* err;             // device error word: kernels whose bounded waits gave up set it (0: none)
     int th_c1, th_c2, th_diag;  // offsets of the irregular-solid-harmonic recurrence tables in tab_d/tab_f
     const double* center;
     const double* radius;
@@ -259,11 +281,27 @@ int launch_sh_g2s(const DevGeom& g, const double* grid, double* coef, cudaStream
 int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream_t st);
 
 // Near field: sets from coefficients (per near source sphere), then spectral evaluation per target sphere.
+// FP32 with g.near_tc: the sets are written as the tiles of the tensor-core kernel at stride
+// near_tile_stride(g.pmax, trac) per slot (`stride` is then not used); the buffer's padding must be zero.
 int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
                      const int* slot_sphere, long long stride, cudaStream_t st);
 // pair_filter: 0 all near pairs, 1 pairs with gap >= 0.1 min radius, 2 the near-singular pairs only
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
                      cudaStream_t st, int pair_filter = 0);
+
+// Neighbour list on the device (nbrlist.cu): near pairs of every problem by the reference's rule
+// 0 < |c_s - c_t|^2 < (1.5 a_s + 1.5 a_t)^2 (problems[].s0/s1 and prob give each sphere's problem).
+// count: near sources per target; scan: CSR offsets start[N+1], near-source slots slot_of[N] (-1 if
+// none), totals {pairs, slots}; fill: sources (ascending per target), near-singular flags, slot_sphere.
+int launch_nbr_count(const double* centers, const double* radii, const int* prob, const Problem* problems, int N,
+                     int* count, cudaStream_t st);
+int launch_nbr_scan(const int* count, int N, int* start, int* slot_of, int* totals, cudaStream_t st);
+int launch_nbr_fill(const double* centers, const double* radii, const int* prob, const Problem* problems, int N,
+                    const int* start, const int* slot_of, int* src, unsigned char* precise, int* slot_sphere,
+                    cudaStream_t st);
+// first overlapping or touching pair (t * N + s, s > t, same problem) by atomicMin into *first
+int launch_overlap_check(const double* centers, const double* radii, const int* prob, const Problem* problems, int N,
+                         unsigned long long* first, cudaStream_t st);
 
 // Geometry update: grid points, normals and far-field copies from the current centres/orientations
 // (org: 3 per problem); writes the buffers that g's read-only views point to

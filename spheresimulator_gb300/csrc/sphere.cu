@@ -18,6 +18,7 @@
 //   traction PV : 3/(2(2n+1)(2n+3)), -3/(2(2n-1)(2n+1)), -3/(2(2n+1))
 // and the inverse transform mirrors the forward one. All stages stay in shared memory.
 #include "smob_internal.h"
+#include "tc_sm100.h"
 
 namespace smob {
 
@@ -25,17 +26,19 @@ namespace {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 
-__device__ __forceinline__ void qrot(const double* q, const double* v, double* o) {
-    const double w = q[0], x = q[1], y = q[2], z = q[3];
-    const double tx = 2 * (y * v[2] - z * v[1]);
-    const double ty = 2 * (z * v[0] - x * v[2]);
-    const double tz = 2 * (x * v[1] - y * v[0]);
+template <typename T>
+__device__ __forceinline__ void qrot(const T* q, const T* v, T* o) {
+    const T w = q[0], x = q[1], y = q[2], z = q[3];
+    const T tx = 2 * (y * v[2] - z * v[1]);
+    const T ty = 2 * (z * v[0] - x * v[2]);
+    const T tz = 2 * (x * v[1] - y * v[0]);
     o[0] = v[0] + w * tx + (y * tz - z * ty);
     o[1] = v[1] + w * ty + (z * tx - x * tz);
     o[2] = v[2] + w * tz + (x * ty - y * tx);
 }
-__device__ __forceinline__ void qinvrot(const double* q, const double* v, double* o) {
-    const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+template <typename T>
+__device__ __forceinline__ void qinvrot(const T* q, const T* v, T* o) {
+    const T qc[4] = {q[0], -q[1], -q[2], -q[3]};
     qrot(qc, v, o);
 }
 
@@ -66,8 +69,13 @@ struct SphereArgs {
     double* out;            // grid output
     double c_id, c_self, c_lop;
     int self_kind;          // -1 none, 0 single layer, 3 traction PV, 4 block-diagonal preconditioner
-    int mode;               // 0 OP, 1 G2S, 2 S2G
+    int mode;               // 0 OP, 1 G2S, 2 S2G; the tensor-core operator (FP32): 3 its first stage (rotate,
+                            // DFT along phi -> fg, rigid-mode sums -> lop), 4 its last stage (fg holds the
+                            // inverse-Legendre values: inverse DFT, rotate back, self, identity and L terms)
     void* coef_out;         // coefficient output (Real complex in OP, double in G2S), may be null
+    float* fg;              // modes 3 and 4: per sphere [3][nt][p+1] complex at fg_stride floats per sphere
+    long long fg_stride;
+    double* lop;            // modes 3 and 4: per sphere the rigid-mode vectors A, B of L (6 doubles)
 };
 
 template <typename Real>
@@ -85,7 +93,9 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
     Real* F = vp + ng;             // [3][nt][P1] complex
     Real* C = F + 6 * nt * P1;     // [3][nc] complex
     __shared__ double red[32];
-    const double q[4] = {g.quat[4 * s], g.quat[4 * s + 1], g.quat[4 * s + 2], g.quat[4 * s + 3]};
+    // rotations and the rigid-mode (L) sums in Real: FP32 in the FP32 operator (the FP64 pipe of this GPU
+    // is 1/58 of the FP32 one), FP64 in the FP64 operator
+    const Real q[4] = {Real(g.quat[4 * s]), Real(g.quat[4 * s + 1]), Real(g.quat[4 * s + 2]), Real(g.quat[4 * s + 3])};
     const double rad = g.radius[s];
     const Real* ct = tab + T.ring;
     const Real* st = ct + nt;
@@ -97,40 +107,42 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
     const Real* sinm = cosm + P1 * nphi;
     const Real* cph = tab + T.cph;
     const Real* sph = cph + nphi;
-    const bool want_lop = a.mode == 0 && a.c_lop != 0.0;
+    const bool want_lop = (a.mode == 0 || a.mode == 3 || a.mode == 4) && a.c_lop != 0.0;
     double A[3] = {0, 0, 0}, B[3] = {0, 0, 0};
 
-    if (a.mode != 2) {
-        double la[6] = {0, 0, 0, 0, 0, 0};
+    if (a.mode != 2 && a.mode != 4) {
+        Real la[6] = {0, 0, 0, 0, 0, 0};
+        const Real rr = Real(rad);
         for (int i = threadIdx.x; i < ng; i += blockDim.x) {
             const int j = i / nphi, k = i - j * nphi;
-            const double v[3] = {a.x[3 * (g0 + i)], a.x[3 * (g0 + i) + 1], a.x[3 * (g0 + i) + 2]};
+            const Real v[3] = {Real(a.x[3 * (g0 + i)]), Real(a.x[3 * (g0 + i) + 1]), Real(a.x[3 * (g0 + i) + 2])};
             if (want_lop) {
-                const double w = g.weights[g0 + i];
-                const double* n = g.norms + 3 * (g0 + i);
+                const Real w = Real(g.weights[g0 + i]);
+                const Real n[3] = {Real(g.norms[3 * (g0 + i)]), Real(g.norms[3 * (g0 + i) + 1]),
+                                   Real(g.norms[3 * (g0 + i) + 2])};
                 la[0] += w * v[0];
                 la[1] += w * v[1];
                 la[2] += w * v[2];
-                la[3] += w * rad * (n[1] * v[2] - n[2] * v[1]);
-                la[4] += w * rad * (n[2] * v[0] - n[0] * v[2]);
-                la[5] += w * rad * (n[0] * v[1] - n[1] * v[0]);
+                la[3] += w * rr * (n[1] * v[2] - n[2] * v[1]);
+                la[4] += w * rr * (n[2] * v[0] - n[0] * v[2]);
+                la[5] += w * rr * (n[0] * v[1] - n[1] * v[0]);
             }
             if (a.self_kind >= 0 || a.mode == 1) {
-                double b[3];
+                Real b[3];
                 qinvrot(q, v, b);
                 const Real cp = cph[k], sp = sph[k], c0 = ct[j], s0 = st[j];
-                const Real h = Real(b[0]) * cp + Real(b[1]) * sp;
-                vr[i] = h * s0 + Real(b[2]) * c0;
-                vt[i] = h * c0 - Real(b[2]) * s0;
-                vp[i] = -Real(b[0]) * sp + Real(b[1]) * cp;
+                const Real h = b[0] * cp + b[1] * sp;
+                vr[i] = h * s0 + b[2] * c0;
+                vt[i] = h * c0 - b[2] * s0;
+                vp[i] = -b[0] * sp + b[1] * cp;
             }
         }
         if (want_lop) {
-            for (int c = 0; c < 6; ++c) la[c] = block_sum_to_all(la[c], red);
+            for (int c = 0; c < 6; ++c) la[c] = block_sum_to_all(la[c], reinterpret_cast<Real*>(red));
             const double fa = 1.0 / (4 * kPi * rad * rad), fb = 3.0 / (8 * kPi * rad * rad * rad * rad);
             for (int c = 0; c < 3; ++c) {
-                A[c] = la[c] * fa;
-                B[c] = la[3 + c] * fb;
+                A[c] = double(la[c]) * fa;
+                B[c] = double(la[3 + c]) * fb;
             }
         }
         if (a.self_kind >= 0 || a.mode == 1) {
@@ -150,6 +162,22 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
                 F[2 * it + 1] = im;
             }
             __syncthreads();
+            if (a.mode == 3) {
+                // first stage of the tensor-core operator: the Legendre stage runs in k_legendre_tc, which
+                // reads one m at a time: stored m-major, [m][component][ring] complex
+                float* fo = a.fg + a.fg_stride * s;
+                for (int i = threadIdx.x; i < 6 * nt * P1; i += blockDim.x) {
+                    const int m = i / (6 * nt), r = i - m * 6 * nt, c = r / (2 * nt), r2 = r - c * 2 * nt;
+                    const int j = r2 >> 1, im = r2 & 1;
+                    fo[i] = float(F[2 * (c * nt * P1 + j * P1 + m) + im]);
+                }
+                if (want_lop && threadIdx.x == 0)
+                    for (int c = 0; c < 3; ++c) {
+                        a.lop[6 * s + c] = A[c];
+                        a.lop[6 * s + 3 + c] = B[c];
+                    }
+                return;
+            }
             // Legendre contraction over rings
             for (int idx = threadIdx.x; idx < nc; idx += blockDim.x) {
                 int n, m;
@@ -201,13 +229,28 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
             if (a.mode == 1) return;
             __syncthreads();
         }
+    } else if (a.mode == 4) {
+        // last stage of the tensor-core operator: the inverse-Legendre values (per ring and m) come from
+        // k_legendre_tc, the rigid-mode vectors from the first stage
+        const float* fi = a.fg + a.fg_stride * s;  // [m][component][ring] complex
+        for (int i = threadIdx.x; i < 6 * nt * P1; i += blockDim.x) {
+            const int m = i / (6 * nt), r = i - m * 6 * nt, c = r / (2 * nt), r2 = r - c * 2 * nt;
+            const int j = r2 >> 1, im = r2 & 1;
+            F[2 * (c * nt * P1 + j * P1 + m) + im] = Real(fi[i]);
+        }
+        if (want_lop)
+            for (int c = 0; c < 3; ++c) {
+                A[c] = a.lop[6 * s + c];
+                B[c] = a.lop[6 * s + 3 + c];
+            }
+        __syncthreads();
     } else {
         for (int i = threadIdx.x; i < 6 * nc; i += blockDim.x) C[i] = Real(a.coef_in[2LL * g.coff[s] + i]);
         __syncthreads();
     }
 
     const bool do_inverse = a.mode == 2 || a.self_kind >= 0;
-    if (do_inverse) {
+    if (do_inverse && a.mode != 4) {
         if (a.mode == 0) {
             // self multipliers (in place)
             for (int idx = threadIdx.x; idx < nc; idx += blockDim.x) {
@@ -297,9 +340,13 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
                 sp += Gp[0] * c0 - Gp[1] * s0;
             }
             const Real cp = cph[k], spp = sph[k], c0 = ct[j], s0 = st[j];
-            const double b[3] = {double(sr * s0 * cp + stt * c0 * cp - sp * spp),
-                                 double(sr * s0 * spp + stt * c0 * spp + sp * cp), double(sr * c0 - stt * s0)};
-            qrot(q, b, o);
+            const Real b[3] = {sr * s0 * cp + stt * c0 * cp - sp * spp, sr * s0 * spp + stt * c0 * spp + sp * cp,
+                               sr * c0 - stt * s0};
+            Real ob[3];
+            qrot(q, b, ob);
+            o[0] = double(ob[0]);
+            o[1] = double(ob[1]);
+            o[2] = double(ob[2]);
         }
         double* dst = a.out + 3 * (g0 + i);
         if (a.mode == 2) {
@@ -326,6 +373,236 @@ __global__ void __launch_bounds__(kSphereThreads) k_sphere(DevGeom g, const Real
     }
 }
 
+// ---------------------------------------------------------------- Legendre stage on the tensor cores
+// The FP32 sphere operator in three launches: k_sphere mode 3 (per sphere: rotation into the body
+// frame, spherical components, DFT along phi, rigid-mode sums), k_legendre_tc (this kernel), k_sphere
+// mode 4 (per sphere: inverse DFT, rotation back, self/identity/L terms). k_legendre_tc handles one
+// order p, one m and a tile of up to kLegSpheres spheres of that order; the Legendre sums of all of
+// them are two tcgen05 TF32 GEMMs (3xTF32 split, ~FP32 accuracy) with M = 128 rows = (sphere, kind):
+//   forward  D_f[(s, k), n] = sum_K A_f[(s, k), K] B_f[n, K], K = (block b, ring j), b = 0, 1, 2 pairing
+//            the weighted tables w_j P, w_j dP, w_j m Ps (n, m at ring j) with the phi-DFT values of the
+//            radial, polar and azimuthal components so that row kind k = 0..5 gives directly
+//            Re/Im of the radial coefficient, of the surface-gradient and of the toroidal coefficient
+//            (times n(n+1)), e.g. Re g = sum_j Ft_re w dP + Fp_im w m Ps;
+//   then, per (s, n), the self operator's multipliers (coefficients written out for the near field);
+//   inverse  D_i[(s, k), j] = sum_K A_i[(s, k), K] B_i[j, K], K = (block b, n), the same pairing with the
+//            unweighted tables: Re/Im of the radial, polar and azimuthal values at ring j.
+// K runs in chunks of 32 through one shared-memory stage (operands built by the threads, B tables
+// precomputed per (p, m) on the host in the operand layout of tc_sm100.h); accumulators in tensor
+// memory (forward at column 0, inverse at column 64). The values of column m are read from and
+// written back to the same per-sphere buffer fg ([m][component][ring] complex, so one m is contiguous).
+// Waits are bounded; a timeout sets err.
+constexpr int kLegSpheres = 21;   // spheres per tile: 6 rows each, 126 of the 128 MMA rows
+constexpr int kLegK = 32;         // K per chunk
+constexpr long long kLegWaitPolls = 1LL << 22;
+
+__host__ __device__ inline int leg_kpad(int p) { return kLegK * ((3 * (p + 1) + kLegK - 1) / kLegK); }
+__host__ __device__ inline int leg_npad(int n) { return 16 * ((n + 15) / 16); }
+
+// value of the A operand row kind k (0..5) in block b (0..2) from the (Re, Im) pairs of three components
+// v0, v1, v2 (radial / polar / azimuthal, or the radial / gradient / toroidal coefficients)
+__device__ __forceinline__ float leg_a(int k, int b, float v0r, float v0i, float v1r, float v1i, float v2r, float v2i) {
+    if (b == 0) return k == 0 ? v0r : (k == 1 ? v0i : 0.f);
+    if (b == 1) return k == 2 ? v1r : (k == 3 ? v1i : (k == 4 ? v2r : (k == 5 ? v2i : 0.f)));
+    // b == 2
+    return k == 2 ? v2i : (k == 3 ? -v2r : (k == 4 ? -v1i : (k == 5 ? v1r : 0.f)));
+}
+
+__global__ void __launch_bounds__(128) k_legendre_tc(DevGeom g, int self_kind, float* __restrict__ fg,
+                                                     long long fg_stride, float* __restrict__ coef_out) {
+    const int4 T = g.leg_tiles[blockIdx.x];  // {order p, first entry in leg_sph, spheres, 0}
+    const int p = T.x, m = blockIdx.y;
+    if (m > p) return;
+    const int nt = p + 1, nn = p + 1 - m, KP = leg_kpad(p), nch = KP / kLegK;
+    const int NF = leg_npad(nn), NI = leg_npad(nt);
+    const int cnt = T.z;
+    extern __shared__ __align__(1024) unsigned char leg_smem[];
+    unsigned char* sA = leg_smem;                     // A chunk hi | lo (2 x 16 KB)
+    unsigned char* sB = leg_smem + 2 * 128 * kLegK * 4;  // B chunk hi | lo (N <= 48)
+    __shared__ float sC[kLegSpheres][6][33];          // forward results (s, kind, n - m)
+    __shared__ float sF[kLegSpheres][6 * 33];         // column m of the tile: [component][ring] complex
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, 128);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+        s_fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const int sl = tid / 6, kind = tid - 6 * (tid / 6);
+    const int sph = sl < cnt ? g.leg_sph[T.y + sl] : 0;
+    const bool row_ok = sl < cnt && (!g.active || g.active[g.prob[sph]]);
+    // column m of every sphere of the tile (fg: per sphere [m][component][ring] complex), coalesced
+    for (int i = tid; i < cnt * 6 * nt; i += 128) {
+        const int s2 = i / (6 * nt), w = i - s2 * 6 * nt;
+        sF[s2][w] = fg[fg_stride * g.leg_sph[T.y + s2] + (long long)m * 6 * nt + w];
+    }
+    __syncthreads();
+    const float* tabs = g.leg_tab + g.leg_off[2 * (p * (kMaxOrder + 1) + m)];
+    const float* tabi = g.leg_tab + g.leg_off[2 * (p * (kMaxOrder + 1) + m) + 1];
+    unsigned phase = 0;
+
+    // one GEMM: D[128 x N] at tensor-memory column dcol, A rows built by `arow(K index) -> value`,
+    // B chunks from `tab` ([chunk][N x kLegK] in the operand layout)
+    auto gemm = [&](int N, const float* tab, uint32_t dcol, auto&& arow) {
+        for (int ch = 0; ch < nch; ++ch) {
+            // B chunk: copy and split
+            const float4* gb = reinterpret_cast<const float4*>(tab + (long long)ch * N * kLegK);
+            for (int v = tid; v < N * kLegK / 4; v += 128) {
+                const float4 b = __ldg(gb + v);
+                float4 h, l;
+                tc::tf32_split(b.x, h.x, l.x);
+                tc::tf32_split(b.y, h.y, l.y);
+                tc::tf32_split(b.z, h.z, l.z);
+                tc::tf32_split(b.w, h.w, l.w);
+                reinterpret_cast<float4*>(sB)[v] = h;
+                reinterpret_cast<float4*>(sB + N * kLegK * 4)[v] = l;
+            }
+            // A chunk: this thread's row
+#pragma unroll 2
+            for (int q = 0; q < kLegK / 4; ++q) {
+                float4 h, l;
+                float v[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) v[e] = arow(ch * kLegK + 4 * q + e);
+                tc::tf32_split(v[0], h.x, l.x);
+                tc::tf32_split(v[1], h.y, l.y);
+                tc::tf32_split(v[2], h.z, l.z);
+                tc::tf32_split(v[3], h.w, l.w);
+                const uint32_t off = tc::kmajor_offset(tid, 4 * q, kLegK);
+                *reinterpret_cast<float4*>(sA + off) = h;
+                *reinterpret_cast<float4*>(sA + 128 * kLegK * 4 + off) = l;
+            }
+            tc::fence_smem_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::idesc_tf32(128, N);
+                const uint32_t a0 = tc::smem_u32(sA), al0 = a0 + 128 * kLegK * 4;
+                const uint32_t b0 = tc::smem_u32(sB), bl0 = b0 + N * kLegK * 4;
+                for (int ks = 0; ks < kLegK / 8; ++ks) {
+                    const uint32_t o = ks * 256;
+                    const uint64_t ah = tc::sdesc(a0 + o, 128, (kLegK / 4) * 128);
+                    const uint64_t al = tc::sdesc(al0 + o, 128, (kLegK / 4) * 128);
+                    const uint64_t bh = tc::sdesc(b0 + o, 128, (kLegK / 4) * 128);
+                    const uint64_t bl = tc::sdesc(bl0 + o, 128, (kLegK / 4) * 128);
+                    tc::mma_tf32(tmem + dcol, ah, bh, idesc, ch > 0 || ks > 0);
+                    tc::mma_tf32(tmem + dcol, ah, bl, idesc, true);
+                    tc::mma_tf32(tmem + dcol, al, bh, idesc, true);
+                }
+                tc::mma_commit(&mbar);
+            }
+            // the stage is refilled next: wait for this chunk's MMAs
+            if (!tc::mbar_wait_bounded(&mbar, phase, kLegWaitPolls)) s_fail = 1;
+            phase ^= 1;
+            __syncthreads();
+            if (s_fail) return false;
+        }
+        return true;
+    };
+
+    // ---- forward: A_f row (s, kind) = the phi-DFT values of column m at ring j (K = b * nt + j)
+    auto arow_f = [&](int k) -> float {
+        if (!row_ok || k >= 3 * nt) return 0.f;
+        const int b = k / nt, j = k - b * nt;
+        const float* f = sF[sl];
+        return leg_a(kind, b, f[2 * j], f[2 * j + 1], f[2 * (nt + j)], f[2 * (nt + j) + 1], f[2 * (2 * nt + j)],
+                     f[2 * (2 * nt + j) + 1]);
+    };
+    bool ok = gemm(NF, tabs, 0, arow_f);
+    float d[64];
+    if (ok) {
+        tc::fence_after_sync();
+        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16), *reinterpret_cast<float(*)[32]>(d));
+        if (NF > 32) tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16) + 32, *reinterpret_cast<float(*)[32]>(d + 32));
+        tc::fence_before_sync();
+        // coefficients of column m (times 1 / (n (n + 1)) for the gradient and toroidal parts)
+        if (row_ok && tid < 6 * kLegSpheres) {
+            const int nc = ncoef(p);
+            const int blk = kind >> 1, im = kind & 1;
+            for (int l = 0; l < nn; ++l) {
+                const int n = m + l;
+                const float inv = blk == 0 ? 1.f : (n > 0 ? 1.f / float(n * (n + 1)) : 0.f);
+                const float v = d[l] * inv;
+                sC[sl][kind][l] = v;
+                if (coef_out) coef_out[2LL * g.coff[sph] + 2 * (blk * nc + cidx(n, m)) + im] = v;
+            }
+        }
+        __syncthreads();
+        // self operator multipliers per (s, n), in place (the formulas of k_sphere)
+        for (int it = tid; it < cnt * nn; it += 128) {
+            const int s2 = it / nn, l = it - s2 * nn, n = m + l;
+            const float dn = float(n);
+            float lh, lg, lx;
+            if (self_kind == 0) {
+                lh = dn / ((2 * dn + 1) * (2 * dn + 3));
+                lg = (dn + 1) / ((2 * dn - 1) * (2 * dn + 1));
+                lx = 1.f / (2 * dn + 1);
+            } else if (self_kind == 4) {
+                const float dh = 0.5f + 3.f / (2 * (2 * dn + 1) * (2 * dn + 3));
+                const float dg = n == 1 ? 1.f : 0.5f - 3.f / (2 * (2 * dn - 1) * (2 * dn + 1));
+                const float dx = n == 1 ? 1.f : 0.5f - 3.f / (2 * (2 * dn + 1));
+                lh = 1.f / dh - 2;
+                lg = 1.f / dg - 2;
+                lx = 1.f / dx - 2;
+            } else {
+                lh = 3.f / (2 * (2 * dn + 1) * (2 * dn + 3));
+                lg = -3.f / (2 * (2 * dn - 1) * (2 * dn + 1));
+                lx = -3.f / (2 * (2 * dn + 1));
+            }
+            for (int c = 0; c < 2; ++c) {
+                const float cr = sC[s2][c][l], cs = sC[s2][2 + c][l], cx = sC[s2][4 + c][l];
+                const float h = (cr - dn * cs) * lh;
+                const float gg = (cr + (dn + 1) * cs) / (2 * dn + 1) * lg;
+                sC[s2][c][l] = h * ((dn + 1) / (2 * dn + 1)) + dn * gg;
+                sC[s2][2 + c][l] = n > 0 ? (-h / (2 * dn + 1) + gg) : 0.f;
+                sC[s2][4 + c][l] = n > 0 ? lx * cx : 0.f;
+            }
+        }
+        __syncthreads();
+        // ---- inverse: A_i row (s, kind) = the multiplied coefficients of column m (K = b * nt + n - m)
+        auto arow_i = [&](int k) -> float {
+            if (!row_ok || k >= 3 * nt) return 0.f;
+            const int b = k / nt, l = k - b * nt;
+            if (l >= nn) return 0.f;
+            return leg_a(kind, b, sC[sl][0][l], sC[sl][1][l], sC[sl][2][l], sC[sl][3][l], sC[sl][4][l], sC[sl][5][l]);
+        };
+        ok = gemm(NI, tabi, 64, arow_i);
+    }
+    if (ok) {
+        tc::fence_after_sync();
+        tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16) + 64, *reinterpret_cast<float(*)[32]>(d));
+        if (NI > 32)
+            tc::tmem_ld_32x32b_x32(tmem + (uint32_t(warp * 32) << 16) + 96, *reinterpret_cast<float(*)[32]>(d + 32));
+        tc::fence_before_sync();
+        if (row_ok && tid < 6 * kLegSpheres) {
+            // kind -> (component, Re/Im) of the values at (ring j, m), doubled for m > 0
+            const float e = m == 0 ? 1.f : 2.f;
+            float* fo = fg + fg_stride * sph + (long long)m * 6 * nt;
+            const int comp = kind >> 1, im = kind & 1;
+            for (int j = 0; j < nt; ++j) fo[2 * (comp * nt + j) + im] = e * d[j];
+        }
+    } else if (tid == 0) {
+        atomicExch(g.err, 2);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 128);
+    }
+}
+
 template <typename Real>
 size_t sphere_smem(int pmax) {
     const int ng = (pmax + 1) * (2 * pmax + 2), nt = pmax + 1, P1 = pmax + 1, nc = ncoef(pmax);
@@ -343,6 +620,22 @@ template <typename Real>
 int launch_sphere(const DevGeom& g, SphereArgs a, cudaStream_t st) {
     k_sphere<Real><<<g.N, kSphereThreads, sphere_smem<Real>(g.pmax), st>>>(g, table_of<Real>(g), a);
     return 1;
+}
+
+constexpr size_t kLegDynSmem = 2 * 128 * kLegK * 4 + 2 * 48 * kLegK * 4;  // A and B chunk stages (44 KB)
+
+// the FP32 sphere operator with its Legendre stage on the tensor cores (three launches)
+int launch_sphere_tc(const DevGeom& g, SphereArgs a, cudaStream_t st) {
+    a.fg = g.fgbuf;
+    a.fg_stride = g.fg_stride;
+    a.lop = g.lopbuf;
+    a.mode = 3;
+    k_sphere<float><<<g.N, kSphereThreads, sphere_smem<float>(g.pmax), st>>>(g, g.tab_f, a);
+    k_legendre_tc<<<dim3(g.n_leg_tiles, g.pmax + 1), 128, kLegDynSmem, st>>>(g, a.self_kind, g.fgbuf, g.fg_stride,
+                                                                           static_cast<float*>(a.coef_out));
+    a.mode = 4;
+    k_sphere<float><<<g.N, kSphereThreads, sphere_smem<float>(g.pmax), st>>>(g, g.tab_f, a);
+    return 3;
 }
 
 __global__ void k_rigid_density(DevGeom g, const double* __restrict__ f6, double* __restrict__ rho) {
@@ -471,6 +764,8 @@ __global__ void k_rigid_average(DevGeom g, const double* __restrict__ u, double 
 }  // namespace
 
 void configure_sphere_kernels() {
+    // 44 KB dynamic + 17 KB static shared memory: above the 48 KB a kernel gets without opting in
+    cudaFuncSetAttribute(k_legendre_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kLegDynSmem));
     cudaFuncSetAttribute(k_sphere<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(sphere_smem<float>(kMaxOrder)));
     cudaFuncSetAttribute(k_sphere<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -480,6 +775,7 @@ void configure_sphere_kernels() {
 int launch_sphere_op(const DevGeom& g, const double* x, double* out, double c_id, double c_self, int self_kind,
                      double c_lop, void* coef, bool fp32, cudaStream_t st) {
     SphereArgs a{x, nullptr, out, c_id, c_self, c_lop, self_kind, 0, coef};
+    if (fp32 && g.sph_tc && self_kind >= 0 && g.n_leg_tiles > 0) return launch_sphere_tc(g, a, st);
     return fp32 ? launch_sphere<float>(g, a, st) : launch_sphere<double>(g, a, st);
 }
 
