@@ -490,14 +490,16 @@ def test_sphere_operator_tensor_cores(oracle, orders):
     g = make(cfg)
     o = oracle_op(oracle, cfg)
     x = np.random.default_rng(45).standard_normal(3 * g.n_points)
+    assert not g.sphere_tc()  # the SIMT operator is the default (faster at these sizes)
     for coefs in ((0.5, 0.0, 1.0), (0.0, 1.0, 0.0), (0.2, 0.8, -0.4)):
         ref = o.apply_p2p(x, *coefs)
+        g.set_sphere_tc(True)
         tc = g.applyP2POP(x, None, *coefs, precision=PREC_MIXED)
         g.set_sphere_tc(False)
         simt = g.applyP2POP(x, None, *coefs, precision=PREC_MIXED)
-        g.set_sphere_tc(True)
         assert rel(tc, ref) < 2e-5 and rel(simt, ref) < 2e-5, (coefs, rel(tc, ref), rel(simt, ref))
         assert rel(tc, simt) < 2e-5
+    g.set_sphere_tc(True)
     assert rel(g.apply(x, precision=PREC_MIXED), o.apply(x)) < 2e-5
 
 
@@ -509,10 +511,9 @@ def test_sphere_tensor_cores_several_tiles():
     g = make(cfg, SphereSTKMobMat)
     x = np.random.default_rng(46).standard_normal(3 * g.n_points)
     ref = g.apply(x, precision=PREC_FP64)
-    tc = g.apply(x, precision=PREC_MIXED)
-    g.set_sphere_tc(False)
     simt = g.apply(x, precision=PREC_MIXED)
     g.set_sphere_tc(True)
+    tc = g.apply(x, precision=PREC_MIXED)
     assert rel(tc, ref) < 2e-5 and rel(tc, simt) < 1e-5
     v = g.solveMob(cfg["force"], tol=1e-10, precision=PREC_MIXED, precond=1)
     assert g.last_stats[0]["status"] == 0
