@@ -829,7 +829,8 @@ def far_once():
 
 def near_once():
     """One near-field pass (FP32 traction on the tensor cores, FP64 traction, FP32 traction on the SIMT
-    pipes) on the first 64 problems of cfg4: the batched shape, where every target point has near pairs."""
+    pipes, then with the sphere operator's Legendre stage on the tensor cores) on the first 64 problems
+    of cfg4: the batched shape, where every target point has near pairs."""
     from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
     c = configs.cfg4(n_problems=64)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"], problem=c["problem"])
@@ -839,9 +840,12 @@ def near_once():
     g.set_near_tc(False)
     g.set_sphere_tc(False)
     c = g.near_field(x, cTrac=1.0, precision=PREC_MIXED)  # the SIMT kernels, for the launch list
+    g.set_sphere_tc(True)
+    d = g.near_field(x, cTrac=1.0, precision=PREC_MIXED)  # the sphere operator with k_legendre_tc
     print(json.dumps({"near_once": "cfg4[:64]", "points": int(g.n_points), "near_pairs": int(g.n_near_pairs),
                       "rel_diff_fp32_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-                      "rel_diff_simt_fp64": float(np.linalg.norm(c - b) / np.linalg.norm(b))}))
+                      "rel_diff_simt_fp64": float(np.linalg.norm(c - b) / np.linalg.norm(b)),
+                      "rel_diff_legendre_tc_fp64": float(np.linalg.norm(d - b) / np.linalg.norm(b))}))
 
 
 def main():
