@@ -827,6 +827,17 @@ def far_once():
                       np.isfinite(b).all() and np.isfinite(d).all())}))
 
 
+def solve_once():
+    """Three mixed-precision cfg2 solves (the first captures the graphs), for a kernel launch list."""
+    from spheresimulator_gb300 import PREC_MIXED, SphereSTKMobMat, configs
+    c = configs.cfg2()
+    mob = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    for _ in range(3):
+        v = mob.solveMob(c["force"], tol=TOL, restart=RESTART, max_iters=1000, precision=PREC_MIXED)
+    print(json.dumps({"solve_once": "cfg2", "iterations": mob.last_stats[0]["iterations"],
+                      "relres": mob.last_stats[0]["relres"], "finite": bool(np.isfinite(v).all())}))
+
+
 def near_once():
     """One near-field pass (FP32 traction on the tensor cores, FP64 traction, FP32 traction on the SIMT
     pipes, then with the sphere operator's Legendre stage on the tensor cores) on the first 64 problems
@@ -879,6 +890,8 @@ def main():
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
+    ap.add_argument("--solve-once", action="store_true",
+                    help="three mixed cfg2 solves and exit; a short program for a kernel launch list")
     ap.add_argument("--near-once", action="store_true",
                     help="one near-field pass (FP32, FP64) on 64 problems of cfg4 and exit; a short program for ncu")
     args = ap.parse_args()
@@ -887,6 +900,9 @@ def main():
         return
     if args.near_once:
         near_once()
+        return
+    if args.solve_once:
+        solve_once()
         return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
