@@ -548,8 +548,10 @@ def run_serving(args, world, rank, local, dist):
     from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SolveServer, configs
     stream = configs.cfg5_stream(seed=5 + rank, n_requests=args.requests, rate=args.rate, nmax=args.nmax)
 
-    def serve(reqs, precision, slots):
-        srv = SolveServer(device=local, max_slots=slots, precision=precision, hbm_budget_bytes=args.hbm_budget)
+    def serve(reqs, precision, slots, small_sms=0):
+        srv = SolveServer(device=local, max_slots=slots, precision=precision, hbm_budget_bytes=args.hbm_budget,
+                          small_sms=small_sms)
+        part = srv.partition_info()
         ids = [None] * len(reqs)
         t_start = time.perf_counter()
 
@@ -569,12 +571,48 @@ def run_serving(args, world, rank, local, dist):
         lat = np.array([x["t_done"] - x["t_submit"] for x in infos])
         span = max(x["t_done"] for x in infos) - min(x["t_submit"] for x in infos)
         ok = all(x["status"] == 0 for x in infos)
+        st["partition_sms"] = list(part)
         return lat, span, st, ok, infos
+
+    sizes_all = np.array([len(r["radii"]) for r in stream])
+
+    def buckets(lat):
+        out = {}
+        for name, lo, hi in (("n<=64", 0, 64), ("64<n<=512", 64, 512), ("n>512", 512, 1 << 30)):
+            m = (sizes_all > lo) & (sizes_all <= hi)
+            if m.any():
+                out[name] = {"requests": int(m.sum()), "p50_ms": round(1e3 * float(np.percentile(lat[m], 50)), 2),
+                             "p99_ms": round(1e3 * float(np.percentile(lat[m], 99)), 2)}
+        return out
 
     barrier(dist)
     with ClockSampler(local) as clk:
-        lat, span, st, ok, infos = serve(stream, PREC_MIXED, args.slots)
+        lat, span, st, ok, infos = serve(stream, PREC_MIXED, args.slots, args.small_sms)
     total = allmax(dist, span)
+    if args.serve_log and rank == 0:
+        with open(args.serve_log, "w") as fh:
+            for r, x in zip(stream, infos):
+                fh.write(json.dumps({"n": len(r["radii"]), "p": int(r["orders"][0]), "tol": r["tol"],
+                                     "arrival": round(r["arrival"], 4), "queue_ms": round(1e3 * (x["t_admit"] - x["t_submit"]), 2),
+                                     "ctx_ms": round(1e3 * (x["t_ctx"] - x["t_admit"]), 2),
+                                     "solve_ms": round(1e3 * (x["t_done"] - x["t_ctx"]), 2),
+                                     "iterations": x["stats"]["iterations"]}) + "\n")
+    # the same stream without the SM partition (stream priorities only), for comparison
+    nopart = None
+    if args.compare_partition and args.small_sms > 0:
+        lat0, span0, _, ok0, _ = serve(stream, PREC_MIXED, args.slots, 0)
+        nopart = {"solves_per_s": round(len(stream) / span0, 4), "p50_ms": round(1e3 * float(np.percentile(lat0, 50)), 2),
+                  "p99_ms": round(1e3 * float(np.percentile(lat0, 99)), 2), "by_size": buckets(lat0), "all_ok": ok0}
+    # the small requests (n <= 64) solved one at a time on an idle server: their solo latency
+    small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= 64][:8]
+    solo = None
+    if small:
+        sl = []
+        for r in small:
+            l1, _, _, _, _ = serve([r], PREC_MIXED, 1, 0)
+            sl.append(float(l1[0]))
+        solo = {"requests": len(small), "p50_ms": round(1e3 * float(np.percentile(sl, 50)), 2),
+                "max_ms": round(1e3 * max(sl), 2)}
     sub = None
     if args.fp64_subset > 0:
         small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= args.fp64_subset]
@@ -602,6 +640,12 @@ def run_serving(args, world, rank, local, dist):
                    "l2": "not flushed: requests arrive in real time, latency measured on the server clock"},
         "latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 2),
                        "p99": round(1e3 * float(np.percentile(lat, 99)), 2)},
+        "latency_by_size": buckets(lat),
+        "small_requests_solo": solo,
+        "without_sm_partition": nopart,
+        "sm_partition": {"small_sms": st["partition_sms"][0], "big_sms": st["partition_sms"][1],
+                         "note": "green contexts: requests with < 1e9 far-field pairs run on the small partition "
+                                 "while a big request runs (on the whole device otherwise); big requests on the rest"},
         "queue_wait_ms_p50": round(1e3 * float(np.percentile([x["t_admit"] - x["t_submit"] for x in infos], 50)), 2),
         "all_converged": ok, "span_s": round(total, 3),
         "requests": {"spheres_min": int(min(sizes)), "spheres_max": int(max(sizes)), "spheres_median": float(np.median(sizes))},
@@ -875,6 +919,12 @@ def main():
     ap.add_argument("--nmax", type=int, default=2048, help="cfg5: largest sphere count of a request")
     ap.add_argument("--slots", type=int, default=8, help="cfg5: requests on the GPU at once")
     ap.add_argument("--hbm-budget", type=float, default=0.0, help="cfg5: admission budget in bytes (0: 64 GB)")
+    ap.add_argument("--small-sms", type=int, default=16,
+                    help="cfg5: SMs reserved (green context) for small requests while big ones run (0: none)")
+    ap.add_argument("--serve-log", default="",
+                    help="cfg5: write one JSON line per request (size, queue and run times) to this file")
+    ap.add_argument("--compare-partition", action="store_true",
+                    help="cfg5: also serve the stream without the SM partition")
     ap.add_argument("--fp64-subset", type=int, default=0,
                     help="cfg5: also serve the requests with at most this many spheres in mixed and plain FP64")
     ap.add_argument("--multi", type=int, default=0,

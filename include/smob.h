@@ -53,7 +53,7 @@ typedef enum {
     SMOB_PREC_FP64 = 0,  /* every kernel in FP64 */
     SMOB_PREC_MIXED = 1, /* solves: FP32 operator inside high-precision iterative refinement (FP64 Arnoldi,
                             Givens; residuals with the float-float operator); operator calls: all FP32 */
-    SMOB_PREC_FLOAT_FLOAT = 2 /* FP64 sphere/near kernels with the far field in float-float (hi+lo float
+    SMOB_PREC_FLOAT_FLOAT = 2 /* FP64 sphere kernels with the far and near fields in float-float (hi+lo float
                                  pairs on the FP32 pipe, ~48 bits): the high-precision operator of MIXED;
                                  for solves, plain restarted GMRES with this operator throughout */
 } smob_precision;
@@ -130,7 +130,9 @@ smob_status smob_project_null_space(smob_ctx* ctx, double* inout);
  * sums every pair, SMOB_PREC_MIXED (FP32) and SMOB_PREC_FLOAT_FLOAT read coarse equivalent sources for
  * well-separated sphere pairs at the context's tolerances (smob_set_far_compression) */
 smob_status smob_far_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
-/* spectral evaluation of the near-pair source spheres at their targets (no direct subtraction) */
+/* spectral evaluation of the near-pair source spheres at their targets (no direct subtraction): FP64,
+ * FP32 (SMOB_PREC_MIXED: tensor cores or SIMT, smob_set_near_tc), or float-float arithmetic on the FP64
+ * coefficients (SMOB_PREC_FLOAT_FLOAT, the kernel of the high-precision passes) */
 smob_status smob_near_field(smob_ctx* ctx, const double* in, double* out, double c_sl, double c_trac, int precision);
 /* per-sphere G2S / S2G in the layout above (Shexp::calcSpectralCoeff / calcGridValue, Shexp.cpp:342-447) */
 smob_status smob_sh_g2s(smob_ctx* ctx, const double* grid3m, double* coeff);
@@ -265,9 +267,11 @@ smob_status smob_solve_mob_multi(smob_ctx* ctx, int n_rhs, const double* force6n
 
 /* ---- serving: a request loop with continuous batching (no counterpart in the reference, which
  * solves one system per time step inside SphereSystem::resolveCollision, SRC/SphereSystem.cpp:403-479).
- * Requests (one independent problem each) are queued FIFO; up to max_slots of them are on the GPU
- * at once, each admitted when a slot is free and its device-memory footprint (smob_request_bytes)
- * fits in what the running requests leave of hbm_budget_bytes. Every request runs on its own
+ * Requests (one independent problem each) are queued FIFO in two queues, small requests (fewer than
+ * 1e9 far-field pairs) and big ones; up to max_slots of them are on the GPU at once, each admitted
+ * when a slot is free and its device-memory footprint (smob_request_bytes) fits in what the running
+ * requests leave of hbm_budget_bytes. The small queue is served first and big requests hold at most
+ * max_slots minus a quarter of the slots (at least one). Every request runs on its own
  * stream with its own device-resident Krylov state, so concurrent requests overlap on the device;
  * a request's result is the same alone or in any mix (each is solved exactly as if alone). */
 typedef struct smob_server smob_server;
@@ -286,6 +290,7 @@ typedef struct {
     double t_submit, t_admit, t_done; /* seconds since the server started */
     double bytes;            /* admission footprint */
     smob_problem_stats stats;
+    double t_ctx;            /* seconds since the server started: the request's context was ready (solve start) */
 } smob_request_info;
 typedef struct {
     int queued, running;
@@ -293,6 +298,8 @@ typedef struct {
     double bytes_in_use, peak_bytes, budget_bytes, uptime_s;
     int peak_running;
 } smob_server_info;
+/* The server keeps freed device memory in the device's stream-ordered pool (its release threshold set
+ * to the maximum) instead of returning it to the driver at every synchronisation. */
 smob_status smob_server_create(smob_server** server, const smob_server_opts* opts);
 smob_status smob_server_submit(smob_server* server, const smob_geometry* geom, const double* force6n, double tol,
                                long long* request_id);
@@ -302,6 +309,16 @@ smob_status smob_server_wait(smob_server* server, long long request_id, double t
                              smob_request_info* info);
 smob_status smob_server_release(smob_server* server, long long request_id);
 smob_status smob_server_stats(smob_server* server, smob_server_info* info);
+/* SM partition of the serving device (no counterpart in the reference): small_sms SMs (rounded up to the
+ * device's partition granularity, 8 on GB300) become a green context that small requests (fewer than
+ * 1e9 far-field pairs) use while a big request is running; big requests run on a green context of the
+ * remaining SMs; with no big request running a small one uses the whole device. Kernels already running
+ * are never preempted, so without the partition a small request waits behind the long CTAs of big
+ * ones. Results are the same bit for bit on any partition. 0 removes the partition. The server must be
+ * idle (nothing queued or running), otherwise SMOB_ERR_STATE. */
+smob_status smob_server_partition(smob_server* server, int small_sms);
+/* SMs of the small and the big partition (0, 0 without a partition) */
+smob_status smob_server_partition_info(smob_server* server, int* small_sms, int* big_sms);
 smob_status smob_server_destroy(smob_server* server);
 /* admission footprint estimate (bytes of device memory) of one request; host-only arithmetic */
 size_t smob_request_bytes(int n_spheres, const int* orders, int restart);

@@ -351,7 +351,8 @@ class SolveServer:
     """Request loop with continuous batching of mobility solves on one GPU (smob_server_*)."""
 
     def __init__(self, device=0, max_slots=8, hbm_budget_bytes=0.0, restart=50, max_iters=2000,
-                 precision=PREC_MIXED, inner_tol=0.0):
+                 precision=PREC_MIXED, inner_tol=0.0, small_sms=0):
+        """small_sms > 0: SMs reserved (green context) for small requests while big ones run"""
         self._L = N.lib()
         opts = N.ServerOpts(int(device), int(max_slots), float(hbm_budget_bytes), int(restart), int(max_iters),
                             int(precision), float(inner_tol))
@@ -359,6 +360,18 @@ class SolveServer:
         N.check(self._L.smob_server_create(ctypes.byref(h), ctypes.byref(opts)))
         self._h = h
         self._n = {}
+        if small_sms:
+            self.partition(small_sms)
+
+    def partition(self, small_sms):
+        """Split the device's SMs: small_sms for small requests while big ones run (0: no split)."""
+        N.check(self._L.smob_server_partition(self._h, int(small_sms)))
+
+    def partition_info(self):
+        """(SMs of the small partition, SMs of the big partition); (0, 0) without a partition."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        N.check(self._L.smob_server_partition_info(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def submit(self, centers, radii, orders, force, tol=1e-8, quats=None, viscosity=1.0):
         c = N.f64(centers).reshape(-1, 3)
@@ -398,7 +411,7 @@ class SolveServer:
     @staticmethod
     def _info(i):
         return {"state": i.state, "status": i.status, "t_submit": i.t_submit, "t_admit": i.t_admit,
-                "t_done": i.t_done, "bytes": i.bytes, "stats": i.stats.as_dict()}
+                "t_ctx": i.t_ctx, "t_done": i.t_done, "bytes": i.bytes, "stats": i.stats.as_dict()}
 
     def close(self):
         if getattr(self, "_h", None):

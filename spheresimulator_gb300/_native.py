@@ -61,7 +61,7 @@ class ServerOpts(ctypes.Structure):
 class RequestInfo(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
                 ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("bytes", ctypes.c_double),
-                ("stats", ProblemStats)]
+                ("stats", ProblemStats), ("t_ctx", ctypes.c_double)]
 
 
 class ServerInfo(ctypes.Structure):
@@ -156,6 +156,8 @@ def lib():
         "smob_server_release": (S, [_VP, ctypes.c_longlong]),
         "smob_server_stats": (S, [_VP, ctypes.POINTER(ServerInfo)]),
         "smob_server_destroy": (S, [_VP]),
+        "smob_server_partition": (S, [_VP, ctypes.c_int]),
+        "smob_server_partition_info": (S, [_VP, _IP, _IP]),
         "smob_request_bytes": (ctypes.c_size_t, [ctypes.c_int, _IP, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():

@@ -28,7 +28,8 @@
 using namespace smob;
 
 namespace smob {
-smob_status create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank);
+smob_status create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank,
+                           void* green_ctx = nullptr);
 }
 
 namespace {
@@ -1446,21 +1447,22 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
             {
                 ProfScope ps(c, "near_sets");
                 check_launch(c, launch_near_sets(g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(),
-                                                 tr ? c->set_stride_trac : c->set_stride_sl, c->st));
+                                                 tr ? c->set_stride_trac : c->set_stride_sl, c->st, dfar));
             }
             const long long stride = tr ? c->set_stride_trac : c->set_stride_sl;
             {
+                // FP32 (tensor cores or SIMT), float-float (the float-float operator) or FP64
                 ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
                 check_launch(c, launch_near_eval(g, sets, stride, tr, fp32, cc, out, c->st,
-                                                 fp32 && c->n_precise ? 1 : 0));
+                                                 fp32 && c->n_precise ? 1 : 0, dfar));
             }
             if (fp32 && c->n_precise) {
-                // near-singular pairs (gap < 0.1 min radius) in FP64 even inside the FP32 operator
-                ProfScope ps(c, "near_singular_fp64");
+                // near-singular pairs (gap < 0.1 min radius) in float-float even inside the FP32 operator
+                ProfScope ps(c, "near_singular_df");
                 check_launch(c, launch_sh_g2s(g, x, c->d_coef64.as<double>(), c->st));
                 check_launch(c, launch_near_sets(g, c->d_coef64.p, tr, false, c->d_sets64.p, nslots,
-                                                 c->d_slot_sphere.as<int>(), stride, c->st));
-                check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, cc, out, c->st, 2));
+                                                 c->d_slot_sphere.as<int>(), stride, c->st, true));
+                check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, cc, out, c->st, 2, true));
             }
         }
         fork.join();
@@ -1519,11 +1521,12 @@ void op_apply_hp_both(smob_ctx* c, const double* x, double* out_t, double c_id, 
             {
                 ProfScope ps(c, "near_sets");
                 check_launch(c, launch_near_sets(g, c->d_coef64.p, tr, false, c->d_sets64.p, nslots,
-                                                 c->d_slot_sphere.as<int>(), stride, c->st));
+                                                 c->d_slot_sphere.as<int>(), stride, c->st, true));
             }
-            ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
+            // float-float near field (the FP64 coefficients' sets as float pairs)
+            ProfScope ps(c, tr ? "near_eval_trac_df" : "near_eval_sl_df");
             check_launch(c, launch_near_eval(g, c->d_sets64.p, stride, tr, false, tr ? c_trac : c_sl, tr ? out_t : out_s,
-                                             c->st, 0));
+                                             c->st, 0, true));
         }
     }
     fork.join();
@@ -2104,10 +2107,39 @@ void set_device(const smob_ctx* c) { CUDA_OK(cudaSetDevice(c->device)); }
 
 // the context's main and side streams (non-blocking, priority prio: 0 is the default) and the
 // fork/join events of the operator passes
-void create_streams(smob_ctx* c, int prio) {
-    CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
+// cuGreenCtxStreamCreate, reached through the runtime (the library does not link libcuda)
+using GreenStreamFn = int (*)(void** stream, void* green_ctx, unsigned flags, int priority);
+GreenStreamFn green_stream_fn() {
+    static GreenStreamFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuGreenCtxStreamCreate", &f, 12050, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return reinterpret_cast<GreenStreamFn>(f);
+    }();
+    return fn;
+}
+
+// green: a green context (an SM partition of the device, CUgreenCtx) whose streams the context runs on,
+// or null for ordinary streams (the whole device)
+void create_streams(smob_ctx* c, int prio, void* green = nullptr) {
+    if (green) {
+        GreenStreamFn fn = green_stream_fn();
+        if (!fn) throw SmobError(SMOB_ERR_CUDA, "cuGreenCtxStreamCreate is not available");
+        void* a = nullptr;
+        void* b = nullptr;
+        if (fn(&a, green, 0x1 /* CU_STREAM_NON_BLOCKING */, prio) != 0 || fn(&b, green, 0x1, prio) != 0)
+            throw SmobError(SMOB_ERR_CUDA, "cuGreenCtxStreamCreate failed");
+        c->st = static_cast<cudaStream_t>(a);
+        c->st2 = static_cast<cudaStream_t>(b);
+    } else {
+        CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
+        CUDA_OK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, prio));
+    }
     c->sh.st = c->st;
-    CUDA_OK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, prio));
     c->sh2.st = c->st2;
     CUDA_OK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CUDA_OK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
@@ -2246,7 +2278,8 @@ smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
 // Context creation with a stream priority: priority_rank 0 is the device's highest stream
 // priority, larger ranks step towards the lowest; -1 keeps the default. The server gives small
 // requests high priority so their kernels are scheduled ahead of large requests' blocks.
-smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank) {
+smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank,
+                                 void* green_ctx) {
     return guarded([&]() -> smob_status {
         need(out != nullptr && geo != nullptr, "null argument");
         *out = nullptr;
@@ -2268,7 +2301,7 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
             CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
             prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
         }
-        create_streams(c.get(), prio);
+        create_streams(c.get(), prio, green_ctx);
         AllocStreamScope scope(c->st);
         configure_sphere_kernels();
         configure_near_kernels();
@@ -2524,6 +2557,7 @@ smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c
         set_device(c);
         all_active(c);
         const bool fp32 = precision == SMOB_PREC_MIXED;
+        const bool df = precision == SMOB_PREC_FLOAT_FLOAT;  // float-float evaluation of the FP64 sets
         const int nslots = (int)c->slot_sphere.size();
         host_io(c, in, out, true, [&](const double* din, double* dout) {
             if (nslots == 0) return;
@@ -2543,10 +2577,10 @@ smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c
                 {
                     ProfScope ps(c, "near_sets");
                     check_launch(c, launch_near_sets(c->g, coef, tr, fp32, sets, nslots, c->d_slot_sphere.as<int>(),
-                                                     stride, c->st));
+                                                     stride, c->st, df));
                 }
                 ProfScope ps(c, tr ? "near_eval_trac" : "near_eval_sl");
-                check_launch(c, launch_near_eval(c->g, sets, stride, tr, fp32, cc, dout, c->st));
+                check_launch(c, launch_near_eval(c->g, sets, stride, tr, fp32, cc, dout, c->st, 0, df));
             }
         });
         prof_flush(c);

@@ -17,6 +17,7 @@
 //       4 pi t_i = n_i div L - x_j n_k d_i d_k L_j + n_k d_i d_k L_r       (traction)
 //       8 pi u_i = L_i - x_j d_i L_j + d_i L_r                             (single layer, x radius)
 //     and rotates back into the lab frame. Accumulation per target point is in a fixed order.
+#include "df.h"
 #include "smob_internal.h"
 #include "tc_sm100.h"
 
@@ -93,7 +94,9 @@ __device__ __forceinline__ void near_assemble(const DevGeom& g, int s, const A* 
 // the K order of the tensor-core contraction.
 __host__ __device__ __forceinline__ int rec_pos(int n, int m, int Nd) { return m * (Nd + 1) - m * (m - 1) / 2 + (n - m); }
 
-// tiled: write the sets as the B operand of k_near_eval_tc instead of [idx][set] complex: per chunk of
+// tiled = 2 (FP64 map): the [idx][set] complex layout with every value as a float pair (hi, lo) in the
+// 8 bytes of the double, for the float-float kernel k_near_eval_df.
+// tiled = 1: write the sets as the B operand of k_near_eval_tc instead of [idx][set] complex: per chunk of
 // kNearTcChunk harmonics (in recurrence order) an NN x 2 kNearTcChunk FP32 tile in the K-major
 // core-matrix layout of tc_sm100.h (row = set, K = (Re, -Im) of each harmonic); the padding (sets
 // >= NS, harmonics past ncoef(p + 3)) stays as cleared at allocation.
@@ -124,6 +127,12 @@ __global__ void k_near_sets(DevGeom g, const Real* __restrict__ coef, const Real
         for (int e = e0; e < e1; ++e) acc += mapval[e] * cin[g.map_col[e]];
         if (!tiled) {
             out[r] = acc;
+            continue;
+        }
+        if (tiled == 2) {
+            // float-float sets for k_near_eval_df: the [idx][set] complex layout, each value (hi, lo)
+            const float hi = float(acc);
+            reinterpret_cast<float2*>(out)[r] = make_float2(hi, float(acc - double(hi)));
             continue;
         }
         // row r = (idx, set, re/im) of the [idx][set] complex layout
@@ -326,6 +335,144 @@ __global__ void __launch_bounds__(kNearThreads, near_ppt<Real, LANES>() == 2 ? 3
             out[3 * i[p] + 1] += c * res[p][1];
             out[3 * i[p] + 2] += c * res[p][2];
         }
+}
+
+// ---------------------------------------------------------------- float-float near field
+// The near field of the high-precision passes (the mixed solve's residual pass, SMOB_PREC_FLOAT_FLOAT,
+// the near-singular pairs of the FP32 passes) in float-float arithmetic on the FP32 pipes instead of
+// FP64: GB300 runs FP64 at 1/58 of the FP32 rate, and the ~10^4 multiply-adds per target and source
+// of the contraction dominate. The body frame (FP64 subtraction and rotation) and the assembly of the
+// traction or velocity stay in FP64; the solid-harmonic recurrence and the contraction with the sets
+// (float pairs written by k_near_sets) run in float-float (~2^-44 relative per operation, far below the
+// 1e-10 the refinement residuals need). One target point per thread, the source's sets staged in shared
+// memory when they fit, as in k_near_eval.
+template <typename T>
+__device__ __forceinline__ df1 dfd(T v) {  // FP64 value as a float pair
+    const float h = float(v);
+    return {h, float(double(v) - double(h))};
+}
+// Re(c Th) for complex c = (cr, ci) and Th = (tr, ti), unnormalised (as df_dot3)
+__device__ __forceinline__ df1 df_cre(const float4& c, const df1& tr, const df1& ti) {
+    const float p0 = v_mul(c.x, tr.h), p1 = v_mul(-c.z, ti.h);
+    float lo = v_add(v_fma(c.x, tr.h, -p0), v_fma(-c.z, ti.h, -p1));
+    lo = v_fma(c.x, tr.l, v_fma(c.y, tr.h, lo));
+    lo = v_fma(-c.z, ti.l, v_fma(-c.w, ti.h, lo));
+    const df1 s = two_sum(p0, p1);
+    return {s.h, v_add(s.l, lo)};
+}
+__device__ __forceinline__ df1 df_neg(df1 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ df1 df_add(df1 a, df1 b) {
+    const df1 s = two_sum(a.h, b.h);
+    return {s.h, v_add(s.l, v_add(a.l, b.l))};
+}
+
+template <bool TRAC, bool STAGE>
+__global__ void __launch_bounds__(kNearThreads, 2)
+    k_near_eval_df(DevGeom g, const float2* __restrict__ sets, long long stride, const double* __restrict__ th,
+                   int th_c1, int th_c2, int th_diag, double c, int pair_filter, int tile_major,
+                   double* __restrict__ out) {
+    constexpr int NS = TRAC ? kNearSetsTrac : kNearSetsSL;
+    const int t = tile_major ? blockIdx.y : blockIdx.x;
+    const int tile = tile_major ? blockIdx.x : blockIdx.y;
+    if (g.active && !g.active[g.prob[t]]) return;
+    const int e0 = g.nbr_start[t], e1 = g.nbr_start[t + 1];
+    const int ng = g.glen[t];
+    if (e0 == e1 || tile * kNearThreads >= ng) return;
+    const int j = tile * kNearThreads + threadIdx.x;
+    const bool valid = j < ng;
+    const int i = g.gidx[t] + (valid ? j : 0);
+    double X[3], Nl[3], res[3] = {0, 0, 0};
+    for (int d = 0; d < 3; ++d) {
+        X[d] = g.coords[3 * i + d];
+        Nl[d] = g.norms[3 * i + d];
+    }
+    // staged: [sets of one source: NS ncoef(pmax+3) complex as float4 (re hi, re lo, im hi, im lo)]
+    // [c1, c2: ncoef(pmax+3) float pairs][diag: pmax+4 float pairs]
+    extern __shared__ __align__(16) unsigned char near_df_smem[];
+    const int ncd = ncoef(g.pmax + 3);
+    float4* sS = reinterpret_cast<float4*>(near_df_smem);
+    float4* t12 = sS + (STAGE ? NS * ncd : 0);  // (c1 hi, c1 lo, c2 hi, c2 lo)
+    float2* tdg = reinterpret_cast<float2*>(t12 + ncd);
+    for (int k = threadIdx.x; k < ncd; k += blockDim.x) {
+        const df1 a = dfd(th[th_c1 + k]), b = dfd(th[th_c2 + k]);
+        t12[k] = make_float4(a.h, a.l, b.h, b.l);
+    }
+    for (int k = threadIdx.x; k < g.pmax + 4; k += blockDim.x) {
+        const df1 a = dfd(th[th_diag + k]);
+        tdg[k] = make_float2(a.h, a.l);
+    }
+    __syncthreads();
+    for (int e = e0; e < e1; ++e) {
+        if (pair_filter == 1 && g.nbr_precise[e]) continue;  // (uniform over the CTA)
+        if (pair_filter == 2 && !g.nbr_precise[e]) continue;
+        const int s = g.nbr_src[e];
+        const float4* S = reinterpret_cast<const float4*>(sets + stride * g.near_src_slot[s]);
+        const int Nd = g.order[s] + 3;
+        if (STAGE) {
+            __syncthreads();  // the previous source's sets are done
+            const int nv = NS * ncoef(Nd);
+            for (int k = threadIdx.x; k < nv; k += blockDim.x) sS[k] = __ldg(S + k);
+            __syncthreads();
+            S = sS;
+        }
+        double xs[3], nb[3];
+        near_frame<double>(g, s, X, Nl, xs, nb);
+        const df1 x = dfd(xs[0]), y = dfd(xs[1]), z = dfd(xs[2]);
+        const df1 r2 = df_sqr3(x, y, z);
+        const df1 ri = df_rsqrt(r2);
+        const df1 ir2 = df_mul_u(ri, ri);
+        const df1 zi = df_mul_u(z, ir2);
+        df1 dr = ri, di = {0.f, 0.f};  // Th_m^m
+        df1 ah[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) ah[k] = {0.f, 0.f};
+        for (int m = 0; m <= Nd; ++m) {
+            if (m > 0) {
+                // Th_m^m = -d_m (x + i y) Th_{m-1}^{m-1} / r^2
+                const float2 dm = tdg[m];
+                const df1 f = df_neg(df_mul_u(df1{dm.x, dm.y}, ir2));
+                const df1 nr = df_mul_u(f, df_add(df_mul_u(x, dr), df_neg(df_mul_u(y, di))));
+                const df1 ni = df_mul_u(f, df_add(df_mul_u(x, di), df_mul_u(y, dr)));
+                dr = nr;
+                di = ni;
+            }
+            df1 pr = {0.f, 0.f}, pi = {0.f, 0.f}, cr = dr, ci = di;
+            for (int n = m; n <= Nd; ++n) {
+                const int idx = n * (n + 1) / 2 + m;
+                const float4* cs = S + NS * idx;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    const df1 v = df_cre(cs[k], cr, ci);
+                    df_acc(ah[k].h, ah[k].l, v);
+                }
+                if (n < Nd) {
+                    // Th_{n+1}^m = -(c1 z Th_n^m + c2 Th_{n-1}^m) / r^2
+                    const float4 a12 = t12[idx];
+                    const df1 a1 = {a12.x, a12.y}, a2 = {a12.z, a12.w};
+                    const df1 a1z = df_mul_u(a1, zi), a2r = df_mul_u(a2, ir2);
+                    const df1 nr = df_neg(df_add(df_mul_u(a1z, cr), df_mul_u(a2r, pr)));
+                    const df1 ni = df_neg(df_add(df_mul_u(a1z, ci), df_mul_u(a2r, pi)));
+                    pr = cr;
+                    pi = ci;
+                    cr = nr;
+                    ci = ni;
+                }
+            }
+        }
+        double acc[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) acc[k] = double(ah[k].h) + double(ah[k].l);
+        double vl[3];
+        near_assemble<TRAC, double, double>(g, s, acc, xs, nb, vl);
+        res[0] += vl[0];
+        res[1] += vl[1];
+        res[2] += vl[2];
+    }
+    if (valid) {
+        out[3 * i] += c * res[0];
+        out[3 * i + 1] += c * res[1];
+        out[3 * i + 2] += c * res[2];
+    }
 }
 
 // ---------------------------------------------------------------- tensor-core near field (FP32 passes)
@@ -554,7 +701,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 }  // namespace
 
 int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
-                     const int* slot_sphere, long long stride, cudaStream_t st) {
+                     const int* slot_sphere, long long stride, cudaStream_t st, bool df) {
     if (nslots <= 0) return 0;
     const size_t sm = size_t(6 * ncoef(g.pmax)) * (fp32 ? sizeof(float) : sizeof(double));
     // each slot's rows (2 x sets x ncoef(p+3), ~10^4) split over kSetSplit CTAs: few near-source spheres
@@ -568,7 +715,7 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
                                                   static_cast<float*>(sets), tiled ? 1 : 0);
     } else {
         k_near_sets<double><<<grid, 256, sm, st>>>(g, static_cast<const double*>(coef), g.map_val_d, trac,
-                                                   slot_sphere, stride, static_cast<double*>(sets), 0);
+                                                   slot_sphere, stride, static_cast<double*>(sets), df ? 2 : 0);
     }
     return 1;
 }
@@ -620,6 +767,13 @@ void configure_near_typed() {
     cudaFuncSetAttribute(k_near_eval<Real, TRAC, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
 }
 
+// dynamic shared memory of the float-float near kernel: one source's sets (staged) and the tables
+template <bool TRAC>
+size_t near_df_smem(int pmax, bool stage) {
+    const size_t ncd = ncoef(pmax + 3);
+    return (stage ? size_t(TRAC ? kNearSetsTrac : kNearSetsSL) * ncd * 16 : 0) + ncd * 16 + size_t(pmax + 4) * 8;
+}
+
 // dynamic shared memory of the tensor-core near kernel: the operand stage and the recurrence tables
 template <bool TRAC>
 size_t near_tc_smem(int pmax) {
@@ -627,6 +781,12 @@ size_t near_tc_smem(int pmax) {
 }
 
 void configure_near_kernels() {
+    cudaFuncSetAttribute(k_near_eval_df<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+    cudaFuncSetAttribute(k_near_eval_df<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kNearStageMax));
+    cudaFuncSetAttribute(k_near_eval_df<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_df_smem<true>(kMaxOrder, false)));
+    cudaFuncSetAttribute(k_near_eval_df<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_df_smem<false>(kMaxOrder, false)));
     cudaFuncSetAttribute(k_near_eval_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(near_tc_smem<true>(kMaxOrder)));
     cudaFuncSetAttribute(k_near_eval_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -637,8 +797,30 @@ void configure_near_kernels() {
     configure_near_typed<double, false>();
 }
 
+template <bool TRAC>
+void launch_near_df_typed(const DevGeom& g, const void* sets, long long stride, double c, int pair_filter,
+                          double* out, cudaStream_t st) {
+    const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);
+    const int tiles = (gmax + kNearThreads - 1) / kNearThreads;
+    const int tm = g.N <= 65535 ? 1 : 0;
+    const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
+    const float2* sp = static_cast<const float2*>(sets);
+    const size_t sm = near_df_smem<TRAC>(g.pmax, true);
+    if (sm <= kNearStageMax)
+        k_near_eval_df<TRAC, true><<<grid, kNearThreads, sm, st>>>(g, sp, stride, g.tab_d, g.th_c1, g.th_c2,
+                                                                   g.th_diag, c, pair_filter, tm, out);
+    else
+        k_near_eval_df<TRAC, false><<<grid, kNearThreads, near_df_smem<TRAC>(g.pmax, false), st>>>(
+            g, sp, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out);
+}
+
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
-                     cudaStream_t st, int pair_filter) {
+                     cudaStream_t st, int pair_filter, bool df) {
+    if (df && !fp32) {
+        if (trac) launch_near_df_typed<true>(g, sets, stride, c, pair_filter, out, st);
+        else launch_near_df_typed<false>(g, sets, stride, c, pair_filter, out, st);
+        return 1;
+    }
     if (fp32 && g.near_tc) {
         // one CTA per (target sphere, 256 of its grid points); tile-major (the tiles of a sphere adjacent)
         const int gmax = (g.pmax + 1) * (2 * g.pmax + 2);

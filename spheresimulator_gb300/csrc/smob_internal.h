@@ -283,11 +283,13 @@ int launch_sh_s2g(const DevGeom& g, const double* coef, double* grid, cudaStream
 // Near field: sets from coefficients (per near source sphere), then spectral evaluation per target sphere.
 // FP32 with g.near_tc: the sets are written as the tiles of the tensor-core kernel at stride
 // near_tile_stride(g.pmax, trac) per slot (`stride` is then not used); the buffer's padding must be zero.
+// df (FP64 coefficients only): the sets as float pairs (hi, lo) for the float-float evaluation
 int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, void* sets, int nslots,
-                     const int* slot_sphere, long long stride, cudaStream_t st);
-// pair_filter: 0 all near pairs, 1 pairs with gap >= 0.1 min radius, 2 the near-singular pairs only
+                     const int* slot_sphere, long long stride, cudaStream_t st, bool df = false);
+// pair_filter: 0 all near pairs, 1 pairs with gap >= 0.1 min radius, 2 the near-singular pairs only;
+// df (with fp32 false and float-pair sets): the float-float kernel instead of the FP64 one
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
-                     cudaStream_t st, int pair_filter = 0);
+                     cudaStream_t st, int pair_filter = 0, bool df = false);
 
 // Neighbour list on the device (nbrlist.cu): near pairs of every problem by the reference's rule
 // 0 < |c_s - c_t|^2 < (1.5 a_s + 1.5 a_t)^2 (problems[].s0/s1 and prob give each sphere's problem).

@@ -518,3 +518,21 @@ def test_sphere_tensor_cores_several_tiles():
     v = g.solveMob(cfg["force"], tol=1e-10, precision=PREC_MIXED, precond=1)
     assert g.last_stats[0]["status"] == 0
     assert rel(v, g.solveMob(cfg["force"], tol=1e-11, precision=PREC_FP64)) < 1e-8
+
+
+@pytest.mark.parametrize("orders", [(8, 8, 8, 8, 8), (6, 12, 16, 24, 32)])
+def test_near_field_float_float(oracle, orders):
+    """The near field of the high-precision passes in float-float on the FP32 pipes (k_near_eval_df:
+    recurrence and contraction as float pairs, FP64 frame and assembly) against the FP64 kernel and the
+    oracle's decomposition, traction and single layer, orders up to 32 (sets staged or read from L2)."""
+    cfg = configs.small_cluster(seed=47, n=5, p=8, gap=0.05, quats=True)
+    cfg["orders"] = np.asarray(orders)
+    g = make(cfg)
+    o = oracle_op(oracle, cfg)
+    x = np.random.default_rng(47).standard_normal(3 * g.n_points)
+    for c_sl, c_tr in ((0.0, 1.0), (1.0, 0.0), (0.3, -0.9)):
+        ref = g.near_field(x, c_sl, c_tr, precision=PREC_FP64)
+        df = g.near_field(x, c_sl, c_tr, precision=PREC_FLOAT_FLOAT)
+        assert rel(df, ref) < 1e-12, rel(df, ref)
+        full = o.far_traction(x, c_tr) + o.far_sl(x, c_sl) + o.near_correction(x, c_sl, c_tr)
+        assert rel(g.far_field(x, c_sl, c_tr, precision=PREC_FLOAT_FLOAT) + df, full) < 1e-11

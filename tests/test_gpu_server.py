@@ -58,3 +58,27 @@ def test_server_admission_respects_budget():
     spans = sorted((x["t_admit"], x["t_done"]) for x in infos)
     for (a0, d0), (a1, d1) in zip(spans, spans[1:]):
         assert a1 >= d0 - 1e-3
+
+
+def test_partitioned_server_results_equal_solo_solves():
+    """With the SMs split into green contexts (small requests on a reserved partition while a big one
+    runs, big requests on the rest), every result still equals its solo solve bit for bit (the kernels
+    are deterministic on any number of SMs), the partition has the requested size rounded to the
+    device's granularity, and the server cannot be re-partitioned while it has work."""
+    big = configs.cfg2()  # 36,992 points: above the 1e9-pair line of a small request
+    smalls = [configs.small_cluster(seed=80 + k, n=n, p=8, gap=0.1, quats=True) for k, n in enumerate((4, 9, 6))]
+    with SolveServer(max_slots=4, precision=PREC_MIXED, small_sms=12) as srv:
+        a, b = srv.partition_info()
+        assert a == 16 and a + b <= 152 and b >= 128  # 12 rounded up to the 8-SM granularity
+        ids = [srv.submit(big["centers"], big["radii"], big["orders"], big["force"], tol=1e-8)]
+        ids += [srv.submit(r["centers"], r["radii"], r["orders"], r["force"], tol=1e-8, quats=r["quats"])
+                for r in smalls]
+        from spheresimulator_gb300 import SmobError
+        with pytest.raises(SmobError):
+            srv.partition(0)  # requests are queued or running
+        out = [srv.wait(i, timeout=600) for i in ids]
+    for r, (vel, info) in zip([big] + smalls, out):
+        assert info["status"] == 0
+        solo = SphereSTKMobMat(r["centers"], r["radii"], r["orders"], quats=r.get("quats"))
+        assert np.array_equal(vel, solo.solveMob(r["force"], tol=1e-8, restart=50, max_iters=2000,
+                                                  precision=PREC_MIXED))
