@@ -596,7 +596,7 @@ def run_serving(args, world, rank, local, dist):
                                      "arrival": round(r["arrival"], 4), "queue_ms": round(1e3 * (x["t_admit"] - x["t_submit"]), 2),
                                      "ctx_ms": round(1e3 * (x["t_ctx"] - x["t_admit"]), 2),
                                      "solve_ms": round(1e3 * (x["t_done"] - x["t_ctx"]), 2),
-                                     "iterations": x["stats"]["iterations"]}) + "\n")
+                                     "iterations": x["stats"]["iterations"], "route": x["route"]}) + "\n")
     # the same stream without the SM partition (stream priorities only), for comparison
     nopart = None
     if args.compare_partition and args.small_sms > 0:

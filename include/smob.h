@@ -291,6 +291,7 @@ typedef struct {
     double bytes;            /* admission footprint */
     smob_problem_stats stats;
     double t_ctx;            /* seconds since the server started: the request's context was ready (solve start) */
+    int route;               /* SMs it ran on: 0 the whole device, 1 the small partition, 2 the big partition */
 } smob_request_info;
 typedef struct {
     int queued, running;
@@ -299,7 +300,9 @@ typedef struct {
     int peak_running;
 } smob_server_info;
 /* The server keeps freed device memory in the device's stream-ordered pool (its release threshold set
- * to the maximum) instead of returning it to the driver at every synchronisation. */
+ * to the maximum) instead of returning it to the driver at every synchronisation, and turns off the
+ * pool's reuse of blocks through inserted cross-stream waits (cudaMemPoolReuseAllowInternalDependencies),
+ * so one request's allocation never waits for another request's queued kernels. */
 smob_status smob_server_create(smob_server** server, const smob_server_opts* opts);
 smob_status smob_server_submit(smob_server* server, const smob_geometry* geom, const double* force6n, double tol,
                                long long* request_id);

@@ -411,7 +411,7 @@ class SolveServer:
     @staticmethod
     def _info(i):
         return {"state": i.state, "status": i.status, "t_submit": i.t_submit, "t_admit": i.t_admit,
-                "t_ctx": i.t_ctx, "t_done": i.t_done, "bytes": i.bytes, "stats": i.stats.as_dict()}
+                "t_ctx": i.t_ctx, "t_done": i.t_done, "route": i.route, "bytes": i.bytes, "stats": i.stats.as_dict()}
 
     def close(self):
         if getattr(self, "_h", None):

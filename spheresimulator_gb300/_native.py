@@ -61,7 +61,8 @@ class ServerOpts(ctypes.Structure):
 class RequestInfo(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
                 ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("bytes", ctypes.c_double),
-                ("stats", ProblemStats), ("t_ctx", ctypes.c_double)]
+                ("stats", ProblemStats), ("t_ctx", ctypes.c_double),
+                ("route", ctypes.c_int)]
 
 
 class ServerInfo(ctypes.Structure):

@@ -2105,6 +2105,14 @@ void need(bool cond, const char* msg) {
 
 void set_device(const smob_ctx* c) { CUDA_OK(cudaSetDevice(c->device)); }
 
+// Entry-point scope: the context's device, and its main stream for every device buffer the call
+// allocates or frees, so a lazily allocated buffer is ordered with the context's own work instead of
+// the legacy default stream that all threads share.
+struct CtxScope {
+    AllocStreamScope alloc;
+    explicit CtxScope(const smob_ctx* c) : alloc((set_device(c), c->st)) {}
+};
+
 // the context's main and side streams (non-blocking, priority prio: 0 is the default) and the
 // fork/join events of the operator passes
 // cuGreenCtxStreamCreate, reached through the runtime (the library does not link libcuda)
@@ -2354,7 +2362,7 @@ smob_status smob_set_geometry(smob_ctx* c, const double* centers, const double* 
         std::vector<double> q = c->quats;
         if (quats)
             for (int i = 0; i < c->N; ++i) unit_quat(quats + 4 * i, &q[4 * i], i);
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         update_geometry(c, ce, q);
         return SMOB_OK;
@@ -2372,7 +2380,7 @@ smob_status smob_step_euler(smob_ctx* c, const double* vel6n, double dt) {
             for (int k = 0; k < 3; ++k) ce[3 * i + k] += vel6n[6 * i + k] * dt;
             quat_step(&c->quats[4 * i], vel6n + 6 * i + 3, dt, &q[4 * i]);
         }
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         update_geometry(c, ce, q);
         return SMOB_OK;
@@ -2391,7 +2399,7 @@ smob_status smob_get_geometry(const smob_ctx* c, double* centers, double* quats)
 smob_status smob_step_euler_device(smob_ctx* c, const double* d_vel6n, double dt) {
     return guarded([&]() -> smob_status {
         need(c && d_vel6n, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         std::vector<double> v(6 * (size_t)c->N);
         CUDA_OK(cudaMemcpyAsync(v.data(), d_vel6n, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, c->st));
         CUDA_OK(cudaStreamSynchronize(c->st));
@@ -2425,7 +2433,7 @@ smob_status smob_apply_p2p(smob_ctx* c, const double* in, double* out, double c_
                            int precision) {
     return guarded([&]() -> smob_status {
         need(c && in && out, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         ensure_tuned(c);
         host_io(c, in, out, true, [&](const double* din, double* dout) {
@@ -2439,7 +2447,7 @@ smob_status smob_apply_p2p(smob_ctx* c, const double* in, double* out, double c_
 smob_status smob_apply_lop(smob_ctx* c, const double* in, double* out, double c_lop) {
     return guarded([&]() -> smob_status {
         need(c && in && out, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         host_io(c, in, out, true, [&](const double* din, double* dout) {
             check_launch(c, launch_sphere_op(c->g, din, dout, 0.0, 0.0, -1, c_lop, nullptr, false, c->st));
@@ -2451,7 +2459,7 @@ smob_status smob_apply_lop(smob_ctx* c, const double* in, double* out, double c_
 smob_status smob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, double alpha, double beta, int precision) {
     return guarded([&]() -> smob_status {
         need(c && X && Y && n_cols >= 1, "invalid argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         ensure_tuned(c);
         const size_t n = 3 * (size_t)c->M;
@@ -2471,7 +2479,7 @@ smob_status smob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, doub
 smob_status smob_project_null_space(smob_ctx* c, double* inout) {
     return guarded([&]() -> smob_status {
         need(c && inout, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
         CUDA_OK(cudaMemcpyAsync(c->d_in.p, inout, bytes, cudaMemcpyHostToDevice, c->st));
@@ -2486,7 +2494,7 @@ smob_status smob_project_null_space(smob_ctx* c, double* inout) {
 smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_sl, double c_trac, int precision) {
     return guarded([&]() -> smob_status {
         need(c && in && out, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);  // the fused float-float path allocates its second partial buffer
         all_active(c);
         ensure_tuned(c);
@@ -2554,7 +2562,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
 smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c_sl, double c_trac, int precision) {
     return guarded([&]() -> smob_status {
         need(c && in && out, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         const bool fp32 = precision == SMOB_PREC_MIXED;
         const bool df = precision == SMOB_PREC_FLOAT_FLOAT;  // float-float evaluation of the FP64 sets
@@ -2591,7 +2599,7 @@ smob_status smob_near_field(smob_ctx* c, const double* in, double* out, double c
 smob_status smob_sh_g2s(smob_ctx* c, const double* grid, double* coeff) {
     return guarded([&]() -> smob_status {
         need(c && grid && coeff, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
         CUDA_OK(cudaMemcpyAsync(c->d_in.p, grid, bytes, cudaMemcpyHostToDevice, c->st));
@@ -2605,7 +2613,7 @@ smob_status smob_sh_g2s(smob_ctx* c, const double* grid, double* coeff) {
 smob_status smob_sh_s2g(smob_ctx* c, const double* coeff, double* grid) {
     return guarded([&]() -> smob_status {
         need(c && grid && coeff, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         all_active(c);
         CUDA_OK(cudaMemcpyAsync(c->d_coef64.p, coeff, sizeof(double) * 2 * c->ncoef_total, cudaMemcpyHostToDevice, c->st));
         check_launch(c, launch_sh_s2g(c->g, c->d_coef64.as<double>(), c->d_out.as<double>(), c->st));
@@ -2648,7 +2656,7 @@ smob_status smob_solve_mob_device(smob_ctx* c, const double* d_force, double* d_
     return guarded([&]() -> smob_status {
         need(c && d_force && d_vel, "null argument");
         check_opts(o);
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         smob_status s = solve_device(c, d_force, d_vel, d_density, o, stats);
         prof_flush(c);
@@ -2661,7 +2669,7 @@ smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double
     return guarded([&]() -> smob_status {
         need(c && force && vel, "null argument");
         check_opts(o);
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         for (int i = 0; i < 6 * c->N; ++i)
             if (!std::isfinite(force[i])) throw SmobError(SMOB_ERR_NONFINITE, "force/torque input is not finite");
@@ -2736,7 +2744,7 @@ smob_status smob_solve_mob_multi(smob_ctx* c, int n_rhs, const double* force, do
         need(c->P == 1 && c->nrep == 1, "several right-hand sides need a context with one problem");
         check_opts(o);
         if (n_rhs == 1) return smob_solve_mob(c, force, vel, density, o, stats);
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         smob_ctx* r = replicated(c, n_rhs);
         return smob_solve_mob(r, force, vel, density, o, stats);
@@ -2773,7 +2781,7 @@ smob_status smob_mob_apply(smob_ctx* c, const double* X, double* Y, int n_cols, 
 smob_status smob_device_alloc(smob_ctx* c, size_t bytes, void** ptr) {
     return guarded([&]() -> smob_status {
         need(c && ptr, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         CUDA_OK(cudaMalloc(ptr, bytes ? bytes : 16));
         return SMOB_OK;
     });
@@ -2782,7 +2790,7 @@ smob_status smob_device_alloc(smob_ctx* c, size_t bytes, void** ptr) {
 smob_status smob_device_free(smob_ctx* c, void* ptr) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         if (ptr) CUDA_OK(cudaFree(ptr));
         return SMOB_OK;
     });
@@ -2791,7 +2799,7 @@ smob_status smob_device_free(smob_ctx* c, void* ptr) {
 smob_status smob_memcpy_h2d(smob_ctx* c, void* dst, const void* src, size_t bytes) {
     return guarded([&]() -> smob_status {
         need(c && dst && src, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         CUDA_OK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st));
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
@@ -2801,7 +2809,7 @@ smob_status smob_memcpy_h2d(smob_ctx* c, void* dst, const void* src, size_t byte
 smob_status smob_memcpy_d2h(smob_ctx* c, void* dst, const void* src, size_t bytes) {
     return guarded([&]() -> smob_status {
         need(c && dst && src, "null argument");
-        set_device(c);
+        CtxScope ctx_scope(c);
         CUDA_OK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st));
         CUDA_OK(cudaStreamSynchronize(c->st));
         return SMOB_OK;
@@ -2869,7 +2877,7 @@ smob_status smob_launch_count(const smob_ctx* c, long long* launches) {
 smob_status smob_set_graphs(smob_ctx* c, int on) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         c->use_graphs = on != 0;
         if (!c->use_graphs) c->drop_graphs();
@@ -2893,7 +2901,7 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
         need(c != nullptr, "null context");
         need(std::isfinite(eps) && eps < 1e-3, "far-field tolerance must be below 1e-3 (<= 0: off)");
         need(std::isfinite(eps_hp) && eps_hp < 1e-9, "float-float far-field tolerance must be below 1e-9 (<= 0: off)");
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old coarse tables
         for (auto& kv : c->multi) smob_destroy(kv.second);  // several-RHS copies follow the new tolerance
@@ -2912,7 +2920,7 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
 smob_status smob_set_far_coarse_targets(smob_ctx* c, int on) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old coarse tables
         for (auto& kv : c->multi) smob_destroy(kv.second);
@@ -3056,7 +3064,7 @@ smob_status smob_tc_info(const smob_ctx* c, int* near_tc, int* sphere_tc) {
 smob_status smob_set_sphere_tc(smob_ctx* c, int on) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         c->drop_graphs();  // captured blocks hold the other kernels
         for (auto& kv : c->multi) smob_set_sphere_tc(kv.second, on);
         c->sph_tc = on != 0;
@@ -3068,7 +3076,7 @@ smob_status smob_set_sphere_tc(smob_ctx* c, int on) {
 smob_status smob_set_near_tc(smob_ctx* c, int on) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         c->drop_graphs();  // captured blocks hold the other kernel
         for (auto& kv : c->multi) smob_set_near_tc(kv.second, on);
         c->near_tc = on != 0;
@@ -3085,7 +3093,7 @@ smob_status smob_set_far_tile(smob_ctx* c, int targets_per_thread) {
         need(c != nullptr, "null context");
         const int k = targets_per_thread == 1 ? 0 : (targets_per_thread == 2 ? 1 : (targets_per_thread == 4 ? 2 : -1));
         need(k >= 0, "targets_per_thread must be 1, 2 or 4");
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope as(c->st);
         c->drop_graphs();  // captured blocks hold the old item list and kernel variant
         c->tpt = targets_per_thread;
@@ -3100,7 +3108,7 @@ smob_status smob_set_far_tile(smob_ctx* c, int targets_per_thread) {
 smob_status smob_timer_mark(smob_ctx* c) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         if (!c->ev_a) {
             CUDA_OK(cudaEventCreate(&c->ev_a));
             CUDA_OK(cudaEventCreate(&c->ev_b));
@@ -3126,7 +3134,7 @@ smob_status smob_timer_elapsed(smob_ctx* c, double* ms) {
 smob_status smob_flush_l2(smob_ctx* c, size_t bytes) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
-        set_device(c);
+        CtxScope ctx_scope(c);
         AllocStreamScope scope(c->st);
         c->d_flush.alloc(bytes);
         CUDA_OK(cudaMemsetAsync(c->d_flush.p, int(c->flush_val++ & 0xff), bytes, c->st));

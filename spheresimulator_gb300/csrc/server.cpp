@@ -231,12 +231,18 @@ smob_status smob_server_create(smob_server** out, const smob_server_opts* o) {
     }
     // Freed device memory stays in the device's stream-ordered pool instead of going back to the driver
     // at every synchronisation: requests allocate and free gigabytes while others run, and returning and
-    // re-mapping that memory each time would stall the other requests' streams
+    // re-mapping that memory each time would stall the other requests' streams.
+    // The pool may not hand a block freed on one request's stream to another request's allocation by
+    // making the second stream wait for the first (the pool's "internal dependencies"): a small request
+    // would then wait for whatever a big request had queued before its free, seconds of kernels.
+    // Blocks whose free has completed on the device are still reused across streams.
     if (cudaSetDevice(o->device) == cudaSuccess) {
         cudaMemPool_t pool = nullptr;
         if (cudaDeviceGetDefaultMemPool(&pool, o->device) == cudaSuccess) {
             unsigned long long keep = ~0ULL;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            int no = 0;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
         }
     }
     cudaGetLastError();
@@ -301,6 +307,7 @@ static void fill_info(const Request* r, smob_request_info* info) {
     info->t_admit = r->t_admit;
     info->t_done = r->t_done;
     info->t_ctx = r->t_ctx;
+    info->route = r->route;
     info->bytes = double(r->bytes);
     info->stats = r->stats;
 }
