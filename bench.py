@@ -597,12 +597,14 @@ def run_serving(args, world, rank, local, dist):
                                      "ctx_ms": round(1e3 * (x["t_ctx"] - x["t_admit"]), 2),
                                      "solve_ms": round(1e3 * (x["t_done"] - x["t_ctx"]), 2),
                                      "iterations": x["stats"]["iterations"], "route": x["route"]}) + "\n")
-    # the same stream without the SM partition (stream priorities only), for comparison
-    nopart = None
-    if args.compare_partition and args.small_sms > 0:
-        lat0, span0, _, ok0, _ = serve(stream, PREC_MIXED, args.slots, 0)
-        nopart = {"solves_per_s": round(len(stream) / span0, 4), "p50_ms": round(1e3 * float(np.percentile(lat0, 50)), 2),
-                  "p99_ms": round(1e3 * float(np.percentile(lat0, 99)), 2), "by_size": buckets(lat0), "all_ok": ok0}
+    # the same stream with the other SM arrangement (a green-context partition, or none), for comparison
+    other = None
+    if args.compare_partition > 0:
+        alt_sms = 0 if args.small_sms > 0 else args.compare_partition
+        lat0, span0, st0, ok0, _ = serve(stream, PREC_MIXED, args.slots, alt_sms)
+        other = {"small_sms": st0["partition_sms"][0], "big_sms": st0["partition_sms"][1],
+                 "solves_per_s": round(len(stream) / span0, 4), "p50_ms": round(1e3 * float(np.percentile(lat0, 50)), 2),
+                 "p99_ms": round(1e3 * float(np.percentile(lat0, 99)), 2), "by_size": buckets(lat0), "all_ok": ok0}
     # the small requests (n <= 64) solved one at a time on an idle server: their solo latency
     small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= 64][:8]
     solo = None
@@ -642,10 +644,11 @@ def run_serving(args, world, rank, local, dist):
                        "p99": round(1e3 * float(np.percentile(lat, 99)), 2)},
         "latency_by_size": buckets(lat),
         "small_requests_solo": solo,
-        "without_sm_partition": nopart,
         "sm_partition": {"small_sms": st["partition_sms"][0], "big_sms": st["partition_sms"][1],
-                         "note": "green contexts: requests with < 1e9 far-field pairs run on the small partition "
-                                 "while a big request runs (on the whole device otherwise); big requests on the rest"},
+                         "note": "0/0: no partition, stream priorities by size only; otherwise green contexts: "
+                                 "requests with < 1e9 far-field pairs run on the small partition while a big "
+                                 "request runs (on the whole device otherwise), big requests on the rest"},
+        "other_sm_arrangement": other,
         "queue_wait_ms_p50": round(1e3 * float(np.percentile([x["t_admit"] - x["t_submit"] for x in infos], 50)), 2),
         "all_converged": ok, "span_s": round(total, 3),
         "requests": {"spheres_min": int(min(sizes)), "spheres_max": int(max(sizes)), "spheres_median": float(np.median(sizes))},
@@ -919,12 +922,14 @@ def main():
     ap.add_argument("--nmax", type=int, default=2048, help="cfg5: largest sphere count of a request")
     ap.add_argument("--slots", type=int, default=8, help="cfg5: requests on the GPU at once")
     ap.add_argument("--hbm-budget", type=float, default=0.0, help="cfg5: admission budget in bytes (0: 64 GB)")
-    ap.add_argument("--small-sms", type=int, default=16,
-                    help="cfg5: SMs reserved (green context) for small requests while big ones run (0: none)")
+    ap.add_argument("--small-sms", type=int, default=0,
+                    help="cfg5: SMs reserved (green context) for small requests while big ones run (0: none, "
+                         "stream priorities by size only)")
     ap.add_argument("--serve-log", default="",
                     help="cfg5: write one JSON line per request (size, queue and run times) to this file")
-    ap.add_argument("--compare-partition", action="store_true",
-                    help="cfg5: also serve the stream without the SM partition")
+    ap.add_argument("--compare-partition", type=int, default=0, metavar="SMS",
+                    help="cfg5: also serve the stream with this many SMs reserved for small requests (without a "
+                         "partition when --small-sms is set)")
     ap.add_argument("--fp64-subset", type=int, default=0,
                     help="cfg5: also serve the requests with at most this many spheres in mixed and plain FP64")
     ap.add_argument("--multi", type=int, default=0,

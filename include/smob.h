@@ -342,9 +342,19 @@ smob_status smob_profile_get(const smob_ctx* ctx, int i, char* name, int name_le
 smob_status smob_profile_reset(smob_ctx* ctx);
 /* total kernel launches issued by the library on this context since creation */
 smob_status smob_launch_count(const smob_ctx* ctx, long long* launches);
-/* CUDA graphs for the Arnoldi steps of the solves (default on): blocks of steps are captured once per
- * context and replayed; the host checks the per-problem stop flags between blocks */
+/* CUDA graphs for the solves (default on). With the loop graph on (the default) a solve's whole
+ * restart-cycle loop is one graph launch whose decisions run on the device: per-problem stop tests,
+ * the Arnoldi steps (a switch over the step index inside a while node), the residual choice and the
+ * next cycle (conditional graph nodes set by single-CTA decision kernels). With the loop graph off,
+ * or where conditional nodes are unavailable, the host drives the cycles and replays captured blocks
+ * of four steps, checking the per-problem stop flags between blocks. Results are the same bits. */
 smob_status smob_set_graphs(smob_ctx* ctx, int on);
+smob_status smob_set_loop_graph(smob_ctx* ctx, int on);
+/* on: the loop graph is selected; available: building one has not failed on this context */
+smob_status smob_loop_graph_info(const smob_ctx* ctx, int* on, int* available);
+/* kernels run on this context since creation (graph nodes included) and launches issued from the host
+ * (kernels launched outside graphs plus graph launches) */
+smob_status smob_launch_stats(const smob_ctx* ctx, long long* kernels, long long* host_calls);
 /* far-field tile shape chosen by the autotuner at smob_create: FP32 targets per thread (1, 2 or 4),
  * the measured milliseconds of the three variants (0 when the choice came from the process cache) */
 smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* variant_ms, int* from_cache);

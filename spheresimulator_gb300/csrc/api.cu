@@ -103,6 +103,54 @@ struct StreamHolder {
     }
 };
 
+// Pinned host staging for every copy between the host and a context's stream. A device-to-host copy
+// into pageable memory blocks its thread until the stream reaches the copy, and the driver stages
+// pageable copies through buffers the whole process shares: while one server request waits there
+// for seconds of its own queued kernels, the other requests' pageable copies (a few bytes of solver
+// state per Krylov block) wait with it. Pinned copies are plain stream-ordered DMA.
+// Blocks come from a process-wide free list (portable, so any context, green ones included, may use
+// them) and go back to it when the context is destroyed: freeing pinned memory can synchronize the
+// device, which a server with requests in flight must not do.
+std::mutex g_pin_mu;
+std::multimap<size_t, void*> g_pin_free;
+
+void* pin_acquire(size_t bytes, size_t* cap) {
+    size_t want = 64 << 10;
+    while (want < bytes) want <<= 1;
+    {
+        std::lock_guard<std::mutex> lk(g_pin_mu);
+        auto it = g_pin_free.lower_bound(want);
+        if (it != g_pin_free.end()) {
+            void* p = it->second;
+            *cap = it->first;
+            g_pin_free.erase(it);
+            return p;
+        }
+    }
+    void* p = nullptr;
+    CUDA_OK(cudaHostAlloc(&p, want, cudaHostAllocPortable));
+    *cap = want;
+    return p;
+}
+
+void pin_release(void* p, size_t cap) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    g_pin_free.emplace(cap, p);
+}
+
+// A context's staging block, handed out by bumping an offset; the offset goes back to 0 only after
+// the context's stream was synchronized, so a host-to-device copy's source stays untouched until the
+// copy ran without the host waiting for it.
+struct HostStage {
+    char* p = nullptr;
+    size_t cap = 0, used = 0;
+    HostStage() = default;
+    HostStage(const HostStage&) = delete;
+    HostStage& operator=(const HostStage&) = delete;
+    ~HostStage() { pin_release(p, cap); }
+};
+
 constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host check of the stop flags
 // FP32 far field from coarse equivalent sources: per-pair tolerance (relative to the source sphere's
@@ -143,6 +191,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 struct smob_ctx {
     StreamHolder sh;   // first member: destroyed last, after all buffers were freed on it
     StreamHolder sh2;  // side stream of the operator passes (far field beside sphere/near kernels)
+    HostStage stage;   // pinned staging of the copies on st (smob_destroy synchronizes st first)
     int device = 0;
     cudaStream_t st = nullptr, st2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -237,12 +286,17 @@ struct smob_ctx {
     DBuf d_ru, d_rcoef, d_rscale;
     int rk = 0, rprec = -1;
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
+    // graph-driven restart loop: per-problem state, scalars and body counters, residual masks, the
+    // Arnoldi step counter and per-step run counts
+    DBuf d_track, d_sparams, d_updmask, d_hpmask, d_jdev, d_runs_j;
     DBuf d_red_count;     // per (problem, vector) counters of the fused dot reductions
     int red_cstride = 0;  // counters per problem
     bool have_xlast = false;
 
     DevGeom g{};
-    long long launches = 0;
+    long long launches = 0;    // kernels run (graph nodes included)
+    long long host_calls = 0;  // launches issued from the host: kernels outside graphs and graph launches
+    bool capturing = false;    // a stream capture of the context's work is open
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     DBuf d_flush;
     unsigned flush_val = 1;
@@ -253,9 +307,22 @@ struct smob_ctx {
     };
     bool use_graphs = true;
     std::map<long long, Graph> graphs;
+    // the whole restart-cycle loop as one graph with device-side decisions (solve_device), per
+    // (precisions, preconditioner, restart, iteration limit); kernels per body for the launch count
+    struct LoopGraph {
+        cudaGraphExec_t exec = nullptr;
+        long long k_top = 0, k_cycle = 0, k_upd = 0, k_hp = 0;
+        std::vector<long long> k_step;  // per step index j: step(j) and the step-control kernel
+    };
+    std::map<std::vector<int>, LoopGraph> loop_graphs;
+    bool loop_graph_ok = true;  // false once building one failed (the host-driven loop runs instead)
+    bool loop_graph_on = false;  // smob_set_loop_graph
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
+        for (auto& kv : loop_graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        loop_graphs.clear();
     }
 
     // profiling
@@ -360,8 +427,55 @@ void prof_flush(smob_ctx* c) {
 void check_launch(smob_ctx* c, int n) {
     if (n < 0) throw SmobError(SMOB_ERR_STATE, "kernel launch refused: more vectors than the work buffers hold");
     c->launches += n;
+    if (!c->capturing) c->host_calls += n;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw SmobError(SMOB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+}
+
+// staging space of `bytes` in the context's pinned block, valid until the next stage_sync
+void* stage_alloc(smob_ctx* c, size_t bytes) {
+    bytes = (bytes + 15) & ~size_t(15);
+    HostStage& h = c->stage;
+    if (h.used + bytes > h.cap) {
+        if (h.used > 0) {  // copies issued since the last synchronization may still use the block
+            CUDA_OK(cudaStreamSynchronize(c->st));
+            h.used = 0;
+        }
+        if (bytes > h.cap) {
+            pin_release(h.p, h.cap);
+            h.p = nullptr;
+            h.cap = 0;
+            size_t cap = 0;
+            h.p = static_cast<char*>(pin_acquire(bytes, &cap));
+            h.cap = cap;
+        }
+    }
+    void* r = h.p + h.used;
+    h.used += bytes;
+    return r;
+}
+
+// the copies issued through the stage have run (their host destinations may be read)
+void stage_sync(smob_ctx* c) {
+    CUDA_OK(cudaStreamSynchronize(c->st));
+    c->stage.used = 0;
+}
+
+// host to device on the context's stream without waiting: the source is copied into the stage first
+void h2d(smob_ctx* c, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return;
+    void* s = stage_alloc(c, bytes);
+    std::memcpy(s, src, bytes);
+    CUDA_OK(cudaMemcpyAsync(dst, s, bytes, cudaMemcpyHostToDevice, c->st));
+}
+
+// device to host on the context's stream; returns when the data is in dst
+void d2h(smob_ctx* c, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return;
+    void* s = stage_alloc(c, bytes);
+    CUDA_OK(cudaMemcpyAsync(s, src, bytes, cudaMemcpyDeviceToHost, c->st));
+    stage_sync(c);
+    std::memcpy(dst, s, bytes);
 }
 
 // counters of the fused dot reductions: nvec per problem, zeroed (the kernels leave them zero)
@@ -392,8 +506,7 @@ void check_overlap(smob_ctx* c, const double* d_centers) {
     check_launch(c, launch_overlap_check(d_centers, c->d_radius.as<double>(), c->d_prob.as<int>(),
                                          c->d_problems.as<Problem>(), c->N, first.as<unsigned long long>(), c->st));
     unsigned long long h = 0;
-    CUDA_OK(cudaMemcpyAsync(&h, first.p, sizeof(h), cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    d2h(c, &h, first.p, sizeof(h));
     if (h != ~0ULL) {
         const long long t = (long long)(h / (unsigned long long)c->N), sp = (long long)(h % (unsigned long long)c->N);
         throw SmobError(SMOB_ERR_ARG, "spheres " + std::to_string(t) + " and " + std::to_string(sp) +
@@ -419,8 +532,7 @@ void build_near(smob_ctx* c) {
     check_launch(c, launch_nbr_scan(count.as<int>(), N, c->d_nbr_start.as<int>(), c->d_near_slot.as<int>(),
                                     totals.as<int>(), c->st));
     int tot[2] = {0, 0};
-    CUDA_OK(cudaMemcpyAsync(tot, totals.p, sizeof(tot), cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    d2h(c, tot, totals.p, sizeof(tot));
     c->d_nbr_src.alloc(sizeof(int) * std::max(tot[0], 1));
     c->d_nbr_precise.alloc(std::max(tot[0], 1));
     c->d_slot_sphere.alloc(sizeof(int) * std::max(tot[1], 1));
@@ -432,19 +544,29 @@ void build_near(smob_ctx* c) {
     c->nbr_precise.resize(tot[0]);
     c->near_src_slot.resize(N);
     c->slot_sphere.resize(tot[1]);
-    CUDA_OK(cudaMemcpyAsync(c->nbr_start.data(), c->d_nbr_start.p, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost,
-                            c->st));
-    if (tot[0] > 0) {
-        CUDA_OK(cudaMemcpyAsync(c->nbr_src.data(), c->d_nbr_src.p, sizeof(int) * tot[0], cudaMemcpyDeviceToHost, c->st));
-        CUDA_OK(cudaMemcpyAsync(c->nbr_precise.data(), c->d_nbr_precise.p, tot[0], cudaMemcpyDeviceToHost, c->st));
+    // the lists in one staged batch: the copies, one synchronization, then the host mirrors
+    struct Part {
+        void* dst;
+        const void* src;
+        size_t bytes;
+        void* staged;
+    } parts[] = {{c->nbr_start.data(), c->d_nbr_start.p, sizeof(int) * (N + 1), nullptr},
+                 {c->nbr_src.data(), c->d_nbr_src.p, sizeof(int) * tot[0], nullptr},
+                 {c->nbr_precise.data(), c->d_nbr_precise.p, size_t(tot[0]), nullptr},
+                 {c->near_src_slot.data(), c->d_near_slot.p, sizeof(int) * N, nullptr},
+                 {c->slot_sphere.data(), c->d_slot_sphere.p, sizeof(int) * tot[1], nullptr}};
+    size_t all = 0;
+    for (const Part& q : parts) all += (q.bytes + 15) & ~size_t(15);
+    stage_alloc(c, all);  // room for the whole batch (synchronizes or grows the block first if needed)
+    c->stage.used -= all;
+    for (Part& q : parts) {
+        if (q.bytes == 0) continue;
+        q.staged = stage_alloc(c, q.bytes);
+        CUDA_OK(cudaMemcpyAsync(q.staged, q.src, q.bytes, cudaMemcpyDeviceToHost, c->st));
     }
-    if (N > 0)
-        CUDA_OK(cudaMemcpyAsync(c->near_src_slot.data(), c->d_near_slot.p, sizeof(int) * N, cudaMemcpyDeviceToHost,
-                                c->st));
-    if (tot[1] > 0)
-        CUDA_OK(cudaMemcpyAsync(c->slot_sphere.data(), c->d_slot_sphere.p, sizeof(int) * tot[1],
-                                cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    stage_sync(c);
+    for (const Part& q : parts)
+        if (q.bytes) std::memcpy(q.dst, q.staged, q.bytes);
 }
 
 void problem_origins(smob_ctx* c);
@@ -1348,11 +1470,7 @@ void autotune_far32(smob_ctx* c) {
     c->d_items32.upload(c->items32);
 }
 
-void set_active(smob_ctx* c, const std::vector<unsigned char>& act) {
-    CUDA_OK(cudaMemcpyAsync(c->d_active.p, act.data(), act.size(), cudaMemcpyHostToDevice, c->st));
-    // the host vector must stay valid until the copy ran: make it synchronous with the stream
-    CUDA_OK(cudaStreamSynchronize(c->st));
-}
+void set_active(smob_ctx* c, const std::vector<unsigned char>& act) { h2d(c, c->d_active.p, act.data(), act.size()); }
 
 // ---------------------------------------------------------------- the operator
 // operator precisions: every kernel in FP64; every kernel in FP32; or FP64 sphere and near
@@ -1565,6 +1683,12 @@ void ensure_solver(smob_ctx* c, int m) {
     c->d_hn.alloc(sizeof(double) * c->P);
     c->d_beta.alloc(sizeof(double) * c->P);
     c->d_incycle.alloc(c->P);
+    c->d_track.alloc(sizeof(SolveTrack) * c->P);
+    c->d_sparams.alloc(sizeof(SolveParams));
+    c->d_updmask.alloc(c->P);
+    c->d_hpmask.alloc(c->P);
+    c->d_jdev.alloc(sizeof(int));
+    c->d_runs_j.alloc(sizeof(int) * std::max(m, c->restart_cap));
     if (!c->d_xlast.p) {
         c->d_xlast.alloc(sizeof(double) * n);
         CUDA_OK(cudaMemsetAsync(c->d_xlast.p, 0, sizeof(double) * n, c->st));
@@ -1575,8 +1699,7 @@ std::vector<double> seg_norms(smob_ctx* c, const double* v, const unsigned char*
     KrylovLaunch L = c->kl();
     check_launch(c, launch_dots(L, v, 0, 1, v, active, c->d_norm.as<double>(), 1, 0, false, true, c->st));
     std::vector<double> h(c->P);
-    CUDA_OK(cudaMemcpyAsync(h.data(), c->d_norm.p, sizeof(double) * c->P, cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    d2h(c, h.data(), c->d_norm.p, sizeof(double) * c->P);
     return h;
 }
 
@@ -1617,7 +1740,7 @@ std::vector<double> recycle_guess(smob_ctx* c, const std::vector<double>& f, dou
     for (int p = 0; p < P; ++p)
         if (fn2[p] > 0) est[p] = std::sqrt(res2[p] / fn2[p]);
     KrylovLaunch L = c->kl();
-    CUDA_OK(cudaMemcpyAsync(c->d_rcoef.p, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, c->st));
+    h2d(c, c->d_rcoef.p, h.data(), sizeof(double) * h.size());
     for (int k = 0; k < nparts; ++k) {
         if (!parts[k]) continue;
         CUDA_OK(cudaMemsetAsync(parts[k], 0, sizeof(double) * n, c->st));
@@ -1675,8 +1798,8 @@ void recycle_add(smob_ctx* c, const std::vector<double>& f, const double* const*
     // device: part_k = (v_k - U_k coef) / nu with the same coefficients
     KrylovLaunch L = c->kl();
     const unsigned char* act = c->d_active.as<unsigned char>();
-    CUDA_OK(cudaMemcpyAsync(c->d_rcoef.p, coef.data(), sizeof(double) * coef.size(), cudaMemcpyHostToDevice, st));
-    CUDA_OK(cudaMemcpyAsync(c->d_rscale.p, sc.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
+    h2d(c, c->d_rcoef.p, coef.data(), sizeof(double) * coef.size());
+    h2d(c, c->d_rscale.p, sc.data(), sizeof(double) * P);
     set_active(c, keep);
     for (int m = 0; m < kRecycleParts; ++m) {
         double* base = c->d_ru.as<double>() + n * m;
@@ -1689,8 +1812,235 @@ void recycle_add(smob_ctx* c, const std::vector<double>& f, const double* const*
                                           kRecycleMax, -1.0, act, u, st));
         check_launch(c, launch_scale(L, u, c->d_rscale.as<double>(), 1, false, act, u, st));
     }
-    CUDA_OK(cudaStreamSynchronize(st));  // coef and sc must outlive their copies
     if (std::any_of(sc.begin(), sc.end(), [](double v) { return v != 0.0; })) c->rk++;
+}
+
+// ---------------------------------------------------------------- graph-driven restart loop
+// The restart-cycle loop of solve_device as one CUDA graph whose control flow runs on the device:
+//
+//   decide                                     per problem: stop, or join the next cycle
+//   while (a problem is in the cycle) {        conditional WHILE node
+//     V_0 = r / beta, cycle init, step j = 0
+//     while (a problem is active) {            conditional WHILE node
+//       switch (j) { step(0) | ... | step(m-1) }   conditional SWITCH node: the Arnoldi step j
+//       step control: j += 1, continue while a problem is active and j < m
+//     }
+//     x += V y; residual decision per problem
+//     if (a problem takes the FP32 update) { r -= A32 dx }          conditional IF node
+//     if (a problem takes the high-precision residual) { r = ... }  conditional IF node
+//     beta = |r|; decide
+//   }
+//
+// One graph launch per solve replaces the host loop's per-block synchronizations, per-cycle state
+// round trips and the hundreds of launches of a solve. Every decision kernel applies the host loop's
+// rules to the same values (krylov.cu), the bodies are the host loop's own launch sequences captured
+// once per step index, and skipped bodies are exactly the steps the host loop does not launch or that
+// launch kernels that return at once (every problem inactive), so both loops give the same bits.
+struct LoopArgs {
+    int m, maxit;
+    bool mixed;
+    int hp, cyc_prec;
+    bool pc;
+    double tol, inner_tol;
+};
+
+// captures the work f() issues on c->st (and on streams that join it) into graph g after the nodes
+// deps; returns the nodes the capture ended on
+template <typename F>
+std::vector<cudaGraphNode_t> capture_into(smob_ctx* c, cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, F&& f) {
+    CUDA_OK(cudaStreamBeginCaptureToGraph(c->st, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                          cudaStreamCaptureModeThreadLocal));
+    std::vector<cudaGraphNode_t> tail;
+    struct Capturing {
+        smob_ctx* c;
+        explicit Capturing(smob_ctx* x) : c(x) { c->capturing = true; }
+        ~Capturing() { c->capturing = false; }
+    } capturing(c);
+    try {
+        f();
+        cudaStreamCaptureStatus status;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        CUDA_OK(cudaStreamGetCaptureInfo(c->st, &status, nullptr, nullptr, &d, nullptr, &nd));
+        tail.assign(d, d + nd);
+    } catch (...) {
+        cudaGraph_t out = nullptr;
+        cudaStreamEndCapture(c->st, &out);
+        cudaGetLastError();
+        throw;
+    }
+    cudaGraph_t out = nullptr;
+    CUDA_OK(cudaStreamEndCapture(c->st, &out));
+    return tail;
+}
+
+// a conditional node (while / switch / if) after deps; its body graphs in bodies[0 .. size-1]
+cudaGraphNode_t add_conditional(cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle h,
+                                cudaGraphConditionalNodeType type, unsigned size, cudaGraph_t* bodies) {
+    cudaGraphNodeParams prm = {};
+    prm.type = cudaGraphNodeTypeConditional;
+    prm.conditional.handle = h;
+    prm.conditional.type = type;
+    prm.conditional.size = size;
+    cudaGraphNode_t node = nullptr;
+    CUDA_OK(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &prm));
+    for (unsigned i = 0; i < size; ++i) bodies[i] = prm.conditional.phGraph_out[i];
+    return node;
+}
+
+// Runs the restart loop as one graph launch (built on first use per LoopArgs shape). The per-problem
+// state goes in and comes back in one copy each way. Returns false, with nothing changed, when the
+// graph cannot be built (conditional nodes unavailable): the caller runs the host loop instead.
+template <class Step, class Upd, class HpOps, class ExplOps, class CycUpd>
+bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, HpOps& hp_residual_ops,
+                    ExplOps& explicit_residual_ops, CycUpd& cycle_update_ops, std::vector<char>& done,
+                    std::vector<char>& conv, std::vector<double>& beta, const std::vector<double>& bnorm,
+                    std::vector<char>& hp_now, std::vector<char>& hp_resid_done, std::vector<char>& x_moved,
+                    std::vector<int>& cycles, std::vector<int>& passes64, std::vector<int>& passes32x) {
+    const int P = c->P, m = a.m;
+    cudaStream_t st = c->st;
+    KrylovLaunch L = c->kl();
+    auto* track = c->d_track.as<SolveTrack>();
+    auto* sp = c->d_sparams.as<SolveParams>();
+    unsigned char* act = c->d_active.as<unsigned char>();
+    unsigned char* incyc = c->d_incycle.as<unsigned char>();
+    unsigned char* updm = c->d_updmask.as<unsigned char>();
+    unsigned char* hpm = c->d_hpmask.as<unsigned char>();
+    KrylovState* ks = c->d_ks.as<KrylovState>();
+    double* beta_d = c->d_beta.as<double>();
+    double* norm = c->d_norm.as<double>();
+    const double* r = c->d_r.as<double>();
+    double* V = c->d_V.as<double>();
+    int* jdev = c->d_jdev.as<int>();
+    int* runs_j = c->d_runs_j.as<int>();
+    const std::vector<int> key{a.mixed ? 1 : 0, a.hp, a.cyc_prec, a.pc ? 1 : 0, m, a.maxit};
+    auto it = c->loop_graphs.find(key);
+    if (it == c->loop_graphs.end()) {
+        smob_ctx::LoopGraph lg;
+        const long long before = c->launches;
+        auto count = [&](auto&& f) {
+            const long long k0 = c->launches;
+            f();
+            return c->launches - k0;
+        };
+        cudaGraph_t G = nullptr;
+        try {
+            CUDA_OK(cudaGraphCreate(&G, 0));
+            cudaGraphConditionalHandle hc, hi, hsel, hu, hh;
+            CUDA_OK(cudaGraphConditionalHandleCreate(&hc, G, 0, cudaGraphCondAssignDefault));
+            auto tail = capture_into(c, G, {}, [&] {
+                lg.k_top = count([&] {
+                    check_launch(c, launch_loop_decide(P, false, track, ks, sp, nullptr, incyc, act, beta_d, a.maxit,
+                                                       hc, st));
+                });
+            });
+            cudaGraph_t body = nullptr;
+            add_conditional(G, tail, hc, cudaGraphCondTypeWhile, 1, &body);
+            CUDA_OK(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
+            CUDA_OK(cudaGraphConditionalHandleCreate(&hu, body, 0, cudaGraphCondAssignDefault));
+            CUDA_OK(cudaGraphConditionalHandleCreate(&hh, body, 0, cudaGraphCondAssignDefault));
+            long long kc = 0;
+            tail = capture_into(c, body, {}, [&] {
+                kc += count([&] {
+                    check_launch(c, launch_scale(L, r, beta_d, 1, true, act, V, st));
+                    check_launch(c, launch_cycle_init(L, m, incyc, beta_d, ks, c->d_H.as<double>(),
+                                                      c->d_g.as<double>(), st));
+                    check_launch(c, launch_inner_begin(jdev, hi, st));
+                });
+            });
+            cudaGraph_t inner = nullptr;
+            cudaGraphNode_t inode = add_conditional(body, tail, hi, cudaGraphCondTypeWhile, 1, &inner);
+            CUDA_OK(cudaGraphConditionalHandleCreate(&hsel, inner, 0, cudaGraphCondAssignDefault));
+            std::vector<cudaGraph_t> steps(m, nullptr);
+            cudaGraphNode_t snode = add_conditional(inner, {}, hsel, cudaGraphCondTypeSwitch, m, steps.data());
+            lg.k_step.assign(m, 0);
+            for (int j = 0; j < m; ++j) capture_into(c, steps[j], {}, [&] { lg.k_step[j] = count([&] { step(j); }); });
+            long long knext = 0;
+            capture_into(c, inner, {snode}, [&] {
+                knext = count([&] { check_launch(c, launch_step_next(P, act, jdev, runs_j, m, hi, hsel, st)); });
+            });
+            for (long long& k : lg.k_step) k += knext;
+            const double* dx = nullptr;
+            tail = capture_into(c, body, {inode}, [&] {
+                kc += count([&] {
+                    dx = cycle_update_ops();
+                    check_launch(c, launch_resid_decide(P, track, sp, incyc, updm, hpm, hu, hh, st));
+                });
+            });
+            cudaGraph_t ub = nullptr, hb = nullptr;
+            cudaGraphNode_t unode = add_conditional(body, tail, hu, cudaGraphCondTypeIf, 1, &ub);
+            capture_into(c, ub, {}, [&] {
+                lg.k_upd = count([&] {
+                    CUDA_OK(cudaMemcpyAsync(act, updm, P, cudaMemcpyDeviceToDevice, st));
+                    upd_ops(dx);
+                    check_launch(c, launch_track_mark(P, track, updm, 0, st));
+                });
+            });
+            cudaGraphNode_t hnode = add_conditional(body, {unode}, hh, cudaGraphCondTypeIf, 1, &hb);
+            capture_into(c, hb, {}, [&] {
+                lg.k_hp = count([&] {
+                    CUDA_OK(cudaMemcpyAsync(act, hpm, P, cudaMemcpyDeviceToDevice, st));
+                    if (a.mixed) hp_residual_ops();
+                    else explicit_residual_ops();
+                    check_launch(c, launch_track_mark(P, track, hpm, 1, st));
+                });
+            });
+            capture_into(c, body, {hnode}, [&] {
+                kc += count([&] {
+                    CUDA_OK(cudaMemcpyAsync(act, incyc, P, cudaMemcpyDeviceToDevice, st));
+                    check_launch(c, launch_dots(L, r, 0, 1, r, act, norm, 1, 0, false, true, st));
+                    check_launch(c, launch_loop_decide(P, true, track, ks, sp, norm, incyc, act, beta_d, a.maxit, hc,
+                                                       st));
+                });
+            });
+            lg.k_cycle = kc;
+            CUDA_OK(cudaGraphInstantiate(&lg.exec, G, 0));
+            cudaGraphDestroy(G);
+            c->launches = before;
+        } catch (const SmobError&) {
+            if (G) cudaGraphDestroy(G);
+            cudaGetLastError();
+            c->launches = before;
+            c->loop_graph_ok = false;
+            return false;
+        }
+        it = c->loop_graphs.emplace(key, std::move(lg)).first;
+    }
+    const smob_ctx::LoopGraph& lg = it->second;
+    std::vector<SolveTrack> tr(P);
+    for (int p = 0; p < P; ++p)
+        tr[p] = SolveTrack{bnorm[p], beta[p], done[p], conv[p], hp_now[p], hp_resid_done[p], x_moved[p],
+                           cycles[p], passes64[p], passes32x[p]};
+    const SolveParams prm{a.tol, a.inner_tol, a.mixed ? 1 : 0, 0, 0, 0};
+    h2d(c, track, tr.data(), sizeof(SolveTrack) * P);
+    h2d(c, sp, &prm, sizeof(prm));
+    CUDA_OK(cudaMemsetAsync(runs_j, 0, sizeof(int) * m, st));
+    CUDA_OK(cudaGraphLaunch(lg.exec, st));
+    auto* tr_s = static_cast<SolveTrack*>(stage_alloc(c, sizeof(SolveTrack) * P));
+    auto* sp_s = static_cast<SolveParams*>(stage_alloc(c, sizeof(SolveParams)));
+    auto* rj_s = static_cast<int*>(stage_alloc(c, sizeof(int) * m));
+    CUDA_OK(cudaMemcpyAsync(tr_s, track, sizeof(SolveTrack) * P, cudaMemcpyDeviceToHost, st));
+    CUDA_OK(cudaMemcpyAsync(sp_s, sp, sizeof(SolveParams), cudaMemcpyDeviceToHost, st));
+    CUDA_OK(cudaMemcpyAsync(rj_s, runs_j, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
+    stage_sync(c);
+    for (int p = 0; p < P; ++p) {
+        const SolveTrack& t = tr_s[p];
+        beta[p] = t.beta;
+        done[p] = char(t.done);
+        conv[p] = char(t.conv);
+        hp_now[p] = char(t.hp_now);
+        hp_resid_done[p] = char(t.hp_done);
+        x_moved[p] = char(t.x_moved);
+        cycles[p] = t.cycles;
+        passes64[p] = t.passes64;
+        passes32x[p] = t.passes32x;
+    }
+    long long k = lg.k_top + (long long)sp_s->cycles_run * lg.k_cycle + (long long)sp_s->upd_run * lg.k_upd +
+                  (long long)sp_s->hp_run * lg.k_hp;
+    for (int j = 0; j < m; ++j) k += (long long)rj_s[j] * lg.k_step[j];
+    c->launches += k;
+    c->host_calls += 1;
+    return true;
 }
 
 // the mobility solve on device pointers (SphereSTKMobMat::solveMob, BIE/SphereSTKMobMat.cpp:146-286)
@@ -1740,7 +2090,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     set_active(c, all);
     std::vector<KrylovState> hks(P);
     for (auto& k : hks) k = KrylovState{0, 0, 0, 0, 0, 0, 0};
-    CUDA_OK(cudaMemcpyAsync(ks, hks.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
+    h2d(c, ks, hks.data(), sizeof(KrylovState) * P);
     std::vector<int> passes64(P, 0), cycles(P, 0), passes32x(P, 0);
     std::vector<char> hp_resid_done(P, 0);  // a high-precision residual after a cycle exists
     // MIXED: beta[p] is a high-precision residual norm (or one updated from it by a small FP32 step);
@@ -1758,8 +2108,8 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     }
     // MIXED: one fused high-precision pass on the problems in mask gives r = -(I/2 + K)(rho + x) - L x
     // and the single layer u_hp = S[rho + x] (the final velocity then needs only S32[x - x_hp])
-    auto hp_residual = [&](const std::vector<unsigned char>& mask) {
-        set_active(c, mask);
+    // the device work of hp_residual on the problems already marked active
+    auto hp_residual_ops = [&]() {
         CUDA_OK(cudaMemcpyAsync(dens, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, dens, st));
         CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
@@ -1769,6 +2119,10 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         check_launch(c, launch_axpby_seg(L, 1.0, u, 0.0, act, r, st));
         check_launch(c, launch_axpby_seg(L, 1.0, w, 0.0, act, uhp, st));
         check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, xhp, st));
+    };
+    auto hp_residual = [&](const std::vector<unsigned char>& mask) {
+        set_active(c, mask);
+        hp_residual_ops();
         for (int p = 0; p < P; ++p)
             if (mask[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
     };
@@ -1791,8 +2145,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     std::vector<double> hforce;
     if (recycle) {
         hforce.resize(6 * (size_t)c->N);
-        CUDA_OK(cudaMemcpyAsync(hforce.data(), d_force, sizeof(double) * hforce.size(), cudaMemcpyDeviceToHost, st));
-        CUDA_OK(cudaStreamSynchronize(st));
+        d2h(c, hforce.data(), d_force, sizeof(double) * hforce.size());
     }
     if (recycle && c->rk > 0) {
         // MIXED from MIXED columns: a force in the span (to far below the tolerance) takes the
@@ -1857,9 +2210,67 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     std::vector<KrylovState> kst(P);
     std::vector<unsigned char> hact(P);
     const long long hs = (long long)m * (m + 1);
-    while (true) {
-        CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
-        CUDA_OK(cudaStreamSynchronize(st));
+    // one Arnoldi step: w = A V_j (A = I/2 + K + L, SphereSTKMobMat.cpp:17), CGS2 into H[:, j],
+    // Givens update and the per-problem stop test on the device (problems that stop skip all
+    // later work through the active flags)
+    auto step = [&](int j) {
+        const double* Vj = V + n * j;
+        if (pc) {  // right preconditioning: w = A P V_j
+            apply_precond(Vj, pz);
+            Vj = pz;
+        }
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, cyc_prec);
+        double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
+        double* hscr = c->d_y.as<double>();
+        for (int pass = 0; pass < 2; ++pass) {
+            check_launch(c, launch_dots(L, V, (long long)n, j + 1, w, act, hscr, m, 0, false, false, st, Hcol, hs,
+                                        pass == 1));
+            check_launch(c, launch_update(L, V, (long long)n, j + 1, nullptr, hscr, m, -1.0, act, w, st));
+        }
+        check_launch(c, launch_dots(L, w, 0, 1, w, act, c->d_hn.as<double>(), 1, 0, false, true, st));
+        check_launch(c, launch_givens(L, j, m, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_cs.as<double>(),
+                                      c->d_sn.as<double>(), c->d_hn.as<double>(), act, maxit, st));
+        if (j + 1 < m) check_launch(c, launch_scale(L, w, c->d_hn.as<double>(), 1, true, act, V + n * (j + 1), st));
+    };
+    // residual of the FP32-update problems (MIXED): r -= A32 dx on the problems already marked active
+    auto upd_ops = [&](const double* dx) {
+        CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        op_apply(c, dx, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
+        check_launch(c, launch_axpby_seg(L, -1.0, u, 1.0, act, r, st));
+    };
+    // explicit residual r = b - A x in the solve's precision (FP64 / float-float solves)
+    auto explicit_residual_ops = [&]() {
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
+        check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+        check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+    };
+    // x += V y (P V y when preconditioned) for the problems of the cycle (after the Arnoldi steps);
+    // returns the correction dx
+    auto cycle_update_ops = [&]() -> const double* {
+        check_launch(c, launch_trisolve(L, m, incyc, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_y.as<double>(),
+                                        c->d_kc.as<int>(), st));
+        CUDA_OK(cudaMemcpyAsync(act, incyc, P, cudaMemcpyDeviceToDevice, st));
+        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+        check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, w, st));
+        double* dx = w;  // the correction of this cycle: V y, or P V y when preconditioned
+        if (pc) {
+            apply_precond(w, pz);
+            dx = pz;
+        }
+        check_launch(c, launch_axpby_seg(L, 1.0, dx, 1.0, act, x, st));
+        return dx;
+    };
+
+    const bool loop_graph = c->use_graphs && c->loop_graph_on && c->loop_graph_ok && !c->prof;
+    bool loop_done = false;
+    if (loop_graph) loop_done = run_loop_graph(c, LoopArgs{m, maxit, mixed, hp, cyc_prec, pc, tol, inner_tol}, step,
+                                               upd_ops, hp_residual_ops, explicit_residual_ops, cycle_update_ops, done,
+                                               conv, beta, bnorm, hp_now, hp_resid_done, x_moved, cycles, passes64,
+                                               passes32x);
+    while (!loop_done) {
+        d2h(c, kst.data(), ks, sizeof(KrylovState) * P);
         std::vector<unsigned char> cyc(P, 0);
         int ncyc = 0;
         for (int p = 0; p < P; ++p) {
@@ -1880,36 +2291,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             kst[p].cycle_fp32 = mixed ? 1 : 0;
         }
         if (ncyc == 0) break;
-        CUDA_OK(cudaMemcpyAsync(ks, kst.data(), sizeof(KrylovState) * P, cudaMemcpyHostToDevice, st));
-        CUDA_OK(cudaMemcpyAsync(incyc, cyc.data(), P, cudaMemcpyHostToDevice, st));
-        CUDA_OK(cudaMemcpyAsync(c->d_beta.p, beta.data(), sizeof(double) * P, cudaMemcpyHostToDevice, st));
+        h2d(c, ks, kst.data(), sizeof(KrylovState) * P);
+        h2d(c, incyc, cyc.data(), P);
+        h2d(c, c->d_beta.p, beta.data(), sizeof(double) * P);
         set_active(c, cyc);
         check_launch(c, launch_scale(L, r, c->d_beta.as<double>(), 1, true, act, V, st));
         check_launch(c, launch_cycle_init(L, m, incyc, c->d_beta.as<double>(), ks, c->d_H.as<double>(),
                                           c->d_g.as<double>(), st));
-        // one Arnoldi step: w = A V_j (A = I/2 + K + L, SphereSTKMobMat.cpp:17), CGS2 into H[:, j],
-        // Givens update and the per-problem stop test on the device (problems that stop skip all
-        // later work through the active flags)
-        auto step = [&](int j) {
-            const double* Vj = V + n * j;
-            if (pc) {  // right preconditioning: w = A P V_j
-                apply_precond(Vj, pz);
-                Vj = pz;
-            }
-            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-            op_apply(c, Vj, w, 0.5, 0.0, 1.0, 1.0, cyc_prec);
-            double* Hcol = c->d_H.as<double>() + (long long)j * (m + 1);
-            double* hscr = c->d_y.as<double>();
-            for (int pass = 0; pass < 2; ++pass) {
-                check_launch(c, launch_dots(L, V, (long long)n, j + 1, w, act, hscr, m, 0, false, false, st, Hcol, hs,
-                                            pass == 1));
-                check_launch(c, launch_update(L, V, (long long)n, j + 1, nullptr, hscr, m, -1.0, act, w, st));
-            }
-            check_launch(c, launch_dots(L, w, 0, 1, w, act, c->d_hn.as<double>(), 1, 0, false, true, st));
-            check_launch(c, launch_givens(L, j, m, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_cs.as<double>(),
-                                          c->d_sn.as<double>(), c->d_hn.as<double>(), act, maxit, st));
-            if (j + 1 < m) check_launch(c, launch_scale(L, w, c->d_hn.as<double>(), 1, true, act, V + n * (j + 1), st));
-        };
         // Steps run in blocks of kGraphBlock; with graphs on, each block is captured once per context
         // (per block start, cycle precision and restart length) and replayed, and the host looks at
         // the active flags only between blocks (steps after every problem stopped inside a block
@@ -1926,7 +2314,9 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
                     const long long before = c->launches;
                     cudaGraph_t gr;
                     CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                    c->capturing = true;
                     for (int j = j0; j < j0 + cnt; ++j) step(j);
+                    c->capturing = false;
                     CUDA_OK(cudaStreamEndCapture(st, &gr));
                     cudaGraphExec_t ex;
                     CUDA_OK(cudaGraphInstantiate(&ex, gr, 0));
@@ -1936,25 +2326,15 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
                 }
                 CUDA_OK(cudaGraphLaunch(it->second.exec, st));
                 c->launches += it->second.kernels;
+                c->host_calls += 1;
             } else {
                 for (int j = j0; j < j0 + cnt; ++j) step(j);
             }
-            CUDA_OK(cudaMemcpyAsync(hact.data(), act, P, cudaMemcpyDeviceToHost, st));
-            CUDA_OK(cudaStreamSynchronize(st));
+            d2h(c, hact.data(), act, P);
             if (std::none_of(hact.begin(), hact.end(), [](unsigned char a) { return a != 0; })) break;
         }
         // d = V y and x += d for the problems of this cycle
-        check_launch(c, launch_trisolve(L, m, incyc, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_y.as<double>(),
-                                        c->d_kc.as<int>(), st));
-        set_active(c, cyc);
-        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        check_launch(c, launch_update(L, V, (long long)n, m, c->d_kc.as<int>(), c->d_y.as<double>(), m, 1.0, act, w, st));
-        double* dx = w;  // the correction of this cycle: V y, or P V y when preconditioned
-        if (pc) {
-            apply_precond(w, pz);
-            dx = pz;
-        }
-        check_launch(c, launch_axpby_seg(L, 1.0, dx, 1.0, act, x, st));
+        const double* dx = cycle_update_ops();
         // Residual, decided per problem (so a problem takes the same steps alone or in any batch).
         // FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos' restart).
         // MIXED, once the previous high-precision residual is below 1e-4 |b|: r <- r - A32 d, whose
@@ -1970,9 +2350,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         }
         if (any_upd) {
             set_active(c, upd);
-            CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-            op_apply(c, dx, u, 0.5, 0.0, 1.0, 1.0, OP_FP32);
-            check_launch(c, launch_axpby_seg(L, -1.0, u, 1.0, act, r, st));
+            upd_ops(dx);
             for (int p = 0; p < P; ++p)
                 if (upd[p]) passes32x[p]++, x_moved[p] = 1;
         }
@@ -1980,10 +2358,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
             hp_residual(hpres);
         } else if (any_hp) {
             set_active(c, hpres);
-            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, hp);
-            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+            explicit_residual_ops();
             for (int p = 0; p < P; ++p)
                 if (hpres[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
         }
@@ -2039,10 +2414,13 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         recycle_add(c, hforce, parts, kRecycleParts, o->precision, keep);
         set_active(c, all);
     }
-    CUDA_OK(cudaMemcpyAsync(kst.data(), ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
-    int dev_err = 0;
-    CUDA_OK(cudaMemcpyAsync(&dev_err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CUDA_OK(cudaStreamSynchronize(st));
+    auto* kst_s = static_cast<KrylovState*>(stage_alloc(c, sizeof(KrylovState) * P));
+    auto* err_s = static_cast<int*>(stage_alloc(c, sizeof(int)));
+    CUDA_OK(cudaMemcpyAsync(kst_s, ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
+    CUDA_OK(cudaMemcpyAsync(err_s, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    stage_sync(c);
+    std::copy(kst_s, kst_s + P, kst.begin());
+    const int dev_err = *err_s;
     if (dev_err != 0) {
         CUDA_OK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), st));
         throw SmobError(SMOB_ERR_CUDA, "a tensor-core near-field kernel gave up waiting for its MMAs (results void)");
@@ -2075,8 +2453,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
 // that gave up a bounded wait (tensor-core near field) wrote nothing, so the call's results are void.
 void check_device_error(smob_ctx* c) {
     int h = 0;
-    CUDA_OK(cudaMemcpyAsync(&h, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-    CUDA_OK(cudaStreamSynchronize(c->st));
+    d2h(c, &h, c->d_err.p, sizeof(int));
     if (h != 0) {
         CUDA_OK(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->st));
         throw SmobError(SMOB_ERR_CUDA, "a tensor-core near-field kernel gave up waiting for its MMAs (results void)");
@@ -2229,12 +2606,12 @@ void update_geometry(smob_ctx* c, const std::vector<double>& centers, const std:
 template <typename F>
 void host_io(smob_ctx* c, const double* in, double* out, bool load_out, F&& f) {
     const size_t bytes = sizeof(double) * 3 * (size_t)c->M;
-    CUDA_OK(cudaMemcpyAsync(c->d_in.p, in, bytes, cudaMemcpyHostToDevice, c->st));
-    if (load_out) CUDA_OK(cudaMemcpyAsync(c->d_out.p, out, bytes, cudaMemcpyHostToDevice, c->st));
+    h2d(c, c->d_in.p, in, bytes);
+    if (load_out) h2d(c, c->d_out.p, out, bytes);
     else CUDA_OK(cudaMemsetAsync(c->d_out.p, 0, bytes, c->st));
     f(c->d_in.as<double>(), c->d_out.as<double>());
-    CUDA_OK(cudaMemcpyAsync(out, c->d_out.p, bytes, cudaMemcpyDeviceToHost, c->st));
-    check_device_error(c);  // synchronizes the stream
+    d2h(c, out, c->d_out.p, bytes);
+    check_device_error(c);
 }
 
 int op_prec(int precision) {
@@ -2401,8 +2778,7 @@ smob_status smob_step_euler_device(smob_ctx* c, const double* d_vel6n, double dt
         need(c && d_vel6n, "null argument");
         CtxScope ctx_scope(c);
         std::vector<double> v(6 * (size_t)c->N);
-        CUDA_OK(cudaMemcpyAsync(v.data(), d_vel6n, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, c->st));
-        CUDA_OK(cudaStreamSynchronize(c->st));
+        d2h(c, v.data(), d_vel6n, sizeof(double) * v.size());
         return smob_step_euler(c, v.data(), dt);
     });
 }
@@ -2674,13 +3050,11 @@ smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double
         for (int i = 0; i < 6 * c->N; ++i)
             if (!std::isfinite(force[i])) throw SmobError(SMOB_ERR_NONFINITE, "force/torque input is not finite");
         ensure_solver(c, std::max(1, o->restart));
-        CUDA_OK(cudaMemcpyAsync(c->d_force.p, force, sizeof(double) * 6 * c->N, cudaMemcpyHostToDevice, c->st));
+        h2d(c, c->d_force.p, force, sizeof(double) * 6 * c->N);
         smob_status s = solve_device(c, c->d_force.as<double>(), c->d_vel.as<double>(),
                                      density ? c->d_out.as<double>() : nullptr, o, stats);
-        CUDA_OK(cudaMemcpyAsync(vel, c->d_vel.p, sizeof(double) * 6 * c->N, cudaMemcpyDeviceToHost, c->st));
-        if (density)
-            CUDA_OK(cudaMemcpyAsync(density, c->d_out.p, sizeof(double) * 3 * c->M, cudaMemcpyDeviceToHost, c->st));
-        CUDA_OK(cudaStreamSynchronize(c->st));
+        d2h(c, vel, c->d_vel.p, sizeof(double) * 6 * c->N);
+        if (density) d2h(c, density, c->d_out.p, sizeof(double) * 3 * c->M);
         prof_flush(c);
         return s;
     });
@@ -2729,6 +3103,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
         if (f.problem == 0) r->items_rep.push_back(f);
     r->d_items_rep.upload(r->items_rep);
     r->use_graphs = c->use_graphs;
+    r->loop_graph_on = c->loop_graph_on;
     CUDA_OK(cudaStreamSynchronize(r->st));
     c->multi[k] = r.get();
     return r.release();
@@ -2881,6 +3256,35 @@ smob_status smob_set_graphs(smob_ctx* c, int on) {
         CUDA_OK(cudaStreamSynchronize(c->st));
         c->use_graphs = on != 0;
         if (!c->use_graphs) c->drop_graphs();
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_loop_graph(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        CtxScope ctx_scope(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        c->loop_graph_on = on != 0;
+        for (auto& kv : c->multi) smob_set_loop_graph(kv.second, on);
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_loop_graph_info(const smob_ctx* c, int* on, int* available) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (on) *on = c->use_graphs && c->loop_graph_on ? 1 : 0;
+        if (available) *available = c->loop_graph_ok ? 1 : 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_launch_stats(const smob_ctx* c, long long* kernels, long long* host_calls) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        if (kernels) *kernels = c->launches;
+        if (host_calls) *host_calls = c->host_calls;
         return SMOB_OK;
     });
 }

@@ -176,6 +176,116 @@ __global__ void k_kcount(int P, const KrylovState* __restrict__ ks, int* __restr
     if (p < P) kc[p] = ks[p].kcount;
 }
 
+// ---- loop control (one CTA; thread 0 alone sets the conditional handles)
+constexpr int kCtlThreads = 256;
+
+// The per-problem rules are those of the host-driven loop in api.cu, operation for operation, so
+// both loops take the same decisions on the same values.
+__global__ void k_loop_decide(int P, int merge, SolveTrack* __restrict__ t, KrylovState* __restrict__ ks,
+                              SolveParams* __restrict__ sp, const double* __restrict__ norm,
+                              unsigned char* __restrict__ in_cycle, unsigned char* __restrict__ active,
+                              double* __restrict__ beta_out, int maxit, cudaGraphConditionalHandle h_cycle) {
+    const double tol = sp->tol, inner_tol = sp->inner_tol;
+    const int mixed = sp->mixed;
+    int any = 0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        SolveTrack tr = t[p];
+        if (merge && in_cycle[p]) tr.beta = norm[p];
+        unsigned char cyc = 0;
+        if (!tr.done) {
+            if (tr.beta / tr.bnorm < tol && tr.hp_now) {
+                tr.done = 1;
+                tr.conv = 1;
+            } else if (ks[p].iters >= maxit || ks[p].nonfinite) {
+                tr.done = 1;
+            } else {
+                cyc = 1;
+                tr.cycles += 1;
+                const double a = __dmul_rn(inner_tol, tr.beta), b = __dmul_rn(__dmul_rn(0.5, tol), tr.bnorm);
+                ks[p].tol_abs = mixed ? (a < b ? b : a) : __dmul_rn(tol, tr.bnorm);
+                ks[p].cycle_fp32 = mixed ? 1 : 0;
+            }
+        }
+        in_cycle[p] = cyc;
+        active[p] = cyc;
+        beta_out[p] = tr.beta;
+        t[p] = tr;
+        any |= cyc;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        if (any) sp->cycles_run += 1;
+        cudaGraphSetConditional(h_cycle, any ? 1u : 0u);
+    }
+}
+
+__global__ void k_inner_begin(int* __restrict__ jdev, cudaGraphConditionalHandle h_inner) {
+    if (threadIdx.x == 0) {
+        *jdev = 0;
+        cudaGraphSetConditional(h_inner, 1u);
+    }
+}
+
+__global__ void k_step_next(int P, const unsigned char* __restrict__ active, int* __restrict__ jdev,
+                            int* __restrict__ runs_j, int m, cudaGraphConditionalHandle h_inner,
+                            cudaGraphConditionalHandle h_sel) {
+    int any = 0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) any |= active[p] ? 1 : 0;
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        const int j = *jdev;
+        runs_j[j] += 1;
+        const int next = j + 1;
+        *jdev = next;
+        const bool more = any && next < m;
+        cudaGraphSetConditional(h_sel, more ? (unsigned)next : 0u);
+        cudaGraphSetConditional(h_inner, more ? 1u : 0u);
+    }
+}
+
+__global__ void k_resid_decide(int P, const SolveTrack* __restrict__ t, SolveParams* __restrict__ sp,
+                               const unsigned char* __restrict__ in_cycle, unsigned char* __restrict__ upd,
+                               unsigned char* __restrict__ hpm, cudaGraphConditionalHandle h_upd,
+                               cudaGraphConditionalHandle h_hp) {
+    const int mixed = sp->mixed;
+    int any_u = 0, any_h = 0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        unsigned char u = 0, h = 0;
+        if (in_cycle[p]) {
+            const SolveTrack tr = t[p];
+            if (mixed && tr.hp_done && tr.beta <= __dmul_rn(1e-4, tr.bnorm)) u = 1;
+            else h = 1;
+        }
+        upd[p] = u;
+        hpm[p] = h;
+        any_u |= u;
+        any_h |= h;
+    }
+    any_u = __syncthreads_or(any_u);
+    any_h = __syncthreads_or(any_h);
+    if (threadIdx.x == 0) {
+        if (any_u) sp->upd_run += 1;
+        if (any_h) sp->hp_run += 1;
+        cudaGraphSetConditional(h_upd, any_u ? 1u : 0u);
+        cudaGraphSetConditional(h_hp, any_h ? 1u : 0u);
+    }
+}
+
+__global__ void k_track_mark(int P, SolveTrack* __restrict__ t, const unsigned char* __restrict__ mask, int kind) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !mask[p]) return;
+    SolveTrack& tr = t[p];
+    if (kind == 0) {
+        tr.passes32x += 1;
+        tr.x_moved = 1;
+    } else {
+        tr.passes64 += 1;
+        tr.hp_done = 1;
+        tr.hp_now = 1;
+        tr.x_moved = 0;
+    }
+}
+
 }  // namespace
 
 int launch_dots(const KrylovLaunch& L, const double* A, long long lda, int nvec, const double* b,
@@ -226,6 +336,36 @@ int launch_trisolve(const KrylovLaunch& L, int m, const unsigned char* in_cycle,
     k_trisolve<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, m, in_cycle, ks, H, g, y);
     k_kcount<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, ks, kc);
     return 2;
+}
+
+int launch_loop_decide(int P, bool merge, SolveTrack* t, KrylovState* ks, SolveParams* sp, const double* norm,
+                       unsigned char* in_cycle, unsigned char* active, double* beta_out, int maxit,
+                       unsigned long long h_cycle, cudaStream_t st) {
+    k_loop_decide<<<1, kCtlThreads, 0, st>>>(P, merge ? 1 : 0, t, ks, sp, norm, in_cycle, active, beta_out, maxit,
+                                             h_cycle);
+    return 1;
+}
+
+int launch_inner_begin(int* jdev, unsigned long long h_inner, cudaStream_t st) {
+    k_inner_begin<<<1, 32, 0, st>>>(jdev, h_inner);
+    return 1;
+}
+
+int launch_step_next(int P, const unsigned char* active, int* jdev, int* runs_j, int m, unsigned long long h_inner,
+                     unsigned long long h_sel, cudaStream_t st) {
+    k_step_next<<<1, kCtlThreads, 0, st>>>(P, active, jdev, runs_j, m, h_inner, h_sel);
+    return 1;
+}
+
+int launch_resid_decide(int P, const SolveTrack* t, SolveParams* sp, const unsigned char* in_cycle, unsigned char* upd,
+                        unsigned char* hpm, unsigned long long h_upd, unsigned long long h_hp, cudaStream_t st) {
+    k_resid_decide<<<1, kCtlThreads, 0, st>>>(P, t, sp, in_cycle, upd, hpm, h_upd, h_hp);
+    return 1;
+}
+
+int launch_track_mark(int P, SolveTrack* t, const unsigned char* mask, int kind, cudaStream_t st) {
+    k_track_mark<<<(P + 127) / 128, 128, 0, st>>>(P, t, mask, kind);
+    return 1;
 }
 
 }  // namespace smob

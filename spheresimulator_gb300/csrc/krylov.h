@@ -50,4 +50,49 @@ int launch_givens(const KrylovLaunch& L, int j, int m, KrylovState* ks, double* 
 int launch_trisolve(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const KrylovState* ks, const double* H,
                     const double* g, double* y, int* kc, cudaStream_t st);
 
+// ---- device-side control of the restart-cycle loop (graph-driven solve)
+// The loop's decisions, taken on the host between Krylov blocks otherwise, run as single-CTA kernels
+// inside one CUDA graph and steer its conditional nodes (while / switch / if). These kernels call
+// cudaGraphSetConditional, so they may only run as nodes of such a graph.
+
+// per-problem solve state, device-resident while the graph runs
+struct SolveTrack {
+    double bnorm;       // |b|
+    double beta;        // current residual norm (high precision, or updated from one by an FP32 step)
+    int done, conv;     // finished; converged
+    int hp_now;         // beta is (derived from) a high-precision residual: it may end the solve
+    int hp_done;        // a high-precision residual after a cycle exists (u_hp, x_hp are valid)
+    int x_moved;        // x changed since the last high-precision residual
+    int cycles;         // restart cycles run
+    int passes64;       // high-precision operator passes outside the Arnoldi steps
+    int passes32x;      // FP32 operator passes outside the Arnoldi steps
+};
+
+// the solve's scalars and the loop's body counters (bodies run, for the kernel count)
+struct SolveParams {
+    double tol, inner_tol;
+    int mixed;
+    int cycles_run, upd_run, hp_run;
+};
+
+// next cycle: (merge) beta of the problems of the cycle that ended = norm; then per problem: stop
+// (converged / iteration limit / non-finite) or join the cycle (in_cycle, active, the cycle's stop
+// threshold in ks); beta_out = beta; while-handle = any problem in the cycle
+int launch_loop_decide(int P, bool merge, SolveTrack* t, KrylovState* ks, SolveParams* sp, const double* norm,
+                       unsigned char* in_cycle, unsigned char* active, double* beta_out, int maxit,
+                       unsigned long long h_cycle, cudaStream_t st);
+// start of the Arnoldi steps of a cycle: step counter 0, inner while-handle 1 (the switch handle is
+// already 0: its default, and the last step of the previous cycle resets it)
+int launch_inner_begin(int* jdev, unsigned long long h_inner, cudaStream_t st);
+// after step j: counts it; the next step runs (switch-handle j+1) while a problem is active and
+// j+1 < m, otherwise the inner loop ends and the switch handle goes back to 0
+int launch_step_next(int P, const unsigned char* active, int* jdev, int* runs_j, int m, unsigned long long h_inner,
+                     unsigned long long h_sel, cudaStream_t st);
+// residual of the cycle's problems: FP32 update (MIXED, a high-precision residual exists and
+// beta <= 1e-4 |b|) or a high-precision residual; masks and if-handles for both
+int launch_resid_decide(int P, const SolveTrack* t, SolveParams* sp, const unsigned char* in_cycle, unsigned char* upd,
+                        unsigned char* hpm, unsigned long long h_upd, unsigned long long h_hp, cudaStream_t st);
+// bookkeeping of a residual pass on the problems in mask: kind 0 FP32 update, kind 1 high precision
+int launch_track_mark(int P, SolveTrack* t, const unsigned char* mask, int kind, cudaStream_t st);
+
 }  // namespace smob
