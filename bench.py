@@ -175,11 +175,27 @@ def run_native(args, world, rank, local, dist):
 
     # ---- headline: mixed precision, inputs resident
     barrier(dist)
-    l0 = mob.launch_count()
+    l0, hc0 = mob.launch_stats()
     with ClockSampler(local) as clk:
         ms_mixed, st_mixed = timed(PREC_MIXED, args.steps)
-    launches = (mob.launch_count() - l0) / max(args.steps, 1)
+    l1, hc1 = mob.launch_stats()
+    launches = (l1 - l0) / max(args.steps, 1)
+    host_calls = (hc1 - hc0) / max(args.steps, 1)
     total_s = allmax(dist, ms_mixed.sum() / 1e3)
+    # the same solves with the host-driven restart loop (captured 4-step blocks, host checks between them)
+    mob.set_loop_graph(False)
+    timed(PREC_MIXED, 2)
+    l0, hc0 = mob.launch_stats()
+    k_host = max(3, min(args.steps, 10))
+    ms_hostloop, _ = timed(PREC_MIXED, k_host)
+    l1, hc1 = mob.launch_stats()
+    mob.set_loop_graph(True)
+    loop_graph = {"on": mob.loop_graph_info()[0], "kernels_per_solve": round(launches, 1),
+                  "host_launch_calls_per_solve": round(host_calls, 1),
+                  "host_loop": {"solves_per_s": round(1e3 / float(ms_hostloop.mean()), 3),
+                                "p50_ms": round(float(np.percentile(ms_hostloop, 50)), 3), "steps": k_host,
+                                "kernels_per_solve": round((l1 - l0) / k_host, 1),
+                                "host_launch_calls_per_solve": round((hc1 - hc0) / k_host, 1)}}
     vel_mixed = np.zeros(n6)
     N.check(L.smob_memcpy_d2h(h, vel_mixed.ctypes.data_as(ctypes.c_void_p), d_vel, 8 * n6))
 
@@ -400,6 +416,8 @@ def run_native(args, world, rank, local, dist):
                 "h2d_bytes_per_step": 8 * n6, "d2h_bytes_per_step": 8 * n6,
                 "host_buffers": "pinned" if pinned else "pageable"},
         "gpu_launches": int(round(launches)),
+        "host_launch_calls": int(round(host_calls)),
+        "loop_graph": loop_graph,
         "clocks": clk.summary(),
     }
     return line
@@ -443,13 +461,25 @@ def run_config(args, world, rank, local, dist):
     for _ in range(args.warmup):
         solve(PREC_MIXED)
     barrier(dist)
-    l0 = mob.launch_count()
+    l0, hc0 = mob.launch_stats()
     ms, sts = [], None
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             t, sts, vel = solve(PREC_MIXED)
             ms.append(t)
-    launches = (mob.launch_count() - l0) / max(args.steps, 1)
+    l1, hc1 = mob.launch_stats()
+    launches = (l1 - l0) / max(args.steps, 1)
+    host_calls = (hc1 - hc0) / max(args.steps, 1)
+    # one batched solve with the host-driven restart loop, for its launch counts and time
+    mob.set_loop_graph(False)
+    l0, hc0 = mob.launch_stats()
+    t_host, _, _ = solve(PREC_MIXED)
+    l1, hc1 = mob.launch_stats()
+    mob.set_loop_graph(True)
+    loop_graph = {"on": mob.loop_graph_info()[0], "kernels_per_step": round(launches, 1),
+                  "host_launch_calls_per_step": round(host_calls, 1),
+                  "host_loop": {"ms_per_step": round(t_host, 3), "kernels_per_step": l1 - l0,
+                                "host_launch_calls_per_step": hc1 - hc0}}
     ms = np.array(ms)
     total_s = allmax(dist, ms.sum() / 1e3)
     ref_name = {"ff": PREC_FLOAT_FLOAT, "fp64": PREC_FP64}.get(args.ref)
@@ -535,6 +565,8 @@ def run_config(args, world, rank, local, dist):
                                    % (dt2, pairs / P, passes)},
         "e2e": None,
         "gpu_launches": int(round(launches)),
+        "host_launch_calls": int(round(host_calls)),
+        "loop_graph": loop_graph,
         "clocks": clk.summary(),
     }
 

@@ -177,8 +177,25 @@ class _Context:
         return v.value
 
     def set_graphs(self, on=True):
-        """CUDA graphs for the Arnoldi steps of the solves (on by default)."""
+        """CUDA graphs for the solves (on by default)."""
         N.check(self._L.smob_set_graphs(self._h, int(on)))
+
+    def set_loop_graph(self, on=True):
+        """The whole restart-cycle loop as one graph launch with device-side decisions (with graphs on);
+        off: the host drives the cycles and replays captured blocks of Arnoldi steps."""
+        N.check(self._L.smob_set_loop_graph(self._h, int(on)))
+
+    def loop_graph_info(self):
+        """(selected, available): the loop graph is selected; building one has not failed here."""
+        on, ok = ctypes.c_int(), ctypes.c_int()
+        N.check(self._L.smob_loop_graph_info(self._h, ctypes.byref(on), ctypes.byref(ok)))
+        return bool(on.value), bool(ok.value)
+
+    def launch_stats(self):
+        """(kernels run, host launch calls) on this context since creation."""
+        k, h = ctypes.c_longlong(), ctypes.c_longlong()
+        N.check(self._L.smob_launch_stats(self._h, ctypes.byref(k), ctypes.byref(h)))
+        return k.value, h.value
 
     def near_tc(self):
         """True if the FP32 near field runs on the tensor cores"""

@@ -131,6 +131,9 @@ def lib():
         "smob_launch_count": (S, [_VP, ctypes.POINTER(ctypes.c_longlong)]),
         "smob_tuning": (S, [_VP, _IP, _DP, _IP]),
         "smob_set_graphs": (S, [_VP, ctypes.c_int]),
+        "smob_set_loop_graph": (S, [_VP, ctypes.c_int]),
+        "smob_loop_graph_info": (S, [_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+        "smob_launch_stats": (S, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
         "smob_set_near_tc": (S, [_VP, ctypes.c_int]),
         "smob_set_sphere_tc": (S, [_VP, ctypes.c_int]),

@@ -77,6 +77,12 @@ struct DBuf {
     }
     void alloc(size_t b) {
         if (b <= bytes && p) return;
+        // an allocation inside a stream capture would become graph-owned memory that the buffer
+        // then outlives: every buffer a captured pass uses is allocated before the capture
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (g_alloc_stream && cudaStreamIsCapturing(g_alloc_stream, &cs) == cudaSuccess &&
+            cs != cudaStreamCaptureStatusNone)
+            throw SmobError(SMOB_ERR_STATE, "device buffer allocation inside a graph capture");
         release();
         if (b == 0) b = 16;
         s = g_alloc_stream;
@@ -316,7 +322,7 @@ struct smob_ctx {
     };
     std::map<std::vector<int>, LoopGraph> loop_graphs;
     bool loop_graph_ok = true;  // false once building one failed (the host-driven loop runs instead)
-    bool loop_graph_on = false;  // smob_set_loop_graph
+    bool loop_graph_on = true;  // smob_set_loop_graph
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
@@ -2011,7 +2017,7 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
     for (int p = 0; p < P; ++p)
         tr[p] = SolveTrack{bnorm[p], beta[p], done[p], conv[p], hp_now[p], hp_resid_done[p], x_moved[p],
                            cycles[p], passes64[p], passes32x[p]};
-    const SolveParams prm{a.tol, a.inner_tol, a.mixed ? 1 : 0, 0, 0, 0};
+    const SolveParams prm{a.tol, a.inner_tol, a.mixed ? 1 : 0, a.maxit + 1, 0, 0, 0, 0};
     h2d(c, track, tr.data(), sizeof(SolveTrack) * P);
     h2d(c, sp, &prm, sizeof(prm));
     CUDA_OK(cudaMemsetAsync(runs_j, 0, sizeof(int) * m, st));
@@ -2023,6 +2029,10 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
     CUDA_OK(cudaMemcpyAsync(sp_s, sp, sizeof(SolveParams), cudaMemcpyDeviceToHost, st));
     CUDA_OK(cudaMemcpyAsync(rj_s, runs_j, sizeof(int) * m, cudaMemcpyDeviceToHost, st));
     stage_sync(c);
+    if (sp_s->overrun) {
+        c->loop_graph_ok = false;
+        throw SmobError(SMOB_ERR_STATE, "the graph-driven restart loop ran more cycles than iterations (results void)");
+    }
     for (int p = 0; p < P; ++p) {
         const SolveTrack& t = tr_s[p];
         beta[p] = t.beta;
@@ -2102,6 +2112,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         c->d_dens.alloc(sizeof(double) * n);
         c->d_uhp.alloc(sizeof(double) * n);
         c->d_xhp.alloc(sizeof(double) * n);
+        c->d_partial64_sl.alloc(sizeof(double) * c->partial64);  // op_apply_hp_both (before any capture)
         dens = c->d_dens.as<double>();
         uhp = c->d_uhp.as<double>();
         xhp = c->d_xhp.as<double>();
@@ -2315,7 +2326,17 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
                     cudaGraph_t gr;
                     CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                     c->capturing = true;
-                    for (int j = j0; j < j0 + cnt; ++j) step(j);
+                    try {
+                        for (int j = j0; j < j0 + cnt; ++j) step(j);
+                    } catch (...) {
+                        c->capturing = false;
+                        cudaGraph_t t = nullptr;
+                        cudaStreamEndCapture(st, &t);
+                        if (t) cudaGraphDestroy(t);
+                        cudaGetLastError();
+                        c->launches = before;
+                        throw;
+                    }
                     c->capturing = false;
                     CUDA_OK(cudaStreamEndCapture(st, &gr));
                     cudaGraphExec_t ex;

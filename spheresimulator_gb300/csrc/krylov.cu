@@ -214,6 +214,10 @@ __global__ void k_loop_decide(int P, int merge, SolveTrack* __restrict__ t, Kryl
     }
     any = __syncthreads_or(any);
     if (threadIdx.x == 0) {
+        if (any && sp->cycles_run >= sp->max_cycles) {
+            sp->overrun = 1;
+            any = 0;
+        }
         if (any) sp->cycles_run += 1;
         cudaGraphSetConditional(h_cycle, any ? 1u : 0u);
     }

@@ -72,7 +72,10 @@ struct SolveTrack {
 struct SolveParams {
     double tol, inner_tol;
     int mixed;
+    int max_cycles;  // bound on the cycles of one launch: every cycle advances each of its problems by one
+                     // iteration at least, so more than the iteration limit means a broken loop
     int cycles_run, upd_run, hp_run;
+    int overrun;     // set when the bound stopped the loop (the solve's results are void)
 };
 
 // next cycle: (merge) beta of the problems of the cycle that ended = norm; then per problem: stop
