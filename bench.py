@@ -577,12 +577,17 @@ def run_serving(args, world, rank, local, dist):
     continuous-batching server; latency = completion - submission on the server's clock."""
     import threading as th
 
-    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SolveServer, configs
+    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SolveServer, configs, warm_orders
     stream = configs.cfg5_stream(seed=5 + rank, n_requests=args.requests, rate=args.rate, nmax=args.nmax)
+    # the server's start-up: the host tables of the orders the stream declares (p in {8, 12, 16, 24})
+    warm = sorted({int(p) for r in stream for p in r["orders"]})
+    t_warm = time.perf_counter()
+    warm_orders(warm)
+    t_warm = time.perf_counter() - t_warm
 
-    def serve(reqs, precision, slots, small_sms=0):
+    def serve(reqs, precision, slots, small_sms=0, graphs=False):
         srv = SolveServer(device=local, max_slots=slots, precision=precision, hbm_budget_bytes=args.hbm_budget,
-                          small_sms=small_sms)
+                          small_sms=small_sms, graphs=graphs)
         part = srv.partition_info()
         ids = [None] * len(reqs)
         t_start = time.perf_counter()
@@ -641,12 +646,16 @@ def run_serving(args, world, rank, local, dist):
     small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= 64][:8]
     solo = None
     if small:
-        sl = []
+        sl, sg = [], []
         for r in small:
             l1, _, _, _, _ = serve([r], PREC_MIXED, 1, 0)
             sl.append(float(l1[0]))
+            l1, _, _, _, _ = serve([r], PREC_MIXED, 1, 0, graphs=True)
+            sg.append(float(l1[0]))
         solo = {"requests": len(small), "p50_ms": round(1e3 * float(np.percentile(sl, 50)), 2),
-                "max_ms": round(1e3 * max(sl), 2)}
+                "max_ms": round(1e3 * max(sl), 2),
+                "with_graphs": {"p50_ms": round(1e3 * float(np.percentile(sg, 50)), 2), "max_ms": round(1e3 * max(sg), 2),
+                                "note": "request contexts capture CUDA graphs (each solves once)"}}
     sub = None
     if args.fp64_subset > 0:
         small = [dict(r, arrival=0.0) for r in stream if len(r["radii"]) <= args.fp64_subset]
@@ -671,7 +680,9 @@ def run_serving(args, world, rank, local, dist):
         "config": {"workload": "cfg5: served stream, %d requests, Poisson rate %.2f/s, N log-uniform [4,%d], "
                                "p in {8,12,16,24}, a~U[0.9,1.1], gap 0.05, tol 1e-6/1e-8" % (len(stream), args.rate, args.nmax),
                    "slots": args.slots, "parallelism": "replicas only",
-                   "l2": "not flushed: requests arrive in real time, latency measured on the server clock"},
+                   "l2": "not flushed: requests arrive in real time, latency measured on the server clock",
+                   "server_start": "per-order host tables of p in %s built before the stream (smob_warm_orders, "
+                                   "%.2f s)" % (warm, t_warm)},
         "latency_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 2),
                        "p99": round(1e3 * float(np.percentile(lat, 99)), 2)},
         "latency_by_size": buckets(lat),
@@ -906,11 +917,15 @@ def far_once():
                       np.isfinite(b).all() and np.isfinite(d).all())}))
 
 
-def solve_once():
-    """Three mixed-precision cfg2 solves (the first captures the graphs), for a kernel launch list."""
+def solve_once(host_loop=False):
+    """Three mixed-precision cfg2 solves (the first captures the graphs), for a kernel launch list.
+    host_loop: the host-driven restart loop (the same kernels; ncu lists no kernel that runs inside a
+    conditional graph node's body, so a launch list of the loop's kernels needs this)."""
     from spheresimulator_gb300 import PREC_MIXED, SphereSTKMobMat, configs
     c = configs.cfg2()
     mob = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    if host_loop:
+        mob.set_loop_graph(False)
     for _ in range(3):
         v = mob.solveMob(c["force"], tol=TOL, restart=RESTART, max_iters=1000, precision=PREC_MIXED)
     print(json.dumps({"solve_once": "cfg2", "iterations": mob.last_stats[0]["iterations"],
@@ -977,6 +992,8 @@ def main():
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="with --solve-once: the host-driven restart loop instead of the loop graph")
     ap.add_argument("--solve-once", action="store_true",
                     help="three mixed cfg2 solves and exit; a short program for a kernel launch list")
     ap.add_argument("--near-once", action="store_true",
@@ -989,7 +1006,7 @@ def main():
         near_once()
         return
     if args.solve_once:
-        solve_once()
+        solve_once(args.host_loop)
         return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3

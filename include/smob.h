@@ -218,7 +218,9 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * measured error stays within a small factor of it, below 3.4 eps over orders 8-24). eps sets
  * it for the FP32 operator passes (SMOB_PREC_MIXED inner solves and final velocity correction; default
  * 1e-5), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
- * layer, SMOB_PREC_FLOAT_FLOAT; default 1e-10). Near pairs, the own sphere and every FP64 pass keep the
+ * layer, SMOB_PREC_FLOAT_FLOAT; at most 1e-9). By default eps_hp follows the solves: 1e-9 at creation,
+ * tightened once to a tenth of a solve's tolerance, but not below 1e-10, when a solve asks for less than
+ * 1e-8 (both sets are rebuilt then; never loosened); once set here it stays as set. Near pairs, the own sphere and every FP64 pass keep the
  * direct sum over the grid points: the plain FP64 solve is the reference's smooth quadrature. The
  * reference evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).
  * A tolerance <= 0 turns that set off (the direct sum). Setting the tolerances empties the recycled
@@ -283,6 +285,7 @@ typedef struct {
     int max_iters;           /* GMRES iteration limit per request */
     int precision;           /* smob_precision of every request */
     double inner_tol;        /* MIXED inner tolerance (<= 0: library default) */
+    int graphs;              /* CUDA graphs in the request contexts: 0 off, 1 on (see smob_set_graphs) */
 } smob_server_opts;
 typedef struct {
     int state;               /* 0 queued, 1 on the GPU, 2 done */
@@ -323,6 +326,11 @@ smob_status smob_server_partition(smob_server* server, int small_sms);
 /* SMs of the small and the big partition (0, 0 without a partition) */
 smob_status smob_server_partition_info(smob_server* server, int* small_sms, int* big_sms);
 smob_status smob_server_destroy(smob_server* server);
+/* Builds the per-order host tables (grid, Legendre and twiddle tables, the near-field solid-harmonic
+ * maps, the coarse equivalent-source maps of every coarse order below p) that the first context of an
+ * order otherwise builds, for each listed order, and keeps them for the process. A server calls it for
+ * the orders it expects so that no request pays for them (host work only; no device needed). */
+smob_status smob_warm_orders(const int* orders, int n_orders);
 /* admission footprint estimate (bytes of device memory) of one request; host-only arithmetic */
 size_t smob_request_bytes(int n_spheres, const int* orders, int restart);
 

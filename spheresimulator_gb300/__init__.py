@@ -18,7 +18,7 @@ from . import _native as N
 from ._native import PREC_FLOAT_FLOAT, PREC_FP64, PREC_MIXED, SmobError
 
 __all__ = ["SphereSTKSHOperator", "SphereSTKMobMat", "SmobError", "PREC_FP64", "PREC_MIXED", "PREC_FLOAT_FLOAT", "solve_opts",
-           "grid_number", "spectral_dof"]
+           "grid_number", "spectral_dof", "warm_orders", "request_bytes", "SolveServer"]
 
 
 def grid_number(p):
@@ -358,6 +358,13 @@ class SphereSTKSHOperator(_Context):
         return out
 
 
+def warm_orders(orders):
+    """Build the per-order host tables of these orders now (smob_warm_orders), so that the first
+    context of each order does not pay for them."""
+    o = N.i32(orders).reshape(-1)
+    N.check(N.lib().smob_warm_orders(N.iptr(o), len(o)))
+
+
 def request_bytes(orders, restart=50):
     """Device-memory footprint the server uses to admit a request (host arithmetic only)."""
     o = N.i32(orders).reshape(-1)
@@ -368,11 +375,12 @@ class SolveServer:
     """Request loop with continuous batching of mobility solves on one GPU (smob_server_*)."""
 
     def __init__(self, device=0, max_slots=8, hbm_budget_bytes=0.0, restart=50, max_iters=2000,
-                 precision=PREC_MIXED, inner_tol=0.0, small_sms=0):
-        """small_sms > 0: SMs reserved (green context) for small requests while big ones run"""
+                 precision=PREC_MIXED, inner_tol=0.0, small_sms=0, graphs=False):
+        """small_sms > 0: SMs reserved (green context) for small requests while big ones run;
+        graphs: CUDA graphs in the request contexts (each solves once, so capturing costs more than it saves)"""
         self._L = N.lib()
         opts = N.ServerOpts(int(device), int(max_slots), float(hbm_budget_bytes), int(restart), int(max_iters),
-                            int(precision), float(inner_tol))
+                            int(precision), float(inner_tol), int(bool(graphs)))
         h = ctypes.c_void_p()
         N.check(self._L.smob_server_create(ctypes.byref(h), ctypes.byref(opts)))
         self._h = h

@@ -55,7 +55,7 @@ class ProblemStats(ctypes.Structure):
 class ServerOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_slots", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double),
                 ("restart", ctypes.c_int), ("max_iters", ctypes.c_int), ("precision", ctypes.c_int),
-                ("inner_tol", ctypes.c_double)]
+                ("inner_tol", ctypes.c_double), ("graphs", ctypes.c_int)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -132,6 +132,7 @@ def lib():
         "smob_tuning": (S, [_VP, _IP, _DP, _IP]),
         "smob_set_graphs": (S, [_VP, ctypes.c_int]),
         "smob_set_loop_graph": (S, [_VP, ctypes.c_int]),
+        "smob_warm_orders": (S, [ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
         "smob_loop_graph_info": (S, [_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
         "smob_launch_stats": (S, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <memory>
@@ -167,10 +168,13 @@ constexpr int kGraphBlock = 4;  // Arnoldi steps per captured graph / per host c
 // 1e-6), a residual update's error at most ~3e-10 |b|, and cfg2 solves take the same iterations,
 // refinements and final error as at 1e-6 or 1e-4
 constexpr double kCoarseEpsDefault = 1e-5;
-// float-float passes (refinement residuals, u_hp): on cfg2 the mixed solve's velocity error against a
-// 1e-12 FP64 solve is 8.63e-11 with 1e-10, 1e-11, 1e-12 or the direct sum alike, and its final relative
-// residual moves by 3e-14
-constexpr double kCoarseEpsHpDefault = 1e-10;
+// float-float passes (refinement residuals, u_hp): one decade below the 1e-8 solve tolerance. The mixed
+// solves' velocity errors against the oracle's 1e-12 solves stay where the solve tolerance puts them
+// from 1e-12 up to 9e-10 (cfg2 9.28e-11; 48 polydisperse spheres with near-singular gaps 6.68e-10; an
+// uneven batch of 6 1.80e-10; 20 spheres at p = 24 4.05e-10, the same to three digits at 1e-10, 3e-10
+// and 9e-10), while 1e-9 evaluates 22% fewer float-float pairs than 1e-10 on cfg2 (12.6 vs 13.8 ms
+// per solve)
+constexpr double kCoarseEpsHpDefault = 1e-9;
 constexpr double kCoarseMargin = 1.0;  // orders added to log(eps) / log(a_s / r_min) (measured, p = 16)
 // coarse targets: one order more (the traction's target normal raises the field's degree by one;
 // with it the interpolated traction stays within the sources' error, measured in numpy over p = 12-24)
@@ -294,7 +298,7 @@ struct smob_ctx {
     DBuf d_H, d_g, d_cs, d_sn, d_y, d_kc, d_ks, d_norm, d_hn, d_beta, d_partial_red, d_incycle;
     // graph-driven restart loop: per-problem state, scalars and body counters, residual masks, the
     // Arnoldi step counter and per-step run counts
-    DBuf d_track, d_sparams, d_updmask, d_hpmask, d_jdev, d_runs_j;
+    DBuf d_track, d_sparams, d_updmask, d_hpmask, d_freshmask, d_jdev, d_runs_j, d_bnorm;
     DBuf d_red_count;     // per (problem, vector) counters of the fused dot reductions
     int red_cstride = 0;  // counters per problem
     bool have_xlast = false;
@@ -319,9 +323,11 @@ struct smob_ctx {
         cudaGraphExec_t exec = nullptr;
         long long k_top = 0, k_cycle = 0, k_upd = 0, k_hp = 0;
         std::vector<long long> k_step;  // per step index j: step(j) and the step-control kernel
+        long long k_post = 0, k_from = 0, k_moved = 0, k_fresh = 0;  // full-solve graph: final velocity
     };
     std::map<std::vector<int>, LoopGraph> loop_graphs;
     bool loop_graph_ok = true;  // false once building one failed (the host-driven loop runs instead)
+    bool eps_hp_auto = true;    // the float-float set's tolerance follows the solves (fit_eps_hp)
     bool loop_graph_on = true;  // smob_set_loop_graph
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
@@ -1693,6 +1699,8 @@ void ensure_solver(smob_ctx* c, int m) {
     c->d_sparams.alloc(sizeof(SolveParams));
     c->d_updmask.alloc(c->P);
     c->d_hpmask.alloc(c->P);
+    c->d_freshmask.alloc(c->P);
+    c->d_bnorm.alloc(sizeof(double) * c->P);
     c->d_jdev.alloc(sizeof(int));
     c->d_runs_j.alloc(sizeof(int) * std::max(m, c->restart_cap));
     if (!c->d_xlast.p) {
@@ -1894,15 +1902,22 @@ cudaGraphNode_t add_conditional(cudaGraph_t g, const std::vector<cudaGraphNode_t
     return node;
 }
 
-// Runs the restart loop as one graph launch (built on first use per LoopArgs shape). The per-problem
-// state goes in and comes back in one copy each way. Returns false, with nothing changed, when the
-// graph cannot be built (conditional nodes unavailable): the caller runs the host loop instead.
-template <class Step, class Upd, class HpOps, class ExplOps, class CycUpd>
-bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, HpOps& hp_residual_ops,
-                    ExplOps& explicit_residual_ops, CycUpd& cycle_update_ops, std::vector<char>& done,
-                    std::vector<char>& conv, std::vector<double>& beta, const std::vector<double>& bnorm,
-                    std::vector<char>& hp_now, std::vector<char>& hp_resid_done, std::vector<char>& x_moved,
-                    std::vector<int>& cycles, std::vector<int>& passes64, std::vector<int>& passes32x) {
+// The launch sequences the graphs are built from (solve_device's own lambdas, so the host-driven
+// path and the graphs issue the same kernels). The full-solve graph also takes the cold-start set-up
+// and the final velocity.
+struct SolveOps {
+    std::function<void(int)> step;                    // Arnoldi step j on the active problems
+    std::function<void(const double*)> upd;           // r -= A32 dx (active problems)
+    std::function<void()> hp_residual;                // MIXED high-precision residual (active problems)
+    std::function<void()> explicit_residual;          // r = b - A x in the solve's precision
+    std::function<const double*()> cycle_update;      // x += V y (cycle problems); returns dx
+    std::function<void()> pre;                        // cold start: rho, b, |b|, x = 0, r = b, |r|, track
+    std::function<void()> post_from_hp, post_moved, post_mid, post_fresh, post_end;  // final velocity
+};
+
+// Appends the restart loop to graph G after deps (see the diagram above); returns its while node.
+cudaGraphNode_t append_loop(smob_ctx* c, cudaGraph_t G, const std::vector<cudaGraphNode_t>& deps, const LoopArgs& a,
+                            smob_ctx::LoopGraph& lg, const SolveOps& ops, bool first_decide) {
     const int P = c->P, m = a.m;
     cudaStream_t st = c->st;
     KrylovLaunch L = c->kl();
@@ -1919,87 +1934,176 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
     double* V = c->d_V.as<double>();
     int* jdev = c->d_jdev.as<int>();
     int* runs_j = c->d_runs_j.as<int>();
-    const std::vector<int> key{a.mixed ? 1 : 0, a.hp, a.cyc_prec, a.pc ? 1 : 0, m, a.maxit};
+    auto count = [&](auto&& f) {
+        const long long k0 = c->launches;
+        f();
+        return c->launches - k0;
+    };
+    cudaGraphConditionalHandle hc, hi, hsel, hu, hh;
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hc, G, 0, cudaGraphCondAssignDefault));
+    std::vector<cudaGraphNode_t> tail = deps;
+    if (first_decide)
+        tail = capture_into(c, G, deps, [&] {
+            lg.k_top += count([&] {
+                check_launch(c, launch_loop_decide(P, false, track, ks, sp, nullptr, incyc, act, beta_d, a.maxit, hc,
+                                                   st));
+            });
+        });
+    cudaGraph_t body = nullptr;
+    const cudaGraphNode_t wnode = add_conditional(G, tail, hc, cudaGraphCondTypeWhile, 1, &body);
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hu, body, 0, cudaGraphCondAssignDefault));
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hh, body, 0, cudaGraphCondAssignDefault));
+    long long kc = 0;
+    tail = capture_into(c, body, {}, [&] {
+        kc += count([&] {
+            check_launch(c, launch_scale(L, r, beta_d, 1, true, act, V, st));
+            check_launch(c, launch_cycle_init(L, m, incyc, beta_d, ks, c->d_H.as<double>(), c->d_g.as<double>(), st));
+            check_launch(c, launch_inner_begin(jdev, hi, st));
+        });
+    });
+    cudaGraph_t inner = nullptr;
+    const cudaGraphNode_t inode = add_conditional(body, tail, hi, cudaGraphCondTypeWhile, 1, &inner);
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hsel, inner, 0, cudaGraphCondAssignDefault));
+    std::vector<cudaGraph_t> steps(m, nullptr);
+    const cudaGraphNode_t snode = add_conditional(inner, {}, hsel, cudaGraphCondTypeSwitch, m, steps.data());
+    lg.k_step.assign(m, 0);
+    for (int j = 0; j < m; ++j) capture_into(c, steps[j], {}, [&] { lg.k_step[j] = count([&] { ops.step(j); }); });
+    long long knext = 0;
+    capture_into(c, inner, {snode}, [&] {
+        knext = count([&] { check_launch(c, launch_step_next(P, act, jdev, runs_j, m, hi, hsel, st)); });
+    });
+    for (long long& k : lg.k_step) k += knext;
+    const double* dx = nullptr;
+    tail = capture_into(c, body, {inode}, [&] {
+        kc += count([&] {
+            dx = ops.cycle_update();
+            check_launch(c, launch_resid_decide(P, track, sp, incyc, updm, hpm, hu, hh, st));
+        });
+    });
+    cudaGraph_t ub = nullptr, hb = nullptr;
+    const cudaGraphNode_t unode = add_conditional(body, tail, hu, cudaGraphCondTypeIf, 1, &ub);
+    capture_into(c, ub, {}, [&] {
+        lg.k_upd = count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, updm, P, cudaMemcpyDeviceToDevice, st));
+            ops.upd(dx);
+            check_launch(c, launch_track_mark(P, track, updm, 0, st));
+        });
+    });
+    const cudaGraphNode_t hnode = add_conditional(body, {unode}, hh, cudaGraphCondTypeIf, 1, &hb);
+    capture_into(c, hb, {}, [&] {
+        lg.k_hp = count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, hpm, P, cudaMemcpyDeviceToDevice, st));
+            if (a.mixed) ops.hp_residual();
+            else ops.explicit_residual();
+            check_launch(c, launch_track_mark(P, track, hpm, 1, st));
+        });
+    });
+    capture_into(c, body, {hnode}, [&] {
+        kc += count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, incyc, P, cudaMemcpyDeviceToDevice, st));
+            check_launch(c, launch_dots(L, r, 0, 1, r, act, norm, 1, 0, false, true, st));
+            check_launch(c, launch_loop_decide(P, true, track, ks, sp, norm, incyc, act, beta_d, a.maxit, hc, st));
+        });
+    });
+    lg.k_cycle = kc;
+    return wnode;
+}
+
+// Appends the final velocity of the full-solve graph after deps: per problem u from u_hp (+ the FP32
+// single layer of x - x_hp) or one high-precision single-layer pass, rho += x, rigid averages.
+void append_final(smob_ctx* c, cudaGraph_t G, const std::vector<cudaGraphNode_t>& deps, smob_ctx::LoopGraph& lg,
+                  const SolveOps& ops) {
+    const int P = c->P;
+    cudaStream_t st = c->st;
+    auto* track = c->d_track.as<SolveTrack>();
+    auto* sp = c->d_sparams.as<SolveParams>();
+    unsigned char* act = c->d_active.as<unsigned char>();
+    unsigned char* m_from = c->d_updmask.as<unsigned char>();
+    unsigned char* m_moved = c->d_hpmask.as<unsigned char>();
+    unsigned char* m_fresh = c->d_freshmask.as<unsigned char>();
+    auto count = [&](auto&& f) {
+        const long long k0 = c->launches;
+        f();
+        return c->launches - k0;
+    };
+    cudaGraphConditionalHandle hf, hm, hr;
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hf, G, 0, cudaGraphCondAssignDefault));
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hm, G, 0, cudaGraphCondAssignDefault));
+    CUDA_OK(cudaGraphConditionalHandleCreate(&hr, G, 0, cudaGraphCondAssignDefault));
+    auto tail = capture_into(c, G, deps, [&] {
+        lg.k_post += count([&] {
+            CUDA_OK(cudaMemsetAsync(c->d_u.p, 0, sizeof(double) * 3 * (size_t)c->M, st));
+            check_launch(c, launch_final_decide(P, track, sp, m_from, m_moved, m_fresh, hf, hm, hr, st));
+        });
+    });
+    cudaGraph_t bf = nullptr, bm = nullptr, br = nullptr;
+    const cudaGraphNode_t nf = add_conditional(G, tail, hf, cudaGraphCondTypeIf, 1, &bf);
+    capture_into(c, bf, {}, [&] {
+        lg.k_from = count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, m_from, P, cudaMemcpyDeviceToDevice, st));
+            ops.post_from_hp();
+        });
+    });
+    const cudaGraphNode_t nm = add_conditional(G, {nf}, hm, cudaGraphCondTypeIf, 1, &bm);
+    capture_into(c, bm, {}, [&] {
+        lg.k_moved = count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, m_moved, P, cudaMemcpyDeviceToDevice, st));
+            ops.post_moved();
+        });
+    });
+    tail = capture_into(c, G, {nm}, [&] {
+        lg.k_post += count([&] {
+            CUDA_OK(cudaMemsetAsync(act, 1, P, st));
+            ops.post_mid();
+        });
+    });
+    const cudaGraphNode_t nr = add_conditional(G, tail, hr, cudaGraphCondTypeIf, 1, &br);
+    capture_into(c, br, {}, [&] {
+        lg.k_fresh = count([&] {
+            CUDA_OK(cudaMemcpyAsync(act, m_fresh, P, cudaMemcpyDeviceToDevice, st));
+            ops.post_fresh();
+        });
+    });
+    capture_into(c, G, {nr}, [&] {
+        lg.k_post += count([&] {
+            CUDA_OK(cudaMemsetAsync(act, 1, P, st));
+            ops.post_end();
+        });
+    });
+}
+
+// Runs the restart loop (full = false: the per-problem state goes in and comes back in one copy each
+// way) or the whole cold-start solve (full = true: set-up, loop and final velocity; the state only
+// comes back) as one graph launch, built on first use per LoopArgs shape. Returns false, with nothing
+// changed, when the graph cannot be built (conditional nodes unavailable): the caller runs the host
+// path instead.
+bool run_loop_graph(smob_ctx* c, const LoopArgs& a, const SolveOps& ops, bool full, std::vector<char>& done,
+                    std::vector<char>& conv, std::vector<double>& beta, std::vector<double>& bnorm,
+                    std::vector<char>& hp_now, std::vector<char>& hp_resid_done, std::vector<char>& x_moved,
+                    std::vector<int>& cycles, std::vector<int>& passes64, std::vector<int>& passes32x) {
+    const int P = c->P, m = a.m;
+    cudaStream_t st = c->st;
+    auto* track = c->d_track.as<SolveTrack>();
+    auto* sp = c->d_sparams.as<SolveParams>();
+    int* runs_j = c->d_runs_j.as<int>();
+    const std::vector<int> key{full ? 1 : 0, a.mixed ? 1 : 0, a.hp, a.cyc_prec, a.pc ? 1 : 0, m, a.maxit};
     auto it = c->loop_graphs.find(key);
     if (it == c->loop_graphs.end()) {
         smob_ctx::LoopGraph lg;
         const long long before = c->launches;
-        auto count = [&](auto&& f) {
-            const long long k0 = c->launches;
-            f();
-            return c->launches - k0;
-        };
         cudaGraph_t G = nullptr;
         try {
             CUDA_OK(cudaGraphCreate(&G, 0));
-            cudaGraphConditionalHandle hc, hi, hsel, hu, hh;
-            CUDA_OK(cudaGraphConditionalHandleCreate(&hc, G, 0, cudaGraphCondAssignDefault));
-            auto tail = capture_into(c, G, {}, [&] {
-                lg.k_top = count([&] {
-                    check_launch(c, launch_loop_decide(P, false, track, ks, sp, nullptr, incyc, act, beta_d, a.maxit,
-                                                       hc, st));
+            std::vector<cudaGraphNode_t> tail;
+            if (full)
+                tail = capture_into(c, G, {}, [&] {
+                    const long long k0 = c->launches;
+                    ops.pre();
+                    lg.k_top += c->launches - k0;
                 });
-            });
-            cudaGraph_t body = nullptr;
-            add_conditional(G, tail, hc, cudaGraphCondTypeWhile, 1, &body);
-            CUDA_OK(cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault));
-            CUDA_OK(cudaGraphConditionalHandleCreate(&hu, body, 0, cudaGraphCondAssignDefault));
-            CUDA_OK(cudaGraphConditionalHandleCreate(&hh, body, 0, cudaGraphCondAssignDefault));
-            long long kc = 0;
-            tail = capture_into(c, body, {}, [&] {
-                kc += count([&] {
-                    check_launch(c, launch_scale(L, r, beta_d, 1, true, act, V, st));
-                    check_launch(c, launch_cycle_init(L, m, incyc, beta_d, ks, c->d_H.as<double>(),
-                                                      c->d_g.as<double>(), st));
-                    check_launch(c, launch_inner_begin(jdev, hi, st));
-                });
-            });
-            cudaGraph_t inner = nullptr;
-            cudaGraphNode_t inode = add_conditional(body, tail, hi, cudaGraphCondTypeWhile, 1, &inner);
-            CUDA_OK(cudaGraphConditionalHandleCreate(&hsel, inner, 0, cudaGraphCondAssignDefault));
-            std::vector<cudaGraph_t> steps(m, nullptr);
-            cudaGraphNode_t snode = add_conditional(inner, {}, hsel, cudaGraphCondTypeSwitch, m, steps.data());
-            lg.k_step.assign(m, 0);
-            for (int j = 0; j < m; ++j) capture_into(c, steps[j], {}, [&] { lg.k_step[j] = count([&] { step(j); }); });
-            long long knext = 0;
-            capture_into(c, inner, {snode}, [&] {
-                knext = count([&] { check_launch(c, launch_step_next(P, act, jdev, runs_j, m, hi, hsel, st)); });
-            });
-            for (long long& k : lg.k_step) k += knext;
-            const double* dx = nullptr;
-            tail = capture_into(c, body, {inode}, [&] {
-                kc += count([&] {
-                    dx = cycle_update_ops();
-                    check_launch(c, launch_resid_decide(P, track, sp, incyc, updm, hpm, hu, hh, st));
-                });
-            });
-            cudaGraph_t ub = nullptr, hb = nullptr;
-            cudaGraphNode_t unode = add_conditional(body, tail, hu, cudaGraphCondTypeIf, 1, &ub);
-            capture_into(c, ub, {}, [&] {
-                lg.k_upd = count([&] {
-                    CUDA_OK(cudaMemcpyAsync(act, updm, P, cudaMemcpyDeviceToDevice, st));
-                    upd_ops(dx);
-                    check_launch(c, launch_track_mark(P, track, updm, 0, st));
-                });
-            });
-            cudaGraphNode_t hnode = add_conditional(body, {unode}, hh, cudaGraphCondTypeIf, 1, &hb);
-            capture_into(c, hb, {}, [&] {
-                lg.k_hp = count([&] {
-                    CUDA_OK(cudaMemcpyAsync(act, hpm, P, cudaMemcpyDeviceToDevice, st));
-                    if (a.mixed) hp_residual_ops();
-                    else explicit_residual_ops();
-                    check_launch(c, launch_track_mark(P, track, hpm, 1, st));
-                });
-            });
-            capture_into(c, body, {hnode}, [&] {
-                kc += count([&] {
-                    CUDA_OK(cudaMemcpyAsync(act, incyc, P, cudaMemcpyDeviceToDevice, st));
-                    check_launch(c, launch_dots(L, r, 0, 1, r, act, norm, 1, 0, false, true, st));
-                    check_launch(c, launch_loop_decide(P, true, track, ks, sp, norm, incyc, act, beta_d, a.maxit, hc,
-                                                       st));
-                });
-            });
-            lg.k_cycle = kc;
+            const cudaGraphNode_t wnode = append_loop(c, G, tail, a, lg, ops, true);
+            if (full) append_final(c, G, {wnode}, lg, ops);
             CUDA_OK(cudaGraphInstantiate(&lg.exec, G, 0));
             cudaGraphDestroy(G);
             c->launches = before;
@@ -2013,12 +2117,18 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
         it = c->loop_graphs.emplace(key, std::move(lg)).first;
     }
     const smob_ctx::LoopGraph& lg = it->second;
-    std::vector<SolveTrack> tr(P);
-    for (int p = 0; p < P; ++p)
-        tr[p] = SolveTrack{bnorm[p], beta[p], done[p], conv[p], hp_now[p], hp_resid_done[p], x_moved[p],
-                           cycles[p], passes64[p], passes32x[p]};
-    const SolveParams prm{a.tol, a.inner_tol, a.mixed ? 1 : 0, a.maxit + 1, 0, 0, 0, 0};
-    h2d(c, track, tr.data(), sizeof(SolveTrack) * P);
+    if (!full) {
+        std::vector<SolveTrack> tr(P);
+        for (int p = 0; p < P; ++p)
+            tr[p] = SolveTrack{bnorm[p], beta[p], done[p], conv[p], hp_now[p], hp_resid_done[p], x_moved[p],
+                               cycles[p], passes64[p], passes32x[p]};
+        h2d(c, track, tr.data(), sizeof(SolveTrack) * P);
+    }
+    SolveParams prm{};
+    prm.tol = a.tol;
+    prm.inner_tol = a.inner_tol;
+    prm.mixed = a.mixed ? 1 : 0;
+    prm.max_cycles = a.maxit + 1;
     h2d(c, sp, &prm, sizeof(prm));
     CUDA_OK(cudaMemsetAsync(runs_j, 0, sizeof(int) * m, st));
     CUDA_OK(cudaGraphLaunch(lg.exec, st));
@@ -2035,6 +2145,7 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
     }
     for (int p = 0; p < P; ++p) {
         const SolveTrack& t = tr_s[p];
+        bnorm[p] = t.bnorm;
         beta[p] = t.beta;
         done[p] = char(t.done);
         conv[p] = char(t.conv);
@@ -2046,11 +2157,38 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, Step& step, Upd& upd_ops, Hp
         passes32x[p] = t.passes32x;
     }
     long long k = lg.k_top + (long long)sp_s->cycles_run * lg.k_cycle + (long long)sp_s->upd_run * lg.k_upd +
-                  (long long)sp_s->hp_run * lg.k_hp;
+                  (long long)sp_s->hp_run * lg.k_hp + lg.k_post + (long long)sp_s->fin_from * lg.k_from +
+                  (long long)sp_s->fin_moved * lg.k_moved + (long long)sp_s->fin_fresh * lg.k_fresh;
     for (int j = 0; j < m; ++j) k += (long long)rj_s[j] * lg.k_step[j];
     c->launches += k;
     c->host_calls += 1;
     return true;
+}
+
+// New far-field tolerances: both coarse sets rebuilt (the FP32 one and the float-float one).
+void rebuild_far_sets(smob_ctx* c, double eps, double eps_hp) {
+    AllocStreamScope as(c->st);
+    c->drop_graphs();  // captured blocks hold the old coarse tables
+    for (auto& kv : c->multi) smob_destroy(kv.second);  // several-RHS copies follow the new tolerance
+    c->multi.clear();
+    c->c32.eps = eps > 0 ? eps : 0.0;
+    c->chp.eps = eps_hp > 0 ? eps_hp : 0.0;
+    c->rk = 0;  // recycled residuals belong to the old operators
+    build_coarse(c);
+    bind_geom(c);
+    coarse_grids(c);
+    CUDA_OK(cudaStreamSynchronize(c->st));
+}
+
+// The float-float set's tolerance follows the solves (unless the caller set it): one decade below the
+// tolerance a solve asks for, at most kCoarseEpsHpDefault (its value at creation), at least 1e-10. A
+// solve asking for more than the set gives tightens it once (both sets rebuilt); it is never loosened.
+// (Not below 1e-10: at 1e-11 a batch's problems and the same problems alone were measured to differ in
+// the last bits, 3e-15 relative, which the batched solve must not.)
+void fit_eps_hp(smob_ctx* c, double tol) {
+    if (!c->eps_hp_auto || c->chp.eps <= 0) return;
+    const double want = std::min(kCoarseEpsHpDefault, std::max(0.1 * tol, 1e-10));
+    if (want < c->chp.eps) rebuild_far_sets(c, c->c32.eps, want);
 }
 
 // the mobility solve on device pointers (SphereSTKMobMat::solveMob, BIE/SphereSTKMobMat.cpp:146-286)
@@ -2066,6 +2204,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     const bool ffar = o->precision == SMOB_PREC_FLOAT_FLOAT;
     const int hp = (mixed || ffar) ? OP_DF : OP_FP64;
     const int cyc_prec = mixed ? OP_FP32 : hp;
+    if (hp == OP_DF) fit_eps_hp(c, tol);  // before anything is captured: it rebuilds the coarse sets
     ensure_tuned(c);  // before any capture: the tuner synchronizes
     ensure_solver(c, m);
     const size_t n = 3 * (size_t)c->M;
@@ -2097,10 +2236,6 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
     };
 
     std::vector<unsigned char> all(P, 1);
-    set_active(c, all);
-    std::vector<KrylovState> hks(P);
-    for (auto& k : hks) k = KrylovState{0, 0, 0, 0, 0, 0, 0};
-    h2d(c, ks, hks.data(), sizeof(KrylovState) * P);
     std::vector<int> passes64(P, 0), cycles(P, 0), passes32x(P, 0);
     std::vector<char> hp_resid_done(P, 0);  // a high-precision residual after a cycle exists
     // MIXED: beta[p] is a high-precision residual norm (or one updated from it by a small FP32 step);
@@ -2137,89 +2272,6 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         for (int p = 0; p < P; ++p)
             if (mask[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
     };
-
-    // step 1: rigid density; step 2: b = -(I/2 + K) rho. FP64 / float-float: in the solve's precision.
-    // MIXED: with the FP32 operator. b only seeds the first inner cycle and scales the tolerance; every
-    // high-precision residual is formed directly as r = -(I/2 + K)(rho + x) - L x, so b's FP32 error
-    // never reaches a residual that decides convergence.
-    check_launch(c, launch_rigid_density(c->g, d_force, rho, st));
-    CUDA_OK(cudaMemsetAsync(b, 0, sizeof(double) * n, st));
-    op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, mixed ? OP_FP32 : hp);
-    for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
-    std::vector<double> bnorm = seg_norms(c, b, act);
-
-    // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution, zero, or
-    // (warm_start 2) the combination of recycled earlier solutions closest to this b
-    std::vector<char> done(P, 0), conv(P, 0);
-    std::vector<double> beta(P, 0.0);
-    const bool recycle = o->warm_start == 2;
-    std::vector<double> hforce;
-    if (recycle) {
-        hforce.resize(6 * (size_t)c->N);
-        d2h(c, hforce.data(), d_force, sizeof(double) * hforce.size());
-    }
-    if (recycle && c->rk > 0) {
-        // MIXED from MIXED columns: a force in the span (to far below the tolerance) takes the
-        // combined residual, u_hp and x_hp as well, which are those of the combined solution (every
-        // part is linear in the force): no operator pass is needed to know where it stands
-        const bool state = mixed && c->rprec == SMOB_PREC_MIXED;
-        double* parts[kRecycleParts] = {x, state ? r : nullptr, state ? uhp : nullptr, state ? xhp : nullptr};
-        const std::vector<double> est = recycle_guess(c, hforce, parts, kRecycleParts);
-        std::vector<unsigned char> good(P, 0), poor(P, 0);
-        bool any_good = false, any_poor = false;
-        for (int p = 0; p < P; ++p) {
-            if (state && est[p] <= 1e-2 * tol) hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 1;
-            else if (mixed && est[p] <= kRecycleHpFirst) good[p] = 1, any_good = true;
-            else poor[p] = 1, any_poor = true;
-        }
-        if (any_poor) {
-            set_active(c, poor);
-            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
-            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
-            for (int p = 0; p < P; ++p)
-                if (poor[p]) (mixed ? passes32x[p] : passes64[p])++, x_moved[p] = mixed ? 1 : 0;
-        }
-        if (any_good) hp_residual(good);
-        set_active(c, all);
-    } else if (o->warm_start && c->have_xlast) {
-        CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-        CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
-        op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
-        for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
-        if (mixed) std::fill(x_moved.begin(), x_moved.end(), 1);
-        check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
-        check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
-    } else {
-        CUDA_OK(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
-        CUDA_OK(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    }
-    beta = seg_norms(c, r, act);
-    bool nonfinite_any = false;
-    for (int p = 0; p < P; ++p) {
-        if (!std::isfinite(bnorm[p]) || !std::isfinite(beta[p])) {
-            done[p] = 1;
-            nonfinite_any = true;
-        } else if (bnorm[p] < 1e-5) {  // forcing is zero: density correction is zero (SphereSTKMobMat.cpp:217)
-            done[p] = 1;
-            conv[p] = 1;
-        }
-    }
-    if (std::any_of(done.begin(), done.end(), [](char d) { return d; })) {
-        // zero the correction of finished problems
-        std::vector<unsigned char> zm(P, 0);
-        for (int p = 0; p < P; ++p) zm[p] = done[p] ? 1 : 0;
-        set_active(c, zm);
-        check_launch(c, launch_axpby_seg(L, 0.0, x, 0.0, act, x, st));
-    }
-
-    // Restart cycles in lockstep over the problems still running. FP64: each cycle is a
-    // GMRES(m) cycle on the FP64 operator, followed by the explicit residual (Belos' restart).
-    // MIXED: each cycle solves A d = r with the FP32 operator (FP64 Arnoldi/Givens) to a relative
-    // inner tolerance, x += d, and the refinement residual r = b - A x uses the FP64 operator.
-    std::vector<KrylovState> kst(P);
-    std::vector<unsigned char> hact(P);
     const long long hs = (long long)m * (m + 1);
     // one Arnoldi step: w = A V_j (A = I/2 + K + L, SphereSTKMobMat.cpp:17), CGS2 into H[:, j],
     // Givens update and the per-problem stop test on the device (problems that stop skip all
@@ -2274,167 +2326,309 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         return dx;
     };
 
-    const bool loop_graph = c->use_graphs && c->loop_graph_on && c->loop_graph_ok && !c->prof;
-    bool loop_done = false;
-    if (loop_graph) loop_done = run_loop_graph(c, LoopArgs{m, maxit, mixed, hp, cyc_prec, pc, tol, inner_tol}, step,
-                                               upd_ops, hp_residual_ops, explicit_residual_ops, cycle_update_ops, done,
-                                               conv, beta, bnorm, hp_now, hp_resid_done, x_moved, cycles, passes64,
-                                               passes32x);
-    while (!loop_done) {
-        d2h(c, kst.data(), ks, sizeof(KrylovState) * P);
-        std::vector<unsigned char> cyc(P, 0);
-        int ncyc = 0;
-        for (int p = 0; p < P; ++p) {
-            if (done[p]) continue;
-            if (beta[p] / bnorm[p] < tol && hp_now[p]) {
-                done[p] = 1;
-                conv[p] = 1;
-                continue;
-            }
-            if (kst[p].iters >= maxit || kst[p].nonfinite) {
-                done[p] = 1;
-                continue;
-            }
-            cyc[p] = 1;
-            ++ncyc;
-            cycles[p]++;
-            kst[p].tol_abs = mixed ? std::max(inner_tol * beta[p], 0.5 * tol * bnorm[p]) : tol * bnorm[p];
-            kst[p].cycle_fp32 = mixed ? 1 : 0;
-        }
-        if (ncyc == 0) break;
-        h2d(c, ks, kst.data(), sizeof(KrylovState) * P);
-        h2d(c, incyc, cyc.data(), P);
-        h2d(c, c->d_beta.p, beta.data(), sizeof(double) * P);
-        set_active(c, cyc);
-        check_launch(c, launch_scale(L, r, c->d_beta.as<double>(), 1, true, act, V, st));
-        check_launch(c, launch_cycle_init(L, m, incyc, c->d_beta.as<double>(), ks, c->d_H.as<double>(),
-                                          c->d_g.as<double>(), st));
-        // Steps run in blocks of kGraphBlock; with graphs on, each block is captured once per context
-        // (per block start, cycle precision and restart length) and replayed, and the host looks at
-        // the active flags only between blocks (steps after every problem stopped inside a block
-        // launch kernels that return at once). A profiled solve checks after every step, so each
-        // kernel it times did its full work.
-        const bool graphs = c->use_graphs && !c->prof;
-        const int blk = c->prof ? 1 : kGraphBlock;
-        for (int j0 = 0; j0 < m; j0 += blk) {
-            const int cnt = std::min(blk, m - j0);
-            if (graphs) {
-                const long long key = (((long long)cyc_prec * 2 + (pc ? 1 : 0)) * 4096 + m) * 4096 + j0;
-                auto it = c->graphs.find(key);
-                if (it == c->graphs.end()) {
-                    const long long before = c->launches;
-                    cudaGraph_t gr;
-                    CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                    c->capturing = true;
-                    try {
-                        for (int j = j0; j < j0 + cnt; ++j) step(j);
-                    } catch (...) {
-                        c->capturing = false;
-                        cudaGraph_t t = nullptr;
-                        cudaStreamEndCapture(st, &t);
-                        if (t) cudaGraphDestroy(t);
-                        cudaGetLastError();
-                        c->launches = before;
-                        throw;
-                    }
-                    c->capturing = false;
-                    CUDA_OK(cudaStreamEndCapture(st, &gr));
-                    cudaGraphExec_t ex;
-                    CUDA_OK(cudaGraphInstantiate(&ex, gr, 0));
-                    cudaGraphDestroy(gr);
-                    it = c->graphs.emplace(key, smob_ctx::Graph{ex, c->launches - before}).first;
-                    c->launches = before;
-                }
-                CUDA_OK(cudaGraphLaunch(it->second.exec, st));
-                c->launches += it->second.kernels;
-                c->host_calls += 1;
-            } else {
-                for (int j = j0; j < j0 + cnt; ++j) step(j);
-            }
-            d2h(c, hact.data(), act, P);
-            if (std::none_of(hact.begin(), hact.end(), [](unsigned char a) { return a != 0; })) break;
-        }
-        // d = V y and x += d for the problems of this cycle
-        const double* dx = cycle_update_ops();
-        // Residual, decided per problem (so a problem takes the same steps alone or in any batch).
-        // FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos' restart).
-        // MIXED, once the previous high-precision residual is below 1e-4 |b|: r <- r - A32 d, whose
-        // FP32 error ~eps32 * kappa * |r_prev| (<= ~1e-10 |b|) is far below the 1e-8 target.
-        // MIXED otherwise: one fused high-precision pass gives r = -(I/2 + K)(rho + x) - L x and the
-        // single layer u_hp = S[rho + x] (the final velocity then needs only S32[x - x_hp]).
-        std::vector<unsigned char> upd(P, 0), hpres(P, 0);
-        bool any_upd = false, any_hp = false;
-        for (int p = 0; p < P; ++p) {
-            if (!cyc[p]) continue;
-            if (mixed && hp_resid_done[p] && beta[p] <= 1e-4 * bnorm[p]) upd[p] = 1, any_upd = true;
-            else hpres[p] = 1, any_hp = true;
-        }
-        if (any_upd) {
-            set_active(c, upd);
-            upd_ops(dx);
-            for (int p = 0; p < P; ++p)
-                if (upd[p]) passes32x[p]++, x_moved[p] = 1;
-        }
-        if (any_hp && mixed) {
-            hp_residual(hpres);
-        } else if (any_hp) {
-            set_active(c, hpres);
-            explicit_residual_ops();
-            for (int p = 0; p < P; ++p)
-                if (hpres[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
-        }
-        set_active(c, cyc);
-        std::vector<double> nb = seg_norms(c, r, act);
-        for (int p = 0; p < P; ++p)
-            if (cyc[p]) beta[p] = nb[p];
-    }
-
-    // step 4: rho += mu; u = S[rho] (high precision); rigid averages / viscosity (SphereSTKMobMat.cpp:243-285).
-    // MIXED problems with a high-precision residual already hold u_hp = S[rho + x_hp]:
-    // u = u_hp + S32[x - x_hp], the FP32 part acting on the last small correction only.
-    CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
-    std::vector<unsigned char> from_hp(P, 0), moved(P, 0), fresh(P, 0);
-    bool any_from_hp = false, any_moved = false, any_fresh = false;
-    for (int p = 0; p < P; ++p) {
-        if (mixed && hp_resid_done[p]) {
-            from_hp[p] = 1, any_from_hp = true;
-            if (x_moved[p]) moved[p] = 1, any_moved = true;
-        } else {
-            fresh[p] = 1, any_fresh = true;
-        }
-    }
-    if (any_from_hp) {
-        set_active(c, from_hp);
-        check_launch(c, launch_axpby_seg(L, 1.0, uhp, 0.0, act, u, st));
-    }
-    if (any_moved) {
-        set_active(c, moved);
+    // step 4's pieces (final velocity), on the problems already marked active
+    auto post_from_hp = [&]() { check_launch(c, launch_axpby_seg(L, 1.0, uhp, 0.0, act, u, st)); };
+    auto post_moved = [&]() {
         check_launch(c, launch_axpby_seg(L, 1.0, x, 0.0, act, w, st));
         check_launch(c, launch_axpby_seg(L, -1.0, xhp, 1.0, act, w, st));
         op_apply(c, w, u, 0.0, 1.0, 0.0, 0.0, OP_FP32);
-        for (int p = 0; p < P; ++p)
-            if (moved[p]) passes32x[p]++;
+    };
+    auto post_mid = [&]() { check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, rho, st)); };
+    auto post_fresh = [&]() { op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, hp); };
+    auto post_end = [&](double* vel) {
+        check_launch(c, launch_rigid_average(c->g, u, 1.0 / c->viscosity, vel, st));
+        CUDA_OK(cudaMemcpyAsync(c->d_xlast.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    };
+    // step 1: rigid density; step 2: b = -(I/2 + K) rho. FP64 / float-float: in the solve's precision.
+    // MIXED: with the FP32 operator. b only seeds the first inner cycle and scales the tolerance; every
+    // high-precision residual is formed directly as r = -(I/2 + K)(rho + x) - L x, so b's FP32 error
+    // never reaches a residual that decides convergence.
+    auto pre_b = [&](const double* force) {
+        check_launch(c, launch_rigid_density(c->g, force, rho, st));
+        CUDA_OK(cudaMemsetAsync(b, 0, sizeof(double) * n, st));
+        op_apply(c, rho, b, -0.5, 0.0, -1.0, 0.0, mixed ? OP_FP32 : hp);
+    };
+
+    SolveOps ops;
+    ops.step = step;
+    ops.upd = upd_ops;
+    ops.hp_residual = hp_residual_ops;
+    ops.explicit_residual = explicit_residual_ops;
+    ops.cycle_update = cycle_update_ops;
+    // the cold start of the full-solve graph: steps 1-2, x = 0, r = b and the per-problem state
+    ops.pre = [&]() {
+        CUDA_OK(cudaMemsetAsync(act, 1, P, st));
+        CUDA_OK(cudaMemsetAsync(ks, 0, sizeof(KrylovState) * P, st));
+        pre_b(c->d_force.as<double>());
+        check_launch(c, launch_dots(L, b, 0, 1, b, act, c->d_bnorm.as<double>(), 1, 0, false, true, st));
+        CUDA_OK(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+        CUDA_OK(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        check_launch(c, launch_dots(L, r, 0, 1, r, act, c->d_norm.as<double>(), 1, 0, false, true, st));
+        check_launch(c, launch_track_init(P, mixed, c->d_bnorm.as<double>(), c->d_norm.as<double>(),
+                                          c->d_track.as<SolveTrack>(), st));
+    };
+    ops.post_from_hp = post_from_hp;
+    ops.post_moved = post_moved;
+    ops.post_mid = post_mid;
+    ops.post_fresh = post_fresh;
+    ops.post_end = [&]() { post_end(c->d_vel.as<double>()); };
+
+    const bool graph_path = c->use_graphs && c->loop_graph_on && c->loop_graph_ok && !c->prof;
+    const LoopArgs la{m, maxit, mixed, hp, cyc_prec, pc, tol, inner_tol};
+    std::vector<double> bnorm(P, 0.0), beta(P, 0.0);
+    std::vector<char> done(P, 0), conv(P, 0);
+    std::vector<KrylovState> kst(P);
+    bool nonfinite_any = false;
+    // A cold-start solve is one graph launch (set-up, restart loop, final velocity); the caller's
+    // force and velocity buffers are copied to and from the context's own, which the graph holds.
+    bool full_done = false;
+    if (graph_path && o->warm_start == SMOB_WARM_NONE) {
+        if (d_force != c->d_force.as<double>())
+            CUDA_OK(cudaMemcpyAsync(c->d_force.p, d_force, sizeof(double) * 6 * c->N, cudaMemcpyDeviceToDevice, st));
+        full_done = run_loop_graph(c, la, ops, true, done, conv, beta, bnorm, hp_now, hp_resid_done, x_moved, cycles,
+                                   passes64, passes32x);
+        if (full_done) {
+            if (d_vel != c->d_vel.as<double>())
+                CUDA_OK(cudaMemcpyAsync(d_vel, c->d_vel.p, sizeof(double) * 6 * c->N, cudaMemcpyDeviceToDevice, st));
+            if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            c->have_xlast = true;
+        }
     }
-    set_active(c, all);
-    check_launch(c, launch_axpby_seg(L, 1.0, x, 1.0, act, rho, st));
-    if (any_fresh) {
-        set_active(c, fresh);
-        op_apply(c, rho, u, 0.0, 1.0, 0.0, 0.0, hp);
-        for (int p = 0; p < P; ++p)
-            if (fresh[p]) passes64[p]++;
+    const bool recycle = o->warm_start == 2;
+    if (!full_done) {
         set_active(c, all);
-    }
-    check_launch(c, launch_rigid_average(c->g, u, 1.0 / c->viscosity, d_vel, st));
-    if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    CUDA_OK(cudaMemcpyAsync(c->d_xlast.p, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-    c->have_xlast = true;
-    if (recycle) {
-        std::vector<unsigned char> keep(P, 0);
-        for (int p = 0; p < P; ++p) keep[p] = conv[p] && std::isfinite(bnorm[p]) && bnorm[p] >= 1e-5 ? 1 : 0;
-        const double* parts[kRecycleParts] = {x, mixed ? r : nullptr, uhp, xhp};
-        recycle_add(c, hforce, parts, kRecycleParts, o->precision, keep);
+        std::vector<KrylovState> hks(P);
+        for (auto& k : hks) k = KrylovState{0, 0, 0, 0, 0, 0, 0};
+        h2d(c, ks, hks.data(), sizeof(KrylovState) * P);
+
+        pre_b(d_force);
+        for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
+        bnorm = seg_norms(c, b, act);
+
+        // initial guess (SphereSTKMobMat.cpp:222): warm start from the previous solution, zero, or
+        // (warm_start 2) the combination of recycled earlier solutions closest to this b
+        std::vector<double> hforce;
+        if (recycle) {
+            hforce.resize(6 * (size_t)c->N);
+            d2h(c, hforce.data(), d_force, sizeof(double) * hforce.size());
+        }
+        if (recycle && c->rk > 0) {
+            // MIXED from MIXED columns: a force in the span (to far below the tolerance) takes the
+            // combined residual, u_hp and x_hp as well, which are those of the combined solution (every
+            // part is linear in the force): no operator pass is needed to know where it stands
+            const bool state = mixed && c->rprec == SMOB_PREC_MIXED;
+            double* parts[kRecycleParts] = {x, state ? r : nullptr, state ? uhp : nullptr, state ? xhp : nullptr};
+            const std::vector<double> est = recycle_guess(c, hforce, parts, kRecycleParts);
+            std::vector<unsigned char> good(P, 0), poor(P, 0);
+            bool any_good = false, any_poor = false;
+            for (int p = 0; p < P; ++p) {
+                if (state && est[p] <= 1e-2 * tol) hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 1;
+                else if (mixed && est[p] <= kRecycleHpFirst) good[p] = 1, any_good = true;
+                else poor[p] = 1, any_poor = true;
+            }
+            if (any_poor) {
+                set_active(c, poor);
+                CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+                op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
+                check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+                check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+                for (int p = 0; p < P; ++p)
+                    if (poor[p]) (mixed ? passes32x[p] : passes64[p])++, x_moved[p] = mixed ? 1 : 0;
+            }
+            if (any_good) hp_residual(good);
+            set_active(c, all);
+        } else if (o->warm_start && c->have_xlast) {
+            CUDA_OK(cudaMemcpyAsync(x, c->d_xlast.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            CUDA_OK(cudaMemsetAsync(w, 0, sizeof(double) * n, st));
+            op_apply(c, x, w, 0.5, 0.0, 1.0, 1.0, mixed ? OP_FP32 : hp);
+            for (int p = 0; p < P; ++p) (mixed ? passes32x[p] : passes64[p])++;
+            if (mixed) std::fill(x_moved.begin(), x_moved.end(), 1);
+            check_launch(c, launch_axpby_seg(L, 1.0, b, 0.0, act, r, st));
+            check_launch(c, launch_axpby_seg(L, -1.0, w, 1.0, act, r, st));
+        } else {
+            CUDA_OK(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+            CUDA_OK(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        }
+        beta = seg_norms(c, r, act);
+        for (int p = 0; p < P; ++p) {
+            if (!std::isfinite(bnorm[p]) || !std::isfinite(beta[p])) {
+                done[p] = 1;
+                nonfinite_any = true;
+            } else if (bnorm[p] < 1e-5) {  // forcing is zero: density correction is zero (SphereSTKMobMat.cpp:217)
+                done[p] = 1;
+                conv[p] = 1;
+            }
+        }
+        if (std::any_of(done.begin(), done.end(), [](char d) { return d; })) {
+            // zero the correction of finished problems
+            std::vector<unsigned char> zm(P, 0);
+            for (int p = 0; p < P; ++p) zm[p] = done[p] ? 1 : 0;
+            set_active(c, zm);
+            check_launch(c, launch_axpby_seg(L, 0.0, x, 0.0, act, x, st));
+        }
+
+        // Restart cycles in lockstep over the problems still running. FP64: each cycle is a
+        // GMRES(m) cycle on the FP64 operator, followed by the explicit residual (Belos' restart).
+        // MIXED: each cycle solves A d = r with the FP32 operator (FP64 Arnoldi/Givens) to a relative
+        // inner tolerance, x += d, and the refinement residual r = b - A x uses the FP64 operator.
+        std::vector<unsigned char> hact(P);
+        bool loop_done = false;
+        if (graph_path)
+            loop_done = run_loop_graph(c, la, ops, false, done, conv, beta, bnorm, hp_now, hp_resid_done, x_moved, cycles,
+                                       passes64, passes32x);
+        while (!loop_done) {
+            d2h(c, kst.data(), ks, sizeof(KrylovState) * P);
+            std::vector<unsigned char> cyc(P, 0);
+            int ncyc = 0;
+            for (int p = 0; p < P; ++p) {
+                if (done[p]) continue;
+                if (beta[p] / bnorm[p] < tol && hp_now[p]) {
+                    done[p] = 1;
+                    conv[p] = 1;
+                    continue;
+                }
+                if (kst[p].iters >= maxit || kst[p].nonfinite) {
+                    done[p] = 1;
+                    continue;
+                }
+                cyc[p] = 1;
+                ++ncyc;
+                cycles[p]++;
+                kst[p].tol_abs = mixed ? std::max(inner_tol * beta[p], 0.5 * tol * bnorm[p]) : tol * bnorm[p];
+                kst[p].cycle_fp32 = mixed ? 1 : 0;
+            }
+            if (ncyc == 0) break;
+            h2d(c, ks, kst.data(), sizeof(KrylovState) * P);
+            h2d(c, incyc, cyc.data(), P);
+            h2d(c, c->d_beta.p, beta.data(), sizeof(double) * P);
+            set_active(c, cyc);
+            check_launch(c, launch_scale(L, r, c->d_beta.as<double>(), 1, true, act, V, st));
+            check_launch(c, launch_cycle_init(L, m, incyc, c->d_beta.as<double>(), ks, c->d_H.as<double>(),
+                                              c->d_g.as<double>(), st));
+            // Steps run in blocks of kGraphBlock; with graphs on, each block is captured once per context
+            // (per block start, cycle precision and restart length) and replayed, and the host looks at
+            // the active flags only between blocks (steps after every problem stopped inside a block
+            // launch kernels that return at once). A profiled solve checks after every step, so each
+            // kernel it times did its full work.
+            const bool graphs = c->use_graphs && !c->prof;
+            const int blk = c->prof ? 1 : kGraphBlock;
+            for (int j0 = 0; j0 < m; j0 += blk) {
+                const int cnt = std::min(blk, m - j0);
+                if (graphs) {
+                    const long long key = (((long long)cyc_prec * 2 + (pc ? 1 : 0)) * 4096 + m) * 4096 + j0;
+                    auto it = c->graphs.find(key);
+                    if (it == c->graphs.end()) {
+                        const long long before = c->launches;
+                        cudaGraph_t gr;
+                        CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                        c->capturing = true;
+                        try {
+                            for (int j = j0; j < j0 + cnt; ++j) step(j);
+                        } catch (...) {
+                            c->capturing = false;
+                            cudaGraph_t t = nullptr;
+                            cudaStreamEndCapture(st, &t);
+                            if (t) cudaGraphDestroy(t);
+                            cudaGetLastError();
+                            c->launches = before;
+                            throw;
+                        }
+                        c->capturing = false;
+                        CUDA_OK(cudaStreamEndCapture(st, &gr));
+                        cudaGraphExec_t ex;
+                        CUDA_OK(cudaGraphInstantiate(&ex, gr, 0));
+                        cudaGraphDestroy(gr);
+                        it = c->graphs.emplace(key, smob_ctx::Graph{ex, c->launches - before}).first;
+                        c->launches = before;
+                    }
+                    CUDA_OK(cudaGraphLaunch(it->second.exec, st));
+                    c->launches += it->second.kernels;
+                    c->host_calls += 1;
+                } else {
+                    for (int j = j0; j < j0 + cnt; ++j) step(j);
+                }
+                d2h(c, hact.data(), act, P);
+                if (std::none_of(hact.begin(), hact.end(), [](unsigned char a) { return a != 0; })) break;
+            }
+            // d = V y and x += d for the problems of this cycle
+            const double* dx = cycle_update_ops();
+            // Residual, decided per problem (so a problem takes the same steps alone or in any batch).
+            // FP64 / float-float solves: explicit r = b - A x with the cycle's operator (Belos' restart).
+            // MIXED, once the previous high-precision residual is below 1e-4 |b|: r <- r - A32 d, whose
+            // FP32 error ~eps32 * kappa * |r_prev| (<= ~1e-10 |b|) is far below the 1e-8 target.
+            // MIXED otherwise: one fused high-precision pass gives r = -(I/2 + K)(rho + x) - L x and the
+            // single layer u_hp = S[rho + x] (the final velocity then needs only S32[x - x_hp]).
+            std::vector<unsigned char> upd(P, 0), hpres(P, 0);
+            bool any_upd = false, any_hp = false;
+            for (int p = 0; p < P; ++p) {
+                if (!cyc[p]) continue;
+                if (mixed && hp_resid_done[p] && beta[p] <= 1e-4 * bnorm[p]) upd[p] = 1, any_upd = true;
+                else hpres[p] = 1, any_hp = true;
+            }
+            if (any_upd) {
+                set_active(c, upd);
+                upd_ops(dx);
+                for (int p = 0; p < P; ++p)
+                    if (upd[p]) passes32x[p]++, x_moved[p] = 1;
+            }
+            if (any_hp && mixed) {
+                hp_residual(hpres);
+            } else if (any_hp) {
+                set_active(c, hpres);
+                explicit_residual_ops();
+                for (int p = 0; p < P; ++p)
+                    if (hpres[p]) passes64[p]++, hp_resid_done[p] = 1, hp_now[p] = 1, x_moved[p] = 0;
+            }
+            set_active(c, cyc);
+            std::vector<double> nb = seg_norms(c, r, act);
+            for (int p = 0; p < P; ++p)
+                if (cyc[p]) beta[p] = nb[p];
+        }
+
+        // step 4: rho += mu; u = S[rho] (high precision); rigid averages / viscosity (SphereSTKMobMat.cpp:243-285).
+        // MIXED problems with a high-precision residual already hold u_hp = S[rho + x_hp]:
+        // u = u_hp + S32[x - x_hp], the FP32 part acting on the last small correction only.
+        CUDA_OK(cudaMemsetAsync(u, 0, sizeof(double) * n, st));
+        std::vector<unsigned char> from_hp(P, 0), moved(P, 0), fresh(P, 0);
+        bool any_from_hp = false, any_moved = false, any_fresh = false;
+        for (int p = 0; p < P; ++p) {
+            if (mixed && hp_resid_done[p]) {
+                from_hp[p] = 1, any_from_hp = true;
+                if (x_moved[p]) moved[p] = 1, any_moved = true;
+            } else {
+                fresh[p] = 1, any_fresh = true;
+            }
+        }
+        if (any_from_hp) {
+            set_active(c, from_hp);
+            post_from_hp();
+        }
+        if (any_moved) {
+            set_active(c, moved);
+            post_moved();
+            for (int p = 0; p < P; ++p)
+                if (moved[p]) passes32x[p]++;
+        }
         set_active(c, all);
-    }
+        post_mid();
+        if (any_fresh) {
+            set_active(c, fresh);
+            post_fresh();
+            for (int p = 0; p < P; ++p)
+                if (fresh[p]) passes64[p]++;
+            set_active(c, all);
+        }
+        post_end(d_vel);
+        if (d_density) CUDA_OK(cudaMemcpyAsync(d_density, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        c->have_xlast = true;
+        if (recycle) {
+            std::vector<unsigned char> keep(P, 0);
+            for (int p = 0; p < P; ++p) keep[p] = conv[p] && std::isfinite(bnorm[p]) && bnorm[p] >= 1e-5 ? 1 : 0;
+            const double* parts[kRecycleParts] = {x, mixed ? r : nullptr, uhp, xhp};
+            recycle_add(c, hforce, parts, kRecycleParts, o->precision, keep);
+            set_active(c, all);
+        }
+    }  // regular path
     auto* kst_s = static_cast<KrylovState*>(stage_alloc(c, sizeof(KrylovState) * P));
     auto* err_s = static_cast<int*>(stage_alloc(c, sizeof(int)));
     CUDA_OK(cudaMemcpyAsync(kst_s, ks, sizeof(KrylovState) * P, cudaMemcpyDeviceToHost, st));
@@ -3325,19 +3519,10 @@ smob_status smob_set_far_compression(smob_ctx* c, double eps, double eps_hp) {
     return guarded([&]() -> smob_status {
         need(c != nullptr, "null context");
         need(std::isfinite(eps) && eps < 1e-3, "far-field tolerance must be below 1e-3 (<= 0: off)");
-        need(std::isfinite(eps_hp) && eps_hp < 1e-9, "float-float far-field tolerance must be below 1e-9 (<= 0: off)");
+        need(std::isfinite(eps_hp) && eps_hp <= 1e-9, "float-float far-field tolerance must be at most 1e-9 (<= 0: off)");
         CtxScope ctx_scope(c);
-        AllocStreamScope as(c->st);
-        c->drop_graphs();  // captured blocks hold the old coarse tables
-        for (auto& kv : c->multi) smob_destroy(kv.second);  // several-RHS copies follow the new tolerance
-        c->multi.clear();
-        c->c32.eps = eps > 0 ? eps : 0.0;
-        c->chp.eps = eps_hp > 0 ? eps_hp : 0.0;
-        c->rk = 0;  // recycled residuals belong to the old operators
-        build_coarse(c);
-        bind_geom(c);
-        coarse_grids(c);
-        CUDA_OK(cudaStreamSynchronize(c->st));
+        c->eps_hp_auto = false;  // the caller's choice from now on
+        rebuild_far_sets(c, eps, eps_hp);
         return SMOB_OK;
     });
 }
@@ -3473,6 +3658,26 @@ smob_status smob_far_pairs_set(const smob_ctx* c, int hp, long long* direct, lon
         if (direct) *direct = dir;
         if (evaluated) *evaluated = ev;
         if (coarse_macs) *coarse_macs = macs;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_warm_orders(const int* orders, int n_orders) {
+    return guarded([&]() -> smob_status {
+        need(orders != nullptr || n_orders == 0, "null orders");
+        for (int i = 0; i < n_orders; ++i)
+            need(orders[i] >= 1 && orders[i] <= kMaxOrder, "orders must lie in 1..32");
+        for (int i = 0; i < n_orders; ++i) {
+            const int p = orders[i];
+            host_tables(p);
+            near_map(p, true);
+            near_map(p, false);
+            for (int pe : kCoarseLadder) {
+                if (pe >= p) break;
+                coarse_map(p, pe);
+                coarse_map_d(p, pe);
+            }
+        }
         return SMOB_OK;
     });
 }

@@ -275,6 +275,63 @@ __global__ void k_resid_decide(int P, const SolveTrack* __restrict__ t, SolvePar
     }
 }
 
+__global__ void k_track_init(int P, int mixed, const double* __restrict__ bnorm, const double* __restrict__ rnorm,
+                             SolveTrack* __restrict__ t) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    SolveTrack tr;
+    tr.bnorm = bnorm[p];
+    tr.beta = rnorm[p];
+    tr.done = 0;
+    tr.conv = 0;
+    if (!isfinite(tr.bnorm) || !isfinite(tr.beta)) {
+        tr.done = 1;
+    } else if (tr.bnorm < 1e-5) {  // forcing is zero: density correction is zero (SphereSTKMobMat.cpp:217)
+        tr.done = 1;
+        tr.conv = 1;
+    }
+    tr.hp_now = mixed ? 0 : 1;
+    tr.hp_done = 0;
+    tr.x_moved = 0;
+    tr.cycles = 0;
+    tr.passes64 = mixed ? 0 : 1;
+    tr.passes32x = mixed ? 1 : 0;
+    t[p] = tr;
+}
+
+__global__ void k_final_decide(int P, SolveTrack* __restrict__ t, SolveParams* __restrict__ sp,
+                               unsigned char* __restrict__ from_hp, unsigned char* __restrict__ moved,
+                               unsigned char* __restrict__ fresh, cudaGraphConditionalHandle h_from,
+                               cudaGraphConditionalHandle h_moved, cudaGraphConditionalHandle h_fresh) {
+    const int mixed = sp->mixed;
+    int any_f = 0, any_m = 0, any_r = 0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        SolveTrack& tr = t[p];
+        const unsigned char f = (mixed && tr.hp_done) ? 1 : 0;
+        const unsigned char mv = (f && tr.x_moved) ? 1 : 0;
+        const unsigned char fr = f ? 0 : 1;
+        if (mv) tr.passes32x += 1;
+        if (fr) tr.passes64 += 1;
+        from_hp[p] = f;
+        moved[p] = mv;
+        fresh[p] = fr;
+        any_f |= f;
+        any_m |= mv;
+        any_r |= fr;
+    }
+    any_f = __syncthreads_or(any_f);
+    any_m = __syncthreads_or(any_m);
+    any_r = __syncthreads_or(any_r);
+    if (threadIdx.x == 0) {
+        sp->fin_from = any_f ? 1 : 0;
+        sp->fin_moved = any_m ? 1 : 0;
+        sp->fin_fresh = any_r ? 1 : 0;
+        cudaGraphSetConditional(h_from, any_f ? 1u : 0u);
+        cudaGraphSetConditional(h_moved, any_m ? 1u : 0u);
+        cudaGraphSetConditional(h_fresh, any_r ? 1u : 0u);
+    }
+}
+
 __global__ void k_track_mark(int P, SolveTrack* __restrict__ t, const unsigned char* __restrict__ mask, int kind) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P || !mask[p]) return;
@@ -364,6 +421,18 @@ int launch_step_next(int P, const unsigned char* active, int* jdev, int* runs_j,
 int launch_resid_decide(int P, const SolveTrack* t, SolveParams* sp, const unsigned char* in_cycle, unsigned char* upd,
                         unsigned char* hpm, unsigned long long h_upd, unsigned long long h_hp, cudaStream_t st) {
     k_resid_decide<<<1, kCtlThreads, 0, st>>>(P, t, sp, in_cycle, upd, hpm, h_upd, h_hp);
+    return 1;
+}
+
+int launch_track_init(int P, bool mixed, const double* bnorm, const double* rnorm, SolveTrack* t, cudaStream_t st) {
+    k_track_init<<<(P + 127) / 128, 128, 0, st>>>(P, mixed ? 1 : 0, bnorm, rnorm, t);
+    return 1;
+}
+
+int launch_final_decide(int P, SolveTrack* t, SolveParams* sp, unsigned char* from_hp, unsigned char* moved,
+                        unsigned char* fresh, unsigned long long h_from, unsigned long long h_moved,
+                        unsigned long long h_fresh, cudaStream_t st) {
+    k_final_decide<<<1, kCtlThreads, 0, st>>>(P, t, sp, from_hp, moved, fresh, h_from, h_moved, h_fresh);
     return 1;
 }
 

@@ -76,6 +76,8 @@ struct SolveParams {
                      // iteration at least, so more than the iteration limit means a broken loop
     int cycles_run, upd_run, hp_run;
     int overrun;     // set when the bound stopped the loop (the solve's results are void)
+    int fin_from, fin_moved, fin_fresh;  // full-solve graph: final-velocity bodies run
+    int pad;
 };
 
 // next cycle: (merge) beta of the problems of the cycle that ended = norm; then per problem: stop
@@ -97,5 +99,14 @@ int launch_resid_decide(int P, const SolveTrack* t, SolveParams* sp, const unsig
                         unsigned char* hpm, unsigned long long h_upd, unsigned long long h_hp, cudaStream_t st);
 // bookkeeping of a residual pass on the problems in mask: kind 0 FP32 update, kind 1 high precision
 int launch_track_mark(int P, SolveTrack* t, const unsigned char* mask, int kind, cudaStream_t st);
+// cold start of the full-solve graph: the per-problem state from |b| and |r| (non-finite: stopped;
+// |b| < 1e-5: converged, zero correction), the set-up pass counted in the solve's precision
+int launch_track_init(int P, bool mixed, const double* bnorm, const double* rnorm, SolveTrack* t, cudaStream_t st);
+// final velocity of the full-solve graph: per problem u from u_hp (MIXED with a high-precision
+// residual; plus the FP32 single layer of x - x_hp where x moved since) or a fresh high-precision
+// single-layer pass; masks and if-handles, pass counts
+int launch_final_decide(int P, SolveTrack* t, SolveParams* sp, unsigned char* from_hp, unsigned char* moved,
+                        unsigned char* fresh, unsigned long long h_from, unsigned long long h_moved,
+                        unsigned long long h_fresh, cudaStream_t st);
 
 }  // namespace smob

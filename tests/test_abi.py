@@ -73,6 +73,8 @@ def test_structures_match_header():
     assert ctypes.sizeof(N.Geometry) == 56
     assert ctypes.sizeof(N.SolveOpts) == 40
     assert ctypes.sizeof(N.ProblemStats) == 40
+    assert ctypes.sizeof(N.ServerOpts) == 48  # ... inner_tol, graphs (+4 padding)
+    assert ctypes.sizeof(N.RequestInfo) == 96  # ... stats, t_ctx, route (+4 padding)
 
 
 def test_warm_start_codes():
@@ -92,3 +94,12 @@ def test_warm_start_codes():
     k = ctypes.c_int()
     assert L.smob_recycle_info(None, ctypes.byref(k), None) == N.SMOB_ERR_ARG
     assert L.smob_recycle_clear(None) == N.SMOB_ERR_ARG
+
+
+def test_warm_orders_is_host_only():
+    """smob_warm_orders builds the per-order host tables without a device and checks its orders."""
+    from spheresimulator_gb300 import SmobError, warm_orders
+    warm_orders([8, 12])
+    warm_orders([])
+    with pytest.raises(SmobError):
+        warm_orders([33])

@@ -43,9 +43,11 @@ def test_float_float_far_field_with_coarse_sources():
     c = _spread(seed=9, n=24, p=12, box=26.0)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
     eps_hp, pts, ent = g.far_compression_info(hp=True)
-    assert eps_hp == 1e-10 and ent > 0 and pts > 0
+    assert eps_hp == 1e-9 and ent > 0 and pts > 0  # the default set
     x = np.random.default_rng(9).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
+    assert _rel(g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT), fp64) < 1e-9
+    g.set_far_compression(1e-5, 1e-10)  # the bounds below are those of a 1e-10 set
     comp = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
     g.set_far_compression(1e-7, 0)
     assert g.far_compression_info(hp=True)[1:] == (0, 0)
@@ -207,6 +209,7 @@ def test_float_float_coarse_targets():
     targets and the FP64 sum, and a mixed solve against the FP64 solve."""
     c = _spread(seed=35, n=16, p=16, box=60.0)
     g = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
+    g.set_far_compression(1e-5, 1e-10)
     x = np.random.default_rng(35).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
     on = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FLOAT_FLOAT)
