@@ -700,8 +700,11 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_rep(DevGeom g, const FarI
 // 128 / w slices of w threads: thread (node, slice) takes every (128 / w)-th staged pair of source
 // points, so small entries keep every thread busy. A thread's target sits duplicated in both FP32x2
 // lanes and the sources are staged two to a pack, (x1,x2,y1,y2) (z1,z2,fx1,fx2) (fy1,fy2,fz1,fz2):
-// one packed pair_x2 evaluates two pairs (an odd tile ends with a zero-strength point 1e18 away).
-// The lanes' and slices' sums are added in a fixed order.
+// one packed pair_x2 evaluates two pairs (a candidate with an odd count ends with a zero-strength
+// point 1e18 away). Consecutive candidates share a staged tile until it holds kFarTile32 sources (a
+// candidate larger than the room left continues in the next tile), so the many small coarse levels
+// of an entry cost one pair of barriers per tile, not per candidate. The lanes' and slices' sums are
+// added in a fixed order.
 template <bool TRAC>
 __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWork* __restrict__ works,
                                                          const float4* __restrict__ src, float* __restrict__ partial) {
@@ -723,31 +726,45 @@ __global__ void __launch_bounds__(kFarThreads) k_far32_ct(DevGeom g, const CtWor
     const float2 TX = f2(P.x, P.x), TY = f2(P.y, P.y), TZ = f2(P.z, P.z);
     const float2 NX = f2(Nn.x, Nn.x), NY = f2(Nn.y, Nn.y), NZ = f2(Nn.z, Nn.z);
     float2 AX = f2(0.f, 0.f), AY = AX, AZ = AX;
-    for (int i = w.sa; i < w.sb; ++i) {
-        const int2 cc = cs.ctcand[i];  // CTA-uniform
-        if (cc.y == 0) continue;       // a boundary candidate of a neighbouring level
-        const bool coarse = cc.y < 0;
-        const float4* SP = coarse ? cs.cpos32 : g.pos32;
-        const float4* SF = coarse ? cs.csrc : src;
-        const int g0 = cc.x, gl = coarse ? -cc.y : cc.y;
-        for (int base = 0; base < gl; base += kFarTile32) {
-            const int n = min(kFarTile32, gl - base);
-            const int np = (n + 1) >> 1;
-            __syncthreads();
-            for (int k = threadIdx.x; k < np; k += kFarThreads) {
-                const int k1 = 2 * k, k2 = 2 * k + 1;
-                const float4 p1 = SP[g0 + base + k1], f1 = SF[g0 + base + k1];
-                const float4 p2 = k2 < n ? SP[g0 + base + k2] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
-                const float4 q2 = k2 < n ? SF[g0 + base + k2] : make_float4(0.f, 0.f, 0.f, 0.f);
-                sA[k] = make_float4(p1.x, p2.x, p1.y, p2.y);
-                sB[k] = make_float4(p1.z, p2.z, f1.x, q2.x);
-                sC[k] = make_float4(f1.y, q2.y, f1.z, q2.z);
+    // cursor over the candidates (CTA-uniform: every thread walks the same list): candidate i,
+    // sources [off, ...) of it not staged yet
+    int i = w.sa, off = 0;
+    while (true) {
+        __syncthreads();  // the previous tile has been read
+        int np = 0;       // packs staged in this tile
+        while (i < w.sb && np < kPk) {
+            const int2 cc = cs.ctcand[i];
+            if (cc.y == 0) {  // a boundary candidate of a neighbouring level
+                ++i;
+                continue;
             }
-            __syncthreads();
-#pragma unroll 4
-            for (int k = slice; k < np; k += nslice)
-                pair_x2<TRAC>(TX, TY, TZ, NX, NY, NZ, sA[k], sB[k], sC[k], AX, AY, AZ);
+            const bool coarse = cc.y < 0;
+            const float4* SP = coarse ? cs.cpos32 : g.pos32;
+            const float4* SF = coarse ? cs.csrc : src;
+            const int g0 = cc.x + off, gl = coarse ? -cc.y : cc.y;
+            const int n = min(gl - off, 2 * (kPk - np));  // odd only at the candidate's end
+            const int npk = (n + 1) >> 1;
+            for (int k = threadIdx.x; k < npk; k += kFarThreads) {
+                const int k1 = 2 * k, k2 = 2 * k + 1;
+                const float4 p1 = SP[g0 + k1], f1 = SF[g0 + k1];
+                const float4 p2 = k2 < n ? SP[g0 + k2] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+                const float4 q2 = k2 < n ? SF[g0 + k2] : make_float4(0.f, 0.f, 0.f, 0.f);
+                sA[np + k] = make_float4(p1.x, p2.x, p1.y, p2.y);
+                sB[np + k] = make_float4(p1.z, p2.z, f1.x, q2.x);
+                sC[np + k] = make_float4(f1.y, q2.y, f1.z, q2.z);
+            }
+            np += npk;
+            off += n;
+            if (off >= gl) {
+                ++i;
+                off = 0;
+            }
         }
+        if (np == 0) break;
+        __syncthreads();
+#pragma unroll 4
+        for (int k = slice; k < np; k += nslice)
+            pair_x2<TRAC>(TX, TY, TZ, NX, NY, NZ, sA[k], sB[k], sC[k], AX, AY, AZ);
     }
     red[0][threadIdx.x] = AX.x + AX.y;
     red[1][threadIdx.x] = AY.x + AY.y;
