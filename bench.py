@@ -266,7 +266,16 @@ def run_native(args, world, rank, local, dist):
     solve_dev(PREC_MIXED)
     prof_sph_alt = mob.profile_table()
     mob.set_sphere_tc(sph_tc0)
+    coarse_tc0 = mob.coarse_tc()
+    mob.set_coarse_tc(not coarse_tc0)
+    mob.profile_reset()
+    solve_dev(PREC_MIXED)
+    prof_coarse_alt = mob.profile_table()
     mob.profile(False)
+    # and timed solves with the other coarse-strength kernel
+    timed(PREC_MIXED, 2)
+    ms_coarse_alt, _ = timed(PREC_MIXED, max(3, min(args.steps, 10)))
+    mob.set_coarse_tc(coarse_tc0)
     f32, f64 = ctypes.c_double(), ctypes.c_double()
     N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
     tpt, tms, tcache = ctypes.c_int(), (ctypes.c_double * 3)(), ctypes.c_int()
@@ -402,10 +411,14 @@ def run_native(args, world, rank, local, dist):
                                           round((prof_near_alt if near_tc0 else prof).get("near_eval_trac", (0, 0.0))[1], 4)],
             "sphere_self_ms_tc_simt": [round((prof if sph_tc0 else prof_sph_alt).get("sphere_self", (0, 0.0))[1], 4),
                                        round((prof_sph_alt if sph_tc0 else prof).get("sphere_self", (0, 0.0))[1], 4)],
-            "default_near_tc": near_tc0, "default_sphere_tc": sph_tc0,
+            "far_coarse_ms_tc_simt": [round((prof if coarse_tc0 else prof_coarse_alt).get("far_coarse", (0, 0.0))[1], 4),
+                                      round((prof_coarse_alt if coarse_tc0 else prof).get("far_coarse", (0, 0.0))[1], 4)],
+            "solves_per_s_other_coarse_kernel": round(1e3 / float(ms_coarse_alt.mean()), 3),
+            "default_near_tc": near_tc0, "default_sphere_tc": sph_tc0, "default_coarse_tc": coarse_tc0,
             "note": "per profiled mixed solve (serialised CUDA-event times), tcgen05 kernels vs SIMT kernels: the "
-                    "FP32 near-field contraction as a TF32 GEMM (k_near_eval_tc) and the FP32 sphere operator "
-                    "with its Legendre stage as TF32 GEMMs (k_legendre_tc), 3xTF32 split"},
+                    "FP32 near-field contraction as a TF32 GEMM (k_near_eval_tc), the FP32 sphere operator "
+                    "with its Legendre stage as TF32 GEMMs (k_legendre_tc) and the FP32 coarse strengths as "
+                    "TF32 GEMMs (k_coarse_src_tc), 3xTF32 split"},
         "autotune": {"fp32_targets_per_thread": tpt.value, "variant_ms_tpt_1_2_4": [round(v, 4) for v in tms],
                      "from_cache": bool(tcache.value),
                      "note": "tile of the FP32 grid kernels, tuned when a context first runs them (here the "

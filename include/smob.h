@@ -371,6 +371,13 @@ smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* va
  * ~FP32 accuracy); 0 selects the SIMT kernel (same mathematics, FP32 multiply-adds). FP64 and
  * near-singular pairs always use the FP64 SIMT kernel. */
 smob_status smob_set_near_tc(smob_ctx* ctx, int on);
+/* The FP32 passes' coarse equivalent-source strengths (per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per
+ * sphere]) as 3xTF32 GEMMs on the tcgen05 tensor cores (1; k_coarse_src_tc: 128 coarse nodes x 16
+ * spheres per CTA) or as the SIMT FP32 GEMM (0, the default: faster and more accurate, measured on cfg2
+ * 0.88 vs 1.55 ms per solve and 4.8e-7 vs 2.3e-6 from FP64 in the far field). Each problem's strengths
+ * are the same bits alone or in a batch with either. */
+smob_status smob_set_coarse_tc(smob_ctx* ctx, int on);
+smob_status smob_coarse_tc_info(const smob_ctx* ctx, int* on);
 /* FP32 sphere operator (self terms of the FP32 passes) with the Legendre stage of its transforms on the
  * tensor cores: per order and m, the forward and inverse Legendre sums of up to 21 spheres as tcgen05
  * TF32 GEMMs (3xTF32 split), between per-sphere phi-DFT kernels (three launches per pass). Default 0:

@@ -210,8 +210,18 @@ class _Context:
         return bool(v.value)
 
     def set_sphere_tc(self, on=True):
-        """FP32 sphere operator with its Legendre stage on the tensor cores (default) or the SIMT kernel"""
+        """FP32 sphere operator with its Legendre stage on the tensor cores or the SIMT kernel (default)"""
         N.check(self._L.smob_set_sphere_tc(self._h, int(bool(on))))
+
+    def coarse_tc(self):
+        """True if the FP32 coarse strengths run on the tensor cores"""
+        v = ctypes.c_int()
+        N.check(self._L.smob_coarse_tc_info(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def set_coarse_tc(self, on=True):
+        """FP32 coarse equivalent-source strengths on the tensor cores or the SIMT GEMM (default)"""
+        N.check(self._L.smob_set_coarse_tc(self._h, int(bool(on))))
 
     def set_near_tc(self, on=True):
         """FP32 near field on the tensor cores (default) or on the SIMT pipes"""

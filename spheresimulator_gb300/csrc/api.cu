@@ -243,6 +243,9 @@ struct smob_ctx {
     DBuf d_active;
     DBuf d_err;            // device error word (DevGeom::err)
     bool near_tc = true;   // FP32 near field on the tensor cores
+    // FP32 coarse strengths on the tensor cores (k_coarse_src_tc); off: measured slower and less
+    // accurate than the SIMT GEMM (cfg2: 1.55 vs 0.88 ms per solve, 2.3e-6 vs 4.8e-7 from FP64)
+    bool coarse_tc = false;
     // FP32 sphere operator with the Legendre stage on the tensor cores: off by default, measured slower
     // than the single-kernel SIMT operator (three launches per pass against one; cfg2 2.1 vs 1.1 ms per
     // solve, a 64-problem batch 0.54 vs 0.21 ms per pass)
@@ -258,9 +261,9 @@ struct smob_ctx {
         std::vector<int4> clev;
         std::vector<int2> cent;
         int ncoarse = 0;
-        std::vector<int4> cdesc, cgrp;
+        std::vector<int4> cdesc, cgrp, cdesc_tc;
         std::vector<int2> gent;
-        DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent;
+        DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent, d_cdesc_tc;
         // coarse targets: listed entries with their candidate sources, work items, partial sums and
         // the interpolation side
         bool ctgt = false;
@@ -1090,6 +1093,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     // GEMM tiles of the per-pass strengths: entries grouped by map (p, pe), 8 spheres x kCoarseTileNodes
     // coarse nodes per CTA
     h.cdesc.clear();
+    h.cdesc_tc.clear();
     h.cgrp.clear();
     h.gent.clear();
     struct MapGroup {
@@ -1113,6 +1117,11 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         for (int e = 0; e < (int)mg.ents.size(); e += 8)
             for (int k0 = 0; k0 < mg.cnt; k0 += kCoarseTileNodes)
                 h.cdesc.push_back(make_int4(grp, k0, first + e, std::min(8, (int)mg.ents.size() - e)));
+        if (!h.hp)  // the tensor-core tiles of the FP32 set
+            for (int e = 0; e < (int)mg.ents.size(); e += kCoarseTcSph)
+                for (int k0 = 0; k0 < mg.cnt; k0 += kCoarseTcNodes)
+                    h.cdesc_tc.push_back(
+                        make_int4(grp, k0, first + e, std::min(kCoarseTcSph, (int)mg.ents.size() - e)));
     }
     // Coarse targets: for every sphere t and level l small enough to serve as its targets, the source
     // spheres whose pair may take that level (tgt_level on the device, in FP32 from FP32 centres:
@@ -1259,6 +1268,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.d_clev.upload(h.clev);
     h.d_cent.upload(h.cent);
     h.d_cdesc.upload(h.cdesc);
+    h.d_cdesc_tc.upload(h.cdesc_tc);
     h.d_cgrp.upload(h.cgrp);
     h.d_gent.upload(h.gent);
     if (h.hp) h.d_cmap.upload(mapsd);
@@ -1292,10 +1302,12 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         } else {
             h.d_ct_partial.alloc(sizeof(float) * (size_t)h.ct_partial);
             h.d_ctinterp.alloc(sizeof(float) * 3 * slots);
-            h.d_cmapT.upload(mapsT);
             h.d_ctu.alloc(sizeof(float4) * np);
         }
     }
+    // FP32 set: the transposed maps serve the coarse targets' interpolation and the tensor-core
+    // strength GEMM (its A operand), so they are kept with or without coarse targets
+    if (!h.hp) h.d_cmapT.upload(mapsT);
 }
 
 void build_coarse(smob_ctx* c) {
@@ -1392,6 +1404,8 @@ void bind_geom(smob_ctx* c) {
         cs.crep = c->nrep > 1 ? h.ncoarse / c->nrep : h.ncoarse;
         cs.ncdesc = (int)h.cdesc.size();
         cs.cdesc = h.d_cdesc.as<int4>();
+        cs.ncdesc_tc = (int)h.cdesc_tc.size();
+        cs.cdesc_tc = h.d_cdesc_tc.as<int4>();
         cs.cgrp = h.d_cgrp.as<int4>();
         cs.gent = h.d_gent.as<int2>();
         const bool ct = !h.ctent.empty();
@@ -1399,7 +1413,7 @@ void bind_geom(smob_ctx* c) {
         cs.ctmargin = float(kCoarseTargetMargin);
         cs.cnrm32 = ct ? h.d_cnrm32.as<float4>() : nullptr;
         cs.cnrm32lo = ct && h.hp ? h.d_cnrm32lo.as<float4>() : nullptr;
-        cs.cmapT = ct && !h.hp ? h.d_cmapT.as<float>() : nullptr;
+        cs.cmapT = !h.hp && h.d_cmapT.p ? h.d_cmapT.as<float>() : nullptr;
         cs.cmapTdf = ct && h.hp ? h.d_cmapT.as<float2>() : nullptr;
         cs.ctused = ct ? h.d_ctused.as<int>() : nullptr;
         cs.nctent = ct ? (int)h.ctent.size() : 0;
@@ -1421,6 +1435,12 @@ void bind_geom(smob_ctx* c) {
     g.sph32 = c->d_sph32.as<float4>();
 }
 
+// the FP32 coarse strengths of the current sources: tensor cores or the SIMT GEMM
+int coarse_src(smob_ctx* c, cudaStream_t st) {
+    return c->coarse_tc ? launch_coarse_src_tc(c->g, c->d_src32.as<float4>(), st)
+                        : launch_coarse_src(c->g, c->d_src32.as<float4>(), st);
+}
+
 // Tile-shape autotuner: times the FP32 traction far field with 1, 2 and 4 targets per thread on
 // this context's geometry (CUDA events, best of two) and keeps the fastest. Results are cached per
 // (largest order, size bucket of M) for the process, so contexts of similar shape reuse them.
@@ -1439,7 +1459,7 @@ void autotune_far32(smob_ctx* c) {
         CUDA_OK(cudaEventCreate(&a));
         CUDA_OK(cudaEventCreate(&b));
         CUDA_OK(cudaMemsetAsync(c->d_src32.p, 0, sizeof(float4) * c->M, c->st));
-        check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
+        check_launch(c, coarse_src(c, c->st));
         DBuf items[3];
         for (int k = 0; k < 3; ++k) items[k].upload(c->items_tpt[k]);
         auto run = [&](int k) {
@@ -1551,7 +1571,7 @@ void op_apply(smob_ctx* c, const double* x, double* out, double c_id, double c_s
             }
             if (fp32 && g.cs32.ncent > 0) {
                 ProfScope ps(c, "far_coarse", fs);
-                check_launch(c, launch_coarse_src(g, c->d_src32.as<float4>(), fs));
+                check_launch(c, coarse_src(c, fs));
             }
             if (fp32 && far_ct_on(c)) {
                 far_ct(c, tr, fs);
@@ -3131,7 +3151,7 @@ smob_status smob_far_field(smob_ctx* c, const double* in, double* out, double c_
                     check_launch(c, launch_far_pack(c->g, din, cc, c->d_src32.as<float4>(), c->d_src64.as<double4_32a>(), fp32, c->st));
                     if (fp32 && c->g.cs32.ncent > 0) {
                         ProfScope ps(c, "far_coarse");
-                        check_launch(c, launch_coarse_src(c->g, c->d_src32.as<float4>(), c->st));
+                        check_launch(c, coarse_src(c, c->st));
                     }
                     if (fp32 && far_ct_on(c)) {
                         far_ct(c, tr, c->st);
@@ -3305,6 +3325,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     r->c32.ctgt = false;      // the several-column kernels evaluate the grid targets of every far pair
     r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
     r->chp.ctgt = false;
+    r->coarse_tc = c->coarse_tc;
     r->near_tc = c->near_tc;  // the same near and sphere kernels as the single solves (results equal column
     r->sph_tc = c->sph_tc;    // by column)
     CUDA_OK(cudaSetDevice(c->device));
@@ -3714,6 +3735,26 @@ smob_status smob_set_near_tc(smob_ctx* c, int on) {
         // the tile padding must read as zero again after the SIMT layout used the buffer
         CUDA_OK(cudaMemsetAsync(c->d_sets32.p, 0, c->d_sets32.bytes, c->st));
         CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_coarse_tc(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        CtxScope ctx_scope(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        c->drop_graphs();  // captured passes hold the other kernel
+        for (auto& kv : c->multi) smob_set_coarse_tc(kv.second, on);
+        c->coarse_tc = on != 0;
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_coarse_tc_info(const smob_ctx* c, int* on) {
+    return guarded([&]() -> smob_status {
+        need(c && on, "null argument");
+        *on = c->coarse_tc ? 1 : 0;
         return SMOB_OK;
     });
 }

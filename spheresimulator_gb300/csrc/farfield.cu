@@ -23,6 +23,7 @@
 // fixed order, so results do not depend on scheduling or on other problems in the batch.
 #include "smob_internal.h"
 #include "df.h"
+#include "tc_sm100.h"
 
 namespace smob {
 
@@ -277,6 +278,160 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
             const int k = k0 + ni + 16 * i;
             if (k < cnt) cs.csrc[sout[si] + k] = make_float4(acc[i][0], acc[i][1], acc[i][2], 0.f);
         }
+    }
+}
+
+// The FP32 set's strengths on the tcgen05 tensor cores: per (p, pe) map the GEMM
+//   D [128 coarse nodes x 48] = A [128 x N_g] . B [48 x N_g]^T,
+// A = the transposed map's rows (coarse node k: its N_g fine-node weights), B = the sources of 16
+// spheres, one row per (sphere, component). K runs over the fine nodes in chunks of 32 TF32 values:
+// the threads stage both operands split into TF32 high and low parts (3xTF32: hi.hi + hi.lo + lo.hi,
+// about FP32 accuracy), one thread issues the chunk's 12 MMAs, commits them to an mbarrier and waits
+// (bounded); D stays in tensor memory over the chunks (48 of 64 allocated columns). Each thread then
+// loads its row (coarse node) and writes the 16 spheres' strengths. Every D element is the same sum
+// whichever spheres share its tile, so a problem's strengths do not depend on the batch.
+constexpr int kCsTcSph = kCoarseTcSph, kCsTcN = 3 * kCsTcSph, kCsTcK = 32;
+static_assert(kCoarseTcNodes == 128, "one M = 128 MMA tile per CTA");
+constexpr int kCsTcABytes = 128 * kCsTcK * 4, kCsTcBBytes = kCsTcN * kCsTcK * 4;
+constexpr int kCsTcSmem = 2 * kCsTcABytes + 2 * kCsTcBBytes;  // A hi, A lo, B hi, B lo: 44 KB
+constexpr long long kCsTcWaitPolls = 1LL << 22;
+__global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* __restrict__ src) {
+    const CoarseSet& cs = g.cs32;
+    const int4 d = cs.cdesc_tc[blockIdx.x];
+    const int4 G = cs.cgrp[d.x];
+    const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
+    extern __shared__ __align__(1024) unsigned char cs_smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    __shared__ int s_fail;
+    __shared__ int sbase[kCsTcSph], sout[kCsTcSph];
+    __shared__ unsigned char sact[kCsTcSph];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid < kCsTcSph) {
+        int sb = 0, so = 0;
+        unsigned char a = 0;
+        if (tid < ne) {
+            const int2 e = cs.gent[d.z + tid];
+            sb = g.gidx[e.x];
+            so = e.y;
+            a = (g.active && !g.active[g.prob[e.x]]) ? 0 : 1;
+        }
+        sbase[tid] = sb;
+        sout[tid] = so;
+        sact[tid] = a;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, 64);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+        s_fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, kCsTcN);
+    unsigned char* sAh = cs_smem;
+    unsigned char* sAl = cs_smem + kCsTcABytes;
+    unsigned char* sBh = cs_smem + 2 * kCsTcABytes;
+    unsigned char* sBl = sBh + kCsTcBBytes;
+    const float* __restrict__ mapT = cs.cmapT + G.x;  // [coarse node][fine node]
+    const int krow = k0 + tid;                       // this thread's A row (coarse node)
+    const bool rvalid = krow < cnt;
+    const int nck = (ng + kCsTcK - 1) / kCsTcK;
+    unsigned phase = 0;
+    bool failed = false;
+    for (int ch = 0; ch < nck; ++ch) {
+        const int j0 = ch * kCsTcK;
+        // A: row tid, 32 fine nodes
+#pragma unroll
+        for (int q = 0; q < kCsTcK / 4; ++q) {
+            float v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int j = j0 + 4 * q + e;
+                v[e] = (rvalid && j < ng) ? __ldg(mapT + (long long)krow * ng + j) : 0.f;
+            }
+            float4 h, l;
+            tc::tf32_split(v[0], h.x, l.x);
+            tc::tf32_split(v[1], h.y, l.y);
+            tc::tf32_split(v[2], h.z, l.z);
+            tc::tf32_split(v[3], h.w, l.w);
+            const uint32_t off = tc::kmajor_offset(tid, 4 * q, kCsTcK);
+            *reinterpret_cast<float4*>(sAh + off) = h;
+            *reinterpret_cast<float4*>(sAl + off) = l;
+        }
+        // B: rows 3 s + c (sphere s of the tile, component c), 32 fine nodes
+        for (int v = tid; v < kCsTcSph * kCsTcK; v += 128) {
+            const int si = v / kCsTcK, jj = v % kCsTcK, j = j0 + jj;
+            const float4 f = (si < ne && j < ng) ? src[sbase[si] + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float fc[3] = {f.x, f.y, f.z};
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                float h, l;
+                tc::tf32_split(fc[cc], h, l);
+                const uint32_t off = tc::kmajor_offset(3 * si + cc, jj, kCsTcK);
+                *reinterpret_cast<float*>(sBh + off) = h;
+                *reinterpret_cast<float*>(sBl + off) = l;
+            }
+        }
+        tc::fence_smem_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t ah0 = tc::smem_u32(sAh), al0 = tc::smem_u32(sAl);
+            const uint32_t bh0 = tc::smem_u32(sBh), bl0 = tc::smem_u32(sBl);
+            constexpr uint32_t sbo = (kCsTcK / 4) * 128;
+#pragma unroll
+            for (int ks = 0; ks < kCsTcK / 8; ++ks) {
+                const uint32_t o = ks * 256;
+                const uint64_t ah = tc::sdesc(ah0 + o, 128, sbo), al = tc::sdesc(al0 + o, 128, sbo);
+                const uint64_t bh = tc::sdesc(bh0 + o, 128, sbo), bl = tc::sdesc(bl0 + o, 128, sbo);
+                tc::mma_tf32(tmem, ah, bh, idesc, ch > 0 || ks > 0);
+                tc::mma_tf32(tmem, ah, bl, idesc, true);
+                tc::mma_tf32(tmem, al, bh, idesc, true);
+            }
+            tc::mma_commit(&mbar);
+            if (!tc::mbar_wait_bounded(&mbar, phase, kCsTcWaitPolls)) s_fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) {
+            failed = true;
+            break;
+        }
+    }
+    if (!failed) {
+        tc::fence_after_sync();
+        float da[32], db[32];
+        const uint32_t lane_base = uint32_t(warp * 32) << 16;
+        tc::tmem_ld_32x32b_x32(tmem + lane_base, da);       // columns 0-31
+        tc::tmem_ld_32x32b_x32(tmem + 32 + lane_base, db);  // columns 32-63 (48-63 unused)
+        if (rvalid) {
+#pragma unroll
+            for (int si = 0; si < kCsTcSph; ++si) {
+                if (si >= ne || !sact[si]) continue;
+                float o[3];
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) {
+                    const int col = 3 * si + cc;
+                    o[cc] = col < 32 ? da[col] : db[col - 32];
+                }
+                cs.csrc[sout[si] + krow] = make_float4(o[0], o[1], o[2], 0.f);
+            }
+        }
+    } else if (tid == 0 && g.err) {
+        atomicExch(g.err, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 64);
     }
 }
 
@@ -1507,6 +1662,12 @@ int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st) 
 int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st) {
     if (g.cs32.ncent <= 0 || g.cs32.ncdesc <= 0) return 0;
     k_coarse_src<<<g.cs32.ncdesc, 128 * kCgGroups, 0, st>>>(g, src32);
+    return 1;
+}
+
+int launch_coarse_src_tc(const DevGeom& g, const float4* src32, cudaStream_t st) {
+    if (g.cs32.ncent <= 0 || g.cs32.ncdesc_tc <= 0) return 0;
+    k_coarse_src_tc<<<g.cs32.ncdesc_tc, 128, kCsTcSmem, st>>>(g, src32);
     return 1;
 }
 

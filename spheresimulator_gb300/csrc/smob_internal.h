@@ -42,6 +42,8 @@ inline long long near_tile_stride(int pmax, bool trac) {
 }
 constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per sphere (FP32 far field)
 constexpr int kCoarseTileNodes = 32;     // coarse nodes per CTA of the coarse-strength GEMMs (multiple of 16)
+constexpr int kCoarseTcNodes = 128;      // tensor-core coarse-strength GEMM: coarse nodes (MMA rows) per CTA
+constexpr int kCoarseTcSph = 16;         // and spheres per CTA (three MMA columns each)
 // interpolation tiles of the coarse targets (the host lists at most this many entries per tile; the
 // kernels k_ct_interp / k_ct_interp_df read exactly these): FP32 set 2 entries x 128 grid points,
 // float-float set 1 entry x 256 grid points (two per thread)
@@ -96,6 +98,9 @@ struct CoarseSet {
     const int4* cdesc;         // [ncdesc] {group, first coarse node, first entry in gent, entries (<= 8)}
     const int4* cgrp;          // per group {map offset, fine nodes N_g(p), coarse nodes N_e(pe), 0}
     const int2* gent;          // entries grouped by map: {sphere, first coarse point of that sphere's level}
+    // the same GEMMs on the tensor cores (FP32 set): tiles of 128 coarse nodes x 16 spheres
+    int ncdesc_tc;
+    const int4* cdesc_tc;      // [ncdesc_tc] {group, first coarse node, first entry in gent, entries (<= 16)}
     // Coarse targets: a target sphere t takes the far field of a well-separated source sphere s at the
     // nodes of one of its own coarse levels and interpolates it to its grid (the transposed map);
     // level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s)) + ctmargin, if
@@ -226,6 +231,9 @@ int launch_far_pack(const DevGeom& g, const double* x, double c, float4* src32, 
 // coarse equivalent-source strengths of this pass from the FP32 grid sources (before every FP32
 // launch_far_field when g.ncent > 0)
 int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st);
+// the FP32 coarse strengths as 3xTF32 GEMMs on the tcgen05 tensor cores (cs32.cdesc_tc tiles); a tile
+// that gave up waiting for its MMAs sets *g.err and writes nothing
+int launch_coarse_src_tc(const DevGeom& g, const float4* src32, cudaStream_t st);
 // the float-float set's strengths (hi, lo) from the float-float grid sources of launch_far_pack_df
 int launch_coarse_src_df(const DevGeom& g, const float4* src2, cudaStream_t st);
 // tpt: FP32 targets per thread (1, 2 or 4); FP32 items must cover kFarThreads * tpt targets
