@@ -966,6 +966,22 @@ def near_once():
                       "rel_diff_legendre_tc_fp64": float(np.linalg.norm(d - b) / np.linalg.norm(b))}))
 
 
+def coarse_once():
+    """One FP32 far-field pass with the coarse strengths on the tensor cores, then one with the SIMT
+    GEMM, on the first 64 problems of cfg4 (the batched shape, many spheres per coarse map)."""
+    from spheresimulator_gb300 import PREC_FP64, PREC_MIXED, SphereSTKSHOperator, configs
+    c = configs.cfg4(n_problems=64)
+    g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"], problem=c["problem"])
+    x = np.random.default_rng(0).standard_normal(3 * g.n_points)
+    g.set_coarse_tc(True)
+    a = g.far_field(x, cSL=0.0, cTrac=1.0, precision=PREC_MIXED)
+    g.set_coarse_tc(False)
+    b = g.far_field(x, cSL=0.0, cTrac=1.0, precision=PREC_MIXED)
+    print(json.dumps({"coarse_once": "cfg4[:64]", "points": int(g.n_points),
+                      "coarse_points": int(g.far_compression_info()[1]),
+                      "rel_diff_tc_simt": float(np.linalg.norm(a - b) / np.linalg.norm(b))}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1005,6 +1021,8 @@ def main():
     ap.add_argument("--far-once", action="store_true",
                     help="cfg2: one far-field pass per kernel family (FP32 traction, fused float-float "
                          "traction + single layer, FP64 traction) and exit; a short program for ncu captures")
+    ap.add_argument("--coarse-once", action="store_true",
+                    help="one FP32 far-field pass with tensor-core and with SIMT coarse strengths (for ncu)")
     ap.add_argument("--host-loop", action="store_true",
                     help="with --solve-once: the host-driven restart loop instead of the loop graph")
     ap.add_argument("--solve-once", action="store_true",
@@ -1020,6 +1038,9 @@ def main():
         return
     if args.solve_once:
         solve_once(args.host_loop)
+        return
+    if args.coarse_once:
+        coarse_once()
         return
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3

@@ -1138,7 +1138,11 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     std::vector<double> work_cost;
     h.ctused.assign((size_t)std::max(N, 1) * kCoarseLevels, 0);
     h.ct_partial = 0;
-    if (h.ctgt && !h.cent.empty()) {
+    // Built whenever coarse targets are on and the set compresses (eps > 0), also when no sphere of the
+    // context has a coarse level (the grid entries alone): which far-field kernel runs must not depend on
+    // the data, or a problem would take another kernel (and other bits) alone than in a batch whose
+    // other problems have well-separated pairs.
+    if (h.ctgt && h.eps > 0) {
         const double leps = std::log(h.eps);
         auto dist = [&](int t, int s) {
             double d2 = 0;

@@ -254,3 +254,26 @@ def test_coarse_strengths_on_tensor_cores():
     alone.set_coarse_tc(True)
     v = both.solveMob(F, tol=1e-8, precision=PREC_MIXED)
     assert np.array_equal(alone.solveMob(F[:240], tol=1e-8, precision=PREC_MIXED), v[:240])
+
+
+def test_batch_of_compressed_and_uncompressed_problems():
+    """A problem without well-separated pairs (no coarse level anywhere) batched with one that has
+    them: it is solved alone and in the batch with the same far-field kernels and gives the same bits
+    (the coarse-target machinery is built whenever it is on, whatever the data)."""
+    # three spheres whose pairs are all far pairs (centres 3.2 and 4.5 apart, beyond 1.5 (a_s + a_t))
+    # but too close for any coarse order below p = 8
+    tight = dict(centers=np.array([[0.0, 0.0, 0.0], [3.2, 0.0, 0.0], [0.0, 3.2, 0.0]]), radii=np.ones(3),
+                 orders=np.full(3, 8))
+    far = _spread(seed=62, n=16, p=12, box=36.0)
+    alone = SphereSTKMobMat(tight["centers"], tight["radii"], tight["orders"])
+    assert alone.far_compression_info()[2] == 0  # no coarse entry
+    centers = np.vstack([tight["centers"], far["centers"] + 400.0])
+    radii = np.concatenate([tight["radii"], far["radii"]])
+    orders = np.concatenate([tight["orders"], far["orders"]])
+    prob = np.array([0] * 3 + [1] * 16, dtype=np.int32)
+    both = SphereSTKMobMat(centers, radii, orders, problem=prob)
+    assert both.far_compression_info()[2] > 0
+    F = np.random.default_rng(63).standard_normal(6 * 19)
+    for prec in (PREC_MIXED, PREC_FLOAT_FLOAT):
+        v = both.solveMob(F, tol=1e-10, precision=prec)
+        assert np.array_equal(alone.solveMob(F[:18], tol=1e-10, precision=prec), v[:18]), prec

@@ -113,3 +113,57 @@ def test_loop_graph_cuts_host_launches():
     # graph launch per 4-step block and the cycle kernels
     assert 0 < kg <= kh
     assert hg * 2 < hh and hg <= 32, counts
+
+
+def test_loop_graph_zero_and_mixed_batch_forces():
+    """A problem with zero forcing is converged at once (zero density correction,
+    BIE/SphereSTKMobMat.cpp:217) while its batch partner iterates: the device-side set-up takes the same
+    decisions as the host's."""
+    a = configs.small_cluster(seed=35, n=4, p=8, gap=0.2, quats=True)
+    b = configs.small_cluster(seed=36, n=5, p=8, gap=0.2, quats=True)
+    cfg = dict(centers=np.vstack([a["centers"], b["centers"] + 100.0]), radii=np.concatenate([a["radii"], b["radii"]]),
+               orders=np.concatenate([a["orders"], b["orders"]]), quats=np.vstack([a["quats"], b["quats"]]),
+               problem=np.array([0] * 4 + [1] * 5, dtype=np.int32))
+    F = np.concatenate([np.zeros(24), b["force"]])
+    mob = make(cfg)
+    a_, a2, sa, b_, sb = both_loops(mob, lambda: mob.solveMob(F, tol=1e-10, precision=PREC_MIXED))
+    assert_same(a_, a2, sa, b_, sb)
+    assert sa[0]["iterations"] == 0 and sa[0]["status"] == 0 and np.all(a_[:24] == 0)
+    assert sa[1]["iterations"] > 0 and sa[1]["status"] == 0
+
+
+def test_loop_graph_non_finite_force_through_device_api():
+    """Device-pointer forces are not screened on the host: a non-finite one stops its problem in the
+    set-up (device-side decision in the graph) with SMOB_ERR_NONFINITE, its batch partner converges."""
+    import ctypes
+
+    from spheresimulator_gb300 import _native as N
+    from spheresimulator_gb300 import solve_opts
+    a = configs.small_cluster(seed=37, n=4, p=8, gap=0.2, quats=True)
+    b = configs.small_cluster(seed=38, n=4, p=8, gap=0.2, quats=True)
+    cfg = dict(centers=np.vstack([a["centers"], b["centers"] + 100.0]), radii=np.concatenate([a["radii"], b["radii"]]),
+               orders=np.concatenate([a["orders"], b["orders"]]), quats=np.vstack([a["quats"], b["quats"]]),
+               problem=np.array([0] * 4 + [1] * 4, dtype=np.int32))
+    F = np.concatenate([a["force"], b["force"]])
+    F[3] = np.nan
+    mob = make(cfg)
+    L, h = N.lib(), mob.handle
+    d_f, d_v = ctypes.c_void_p(), ctypes.c_void_p()
+    N.check(L.smob_device_alloc(h, 8 * 48, ctypes.byref(d_f)))
+    N.check(L.smob_device_alloc(h, 8 * 48, ctypes.byref(d_v)))
+    try:
+        N.check(L.smob_memcpy_h2d(h, d_f, F.ctypes.data_as(ctypes.c_void_p), 8 * 48))
+        out = {}
+        for on in (True, False):
+            mob.set_loop_graph(on)
+            stats = (N.ProblemStats * 2)()
+            o = solve_opts(1e-10, 50, 500, PREC_MIXED)
+            code = L.smob_solve_mob_device(h, d_f, d_v, None, ctypes.byref(o), stats)
+            out[on] = (code, [s.as_dict() for s in stats])
+        assert out[True][0] == out[False][0] == N.SMOB_ERR_NONFINITE
+        for x, y in zip(out[True][1], out[False][1]):
+            assert x["status"] == y["status"] and x["iterations"] == y["iterations"]
+        assert out[True][1][0]["status"] == N.SMOB_ERR_NONFINITE and out[True][1][1]["status"] == 0
+    finally:
+        L.smob_device_free(h, d_f)
+        L.smob_device_free(h, d_v)
