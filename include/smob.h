@@ -219,7 +219,7 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
  * it for the FP32 operator passes (SMOB_PREC_MIXED inner solves and final velocity correction; default
  * 1e-5), eps_hp for the float-float passes (the MIXED refinement residuals and high-precision single
  * layer, SMOB_PREC_FLOAT_FLOAT; at most 1e-9). By default eps_hp follows the solves: 1e-9 at creation,
- * tightened once to a tenth of a solve's tolerance, but not below 1e-10, when a solve asks for less than
+ * tightened once to a tenth of a solve's tolerance (not below 1e-12) when a solve asks for less than
  * 1e-8 (both sets are rebuilt then; never loosened); once set here it stays as set. Near pairs, the own sphere and every FP64 pass keep the
  * direct sum over the grid points: the plain FP64 solve is the reference's smooth quadrature. The
  * reference evaluates this far field with an FMM (STKFMM, BIE/SphereSTKSHOperator.cpp:291-292,368-369).

@@ -25,6 +25,7 @@
 #include "krylov.h"
 #include "sh_host.h"
 #include "smob_internal.h"
+#include "tc_sm100.h"
 
 using namespace smob;
 
@@ -263,7 +264,7 @@ struct smob_ctx {
         int ncoarse = 0;
         std::vector<int4> cdesc, cgrp, cdesc_tc;
         std::vector<int2> gent;
-        DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent, d_cdesc_tc;
+        DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent, d_cdesc_tc, d_cmapA;
         // coarse targets: listed entries with their candidate sources, work items, partial sums and
         // the interpolation side
         bool ctgt = false;
@@ -1277,6 +1278,42 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.d_gent.upload(h.gent);
     if (h.hp) h.d_cmap.upload(mapsd);
     else h.d_cmap.upload(maps);
+    if (!h.hp) {
+        // The tensor-core strength GEMM's A operand, prepared once per geometry: per map group, per M
+        // tile of 128 coarse nodes and K chunk of 32 fine nodes, the transposed map's block split into
+        // TF32 high and low parts (both rounded to nearest, ties away), each 16 KB in the MMA's K-major
+        // core-matrix order, so a CTA stages it with straight coalesced copies. cgrp.w: its offset.
+        auto tf32_rna = [](float x) {
+            uint32_t u;
+            std::memcpy(&u, &x, 4);
+            u = (u + 0x1000u) & 0xFFFFE000u;
+            float y;
+            std::memcpy(&y, &u, 4);
+            return y;
+        };
+        std::vector<float> mapA;
+        for (int4& G : h.cgrp) {
+            const int ng = G.y, cnt = G.z, nmt = (cnt + kCoarseTcNodes - 1) / kCoarseTcNodes, nck = (ng + 31) / 32;
+            G.w = (int)mapA.size();
+            mapA.resize(mapA.size() + (size_t)nmt * nck * 2 * kCoarseTcNodes * 32, 0.f);
+            for (int mt = 0; mt < nmt; ++mt)
+                for (int ch = 0; ch < nck; ++ch) {
+                    float* hi = &mapA[(size_t)G.w + (size_t)(mt * nck + ch) * 2 * kCoarseTcNodes * 32];
+                    float* lo = hi + kCoarseTcNodes * 32;
+                    for (int r = 0; r < kCoarseTcNodes; ++r)
+                        for (int k = 0; k < 32; ++k) {
+                            const int kk = mt * kCoarseTcNodes + r, j = ch * 32 + k;
+                            const float v = (kk < cnt && j < ng) ? mapsT[(size_t)G.x + (size_t)kk * ng + j] : 0.f;
+                            const float vh = tf32_rna(v);
+                            const size_t o = tc::kmajor_offset(r, k, 32) / 4;
+                            hi[o] = vh;
+                            lo[o] = tf32_rna(v - vh);
+                        }
+                }
+        }
+        h.d_cmapA.upload(mapA);
+        h.d_cgrp.upload(h.cgrp);  // with the offsets
+    }
     const size_t np = std::max(h.ncoarse, 1);
     h.d_cpos32.alloc(sizeof(float4) * np);
     if (h.hp) h.d_cpos32lo.alloc(sizeof(float4) * np);
@@ -1410,6 +1447,7 @@ void bind_geom(smob_ctx* c) {
         cs.cdesc = h.d_cdesc.as<int4>();
         cs.ncdesc_tc = (int)h.cdesc_tc.size();
         cs.cdesc_tc = h.d_cdesc_tc.as<int4>();
+        cs.cmapA = h.hp ? nullptr : h.d_cmapA.as<float4>();
         cs.cgrp = h.d_cgrp.as<int4>();
         cs.gent = h.d_gent.as<int2>();
         const bool ct = !h.ctent.empty();
@@ -2205,13 +2243,11 @@ void rebuild_far_sets(smob_ctx* c, double eps, double eps_hp) {
 }
 
 // The float-float set's tolerance follows the solves (unless the caller set it): one decade below the
-// tolerance a solve asks for, at most kCoarseEpsHpDefault (its value at creation), at least 1e-10. A
+// tolerance a solve asks for, at most kCoarseEpsHpDefault (its value at creation), at least 1e-12. A
 // solve asking for more than the set gives tightens it once (both sets rebuilt); it is never loosened.
-// (Not below 1e-10: at 1e-11 a batch's problems and the same problems alone were measured to differ in
-// the last bits, 3e-15 relative, which the batched solve must not.)
 void fit_eps_hp(smob_ctx* c, double tol) {
     if (!c->eps_hp_auto || c->chp.eps <= 0) return;
-    const double want = std::min(kCoarseEpsHpDefault, std::max(0.1 * tol, 1e-10));
+    const double want = std::min(kCoarseEpsHpDefault, std::max(0.1 * tol, 1e-12));
     if (want < c->chp.eps) rebuild_far_sets(c, c->c32.eps, want);
 }
 

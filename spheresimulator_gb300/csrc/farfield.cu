@@ -284,12 +284,13 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
 // The FP32 set's strengths on the tcgen05 tensor cores: per (p, pe) map the GEMM
 //   D [128 coarse nodes x 48] = A [128 x N_g] . B [48 x N_g]^T,
 // A = the transposed map's rows (coarse node k: its N_g fine-node weights), B = the sources of 16
-// spheres, one row per (sphere, component). K runs over the fine nodes in chunks of 32 TF32 values:
-// the threads stage both operands split into TF32 high and low parts (3xTF32: hi.hi + hi.lo + lo.hi,
-// about FP32 accuracy), one thread issues the chunk's 12 MMAs, commits them to an mbarrier and waits
-// (bounded); D stays in tensor memory over the chunks (48 of 64 allocated columns). Each thread then
-// loads its row (coarse node) and writes the 16 spheres' strengths. Every D element is the same sum
-// whichever spheres share its tile, so a problem's strengths do not depend on the batch.
+// spheres, one row per (sphere, component). K runs over the fine nodes in chunks of 32 TF32 values,
+// both operands as TF32 high and low parts (3xTF32: hi.hi + hi.lo + lo.hi, about FP32 accuracy): A is
+// copied from its pre-split tiles (cs.cmapA, coalesced float4 loads), B gathered and split by the
+// threads. One thread issues the chunk's 12 MMAs, commits them to an mbarrier and waits (bounded);
+// D stays in tensor memory over the chunks (48 of 64 allocated columns). Each thread then loads its
+// row (coarse node) and writes the 16 spheres' strengths. Every D element is the same sum whichever
+// spheres share its tile, so a problem's strengths do not depend on the batch.
 constexpr int kCsTcSph = kCoarseTcSph, kCsTcN = 3 * kCsTcSph, kCsTcK = 32;
 static_assert(kCoarseTcNodes == 128, "one M = 128 MMA tile per CTA");
 constexpr int kCsTcABytes = 128 * kCsTcK * 4, kCsTcBBytes = kCsTcN * kCsTcK * 4;
@@ -338,31 +339,24 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
     unsigned char* sAl = cs_smem + kCsTcABytes;
     unsigned char* sBh = cs_smem + 2 * kCsTcABytes;
     unsigned char* sBl = sBh + kCsTcBBytes;
-    const float* __restrict__ mapT = cs.cmapT + G.x;  // [coarse node][fine node]
-    const int krow = k0 + tid;                       // this thread's A row (coarse node)
+    const int krow = k0 + tid;  // this thread's D row (coarse node)
     const bool rvalid = krow < cnt;
     const int nck = (ng + kCsTcK - 1) / kCsTcK;
+    // this tile's A chunks: [chunk][hi, lo][128 x 32 in core-matrix order]
+    const float4* __restrict__ At = cs.cmapA + (G.w + (long long)(k0 / 128) * nck * 2 * 128 * kCsTcK) / 4;
     unsigned phase = 0;
     bool failed = false;
     for (int ch = 0; ch < nck; ++ch) {
         const int j0 = ch * kCsTcK;
-        // A: row tid, 32 fine nodes
+        // A: the chunk's pre-split tiles, hi then lo, straight copies
+        {
+            const float4* src_h = At + (long long)ch * 2 * (kCsTcABytes / 16);
+            const float4* src_l = src_h + kCsTcABytes / 16;
 #pragma unroll
-        for (int q = 0; q < kCsTcK / 4; ++q) {
-            float v[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int j = j0 + 4 * q + e;
-                v[e] = (rvalid && j < ng) ? __ldg(mapT + (long long)krow * ng + j) : 0.f;
+            for (int v = tid; v < kCsTcABytes / 16; v += 128) {
+                reinterpret_cast<float4*>(sAh)[v] = __ldg(src_h + v);
+                reinterpret_cast<float4*>(sAl)[v] = __ldg(src_l + v);
             }
-            float4 h, l;
-            tc::tf32_split(v[0], h.x, l.x);
-            tc::tf32_split(v[1], h.y, l.y);
-            tc::tf32_split(v[2], h.z, l.z);
-            tc::tf32_split(v[3], h.w, l.w);
-            const uint32_t off = tc::kmajor_offset(tid, 4 * q, kCsTcK);
-            *reinterpret_cast<float4*>(sAh + off) = h;
-            *reinterpret_cast<float4*>(sAl + off) = l;
         }
         // B: rows 3 s + c (sphere s of the tile, component c), 32 fine nodes
         for (int v = tid; v < kCsTcSph * kCsTcK; v += 128) {
@@ -371,8 +365,8 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
             const float fc[3] = {f.x, f.y, f.z};
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) {
-                float h, l;
-                tc::tf32_split(fc[cc], h, l);
+                // the low part rounded to TF32 as well (the MMA would truncate it), like the A tiles
+                const float h = tc::tf32_hi(fc[cc]), l = tc::tf32_hi(fc[cc] - h);
                 const uint32_t off = tc::kmajor_offset(3 * si + cc, jj, kCsTcK);
                 *reinterpret_cast<float*>(sBh + off) = h;
                 *reinterpret_cast<float*>(sBl + off) = l;

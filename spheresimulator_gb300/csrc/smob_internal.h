@@ -101,6 +101,7 @@ struct CoarseSet {
     // the same GEMMs on the tensor cores (FP32 set): tiles of 128 coarse nodes x 16 spheres
     int ncdesc_tc;
     const int4* cdesc_tc;      // [ncdesc_tc] {group, first coarse node, first entry in gent, entries (<= 16)}
+    const float4* cmapA;       // their A operand, pre-split and tiled per group (offset cgrp.w, in floats)
     // Coarse targets: a target sphere t takes the far field of a well-separated source sphere s at the
     // nodes of one of its own coarse levels and interpolates it to its grid (the transposed map);
     // level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s)) + ctmargin, if

@@ -104,7 +104,11 @@ def test_time_loop_with_warm_start_and_several_columns():
         vc = cold.solveMob(F, tol=1e-10, precision=PREC_MIXED)
         assert warm["status"] == 0 and warm["iterations"] <= cold.last_stats[0]["iterations"]
         assert np.linalg.norm(v - vc) / np.linalg.norm(vc) < 1e-8
+    # several columns: each the same bits as its single solve with the one-target tile, the coarse
+    # targets off and every float-float pair summed (what the several-column kernels evaluate)
     mob.set_far_tile(1)
+    mob.set_far_coarse_targets(False)
+    mob.set_far_compression(1e-5, 0)
     G = np.random.default_rng(6).standard_normal((3, 6 * mob.n_spheres))
     V = mob.solveMobMulti(G, tol=1e-10, precision=PREC_MIXED)
     for j in range(3):
