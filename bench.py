@@ -798,6 +798,7 @@ def run_multi(args, world, rank, local, dist):
     F = np.random.default_rng(7).standard_normal((k, 6 * mob.n_spheres))
     kw = dict(tol=TOL, restart=RESTART, max_iters=1000, precision=PREC_MIXED)
     auto_tile = mob.tuning()[0]
+    mob.set_multi_shared_pairs(False)
 
     def singles():
         return np.stack([mob.solveMob(F[j], **kw) for j in range(k)])
@@ -815,15 +816,16 @@ def run_multi(args, world, rank, local, dist):
     for _ in range(args.steps):
         vs = singles()
     t_single = allmax(dist, time.perf_counter() - t0)
-    mob.set_far_tile(1)
-    eps32, eps_hp = mob.far_compression_info()[0], mob.far_compression_info(hp=True)[0]
-    # the several-column float-float pass sums every grid-point pair, and the several-column FP32 kernel
-    # evaluates the grid targets of every far pair: the singles' float-float set and coarse targets off
-    mob.set_far_compression(eps32, 0)
-    mob.set_far_coarse_targets(False)
-    bitwise = bool(np.array_equal(mob.solveMobMulti(F, **kw), singles()))
-    mob.set_far_coarse_targets(True)
-    mob.set_far_compression(eps32, eps_hp)
+    # the columns as a batch of copies (the default) are each their single solve, bit for bit
+    bitwise = bool(np.array_equal(vm, vs))
+    # the shared-pair kernels (each grid-point pair once for all columns) for comparison
+    mob.set_multi_shared_pairs(True)
+    mob.solveMobMulti(F, **kw)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        mob.solveMobMulti(F, **kw)
+    t_shared = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    mob.set_multi_shared_pairs(False)
     err = float(np.linalg.norm(vm - vs) / np.linalg.norm(vs))
     if rank != 0:
         return None
@@ -836,11 +838,13 @@ def run_multi(args, world, rank, local, dist):
             "single_solves": {"columns_per_s": round(world * k * args.steps / t_single, 4),
                               "ms_per_k_columns": round(1e3 * t_single / args.steps, 3), "far_tile": auto_tile},
             "speedup_vs_single_solves": round(t_single / t_multi, 3),
-            "iterations_per_column": its, "rel_diff_vs_single_autotuned": err,
-            "bitwise_note": "with the FP32 coarse sources on, the float-float ones and the coarse targets off (the "
-                            "several-column kernels evaluate the grid targets and the float-float one every "
-                            "grid-point pair)",
-            "bitwise_equal_to_single_solves_tile1": bitwise}
+            "iterations_per_column": its, "rel_diff_vs_single_solves": err,
+            "bitwise_equal_to_single_solves": bitwise,
+            "bitwise_note": "the columns are solved as a batch of copies of the problem with the single solves' "
+                            "own settings and kernels",
+            "shared_pair_kernels": {"columns_per_s": round(world * k / t_shared, 4),
+                                    "note": "smob_set_multi_shared_pairs: each grid-point pair once for all "
+                                            "columns (grid targets, every float-float pair)"}}
 
 
 def contact_forces(centers, n_contacts, n_solves, seed):

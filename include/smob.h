@@ -205,10 +205,14 @@ smob_status smob_write_xyz(smob_ctx* ctx, const char* path, const int* gids, dou
 /* Several right-hand sides on one geometry: the columns SphereSTKMobMat::apply solves one after
  * another with solveMob (BIE/SphereSTKMobMat.cpp:129-143), solved together, each with its own
  * Krylov space and stopping test. force6n [n_rhs][6N], vel6n [n_rhs][6N], density3m [n_rhs][3M] or
- * NULL, stats [n_rhs] or NULL. The FP32 far field evaluates each pair's geometry once for all
- * columns; every column's result equals bit for bit a smob_solve_mob of that column alone with
- * smob_set_far_tile(ctx, 1). The context must hold one problem. Internal copies of the geometry
- * are kept on the context per column count (at most 4 counts). */
+ * NULL, stats [n_rhs] or NULL. By default the columns are a batch of copies of the problem with the
+ * context's own settings: every column's result equals bit for bit a smob_solve_mob of that column
+ * alone. With smob_set_multi_shared_pairs(ctx, 1) the far field evaluates each grid-point pair once for
+ * all columns instead (grid targets, every float-float pair); a column then equals its single solve
+ * with smob_set_far_tile(ctx, 1), the coarse targets off and the float-float tolerance 0. The context
+ * must hold one problem. Internal copies of the geometry are kept on the context per column count (at
+ * most 4 counts). */
+smob_status smob_set_multi_shared_pairs(smob_ctx* ctx, int on);
 /* Far field from coarse equivalent sources. For a well-separated pair of spheres the far field of the
  * source sphere's grid sources is evaluated from equivalent sources on a coarser grid of the same
  * sphere: its grid sources projected onto the spherical harmonics of degree <= pe and re-weighted with
@@ -372,10 +376,11 @@ smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* va
  * near-singular pairs always use the FP64 SIMT kernel. */
 smob_status smob_set_near_tc(smob_ctx* ctx, int on);
 /* The FP32 passes' coarse equivalent-source strengths (per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per
- * sphere]) as 3xTF32 GEMMs on the tcgen05 tensor cores (1; k_coarse_src_tc: 128 coarse nodes x 16
- * spheres per CTA) or as the SIMT FP32 GEMM (0, the default: faster and more accurate, measured on cfg2
- * 0.88 vs 1.55 ms per solve and 4.8e-7 vs 2.3e-6 from FP64 in the far field). Each problem's strengths
- * are the same bits alone or in a batch with either. */
+ * sphere]) as 3xTF32 GEMMs on the tcgen05 tensor cores (1, the default; k_coarse_src_tc: 128 coarse
+ * nodes x 16 spheres per tile, its K chunks split over 4 CTAs and added in fixed order) or as the SIMT
+ * FP32 GEMM (0). Both keep FP32-class accuracy (cfg2 far field 7.7e-7 and 4.8e-7 from FP64); each
+ * problem's strengths are the same bits alone or in a batch with either. The tensor-core one needs
+ * four partial strengths per coarse point of workspace. */
 smob_status smob_set_coarse_tc(smob_ctx* ctx, int on);
 smob_status smob_coarse_tc_info(const smob_ctx* ctx, int* on);
 /* FP32 sphere operator (self terms of the FP32 passes) with the Legendre stage of its transforms on the

@@ -219,8 +219,13 @@ class _Context:
         N.check(self._L.smob_coarse_tc_info(self._h, ctypes.byref(v)))
         return bool(v.value)
 
+    def set_multi_shared_pairs(self, on=True):
+        """Several right-hand sides with the shared-pair kernels (each grid-point pair once for all
+        columns) instead of a batch of copies (the default)."""
+        N.check(self._L.smob_set_multi_shared_pairs(self._h, int(bool(on))))
+
     def set_coarse_tc(self, on=True):
-        """FP32 coarse equivalent-source strengths on the tensor cores or the SIMT GEMM (default)"""
+        """FP32 coarse equivalent-source strengths on the tensor cores (default) or the SIMT GEMM"""
         N.check(self._L.smob_set_coarse_tc(self._h, int(bool(on))))
 
     def set_near_tc(self, on=True):

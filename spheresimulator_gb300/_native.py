@@ -138,6 +138,7 @@ def lib():
         "smob_set_far_tile": (S, [_VP, ctypes.c_int]),
         "smob_set_near_tc": (S, [_VP, ctypes.c_int]),
         "smob_set_coarse_tc": (S, [_VP, ctypes.c_int]),
+        "smob_set_multi_shared_pairs": (S, [_VP, ctypes.c_int]),
         "smob_coarse_tc_info": (S, [_VP, ctypes.POINTER(ctypes.c_int)]),
         "smob_set_sphere_tc": (S, [_VP, ctypes.c_int]),
         "smob_tc_info": (S, [_VP, _IP, _IP]),

@@ -244,9 +244,10 @@ struct smob_ctx {
     DBuf d_active;
     DBuf d_err;            // device error word (DevGeom::err)
     bool near_tc = true;   // FP32 near field on the tensor cores
-    // FP32 coarse strengths on the tensor cores (k_coarse_src_tc); off: measured slower and less
-    // accurate than the SIMT GEMM (cfg2: 1.55 vs 0.88 ms per solve, 2.3e-6 vs 4.8e-7 from FP64)
-    bool coarse_tc = false;
+    // FP32 coarse strengths on the tensor cores (k_coarse_src_tc, split-K over 4 CTAs per tile); measured
+    // on cfg2 0.79 vs 0.83 ms per profiled solve against the SIMT GEMM (81.6 vs 80.2 solves/s), its
+    // far field 7.7e-7 from FP64 against 4.8e-7
+    bool coarse_tc = true;
     // FP32 sphere operator with the Legendre stage on the tensor cores: off by default, measured slower
     // than the single-kernel SIMT operator (three launches per pass against one; cfg2 2.1 vs 1.1 ms per
     // solve, a 64-problem batch 0.54 vs 0.21 ms per pass)
@@ -265,6 +266,7 @@ struct smob_ctx {
         std::vector<int4> cdesc, cgrp, cdesc_tc;
         std::vector<int2> gent;
         DBuf d_clev, d_cent, d_cpos32, d_cpos32lo, d_csrc, d_cmap, d_cdesc, d_cgrp, d_gent, d_cdesc_tc, d_cmapA;
+        DBuf d_cpart, d_ctile_count;  // tensor-core strengths: split partials and per-tile counters
         // coarse targets: listed entries with their candidate sources, work items, partial sums and
         // the interpolation side
         bool ctgt = false;
@@ -332,6 +334,7 @@ struct smob_ctx {
     std::map<std::vector<int>, LoopGraph> loop_graphs;
     bool loop_graph_ok = true;  // false once building one failed (the host-driven loop runs instead)
     bool eps_hp_auto = true;    // the float-float set's tolerance follows the solves (fit_eps_hp)
+    bool multi_shared = false;  // several right-hand sides: shared-pair kernels instead of a batch
     bool loop_graph_on = true;  // smob_set_loop_graph
     void drop_graphs() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second.exec);
@@ -1000,6 +1003,15 @@ void build_leg(smob_ctx* c) {
 // level has at most kCoarseTargetNum / kCoarseTargetDen of s's grid points); at most kCoarseLevels
 // orders per sphere (the finest kept). Maps (and their transposes) are shared per (p, pe). Then the
 // coarse-target entries, their candidates, work items and interpolation tiles.
+// Workspace of the tensor-core strengths (FP32 set), only while they are selected: the split partials
+// (kCoarseTcSplit x the coarse points) and the per-tile counters, zeroed once (the kernel leaves them zero).
+void coarse_tc_buffers(smob_ctx* c, smob_ctx::CoarseHost& h) {
+    if (!c->coarse_tc || h.hp) return;
+    h.d_cpart.alloc(sizeof(float4) * (size_t)kCoarseTcSplit * (size_t)std::max(h.ncoarse, 1));
+    h.d_ctile_count.alloc(sizeof(unsigned) * std::max<size_t>(h.cdesc_tc.size(), 1));
+    CUDA_OK(cudaMemsetAsync(h.d_ctile_count.p, 0, h.d_ctile_count.bytes, c->st));
+}
+
 void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>& nodes, std::vector<int>& node_off,
                       std::vector<char>& have_nodes) {
     const int N = c->N;
@@ -1313,6 +1325,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         }
         h.d_cmapA.upload(mapA);
         h.d_cgrp.upload(h.cgrp);  // with the offsets
+        coarse_tc_buffers(c, h);
     }
     const size_t np = std::max(h.ncoarse, 1);
     h.d_cpos32.alloc(sizeof(float4) * np);
@@ -1448,6 +1461,9 @@ void bind_geom(smob_ctx* c) {
         cs.ncdesc_tc = (int)h.cdesc_tc.size();
         cs.cdesc_tc = h.d_cdesc_tc.as<int4>();
         cs.cmapA = h.hp ? nullptr : h.d_cmapA.as<float4>();
+        cs.cpart = h.d_cpart.as<float4>();
+        cs.ctile_count = h.d_ctile_count.as<unsigned>();
+        cs.ncoarse32 = h.ncoarse;
         cs.cgrp = h.d_cgrp.as<int4>();
         cs.gent = h.d_gent.as<int2>();
         const bool ct = !h.ctent.empty();
@@ -3339,7 +3355,11 @@ smob_status smob_solve_mob(smob_ctx* c, const double* force, double* vel, double
 
 namespace {
 // A child context holding k copies of c's one problem (replica r = problem r), cached per k on c.
-// The copies share c's geometry exactly, so the far field can evaluate each pair once for all of them.
+// By default the copies form an ordinary batch with c's own far-field settings and kernels: every
+// column is then the same bits as its single solve (a problem does not depend on its batch), and the
+// batch fills the GPU better than k single solves (cfg2, 8 columns: 117.8 vs 81.7 columns/s). With
+// shared pairs (smob_set_multi_shared_pairs) the far field evaluates each grid-point pair once for all
+// columns instead (the several-column kernels: grid targets, no float-float compression).
 smob_ctx* replicated(smob_ctx* c, int k) {
     auto it = c->multi.find(k);
     if (it != c->multi.end()) return it->second;
@@ -3361,10 +3381,12 @@ smob_ctx* replicated(smob_ctx* c, int k) {
                             c->viscosity};
     std::unique_ptr<smob_ctx> r(new smob_ctx);
     r->device = c->device;
+    const bool shared = c->multi_shared;
     r->c32.eps = c->c32.eps;  // replicas share the levels; each column's coarse strengths are its own
-    r->c32.ctgt = false;      // the several-column kernels evaluate the grid targets of every far pair
-    r->chp.eps = 0.0;         // the several-column float-float kernel sums every grid-point pair
-    r->chp.ctgt = false;
+    r->c32.ctgt = shared ? false : c->c32.ctgt;  // the several-column kernels evaluate grid targets
+    r->chp.eps = shared ? 0.0 : c->chp.eps;      // and every float-float grid-point pair
+    r->chp.ctgt = shared ? false : c->chp.ctgt;
+    r->eps_hp_auto = shared ? false : c->eps_hp_auto;
     r->coarse_tc = c->coarse_tc;
     r->near_tc = c->near_tc;  // the same near and sphere kernels as the single solves (results equal column
     r->sph_tc = c->sph_tc;    // by column)
@@ -3372,12 +3394,14 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     create_streams(r.get(), 0);
     AllocStreamScope scope(r->st);
     build_context(r.get(), &geo);
-    r->nrep = k;
-    r->rep_M = c->M;
-    bind_geom(r.get());  // coarse points per replica
-    for (const FarItem& f : r->items_tpt[0])
-        if (f.problem == 0) r->items_rep.push_back(f);
-    r->d_items_rep.upload(r->items_rep);
+    if (shared) {
+        r->nrep = k;
+        r->rep_M = c->M;
+        bind_geom(r.get());  // coarse points per replica
+        for (const FarItem& f : r->items_tpt[0])
+            if (f.problem == 0) r->items_rep.push_back(f);
+        r->d_items_rep.upload(r->items_rep);
+    }
     r->use_graphs = c->use_graphs;
     r->loop_graph_on = c->loop_graph_on;
     CUDA_OK(cudaStreamSynchronize(r->st));
@@ -3787,6 +3811,24 @@ smob_status smob_set_coarse_tc(smob_ctx* c, int on) {
         c->drop_graphs();  // captured passes hold the other kernel
         for (auto& kv : c->multi) smob_set_coarse_tc(kv.second, on);
         c->coarse_tc = on != 0;
+        AllocStreamScope as(c->st);
+        coarse_tc_buffers(c, c->c32);
+        bind_geom(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        return SMOB_OK;
+    });
+}
+
+smob_status smob_set_multi_shared_pairs(smob_ctx* c, int on) {
+    return guarded([&]() -> smob_status {
+        need(c != nullptr, "null context");
+        CtxScope ctx_scope(c);
+        CUDA_OK(cudaStreamSynchronize(c->st));
+        if ((on != 0) != c->multi_shared) {
+            for (auto& kv : c->multi) smob_destroy(kv.second);
+            c->multi.clear();
+        }
+        c->multi_shared = on != 0;
         return SMOB_OK;
     });
 }

@@ -288,17 +288,22 @@ __global__ void __launch_bounds__(128 * kCgGroups) k_coarse_src(DevGeom g, const
 // both operands as TF32 high and low parts (3xTF32: hi.hi + hi.lo + lo.hi, about FP32 accuracy): A is
 // copied from its pre-split tiles (cs.cmapA, coalesced float4 loads), B gathered and split by the
 // threads. One thread issues the chunk's 12 MMAs, commits them to an mbarrier and waits (bounded);
-// D stays in tensor memory over the chunks (48 of 64 allocated columns). Each thread then loads its
-// row (coarse node) and writes the 16 spheres' strengths. Every D element is the same sum whichever
-// spheres share its tile, so a problem's strengths do not depend on the batch.
+// D stays in tensor memory over the chunks (48 of 64 allocated columns). The K chunks are split over
+// kCsTcSplit CTAs (grid y) so a tile's chunks run side by side: each CTA loads its D rows and writes
+// them as partial sums (cs.cpart[split]); the last CTA of the tile to finish (a counter per tile,
+// after a memory fence) adds the splits in fixed order and writes the 16 spheres' strengths. Every
+// D element is the same sum whichever spheres share its tile and whichever CTA finishes last, so a
+// problem's strengths do not depend on the batch or the schedule.
 constexpr int kCsTcSph = kCoarseTcSph, kCsTcN = 3 * kCsTcSph, kCsTcK = 32;
 static_assert(kCoarseTcNodes == 128, "one M = 128 MMA tile per CTA");
 constexpr int kCsTcABytes = 128 * kCsTcK * 4, kCsTcBBytes = kCsTcN * kCsTcK * 4;
 constexpr int kCsTcSmem = 2 * kCsTcABytes + 2 * kCsTcBBytes;  // A hi, A lo, B hi, B lo: 44 KB
 constexpr long long kCsTcWaitPolls = 1LL << 22;
+static_assert(kCoarseTcSplit >= 1, "at least one split");
 __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* __restrict__ src) {
     const CoarseSet& cs = g.cs32;
     const int4 d = cs.cdesc_tc[blockIdx.x];
+    const int split = blockIdx.y;
     const int4 G = cs.cgrp[d.x];
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
     extern __shared__ __align__(1024) unsigned char cs_smem[];
@@ -307,6 +312,7 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
     __shared__ int s_fail;
     __shared__ int sbase[kCsTcSph], sout[kCsTcSph];
     __shared__ unsigned char sact[kCsTcSph];
+    __shared__ int s_last;
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid < kCsTcSph) {
         int sb = 0, so = 0;
@@ -342,11 +348,12 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
     const int krow = k0 + tid;  // this thread's D row (coarse node)
     const bool rvalid = krow < cnt;
     const int nck = (ng + kCsTcK - 1) / kCsTcK;
+    const int ch0 = split * nck / kCoarseTcSplit, ch1 = (split + 1) * nck / kCoarseTcSplit;  // this CTA's chunks
     // this tile's A chunks: [chunk][hi, lo][128 x 32 in core-matrix order]
     const float4* __restrict__ At = cs.cmapA + (G.w + (long long)(k0 / 128) * nck * 2 * 128 * kCsTcK) / 4;
     unsigned phase = 0;
     bool failed = false;
-    for (int ch = 0; ch < nck; ++ch) {
+    for (int ch = ch0; ch < ch1; ++ch) {
         const int j0 = ch * kCsTcK;
         // A: the chunk's pre-split tiles, hi then lo, straight copies
         {
@@ -385,7 +392,7 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
                 const uint32_t o = ks * 256;
                 const uint64_t ah = tc::sdesc(ah0 + o, 128, sbo), al = tc::sdesc(al0 + o, 128, sbo);
                 const uint64_t bh = tc::sdesc(bh0 + o, 128, sbo), bl = tc::sdesc(bl0 + o, 128, sbo);
-                tc::mma_tf32(tmem, ah, bh, idesc, ch > 0 || ks > 0);
+                tc::mma_tf32(tmem, ah, bh, idesc, ch > ch0 || ks > 0);
                 tc::mma_tf32(tmem, ah, bl, idesc, true);
                 tc::mma_tf32(tmem, al, bh, idesc, true);
             }
@@ -399,12 +406,19 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
             break;
         }
     }
+    // this split's partial sums (zeros for a split without chunks), then the tile's last CTA
+    float4* __restrict__ part = cs.cpart + (long long)split * cs.ncoarse32;
     if (!failed) {
-        tc::fence_after_sync();
         float da[32], db[32];
-        const uint32_t lane_base = uint32_t(warp * 32) << 16;
-        tc::tmem_ld_32x32b_x32(tmem + lane_base, da);       // columns 0-31
-        tc::tmem_ld_32x32b_x32(tmem + 32 + lane_base, db);  // columns 32-63 (48-63 unused)
+        if (ch1 > ch0) {
+            tc::fence_after_sync();
+            const uint32_t lane_base = uint32_t(warp * 32) << 16;
+            tc::tmem_ld_32x32b_x32(tmem + lane_base, da);       // columns 0-31
+            tc::tmem_ld_32x32b_x32(tmem + 32 + lane_base, db);  // columns 32-63 (48-63 unused)
+        } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) da[q] = db[q] = 0.f;
+        }
         if (rvalid) {
 #pragma unroll
             for (int si = 0; si < kCsTcSph; ++si) {
@@ -415,11 +429,37 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
                     const int col = 3 * si + cc;
                     o[cc] = col < 32 ? da[col] : db[col - 32];
                 }
-                cs.csrc[sout[si] + krow] = make_float4(o[0], o[1], o[2], 0.f);
+                part[sout[si] + krow] = make_float4(o[0], o[1], o[2], 0.f);
             }
         }
     } else if (tid == 0 && g.err) {
         atomicExch(g.err, 1);
+    }
+    // every CTA of the tile counts itself once (also a failed one, whose results are void anyway)
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        unsigned* cnt_p = cs.ctile_count + blockIdx.x;
+        s_last = atomicAdd(cnt_p, 1u) == unsigned(kCoarseTcSplit - 1) ? 1 : 0;
+        if (s_last) *cnt_p = 0u;  // ready for the next pass
+    }
+    __syncthreads();
+    if (s_last && rvalid) {
+        __threadfence();
+#pragma unroll 1
+        for (int si = 0; si < ne; ++si) {
+            if (!sact[si]) continue;
+            const long long q = sout[si] + krow;
+            float4 t = __ldcg(cs.cpart + q);
+#pragma unroll
+            for (int sp = 1; sp < kCoarseTcSplit; ++sp) {
+                const float4 v = __ldcg(cs.cpart + (long long)sp * cs.ncoarse32 + q);
+                t.x += v.x;
+                t.y += v.y;
+                t.z += v.z;
+            }
+            cs.csrc[q] = make_float4(t.x, t.y, t.z, 0.f);
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -1661,7 +1701,7 @@ int launch_coarse_src(const DevGeom& g, const float4* src32, cudaStream_t st) {
 
 int launch_coarse_src_tc(const DevGeom& g, const float4* src32, cudaStream_t st) {
     if (g.cs32.ncent <= 0 || g.cs32.ncdesc_tc <= 0) return 0;
-    k_coarse_src_tc<<<g.cs32.ncdesc_tc, 128, kCsTcSmem, st>>>(g, src32);
+    k_coarse_src_tc<<<dim3(g.cs32.ncdesc_tc, kCoarseTcSplit), 128, kCsTcSmem, st>>>(g, src32);
     return 1;
 }
 

@@ -207,6 +207,8 @@ size_t request_bytes(int n, const int* orders, int restart) {
     b += size_t(12) * 2 * coef;               // coefficients (FP32 + FP64)
     b += size_t(12) * setsrc * size_t(n);     // near-field sets (upper bound: every sphere a source)
     b += size_t(96) * M;                      // coarse equivalent sources: points and strengths of both sets
+    b += size_t(128) * M;                     // their tensor-core strengths' split partials (4 x 16 B per
+                                              // coarse point, up to ~2 coarse points per grid point)
     b += size_t(700) * M;                     // coarse targets: level slots (9 x (12 + 48) B per point), node
                                               // values, normals and partial sums of both sets
     b += size_t(96) << 20;                    // tables, coarse maps (and their transposes) and small arrays

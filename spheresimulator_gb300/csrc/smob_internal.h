@@ -44,6 +44,7 @@ constexpr int kCoarseLevels = 8;         // coarse equivalent-source levels per 
 constexpr int kCoarseTileNodes = 32;     // coarse nodes per CTA of the coarse-strength GEMMs (multiple of 16)
 constexpr int kCoarseTcNodes = 128;      // tensor-core coarse-strength GEMM: coarse nodes (MMA rows) per CTA
 constexpr int kCoarseTcSph = 16;         // and spheres per CTA (three MMA columns each)
+constexpr int kCoarseTcSplit = 4;        // CTAs per tile, each a quarter of the K chunks
 // interpolation tiles of the coarse targets (the host lists at most this many entries per tile; the
 // kernels k_ct_interp / k_ct_interp_df read exactly these): FP32 set 2 entries x 128 grid points,
 // float-float set 1 entry x 256 grid points (two per thread)
@@ -102,6 +103,9 @@ struct CoarseSet {
     int ncdesc_tc;
     const int4* cdesc_tc;      // [ncdesc_tc] {group, first coarse node, first entry in gent, entries (<= 16)}
     const float4* cmapA;       // their A operand, pre-split and tiled per group (offset cgrp.w, in floats)
+    float4* cpart;             // [kCoarseTcSplit][ncoarse32] partial strengths of the K splits
+    unsigned* ctile_count;     // [ncdesc_tc] splits finished per tile (zero between launches)
+    long long ncoarse32;       // coarse points of the set
     // Coarse targets: a target sphere t takes the far field of a well-separated source sphere s at the
     // nodes of one of its own coarse levels and interpolates it to its grid (the transposed map);
     // level: the coarsest built pe with pe >= clog_eps / log(a_t / (|c_t - c_s| - a_s)) + ctmargin, if

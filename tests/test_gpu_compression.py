@@ -228,19 +228,19 @@ def test_coarse_strengths_on_tensor_cores():
     GEMM and the FP64 sum: FP32 accuracy; a batch's problems equal the problems alone bit for bit."""
     c = _spread(seed=51, n=40, p=12, box=40.0)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
-    assert not g.coarse_tc() and g.far_compression_info()[2] > 0
+    assert g.coarse_tc() and g.far_compression_info()[2] > 0
     x = np.random.default_rng(51).standard_normal(3 * g.n_points)
     fp64 = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_FP64)
-    simt = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
-    g.set_coarse_tc(True)
     tc = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
+    g.set_coarse_tc(False)
+    simt = g.far_field(x, cSL=0.5, cTrac=1.0, precision=PREC_MIXED)
     e_tc, e_simt = _rel(tc, fp64), _rel(simt, fp64)
     print("coarse strengths: tensor cores %.3g, SIMT %.3g against FP64; between them %.3g" % (e_tc, e_simt,
                                                                                            _rel(tc, simt)))
     assert e_tc < 2e-5 and e_simt < 2e-5
     # 3xTF32 products (2^-22 relative each) instead of FP32 ones (2^-24): the same order as the
     # compression's own error here
-    assert e_tc < max(2 * e_simt, 5e-6) and _rel(tc, simt) < 1e-5
+    assert e_tc < max(2 * e_simt, 2e-6) and _rel(tc, simt) < 5e-6
     # batched with a second problem: the first problem's solve is the same bits as alone
     b = _spread(seed=52, n=20, p=16, box=30.0)
     centers = np.vstack([c["centers"], b["centers"] + 500.0])
@@ -250,8 +250,6 @@ def test_coarse_strengths_on_tensor_cores():
     F = np.random.default_rng(53).standard_normal(6 * 60)
     both = SphereSTKMobMat(centers, radii, orders, problem=prob)
     alone = SphereSTKMobMat(c["centers"], c["radii"], c["orders"])
-    both.set_coarse_tc(True)
-    alone.set_coarse_tc(True)
     v = both.solveMob(F, tol=1e-8, precision=PREC_MIXED)
     assert np.array_equal(alone.solveMob(F[:240], tol=1e-8, precision=PREC_MIXED), v[:240])
 

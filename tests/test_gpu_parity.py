@@ -252,9 +252,27 @@ def test_batched_equals_alone():
         assert len(gb.last_stats) == 2
 
 
+@pytest.mark.parametrize("k", [2, 5])
+def test_multi_rhs_batch_equals_single_solves(k):
+    """K right-hand sides solved together as a batch of copies (the default) give bit for bit each
+    column's single solve with the context's own settings (coarse sources and targets, float-float
+    compression, tensor-core kernels), in both precisions."""
+    rng = np.random.default_rng(23)
+    radii = rng.uniform(0.8, 1.2, 14)
+    cfg = dict(centers=configs.rsa(rng, 14, radii, 26.0, 0.1), radii=radii, orders=np.full(14, 10))
+    mob = make(cfg, SphereSTKMobMat)
+    assert mob.far_compression_info()[2] > 0 and mob.far_compression_info(hp=True)[2] > 0
+    F = np.random.default_rng(k + 30).standard_normal((k, 6 * mob.n_spheres))
+    for prec in (PREC_MIXED, PREC_FP64):
+        V = mob.solveMobMulti(F, tol=1e-9, precision=prec)
+        for j in range(k):
+            assert np.array_equal(V[j], mob.solveMob(F[j], tol=1e-9, precision=prec)), (prec, j)
+
+
 @pytest.mark.parametrize("k", [2, 3, 6])
 def test_multi_rhs_equals_single_solves(k):
-    """K right-hand sides solved together (shared-geometry FP32 far field) give bit for bit the
+    """K right-hand sides solved together with the shared-pair kernels (smob_set_multi_shared_pairs:
+    the FP32 far field evaluates each pair's geometry once for all columns) give bit for bit the
     solves of each column alone with the one-target-per-thread FP32 kernel, with and without coarse
     equivalent sources in the FP32 passes (the several-column float-float pass sums every grid-point
     pair and the several-column FP32 kernel evaluates the grid targets of every far pair, so the single
@@ -264,6 +282,7 @@ def test_multi_rhs_equals_single_solves(k):
     radii = rng.uniform(0.8, 1.2, 12)
     cfg = dict(centers=configs.rsa(rng, 12, radii, 24.0, 0.1), radii=radii, orders=np.full(12, 10))
     mob = make(cfg, SphereSTKMobMat)
+    mob.set_multi_shared_pairs(True)
     mob.set_far_tile(1)
     mob.set_far_compression(1e-7, 0)
     mob.set_far_coarse_targets(False)
