@@ -376,9 +376,10 @@ smob_status smob_tuning(const smob_ctx* ctx, int* targets_per_thread, double* va
  * near-singular pairs always use the FP64 SIMT kernel. */
 smob_status smob_set_near_tc(smob_ctx* ctx, int on);
 /* The FP32 passes' coarse equivalent-source strengths (per (p, pe) map a GEMM [N_e x N_g] x [N_g x 3 per
- * sphere]) as 3xTF32 GEMMs on the tcgen05 tensor cores (1, the default; k_coarse_src_tc: 128 coarse
- * nodes x 16 spheres per tile, its K chunks split over 4 CTAs and added in fixed order) or as the SIMT
- * FP32 GEMM (0). Both keep FP32-class accuracy (cfg2 far field 7.7e-7 and 4.8e-7 from FP64); each
+ * sphere]) and their coarse-target interpolation (per map [N_g x N_e] x [N_e x 3 per entry]) as 3xTF32
+ * GEMMs on the tcgen05 tensor cores (1, the default; k_coarse_src_tc: 128 coarse nodes x 16 spheres
+ * per tile, its K chunks split over 4 CTAs and added in fixed order; k_ct_interp_tc: 128 grid points x
+ * 16 entries) or as the SIMT FP32 GEMMs (0). Both keep FP32-class accuracy (cfg2 far field 7.7e-7 and 4.8e-7 from FP64); each
  * problem's strengths are the same bits alone or in a batch with either. The tensor-core one needs
  * four partial strengths per coarse point of workspace. */
 smob_status smob_set_coarse_tc(smob_ctx* ctx, int on);

@@ -225,7 +225,8 @@ class _Context:
         N.check(self._L.smob_set_multi_shared_pairs(self._h, int(bool(on))))
 
     def set_coarse_tc(self, on=True):
-        """FP32 coarse equivalent-source strengths on the tensor cores (default) or the SIMT GEMM"""
+        """FP32 coarse equivalent-source strengths and coarse-target interpolation on the tensor cores
+        (default) or as SIMT GEMMs"""
         N.check(self._L.smob_set_coarse_tc(self._h, int(bool(on))))
 
     def set_near_tc(self, on=True):

@@ -275,6 +275,11 @@ struct smob_ctx {
         std::vector<CtWork> ct_work;
         std::vector<CtITile> ctitile;
         std::vector<int> ctient;
+        // tensor-core interpolation (FP32 set): tiles of 128 grid points x up to kCoarseTcSph entries of
+        // one map, their entry lists, and the maps' A operand pre-split and tiled (offset in the tile)
+        std::vector<CtITile> ctitile_tc;
+        std::vector<int> ctient_tc;
+        DBuf d_ctitile_tc, d_ctient_tc, d_cmapI;
         long long ct_partial = 0;
         DBuf d_ctent, d_ctsrc, d_ctcand, d_ctused, d_ct_work, d_ct_partial, d_ctinterp, d_cmapT, d_cnrm32,
             d_cnrm32lo, d_ctu, d_ctitile, d_ctient;
@@ -1003,6 +1008,16 @@ void build_leg(smob_ctx* c) {
 // level has at most kCoarseTargetNum / kCoarseTargetDen of s's grid points); at most kCoarseLevels
 // orders per sphere (the finest kept). Maps (and their transposes) are shared per (p, pe). Then the
 // coarse-target entries, their candidates, work items and interpolation tiles.
+// x rounded to TF32 (10 explicit mantissa bits; to nearest, ties away from zero), as cvt.rna.tf32 does
+float tf32_rna_host(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u = (u + 0x1000u) & 0xFFFFE000u;
+    float y;
+    std::memcpy(&y, &u, 4);
+    return y;
+}
+
 // Workspace of the tensor-core strengths (FP32 set), only while they are selected: the split partials
 // (kCoarseTcSplit x the coarse points) and the per-tile counters, zeroed once (the kernel leaves them zero).
 void coarse_tc_buffers(smob_ctx* c, smob_ctx::CoarseHost& h) {
@@ -1148,6 +1163,9 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.ct_work.clear();
     h.ctitile.clear();
     h.ctient.clear();
+    h.ctitile_tc.clear();
+    h.ctient_tc.clear();
+    std::vector<float> mapI;  // the interpolation maps' pre-split A tiles (FP32 set)
     std::vector<double> work_cost;
     h.ctused.assign((size_t)std::max(N, 1) * kCoarseLevels, 0);
     h.ct_partial = 0;
@@ -1280,6 +1298,34 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                 h.ctient.insert(h.ctient.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
                 for (int j0 = 0; j0 < ng; j0 += pts) h.ctitile.push_back(CtITile{kv.first, ng, n, first, ne, j0, 0, 0});
             }
+            if (h.hp) continue;
+            // the same entries for the tensor-core kernel: 16 per tile, A = the map [grid point][coarse
+            // node] in tiles of 128 grid points x 32 coarse nodes, split into TF32 hi and lo (rounded to
+            // nearest) in the MMA's core-matrix order
+            const int nmt = (ng + kCoarseTcNodes - 1) / kCoarseTcNodes, nck = (n + 31) / 32;
+            const int aoff = (int)mapI.size();
+            mapI.resize(mapI.size() + (size_t)nmt * nck * 2 * kCoarseTcNodes * 32, 0.f);
+            for (int mt = 0; mt < nmt; ++mt)
+                for (int ch = 0; ch < nck; ++ch) {
+                    float* hi = &mapI[(size_t)aoff + (size_t)(mt * nck + ch) * 2 * kCoarseTcNodes * 32];
+                    float* lo = hi + kCoarseTcNodes * 32;
+                    for (int r = 0; r < kCoarseTcNodes; ++r)
+                        for (int k = 0; k < 32; ++k) {
+                            const int j = mt * kCoarseTcNodes + r, kk = ch * 32 + k;
+                            const float v = (j < ng && kk < n) ? maps[(size_t)kv.first + (size_t)j * n + kk] : 0.f;
+                            const float vh = tf32_rna_host(v);
+                            const size_t o = tc::kmajor_offset(r, k, 32) / 4;
+                            hi[o] = vh;
+                            lo[o] = tf32_rna_host(v - vh);
+                        }
+                }
+            for (size_t a = 0; a < kv.second.size(); a += kCoarseTcSph) {
+                const int first = (int)h.ctient_tc.size();
+                const int ne = (int)std::min<size_t>(kCoarseTcSph, kv.second.size() - a);
+                h.ctient_tc.insert(h.ctient_tc.end(), kv.second.begin() + a, kv.second.begin() + a + ne);
+                for (int j0 = 0; j0 < ng; j0 += kCoarseTcNodes)
+                    h.ctitile_tc.push_back(CtITile{aoff, ng, n, first, ne, j0, 0, 0});
+            }
         }
     }
     h.d_clev.upload(h.clev);
@@ -1295,14 +1341,6 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         // tile of 128 coarse nodes and K chunk of 32 fine nodes, the transposed map's block split into
         // TF32 high and low parts (both rounded to nearest, ties away), each 16 KB in the MMA's K-major
         // core-matrix order, so a CTA stages it with straight coalesced copies. cgrp.w: its offset.
-        auto tf32_rna = [](float x) {
-            uint32_t u;
-            std::memcpy(&u, &x, 4);
-            u = (u + 0x1000u) & 0xFFFFE000u;
-            float y;
-            std::memcpy(&y, &u, 4);
-            return y;
-        };
         std::vector<float> mapA;
         for (int4& G : h.cgrp) {
             const int ng = G.y, cnt = G.z, nmt = (cnt + kCoarseTcNodes - 1) / kCoarseTcNodes, nck = (ng + 31) / 32;
@@ -1316,10 +1354,10 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
                         for (int k = 0; k < 32; ++k) {
                             const int kk = mt * kCoarseTcNodes + r, j = ch * 32 + k;
                             const float v = (kk < cnt && j < ng) ? mapsT[(size_t)G.x + (size_t)kk * ng + j] : 0.f;
-                            const float vh = tf32_rna(v);
+                            const float vh = tf32_rna_host(v);
                             const size_t o = tc::kmajor_offset(r, k, 32) / 4;
                             hi[o] = vh;
-                            lo[o] = tf32_rna(v - vh);
+                            lo[o] = tf32_rna_host(v - vh);
                         }
                 }
         }
@@ -1339,6 +1377,11 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
         h.d_ct_work.upload(h.ct_work);
         h.d_ctitile.upload(h.ctitile);
         h.d_ctient.upload(h.ctient);
+        if (!h.hp) {
+            h.d_ctitile_tc.upload(h.ctitile_tc);
+            h.d_ctient_tc.upload(h.ctient_tc);
+            h.d_cmapI.upload(mapI);
+        }
         const size_t slots = (size_t)(kCoarseLevels + 1) * (size_t)std::max(c->M, 1);
         h.d_cnrm32.alloc(sizeof(float4) * np);
         if (h.hp) {
@@ -1434,6 +1477,7 @@ void bind_geom(smob_ctx* c) {
     g.map_val_f = c->d_map_val_f.as<float>();
     g.active = c->d_active.as<unsigned char>();
     g.near_tc = c->near_tc ? 1 : 0;
+    g.coarse_tc = c->coarse_tc ? 1 : 0;
     g.err = c->d_err.as<int>();
     g.sph_tc = c->sph_tc ? 1 : 0;
     g.n_leg_tiles = c->n_leg_tiles;
@@ -1480,6 +1524,10 @@ void bind_geom(smob_ctx* c) {
         cs.ctcand = ct ? h.d_ctcand.as<int2>() : nullptr;
         cs.ctinterp = ct && !h.hp ? h.d_ctinterp.as<float>() : nullptr;
         cs.ctinterpd = ct && h.hp ? h.d_ctinterp.as<double>() : nullptr;
+        cs.nctitile_tc = ct && !h.hp ? (int)h.ctitile_tc.size() : 0;
+        cs.ctitile_tc = ct && !h.hp ? h.d_ctitile_tc.as<CtITile>() : nullptr;
+        cs.ctient_tc = ct && !h.hp ? h.d_ctient_tc.as<int>() : nullptr;
+        cs.cmapI = ct && !h.hp ? h.d_cmapI.as<float4>() : nullptr;
         cs.nctitile = ct ? (int)h.ctitile.size() : 0;
         cs.ctitile = ct ? h.d_ctitile.as<CtITile>() : nullptr;
         cs.ctient = ct ? h.d_ctient.as<int>() : nullptr;

@@ -1088,6 +1088,151 @@ __global__ void __launch_bounds__(128) k_ct_interp(DevGeom g) {
     }
 }
 
+// The interpolation on the tcgen05 tensor cores (FP32 set): per map the GEMM
+//   D [128 grid points x 48] = A [128 x N_e] . B [48 x N_e]^T,
+// A = the map [grid point][coarse node] (pre-split to 3xTF32 and tiled once per geometry, cmapI), B =
+// the coarse-node field of 16 entries, one row per (entry, component), gathered from ctu and split by
+// the threads; K runs over the coarse nodes in chunks of 32. One thread issues each chunk's 12 MMAs
+// and waits (bounded); even and odd chunks accumulate in two tensor-memory tiles (columns 0-47 and
+// 64-111), which halves each accumulation chain, and the two are added in FP32 at the end. Each thread
+// then writes its grid point's values of the 16 entries to their level slots of ctinterp. Every D
+// element is the same sum whichever entries share the tile.
+__global__ void __launch_bounds__(128) k_ct_interp_tc(DevGeom g) {
+    const CoarseSet& cs = g.cs32;
+    const CtITile d = cs.ctitile_tc[blockIdx.x];
+    extern __shared__ __align__(1024) unsigned char ci_smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    __shared__ int s_fail;
+    __shared__ int eq0[kCsTcSph];
+    __shared__ long long ebase[kCsTcSph];
+    __shared__ unsigned char eon[kCsTcSph];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid < kCsTcSph) {
+        eon[tid] = 0;
+        eq0[tid] = 0;
+        ebase[tid] = 0;
+        if (tid < d.ne) {
+            const CtEnt en = cs.ctent[cs.ctient_tc[d.e0 + tid]];
+            eon[tid] = (!g.active || g.active[en.problem]) ? 1 : 0;
+            eq0[tid] = en.q0;
+            ebase[tid] = (long long)en.l * g.M + g.gidx[en.t];
+        }
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, 128);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_fence_init();
+        s_fail = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    constexpr uint32_t idesc = tc::idesc_tf32(128, kCsTcN);
+    unsigned char* sAh = ci_smem;
+    unsigned char* sAl = ci_smem + kCsTcABytes;
+    unsigned char* sBh = ci_smem + 2 * kCsTcABytes;
+    unsigned char* sBl = sBh + kCsTcBBytes;
+    const int j = d.j0 + tid;  // this thread's D row (grid point)
+    const bool rvalid = j < d.ng;
+    const int nck = (d.n + kCsTcK - 1) / kCsTcK;
+    const float4* __restrict__ At = cs.cmapI + ((long long)d.mapoff + (long long)(d.j0 / 128) * nck * 2 * 128 * kCsTcK) / 4;
+    unsigned phase = 0;
+    bool failed = false;
+    for (int ch = 0; ch < nck; ++ch) {
+        const int k0 = ch * kCsTcK;
+        {
+            const float4* src_h = At + (long long)ch * 2 * (kCsTcABytes / 16);
+            const float4* src_l = src_h + kCsTcABytes / 16;
+#pragma unroll
+            for (int v = tid; v < kCsTcABytes / 16; v += 128) {
+                reinterpret_cast<float4*>(sAh)[v] = __ldg(src_h + v);
+                reinterpret_cast<float4*>(sAl)[v] = __ldg(src_l + v);
+            }
+        }
+        for (int v = tid; v < kCsTcSph * kCsTcK; v += 128) {
+            const int e = v / kCsTcK, kk = v % kCsTcK, k = k0 + kk;
+            const float4 u = (e < d.ne && eon[e] && k < d.n) ? cs.ctu[eq0[e] + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float uc[3] = {u.x, u.y, u.z};
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                const float h = tc::tf32_hi(uc[cc]), l = tc::tf32_hi(uc[cc] - h);
+                const uint32_t off = tc::kmajor_offset(3 * e + cc, kk, kCsTcK);
+                *reinterpret_cast<float*>(sBh + off) = h;
+                *reinterpret_cast<float*>(sBl + off) = l;
+            }
+        }
+        tc::fence_smem_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t ah0 = tc::smem_u32(sAh), al0 = tc::smem_u32(sAl);
+            const uint32_t bh0 = tc::smem_u32(sBh), bl0 = tc::smem_u32(sBl);
+            constexpr uint32_t sbo = (kCsTcK / 4) * 128;
+#pragma unroll
+            for (int ks = 0; ks < kCsTcK / 8; ++ks) {
+                const uint32_t o = ks * 256;
+                const uint64_t ah = tc::sdesc(ah0 + o, 128, sbo), al = tc::sdesc(al0 + o, 128, sbo);
+                const uint64_t bh = tc::sdesc(bh0 + o, 128, sbo), bl = tc::sdesc(bl0 + o, 128, sbo);
+                const uint32_t dt = tmem + 64 * (ch & 1);
+                tc::mma_tf32(dt, ah, bh, idesc, ch > 1 || ks > 0);
+                tc::mma_tf32(dt, ah, bl, idesc, true);
+                tc::mma_tf32(dt, al, bh, idesc, true);
+            }
+            tc::mma_commit(&mbar);
+            if (!tc::mbar_wait_bounded(&mbar, phase, kCsTcWaitPolls)) s_fail = 1;
+        }
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) {
+            failed = true;
+            break;
+        }
+    }
+    if (!failed && nck > 0) {
+        tc::fence_after_sync();
+        float da[32], db[32];
+        const uint32_t lane_base = uint32_t(warp * 32) << 16;
+        tc::tmem_ld_32x32b_x32(tmem + lane_base, da);       // even chunks, columns 0-31
+        tc::tmem_ld_32x32b_x32(tmem + 32 + lane_base, db);  // columns 32-63 (48-63 unused)
+        if (nck > 1) {  // odd chunks
+            float ea[32], eb[32];
+            tc::tmem_ld_32x32b_x32(tmem + 64 + lane_base, ea);
+            tc::tmem_ld_32x32b_x32(tmem + 96 + lane_base, eb);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                da[q] += ea[q];
+                db[q] += eb[q];
+            }
+        }
+        if (rvalid) {
+#pragma unroll
+            for (int e = 0; e < kCsTcSph; ++e) {
+                if (e >= d.ne || !eon[e]) continue;
+                float* o = cs.ctinterp + 3LL * (ebase[e] + j);
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) {
+                    const int col = 3 * e + cc;
+                    o[cc] = col < 32 ? da[col] : db[col - 32];
+                }
+            }
+        }
+    } else if (failed && tid == 0 && g.err) {
+        atomicExch(g.err, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, 128);
+    }
+}
+
 template <bool TRAC>
 __global__ void __launch_bounds__(kFarThreads) k_far64(DevGeom g, const FarItem* __restrict__ items,
                                                       const double4_32a* __restrict__ src, double* __restrict__ partial) {
@@ -1794,7 +1939,10 @@ int launch_far_ct(const DevGeom& g, const CtWork* works, int nworks, bool trac, 
     k_ct_sum<<<dim3(g.cs32.nctent, nblk), 128, 0, st>>>(g, partial);
     ++n;
     if (g.cs32.nctitile > 0) {  // grid entries only: nothing to interpolate
-        k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
+        if (g.coarse_tc && g.cs32.nctitile_tc > 0)
+            k_ct_interp_tc<<<g.cs32.nctitile_tc, 128, kCsTcSmem, st>>>(g);
+        else
+            k_ct_interp<<<g.cs32.nctitile, 128, 0, st>>>(g);
         ++n;
     }
     return n;

@@ -130,6 +130,10 @@ struct CoarseSet {
                                // grid by level slot, and the grid entries' sums
     double* ctud;              // float-float set: traction and single layer at the coarse targets [6]
     double* ctinterpd;         // float-float set: as ctinterp with [6] per point
+    int nctitile_tc;           // FP32 set: the tensor-core interpolation's tiles (CtITile with mapoff = the A
+    const struct CtITile* ctitile_tc;  // tile group's offset in cmapI, up to 16 entries), entry lists, and
+    const int* ctient_tc;      // the maps [grid point][coarse node] pre-split and tiled as its A operand
+    const float4* cmapI;
     int nctitile;              // interpolation tiles (CtITile) and their entry lists
     const struct CtITile* ctitile;
     const int* ctient;
@@ -172,6 +176,7 @@ struct DevGeom {
     int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
     int near_lanes;       // lanes per target point in the near-field kernel (1, 2, 4 or 8)
     int near_tc;          // FP32 near field on the tensor cores (k_near_eval_tc, tiled sets); 0: SIMT kernel
+    int coarse_tc;        // FP32 coarse strengths and coarse-target interpolation on the tensor cores
     // FP32 sphere operator with the Legendre stage on the tensor cores (k_legendre_tc; 0: one SIMT kernel):
     // tiles {order p, first entry of leg_sph, spheres (<= 21), 0} of spheres of one order; B operand
     // tables per (p, m), forward and inverse, at leg_off[2 (p (kMaxOrder + 1) + m) + {0, 1}] floats into

@@ -224,8 +224,9 @@ def test_float_float_coarse_targets():
 
 
 def test_coarse_strengths_on_tensor_cores():
-    """The FP32 coarse strengths as 3xTF32 GEMMs on the tensor cores (k_coarse_src_tc) against the SIMT
-    GEMM and the FP64 sum: FP32 accuracy; a batch's problems equal the problems alone bit for bit."""
+    """The FP32 coarse strengths and coarse-target interpolation as 3xTF32 GEMMs on the tensor cores
+    (k_coarse_src_tc, k_ct_interp_tc) against the SIMT GEMMs and the FP64 sum: FP32 accuracy; a batch's
+    problems equal the problems alone bit for bit."""
     c = _spread(seed=51, n=40, p=12, box=40.0)
     g = SphereSTKSHOperator(c["centers"], c["radii"], c["orders"])
     assert g.coarse_tc() and g.far_compression_info()[2] > 0
