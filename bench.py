@@ -272,9 +272,15 @@ def run_native(args, world, rank, local, dist):
     solve_dev(PREC_MIXED)
     prof_coarse_alt = mob.profile_table()
     mob.profile(False)
-    # and timed solves with the other coarse-strength kernel
+    # and timed solves with the other coarse kernels: both SIMT, then only one of the two on the
+    # tensor cores
     timed(PREC_MIXED, 2)
     ms_coarse_alt, _ = timed(PREC_MIXED, max(3, min(args.steps, 10)))
+    coarse_modes = {}
+    for mode in (2, 3):
+        mob.set_coarse_tc(mode)
+        timed(PREC_MIXED, 2)
+        coarse_modes[mode] = round(1e3 / float(timed(PREC_MIXED, max(3, min(args.steps, 10)))[0].mean()), 3)
     mob.set_coarse_tc(coarse_tc0)
     f32, f64 = ctypes.c_double(), ctypes.c_double()
     N.check(L.smob_measure_fma_peaks(local, ctypes.byref(f32), ctypes.byref(f64)))
@@ -414,6 +420,8 @@ def run_native(args, world, rank, local, dist):
             "far_coarse_ms_tc_simt": [round((prof if coarse_tc0 else prof_coarse_alt).get("far_coarse", (0, 0.0))[1], 4),
                                       round((prof_coarse_alt if coarse_tc0 else prof).get("far_coarse", (0, 0.0))[1], 4)],
             "solves_per_s_other_coarse_kernel": round(1e3 / float(ms_coarse_alt.mean()), 3),
+            "solves_per_s_coarse_tc_strengths_only": coarse_modes[2],
+            "solves_per_s_coarse_tc_interpolation_only": coarse_modes[3],
             "default_near_tc": near_tc0, "default_sphere_tc": sph_tc0, "default_coarse_tc": coarse_tc0,
             "note": "per profiled mixed solve (serialised CUDA-event times), tcgen05 kernels vs SIMT kernels: the "
                     "FP32 near-field contraction as a TF32 GEMM (k_near_eval_tc), the FP32 sphere operator "

@@ -379,11 +379,12 @@ smob_status smob_set_near_tc(smob_ctx* ctx, int on);
  * sphere]) and their coarse-target interpolation (per map [N_g x N_e] x [N_e x 3 per entry]) as 3xTF32
  * GEMMs on the tcgen05 tensor cores (1, the default; k_coarse_src_tc: 128 coarse nodes x 16 spheres
  * per tile, its K chunks split over 4 CTAs and added in fixed order; k_ct_interp_tc: 128 grid points x
- * 16 entries) or as the SIMT FP32 GEMMs (0). Both keep FP32-class accuracy (cfg2 far field 7.7e-7 and 4.8e-7 from FP64); each
+ * 16 entries) or as the SIMT FP32 GEMMs. mode: 1 both on the tensor cores (the default), 0 both on
+ * the SIMT pipes, 2 only the strengths, 3 only the interpolation on the tensor cores. Both keep FP32-class accuracy (cfg2 far field 7.7e-7 and 4.8e-7 from FP64); each
  * problem's strengths are the same bits alone or in a batch with either. The tensor-core one needs
  * four partial strengths per coarse point of workspace. */
-smob_status smob_set_coarse_tc(smob_ctx* ctx, int on);
-smob_status smob_coarse_tc_info(const smob_ctx* ctx, int* on);
+smob_status smob_set_coarse_tc(smob_ctx* ctx, int mode);
+smob_status smob_coarse_tc_info(const smob_ctx* ctx, int* mode);
 /* FP32 sphere operator (self terms of the FP32 passes) with the Legendre stage of its transforms on the
  * tensor cores: per order and m, the forward and inverse Legendre sums of up to 21 spheres as tcgen05
  * TF32 GEMMs (3xTF32 split), between per-sphere phi-DFT kernels (three launches per pass). Default 0:

@@ -214,20 +214,22 @@ class _Context:
         N.check(self._L.smob_set_sphere_tc(self._h, int(bool(on))))
 
     def coarse_tc(self):
-        """True if the FP32 coarse strengths run on the tensor cores"""
+        """Mode of the FP32 coarse GEMMs: 1 both on the tensor cores, 0 both SIMT, 2 only the strengths,
+        3 only the coarse-target interpolation on the tensor cores"""
         v = ctypes.c_int()
         N.check(self._L.smob_coarse_tc_info(self._h, ctypes.byref(v)))
-        return bool(v.value)
+        return v.value
 
     def set_multi_shared_pairs(self, on=True):
         """Several right-hand sides with the shared-pair kernels (each grid-point pair once for all
         columns) instead of a batch of copies (the default)."""
         N.check(self._L.smob_set_multi_shared_pairs(self._h, int(bool(on))))
 
-    def set_coarse_tc(self, on=True):
+    def set_coarse_tc(self, mode=1):
         """FP32 coarse equivalent-source strengths and coarse-target interpolation on the tensor cores
-        (default) or as SIMT GEMMs"""
-        N.check(self._L.smob_set_coarse_tc(self._h, int(bool(on))))
+        (mode 1, default; True) or as SIMT GEMMs (0, False); 2 only the strengths, 3 only the
+        interpolation on the tensor cores"""
+        N.check(self._L.smob_set_coarse_tc(self._h, int(mode)))
 
     def set_near_tc(self, on=True):
         """FP32 near field on the tensor cores (default) or on the SIMT pipes"""

@@ -244,10 +244,10 @@ struct smob_ctx {
     DBuf d_active;
     DBuf d_err;            // device error word (DevGeom::err)
     bool near_tc = true;   // FP32 near field on the tensor cores
-    // FP32 coarse strengths on the tensor cores (k_coarse_src_tc, split-K over 4 CTAs per tile); measured
-    // on cfg2 0.79 vs 0.83 ms per profiled solve against the SIMT GEMM (81.6 vs 80.2 solves/s), its
-    // far field 7.7e-7 from FP64 against 4.8e-7
-    bool coarse_tc = true;
+    // FP32 coarse GEMMs on the tensor cores: strengths (k_coarse_src_tc, split-K over 4 CTAs per tile)
+    // and coarse-target interpolation (k_ct_interp_tc); smob_set_coarse_tc modes
+    bool coarse_tc = true;         // strengths
+    bool coarse_interp_tc = true;  // interpolation
     // FP32 sphere operator with the Legendre stage on the tensor cores: off by default, measured slower
     // than the single-kernel SIMT operator (three launches per pass against one; cfg2 2.1 vs 1.1 ms per
     // solve, a 64-problem batch 0.54 vs 0.21 ms per pass)
@@ -1477,7 +1477,7 @@ void bind_geom(smob_ctx* c) {
     g.map_val_f = c->d_map_val_f.as<float>();
     g.active = c->d_active.as<unsigned char>();
     g.near_tc = c->near_tc ? 1 : 0;
-    g.coarse_tc = c->coarse_tc ? 1 : 0;
+    g.coarse_tc = c->coarse_interp_tc ? 1 : 0;
     g.err = c->d_err.as<int>();
     g.sph_tc = c->sph_tc ? 1 : 0;
     g.n_leg_tiles = c->n_leg_tiles;
@@ -3436,6 +3436,7 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     r->chp.ctgt = shared ? false : c->chp.ctgt;
     r->eps_hp_auto = shared ? false : c->eps_hp_auto;
     r->coarse_tc = c->coarse_tc;
+    r->coarse_interp_tc = c->coarse_interp_tc;
     r->near_tc = c->near_tc;  // the same near and sphere kernels as the single solves (results equal column
     r->sph_tc = c->sph_tc;    // by column)
     CUDA_OK(cudaSetDevice(c->device));
@@ -3857,8 +3858,10 @@ smob_status smob_set_coarse_tc(smob_ctx* c, int on) {
         CtxScope ctx_scope(c);
         CUDA_OK(cudaStreamSynchronize(c->st));
         c->drop_graphs();  // captured passes hold the other kernel
+        need(on >= 0 && on <= 3, "coarse tensor-core mode must be 0-3");
         for (auto& kv : c->multi) smob_set_coarse_tc(kv.second, on);
-        c->coarse_tc = on != 0;
+        c->coarse_tc = on == 1 || on == 2;
+        c->coarse_interp_tc = on == 1 || on == 3;
         AllocStreamScope as(c->st);
         coarse_tc_buffers(c, c->c32);
         bind_geom(c);
@@ -3884,7 +3887,7 @@ smob_status smob_set_multi_shared_pairs(smob_ctx* c, int on) {
 smob_status smob_coarse_tc_info(const smob_ctx* c, int* on) {
     return guarded([&]() -> smob_status {
         need(c && on, "null argument");
-        *on = c->coarse_tc ? 1 : 0;
+        *on = c->coarse_tc ? (c->coarse_interp_tc ? 1 : 2) : (c->coarse_interp_tc ? 3 : 0);
         return SMOB_OK;
     });
 }

@@ -176,7 +176,7 @@ struct DevGeom {
     int pmax;             // largest SH order present (sizes shared memory of the per-sphere kernels)
     int near_lanes;       // lanes per target point in the near-field kernel (1, 2, 4 or 8)
     int near_tc;          // FP32 near field on the tensor cores (k_near_eval_tc, tiled sets); 0: SIMT kernel
-    int coarse_tc;        // FP32 coarse strengths and coarse-target interpolation on the tensor cores
+    int coarse_tc;        // FP32 coarse-target interpolation on the tensor cores (k_ct_interp_tc)
     // FP32 sphere operator with the Legendre stage on the tensor cores (k_legendre_tc; 0: one SIMT kernel):
     // tiles {order p, first entry of leg_sph, spheres (<= 21), 0} of spheres of one order; B operand
     // tables per (p, m), forward and inverse, at leg_off[2 (p (kMaxOrder + 1) + m) + {0, 1}] floats into
