@@ -606,7 +606,8 @@ def run_serving(args, world, rank, local, dist):
     warm_orders(warm)
     t_warm = time.perf_counter() - t_warm
 
-    def serve(reqs, precision, slots, small_sms=0, graphs=False):
+    def serve(reqs, precision, slots, small_sms=0, graphs=None):
+        graphs = args.server_graphs if graphs is None else graphs
         srv = SolveServer(device=local, max_slots=slots, precision=precision, hbm_budget_bytes=args.hbm_budget,
                           small_sms=small_sms, graphs=graphs)
         part = srv.partition_info()
@@ -1015,6 +1016,9 @@ def main():
                          "stream priorities by size only)")
     ap.add_argument("--serve-log", default="",
                     help="cfg5: write one JSON line per request (size, queue and run times) to this file")
+    ap.add_argument("--server-graphs", type=int, default=0, choices=[0, 1, 2],
+                    help="cfg5: CUDA graphs in request contexts: 0 none (eager launches, the default: "
+                         "the lowest small-request latency), 1 all, 2 big requests")
     ap.add_argument("--compare-partition", type=int, default=0, metavar="SMS",
                     help="cfg5: also serve the stream with this many SMs reserved for small requests (without a "
                          "partition when --small-sms is set)")

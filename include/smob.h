@@ -289,7 +289,8 @@ typedef struct {
     int max_iters;           /* GMRES iteration limit per request */
     int precision;           /* smob_precision of every request */
     double inner_tol;        /* MIXED inner tolerance (<= 0: library default) */
-    int graphs;              /* CUDA graphs in the request contexts: 0 off, 1 on (see smob_set_graphs) */
+    int graphs;              /* CUDA graphs in the request contexts: 0 off, 1 on, 2 big requests only
+                                (see smob_set_graphs) */
 } smob_server_opts;
 typedef struct {
     int state;               /* 0 queued, 1 on the GPU, 2 done */

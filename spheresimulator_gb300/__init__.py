@@ -395,10 +395,11 @@ class SolveServer:
     def __init__(self, device=0, max_slots=8, hbm_budget_bytes=0.0, restart=50, max_iters=2000,
                  precision=PREC_MIXED, inner_tol=0.0, small_sms=0, graphs=False):
         """small_sms > 0: SMs reserved (green context) for small requests while big ones run;
-        graphs: CUDA graphs in the request contexts (each solves once, so capturing costs more than it saves)"""
+        graphs: CUDA graphs in the request contexts: False/0 none (each solves once), True/1 all, 2 big
+        requests only"""
         self._L = N.lib()
         opts = N.ServerOpts(int(device), int(max_slots), float(hbm_budget_bytes), int(restart), int(max_iters),
-                            int(precision), float(inner_tol), int(bool(graphs)))
+                            int(precision), float(inner_tol), int(graphs))
         h = ctypes.c_void_p()
         N.check(self._L.smob_server_create(ctypes.byref(h), ctypes.byref(opts)))
         self._h = h

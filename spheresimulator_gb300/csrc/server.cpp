@@ -173,8 +173,9 @@ struct smob_server {
         void* green = r->route == 1 ? static_cast<void*>(g_small) : (r->route == 2 ? static_cast<void*>(g_big) : nullptr);
         smob_status s = smob::create_context(&ctx, &g, opts.device, rank, green);
         r->t_ctx = now();
-        // a request context solves once: capturing its graphs would cost more than replaying them saves
-        if (s == SMOB_OK && !opts.graphs) s = smob_set_graphs(ctx, 0);
+        // a request context solves once: capturing its graphs costs a small request more than replaying
+        // them saves; a big one gains from the one-launch solve (graphs 2: big requests only)
+        if (s == SMOB_OK && (opts.graphs == 0 || (opts.graphs == 2 && r->small))) s = smob_set_graphs(ctx, 0);
         if (s == SMOB_OK) {
             smob_solve_opts o{r->tol, opts.restart, opts.max_iters, opts.precision, SMOB_WARM_NONE, opts.inner_tol, 0};
             r->vel.assign(6 * r->n, 0.0);
