@@ -1027,6 +1027,16 @@ void coarse_tc_buffers(smob_ctx* c, smob_ctx::CoarseHost& h) {
     CUDA_OK(cudaMemsetAsync(h.d_ctile_count.p, 0, h.d_ctile_count.bytes, c->st));
 }
 
+// Nodes of an entry's next far-field work block with rem nodes left: the cap while rem fills it, else
+// a power of two from floor up, taken whole if rem fills at least 3/4 of it (one CTA with a few idle
+// nodes), else its half (a full block; the rest in smaller ones).
+int ct_block_nodes(int rem, int cap, int floor) {
+    if (rem >= cap) return cap;
+    int hi = floor;
+    while (hi < rem) hi <<= 1;
+    return (hi == floor || 4 * rem >= 3 * hi) ? hi : hi >> 1;
+}
+
 void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>& nodes, std::vector<int>& node_off,
                       std::vector<char>& have_nodes) {
     const int N = c->N;
@@ -1155,7 +1165,7 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     // spheres whose pair may take that level (tgt_level on the device, in FP32 from FP32 centres:
     // listed here in FP64 with a margin of kCtRuleSlack orders on both sides of each level boundary,
     // so a pair near a boundary is a candidate of both levels and the device check picks one). Work
-    // items: node blocks of 128, 64 or 32 threads x candidate ranges of about kCtSrcPoints source points.
+    // items: node blocks (ct_block_nodes) x candidate ranges of about kCtSrcPoints source points.
     constexpr double kCtRuleSlack = 1e-3;
     constexpr int kCtSrcPoints = 512;
     h.ctent.clear();
@@ -1225,8 +1235,9 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
             h.ctent.push_back(e);
             if (l >= 0) h.ctused[(size_t)t * kCoarseLevels + l] = 1;
             for (int k0 = 0, rem = e.n; rem > 0 && e.nchunks > 0;) {
-                // float-float set: 64 nodes per CTA (two per thread of kFarThreadsDF)
-                const int w = h.hp ? 2 * kFarThreadsDF : (rem > 96 ? 128 : (rem > 32 ? 64 : 32));
+                // FP32: blocks of 128 ... 8 nodes on kFarThreads threads; float-float: 64 ... 4 nodes
+                // (two per thread of kFarThreadsDF); the rest of the CTA takes slices of the sources
+                const int w = h.hp ? ct_block_nodes(rem, 2 * kFarThreadsDF, 4) : ct_block_nodes(rem, kFarThreads, 8);
                 const int nb = std::min(w, rem);
                 for (int ci = 0; ci < e.nchunks; ++ci) {
                     h.ct_work.push_back(CtWork{ei, k0, nb, w, chunks[ci].first, chunks[ci].second, ci, 0});

@@ -1450,10 +1450,13 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
 }
 
 // The fused float-float pass with the float-float set's coarse targets: one CTA of kFarThreadsDF
-// threads per work item, nodes [k0, k0 + 64) of an entry (coarse nodes of level l, or the sphere's
-// grid points for l = -1), two per thread as the packed lanes of df_pair, against the entry's
-// candidates as k_ct_classify resolved them (float-float coarse level or grid). Partial sums
-// [chunk][node][6] (traction, single layer).
+// threads per work item, nodes [k0, k0 + nb) of an entry (coarse nodes of level l, or the sphere's
+// grid points for l = -1), against the entry's candidates as k_ct_classify resolved them (float-float
+// coarse level or grid). A block of w nodes (w = 64, 32, ..., 4) runs as w / 2 threads holding two
+// nodes each, the packed lanes of df_pair, times 64 / w slices: slice i takes every (64 / w)-th staged
+// source, and the slices' float-float sums are added in slice order. So an entry's last few nodes
+// cost a fraction of a CTA, not a whole 64-node one. Partial sums [chunk][node][6] (traction, single
+// layer).
 __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     k_far_df_ct(DevGeom g, const CtWork* __restrict__ works, const float4* __restrict__ src,
                 double* __restrict__ partial) {
@@ -1465,11 +1468,13 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     __shared__ float4 sph[kFarTile], spl[kFarTile], sfh[kFarTile], sfl[kFarTile];
     const bool grid = e.l < 0;  // CTA-uniform
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int hw = w.w >> 1, nslice = NT / hw;  // threads per slice, slices
+    const int j = threadIdx.x % hw, slice = threadIdx.x / hw;
     float4 PH[2], PL[2], NH[2], NL[2];
     bool val[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const int node = threadIdx.x + h * NT;
+        const int node = j + h * hw;
         val[h] = node < w.nb;
         const int cn = e.q0 + w.k0 + node;
         // an empty slot sits 1e18 away: its terms are finite (and not written)
@@ -1486,6 +1491,7 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
     acc.xh = acc.xl = acc.yh = acc.yl = acc.zh = acc.zl = f2(0.f, 0.f);
     acc.sxh = acc.sxl = acc.syh = acc.syl = acc.szh = acc.szl = f2(0.f, 0.f);
     const float2 one = f2(1.f, 1.f);
+    __shared__ float2 red[12][NT];
     for (int i = w.sa; i < w.sb; ++i) {
         const int2 cc = cs.ctcand[i];  // CTA-uniform
         if (cc.y == 0) continue;       // a boundary candidate of a neighbouring level
@@ -1504,13 +1510,33 @@ __global__ void __launch_bounds__(kFarThreadsDF, 384 / kFarThreadsDF)
                 sfl[k] = QF[2 * (g0 + base + k) + 1];
             }
             __syncthreads();
-            for (int k = 0; k < n; ++k) df_pair<2>(tx, ty, tz, n0, n1, n2, sph[k], spl[k], sfh[k], sfl[k], false, one, acc);
+            for (int k = slice; k < n; k += nslice)
+                df_pair<2>(tx, ty, tz, n0, n1, n2, sph[k], spl[k], sfh[k], sfl[k], false, one, acc);
+        }
+    }
+    if (nslice > 1) {  // CTA-uniform
+        red[0][threadIdx.x] = acc.xh, red[1][threadIdx.x] = acc.xl;
+        red[2][threadIdx.x] = acc.yh, red[3][threadIdx.x] = acc.yl;
+        red[4][threadIdx.x] = acc.zh, red[5][threadIdx.x] = acc.zl;
+        red[6][threadIdx.x] = acc.sxh, red[7][threadIdx.x] = acc.sxl;
+        red[8][threadIdx.x] = acc.syh, red[9][threadIdx.x] = acc.syl;
+        red[10][threadIdx.x] = acc.szh, red[11][threadIdx.x] = acc.szl;
+        __syncthreads();
+        if (slice != 0) return;
+        for (int sl = 1; sl < nslice; ++sl) {
+            const int t = j + sl * hw;
+            df_acc(acc.xh, acc.xl, df2{red[0][t], red[1][t]});
+            df_acc(acc.yh, acc.yl, df2{red[2][t], red[3][t]});
+            df_acc(acc.zh, acc.zl, df2{red[4][t], red[5][t]});
+            df_acc(acc.sxh, acc.sxl, df2{red[6][t], red[7][t]});
+            df_acc(acc.syh, acc.syl, df2{red[8][t], red[9][t]});
+            df_acc(acc.szh, acc.szl, df2{red[10][t], red[11][t]});
         }
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         if (!val[h]) continue;
-        double* o = partial + e.poff + 6LL * ((long long)w.chunk * e.n + w.k0 + threadIdx.x + h * NT);
+        double* o = partial + e.poff + 6LL * ((long long)w.chunk * e.n + w.k0 + j + h * hw);
         o[0] = h ? double(acc.xh.y) + double(acc.xl.y) : double(acc.xh.x) + double(acc.xl.x);
         o[1] = h ? double(acc.yh.y) + double(acc.yl.y) : double(acc.yh.x) + double(acc.yl.x);
         o[2] = h ? double(acc.zh.y) + double(acc.zl.y) : double(acc.zh.x) + double(acc.zl.x);

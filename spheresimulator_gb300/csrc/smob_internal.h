@@ -156,9 +156,9 @@ struct CtEnt {
     long long pad;
 };
 
-// one coarse-target work item: nodes [k0, k0 + nb) of entry ent with w threads per slice (32, 64 or
-// 128; 128 / w slices share the sources; float-float set: 64 nodes, two per thread) against candidates
-// [sa, sb) of the entry, partial chunk
+// one coarse-target work item: nodes [k0, k0 + nb) of entry ent in a block of w nodes (FP32: 128 ... 8,
+// one per thread of a slice, 128 / w slices share the sources; float-float set: 64 ... 4, two per thread,
+// 64 / w slices) against candidates [sa, sb) of the entry, partial chunk
 struct CtWork {
     int ent, k0, nb, w;
     int sa, sb, chunk, pad;
