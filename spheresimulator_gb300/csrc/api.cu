@@ -2840,8 +2840,8 @@ struct CtxScope {
     explicit CtxScope(const smob_ctx* c) : alloc((set_device(c), c->st)) {}
 };
 
-// the context's main and side streams (non-blocking, priority prio: 0 is the default) and the
-// fork/join events of the operator passes
+// the context's main and side streams (non-blocking, priorities prio and far_prio: 0 is the default)
+// and the fork/join events of the operator passes
 // cuGreenCtxStreamCreate, reached through the runtime (the library does not link libcuda)
 using GreenStreamFn = int (*)(void** stream, void* green_ctx, unsigned flags, int priority);
 GreenStreamFn green_stream_fn() {
@@ -2860,19 +2860,19 @@ GreenStreamFn green_stream_fn() {
 
 // green: a green context (an SM partition of the device, CUgreenCtx) whose streams the context runs on,
 // or null for ordinary streams (the whole device)
-void create_streams(smob_ctx* c, int prio, void* green = nullptr) {
+void create_streams(smob_ctx* c, int prio, int far_prio, void* green = nullptr) {
     if (green) {
         GreenStreamFn fn = green_stream_fn();
         if (!fn) throw SmobError(SMOB_ERR_CUDA, "cuGreenCtxStreamCreate is not available");
         void* a = nullptr;
         void* b = nullptr;
-        if (fn(&a, green, 0x1 /* CU_STREAM_NON_BLOCKING */, prio) != 0 || fn(&b, green, 0x1, prio) != 0)
+        if (fn(&a, green, 0x1 /* CU_STREAM_NON_BLOCKING */, prio) != 0 || fn(&b, green, 0x1, far_prio) != 0)
             throw SmobError(SMOB_ERR_CUDA, "cuGreenCtxStreamCreate failed");
         c->st = static_cast<cudaStream_t>(a);
         c->st2 = static_cast<cudaStream_t>(b);
     } else {
         CUDA_OK(cudaStreamCreateWithPriority(&c->st, cudaStreamNonBlocking, prio));
-        CUDA_OK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, prio));
+        CUDA_OK(cudaStreamCreateWithPriority(&c->st2, cudaStreamNonBlocking, far_prio));
     }
     c->sh.st = c->st;
     c->sh2.st = c->st2;
@@ -3030,13 +3030,17 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
         std::unique_ptr<smob_ctx> c(new smob_ctx);
         c->device = device;
         CUDA_OK(cudaSetDevice(device));
-        int prio = 0;
+        int least = 0, greatest = 0;
+        CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        int prio = 0, far_prio = 0;
         if (priority_rank >= 0) {
-            int least = 0, greatest = 0;
-            CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-            prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
+            prio = far_prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
+        } else {
+            // the main stream's chain of small sphere and near-field kernels goes first; the far field's
+            // many CTAs fill the SMs that chain leaves free
+            prio = std::max(greatest, far_prio - 1);
         }
-        create_streams(c.get(), prio, green_ctx);
+        create_streams(c.get(), prio, far_prio, green_ctx);
         AllocStreamScope scope(c->st);
         configure_sphere_kernels();
         configure_near_kernels();
@@ -3451,7 +3455,9 @@ smob_ctx* replicated(smob_ctx* c, int k) {
     r->near_tc = c->near_tc;  // the same near and sphere kernels as the single solves (results equal column
     r->sph_tc = c->sph_tc;    // by column)
     CUDA_OK(cudaSetDevice(c->device));
-    create_streams(r.get(), 0);
+    int least = 0, greatest = 0;
+    CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    create_streams(r.get(), std::max(greatest, -1), 0);  // the priorities of a default context
     AllocStreamScope scope(r->st);
     build_context(r.get(), &geo);
     if (shared) {
