@@ -369,6 +369,7 @@ struct smob_ctx {
         L.problems = d_problems.as<Problem>();
         L.P = P;
         L.partial = d_partial_red.as<double>();
+        L.partial_cap = (long long)(d_partial_red.bytes / sizeof(double));
         L.counters = d_red_count.as<unsigned>();
         L.cstride = red_cstride;
         return L;
@@ -1814,7 +1815,8 @@ void ensure_solver(smob_ctx* c, int m) {
         c->d_cs.alloc(sizeof(double) * c->P * m);
         c->d_sn.alloc(sizeof(double) * c->P * m);
         c->d_y.alloc(sizeof(double) * c->P * m);
-        c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * (m + 1));
+        // dots of up to m + 1 vectors per chunk; the fused update-norm step's kElemBlocks per chunk
+        c->d_partial_red.alloc(sizeof(double) * c->chunks.size() * std::max(m + 1, kElemBlocks));
         alloc_red_counters(c, m + 1);
         c->restart_cap = m;
     }
@@ -2424,11 +2426,12 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
         for (int pass = 0; pass < 2; ++pass) {
             check_launch(c, launch_dots(L, V, (long long)n, j + 1, w, act, hscr, m, 0, false, false, st, Hcol, hs,
                                         pass == 1));
-            check_launch(c, launch_update(L, V, (long long)n, j + 1, nullptr, hscr, m, -1.0, act, w, st));
+            if (pass == 0) check_launch(c, launch_update(L, V, (long long)n, j + 1, nullptr, hscr, m, -1.0, act, w, st));
         }
-        check_launch(c, launch_dots(L, w, 0, 1, w, act, c->d_hn.as<double>(), 1, 0, false, true, st));
-        check_launch(c, launch_givens(L, j, m, ks, c->d_H.as<double>(), c->d_g.as<double>(), c->d_cs.as<double>(),
-                                      c->d_sn.as<double>(), c->d_hn.as<double>(), act, maxit, st));
+        // second update, |w| and the Givens step in one kernel
+        check_launch(c, launch_update_norm_givens(L, V, (long long)n, j + 1, hscr, m, act, w, c->d_hn.as<double>(), j, m,
+                                                  ks, c->d_H.as<double>(), c->d_g.as<double>(),
+                                                  c->d_cs.as<double>(), c->d_sn.as<double>(), maxit, st));
         if (j + 1 < m) check_launch(c, launch_scale(L, w, c->d_hn.as<double>(), 1, true, act, V + n * (j + 1), st));
     };
     // residual of the FP32-update problems (MIXED): r -= A32 dx on the problems already marked active

@@ -28,9 +28,10 @@ __device__ __forceinline__ double block_reduce(double v, double* red) {
 
 // Chunk dot products <A_i, b> with the final sum fused in: every CTA writes its chunk's partial, and
 // the last CTA of a (problem, vector) to finish (a counter per pair, after a memory fence) adds that
-// problem's partials in chunk order and writes out[p*ostride + ooff + i] (+)= sum (sqrt if take_sqrt;
-// optionally also out2), then resets the counter. The order of the final sum is fixed, so the result
-// does not depend on which CTA finishes last.
+// problem's partials (thread t every blockDim.x-th chunk from t on, then the block's fixed reduction
+// tree) and writes out[p*ostride + ooff + i] (+)= sum (sqrt if take_sqrt; optionally also out2), then
+// resets the counter. The order of the final sum is fixed, so the result does not depend on which CTA
+// finishes last.
 __global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* __restrict__ A, long long lda,
                              const double* __restrict__ b, const unsigned char* __restrict__ active,
                              double* __restrict__ partial, int nchunks, const Problem* __restrict__ probs,
@@ -45,15 +46,22 @@ __global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* 
     double s = 0;
     for (long long l = ch.l0 + threadIdx.x; l < ch.l1; l += blockDim.x) s = fma(a[l], b[l], s);
     s = block_reduce(s, red);
-    if (threadIdx.x != 0) return;
-    partial[(long long)i * nchunks + blockIdx.x] = s;
-    __threadfence();
+    __shared__ int last;
     const Problem pr = probs[ch.problem];
     unsigned* cnt = counters + (long long)ch.problem * cstride + i;
-    if (atomicAdd(cnt, 1u) != (unsigned)(pr.c1 - pr.c0 - 1)) return;
+    if (threadIdx.x == 0) {
+        partial[(long long)i * nchunks + blockIdx.x] = s;
+        __threadfence();
+        last = atomicAdd(cnt, 1u) == (unsigned)(pr.c1 - pr.c0 - 1);
+    }
+    __syncthreads();
+    if (!last) return;  // CTA-uniform
     // the last chunk of this (problem, vector): every partial is written
+    __threadfence();
     double t = 0;
-    for (int c = pr.c0; c < pr.c1; ++c) t += __ldcg(partial + (long long)i * nchunks + c);
+    for (int c = pr.c0 + threadIdx.x; c < pr.c1; c += blockDim.x) t += __ldcg(partial + (long long)i * nchunks + c);
+    t = block_reduce(t, red);
+    if (threadIdx.x != 0) return;
     *cnt = 0u;
     if (take_sqrt) t = sqrt(t);
     double* o = out + ostride * ch.problem + ooff + i;
@@ -66,8 +74,6 @@ __global__ void k_chunk_dots(const VecChunk* __restrict__ chunks, const double* 
 
 // Elementwise kernels: grid (chunk, kElemBlocks), one element per thread, so a small problem's
 // few chunks still spread over the whole GPU. Per element the arithmetic is independent of the grid.
-constexpr int kElemThreads = 256;
-constexpr int kElemBlocks = kVecChunk / kElemThreads;
 
 // w[l] += sign * sum_{i < n_p} h[p*hstride + i] * V[i*ldv + l]
 __global__ void k_chunk_update(const VecChunk* __restrict__ chunks, const double* __restrict__ V, long long ldv,
@@ -120,16 +126,15 @@ __global__ void k_cycle_init(int P, int m, const unsigned char* __restrict__ in_
     ks[p].kcount = 0;
 }
 
-__global__ void k_givens(int P, int j, int m, KrylovState* __restrict__ ks, double* __restrict__ H,
-                         double* __restrict__ gv, double* __restrict__ cs, double* __restrict__ sn,
-                         const double* __restrict__ hnorm, unsigned char* __restrict__ active, int maxit) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P || !active[p]) return;
+// Givens step of column j for problem p: rotate H[:, j] by the previous rotations, make the new one
+// from (H[j, j], hn), update g and the per-problem stop test
+__device__ void givens_one(int p, int j, int m, KrylovState* __restrict__ ks, double* __restrict__ H,
+                           double* __restrict__ gv, double* __restrict__ cs, double* __restrict__ sn, double hn,
+                           unsigned char* __restrict__ active, int maxit) {
     double* Hc = H + (long long)p * m * (m + 1) + (long long)j * (m + 1);
     double* c = cs + (long long)p * m;
     double* s = sn + (long long)p * m;
     double* g = gv + (long long)p * (m + 1);
-    const double hn = hnorm[p];
     Hc[j + 1] = hn;
     for (int i = 0; i < j; ++i) {
         const double a = Hc[i], b = Hc[i + 1];
@@ -152,6 +157,66 @@ __global__ void k_givens(int P, int j, int m, KrylovState* __restrict__ ks, doub
     const bool finite = isfinite(g[j + 1]) && isfinite(hn);
     if (!finite) k.nonfinite = 1;
     if (!finite || fabs(g[j + 1]) < k.tol_abs || hn == 0.0 || j + 1 == m || k.iters >= maxit) active[p] = 0;
+}
+
+__global__ void k_givens(int P, int j, int m, KrylovState* __restrict__ ks, double* __restrict__ H,
+                         double* __restrict__ gv, double* __restrict__ cs, double* __restrict__ sn,
+                         const double* __restrict__ hnorm, unsigned char* __restrict__ active, int maxit) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P || !active[p]) return;
+    givens_one(p, j, m, ks, H, gv, cs, sn, hnorm[p], active, maxit);
+}
+
+// w[l] -= sum_{i < nvec} h[p*hstride + i] * V[i*ldv + l] (the arithmetic of k_chunk_update), then |w|^2
+// per CTA into partial[chunk * kElemBlocks + blockIdx.y]; the last CTA of a problem (a counter per
+// problem, after a memory fence) adds the problem's partials, thread t taking every kElemThreads-th one
+// from t on, then the block's fixed reduction tree; thread 0 writes hnorm[p] = sqrt of the sum, resets
+// the counter and runs the Givens step of column j. The final sum's order is fixed, so the result does
+// not depend on which CTA finishes last.
+__global__ void __launch_bounds__(kElemThreads)
+    k_chunk_update_norm_givens(const VecChunk* __restrict__ chunks, const Problem* __restrict__ probs,
+                               const double* __restrict__ V, long long ldv, int nvec, const double* __restrict__ h,
+                               long long hstride, unsigned char* __restrict__ active, double* __restrict__ w,
+                               double* __restrict__ partial, unsigned* __restrict__ counters, int cstride,
+                               double* __restrict__ hnorm, int j, int m, KrylovState* __restrict__ ks,
+                               double* __restrict__ H, double* __restrict__ gv, double* __restrict__ cs,
+                               double* __restrict__ sn, int maxit) {
+    __shared__ double red[kElemThreads / 32];
+    const VecChunk ch = chunks[blockIdx.x];
+    if (!active[ch.problem]) return;  // CTA-uniform
+    const long long l = ch.l0 + (long long)blockIdx.y * kElemThreads + threadIdx.x;
+    double sq = 0;
+    if (l < ch.l1) {
+        const double* hp = h + hstride * ch.problem;
+        double s = 0;
+        for (int i = 0; i < nvec; ++i) s = fma(hp[i], V[ldv * i + l], s);
+        const double v = fma(-1.0, s, w[l]);
+        w[l] = v;
+        sq = v * v;
+    }
+    sq = block_reduce(sq, red);
+    __shared__ int last;
+    const Problem pr = probs[ch.problem];
+    unsigned* cnt = counters + (long long)ch.problem * cstride;
+    if (threadIdx.x == 0) {
+        partial[(long long)blockIdx.x * kElemBlocks + blockIdx.y] = sq;
+        __threadfence();
+        last = atomicAdd(cnt, 1u) == (unsigned)((pr.c1 - pr.c0) * kElemBlocks - 1);
+    }
+    __syncthreads();
+    if (!last) return;  // CTA-uniform
+    // the last CTA of this problem: every partial is written
+    __threadfence();
+    double t = 0;
+    for (long long q = (long long)pr.c0 * kElemBlocks + threadIdx.x; q < (long long)pr.c1 * kElemBlocks;
+         q += kElemThreads)
+        t += __ldcg(partial + q);
+    t = block_reduce(t, red);
+    if (threadIdx.x != 0) return;
+    *cnt = 0u;
+    const double hn = sqrt(t);
+    hnorm[ch.problem] = hn;
+    givens_one(ch.problem, j, m, ks, H, gv, cs, sn, hn, active, maxit);
 }
 
 __global__ void k_trisolve(int P, int m, const unsigned char* __restrict__ in_cycle, const KrylovState* __restrict__ ks,
@@ -383,6 +448,17 @@ int launch_axpby_seg(const KrylovLaunch& L, double a, const double* x, double b,
 int launch_cycle_init(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const double* beta, KrylovState* ks,
                       double* H, double* g, cudaStream_t st) {
     k_cycle_init<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, m, in_cycle, beta, ks, H, g);
+    return 1;
+}
+
+int launch_update_norm_givens(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const double* h,
+                              long long hstride, unsigned char* active, double* w, double* hnorm, int j, int m,
+                              KrylovState* ks, double* H, double* g, double* cs, double* sn, int maxit,
+                              cudaStream_t st) {
+    if ((long long)L.nchunks * kElemBlocks > L.partial_cap || L.cstride < 1) return -1;
+    k_chunk_update_norm_givens<<<dim3(L.nchunks, kElemBlocks), kElemThreads, 0, st>>>(
+        L.chunks, L.problems, V, ldv, nvec, h, hstride, active, w, L.partial, L.counters, L.cstride, hnorm, j, m, ks,
+        H, g, cs, sn, maxit);
     return 1;
 }
 

@@ -21,12 +21,17 @@ struct KrylovState {
     int nonfinite;     // NaN/Inf met
 };
 
+// elementwise kernels: grid (chunk, kElemBlocks) of kElemThreads threads, one element per thread
+constexpr int kElemThreads = 256;
+constexpr int kElemBlocks = kVecChunk / kElemThreads;
+
 struct KrylovLaunch {
     const VecChunk* chunks;
     int nchunks;
     const Problem* problems;
     int P;
     double* partial;  // nchunks * max_nvec
+    long long partial_cap;  // doubles in partial
     unsigned* counters;  // P * cstride, zero between launches (launch_dots' last chunk of each sum resets it)
     int cstride;         // counters per problem (the most vectors one launch_dots may take)
 };
@@ -47,6 +52,13 @@ int launch_cycle_init(const KrylovLaunch& L, int m, const unsigned char* in_cycl
                       double* H, double* g, cudaStream_t st);
 int launch_givens(const KrylovLaunch& L, int j, int m, KrylovState* ks, double* H, double* g, double* cs, double* sn,
                   const double* hnorm, unsigned char* active, int maxit, cudaStream_t st);
+// The second CGS2 update of an Arnoldi step fused with what follows it: w -= V h (as launch_update
+// with sign -1), |w| into hnorm, and the Givens step of column j (launch_givens), the last two by the
+// last CTA of each problem. Needs nchunks * kElemBlocks partials; returns -1 if L.partial is smaller.
+int launch_update_norm_givens(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const double* h,
+                              long long hstride, unsigned char* active, double* w, double* hnorm, int j, int m,
+                              KrylovState* ks, double* H, double* g, double* cs, double* sn, int maxit,
+                              cudaStream_t st);
 int launch_trisolve(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const KrylovState* ks, const double* H,
                     const double* g, double* y, int* kc, cudaStream_t st);
 
