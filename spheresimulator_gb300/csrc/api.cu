@@ -1346,8 +1346,17 @@ void build_coarse_set(smob_ctx* c, smob_ctx::CoarseHost& h, std::vector<double>&
     h.d_cdesc_tc.upload(h.cdesc_tc);
     h.d_cgrp.upload(h.cgrp);
     h.d_gent.upload(h.gent);
-    if (h.hp) h.d_cmap.upload(mapsd);
-    else h.d_cmap.upload(maps);
+    if (h.hp) {
+        // the float-float strength GEMM's maps as (hi, lo) float pairs
+        std::vector<float2> mapsf2(mapsd.size());
+        for (size_t i = 0; i < mapsd.size(); ++i) {
+            const float hi = float(mapsd[i]);
+            mapsf2[i] = make_float2(hi, float(mapsd[i] - double(hi)));
+        }
+        h.d_cmap.upload(mapsf2);
+    } else {
+        h.d_cmap.upload(maps);
+    }
     if (!h.hp) {
         // The tensor-core strength GEMM's A operand, prepared once per geometry: per map group, per M
         // tile of 128 coarse nodes and K chunk of 32 fine nodes, the transposed map's block split into
@@ -1509,7 +1518,7 @@ void bind_geom(smob_ctx* c) {
         cs.cpos32 = h.d_cpos32.as<float4>();
         cs.cpos32lo = h.hp ? h.d_cpos32lo.as<float4>() : nullptr;
         cs.cmap = h.hp ? nullptr : h.d_cmap.as<float>();
-        cs.cmapd = h.hp ? h.d_cmap.as<double>() : nullptr;
+        cs.cmapf2 = h.hp ? h.d_cmap.as<float2>() : nullptr;
         cs.csrc = h.d_csrc.as<float4>();
         cs.crep = c->nrep > 1 ? h.ncoarse / c->nrep : h.ncoarse;
         cs.ncdesc = (int)h.cdesc.size();

@@ -469,17 +469,20 @@ __global__ void __launch_bounds__(128) k_coarse_src_tc(DevGeom g, const float4* 
     }
 }
 
-// The float-float set's strengths: the same GEMM tiles in FP64 (maps in FP64, sources hi + lo), two
-// split-K groups of 128 threads; each strength is stored as a hi/lo float pair like the grid sources.
+// The float-float set's strengths: the same GEMM tiles in float-float arithmetic on the FP32 pipes
+// (the FP64 pipe issues 1/58 of their rate): maps stored as (hi, lo) float pairs, sources as the hi/lo
+// float4 pairs of the grid, products by df_mul_u and sums by df_acc (~2^-44 relative to the sum of
+// |terms|), two split-K groups of 128 threads added as float-float pairs; each strength is stored as a
+// normalised hi/lo float pair like the grid sources.
 constexpr int kCgGroupsD = 2;
 __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, const float4* __restrict__ src2) {
     const CoarseSet& cs = g.cshp;
     const int4 d = cs.cdesc[blockIdx.x];
     const int4 G = cs.cgrp[d.x];
     const int k0 = d.y, ne = d.w, ng = G.y, cnt = G.z;
-    __shared__ double Ms[kCgGroupsD][kCgK][kCgNodes];
-    __shared__ double4_32a Fs[kCgGroupsD][kCgK][kCgSph];
-    __shared__ double red[kCgGroupsD - 1][3 * kCgNi][128];
+    __shared__ float2 Ms[kCgGroupsD][kCgK][kCgNodes];
+    __shared__ float4 Fh[kCgGroupsD][kCgK][kCgSph], Fl[kCgGroupsD][kCgK][kCgSph];
+    __shared__ float2 red[kCgGroupsD - 1][3 * kCgNi][128];
     __shared__ int sbase[kCgSph], sout[kCgSph];
     __shared__ unsigned char sact[kCgSph];
     const int grp = threadIdx.x >> 7, t = threadIdx.x & 127;
@@ -498,37 +501,38 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
     }
     __syncthreads();
     const int si = t >> 4, ni = t & 15;
-    double acc[kCgNi][3];
+    float ah[kCgNi][3], al[kCgNi][3];
 #pragma unroll
-    for (int i = 0; i < kCgNi; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.0;
-    const double* __restrict__ map = cs.cmapd + G.x;
+    for (int i = 0; i < kCgNi; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ah[i][c] = al[i][c] = 0.f;
+    const float2* __restrict__ map = cs.cmapf2 + G.x;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int jb = 0; jb < ng; jb += kCgK * kCgGroupsD) {
         const int j0 = jb + grp * kCgK;
 #pragma unroll
         for (int r = 0; r < kCgK * kCgNodes / 128; ++r) {
             const int idx = t + 128 * r, jj = idx / kCgNodes, kk = idx % kCgNodes;
-            Ms[grp][jj][kk] =
-                (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk) : 0.0;
+            Ms[grp][jj][kk] = (j0 + jj < ng && k0 + kk < cnt) ? __ldg(map + (long long)(j0 + jj) * cnt + k0 + kk)
+                                                              : make_float2(0.f, 0.f);
         }
         if (t < kCgK * kCgSph) {
             const int jj = t / kCgSph, ss = t % kCgSph;
-            double4_32a f = make_double4_32a(0, 0, 0, 0);
-            if (j0 + jj < ng && ss < ne) {
-                const float4 h = src2[2LL * (sbase[ss] + j0 + jj)], l = src2[2LL * (sbase[ss] + j0 + jj) + 1];
-                f = make_double4_32a(double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z), 0.0);
-            }
-            Fs[grp][jj][ss] = f;
+            const bool in = j0 + jj < ng && ss < ne;
+            Fh[grp][jj][ss] = in ? src2[2LL * (sbase[ss] + j0 + jj)] : z4;
+            Fl[grp][jj][ss] = in ? src2[2LL * (sbase[ss] + j0 + jj) + 1] : z4;
         }
         __syncthreads();
 #pragma unroll 4
         for (int jj = 0; jj < kCgK; ++jj) {
-            const double4_32a f = Fs[grp][jj][si];
+            const float4 fh = Fh[grp][jj][si], fl = Fl[grp][jj][si];
 #pragma unroll
             for (int i = 0; i < kCgNi; ++i) {
-                const double m = Ms[grp][jj][ni + 16 * i];
-                acc[i][0] = fma(m, f.x, acc[i][0]);
-                acc[i][1] = fma(m, f.y, acc[i][1]);
-                acc[i][2] = fma(m, f.z, acc[i][2]);
+                const float2 m = Ms[grp][jj][ni + 16 * i];
+                const df1 mm{m.x, m.y};
+                df_acc(ah[i][0], al[i][0], df_mul_u(mm, df1{fh.x, fl.x}));
+                df_acc(ah[i][1], al[i][1], df_mul_u(mm, df1{fh.y, fl.y}));
+                df_acc(ah[i][2], al[i][2], df_mul_u(mm, df1{fh.z, fl.z}));
             }
         }
         __syncthreads();
@@ -537,22 +541,28 @@ __global__ void __launch_bounds__(128 * kCgGroupsD) k_coarse_src_df(DevGeom g, c
 #pragma unroll
         for (int i = 0; i < kCgNi; ++i)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = acc[i][c];
+            for (int c = 0; c < 3; ++c) red[grp - 1][3 * i + c][t] = make_float2(ah[i][c], al[i][c]);
     }
     __syncthreads();
     if (grp == 0 && si < ne && sact[si]) {
 #pragma unroll
         for (int i = 0; i < kCgNi; ++i) {
+            float o[3], ol[3];
 #pragma unroll
-            for (int q = 0; q < kCgGroupsD - 1; ++q)
+            for (int c = 0; c < 3; ++c) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) acc[i][c] += red[q][3 * i + c][t];
+                for (int q = 0; q < kCgGroupsD - 1; ++q) {
+                    const float2 v = red[q][3 * i + c][t];
+                    df_acc(ah[i][c], al[i][c], df1{v.x, v.y});
+                }
+                const df1 s = two_sum(ah[i][c], al[i][c]);  // normalised: lo within half an ulp of hi
+                o[c] = s.h;
+                ol[c] = s.l;
+            }
             const int k = k0 + ni + 16 * i;
             if (k < cnt) {
-                const float hx = float(acc[i][0]), hy = float(acc[i][1]), hz = float(acc[i][2]);
-                cs.csrc[2LL * (sout[si] + k)] = make_float4(hx, hy, hz, 0.f);
-                cs.csrc[2LL * (sout[si] + k) + 1] = make_float4(float(acc[i][0] - double(hx)), float(acc[i][1] - double(hy)),
-                                                                float(acc[i][2] - double(hz)), 0.f);
+                cs.csrc[2LL * (sout[si] + k)] = make_float4(o[0], o[1], o[2], 0.f);
+                cs.csrc[2LL * (sout[si] + k) + 1] = make_float4(ol[0], ol[1], ol[2], 0.f);
             }
         }
     }

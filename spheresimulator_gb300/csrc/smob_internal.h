@@ -91,7 +91,7 @@ struct CoarseSet {
     const float4* cpos32;      // coarse points: x, y, z relative to the problem origin, w = sphere id bits
     const float4* cpos32lo;    // float-float set: the coordinates' low parts
     const float* cmap;         // FP32 set: coarse maps, [fine node][coarse node] per (p, pe)
-    const double* cmapd;       // float-float set: the same maps in FP64
+    const float2* cmapf2;      // float-float set: the same maps as (hi, lo) float pairs
     float4* csrc;              // strengths of the current pass (float-float set: hi, lo interleaved)
     int crep;                  // coarse points of one replica (several-RHS contexts; else all of them)
     // the strengths as small GEMMs, one per (p, pe) map: CTA tiles of kCoarseTileNodes coarse nodes x 8 spheres
