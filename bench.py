@@ -45,8 +45,8 @@ L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = ("cfg2: 64 spheres a=1, seeded RSA in box 20 (min gap 0.1), p=16 (36992 points), "
             "N(0,1) force/torque, GMRES(50) to 1e-8 relative residual")
 # DRAM bytes (read + write) of one FP32 traction far-field launch on this workload, from an ncu capture
-# (GB300, k_far32<1, 1> with coarse equivalent sources: 4,226,304 read, 0 written)
-CFG2_FAR32_DRAM_BYTES = 4346112
+# (GB300, k_far32_ct<1>, the entry kernel with coarse sources and targets: 4,364,032 read, 0 written)
+CFG2_FAR32_DRAM_BYTES = 4364032
 
 
 def dist_init():
