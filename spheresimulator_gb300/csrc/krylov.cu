@@ -159,14 +159,6 @@ __device__ void givens_one(int p, int j, int m, KrylovState* __restrict__ ks, do
     if (!finite || fabs(g[j + 1]) < k.tol_abs || hn == 0.0 || j + 1 == m || k.iters >= maxit) active[p] = 0;
 }
 
-__global__ void k_givens(int P, int j, int m, KrylovState* __restrict__ ks, double* __restrict__ H,
-                         double* __restrict__ gv, double* __restrict__ cs, double* __restrict__ sn,
-                         const double* __restrict__ hnorm, unsigned char* __restrict__ active, int maxit) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P || !active[p]) return;
-    givens_one(p, j, m, ks, H, gv, cs, sn, hnorm[p], active, maxit);
-}
-
 // w[l] -= sum_{i < nvec} h[p*hstride + i] * V[i*ldv + l] (the arithmetic of k_chunk_update), then |w|^2
 // per CTA into partial[chunk * kElemBlocks + blockIdx.y]; the last CTA of a problem (a counter per
 // problem, after a memory fence) adds the problem's partials, thread t taking every kElemThreads-th one
@@ -459,12 +451,6 @@ int launch_update_norm_givens(const KrylovLaunch& L, const double* V, long long 
     k_chunk_update_norm_givens<<<dim3(L.nchunks, kElemBlocks), kElemThreads, 0, st>>>(
         L.chunks, L.problems, V, ldv, nvec, h, hstride, active, w, L.partial, L.counters, L.cstride, hnorm, j, m, ks,
         H, g, cs, sn, maxit);
-    return 1;
-}
-
-int launch_givens(const KrylovLaunch& L, int j, int m, KrylovState* ks, double* H, double* g, double* cs, double* sn,
-                  const double* hnorm, unsigned char* active, int maxit, cudaStream_t st) {
-    k_givens<<<(L.P + 63) / 64, 64, 0, st>>>(L.P, j, m, ks, H, g, cs, sn, hnorm, active, maxit);
     return 1;
 }
 

@@ -50,10 +50,8 @@ int launch_axpby_seg(const KrylovLaunch& L, double a, const double* x, double b,
                      cudaStream_t st);
 int launch_cycle_init(const KrylovLaunch& L, int m, const unsigned char* in_cycle, const double* beta, KrylovState* ks,
                       double* H, double* g, cudaStream_t st);
-int launch_givens(const KrylovLaunch& L, int j, int m, KrylovState* ks, double* H, double* g, double* cs, double* sn,
-                  const double* hnorm, unsigned char* active, int maxit, cudaStream_t st);
 // The second CGS2 update of an Arnoldi step fused with what follows it: w -= V h (as launch_update
-// with sign -1), |w| into hnorm, and the Givens step of column j (launch_givens), the last two by the
+// with sign -1), |w| into hnorm, and the Givens step of column j (rotations, g, the stop test), the last two by the
 // last CTA of each problem. Needs nchunks * kElemBlocks partials; returns -1 if L.partial is smaller.
 int launch_update_norm_givens(const KrylovLaunch& L, const double* V, long long ldv, int nvec, const double* h,
                               long long hstride, unsigned char* active, double* w, double* hnorm, int j, int m,
