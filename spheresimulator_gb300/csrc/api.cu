@@ -2252,7 +2252,8 @@ bool run_loop_graph(smob_ctx* c, const LoopArgs& a, const SolveOps& ops, bool fu
                 });
             const cudaGraphNode_t wnode = append_loop(c, G, tail, a, lg, ops, true);
             if (full) append_final(c, G, {wnode}, lg, ops);
-            CUDA_OK(cudaGraphInstantiate(&lg.exec, G, 0));
+            // each kernel node keeps the priority of the stream it was captured on (main above far field)
+            CUDA_OK(cudaGraphInstantiate(&lg.exec, G, cudaGraphInstantiateFlagUseNodePriority));
             cudaGraphDestroy(G);
             c->launches = before;
         } catch (const SmobError&) {
@@ -2683,7 +2684,7 @@ smob_status solve_device(smob_ctx* c, const double* d_force, double* d_vel, doub
                         c->capturing = false;
                         CUDA_OK(cudaStreamEndCapture(st, &gr));
                         cudaGraphExec_t ex;
-                        CUDA_OK(cudaGraphInstantiate(&ex, gr, 0));
+                        CUDA_OK(cudaGraphInstantiate(&ex, gr, cudaGraphInstantiateFlagUseNodePriority));
                         cudaGraphDestroy(gr);
                         it = c->graphs.emplace(key, smob_ctx::Graph{ex, c->launches - before}).first;
                         c->launches = before;
@@ -3023,7 +3024,8 @@ smob_status smob_create(smob_ctx** out, const smob_geometry* geo, int device) {
 }  // extern "C"
 
 // Context creation with a stream priority: priority_rank 0 is the device's highest stream
-// priority, larger ranks step towards the lowest; -1 keeps the default. The server gives small
+// priority, larger ranks step towards the lowest (two steps per rank: the main stream, then the far
+// field's); -1 keeps the default (main stream one step above the far field's). The server gives small
 // requests high priority so their kernels are scheduled ahead of large requests' blocks.
 smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int device, int priority_rank,
                                  void* green_ctx) {
@@ -3044,12 +3046,16 @@ smob_status smob::create_context(smob_ctx** out, const smob_geometry* geo, int d
         CUDA_OK(cudaSetDevice(device));
         int least = 0, greatest = 0;
         CUDA_OK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        // The main stream's chain of small sphere and near-field kernels goes one step ahead of the far
+        // field's stream, whose many CTAs fill the SMs that chain leaves free. A ranked context (the
+        // server: 0 for its smallest requests) takes the pair of steps 2 rank, 2 rank + 1 from the
+        // device's greatest priority (numerically smallest), so every stream of a lower rank stays
+        // ahead of both of a higher one's.
         int prio = 0, far_prio = 0;
         if (priority_rank >= 0) {
-            prio = far_prio = std::min(least, greatest + priority_rank);  // greatest is numerically smallest
+            prio = std::min(least, greatest + 2 * priority_rank);
+            far_prio = std::min(least, greatest + 2 * priority_rank + 1);
         } else {
-            // the main stream's chain of small sphere and near-field kernels goes first; the far field's
-            // many CTAs fill the SMs that chain leaves free
             prio = std::max(greatest, far_prio - 1);
         }
         create_streams(c.get(), prio, far_prio, green_ctx);
