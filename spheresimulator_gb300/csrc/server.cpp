@@ -234,6 +234,10 @@ smob_status smob_server_create(smob_server** out, const smob_server_opts* o) {
         smob::set_last_error("server options: max_slots, restart and max_iters must be positive");
         return SMOB_ERR_ARG;
     }
+    if (o->graphs < 0 || o->graphs > 2) {
+        smob::set_last_error("server options: graphs must be 0 (none), 1 (all requests) or 2 (big requests)");
+        return SMOB_ERR_ARG;
+    }
     // Freed device memory stays in the device's stream-ordered pool instead of going back to the driver
     // at every synchronisation: requests allocate and free gigabytes while others run, and returning and
     // re-mapping that memory each time would stall the other requests' streams.

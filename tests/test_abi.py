@@ -103,3 +103,18 @@ def test_warm_orders_is_host_only():
     warm_orders([])
     with pytest.raises(SmobError):
         warm_orders([33])
+
+
+def test_server_options_are_checked_on_host():
+    """smob_server_create rejects bad options before it touches a device."""
+    from spheresimulator_gb300 import _native as N
+    L = N.lib()
+    srv = ctypes.c_void_p()
+    assert L.smob_server_create(ctypes.byref(srv), None) == N.SMOB_ERR_ARG
+    o = N.ServerOpts(device=0, max_slots=2, hbm_budget_bytes=0.0, restart=50, max_iters=200, precision=0,
+                     inner_tol=0.0, graphs=3)
+    assert L.smob_server_create(ctypes.byref(srv), ctypes.byref(o)) == N.SMOB_ERR_ARG
+    assert b"graphs" in L.smob_last_error()
+    o.graphs, o.max_slots = 0, 0
+    assert L.smob_server_create(ctypes.byref(srv), ctypes.byref(o)) == N.SMOB_ERR_ARG
+    assert not srv.value
