@@ -487,11 +487,15 @@ __global__ void __launch_bounds__(kNearThreads, 2)
 //   D [128 x NN] per tile in tensor memory (tile 0 at column 0, tile 1 at column 32), FP32: row i holds
 //     target i's NS contractions.
 // Products in 3xTF32 (a_hi b_hi + a_hi b_lo + a_lo b_hi, the split made as the operands are staged).
-// One operand stage per CTA (~72 KB, three CTAs per SM): the threads fill the chunk, one thread issues
-// the MMAs, commits them to an mbarrier and waits for them (bounded) while the other warps sleep at the
-// barrier and the other CTAs of the SM generate their chunks. After a source's last chunk each warp
-// loads its 32 rows (tcgen05.ld) and assembles the traction or velocity in FP32. On a wait timeout the
-// CTA records it in err, writes nothing and releases its tensor memory.
+// STAGES = 1: one operand stage per CTA (~72 KB, three CTAs per SM): the threads fill the chunk, one
+// thread issues the MMAs, commits them to an mbarrier and waits for them (bounded) while the other warps
+// sleep at the barrier and the other CTAs of the SM generate their chunks. STAGES = 2 (grids of about
+// one CTA per SM, where no other CTA hides that wait): two stages and an mbarrier per stage; the thread
+// that issues chunk k's MMAs then waits for chunk k - 1's, which ran while the threads generated chunk
+// k, so the MMAs overlap the generation of the next chunk. The MMAs, their order and the accumulator
+// are the same in both, so are the results. After a source's last chunk each warp loads its 32 rows
+// (tcgen05.ld) and assembles the traction or velocity in FP32. On a wait timeout the CTA records it in
+// err, writes nothing and releases its tensor memory.
 constexpr int kTcK = 2 * kNearTcChunk;          // K per chunk (TF32 elements)
 constexpr int kTcABytes = 128 * kTcK * 4;       // one A operand tile chunk (16 KB)
 constexpr int kTcThreads = 256;                 // two M tiles
@@ -503,8 +507,8 @@ __host__ __device__ constexpr int tc_nn() { return TRAC ? 32 : 16; }
 template <bool TRAC>
 __host__ __device__ constexpr int tc_stage_bytes() { return 4 * kTcABytes + 2 * tc_nn<TRAC>() * kTcK * 4; }
 
-template <bool TRAC>
-__global__ void __launch_bounds__(kTcThreads, 2)
+template <bool TRAC, int STAGES>
+__global__ void __launch_bounds__(kTcThreads, STAGES == 1 ? 2 : 1)
     k_near_eval_tc(DevGeom g, const float* __restrict__ tiles, long long tstride, const float* __restrict__ th,
                    int th_c1, int th_c2, int th_diag, double c, int pair_filter, int tile_major, double* __restrict__ out,
                    int* __restrict__ err) {
@@ -523,15 +527,13 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     if (!any) return;
 
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[STAGES];
     __shared__ uint32_t tbase;
     __shared__ int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, mt = tid >> 7, row = tid & 127;
-    unsigned char* sA = tc_smem + mt * 2 * kTcABytes;  // this thread's tile: hi, then lo
-    unsigned char* sB = tc_smem + 4 * kTcABytes;       // hi, then lo
-    // recurrence tables after the stage: (c1, c2) pairs, then the diagonal factors
+    // recurrence tables after the stages: (c1, c2) pairs, then the diagonal factors
     const int ncd = ncoef(g.pmax + 3);
-    float2* t12 = reinterpret_cast<float2*>(tc_smem + tc_stage_bytes<TRAC>());
+    float2* t12 = reinterpret_cast<float2*>(tc_smem + STAGES * tc_stage_bytes<TRAC>());
     float* dg = reinterpret_cast<float*>(t12 + ncd);
     for (int k = tid; k < ncd; k += kTcThreads) t12[k] = make_float2(th[th_c1 + k], th[th_c2 + k]);
     for (int k = tid; k < g.pmax + 4; k += kTcThreads) dg[k] = th[th_diag + k];
@@ -540,7 +542,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&mbar, 1);
+#pragma unroll
+        for (int q = 0; q < STAGES; ++q) tc::mbar_init(&mbar[q], 1);
         tc::mbar_fence_init();
         s_fail = 0;
     }
@@ -559,7 +562,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         X[d] = g.coords[3 * i + d];
         Nl[d] = float(g.norms[3 * i + d]);
     }
-    unsigned phase = 0;
+    unsigned phases = 0;  // bit q: the parity the next wait on mbar[q] expects
     bool failed = false;
     for (int e = e0; e < e1 && !failed; ++e) {
         if (pair_filter == 1 && g.nbr_precise[e]) continue;
@@ -579,6 +582,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         float pr = 0.f, pi = 0.f, cr = dr, ci = di;
         const float zi = z * ir2;
         for (int ch = 0; ch < nck; ++ch) {
+            const int stg = STAGES == 2 ? (ch & 1) : 0;
+            unsigned char* const stage = tc_smem + stg * tc_stage_bytes<TRAC>();
+            unsigned char* sA = stage + mt * 2 * kTcABytes;  // this thread's tile: hi, then lo
+            unsigned char* sB = stage + 4 * kTcABytes;       // hi, then lo
             // B chunk (one float4 per thread for NN = 32): copy and split
             const float4* gB = reinterpret_cast<const float4*>(T + (long long)ch * NN * kTcK);
             for (int v = tid; v < NN * kTcK / 4; v += kTcThreads) {
@@ -646,7 +653,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                 const uint32_t b0 = tc::smem_u32(sB), bl0 = b0 + BBYTES;
 #pragma unroll
                 for (int tt = 0; tt < 2; ++tt) {
-                    const uint32_t a0 = tc::smem_u32(tc_smem + tt * 2 * kTcABytes), al0 = a0 + kTcABytes;
+                    const uint32_t a0 = tc::smem_u32(stage + tt * 2 * kTcABytes), al0 = a0 + kTcABytes;
 #pragma unroll
                     for (int ks = 0; ks < kTcK / 8; ++ks) {
                         const uint32_t o = ks * 256;
@@ -660,11 +667,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                         tc::mma_tf32(d, al, bh, idesc, true);
                     }
                 }
-                tc::mma_commit(&mbar);
-                // one thread waits for the chunk's MMAs; the others sleep at the barrier below
-                if (!tc::mbar_wait_bounded(&mbar, phase, kTcWaitPolls)) s_fail = 1;
+                tc::mma_commit(&mbar[stg]);
+                // one thread waits (the others sleep at the barrier below): for this chunk's MMAs with
+                // one stage, for the previous chunk's with two (its stage is filled next)
+                if (STAGES == 1) {
+                    if (!tc::mbar_wait_bounded(&mbar[0], phases & 1u, kTcWaitPolls)) s_fail = 1;
+                } else if (ch > 0) {
+                    if (!tc::mbar_wait_bounded(&mbar[stg ^ 1], (phases >> (stg ^ 1)) & 1u, kTcWaitPolls)) s_fail = 1;
+                }
             }
-            phase ^= 1;
+            if (STAGES == 1) phases ^= 1u;
+            else if (ch > 0) phases ^= 1u << (stg ^ 1);
             __syncthreads();
             if (s_fail) {
                 failed = true;
@@ -672,6 +685,16 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             }
         }
         if (failed) break;
+        if (STAGES == 2) {  // the source's last chunk
+            const int lst = (nck - 1) & 1;
+            if (tid == 0 && !tc::mbar_wait_bounded(&mbar[lst], (phases >> lst) & 1u, kTcWaitPolls)) s_fail = 1;
+            phases ^= 1u << lst;
+            __syncthreads();
+            if (s_fail) {
+                failed = true;
+                break;
+            }
+        }
         tc::fence_after_sync();
         float acc[32];
         tc::tmem_ld_32x32b_x32(tmem + 32 * mt + (uint32_t((warp & 3) * 32) << 16), acc);
@@ -774,10 +797,10 @@ size_t near_df_smem(int pmax, bool stage) {
     return (stage ? size_t(TRAC ? kNearSetsTrac : kNearSetsSL) * ncd * 16 : 0) + ncd * 16 + size_t(pmax + 4) * 8;
 }
 
-// dynamic shared memory of the tensor-core near kernel: the operand stage and the recurrence tables
+// dynamic shared memory of the tensor-core near kernel: the operand stages and the recurrence tables
 template <bool TRAC>
-size_t near_tc_smem(int pmax) {
-    return size_t(tc_stage_bytes<TRAC>()) + size_t(2 * ncoef(pmax + 3) + pmax + 4) * sizeof(float);
+size_t near_tc_smem(int pmax, int stages) {
+    return size_t(stages) * size_t(tc_stage_bytes<TRAC>()) + size_t(2 * ncoef(pmax + 3) + pmax + 4) * sizeof(float);
 }
 
 void configure_near_kernels() {
@@ -787,10 +810,14 @@ void configure_near_kernels() {
                          int(near_df_smem<true>(kMaxOrder, false)));
     cudaFuncSetAttribute(k_near_eval_df<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(near_df_smem<false>(kMaxOrder, false)));
-    cudaFuncSetAttribute(k_near_eval_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(near_tc_smem<true>(kMaxOrder)));
-    cudaFuncSetAttribute(k_near_eval_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(near_tc_smem<false>(kMaxOrder)));
+    cudaFuncSetAttribute(k_near_eval_tc<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<true>(kMaxOrder, 1)));
+    cudaFuncSetAttribute(k_near_eval_tc<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<false>(kMaxOrder, 1)));
+    cudaFuncSetAttribute(k_near_eval_tc<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<true>(kMaxOrder, 2)));
+    cudaFuncSetAttribute(k_near_eval_tc<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(near_tc_smem<false>(kMaxOrder, 2)));
     configure_near_typed<float, true>();
     configure_near_typed<float, false>();
     configure_near_typed<double, true>();
@@ -828,14 +855,24 @@ int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool 
         const int tm = g.N <= 65535 ? 1 : 0;
         const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
         const float* tl = static_cast<const float*>(sets);
-        if (trac)
-            k_near_eval_tc<true><<<grid, kTcThreads, near_tc_smem<true>(g.pmax), st>>>(
-                g, tl, near_tile_stride(g.pmax, true), g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out,
-                g.err);
+        // two operand stages when the grid is about one wave of one CTA per SM (the same results)
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const bool two = (long long)grid.x * grid.y <= 2LL * sms;
+        const long long tsv = near_tile_stride(g.pmax, trac);
+        if (trac && two)
+            k_near_eval_tc<true, 2><<<grid, kTcThreads, near_tc_smem<true>(g.pmax, 2), st>>>(
+                g, tl, tsv, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out, g.err);
+        else if (trac)
+            k_near_eval_tc<true, 1><<<grid, kTcThreads, near_tc_smem<true>(g.pmax, 1), st>>>(
+                g, tl, tsv, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out, g.err);
+        else if (two)
+            k_near_eval_tc<false, 2><<<grid, kTcThreads, near_tc_smem<false>(g.pmax, 2), st>>>(
+                g, tl, tsv, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out, g.err);
         else
-            k_near_eval_tc<false><<<grid, kTcThreads, near_tc_smem<false>(g.pmax), st>>>(
-                g, tl, near_tile_stride(g.pmax, false), g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm,
-                out, g.err);
+            k_near_eval_tc<false, 1><<<grid, kTcThreads, near_tc_smem<false>(g.pmax, 1), st>>>(
+                g, tl, tsv, g.tab_f, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out, g.err);
         return 1;
     }
     switch (g.near_lanes) {
