@@ -586,18 +586,13 @@ __global__ void __launch_bounds__(kTcThreads, STAGES == 1 ? 2 : 1)
             unsigned char* const stage = tc_smem + stg * tc_stage_bytes<TRAC>();
             unsigned char* sA = stage + mt * 2 * kTcABytes;  // this thread's tile: hi, then lo
             unsigned char* sB = stage + 4 * kTcABytes;       // hi, then lo
-            // B chunk (one float4 per thread for NN = 32): copy and split
+            // B chunk (at most one float4 per thread): its load is issued first and lands while the
+            // thread generates its A chunk; split and stored after that
+            constexpr int kBVec = NN * kTcK / 4;
+            static_assert(kBVec <= kTcThreads, "one B float4 per thread at most");
             const float4* gB = reinterpret_cast<const float4*>(T + (long long)ch * NN * kTcK);
-            for (int v = tid; v < NN * kTcK / 4; v += kTcThreads) {
-                const float4 b = __ldg(gB + v);
-                float4 h, l;
-                tc::tf32_split(b.x, h.x, l.x);
-                tc::tf32_split(b.y, h.y, l.y);
-                tc::tf32_split(b.z, h.z, l.z);
-                tc::tf32_split(b.w, h.w, l.w);
-                reinterpret_cast<float4*>(sB)[v] = h;
-                reinterpret_cast<float4*>(sB + BBYTES)[v] = l;
-            }
+            float4 bpre = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (tid < kBVec) bpre = __ldg(gB + tid);
             // A chunk: the next kNearTcChunk harmonics of this thread's target, 4 K values at a time
 #pragma unroll
             for (int qd = 0; qd < kTcK / 4; ++qd) {
@@ -644,6 +639,15 @@ __global__ void __launch_bounds__(kTcThreads, STAGES == 1 ? 2 : 1)
                 const uint32_t off = tc::kmajor_offset(row, 4 * qd, kTcK);
                 *reinterpret_cast<float4*>(sA + off) = h;
                 *reinterpret_cast<float4*>(sA + kTcABytes + off) = l;
+            }
+            if (tid < kBVec) {
+                float4 h, l;
+                tc::tf32_split(bpre.x, h.x, l.x);
+                tc::tf32_split(bpre.y, h.y, l.y);
+                tc::tf32_split(bpre.z, h.z, l.z);
+                tc::tf32_split(bpre.w, h.w, l.w);
+                reinterpret_cast<float4*>(sB)[tid] = h;
+                reinterpret_cast<float4*>(sB + BBYTES)[tid] = l;
             }
             tc::fence_smem_async();
             tc::fence_before_sync();
