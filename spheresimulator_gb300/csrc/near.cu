@@ -17,6 +17,8 @@
 //       4 pi t_i = n_i div L - x_j n_k d_i d_k L_j + n_k d_i d_k L_r       (traction)
 //       8 pi u_i = L_i - x_j d_i L_j + d_i L_r                             (single layer, x radius)
 //     and rotates back into the lab frame. Accumulation per target point is in a fixed order.
+#include <atomic>
+
 #include "df.h"
 #include "smob_internal.h"
 #include "tc_sm100.h"
@@ -845,6 +847,20 @@ void launch_near_df_typed(const DevGeom& g, const void* sets, long long stride, 
             g, sp, stride, g.tab_d, g.th_c1, g.th_c2, g.th_diag, c, pair_filter, tm, out);
 }
 
+// SMs of the current device, looked up once per device
+static int sm_count() {
+    constexpr int kDevices = 64;
+    static std::atomic<int> cache[kDevices];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = dev >= 0 && dev < kDevices ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (v == 0) {
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        if (dev >= 0 && dev < kDevices) cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool trac, bool fp32, double c, double* out,
                      cudaStream_t st, int pair_filter, bool df) {
     if (df && !fp32) {
@@ -860,10 +876,7 @@ int launch_near_eval(const DevGeom& g, const void* sets, long long stride, bool 
         const dim3 grid = tm ? dim3(tiles, g.N) : dim3(g.N, tiles);
         const float* tl = static_cast<const float*>(sets);
         // two operand stages when the grid is about one wave of one CTA per SM (the same results)
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const bool two = (long long)grid.x * grid.y <= 2LL * sms;
+        const bool two = (long long)grid.x * grid.y <= 2LL * sm_count();
         const long long tsv = near_tile_stride(g.pmax, trac);
         if (trac && two)
             k_near_eval_tc<true, 2><<<grid, kTcThreads, near_tc_smem<true>(g.pmax, 2), st>>>(
