@@ -310,7 +310,9 @@ typedef struct {
 /* The server keeps freed device memory in the device's stream-ordered pool (its release threshold set
  * to the maximum) instead of returning it to the driver at every synchronisation, and turns off the
  * pool's reuse of blocks through inserted cross-stream waits (cudaMemPoolReuseAllowInternalDependencies),
- * so one request's allocation never waits for another request's queued kernels. */
+ * so one request's allocation never waits for another request's queued kernels.
+ * SMOB_ERR_ARG (before any device work) for max_slots, restart or max_iters below 1, or graphs
+ * outside 0..2. */
 smob_status smob_server_create(smob_server** server, const smob_server_opts* opts);
 smob_status smob_server_submit(smob_server* server, const smob_geometry* geom, const double* force6n, double tol,
                                long long* request_id);
