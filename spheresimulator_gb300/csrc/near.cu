@@ -733,10 +733,12 @@ int launch_near_sets(const DevGeom& g, const void* coef, bool trac, bool fp32, v
                      const int* slot_sphere, long long stride, cudaStream_t st, bool df) {
     if (nslots <= 0) return 0;
     const size_t sm = size_t(6 * ncoef(g.pmax)) * (fp32 ? sizeof(float) : sizeof(double));
-    // each slot's rows (2 x sets x ncoef(p+3), ~10^4) split over kSetSplit CTAs: few near-source spheres
-    // still give the GPU enough CTAs
-    constexpr int kSetSplit = 8;
-    const dim3 grid(nslots, kSetSplit);
+    // each slot's rows (2 x sets x ncoef(p+3), ~10^4) split over CTAs: few near-source spheres still give
+    // the GPU enough CTAs. Each row is one thread's fixed sum, so the split leaves every value unchanged;
+    // 32 for at most 64 slots (cfg2: the sets 0.39 instead of 0.50 ms per solve, 97.0 against 96.7
+    // solves/s), else 8, where each CTA's copy of the coefficients would cost more than the finer split
+    const int split = nslots <= 64 ? 32 : 8;
+    const dim3 grid(nslots, split);
     if (fp32) {
         const bool tiled = g.near_tc != 0;
         k_near_sets<float><<<grid, 256, sm, st>>>(g, static_cast<const float*>(coef), g.map_val_f, trac, slot_sphere,
